@@ -1,0 +1,410 @@
+"""Benchmark of the MLS-MPM substep on one GB300 (metric: particle-substeps/s).
+
+Workload (default, N=1): the single large multi-material scene - grid 128^3 cells (129^3
+nodes) over the unit cube, ~1M particles: a liquid block 0.3^3 (E=1e5, nu=0.3), a
+Drucker-Prager sand block 0.2^3 (friction angle 45 deg) and an elastic sphere of radius
+0.1, stacked in z and dropped onto the ground; seed-jittered lattices (spacing chosen for
+~1M particles: (V_total/1e6)^(1/3)); substep dt = 1e-4.  One bench step = one
+`scene.step()` of 10 substeps.  Inputs are synthetic (seeded), generated here.
+
+--impl reference times the CPU restatement of the reference algorithm (the oracle, fp32,
+all host cores via OpenMP) on the same workload; the reference itself (Genesis on the
+Quadrants JIT) cannot be installed on these machines.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SUBSTEPS_PER_STEP = 10
+SUBSTEP_DT = 1e-4
+GRID_DENSITY = 128
+SEED = 2024
+METRIC = "particle-substeps/s on 1 GB300 (plain, batched, served p50/p99) at stated tol"
+# per-kernel algorithmic bytes (per particle, per touched node); see the design doc
+ALG_BYTES = {
+    "p2g": (144, 16),   # read pos,vel,C,F,Jp,material (104 B) + write F,Jp (40 B); grid write 16 B/node
+    "grid_op": (0, 32),  # read (momentum,mass) 16 B + write velocity 16 B per touched node
+    "g2p": (72, 16),    # read pos 12 B + write pos,vel,C 60 B; read node velocity 16 B/node
+    "scan": (0, 0),
+    "perm": (0, 0),
+}
+SUBSTEP_ALG = (204, 32)  # whole substep: 204 B/particle + 32 B/touched node
+
+
+def workload_boxes():
+    liquid = ((0.5, 0.5, 0.2), 0.3)
+    sand = ((0.5, 0.5, 0.5), 0.2)
+    sphere = ((0.5, 0.5, 0.75), 0.1)
+    v_total = liquid[1] ** 3 + sand[1] ** 3 + 4.0 / 3.0 * np.pi * sphere[1] ** 3
+    spacing = (v_total / 1e6) ** (1.0 / 3.0)
+    return liquid, sand, sphere, spacing
+
+
+def jitter(pos, spacing, rng):
+    return pos + rng.uniform(-0.25 * spacing, 0.25 * spacing, size=pos.shape)
+
+
+def build_c2_scene(gs, n_envs=0):
+    """The ~1M-particle three-material scene through the Genesis-style API."""
+    import torch
+
+    liquid, sand, sphere, spacing = workload_boxes()
+    scene = gs.Scene(
+        sim_options=gs.options.SimOptions(dt=SUBSTEP_DT * SUBSTEPS_PER_STEP, substeps=SUBSTEPS_PER_STEP),
+        mpm_options=gs.options.MPMOptions(lower_bound=(0, 0, 0), upper_bound=(1, 1, 1), grid_density=GRID_DENSITY,
+                                          particle_size=spacing),
+    )
+    rng = np.random.default_rng(SEED)
+    ents = [
+        scene.add_entity(material=gs.materials.MPM.Liquid(E=1e5, nu=0.3, sampler="regular"),
+                         morph=gs.morphs.Box(pos=liquid[0], size=(liquid[1],) * 3)),
+        scene.add_entity(material=gs.materials.MPM.Sand(friction_angle=45.0, sampler="regular"),
+                         morph=gs.morphs.Box(pos=sand[0], size=(sand[1],) * 3)),
+        scene.add_entity(material=gs.materials.MPM.Elastic(sampler="regular"),
+                         morph=gs.morphs.Sphere(pos=sphere[0], radius=sphere[1])),
+    ]
+    scene.build(n_envs=n_envs)
+    for e in ents:
+        p = jitter(e.init_particles, spacing, rng)
+        e.set_particles_pos(torch.tensor(p, dtype=torch.float32, device="cuda"))
+    return scene, ents, spacing
+
+
+def oracle_c2_state():
+    """Same workload on the host for the CPU baseline (fp32 oracle)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    import genesis_gb300 as gs
+    from genesis_gb300 import morphs
+
+    liquid, sand, sphere, spacing = workload_boxes()
+    rng = np.random.default_rng(SEED)
+    mats = [gs.materials.MPM.Liquid(E=1e5, nu=0.3), gs.materials.MPM.Sand(friction_angle=45.0),
+            gs.materials.MPM.Elastic()]
+    parts = [
+        morphs.Box(pos=liquid[0], size=(liquid[1],) * 3).sample(spacing, "regular"),
+        morphs.Box(pos=sand[0], size=(sand[1],) * 3).sample(spacing, "regular"),
+        morphs.Sphere(pos=sphere[0], radius=sphere[1]).sample(spacing, "regular"),
+    ]
+    pos = np.concatenate([jitter(p, spacing, rng) for p in parts])
+    n = len(pos)
+    mat_idx = np.concatenate([np.full(len(p), i, np.int32) for i, p in enumerate(parts)])
+    jp = np.concatenate([np.full(len(p), m._default_Jp) for p, m in zip(parts, mats)])
+    st = dict(pos=pos, vel=np.zeros((n, 3)), C=np.zeros((n, 3, 3)), F=np.tile(np.eye(3), (n, 1, 1)), Jp=jp,
+              mat=mat_idx, active=np.ones(n, bool))
+    sc = O.make_scene(SUBSTEP_DT, grid_density=GRID_DENSITY, particle_size=spacing)
+    oms = [O.from_c_material(m.to_c(0)) for m in mats]
+    return O, sc, oms, st
+
+
+def cpu_baseline(target_s=10.0):
+    """Oracle fp32 on all host cores, bounded sample of the workload (whole scene, a few substeps)."""
+    O, sc, oms, st = oracle_c2_state()
+    cores = os.cpu_count() or 1
+    n = len(st["pos"])
+    t0 = time.perf_counter()
+    st, _, _ = O.run(sc, oms, st, 1, dtype=np.float32, threads=cores)
+    t1 = time.perf_counter() - t0
+    k = int(max(1, min(50, target_s / max(t1, 1e-3))))
+    t0 = time.perf_counter()
+    O.run(sc, oms, st, k, dtype=np.float32, threads=cores)
+    dt = time.perf_counter() - t0
+    return {
+        "value": n * k / dt,
+        "unit": "particle-substeps/s",
+        "cores": cores,
+        "kind": "port",
+        "sample": f"full workload ({n} particles), {k} substeps after 1 warm-up substep, fp32 oracle, "
+        f"OpenMP {cores} threads, {dt:.1f} s",
+    }
+
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.samples = []
+        self.proc = None
+        self.dev = device_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def load_traffic(kernel):
+    p = os.path.join(ROOT, "profiles", f"{kernel}_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d
+    return None
+
+
+def run_ours(args, rank, world):
+    import ctypes
+
+    import torch
+
+    import __graft_entry__ as g
+
+    g.build()
+    import genesis_gb300 as gs
+    from genesis_gb300 import _lib
+
+    gs.init(backend=gs.gpu, seed=SEED)
+    scene, ents, spacing = build_c2_scene(gs)
+    solver = scene.sim.mpm_solver
+    n = solver.n_particles
+    lib = _lib.load()
+    stream = torch.cuda.current_stream()
+
+    # warm-up (also captures the CUDA graph)
+    for _ in range(args.warmup):
+        scene.step()
+    torch.cuda.synchronize()
+
+    # --- timed region: K steps of 10 substeps, CUDA graph path, inputs resident in HBM
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        solver.substeps(SUBSTEPS_PER_STEP)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    solver.check_state()
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = t.item()
+    total_units = n * SUBSTEPS_PER_STEP * args.steps * world
+    value = total_units / (ms / 1e3)
+
+    # --- per-kernel durations over a second timed region of the same K steps (events per kernel)
+    lib.mpm_set_profiling(solver.ctx, 1)
+    lib.mpm_kernel_times(solver.ctx, None, None, 1)
+    for _ in range(args.steps):
+        solver.substeps(SUBSTEPS_PER_STEP)
+    kms = (ctypes.c_double * 5)()
+    kcnt = (ctypes.c_int64 * 5)()
+    lib.mpm_kernel_times(solver.ctx, kms, kcnt, 1)
+    lib.mpm_set_profiling(solver.ctx, 0)
+    touched = ctypes.c_int64()
+    _lib.check(lib.mpm_count_touched_nodes(solver.ctx, ctypes.byref(touched), ctypes.c_void_p(stream.cuda_stream)))
+    names = ["p2g", "grid_op", "g2p", "scan", "perm"]
+    per_kernel = {nm: {"ms_avg": kms[i] / max(1, kcnt[i]), "launches": int(kcnt[i])} for i, nm in enumerate(names)}
+    total_k = sum(kms[i] for i in range(5))
+    for i, nm in enumerate(names):
+        per_kernel[nm]["share"] = kms[i] / total_k if total_k else None
+    dom = max(names, key=lambda nm: per_kernel[nm]["ms_avg"] * per_kernel[nm]["launches"])
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as f:
+            peak = float(json.load(f)["hbm_gbs"])
+        peak_src = "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    bp, bn = ALG_BYTES[dom]
+    alg = bp * n + bn * touched.value
+    achieved = alg / (per_kernel[dom]["ms_avg"] / 1e3) / 1e9
+    substep_ms = total_k / max(1, kcnt[0])
+    sub_alg = SUBSTEP_ALG[0] * n + SUBSTEP_ALG[1] * touched.value
+    tr = load_traffic(dom)
+    roofline = {
+        "bound": "hbm",
+        "kernel": dom,
+        "achieved": achieved,
+        "peak": peak,
+        "unit": "GB/s",
+        "frac": achieved / peak,
+        "peak_source": peak_src,
+        "traffic": (tr["bytes_per_particle"] * n + tr.get("bytes_per_touched_node", 0) * touched.value) if tr else None,
+        "algorithmic_bytes": alg,
+        "substep": {"algorithmic_bytes": sub_alg, "ms": substep_ms,
+                    "achieved": sub_alg / (substep_ms / 1e3) / 1e9,
+                    "frac": sub_alg / (substep_ms / 1e3) / 1e9 / peak},
+    }
+
+    # --- e2e: through the public API with host buffers: H2D state from pinned memory, 10 substeps,
+    # D2H of positions, every step
+    st = solver.get_state()
+    host = {k: getattr(st, k).cpu().pin_memory() for k in ("pos", "vel", "C", "F", "Jp", "active")}
+    h2d = sum(t.numel() * t.element_size() for t in host.values())
+    out_host = torch.empty_like(host["pos"]).pin_memory()
+    d2h = out_host.numel() * out_host.element_size()
+
+    class _S:
+        pass
+
+    def e2e_step():
+        s = _S()
+        for k, v in host.items():
+            setattr(s, k, v.to("cuda", non_blocking=True))
+        solver.set_state(0, s)
+        solver.substeps(SUBSTEPS_PER_STEP)
+        dst = ents[0].solver.get_state()
+        out_host.copy_(dst.pos, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": n * SUBSTEPS_PER_STEP * args.steps * world / e2e_s, "unit": "particle-substeps/s",
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+    result = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "particle-substeps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded jittered lattices)",
+        "config": {
+            "workload": "plain large: 129^3-node grid, ~1M particles (liquid 0.3^3 + sand 0.2^3 + elastic sphere "
+                        "r=0.1), dt=1e-4, step = 10 substeps",
+            "n_particles": n,
+            "substeps_per_step": SUBSTEPS_PER_STEP,
+            "touched_nodes": touched.value,
+            "parallelism": "replicas only" if world > 1 else "single GPU",
+            "l2": "inputs larger than L2 (particle state double buffer 2 x 108 MB)",
+            "path": "CUDA graph of 2 substeps",
+        },
+        "roofline": roofline,
+        "kernels": per_kernel,
+        "e2e": e2e,
+        "gpu_launches": 7 * SUBSTEPS_PER_STEP * args.steps,
+        "clocks": clk,
+    }
+    if rank == 0 and not args.skip_cpu:
+        result["cpu_baseline"] = cpu_baseline()
+    return result
+
+
+def run_reference(args):
+    """The CPU implementation of the path (oracle restatement), all host cores, same metric."""
+    O, sc, oms, st = oracle_c2_state()
+    cores = os.cpu_count() or 1
+    n = len(st["pos"])
+    for _ in range(args.warmup):
+        st, _, _ = O.run(sc, oms, st, 1, dtype=np.float32, threads=cores)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st, _, _ = O.run(sc, oms, st, 1, dtype=np.float32, threads=cores)
+    dt = time.perf_counter() - t0
+    v = n * args.steps / dt
+    return {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": v,
+        "unit": "particle-substeps/s",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": dt * 1e3 / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded jittered lattices)",
+        "config": {"workload": "plain large: 129^3-node grid, ~1M particles (liquid + sand + elastic sphere), "
+                               "dt=1e-4; each step = 1 substep of the whole scene on the CPU", "n_particles": n},
+        "cpu_baseline": {"value": v, "unit": "particle-substeps/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} substeps of the full {n}-particle scene, fp32, OpenMP {cores} threads"},
+        "e2e": {"value": v, "unit": "particle-substeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "The reference (Genesis + Quadrants JIT) is not installable here; this is the oracle restatement "
+                "of its algorithm on the host cores.",
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)))
+        return
+    if world > 1:
+        import torch
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        torch.distributed.init_process_group("nccl")
+    res = run_ours(args, rank, world)
+    if rank == 0:
+        print(json.dumps(res))
+    if world > 1:
+        import torch
+
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

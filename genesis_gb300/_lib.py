@@ -1,0 +1,153 @@
+"""ctypes binding of libgbmpm.so (declared in include/gbmpm.h).
+
+There is no fallback: if the library is missing or fails to load, every solver call raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from .exceptions import GenesisException
+
+c_int32, c_int64, c_double, c_void_p, c_float = (
+    ctypes.c_int32,
+    ctypes.c_int64,
+    ctypes.c_double,
+    ctypes.c_void_p,
+    ctypes.c_float,
+)
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libgbmpm.so")
+
+MPM_OK = 0
+STATUS_NAMES = {
+    1: "MPM_ERR_BAD_ARG",
+    2: "MPM_ERR_CUDA",
+    3: "MPM_ERR_OOM",
+    4: "MPM_ERR_NAN",
+    5: "MPM_ERR_OOB",
+    6: "MPM_ERR_TIMEOUT",
+    7: "MPM_ERR_STATE",
+}
+STATUS_NAN = 0x1
+STATUS_OOB = 0x2
+
+# material types / flags (mpm_material_type, MPM_MATF_*)
+MAT_ELASTIC, MAT_LIQUID, MAT_SAND, MAT_SNOW, MAT_ELASTOPLASTIC, MAT_MUSCLE = range(6)
+MATF_NEOHOOKEAN = 0x1
+MATF_VON_MISES = 0x2
+
+# fields of mpm_set_particles / mpm_get_particles
+FIELD_POS, FIELD_VEL, FIELD_C, FIELD_F, FIELD_JP, FIELD_ACTIVE, FIELD_ACTU, FIELD_FREE, FIELD_MUSCLE_DIR = range(9)
+FIELD_POS_RESET = 9
+
+
+class MpmMaterial(ctypes.Structure):
+    _fields_ = [
+        ("type", c_int32),
+        ("flags", c_int32),
+        ("scene", c_int32),
+        ("reserved", c_int32),
+        ("mu", c_double),
+        ("lam", c_double),
+        ("rho", c_double),
+        ("default_Jp", c_double),
+        ("friction_alpha", c_double),
+        ("yield_lower", c_double),
+        ("yield_higher", c_double),
+        ("von_mises_yield_stress", c_double),
+        ("stiffness", c_double),
+    ]
+
+
+class MpmSceneConfig(ctypes.Structure):
+    _fields_ = [
+        ("substep_dt", c_double),
+        ("gravity", c_double * 3),
+        ("lower_bound", c_double * 3),
+        ("upper_bound", c_double * 3),
+        ("grid_density", c_double),
+        ("particle_size", c_double),
+        ("mass_eps", c_double),
+        ("restitution", c_double),
+        ("n_particles", c_int64),
+    ]
+
+
+_P = c_void_p
+# name -> (restype, argtypes)
+_SIGNATURES = {
+    "mpm_ctx_create": (c_int32, [ctypes.POINTER(MpmSceneConfig), c_int64, ctypes.POINTER(MpmMaterial), c_int32, c_int32, ctypes.POINTER(c_void_p)]),
+    "mpm_ctx_destroy": (c_int32, [_P]),
+    "mpm_last_error": (ctypes.c_char_p, [_P]),
+    "mpm_add_particles": (c_int32, [_P, c_int64, c_int64, c_int64, c_int64, c_int32, c_int32, _P, _P]),
+    "mpm_get_state": (c_int32, [_P, c_int64, c_int64, _P, _P, _P, _P, _P, _P, _P]),
+    "mpm_set_state": (c_int32, [_P, c_int64, c_int64, _P, _P, _P, _P, _P, _P, _P]),
+    "mpm_set_particles": (c_int32, [_P, c_int32, c_int64, c_int64, c_int64, c_int64, _P, _P]),
+    "mpm_get_particles": (c_int32, [_P, c_int32, c_int64, c_int64, c_int64, c_int64, _P, _P]),
+    "mpm_set_gravity": (c_int32, [_P, c_int64, c_int64, ctypes.POINTER(c_double)]),
+    "mpm_substeps": (c_int32, [_P, c_int32, _P]),
+    "mpm_substep_pre": (c_int32, [_P, _P]),
+    "mpm_substep_grid_op": (c_int32, [_P, _P]),
+    "mpm_substep_post": (c_int32, [_P, _P]),
+    "mpm_get_grid": (c_int32, [_P, c_int64, _P, _P]),
+    "mpm_count_touched_nodes": (c_int32, [_P, ctypes.POINTER(c_int64), _P]),
+    "mpm_status_word": (c_int32, [_P, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(c_int64), c_int32, _P]),
+    "mpm_set_tuning": (c_int32, [_P, c_int32, c_int32, c_int32]),
+    "mpm_get_info": (c_int32, [_P, ctypes.POINTER(c_int64), ctypes.POINTER(c_int64), ctypes.POINTER(c_int64)]),
+    "mpm_scene_grid_res": (c_int32, [_P, c_int64, ctypes.POINTER(c_int32)]),
+    "mpm_set_profiling": (c_int32, [_P, c_int32]),
+    "mpm_kernel_times": (c_int32, [_P, ctypes.POINTER(c_double), ctypes.POINTER(c_int64), c_int32]),
+    "mpm_version": (c_int32, []),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+def exported_symbols() -> list[str]:
+    """Names the binding expects the library to export (also checked by the CPU tests)."""
+    return sorted(_SIGNATURES)
+
+
+def load(path: str | None = None):
+    """Load libgbmpm.so once; raise GenesisException if it is missing (no CPU fallback)."""
+    global _lib
+    with _lock:
+        if _lib is not None and path is None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise GenesisException(
+                f"libgbmpm.so not found at {p}. Build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+                "(the MPM solver has no CPU fallback)."
+            )
+        lib = ctypes.CDLL(p)
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        if path is None:
+            _lib = lib
+        return lib
+
+
+def check(ret: int, ctx=None, what: str = "") -> None:
+    """Map a status code to GenesisException carrying the library's error text."""
+    if ret == MPM_OK:
+        return
+    lib = load()
+    msg = lib.mpm_last_error(ctx)
+    msg = msg.decode() if msg else ""
+    raise GenesisException(f"{what}: {STATUS_NAMES.get(ret, ret)}: {msg}")
+
+
+def ptr(t) -> int | None:
+    """Device pointer of a contiguous torch tensor (None for None)."""
+    if t is None:
+        return None
+    if not t.is_contiguous():
+        raise GenesisException("tensor must be contiguous")
+    return t.data_ptr()

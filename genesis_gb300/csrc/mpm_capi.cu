@@ -1,0 +1,848 @@
+// mpm_capi.cu - host runtime of libgbmpm.so: context (device memory pool, scene and
+// material tables), launch sequencing, CUDA-graph capture of the substep loop, per-kernel
+// event timing, and the extern "C" entry points declared in include/gbmpm.h.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "gbmpm.h"
+#include "mpm_kernels.cuh"
+
+using namespace gbmpm;
+
+namespace {
+std::mutex g_err_mu;
+std::string g_create_err;
+
+// Kernel groups timed in profiling mode.
+enum { KT_P2G = 0, KT_GRID = 1, KT_G2P = 2, KT_SCAN = 3, KT_PERM = 4, KT_N = 5 };
+
+struct TimedPair {
+  int kind;
+  cudaEvent_t a, b;
+};
+}  // namespace
+
+struct mpm_ctx {
+  int device = 0;
+  int n_sm = 1;
+  std::string err;
+
+  // tables
+  int64_t n_scenes = 0, n_mats = 0;
+  std::vector<SceneDev> scenes_h;
+  std::vector<MaterialDev> mats_h;
+  std::vector<int64_t> pbegin_h;
+  std::vector<int32_t> first_mat_h;
+  std::vector<int32_t> mat_count_h;
+  int64_t cap = 0, n = 0, K = 0;
+  int nf = NF_BASE;
+  float eps_norm = 1.1920929e-7f;
+
+  // device memory
+  SceneDev* d_scenes = nullptr;
+  MaterialDev* d_mats = nullptr;
+  int32_t* d_block_scene = nullptr;
+  int64_t* d_pbegin = nullptr;
+  int32_t* d_first_mat = nullptr;
+  float* d_pbuf[2] = {nullptr, nullptr};
+  float4* d_grid[2] = {nullptr, nullptr};
+  int32_t* d_flags[2] = {nullptr, nullptr};
+  int32_t* d_list[2] = {nullptr, nullptr};
+  int32_t* d_nlist = nullptr;  // [2]
+  int32_t* d_key = nullptr;
+  int32_t* d_rank = nullptr;
+  int32_t* d_count = nullptr;
+  int32_t* d_offset = nullptr;
+  int32_t* d_perm = nullptr;
+  int4* d_items = nullptr;
+  int32_t* d_nitems = nullptr;
+  int2* d_partials = nullptr;
+  uint32_t* d_status = nullptr;
+  unsigned long long* d_fp64 = nullptr;
+  unsigned long long* d_tmp64 = nullptr;
+  uint32_t* d_pin = nullptr;
+  int64_t max_items = 0;
+  int n_tiles = 0;
+  std::vector<void*> allocs;
+
+  // state machine
+  int cur = 0;          // particle buffer holding the current state; grid parity of the next P2G
+  bool sorted = false;  // perm/items valid for pbuf[cur]
+  int phase = 0;        // 0 ready, 1 after P2G, 2 after grid op
+
+  // tuning / launch
+  int p2g_threads = 256, ppt = 2;
+  bool use_graph = true;
+  int p2g_blocks = 0, g2p_blocks = 0, grid_blocks = 0, io_blocks = 0;
+
+  // streams, graph, timing
+  cudaStream_t cs = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  bool graph_valid = false;
+  bool profiling = false;
+  std::vector<TimedPair> pending;
+  std::vector<cudaEvent_t> ev_pool;
+  double ktime_ms[KT_N] = {0, 0, 0, 0, 0};
+  int64_t kcount[KT_N] = {0, 0, 0, 0, 0};
+};
+
+namespace {
+
+int fail(mpm_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  else {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_create_err = msg;
+  }
+  return code;
+}
+
+#define CK(call)                                                                                    \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess)                                                                          \
+      return fail(ctx, MPM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));           \
+  } while (0)
+
+#define CKL()                                                                                       \
+  do {                                                                                              \
+    cudaError_t e_ = cudaGetLastError();                                                            \
+    if (e_ != cudaSuccess) return fail(ctx, MPM_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+int dalloc(mpm_ctx* ctx, T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, MPM_ERR_OOM, std::string("cudaMalloc of ") + std::to_string(count * sizeof(T)) + " bytes: " +
+                                      cudaGetErrorString(e));
+  }
+  ctx->allocs.push_back((void*)*p);
+  return MPM_OK;
+}
+
+KParams make_params(mpm_ctx* ctx, int src, int dst, int g) {
+  KParams P;
+  std::memset(&P, 0, sizeof(P));
+  P.scenes = ctx->d_scenes;
+  P.mats = ctx->d_mats;
+  P.block_scene = ctx->d_block_scene;
+  P.src = ctx->d_pbuf[src];
+  P.dst = ctx->d_pbuf[dst];
+  P.cap = ctx->cap;
+  P.nf = ctx->nf;
+  P.chunk = ctx->p2g_threads * ctx->ppt;
+  P.n = ctx->n;
+  P.K = ctx->K;
+  P.grid = ctx->d_grid[g];
+  P.grid_other = ctx->d_grid[1 - g];
+  P.flags = ctx->d_flags[g];
+  P.flags_other = ctx->d_flags[1 - g];
+  P.list = ctx->d_list[g];
+  P.nlist = ctx->d_nlist + g;
+  P.list_other = ctx->d_list[1 - g];
+  P.nlist_other = ctx->d_nlist + (1 - g);
+  P.key = ctx->d_key;
+  P.rank = ctx->d_rank;
+  P.count = ctx->d_count;
+  P.offset = ctx->d_offset;
+  P.perm = ctx->d_perm;
+  P.items = ctx->d_items;
+  P.n_items = ctx->d_nitems;
+  P.partials = ctx->d_partials;
+  P.pin = ctx->d_pin;
+  P.eps_norm = ctx->eps_norm;
+  P.status = ctx->d_status;
+  P.fp64_count = ctx->d_fp64;
+  return P;
+}
+
+cudaEvent_t pool_event(mpm_ctx* ctx) {
+  if (!ctx->ev_pool.empty()) {
+    cudaEvent_t e = ctx->ev_pool.back();
+    ctx->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+struct Timer {
+  mpm_ctx* ctx;
+  cudaStream_t s;
+  int kind;
+  cudaEvent_t a = nullptr;
+  Timer(mpm_ctx* c, cudaStream_t st, int k) : ctx(c), s(st), kind(k) {
+    if (ctx->profiling) {
+      a = pool_event(ctx);
+      cudaEventRecord(a, s);
+    }
+  }
+  ~Timer() {
+    if (ctx->profiling) {
+      cudaEvent_t b = pool_event(ctx);
+      cudaEventRecord(b, s);
+      ctx->pending.push_back({kind, a, b});
+    }
+  }
+};
+
+int launch_sort(mpm_ctx* ctx, const KParams& P, cudaStream_t s) {
+  {
+    Timer t(ctx, s, KT_SCAN);
+    k_scan_reduce<<<ctx->n_tiles, SCAN_THREADS, 0, s>>>(P);
+    k_scan_partials<<<1, SCAN_THREADS, 0, s>>>(P, ctx->n_tiles);
+    k_scan_apply<<<ctx->n_tiles, SCAN_THREADS, 0, s>>>(P);
+  }
+  CKL();
+  if (ctx->n > 0) {
+    Timer t(ctx, s, KT_PERM);
+    k_perm<<<ctx->io_blocks, 256, 0, s>>>(P);
+  }
+  CKL();
+  return MPM_OK;
+}
+
+// Keys of the current state (after load / set_state), then the sort.
+int launch_rekey(mpm_ctx* ctx, cudaStream_t s) {
+  KParams P = make_params(ctx, ctx->cur, ctx->cur, ctx->cur);
+  if (ctx->n > 0) {
+    k_keys<<<ctx->g2p_blocks, 256, 0, s>>>(P);
+    CKL();
+  }
+  int r = launch_sort(ctx, P, s);
+  if (r) return r;
+  ctx->sorted = true;
+  return MPM_OK;
+}
+
+int launch_pre(mpm_ctx* ctx, int c, cudaStream_t s) {
+  KParams P = make_params(ctx, c, 1 - c, c);
+  Timer t(ctx, s, KT_P2G);
+  k_p2g<<<ctx->p2g_blocks, ctx->p2g_threads, 0, s>>>(P);
+  CKL();
+  return MPM_OK;
+}
+
+int launch_grid(mpm_ctx* ctx, int c, cudaStream_t s) {
+  KParams P = make_params(ctx, c, 1 - c, c);
+  Timer t(ctx, s, KT_GRID);
+  k_grid_op<<<ctx->grid_blocks, 256, 0, s>>>(P);
+  CKL();
+  return MPM_OK;
+}
+
+int launch_post(mpm_ctx* ctx, int c, cudaStream_t s) {
+  KParams P = make_params(ctx, c, 1 - c, c);
+  {
+    Timer t(ctx, s, KT_G2P);
+    k_g2p<<<ctx->g2p_blocks, 256, 0, s>>>(P);
+  }
+  CKL();
+  return launch_sort(ctx, P, s);
+}
+
+int launch_substep(mpm_ctx* ctx, int c, cudaStream_t s) {
+  int r = launch_pre(ctx, c, s);
+  if (!r) r = launch_grid(ctx, c, s);
+  if (!r) r = launch_post(ctx, c, s);
+  return r;
+}
+
+int compute_launch_shapes(mpm_ctx* ctx) {
+  int occ = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_p2g, ctx->p2g_threads, 0));
+  ctx->p2g_blocks = ctx->n_sm * (occ > 0 ? occ : 1);
+  int occ2 = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, k_g2p, 256, 0));
+  int64_t want = (ctx->n + 255) / 256;
+  int64_t lim = (int64_t)ctx->n_sm * (occ2 > 0 ? occ2 : 1);
+  ctx->g2p_blocks = (int)(want < 1 ? 1 : (want < lim ? want : lim));
+  ctx->grid_blocks = ctx->n_sm * 8;
+  int64_t io = (ctx->n + 255) / 256;
+  ctx->io_blocks = (int)(io < 1 ? 1 : (io < ctx->n_sm * 16 ? io : ctx->n_sm * 16));
+  return MPM_OK;
+}
+
+void drop_graph(mpm_ctx* ctx) {
+  if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+  ctx->gexec = nullptr;
+  ctx->graph_valid = false;
+}
+
+// Two substeps (parity 0 then 1) captured once; replays keep `cur` at 0.
+int ensure_graph(mpm_ctx* ctx) {
+  if (ctx->graph_valid) return MPM_OK;
+  drop_graph(ctx);
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(ctx->cs, cudaStreamCaptureModeThreadLocal));
+  int r = launch_substep(ctx, 0, ctx->cs);
+  if (!r) r = launch_substep(ctx, 1, ctx->cs);
+  cudaError_t e = cudaStreamEndCapture(ctx->cs, &g);
+  if (r) {
+    if (g) cudaGraphDestroy(g);
+    return r;
+  }
+  if (e != cudaSuccess) return fail(ctx, MPM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&ctx->gexec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(ctx, MPM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  ctx->graph_valid = true;
+  return MPM_OK;
+}
+
+int enter(mpm_ctx* ctx, void* stream) {
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaEventRecord(ctx->ev_in, (cudaStream_t)stream));
+  CK(cudaStreamWaitEvent(ctx->cs, ctx->ev_in, 0));
+  return MPM_OK;
+}
+
+int leave(mpm_ctx* ctx, void* stream) {
+  CK(cudaEventRecord(ctx->ev_out, ctx->cs));
+  CK(cudaStreamWaitEvent((cudaStream_t)stream, ctx->ev_out, 0));
+  return MPM_OK;
+}
+
+bool scene_range_ok(mpm_ctx* ctx, int64_t s0, int64_t s1) { return s0 >= 0 && s1 <= ctx->n_scenes && s0 < s1; }
+
+}  // namespace
+
+// =====================================================================================
+extern "C" {
+
+const char* mpm_last_error(const mpm_ctx* ctx) {
+  if (ctx) return ctx->err.c_str();
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  return g_create_err.c_str();
+}
+
+int mpm_ctx_create(const mpm_scene_config* scenes, int64_t n_scenes, const mpm_material* materials,
+                   int32_t n_materials, int32_t device, mpm_ctx** out) {
+  if (!out) return fail(nullptr, MPM_ERR_BAD_ARG, "out is NULL");
+  *out = nullptr;
+  if (!scenes || n_scenes <= 0) return fail(nullptr, MPM_ERR_BAD_ARG, "need at least one scene");
+  if (n_materials < 0 || (n_materials > 0 && !materials)) return fail(nullptr, MPM_ERR_BAD_ARG, "bad material table");
+  if ((int64_t)n_materials > (int64_t)INFO_MAT_MASK) return fail(nullptr, MPM_ERR_BAD_ARG, "too many materials");
+
+  mpm_ctx* ctx = new mpm_ctx();
+  ctx->device = device;
+  ctx->n_scenes = n_scenes;
+  ctx->n_mats = n_materials;
+
+  // materials: grouped by scene in ascending order
+  std::vector<int32_t> mat_begin(n_scenes, -1), mat_count(n_scenes, 0);
+  bool muscle = false;
+  int32_t prev_scene = -1;
+  for (int32_t i = 0; i < n_materials; ++i) {
+    const mpm_material& m = materials[i];
+    if (m.scene < 0 || m.scene >= n_scenes || m.scene < prev_scene) {
+      delete ctx;
+      return fail(nullptr, MPM_ERR_BAD_ARG, "materials must be grouped by scene in ascending scene order");
+    }
+    if (m.type < MPM_MAT_ELASTIC || m.type > MPM_MAT_MUSCLE) {
+      delete ctx;
+      return fail(nullptr, MPM_ERR_BAD_ARG, "unknown material type");
+    }
+    prev_scene = m.scene;
+    if (mat_begin[m.scene] < 0) mat_begin[m.scene] = i;
+    mat_count[m.scene]++;
+    muscle = muscle || m.type == MPM_MAT_MUSCLE;
+  }
+  ctx->nf = muscle ? NF_MUSCLE : NF_BASE;
+  ctx->mat_count_h = mat_count;
+
+  // scenes: derived constants exactly as MPMSolver.__init__ (mpm_solver.py:32-80)
+  int64_t K = 0, P = 0;
+  ctx->pbegin_h.resize(n_scenes + 1);
+  ctx->first_mat_h.resize(n_scenes);
+  std::vector<int32_t> block_scene_h;
+  for (int64_t s = 0; s < n_scenes; ++s) {
+    const mpm_scene_config& c = scenes[s];
+    if (!(c.grid_density > 0) || !(c.particle_size > 0) || !(c.substep_dt > 0) || c.n_particles < 0) {
+      delete ctx;
+      return fail(nullptr, MPM_ERR_BAD_ARG, "scene " + std::to_string(s) + ": invalid grid_density/particle_size/dt");
+    }
+    SceneDev S;
+    std::memset(&S, 0, sizeof(S));
+    const double dx = 1.0 / c.grid_density;
+    const double inv_dx = c.grid_density;
+    int64_t lo_cell[3], hi_cell[3], res[3];
+    double nodes = 1.0;
+    for (int d = 0; d < 3; ++d) {
+      if (!(c.upper_bound[d] > c.lower_bound[d])) {
+        delete ctx;
+        return fail(nullptr, MPM_ERR_BAD_ARG, "Invalid pair of upper_bound and lower_bound.");
+      }
+      lo_cell[d] = (int64_t)std::nearbyint(c.grid_density * c.lower_bound[d]);
+      hi_cell[d] = (int64_t)std::nearbyint(c.grid_density * c.upper_bound[d]);
+      res[d] = hi_cell[d] - lo_cell[d] + 1;
+      nodes *= (double)res[d];
+    }
+    if (nodes > 1e9) {
+      delete ctx;
+      return fail(nullptr, MPM_ERR_BAD_ARG,
+                  "Grid size larger than 1e9 not supported by MPM solver. Please reduce 'grid_density', or set "
+                  "tighter boundaries via 'lower_bound' / 'upper_bound'.");
+    }
+    const double pvol = c.particle_size * c.particle_size * c.particle_size * 1e3;
+    S.dx = (float)dx;
+    S.inv_dx = (float)inv_dx;
+    S.dt = (float)c.substep_dt;
+    S.stress_scale = (float)(-c.substep_dt * pvol * 4.0 * inv_dx * inv_dx);
+    for (int d = 0; d < 3; ++d) {
+      S.grav[d] = (float)c.gravity[d];
+      S.lo[d] = (float)(c.lower_bound[d] + 3.0 * dx);
+      S.hi[d] = (float)(c.upper_bound[d] - 3.0 * dx);
+      S.res[d] = (int32_t)res[d];
+      S.offset[d] = (int32_t)lo_cell[d];
+      S.bres[d] = (int32_t)((res[d] + BLK - 1) / BLK);
+    }
+    S.eps = (float)c.mass_eps;
+    S.restitution = (float)c.restitution;
+    S.mat_begin = mat_begin[s] < 0 ? 0 : mat_begin[s];
+    S.block_base = K;
+    S.p_begin = P;
+    S.n_particles = c.n_particles;
+    if (c.n_particles > 0 && mat_count[s] == 0) {
+      delete ctx;
+      return fail(nullptr, MPM_ERR_BAD_ARG, "scene " + std::to_string(s) + " has particles but no material");
+    }
+    const int64_t nb = (int64_t)S.bres[0] * S.bres[1] * S.bres[2];
+    block_scene_h.insert(block_scene_h.end(), nb, (int32_t)s);
+    K += nb;
+    ctx->pbegin_h[s] = P;
+    ctx->first_mat_h[s] = S.mat_begin;
+    P += c.n_particles;
+    ctx->scenes_h.push_back(S);
+    if (s == 0) ctx->eps_norm = (float)c.mass_eps;
+  }
+  ctx->pbegin_h[n_scenes] = P;
+  if (K + 2 >= (int64_t)INT32_MAX / 2 || P >= (int64_t)INT32_MAX / 2) {
+    delete ctx;
+    return fail(nullptr, MPM_ERR_BAD_ARG, "too many grid blocks or particles for one context");
+  }
+  ctx->K = K;
+  ctx->n = P;
+  ctx->cap = ((P + 63) / 64) * 64;
+  if (ctx->cap == 0) ctx->cap = 64;
+
+  for (int32_t i = 0; i < n_materials; ++i) {
+    const mpm_material& m = materials[i];
+    const mpm_scene_config& c = scenes[m.scene];
+    MaterialDev M;
+    std::memset(&M, 0, sizeof(M));
+    M.type = m.type;
+    M.flags = m.flags;
+    M.scene = m.scene;
+    M.mu = (float)m.mu;
+    M.lam = (float)m.lam;
+    const float pvol = (float)(c.particle_size * c.particle_size * c.particle_size * 1e3);
+    M.mass = pvol * (float)m.rho;  // mpm_solver.py:822, fp32 product
+    M.default_Jp = (float)m.default_Jp;
+    M.alpha = (float)m.friction_alpha;
+    M.sand_coef = m.mu != 0.0 ? (float)((3.0 * m.lam + 2.0 * m.mu) / (2.0 * m.mu)) : 0.f;
+    M.clamp_lo = (float)(1.0 - m.yield_lower);
+    M.clamp_hi = (float)(1.0 + m.yield_higher);
+    M.vm_ratio = m.mu != 0.0 ? (float)(m.von_mises_yield_stress / (2.0 * m.mu)) : 0.f;
+    M.stiffness = (float)m.stiffness;
+    ctx->mats_h.push_back(M);
+  }
+
+  int r = MPM_OK;
+  do {
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+      r = fail(nullptr, MPM_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+      break;
+    }
+    cudaDeviceProp prop;
+    e = cudaGetDeviceProperties(&prop, device);
+    if (e != cudaSuccess) {
+      r = fail(nullptr, MPM_ERR_CUDA, std::string("cudaGetDeviceProperties: ") + cudaGetErrorString(e));
+      break;
+    }
+    ctx->n_sm = prop.multiProcessorCount;
+    ctx->max_items = ctx->cap / 32 + K + 4;
+    ctx->n_tiles = (int)((K + 2 + SCAN_TILE - 1) / SCAN_TILE);
+    if ((r = dalloc(ctx, &ctx->d_scenes, n_scenes))) break;
+    if ((r = dalloc(ctx, &ctx->d_mats, n_materials > 0 ? n_materials : 1))) break;
+    if ((r = dalloc(ctx, &ctx->d_block_scene, K))) break;
+    if ((r = dalloc(ctx, &ctx->d_pbegin, n_scenes + 1))) break;
+    if ((r = dalloc(ctx, &ctx->d_first_mat, n_scenes))) break;
+    for (int b = 0; b < 2 && !r; ++b) {
+      if ((r = dalloc(ctx, &ctx->d_pbuf[b], (size_t)ctx->nf * ctx->cap))) break;
+      if ((r = dalloc(ctx, &ctx->d_grid[b], (size_t)K * BLK_NODES))) break;
+      if ((r = dalloc(ctx, &ctx->d_flags[b], K))) break;
+      if ((r = dalloc(ctx, &ctx->d_list[b], K))) break;
+    }
+    if (r) break;
+    if ((r = dalloc(ctx, &ctx->d_nlist, 2))) break;
+    if ((r = dalloc(ctx, &ctx->d_key, ctx->cap))) break;
+    if ((r = dalloc(ctx, &ctx->d_rank, ctx->cap))) break;
+    if ((r = dalloc(ctx, &ctx->d_perm, ctx->cap))) break;
+    if ((r = dalloc(ctx, &ctx->d_count, K + 2))) break;
+    if ((r = dalloc(ctx, &ctx->d_offset, K + 2))) break;
+    if ((r = dalloc(ctx, &ctx->d_items, ctx->max_items))) break;
+    if ((r = dalloc(ctx, &ctx->d_nitems, 1))) break;
+    if ((r = dalloc(ctx, &ctx->d_partials, ctx->n_tiles))) break;
+    if ((r = dalloc(ctx, &ctx->d_status, 1))) break;
+    if ((r = dalloc(ctx, &ctx->d_fp64, 1))) break;
+    if ((r = dalloc(ctx, &ctx->d_tmp64, 1))) break;
+  } while (0);
+  if (r) {
+    if (r != MPM_OK && ctx->err.size()) fail(nullptr, r, ctx->err);
+    mpm_ctx_destroy(ctx);
+    return r;
+  }
+#define CKC(call)                                                                                   \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess) {                                                                        \
+      fail(nullptr, MPM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));              \
+      mpm_ctx_destroy(ctx);                                                                         \
+      return MPM_ERR_CUDA;                                                                          \
+    }                                                                                               \
+  } while (0)
+  CKC(cudaStreamCreateWithFlags(&ctx->cs, cudaStreamNonBlocking));
+  CKC(cudaEventCreateWithFlags(&ctx->ev_in, cudaEventDisableTiming));
+  CKC(cudaEventCreateWithFlags(&ctx->ev_out, cudaEventDisableTiming));
+  CKC(cudaMemcpyAsync(ctx->d_scenes, ctx->scenes_h.data(), sizeof(SceneDev) * n_scenes, cudaMemcpyHostToDevice, ctx->cs));
+  if (n_materials > 0)
+    CKC(cudaMemcpyAsync(ctx->d_mats, ctx->mats_h.data(), sizeof(MaterialDev) * n_materials, cudaMemcpyHostToDevice,
+                        ctx->cs));
+  if (K > 0)
+    CKC(cudaMemcpyAsync(ctx->d_block_scene, block_scene_h.data(), sizeof(int32_t) * K, cudaMemcpyHostToDevice, ctx->cs));
+  CKC(cudaMemcpyAsync(ctx->d_pbegin, ctx->pbegin_h.data(), sizeof(int64_t) * (n_scenes + 1), cudaMemcpyHostToDevice,
+                      ctx->cs));
+  CKC(cudaMemcpyAsync(ctx->d_first_mat, ctx->first_mat_h.data(), sizeof(int32_t) * n_scenes, cudaMemcpyHostToDevice,
+                      ctx->cs));
+  for (int b = 0; b < 2; ++b) {
+    CKC(cudaMemsetAsync(ctx->d_grid[b], 0, sizeof(float4) * (size_t)K * BLK_NODES, ctx->cs));
+    CKC(cudaMemsetAsync(ctx->d_flags[b], 0, sizeof(int32_t) * (size_t)(K > 0 ? K : 1), ctx->cs));
+    CKC(cudaMemsetAsync(ctx->d_pbuf[b], 0, sizeof(float) * (size_t)ctx->nf * ctx->cap, ctx->cs));
+  }
+  CKC(cudaMemsetAsync(ctx->d_nlist, 0, sizeof(int32_t) * 2, ctx->cs));
+  CKC(cudaMemsetAsync(ctx->d_count, 0, sizeof(int32_t) * (K + 2), ctx->cs));
+  CKC(cudaMemsetAsync(ctx->d_nitems, 0, sizeof(int32_t), ctx->cs));
+  CKC(cudaMemsetAsync(ctx->d_status, 0, sizeof(uint32_t), ctx->cs));
+  CKC(cudaMemsetAsync(ctx->d_fp64, 0, sizeof(unsigned long long), ctx->cs));
+  if (compute_launch_shapes(ctx)) {
+    fail(nullptr, MPM_ERR_CUDA, ctx->err);
+    mpm_ctx_destroy(ctx);
+    return MPM_ERR_CUDA;
+  }
+  if (ctx->n > 0 && n_materials > 0) {
+    KParams Pp = make_params(ctx, 0, 0, 0);
+    k_init_particles<<<ctx->io_blocks, 256, 0, ctx->cs>>>(Pp, ctx->d_pbegin, ctx->d_first_mat, n_scenes);
+    CKC(cudaGetLastError());
+  }
+  CKC(cudaStreamSynchronize(ctx->cs));
+#undef CKC
+  *out = ctx;
+  return MPM_OK;
+}
+
+int mpm_ctx_destroy(mpm_ctx* ctx) {
+  if (!ctx) return MPM_OK;
+  cudaSetDevice(ctx->device);
+  if (ctx->cs) cudaStreamSynchronize(ctx->cs);
+  drop_graph(ctx);
+  for (auto& tp : ctx->pending) {
+    cudaEventDestroy(tp.a);
+    cudaEventDestroy(tp.b);
+  }
+  for (auto e : ctx->ev_pool) cudaEventDestroy(e);
+  for (void* p : ctx->allocs) cudaFree(p);
+  if (ctx->d_pin) cudaFree(ctx->d_pin);
+  if (ctx->ev_in) cudaEventDestroy(ctx->ev_in);
+  if (ctx->ev_out) cudaEventDestroy(ctx->ev_out);
+  if (ctx->cs) cudaStreamDestroy(ctx->cs);
+  delete ctx;
+  return MPM_OK;
+}
+
+int mpm_add_particles(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end, int64_t particle_start, int64_t n,
+                      int32_t material, int32_t active, const float* pos, void* stream) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (!scene_range_ok(ctx, scene_begin, scene_end)) return fail(ctx, MPM_ERR_BAD_ARG, "bad scene range");
+  if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "add_particles inside a substep");
+  if (n <= 0) return MPM_OK;
+  if (!pos) return fail(ctx, MPM_ERR_BAD_ARG, "pos is NULL");
+  for (int64_t s = scene_begin; s < scene_end; ++s) {
+    const SceneDev& S = ctx->scenes_h[s];
+    if (material < 0 || material >= ctx->mat_count_h[s]) return fail(ctx, MPM_ERR_BAD_ARG, "material index out of range for scene");
+    if (particle_start < 0 || particle_start + n > S.n_particles)
+      return fail(ctx, MPM_ERR_BAD_ARG, "particle range exceeds the scene's capacity");
+  }
+  int r = enter(ctx, stream);
+  if (r) return r;
+  KParams P = make_params(ctx, ctx->cur, ctx->cur, ctx->cur);
+  k_add_particles<<<ctx->io_blocks, 256, 0, ctx->cs>>>(P, scene_begin, scene_end, particle_start, n, material, active,
+                                                       pos);
+  CKL();
+  ctx->sorted = false;
+  return leave(ctx, stream);
+}
+
+int mpm_get_state(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end, float* pos, float* vel, float* C, float* F,
+                  float* Jp, uint8_t* active, void* stream) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (!scene_range_ok(ctx, scene_begin, scene_end)) return fail(ctx, MPM_ERR_BAD_ARG, "bad scene range");
+  if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "get_state inside a substep");
+  int r = enter(ctx, stream);
+  if (r) return r;
+  KParams P = make_params(ctx, ctx->cur, ctx->cur, ctx->cur);
+  k_get_state<<<ctx->io_blocks, 256, 0, ctx->cs>>>(P, scene_begin, scene_end, pos, vel, C, F, Jp, active);
+  CKL();
+  return leave(ctx, stream);
+}
+
+int mpm_set_state(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end, const float* pos, const float* vel,
+                  const float* C, const float* F, const float* Jp, const uint8_t* active, void* stream) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (!scene_range_ok(ctx, scene_begin, scene_end)) return fail(ctx, MPM_ERR_BAD_ARG, "bad scene range");
+  if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "set_state inside a substep");
+  int r = enter(ctx, stream);
+  if (r) return r;
+  KParams P = make_params(ctx, ctx->cur, ctx->cur, ctx->cur);
+  k_set_state<<<ctx->io_blocks, 256, 0, ctx->cs>>>(P, scene_begin, scene_end, pos, vel, C, F, Jp, active);
+  CKL();
+  ctx->sorted = false;
+  return leave(ctx, stream);
+}
+
+static int particles_field(mpm_ctx* ctx, int32_t field, int write, int64_t s0, int64_t s1, int64_t start, int64_t n,
+                           float* data, void* stream) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (!scene_range_ok(ctx, s0, s1)) return fail(ctx, MPM_ERR_BAD_ARG, "bad scene range");
+  if (field < 0 || field > MPM_FIELD_POS_RESET) return fail(ctx, MPM_ERR_BAD_ARG, "unknown field");
+  if (field == MPM_FIELD_POS_RESET && !write) return fail(ctx, MPM_ERR_BAD_ARG, "POS_RESET is write-only");
+  if ((field == MPM_FIELD_ACTU || field == MPM_FIELD_MUSCLE_DIR) && ctx->nf == NF_BASE)
+    return fail(ctx, MPM_ERR_BAD_ARG, "no muscle material in this context");
+  if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "particle access inside a substep");
+  if (n <= 0) return MPM_OK;
+  if (!data) return fail(ctx, MPM_ERR_BAD_ARG, "data is NULL");
+  int r = enter(ctx, stream);
+  if (r) return r;
+  if (write && field == MPM_FIELD_FREE && !ctx->d_pin) {
+    const size_t words = ((size_t)ctx->K * BLK_NODES + 31) / 32;
+    cudaError_t e = cudaMalloc((void**)&ctx->d_pin, words * sizeof(uint32_t));
+    if (e != cudaSuccess) return fail(ctx, MPM_ERR_OOM, "pin bitmap allocation failed");
+    CK(cudaMemsetAsync(ctx->d_pin, 0, words * sizeof(uint32_t), ctx->cs));
+    drop_graph(ctx);
+  }
+  KParams P = make_params(ctx, ctx->cur, ctx->cur, ctx->cur);
+  k_particles_field<<<ctx->io_blocks, 256, 0, ctx->cs>>>(P, field, write, s0, s1, start, n, data);
+  CKL();
+  if (write && (field == MPM_FIELD_POS || field == MPM_FIELD_POS_RESET || field == MPM_FIELD_ACTIVE))
+    ctx->sorted = false;
+  return leave(ctx, stream);
+}
+
+int mpm_set_particles(mpm_ctx* ctx, int32_t field, int64_t scene_begin, int64_t scene_end, int64_t particle_start,
+                      int64_t n, const float* data, void* stream) {
+  return particles_field(ctx, field, 1, scene_begin, scene_end, particle_start, n, const_cast<float*>(data), stream);
+}
+
+int mpm_get_particles(mpm_ctx* ctx, int32_t field, int64_t scene_begin, int64_t scene_end, int64_t particle_start,
+                      int64_t n, float* data, void* stream) {
+  return particles_field(ctx, field, 0, scene_begin, scene_end, particle_start, n, data, stream);
+}
+
+int mpm_set_gravity(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end, const double* gravity_host) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (!scene_range_ok(ctx, scene_begin, scene_end) || !gravity_host) return fail(ctx, MPM_ERR_BAD_ARG, "bad args");
+  for (int64_t s = scene_begin; s < scene_end; ++s)
+    for (int d = 0; d < 3; ++d) ctx->scenes_h[s].grav[d] = (float)gravity_host[(s - scene_begin) * 3 + d];
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaMemcpyAsync(ctx->d_scenes + scene_begin, ctx->scenes_h.data() + scene_begin,
+                     sizeof(SceneDev) * (scene_end - scene_begin), cudaMemcpyHostToDevice, ctx->cs));
+  CK(cudaStreamSynchronize(ctx->cs));
+  return MPM_OK;
+}
+
+int mpm_substeps(mpm_ctx* ctx, int32_t n_substeps, void* stream) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (n_substeps < 0) return fail(ctx, MPM_ERR_BAD_ARG, "negative substep count");
+  if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "mpm_substeps inside a split substep");
+  if (n_substeps == 0) return MPM_OK;
+  int r = enter(ctx, stream);
+  if (r) return r;
+  if (!ctx->sorted && (r = launch_rekey(ctx, ctx->cs))) return r;
+  int left = n_substeps;
+  const bool graph = ctx->use_graph && !ctx->profiling && left >= 2;
+  if (graph) {
+    if (ctx->cur == 1) {
+      if ((r = launch_substep(ctx, 1, ctx->cs))) return r;
+      ctx->cur = 0;
+      --left;
+    }
+    if (left >= 2) {
+      if ((r = ensure_graph(ctx))) return r;
+      for (int i = 0; i + 1 < left; i += 2) CK(cudaGraphLaunch(ctx->gexec, ctx->cs));
+      left &= 1;
+    }
+  }
+  while (left-- > 0) {
+    if ((r = launch_substep(ctx, ctx->cur, ctx->cs))) return r;
+    ctx->cur ^= 1;
+  }
+  return leave(ctx, stream);
+}
+
+int mpm_substep_pre(mpm_ctx* ctx, void* stream) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "substep_pre called twice");
+  int r = enter(ctx, stream);
+  if (r) return r;
+  if (!ctx->sorted && (r = launch_rekey(ctx, ctx->cs))) return r;
+  if ((r = launch_pre(ctx, ctx->cur, ctx->cs))) return r;
+  ctx->phase = 1;
+  return leave(ctx, stream);
+}
+
+int mpm_substep_grid_op(mpm_ctx* ctx, void* stream) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (ctx->phase != 1) return fail(ctx, MPM_ERR_STATE, "grid_op must follow substep_pre");
+  int r = enter(ctx, stream);
+  if (r) return r;
+  if ((r = launch_grid(ctx, ctx->cur, ctx->cs))) return r;
+  ctx->phase = 2;
+  return leave(ctx, stream);
+}
+
+int mpm_substep_post(mpm_ctx* ctx, void* stream) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (ctx->phase != 2) return fail(ctx, MPM_ERR_STATE, "substep_post must follow grid_op");
+  int r = enter(ctx, stream);
+  if (r) return r;
+  if ((r = launch_post(ctx, ctx->cur, ctx->cs))) return r;
+  ctx->cur ^= 1;
+  ctx->phase = 0;
+  return leave(ctx, stream);
+}
+
+int mpm_get_grid(mpm_ctx* ctx, int64_t scene, float* out, void* stream) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (scene < 0 || scene >= ctx->n_scenes || !out) return fail(ctx, MPM_ERR_BAD_ARG, "bad args");
+  const int g = ctx->phase == 0 ? (ctx->cur ^ 1) : ctx->cur;
+  int r = enter(ctx, stream);
+  if (r) return r;
+  KParams P = make_params(ctx, ctx->cur, ctx->cur, g);
+  k_get_grid<<<ctx->n_sm * 8, 256, 0, ctx->cs>>>(P, scene, out);
+  CKL();
+  return leave(ctx, stream);
+}
+
+int mpm_count_touched_nodes(mpm_ctx* ctx, int64_t* out_host, void* stream) {
+  if (!ctx || !out_host) return MPM_ERR_BAD_ARG;
+  const int g = ctx->phase == 0 ? (ctx->cur ^ 1) : ctx->cur;
+  int r = enter(ctx, stream);
+  if (r) return r;
+  KParams P = make_params(ctx, ctx->cur, ctx->cur, g);
+  CK(cudaMemsetAsync(ctx->d_tmp64, 0, sizeof(unsigned long long), ctx->cs));
+  k_count_touched<<<ctx->n_sm * 8, 256, 0, ctx->cs>>>(P, ctx->d_tmp64);
+  CKL();
+  unsigned long long v = 0;
+  CK(cudaMemcpyAsync(&v, ctx->d_tmp64, sizeof(v), cudaMemcpyDeviceToHost, ctx->cs));
+  CK(cudaStreamSynchronize(ctx->cs));
+  *out_host = (int64_t)v;
+  return leave(ctx, stream);
+}
+
+int mpm_status_word(mpm_ctx* ctx, uint32_t* status_host, int64_t* fp64_svd_host, int32_t clear, void* stream) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  int r = enter(ctx, stream);
+  if (r) return r;
+  uint32_t st = 0;
+  unsigned long long f64 = 0;
+  CK(cudaMemcpyAsync(&st, ctx->d_status, sizeof(st), cudaMemcpyDeviceToHost, ctx->cs));
+  CK(cudaMemcpyAsync(&f64, ctx->d_fp64, sizeof(f64), cudaMemcpyDeviceToHost, ctx->cs));
+  if (clear) {
+    CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(uint32_t), ctx->cs));
+    CK(cudaMemsetAsync(ctx->d_fp64, 0, sizeof(unsigned long long), ctx->cs));
+  }
+  CK(cudaStreamSynchronize(ctx->cs));
+  if (status_host) *status_host = st;
+  if (fp64_svd_host) *fp64_svd_host = (int64_t)f64;
+  return leave(ctx, stream);
+}
+
+int mpm_set_tuning(mpm_ctx* ctx, int32_t p2g_threads, int32_t particles_per_thread, int32_t use_graph) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (p2g_threads < 64 || p2g_threads > 256 || p2g_threads % 32 || particles_per_thread < 1 ||
+      particles_per_thread > 16)
+    return fail(ctx, MPM_ERR_BAD_ARG, "tuning out of range (threads 64..256 step 32, ppt 1..16)");
+  if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "tuning inside a substep");
+  const bool changed = p2g_threads != ctx->p2g_threads || particles_per_thread != ctx->ppt;
+  ctx->p2g_threads = p2g_threads;
+  ctx->ppt = particles_per_thread;
+  ctx->use_graph = use_graph != 0;
+  if (changed) {
+    drop_graph(ctx);
+    ctx->sorted = false;  // work items depend on the chunk size
+    CK(cudaSetDevice(ctx->device));
+    return compute_launch_shapes(ctx);
+  }
+  return MPM_OK;
+}
+
+int mpm_get_info(const mpm_ctx* ctx, int64_t* n_particles, int64_t* n_blocks, int64_t* n_scenes) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (n_particles) *n_particles = ctx->n;
+  if (n_blocks) *n_blocks = ctx->K;
+  if (n_scenes) *n_scenes = ctx->n_scenes;
+  return MPM_OK;
+}
+
+int mpm_scene_grid_res(const mpm_ctx* ctx, int64_t scene, int32_t* res3_host) {
+  if (!ctx || scene < 0 || scene >= ctx->n_scenes || !res3_host) return MPM_ERR_BAD_ARG;
+  for (int d = 0; d < 3; ++d) res3_host[d] = ctx->scenes_h[scene].res[d];
+  return MPM_OK;
+}
+
+int mpm_set_profiling(mpm_ctx* ctx, int32_t enable) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  ctx->profiling = enable != 0;
+  return MPM_OK;
+}
+
+int mpm_kernel_times(mpm_ctx* ctx, double* ms_host, int64_t* counts_host, int32_t reset) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->cs));
+  for (auto& tp : ctx->pending) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, tp.a, tp.b));
+    ctx->ktime_ms[tp.kind] += ms;
+    ctx->kcount[tp.kind] += 1;
+    ctx->ev_pool.push_back(tp.a);
+    ctx->ev_pool.push_back(tp.b);
+  }
+  ctx->pending.clear();
+  for (int k = 0; k < KT_N; ++k) {
+    if (ms_host) ms_host[k] = ctx->ktime_ms[k];
+    if (counts_host) counts_host[k] = ctx->kcount[k];
+    if (reset) {
+      ctx->ktime_ms[k] = 0;
+      ctx->kcount[k] = 0;
+    }
+  }
+  return MPM_OK;
+}
+
+int mpm_version(void) { return 1; }
+
+}  // extern "C"

@@ -1,0 +1,144 @@
+// mpm_kernels.cuh - device data layout and kernel declarations of the MLS-MPM substep.
+//
+// Layout in HBM (all scenes of a context share one set of buffers):
+//  * particles: two buffers (ping-pong), each NF float planes of `cap` entries (SoA):
+//      0-2 pos, 3-5 vel, 6-14 C (row-major), 15-23 F, 24 Jp, 25 info (bits), 26 pid (bits),
+//      27 actu, 28-30 muscle direction (only when a muscle material exists).
+//    info = global material index (bits 0-23) | ACTIVE | FREE | DEAD.
+//    pid = particle index within its scene (reference particle order for get/set state).
+//  * grid: two buffers of float4 nodes grouped in blocks of 4x4x4 nodes (1 KiB each).
+//    Global block id = scene.block_base + (bx*bres_y + by)*bres_z + bz; node address =
+//    block*64 + (lx*4 + ly)*4 + lz.  Node = (momentum xyz, mass) after P2G and
+//    (velocity xyz, mass) after the grid op.
+//  * sort: particles are bucketed by the grid block that holds their stencil origin (the
+//    cell index at 4^3 granularity).  Buckets [0,K) are grid blocks, K holds inactive
+//    particles, K+1 particles of removed scenes.  key/rank come from G2P (warp-aggregated
+//    atomics on count[]); an exclusive scan gives bucket offsets and P2G work items;
+//    perm[new slot] = old slot drives the gather in the next P2G.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mpm_math.cuh"
+
+namespace gbmpm {
+
+constexpr int BLK = 4;                       // grid block edge (nodes)
+constexpr int BLK_NODES = BLK * BLK * BLK;   // 64
+constexpr int TILE = BLK + 2;                // P2G shared tile edge: block + stencil reach
+constexpr int TILE_NODES = TILE * TILE * TILE;  // 216
+constexpr int SCAN_TILE = 2048;              // buckets per scan CTA (256 threads x 8)
+constexpr int SCAN_THREADS = 256;
+constexpr int SVD_SWEEPS = 4;
+constexpr float SVD_FP64_TOL = 1e-5f;        // residual above which the SVD is redone in FP64
+
+enum : int {
+  PF_POS = 0,
+  PF_VEL = 3,
+  PF_C = 6,
+  PF_F = 15,
+  PF_JP = 24,
+  PF_INFO = 25,
+  PF_PID = 26,
+  PF_ACTU = 27,
+  PF_MDIR = 28,
+  NF_BASE = 27,
+  NF_MUSCLE = 31,
+};
+
+constexpr uint32_t INFO_MAT_MASK = 0x00FFFFFFu;
+constexpr uint32_t INFO_ACTIVE = 1u << 24;
+constexpr uint32_t INFO_FREE = 1u << 25;
+constexpr uint32_t INFO_DEAD = 1u << 26;
+
+struct SceneDev {
+  float dx, inv_dx, dt, stress_scale;  // stress_scale = -dt * p_vol * 4 * inv_dx^2
+  float grav[3], eps;
+  float lo[3], restitution;
+  float hi[3], pad0;
+  int32_t res[3], offset[3];  // grid nodes per axis; grid offset (cell index of node 0)
+  int32_t bres[3], mat_begin; // blocks per axis; first global material of this scene
+  int64_t block_base;         // first global block id of this scene
+  int64_t p_begin;            // first output row of this scene (reference [B, N] layout)
+  int64_t n_particles;
+};
+
+struct KParams {
+  const SceneDev* scenes;
+  const MaterialDev* mats;
+  const int32_t* block_scene;  // [K]
+  float* src;                  // particle planes read by P2G (old order)
+  float* dst;                  // particle planes written by P2G / updated in place by G2P
+  int64_t cap;
+  int32_t nf;
+  int32_t chunk;               // particles per P2G work item
+  int64_t n;                   // particles in use
+  int64_t K;                   // grid blocks (real buckets)
+  float4* grid;                // grid buffer of this substep
+  float4* grid_other;          // the other grid buffer (cleared by the grid op)
+  int32_t* flags;              // [K] block touched in `grid`
+  int32_t* flags_other;
+  int32_t* list;               // active blocks of `grid`
+  int32_t* nlist;
+  int32_t* list_other;
+  int32_t* nlist_other;
+  int32_t* key;                // [cap]
+  int32_t* rank;               // [cap]
+  int32_t* count;              // [K+2]
+  int32_t* offset;             // [K+2]
+  int32_t* perm;               // [cap]
+  int4* items;                 // P2G work items (bucket, begin, end, 0)
+  int32_t* n_items;
+  int2* partials;              // scan tile partials
+  uint32_t* pin;               // per-node bitmap of nodes touched by non-free particles (or null)
+  float eps_norm;              // gs.EPS for Matrix.norm(eps)
+  uint32_t* status;
+  unsigned long long* fp64_count;
+};
+
+// Block key of a world position; returns false if the stencil would leave the grid.
+__device__ __forceinline__ bool stencil_origin(const SceneDev& S, const float* x, int* b) {
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (!isfinite(x[d])) return false;
+    const float t = __fsub_rn(__fmul_rn(x[d], S.inv_dx), 0.5f);
+    const float f = floorf(t);
+    if (f < -1e9f || f > 1e9f) return false;
+    b[d] = (int)f - S.offset[d];
+    if (b[d] < 0 || b[d] > S.res[d] - 3) return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ int64_t block_of(const SceneDev& S, int gx, int gy, int gz) {
+  return S.block_base + ((int64_t)(gx >> 2) * S.bres[1] + (gy >> 2)) * S.bres[2] + (gz >> 2);
+}
+
+__device__ __forceinline__ int64_t node_addr(const SceneDev& S, int gx, int gy, int gz) {
+  return block_of(S, gx, gy, gz) * BLK_NODES + (((gx & 3) * 4 + (gy & 3)) * 4 + (gz & 3));
+}
+
+// ---------------------------------------------------------------- kernels
+__global__ void k_init_particles(KParams P, const int64_t* scene_pbegin, const int32_t* scene_first_mat,
+                                 int64_t n_scenes);
+__global__ void k_add_particles(KParams P, int64_t s0, int64_t s1, int64_t start, int64_t n_add, int32_t mat_local,
+                                int32_t active, const float* pos);
+__global__ void k_get_state(KParams P, int64_t s0, int64_t s1, float* pos, float* vel, float* C, float* F,
+                            float* Jp, uint8_t* active);
+__global__ void k_set_state(KParams P, int64_t s0, int64_t s1, const float* pos, const float* vel, const float* C,
+                            const float* F, const float* Jp, const uint8_t* active);
+__global__ void k_particles_field(KParams P, int field, int write, int64_t s0, int64_t s1, int64_t start,
+                                  int64_t n_sel, float* data);
+__global__ void k_g2p(KParams P);   // G2P + re-keying
+__global__ void k_keys(KParams P);  // re-keying only (after a state change)
+__global__ void k_scan_reduce(KParams P);
+__global__ void k_scan_partials(KParams P, int n_tiles);
+__global__ void k_scan_apply(KParams P);
+__global__ void k_perm(KParams P);
+__global__ void k_p2g(KParams P);
+__global__ void k_grid_op(KParams P);
+__global__ void k_get_grid(KParams P, int64_t scene, float* out);
+__global__ void k_count_touched(KParams P, unsigned long long* out);
+
+}  // namespace gbmpm

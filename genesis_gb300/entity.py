@@ -1,0 +1,285 @@
+"""MPMEntity: the drop-in for genesis/engine/entities/mpm_entity.py (+ particle_entity.py).
+
+Sampling happens at construction (particle_entity.py:234-356); state accessors return
+torch tensors on the CUDA device in the reference's [B, n, ...] layout.  Target setters
+(set_position / set_velocity / set_active) are buffered and applied at the start of the
+next step, like ParticleEntity.process_input (particle_entity.py:424-464).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib
+from .exceptions import GenesisException
+from .states import MPMEntityState
+
+ACTIVE = 1
+INACTIVE = 0
+
+
+class MPMEntity:
+    def __init__(self, scene, solver, material, morph, surface, particle_size, idx, particle_start, name=None):
+        from .morphs import Nowhere
+
+        self._scene = scene
+        self._solver = solver
+        self._material = material
+        self._morph = morph
+        self._surface = surface
+        self._particle_size = particle_size
+        self._idx = idx
+        self._particle_start = particle_start
+        self._name = name
+        self._uid = id(self)
+        self.sampler = material.sampler
+        particles = morph.sample(particle_size, self.sampler)
+        if particles.size == 0:
+            raise GenesisException("Entity has zero particles.")
+        if not isinstance(morph, Nowhere):
+            if not solver.boundary.is_inside(particles):
+                raise GenesisException(
+                    "Entity has particles outside solver boundary. Note that for MPMSolver, boundary is slightly "
+                    "tighter than the specified domain due to safety padding.\n\n"
+                    f"Current boundary:\n{solver.boundary}\n\nEntity to be added:\nmin: {particles.min(0)}\n"
+                    f"max: {particles.max(0)}\n"
+                )
+            origin = np.asarray(morph.pos, dtype=np.float64)
+        else:
+            origin = np.zeros(3)
+        self._particles = np.ascontiguousarray(particles, dtype=np.float64)
+        self._init_particles_offset = self._particles - origin
+        self._n_particles = len(self._particles)
+        self.active = not isinstance(morph, Nowhere)
+        self._tgt = {"pos": None, "vel": None, "act": None}
+
+    # ------------------------------------------------------------------ solver plumbing
+    def _add_to_solver(self):
+        self._solver._add_particles(
+            self._particle_start, self._n_particles, self._material.idx, self.active, self._particles
+        )
+
+    def _envs(self, envs_idx):
+        B = self._solver._B
+        if envs_idx is None:
+            return list(range(B))
+        if self._scene.n_envs == 0:
+            raise GenesisException("`envs_idx` is not supported for non-parallelized scene.")
+        if isinstance(envs_idx, slice):
+            return list(range(B))[envs_idx]
+        if isinstance(envs_idx, (int, np.integer)):
+            return [int(envs_idx)]
+        return [int(e) for e in torch.as_tensor(envs_idx).reshape(-1).tolist()]
+
+    def _get_field(self, field, width, envs_idx):
+        envs = self._envs(envs_idx)
+        out = torch.empty((len(envs), self._n_particles, width), dtype=torch.float32, device="cuda")
+        if envs == list(range(envs[0], envs[0] + len(envs))):
+            self._solver._field(field, 0, envs[0], envs[0] + len(envs), self._particle_start, self._n_particles, out)
+        else:
+            for i, e in enumerate(envs):
+                self._solver._field(field, 0, e, e + 1, self._particle_start, self._n_particles, out[i])
+        return out
+
+    def _write(self, field, envs, v):
+        if envs == list(range(envs[0], envs[0] + len(envs))):
+            self._solver._field(field, 1, envs[0], envs[0] + len(envs), self._particle_start, self._n_particles, v)
+        else:
+            for i, e in enumerate(envs):
+                self._solver._field(field, 1, e, e + 1, self._particle_start, self._n_particles, v[i].contiguous())
+
+    def _set_field(self, field, width, values, envs_idx, particles_idx_local=None):
+        """values broadcast to [B, n_sel, width]; n_sel = all particles or len(particles_idx_local)."""
+        envs = self._envs(envs_idx)
+        B = len(envs)
+        v = torch.as_tensor(values, dtype=torch.float32, device="cuda")
+        if particles_idx_local is None:
+            self._write(field, envs, torch.broadcast_to(v, (B, self._n_particles, width)).contiguous())
+        else:
+            idx = torch.as_tensor(particles_idx_local, device="cuda", dtype=torch.long)
+            idx = torch.broadcast_to(idx.reshape(-1) if idx.ndim <= 1 else idx, (B, idx.shape[-1]))
+            vv = torch.broadcast_to(v, (B, idx.shape[1], width))
+            sel = idx[..., None]
+            if field == _lib.FIELD_POS_RESET:  # reset v, C, F, Jp of the selected particles only
+                resets = (
+                    (_lib.FIELD_POS, 3, vv),
+                    (_lib.FIELD_VEL, 3, torch.zeros_like(vv)),
+                    (_lib.FIELD_C, 9, torch.zeros((B, idx.shape[1], 9), device="cuda")),
+                    (_lib.FIELD_F, 9, torch.eye(3, device="cuda").reshape(1, 1, 9).expand(B, idx.shape[1], 9)),
+                    (_lib.FIELD_JP, 1, torch.full((B, idx.shape[1], 1), float(self._material._default_Jp), device="cuda")),
+                )
+                for f, w, val in resets:
+                    full = self._get_field(f, w, envs_idx)
+                    full.scatter_(1, sel.expand(-1, -1, w), val)
+                    self._write(f, envs, full.contiguous())
+            else:
+                full = self._get_field(field, width, envs_idx)
+                full.scatter_(1, sel.expand(-1, -1, width), vv)
+                self._write(field, envs, full.contiguous())
+        torch.cuda.current_stream().synchronize()
+
+    def _squeeze(self, t):
+        return t[0] if self._scene.n_envs == 0 else t
+
+    # ------------------------------------------------------------------ targets (applied at step start)
+    def set_position(self, value, envs_idx=None):
+        """Per-particle positions, or the centre of mass relative to the initial shape (particle_entity.py:509-527)."""
+        poss = torch.as_tensor(value, dtype=torch.float32, device="cuda")
+        if poss.ndim == 1 or (poss.ndim == 2 and poss.shape[0] != self._n_particles):
+            off = torch.as_tensor(self._init_particles_offset, dtype=torch.float32, device="cuda")
+            poss = off + poss[..., None, :]
+        self._tgt["pos"] = (poss, envs_idx)
+
+    def set_velocity(self, vels, envs_idx=None):
+        self._tgt["vel"] = (torch.as_tensor(vels, dtype=torch.float32, device="cuda"), envs_idx)
+
+    def set_active(self, actives, envs_idx=None):
+        a = torch.as_tensor(actives, device="cuda")
+        self._tgt["act"] = (a, envs_idx)
+        self.active = bool((a == ACTIVE).any())
+
+    def activate(self):
+        self.set_active(ACTIVE)
+
+    def deactivate(self):
+        self.set_active(INACTIVE)
+
+    def process_input(self, in_backward=False):
+        # positions first: setting positions resets velocities (particle_entity.py:448-451)
+        if self._tgt["pos"] is not None:
+            self.set_particles_pos(*self._tgt["pos"][:1], envs_idx=self._tgt["pos"][1])
+        if self._tgt["vel"] is not None:
+            self.set_particles_vel(self._tgt["vel"][0], envs_idx=self._tgt["vel"][1])
+        if self._tgt["act"] is not None:
+            self.set_particles_active(self._tgt["act"][0], envs_idx=self._tgt["act"][1])
+        self._tgt = {"pos": None, "vel": None, "act": None}
+
+    # ------------------------------------------------------------------ immediate setters/getters
+    def set_particles_pos(self, poss, particles_idx_local=None, envs_idx=None):
+        """mpm_solver.py:840-859: positions set, v/F/C/Jp reset."""
+        self._set_field(_lib.FIELD_POS_RESET, 3, poss, envs_idx, particles_idx_local)
+
+    def set_particles_vel(self, vels, particles_idx_local=None, envs_idx=None):
+        self._set_field(_lib.FIELD_VEL, 3, vels, envs_idx, particles_idx_local)
+
+    def set_particles_active(self, actives, particles_idx_local=None, envs_idx=None):
+        a = torch.as_tensor(actives, device="cuda").to(torch.float32)
+        self._set_field(_lib.FIELD_ACTIVE, 1, a[..., None], envs_idx, particles_idx_local)
+
+    def set_particles_actu(self, actus, particles_idx_local=None, envs_idx=None):
+        a = torch.as_tensor(actus, dtype=torch.float32, device="cuda")
+        self._set_field(_lib.FIELD_ACTU, 1, a[..., None], envs_idx, particles_idx_local)
+
+    def set_actuation(self, actus, envs_idx=None):
+        """Muscle actuation of a single-group muscle: one value per env for all its particles."""
+        a = torch.as_tensor(actus, dtype=torch.float32, device="cuda").reshape(-1, 1, 1)
+        self._set_field(_lib.FIELD_ACTU, 1, a, envs_idx)
+
+    def set_muscle_direction(self, muscle_direction):
+        d = torch.as_tensor(muscle_direction, dtype=torch.float32, device="cuda").reshape(-1, 3)
+        d = d.expand(self._n_particles, 3) if d.shape[0] == 1 else d
+        self._set_field(_lib.FIELD_MUSCLE_DIR, 3, d, None)
+
+    def set_free(self, free):
+        f = torch.as_tensor(free, device="cuda").to(torch.float32).reshape(-1)
+        f = f.expand(self._n_particles) if f.numel() == 1 else f
+        self._set_field(_lib.FIELD_FREE, 1, f[:, None], None)
+
+    def get_free(self):
+        return self._get_field(_lib.FIELD_FREE, 1, None)[0, :, 0] != 0
+
+    def get_particles_pos(self, envs_idx=None):
+        return self._squeeze(self._get_field(_lib.FIELD_POS, 3, envs_idx))
+
+    def get_particles_vel(self, envs_idx=None):
+        return self._squeeze(self._get_field(_lib.FIELD_VEL, 3, envs_idx))
+
+    def get_particles_active(self, envs_idx=None):
+        return self._squeeze(self._get_field(_lib.FIELD_ACTIVE, 1, envs_idx)[..., 0] != 0)
+
+    def get_particles_actu(self, envs_idx=None):
+        return self._squeeze(self._get_field(_lib.FIELD_ACTU, 1, envs_idx)[..., 0])
+
+    def get_state(self) -> MPMEntityState:
+        """mpm_entity.py:278-302 / get_frame :305-352."""
+        B = self._solver._B
+        st = MPMEntityState(self, self._scene.sim.cur_step_global, B, self._n_particles, "cuda")
+        st.pos = self._get_field(_lib.FIELD_POS, 3, None)
+        st.vel = self._get_field(_lib.FIELD_VEL, 3, None)
+        st.C = self._get_field(_lib.FIELD_C, 9, None).reshape(B, -1, 3, 3)
+        st.F = self._get_field(_lib.FIELD_F, 9, None).reshape(B, -1, 3, 3)
+        st.Jp = self._get_field(_lib.FIELD_JP, 1, None)[..., 0]
+        st.active = (self._get_field(_lib.FIELD_ACTIVE, 1, None)[..., 0] != 0).to(torch.int64)
+        return st
+
+    def get_mass(self, envs_idx=None):
+        """particle_entity.py:692-714: total mass (particle_volume * rho, unscaled), per env."""
+        envs = self._envs(envs_idx)
+        m = np.float32(np.float32(self._solver.particle_volume) * np.float32(self._material.rho)) * self._n_particles
+        m = float(m) / self._solver.particle_volume_scale
+        out = torch.full((len(envs),), m, dtype=torch.float32, device="cuda")
+        return out[0] if self._scene.n_envs == 0 else out
+
+    def get_particles_in_bbox(self, bbox_min, bbox_max):
+        pos = self._get_field(_lib.FIELD_POS, 3, None)
+        lo = torch.as_tensor(bbox_min, dtype=torch.float32, device="cuda")
+        hi = torch.as_tensor(bbox_max, dtype=torch.float32, device="cuda")
+        return ((pos >= lo) & (pos <= hi)).all(-1)
+
+    # ------------------------------------------------------------------ properties
+    @property
+    def uid(self):
+        return self._uid
+
+    @property
+    def idx(self):
+        return self._idx
+
+    @property
+    def name(self):
+        return self._name
+
+    @property
+    def morph(self):
+        return self._morph
+
+    @property
+    def material(self):
+        return self._material
+
+    @property
+    def surface(self):
+        return self._surface
+
+    @property
+    def solver(self):
+        return self._solver
+
+    @property
+    def scene(self):
+        return self._scene
+
+    @property
+    def sim(self):
+        return self._scene.sim
+
+    @property
+    def n_particles(self):
+        return self._n_particles
+
+    @property
+    def particle_start(self):
+        return self._particle_start
+
+    @property
+    def particle_end(self):
+        return self._particle_start + self._n_particles
+
+    @property
+    def particle_size(self):
+        return self._particle_size
+
+    @property
+    def init_particles(self):
+        return self._particles

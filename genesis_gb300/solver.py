@@ -1,0 +1,370 @@
+"""MPMSolver: the drop-in for genesis/engine/solvers/mpm_solver.py::MPMSolver.
+
+Keeps the reference solver's construction, properties and Solver-protocol methods
+(build, add_entity, add_material, substep_pre_coupling/substep_post_coupling, get_state,
+set_state, set_gravity, ...) and runs every substep through libgbmpm.so.  Each reference
+env is one scene of the library context.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import warnings
+
+import numpy as np
+import torch
+
+from . import _lib
+from .exceptions import GenesisException
+from .states import MPMSolverState
+
+
+class CubeBoundary:
+    """genesis/engine/boundaries/boundaries.py:10-32 (host-side description)."""
+
+    def __init__(self, lower, upper, restitution=0.0):
+        self.restitution = restitution
+        self.upper = np.array(upper, dtype=np.float32)
+        self.lower = np.array(lower, dtype=np.float32)
+        assert (self.upper >= self.lower).all()
+
+    def is_inside(self, pos) -> bool:
+        return bool(np.all(pos < self.upper) and np.all(pos > self.lower))
+
+    def __repr__(self):
+        return f"CubeBoundary(lower={self.lower.tolist()}, upper={self.upper.tolist()})"
+
+
+def _stream_handle():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class MPMSolver:
+    def __init__(self, scene, sim, options):
+        import genesis_gb300 as gs
+
+        self._scene = scene
+        self._sim = sim
+        self._options = options
+        self._dt = options.dt
+        self._substep_dt = options.dt / sim.substeps
+        self._init_gravity = options.gravity
+        self._entities = []
+        self._materials = []
+        self._materials_idx = []
+        self._ctx = None
+        self._B = 1
+        self._eps = gs.EPS
+        # mpm_solver.py:36-80
+        self._grid_density = options.grid_density
+        self._particle_size = options.particle_size
+        self._upper_bound = np.array(options.upper_bound)
+        self._lower_bound = np.array(options.lower_bound)
+        self._enable_CPIC = options.enable_CPIC
+        self._particle_volume_real = float(self._particle_size**3)
+        self._particle_volume_scale = 1e3
+        self._particle_volume = self._particle_volume_real * self._particle_volume_scale
+        self._dx = float(1.0 / self._grid_density)
+        self._inv_dx = float(self._grid_density)
+        self._lower_bound_cell = np.round(self._grid_density * self._lower_bound).astype(np.int32)
+        self._upper_bound_cell = np.round(self._grid_density * self._upper_bound).astype(np.int32)
+        self._grid_res = self._upper_bound_cell - self._lower_bound_cell + 1
+        self._grid_offset = self._lower_bound_cell.copy()
+        if np.prod(self._grid_res.astype(np.float64)) > 1e9:
+            raise GenesisException(
+                "Grid size larger than 1e9 not supported by MPM solver. Please reduce 'grid_density', or set tighter "
+                "boundaries via 'lower_bound' / 'upper_bound'."
+            )
+        self.boundary_padding = 3 * self._dx
+        self.boundary = CubeBoundary(
+            lower=self._lower_bound + self.boundary_padding, upper=self._upper_bound - self.boundary_padding
+        )
+        self._gravity = None
+
+    # ------------------------------------------------------------------ entities / materials
+    @property
+    def is_active(self) -> bool:
+        return self.n_particles > 0
+
+    def add_material(self, material):
+        """mpm_solver.py:272-283: dedupe equal materials, assign material.idx."""
+        for m in self._materials:
+            if material == m:
+                material.idx = m.idx
+                break
+        else:
+            material.idx = len(self._materials_idx)
+            self._materials_idx.append(material.idx)
+        self._materials.append(material)
+
+    def add_entity(self, idx, material, morph, surface, name=None):
+        from .entity import MPMEntity
+
+        self.add_material(material)
+        entity = MPMEntity(
+            scene=self._scene,
+            solver=self,
+            material=material,
+            morph=morph,
+            surface=surface,
+            particle_size=self._particle_size,
+            idx=idx,
+            particle_start=self.n_particles,
+            name=name,
+        )
+        self._entities.append(entity)
+        return entity
+
+    def _unique_materials(self):
+        seen = {}
+        for m in self._materials:
+            seen.setdefault(m.idx, m)
+        return [seen[i] for i in sorted(seen)]
+
+    # ------------------------------------------------------------------ build
+    def build(self, B: int) -> None:
+        self._B = B
+        if not self.is_active:
+            return
+        lib = _lib.load()
+        n = self.n_particles
+        if n * B * 3 > np.iinfo(np.int32).max:
+            raise GenesisException("Particle count too large for int32 indexing.")
+        g = np.asarray(self._init_gravity if self._init_gravity is not None else (0.0, 0.0, 0.0), dtype=np.float64)
+        self._gravity = np.tile(g, (B, 1))
+        cfgs = (_lib.MpmSceneConfig * B)()
+        for b in range(B):
+            c = cfgs[b]
+            c.substep_dt = self._substep_dt
+            for d in range(3):
+                c.gravity[d] = float(g[d])
+                c.lower_bound[d] = float(self._lower_bound[d])
+                c.upper_bound[d] = float(self._upper_bound[d])
+            c.grid_density = float(self._grid_density)
+            c.particle_size = float(self._particle_size)
+            c.mass_eps = float(self._eps)
+            c.restitution = 0.0
+            c.n_particles = n
+        mats = self._unique_materials()
+        mat_arr = (_lib.MpmMaterial * (len(mats) * B))()
+        for b in range(B):
+            for j, m in enumerate(mats):
+                mat_arr[b * len(mats) + j] = m.to_c(b)
+        ctx = ctypes.c_void_p()
+        dev = torch.cuda.current_device()
+        ret = lib.mpm_ctx_create(cfgs, B, mat_arr, len(mats) * B, dev, ctypes.byref(ctx))
+        _lib.check(ret, None, "mpm_ctx_create")
+        self._ctx = ctx
+        self._lib = lib
+        # dt stability warning (mpm_solver.py:230-235)
+        suggested_dt = 2e-2 * self._dx
+        if self._substep_dt > suggested_dt:
+            warnings.warn(
+                f"Current `substep_dt` ({self._substep_dt:.6g}) is greater than suggested_dt ({suggested_dt:.6g}, "
+                "calculated based on `grid_density`). Simulation might be unstable."
+            )
+        for entity in self._entities:
+            entity._add_to_solver()
+
+    def _add_particles(self, particle_start, n, material_idx, active, pos_np):
+        pos = torch.as_tensor(np.ascontiguousarray(pos_np, dtype=np.float32), device="cuda")
+        ret = self._lib.mpm_add_particles(
+            self._ctx, 0, self._B, particle_start, n, material_idx, int(active), _lib.ptr(pos), _stream_handle()
+        )
+        _lib.check(ret, self._ctx, "mpm_add_particles")
+        torch.cuda.current_stream().synchronize()
+
+    def destroy(self) -> None:
+        if self._ctx is not None:
+            self._lib.mpm_ctx_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------------ stepping
+    def process_input(self, in_backward=False):
+        for e in self._entities:
+            e.process_input(in_backward=in_backward)
+
+    def substeps(self, n: int) -> None:
+        """Run n fused substeps (no host sync)."""
+        if self._ctx is None:
+            return
+        _lib.check(self._lib.mpm_substeps(self._ctx, int(n), _stream_handle()), self._ctx, "mpm_substeps")
+
+    def substep_pre_coupling(self, f=0):
+        _lib.check(self._lib.mpm_substep_pre(self._ctx, _stream_handle()), self._ctx, "mpm_substep_pre")
+
+    def couple(self, f=0):
+        """LegacyCoupler.mpm_grid_op for MPM alone (legacy_coupler.py:356-501)."""
+        _lib.check(self._lib.mpm_substep_grid_op(self._ctx, _stream_handle()), self._ctx, "mpm_substep_grid_op")
+
+    def substep_post_coupling(self, f=0):
+        _lib.check(self._lib.mpm_substep_post(self._ctx, _stream_handle()), self._ctx, "mpm_substep_post")
+
+    def check_state(self) -> None:
+        """Raise like mpm_solver.py:542-546 if any substep produced NaN (one host sync)."""
+        if self._ctx is None:
+            return
+        st = ctypes.c_uint32()
+        ret = self._lib.mpm_status_word(self._ctx, ctypes.byref(st), None, 1, _stream_handle())
+        _lib.check(ret, self._ctx, "mpm_status_word")
+        if st.value & _lib.STATUS_NAN:
+            raise GenesisException(
+                "NaN detected in MPM states. Try reducing the time step size or adjusting simulation parameters."
+            )
+        if st.value & _lib.STATUS_OOB:
+            raise GenesisException("MPM particles left the simulation grid (stencil out of bounds).")
+
+    def fp64_svd_count(self, reset: bool = False) -> int:
+        st = ctypes.c_uint32()
+        n = ctypes.c_int64()
+        _lib.check(self._lib.mpm_status_word(self._ctx, ctypes.byref(st), ctypes.byref(n), int(reset), _stream_handle()))
+        return n.value
+
+    # ------------------------------------------------------------------ state io
+    def get_state(self, f=None) -> MPMSolverState | None:
+        if not self.is_active:
+            return None
+        s = MPMSolverState(self._B, self.n_particles, "cuda")
+        ret = self._lib.mpm_get_state(
+            self._ctx, 0, self._B, _lib.ptr(s.pos), _lib.ptr(s.vel), _lib.ptr(s.C), _lib.ptr(s.F), _lib.ptr(s.Jp),
+            _lib.ptr(s.active), _stream_handle()
+        )
+        _lib.check(ret, self._ctx, "mpm_get_state")
+        return s
+
+    def set_state(self, f, state, envs_idx=None) -> None:
+        if not self.is_active:
+            return
+
+        def dev(t, dtype=torch.float32):
+            return None if t is None else t.detach().to(device="cuda", dtype=dtype).contiguous()
+
+        pos, vel, C, F, Jp = (dev(getattr(state, k)) for k in ("pos", "vel", "C", "F", "Jp"))
+        act = dev(state.active, torch.uint8)
+        ret = self._lib.mpm_set_state(
+            self._ctx, 0, self._B, _lib.ptr(pos), _lib.ptr(vel), _lib.ptr(C), _lib.ptr(F), _lib.ptr(Jp), _lib.ptr(act),
+            _stream_handle()
+        )
+        _lib.check(ret, self._ctx, "mpm_set_state")
+        torch.cuda.current_stream().synchronize()
+
+    def get_grid(self, scene: int = 0) -> torch.Tensor:
+        """Dense [gx, gy, gz, 4] grid of one env (momentum+mass after P2G, velocity+mass after the grid op)."""
+        res = (ctypes.c_int32 * 3)()
+        _lib.check(self._lib.mpm_scene_grid_res(self._ctx, scene, res), self._ctx, "mpm_scene_grid_res")
+        out = torch.empty((res[0], res[1], res[2], 4), dtype=torch.float32, device="cuda")
+        _lib.check(self._lib.mpm_get_grid(self._ctx, scene, _lib.ptr(out), _stream_handle()), self._ctx, "mpm_get_grid")
+        return out
+
+    def set_gravity(self, gravity, envs_idx=None) -> None:
+        g = np.asarray(gravity, dtype=np.float64).reshape(-1, 3)
+        envs = list(range(self._B)) if envs_idx is None else [int(e) for e in np.atleast_1d(envs_idx)]
+        if g.shape[0] == 1:
+            g = np.tile(g, (len(envs), 1))
+        for i, e in enumerate(envs):
+            self._gravity[e] = g[i]
+            arr = (ctypes.c_double * 3)(*g[i])
+            _lib.check(self._lib.mpm_set_gravity(self._ctx, e, e + 1, arr), self._ctx, "mpm_set_gravity")
+
+    def get_gravity(self, envs_idx=None):
+        return None if self._gravity is None else self._gravity.copy()
+
+    # field helpers used by entities
+    def _field(self, field, write, s0, s1, start, n, data):
+        fn = self._lib.mpm_set_particles if write else self._lib.mpm_get_particles
+        _lib.check(fn(self._ctx, field, s0, s1, start, n, _lib.ptr(data), _stream_handle()), self._ctx, "particles")
+
+    # ------------------------------------------------------------------ properties
+    @property
+    def n_particles(self) -> int:
+        return sum(e.n_particles for e in self._entities)
+
+    @property
+    def entities(self):
+        return self._entities
+
+    @property
+    def n_entities(self):
+        return len(self._entities)
+
+    @property
+    def dt(self):
+        return self._dt
+
+    @property
+    def substep_dt(self):
+        return self._substep_dt
+
+    @property
+    def grid_density(self):
+        return self._grid_density
+
+    @property
+    def particle_size(self):
+        return self._particle_size
+
+    @property
+    def particle_radius(self):
+        return self._particle_size / 2.0
+
+    @property
+    def upper_bound(self):
+        return self._upper_bound
+
+    @property
+    def lower_bound(self):
+        return self._lower_bound
+
+    @property
+    def dx(self):
+        return self._dx
+
+    @property
+    def inv_dx(self):
+        return self._inv_dx
+
+    @property
+    def particle_volume_real(self):
+        return self._particle_volume_real
+
+    @property
+    def particle_volume(self):
+        return self._particle_volume
+
+    @property
+    def particle_volume_scale(self):
+        return self._particle_volume_scale
+
+    @property
+    def lower_bound_cell(self):
+        return self._lower_bound_cell
+
+    @property
+    def upper_bound_cell(self):
+        return self._upper_bound_cell
+
+    @property
+    def grid_res(self):
+        return self._grid_res
+
+    @property
+    def grid_offset(self):
+        return self._grid_offset
+
+    @property
+    def enable_CPIC(self):
+        return self._enable_CPIC
+
+    @property
+    def gravity(self):
+        return self._gravity
+
+    @property
+    def ctx(self):
+        return self._ctx

@@ -1,0 +1,215 @@
+/*
+ * gbmpm.h - C ABI of the GB300-native MLS-MPM substep library (libgbmpm.so).
+ *
+ * The reference (Genesis, genesis-world 0.4.5) has no native FFI for this path: its MPM
+ * solver is Python written as Quadrants kernels, and the "plugin" boundary is the Solver
+ * protocol that genesis/engine/simulator.py calls.  Every entry point below names the
+ * reference kernel or method it replaces (file:line, paths relative to the Genesis
+ * project root).  The Python package genesis_gb300 binds these with ctypes; a Genesis
+ * maintainer would bind them the same way (a ctypes stub is shown in INTEGRATION.md).
+ *
+ * Conventions
+ *  - Every function returns an mpm_status code (0 = OK).  No C++ exception crosses the ABI.
+ *  - Array arguments are DEVICE pointers unless the name ends in _host.  They use the
+ *    reference's layouts: pos/vel [B, N, 3], C/F [B, N, 3, 3] row-major, Jp [B, N],
+ *    active [B, N] (uint8), all float32, where B is a range of scenes ("envs") and N the
+ *    per-scene particle count.  Ragged scenes are laid out back to back in scene order.
+ *  - `stream` is a cudaStream_t passed as void*; NULL means the legacy default stream.
+ *    Work is enqueued on it; no entry point synchronises the host unless it says so.
+ *  - No pointer passed in is retained after the call returns.
+ */
+#ifndef GBMPM_H
+#define GBMPM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+typedef enum mpm_status {
+  MPM_OK = 0,
+  MPM_ERR_BAD_ARG = 1,   /* invalid argument / configuration (reference: gs.raise_exception) */
+  MPM_ERR_CUDA = 2,      /* a CUDA runtime call failed; mpm_last_error() has the text */
+  MPM_ERR_OOM = 3,       /* device allocation failed */
+  MPM_ERR_NAN = 4,       /* NaN in particle positions (mpm_solver.py:542-546) */
+  MPM_ERR_OOB = 5,       /* a particle's stencil left the grid; the particle was skipped */
+  MPM_ERR_TIMEOUT = 6,   /* a bounded device wait gave up */
+  MPM_ERR_STATE = 7      /* call not valid in the context's current state */
+} mpm_status;
+
+/* Bits of the device status word returned by mpm_status_word(). */
+#define MPM_STATUS_NAN 0x1u
+#define MPM_STATUS_OOB 0x2u
+
+/* ---------------------------------------------------------------- materials */
+/* Material models of genesis/engine/materials/MPM/*.py */
+typedef enum mpm_material_type {
+  MPM_MAT_ELASTIC = 0,       /* elastic.py:32-60 (corotation; flag NEOHOOKEAN for the alternative) */
+  MPM_MAT_LIQUID = 1,        /* liquid.py:30-49 */
+  MPM_MAT_SAND = 2,          /* sand.py:38-84 (Drucker-Prager) */
+  MPM_MAT_SNOW = 3,          /* snow.py:42-74 */
+  MPM_MAT_ELASTOPLASTIC = 4, /* elasto_plastic.py:40-71 (flag VON_MISES selects the von Mises branch) */
+  MPM_MAT_MUSCLE = 5         /* muscle.py:39-53 (flag NEOHOOKEAN selects the passive model) */
+} mpm_material_type;
+
+#define MPM_MATF_NEOHOOKEAN 0x1
+#define MPM_MATF_VON_MISES 0x2
+
+/* One registered material.  The derived constants follow base.py:77-88 (mu, lam),
+ * sand.py:40-45 (alpha, default Jp 0) and muscle.py:46-50 (stiffness = E); the caller
+ * (the Python facade) computes them exactly as the reference does. */
+typedef struct mpm_material {
+  int32_t type;          /* mpm_material_type */
+  int32_t flags;         /* MPM_MATF_* */
+  int32_t scene;         /* scene this material belongs to */
+  int32_t reserved;
+  double mu, lam;        /* Lame parameters (Liquid: mu = 0 unless viscous) */
+  double rho;            /* density */
+  double default_Jp;     /* 1, or 0 for Sand */
+  double friction_alpha; /* Sand: sqrt(2/3)*2 sin(phi)/(3 - sin(phi)) */
+  double yield_lower, yield_higher;  /* Snow / ElastoPlastic clamp */
+  double von_mises_yield_stress;     /* ElastoPlastic von Mises */
+  double stiffness;      /* Muscle actuation stiffness (= E) */
+} mpm_material;
+
+/* ---------------------------------------------------------------- scenes */
+/* One independent MPM scene (a reference "env").  Derived values follow
+ * MPMSolver.__init__ (mpm_solver.py:32-80): dx = 1/grid_density,
+ * grid_res = round(density*ub) - round(density*lb) + 1, grid_offset = round(density*lb),
+ * particle_volume = particle_size^3 * 1e3, boundary = [lb + 3dx, ub - 3dx]. */
+typedef struct mpm_scene_config {
+  double substep_dt;      /* SimOptions.dt / substeps (base_solver.py:25) */
+  double gravity[3];
+  double lower_bound[3];
+  double upper_bound[3];
+  double grid_density;
+  double particle_size;
+  double mass_eps;        /* grid-op mass threshold; the reference uses gs.EPS (fp32: 2^-23) */
+  double restitution;     /* CubeBoundary restitution, 0 in the reference */
+  int64_t n_particles;    /* particle capacity of this scene */
+} mpm_scene_config;
+
+typedef struct mpm_ctx mpm_ctx;
+
+/* Create a context owning all device state for n_scenes scenes and n_materials
+ * materials on CUDA device `device`.
+ * Replaces MPMSolver.__init__/build + init_particle_fields/init_grid_fields
+ * (mpm_solver.py:32-80, 82-148, 201-241) and LegacyCoupler.build for MPM. */
+int mpm_ctx_create(const mpm_scene_config* scenes, int64_t n_scenes,
+                   const mpm_material* materials, int32_t n_materials,
+                   int32_t device, mpm_ctx** out);
+
+/* Free all device state.  Replaces nothing (Quadrants frees fields at exit). */
+int mpm_ctx_destroy(mpm_ctx* ctx);
+
+/* Text of the last error on this context (or of the last failed create if ctx is NULL). */
+const char* mpm_last_error(const mpm_ctx* ctx);
+
+/* Add `n` particles of material `material` (index among the scene's own materials, in
+ * registration order, like Material.idx) to scenes [scene_begin, scene_end),
+ * at per-scene particle indices [particle_start, particle_start + n), with the same
+ * positions `pos` [n, 3] in every scene.  Sets v = 0, F = I, C = 0, Jp = default_Jp,
+ * actu = 0, free = true, muscle direction (0,0,1).
+ * Replaces MPMSolver._kernel_add_particles (mpm_solver.py:806-838). */
+int mpm_add_particles(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end,
+                      int64_t particle_start, int64_t n, int32_t material, int32_t active,
+                      const float* pos, void* stream);
+
+/* Full particle state of scenes [scene_begin, scene_end) in reference layout.
+ * Replaces MPMSolver._kernel_get_state / _kernel_set_state (mpm_solver.py:759-778,
+ * 729-749) and MPMEntity.get_frame (mpm_entity.py:305-352).  Any pointer may be NULL to
+ * skip that field.  set_state marks the particle ordering dirty (re-sorted before the
+ * next substep). */
+int mpm_get_state(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end,
+                  float* pos, float* vel, float* C, float* F, float* Jp, uint8_t* active,
+                  void* stream);
+int mpm_set_state(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end,
+                  const float* pos, const float* vel, const float* C, const float* F,
+                  const float* Jp, const uint8_t* active, void* stream);
+
+/* Per-particle field access over a contiguous per-scene particle range
+ * [particle_start, particle_start + n) of scenes [scene_begin, scene_end); data is
+ * [B, n, width].  Replaces _kernel_{set,get}_particles_{pos,vel,active,actu} and
+ * _kernel_set_particles_{free,muscle_direction,muscle_group} (mpm_solver.py:840-1026).
+ * MPM_FIELD_POS_RESET sets positions and resets v, F, C, Jp like
+ * _kernel_set_particles_pos (mpm_solver.py:840-859). */
+typedef enum mpm_field {
+  MPM_FIELD_POS = 0,        /* float[3] */
+  MPM_FIELD_VEL = 1,        /* float[3] */
+  MPM_FIELD_C = 2,          /* float[9] */
+  MPM_FIELD_F = 3,          /* float[9] */
+  MPM_FIELD_JP = 4,         /* float[1] */
+  MPM_FIELD_ACTIVE = 5,     /* float[1] read/written as 0/1 */
+  MPM_FIELD_ACTU = 6,       /* float[1] */
+  MPM_FIELD_FREE = 7,       /* float[1] 0/1 */
+  MPM_FIELD_MUSCLE_DIR = 8, /* float[3] */
+  MPM_FIELD_POS_RESET = 9   /* float[3], write only */
+} mpm_field;
+int mpm_set_particles(mpm_ctx* ctx, int32_t field, int64_t scene_begin, int64_t scene_end,
+                      int64_t particle_start, int64_t n, const float* data, void* stream);
+int mpm_get_particles(mpm_ctx* ctx, int32_t field, int64_t scene_begin, int64_t scene_end,
+                      int64_t particle_start, int64_t n, float* data, void* stream);
+
+/* Per-scene gravity [scene_end - scene_begin, 3] (host pointer).
+ * Replaces Solver.set_gravity (base_solver.py:43-53). */
+int mpm_set_gravity(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end,
+                    const double* gravity_host);
+
+/* Run n full substeps on every scene.  Replaces, per substep, Simulator.substep
+ * (simulator.py:320-324) = MPMSolver.substep_pre_coupling (mpm_solver.py:503-515:
+ * reset_grid_and_grad, compute_F_tmp, svd, p2g), LegacyCoupler.mpm_grid_op
+ * (legacy_coupler.py:356-501, gravity + boundary, no coupling partners) and
+ * MPMSolver.substep_post_coupling (mpm_solver.py:530-546: g2p, NaN check), plus
+ * copy_frame (mpm_solver.py:556-565), which the double-buffered layout makes unnecessary.
+ * The NaN check is recorded in the device status word instead of syncing every substep.
+ * Captured as a CUDA graph after the first call with the same particle count. */
+int mpm_substeps(mpm_ctx* ctx, int32_t n_substeps, void* stream);
+
+/* The three phases of one substep, for callers that interleave coupling work the way
+ * Simulator.substep does (simulator.py:320-324).  pre = particle sort (if needed) +
+ * F update + SVD + material + P2G; grid_op = legacy_coupler.py:356-501 without partners;
+ * post = G2P + boundary + NaN flag + re-keying for the next sort. */
+int mpm_substep_pre(mpm_ctx* ctx, void* stream);
+int mpm_substep_grid_op(mpm_ctx* ctx, void* stream);
+int mpm_substep_post(mpm_ctx* ctx, void* stream);
+
+/* Copy the dense grid of one scene into out [gx, gy, gz, 4] (x-major, float32):
+ * after mpm_substep_pre it holds (momentum xyz, mass); after mpm_substep_grid_op it
+ * holds (vel_out xyz, mass).  Replaces reading MPMSolver.grid (mpm_solver.py:137-148). */
+int mpm_get_grid(mpm_ctx* ctx, int64_t scene, float* out, void* stream);
+
+/* Number of grid nodes with mass > mass_eps in the current grid buffer of all scenes
+ * (device reduction; synchronises `stream`). */
+int mpm_count_touched_nodes(mpm_ctx* ctx, int64_t* out_host, void* stream);
+
+/* Read and optionally clear the device status word (MPM_STATUS_* bits) and the count of
+ * particles whose SVD was redone in FP64.  Synchronises `stream`.
+ * Replaces MPMSolver._is_state_valid (mpm_solver.py:483-489). */
+int mpm_status_word(mpm_ctx* ctx, uint32_t* status_host, int64_t* fp64_svd_host,
+                    int32_t clear, void* stream);
+
+/* Tuning knobs (the autotuner sets these): P2G threads per CTA (64..512, multiple of 32)
+ * and particles per thread (1..16); the P2G work chunk is their product. */
+int mpm_set_tuning(mpm_ctx* ctx, int32_t p2g_threads, int32_t particles_per_thread,
+                   int32_t use_graph);
+
+/* Per-kernel timing: when enabled, mpm_substeps runs without a graph and brackets every
+ * kernel with CUDA events on its launch stream; mpm_kernel_times synchronises and returns
+ * accumulated milliseconds and launch counts for [P2G, grid op, G2P, scan, perm]. */
+int mpm_set_profiling(mpm_ctx* ctx, int32_t enable);
+int mpm_kernel_times(mpm_ctx* ctx, double* ms_host /*[5]*/, int64_t* counts_host /*[5]*/, int32_t reset);
+
+/* ABI version of this header (1). */
+int mpm_version(void);
+
+/* Sizes: particles in use, number of grid blocks (4^3 nodes each), grid res of a scene. */
+int mpm_get_info(const mpm_ctx* ctx, int64_t* n_particles, int64_t* n_blocks,
+                 int64_t* n_scenes);
+int mpm_scene_grid_res(const mpm_ctx* ctx, int64_t scene, int32_t* res3_host);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBMPM_H */

@@ -1,0 +1,601 @@
+// mpm_oracle.cpp - CPU restatement of the Genesis MLS-MPM substep.  TEST INFRASTRUCTURE:
+// only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it, as the
+// checker and as the timed CPU baseline.  It is never part of the product path.
+//
+// Parity status: the reference (genesis-world 0.4.5) runs on the Quadrants JIT, which is
+// not installed here, so this restatement cannot be compared with the reference executing.
+// Parity is pinned only through golden vectors produced by the reference's own material
+// functions (tests/golden/), the reference's own closed-form constants, and physics
+// known-answer tests; see the tests.  The SVD is unpinned (qd.svd is not vendored).
+//
+// What it follows (paths relative to the Genesis project root):
+//   MPMSolver.__init__ constants      genesis/engine/solvers/mpm_solver.py:32-80
+//   compute_F_tmp / svd               mpm_solver.py:293-307
+//   p2g (material, stress, scatter)   mpm_solver.py:322-421
+//   grid op (no coupling partners)    genesis/engine/couplers/legacy_coupler.py:356-501
+//   g2p + particle boundary           mpm_solver.py:423-481, engine/boundaries/boundaries.py:22-32
+//   materials                         genesis/engine/materials/MPM/{base,elastic,liquid,sand,snow,
+//                                     elasto_plastic,muscle}.py
+// The accumulation order is particle order (deterministic) when threads == 1.  With
+// threads > 1 the scatter uses atomic adds (like the reference's CPU backend) and is
+// used only for timing.
+//
+// Non-free particles: the reference stores vel_in = 0 on their 27 nodes inside the
+// scatter loop, racing with other particles' adds (mpm_solver.py:420-421).  This
+// restatement resolves the race deterministically: such nodes end the scatter with zero
+// momentum (the outcome when the store lands last), which is also what the CUDA path does.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+extern "C" {
+typedef struct oracle_scene {
+  double dt;
+  double gravity[3];
+  double lower_bound[3];
+  double upper_bound[3];
+  double grid_density;
+  double particle_size;
+  double eps;          // gs.EPS (grid-op mass threshold and Matrix.norm eps)
+  double restitution;  // CubeBoundary restitution (0)
+} oracle_scene;
+
+typedef struct oracle_material {
+  int32_t type;   // 0 elastic, 1 liquid, 2 sand, 3 snow, 4 elastoplastic, 5 muscle
+  int32_t flags;  // 1 neohookean, 2 von Mises
+  double mu, lam, rho, default_Jp, alpha, yield_lower, yield_higher, vm_yield, stiffness;
+} oracle_material;
+}
+
+namespace {
+
+template <typename T>
+struct M3 {
+  T a[9];
+  T& operator()(int i, int j) { return a[i * 3 + j]; }
+  T operator()(int i, int j) const { return a[i * 3 + j]; }
+  static M3 zero() {
+    M3 m;
+    for (int k = 0; k < 9; ++k) m.a[k] = 0;
+    return m;
+  }
+  static M3 eye() {
+    M3 m = zero();
+    m.a[0] = m.a[4] = m.a[8] = 1;
+    return m;
+  }
+};
+
+template <typename T>
+M3<T> mul(const M3<T>& A, const M3<T>& B) {
+  M3<T> C = M3<T>::zero();
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      for (int k = 0; k < 3; ++k) C(i, j) += A(i, k) * B(k, j);
+  return C;
+}
+template <typename T>
+M3<T> transpose(const M3<T>& A) {
+  M3<T> C;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) C(i, j) = A(j, i);
+  return C;
+}
+template <typename T>
+M3<T> add(const M3<T>& A, const M3<T>& B, T sb = 1) {
+  M3<T> C;
+  for (int k = 0; k < 9; ++k) C.a[k] = A.a[k] + sb * B.a[k];
+  return C;
+}
+template <typename T>
+M3<T> scale(const M3<T>& A, T s) {
+  M3<T> C;
+  for (int k = 0; k < 9; ++k) C.a[k] = s * A.a[k];
+  return C;
+}
+template <typename T>
+M3<T> diag(T a, T b, T c) {
+  M3<T> m = M3<T>::zero();
+  m(0, 0) = a;
+  m(1, 1) = b;
+  m(2, 2) = c;
+  return m;
+}
+template <typename T>
+T det(const M3<T>& A) {
+  return A(0, 0) * (A(1, 1) * A(2, 2) - A(1, 2) * A(2, 1)) - A(0, 1) * (A(1, 0) * A(2, 2) - A(1, 2) * A(2, 0)) +
+         A(0, 2) * (A(1, 0) * A(2, 1) - A(1, 1) * A(2, 0));
+}
+
+// One-sided (Hestenes) Jacobi SVD iterated to convergence, then brought to the
+// rotation-variant convention: det U = det V = +1, sig0 >= sig1 >= |sig2|, sign in sig2.
+template <typename T>
+void svd_hestenes(const M3<T>& A, M3<T>& U, M3<T>& S, M3<T>& V) {
+  M3<T> W = A;
+  V = M3<T>::eye();
+  const T tol = std::numeric_limits<T>::epsilon();
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    bool rotated = false;
+    const int pq[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+    for (auto& e : pq) {
+      const int p = e[0], q = e[1];
+      T al = 0, be = 0, ga = 0;
+      for (int i = 0; i < 3; ++i) {
+        al += W(i, p) * W(i, p);
+        be += W(i, q) * W(i, q);
+        ga += W(i, p) * W(i, q);
+      }
+      if (std::fabs(ga) <= tol * std::sqrt(al * be) || ga == 0) continue;
+      rotated = true;
+      const T zeta = (be - al) / (2 * ga);
+      const T t = (zeta >= 0 ? 1 : -1) / (std::fabs(zeta) + std::sqrt(1 + zeta * zeta));
+      const T c = 1 / std::sqrt(1 + t * t), s = c * t;
+      for (int i = 0; i < 3; ++i) {
+        const T wp = W(i, p), wq = W(i, q);
+        W(i, p) = c * wp - s * wq;
+        W(i, q) = s * wp + c * wq;
+        const T vp = V(i, p), vq = V(i, q);
+        V(i, p) = c * vp - s * vq;
+        V(i, q) = s * vp + c * vq;
+      }
+    }
+    if (!rotated) break;
+  }
+  T sig[3];
+  for (int k = 0; k < 3; ++k) sig[k] = std::sqrt(W(0, k) * W(0, k) + W(1, k) * W(1, k) + W(2, k) * W(2, k));
+  // sort descending (same column swaps on W and V)
+  for (int a = 0; a < 2; ++a)
+    for (int b = a + 1; b < 3; ++b)
+      if (sig[b] > sig[a]) {
+        std::swap(sig[a], sig[b]);
+        for (int i = 0; i < 3; ++i) {
+          std::swap(W(i, a), W(i, b));
+          std::swap(V(i, a), V(i, b));
+        }
+      }
+  // U = W diag(1/sig), completing null directions orthonormally
+  U = M3<T>::zero();
+  const T small = sig[0] * std::numeric_limits<T>::epsilon() * 8;
+  int rank = 0;
+  for (int k = 0; k < 3; ++k)
+    if (sig[k] > small && sig[k] > 0) {
+      for (int i = 0; i < 3; ++i) U(i, k) = W(i, k) / sig[k];
+      rank = k + 1;
+    }
+  for (int k = rank; k < 3; ++k) {
+    // pick the basis vector least aligned with existing columns, Gram-Schmidt it
+    T best[3] = {0, 0, 0};
+    T bestn = -1;
+    for (int e = 0; e < 3; ++e) {
+      T v[3] = {0, 0, 0};
+      v[e] = 1;
+      for (int j = 0; j < k; ++j) {
+        const T d = U(0, j) * v[0] + U(1, j) * v[1] + U(2, j) * v[2];
+        for (int i = 0; i < 3; ++i) v[i] -= d * U(i, j);
+      }
+      const T n = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+      if (n > bestn) {
+        bestn = n;
+        for (int i = 0; i < 3; ++i) best[i] = v[i] / n;
+      }
+    }
+    for (int i = 0; i < 3; ++i) U(i, k) = best[i];
+  }
+  if (det(V) < 0)
+    for (int i = 0; i < 3; ++i) {
+      V(i, 2) = -V(i, 2);
+      U(i, 2) = -U(i, 2);
+    }
+  if (det(U) < 0) {
+    for (int i = 0; i < 3; ++i) U(i, 2) = -U(i, 2);
+    sig[2] = -sig[2];
+  }
+  S = diag(sig[0], sig[1], sig[2]);
+}
+
+// Matrix.norm(eps) = sqrt(|x|^2 + eps) (upstream Taichi definition; unverified here)
+template <typename T>
+T norm_eps(const T* v, T eps) {
+  return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2] + eps);
+}
+
+template <typename T>
+struct Mat {
+  int type, flags;
+  T mu, lam, rho, default_Jp, alpha, yl, yh, vmy, stiffness;
+};
+
+// base.py:94-99 / elastic.py:48-53
+template <typename T>
+M3<T> stress_default(const Mat<T>& m, const M3<T>& U, const M3<T>& V, const M3<T>& F_new, T J) {
+  M3<T> r = mul(U, transpose(V));
+  M3<T> s = scale(mul(add(F_new, r, T(-1)), transpose(F_new)), 2 * m.mu);
+  return add(s, scale(M3<T>::eye(), m.lam * J * (J - 1)));
+}
+
+// Material update: returns F_new, S_new, Jp_new (update_F_S_Jp of each material).
+template <typename T>
+void update_F_S_Jp(const Mat<T>& m, T J, const M3<T>& F_tmp, const M3<T>& U, const M3<T>& S, const M3<T>& V, T Jp,
+                   T eps, M3<T>& F_new, M3<T>& S_new, T& Jp_new) {
+  switch (m.type) {
+    case 1:  // liquid.py:36-40
+      F_new = scale(M3<T>::eye(), std::pow(J, T(1) / T(3)));
+      S_new = S;
+      Jp_new = Jp;
+      return;
+    case 2: {  // sand.py:47-78
+      M3<T> So = M3<T>::zero();
+      T e[3];
+      for (int i = 0; i < 3; ++i) {
+        e[i] = std::log(std::max(std::fabs(S(i, i)), T(1e-4)));
+        So(i, i) = 1;
+      }
+      const T tr = e[0] + e[1] + e[2] + Jp;
+      T eh[3];
+      for (int i = 0; i < 3; ++i) eh[i] = e[i] - tr / 3;
+      const T ehn = norm_eps(eh, eps);
+      if (tr >= 0) {
+        Jp_new = tr;
+      } else {
+        Jp_new = 0;
+        const T dg = ehn + (3 * m.lam + 2 * m.mu) / (2 * m.mu) * tr * m.alpha;
+        for (int i = 0; i < 3; ++i) So(i, i) = std::exp(e[i] - std::max(T(0), dg) / ehn * eh[i]);
+      }
+      S_new = So;
+      F_new = mul(mul(U, S_new), transpose(V));
+      return;
+    }
+    case 3: {  // snow.py:56-64
+      S_new = M3<T>::zero();
+      Jp_new = Jp;
+      for (int d = 0; d < 3; ++d) {
+        S_new(d, d) = std::min(std::max(S(d, d), 1 - m.yl), 1 + m.yh);
+        Jp_new *= S(d, d) / S_new(d, d);
+      }
+      F_new = mul(mul(U, S_new), transpose(V));
+      return;
+    }
+    case 4: {  // elasto_plastic.py:44-71
+      if (m.flags & 2) {
+        T s[3], e[3];
+        for (int d = 0; d < 3; ++d) {
+          s[d] = std::max(S(d, d), T(0.05));
+          e[d] = std::log(s[d]);
+        }
+        const T mean = (e[0] + e[1] + e[2]) / 3;
+        T eh[3];
+        for (int d = 0; d < 3; ++d) eh[d] = e[d] - mean;
+        const T ehn = norm_eps(eh, eps);
+        const T dg = ehn - m.vmy / (2 * m.mu);
+        if (dg > 0) {
+          for (int d = 0; d < 3; ++d) e[d] -= (dg / ehn) * eh[d];
+          S_new = diag(std::exp(e[0]), std::exp(e[1]), std::exp(e[2]));
+          F_new = mul(mul(U, S_new), transpose(V));
+        } else {
+          S_new = diag(s[0], s[1], s[2]);
+          F_new = F_tmp;
+        }
+      } else {
+        S_new = M3<T>::zero();
+        for (int d = 0; d < 3; ++d) S_new(d, d) = std::min(std::max(S(d, d), 1 - m.yl), 1 + m.yh);
+        F_new = mul(mul(U, S_new), transpose(V));
+      }
+      Jp_new = Jp;
+      return;
+    }
+    default:  // elastic.py:41-46 (elastic and muscle)
+      F_new = F_tmp;
+      S_new = S;
+      Jp_new = Jp;
+      return;
+  }
+}
+
+template <typename T>
+M3<T> update_stress(const Mat<T>& m, const M3<T>& U, const M3<T>& S, const M3<T>& V, const M3<T>& F_tmp,
+                    const M3<T>& F_new, T J, T Jp, T actu, const T* mdir) {
+  switch (m.type) {
+    case 1:  // liquid.py:43-49 (uses F_tmp)
+      return stress_default(m, U, V, F_tmp, J);
+    case 2: {  // sand.py:74-84 (S = S_new)
+      T lsum = 0;
+      M3<T> center = M3<T>::zero();
+      for (int i = 0; i < 3; ++i) {
+        lsum += std::log(S(i, i));
+        center(i, i) = 2 * m.mu * std::log(S(i, i)) * (1 / S(i, i));
+      }
+      for (int i = 0; i < 3; ++i) center(i, i) += m.lam * lsum * (1 / S(i, i));
+      return mul(mul(mul(U, center), transpose(V)), transpose(F_new));
+    }
+    case 3: {  // snow.py:66-74 (Jp before the update)
+      const T h = std::exp(10 * (1 - Jp));
+      Mat<T> mh = m;
+      mh.mu = m.mu * h;
+      mh.lam = m.lam * h;
+      return stress_default(mh, U, V, F_new, J);
+    }
+    case 4:  // base.py default stress
+      return stress_default(m, U, V, F_new, J);
+    default: {  // elastic.py:48-60, muscle.py:46-53
+      M3<T> st;
+      if (m.flags & 1)
+        st = add(scale(mul(F_tmp, transpose(F_tmp)), m.mu), scale(M3<T>::eye(), m.lam * std::log(J) - m.mu));
+      else
+        st = stress_default(m, U, V, F_new, J);
+      if (m.type == 5) {
+        M3<T> AAt;
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) AAt(i, j) = mdir[i] * mdir[j];
+        st = add(st, scale(mul(mul(F_tmp, AAt), transpose(F_tmp)), m.stiffness * actu));
+      }
+      return st;
+    }
+  }
+}
+
+template <typename T>
+struct Scene {
+  T dt, dx, inv_dx, p_vol, eps, restitution;
+  T g[3], lo[3], hi[3];
+  int64_t res[3], off[3];
+};
+
+template <typename T>
+Scene<T> make_scene(const oracle_scene& c) {
+  Scene<T> S;
+  const double dx = 1.0 / c.grid_density;
+  S.dt = (T)c.dt;
+  S.dx = (T)dx;
+  S.inv_dx = (T)c.grid_density;
+  S.p_vol = (T)(c.particle_size * c.particle_size * c.particle_size * 1e3);
+  S.eps = (T)c.eps;
+  S.restitution = (T)c.restitution;
+  for (int d = 0; d < 3; ++d) {
+    S.g[d] = (T)c.gravity[d];
+    S.lo[d] = (T)(c.lower_bound[d] + 3 * dx);
+    S.hi[d] = (T)(c.upper_bound[d] - 3 * dx);
+    const int64_t lo = (int64_t)std::nearbyint(c.grid_density * c.lower_bound[d]);
+    const int64_t hi = (int64_t)std::nearbyint(c.grid_density * c.upper_bound[d]);
+    S.res[d] = hi - lo + 1;
+    S.off[d] = lo;
+  }
+  return S;
+}
+
+template <typename T>
+inline void atomic_add(T& dst, T v, bool atomic) {
+  if (atomic) {
+#pragma omp atomic
+    dst += v;
+  } else {
+    dst += v;
+  }
+}
+
+template <typename T>
+int run(const oracle_scene* sc, const oracle_material* mats, int n_mats, int64_t n, T* pos, T* vel, T* C, T* F,
+        T* Jp, const int32_t* mat, const uint8_t* active, const uint8_t* free_, const T* actu, const T* mdir,
+        int n_substeps, T* grid_out, int64_t* n_touched, int threads) {
+  const Scene<T> S = make_scene<T>(*sc);
+  std::vector<Mat<T>> M(n_mats);
+  for (int i = 0; i < n_mats; ++i) {
+    const oracle_material& m = mats[i];
+    M[i] = {m.type, m.flags, (T)m.mu, (T)m.lam, (T)m.rho, (T)m.default_Jp, (T)m.alpha, (T)m.yield_lower,
+            (T)m.yield_higher, (T)m.vm_yield, (T)m.stiffness};
+  }
+  const int64_t rx = S.res[0], ry = S.res[1], rz = S.res[2];
+  const int64_t nn = rx * ry * rz;
+  std::vector<T> gm(nn), gp(nn * 3), gv(nn * 3);
+  std::vector<uint8_t> pin;
+  bool any_pinned = false;
+  for (int64_t i = 0; i < n && free_; ++i) any_pinned = any_pinned || (active[i] && !free_[i]);
+  if (any_pinned) pin.assign(nn, 0);
+#ifdef _OPENMP
+  if (threads > 0) omp_set_num_threads(threads);
+#endif
+  const bool par = threads > 1;
+  const T stress_scale = (T)(-(double)S.dt * (double)S.p_vol * 4.0 * (double)S.inv_dx * (double)S.inv_dx);
+  for (int step = 0; step < n_substeps; ++step) {
+    // reset_grid_and_grad (mpm_solver.py:577-587)
+    std::fill(gm.begin(), gm.end(), T(0));
+    std::fill(gp.begin(), gp.end(), T(0));
+    std::fill(gv.begin(), gv.end(), T(0));
+    int bad = 0;
+    // p2g
+#pragma omp parallel for schedule(static) if (par) reduction(| : bad)
+    for (int64_t i = 0; i < n; ++i) {
+      if (!active[i]) continue;
+      const Mat<T>& m = M[mat[i]];
+      const T mass = S.p_vol * m.rho;
+      M3<T> Cm, Fm;
+      std::memcpy(Cm.a, C + i * 9, sizeof(T) * 9);
+      std::memcpy(Fm.a, F + i * 9, sizeof(T) * 9);
+      const M3<T> F_tmp = mul(add(M3<T>::eye(), Cm, S.dt), Fm);
+      M3<T> U, Sg, V;
+      svd_hestenes(F_tmp, U, Sg, V);
+      const T J = det(Sg);
+      M3<T> F_new, S_new;
+      T Jp_new;
+      update_F_S_Jp(m, J, F_tmp, U, Sg, V, Jp[i], S.eps, F_new, S_new, Jp_new);
+      const T md[3] = {mdir ? mdir[i * 3] : T(0), mdir ? mdir[i * 3 + 1] : T(0), mdir ? mdir[i * 3 + 2] : T(1)};
+      M3<T> stress = update_stress(m, U, S_new, V, F_tmp, F_new, J, Jp[i], actu ? actu[i] : T(0), md);
+      std::memcpy(F + i * 9, F_new.a, sizeof(T) * 9);
+      Jp[i] = Jp_new;
+      stress = scale(stress, stress_scale);
+      const M3<T> affine = add(stress, Cm, mass);
+      int64_t base[3];
+      T fx[3], w[3][3];
+      for (int d = 0; d < 3; ++d) {
+        const T xs = pos[i * 3 + d] * S.inv_dx;
+        base[d] = (int64_t)std::floor(xs - T(0.5));
+        fx[d] = xs - (T)base[d];
+        w[0][d] = T(0.5) * (T(1.5) - fx[d]) * (T(1.5) - fx[d]);
+        w[1][d] = T(0.75) - (fx[d] - 1) * (fx[d] - 1);
+        w[2][d] = T(0.5) * (fx[d] - T(0.5)) * (fx[d] - T(0.5));
+        const int64_t lo = base[d] - S.off[d];
+        if (lo < 0 || lo + 2 >= S.res[d]) bad = 1;
+      }
+      if (bad) continue;
+      const bool is_free = !free_ || free_[i];
+      for (int ox = 0; ox < 3; ++ox)
+        for (int oy = 0; oy < 3; ++oy)
+          for (int oz = 0; oz < 3; ++oz) {
+            const int o[3] = {ox, oy, oz};
+            T dpos[3];
+            T weight = 1;
+            for (int d = 0; d < 3; ++d) {
+              dpos[d] = ((T)o[d] - fx[d]) * S.dx;
+              weight *= w[o[d]][d];
+            }
+            const int64_t I = ((base[0] - S.off[0] + ox) * ry + (base[1] - S.off[1] + oy)) * rz + (base[2] - S.off[2] + oz);
+            for (int r = 0; r < 3; ++r) {
+              const T a = affine(r, 0) * dpos[0] + affine(r, 1) * dpos[1] + affine(r, 2) * dpos[2];
+              atomic_add(gp[I * 3 + r], weight * (mass * vel[i * 3 + r] + a), par);
+            }
+            atomic_add(gm[I], weight * mass, par);
+            if (!is_free) pin[I] = 1;
+          }
+    }
+    if (bad) return 5;
+    if (any_pinned)
+      for (int64_t I = 0; I < nn; ++I)
+        if (pin[I]) {
+          gp[I * 3] = gp[I * 3 + 1] = gp[I * 3 + 2] = 0;
+          pin[I] = 0;
+        }
+    if (grid_out && step == n_substeps - 1)
+      for (int64_t I = 0; I < nn; ++I) {
+        grid_out[I * 4 + 0] = gp[I * 3 + 0];
+        grid_out[I * 4 + 1] = gp[I * 3 + 1];
+        grid_out[I * 4 + 2] = gp[I * 3 + 2];
+        grid_out[I * 4 + 3] = gm[I];
+      }
+    // grid op (legacy_coupler.py:367-373, 501)
+    int64_t touched = 0;
+#pragma omp parallel for schedule(static) if (par) reduction(+ : touched)
+    for (int64_t I = 0; I < nn; ++I) {
+      if (!(gm[I] > S.eps)) continue;
+      ++touched;
+      const int64_t idx[3] = {I / (ry * rz), (I / rz) % ry, I % rz};
+      T v[3];
+      for (int d = 0; d < 3; ++d) v[d] = (1 / gm[I]) * gp[I * 3 + d] + S.dt * S.g[d];
+      for (int d = 0; d < 3; ++d) {
+        const T p = (T)(idx[d] + S.off[d]) * S.dx;
+        if (p >= S.hi[d] && v[d] >= 0) v[d] *= -S.restitution;
+        else if (p <= S.lo[d] && v[d] <= 0) v[d] *= -S.restitution;
+        gv[I * 3 + d] = v[d];
+      }
+    }
+    if (n_touched && step == n_substeps - 1) *n_touched = touched;
+    // g2p (mpm_solver.py:431-481)
+    int nan = 0;
+#pragma omp parallel for schedule(static) if (par) reduction(| : nan)
+    for (int64_t i = 0; i < n; ++i) {
+      if (!active[i]) continue;
+      int64_t base[3];
+      T fx[3], w[3][3];
+      for (int d = 0; d < 3; ++d) {
+        const T xs = pos[i * 3 + d] * S.inv_dx;
+        base[d] = (int64_t)std::floor(xs - T(0.5));
+        fx[d] = xs - (T)base[d];
+        w[0][d] = T(0.5) * (T(1.5) - fx[d]) * (T(1.5) - fx[d]);
+        w[1][d] = T(0.75) - (fx[d] - 1) * (fx[d] - 1);
+        w[2][d] = T(0.5) * (fx[d] - T(0.5)) * (fx[d] - T(0.5));
+      }
+      T nv[3] = {0, 0, 0};
+      M3<T> nC = M3<T>::zero();
+      for (int ox = 0; ox < 3; ++ox)
+        for (int oy = 0; oy < 3; ++oy)
+          for (int oz = 0; oz < 3; ++oz) {
+            const int o[3] = {ox, oy, oz};
+            T dpos[3];
+            T weight = 1;
+            for (int d = 0; d < 3; ++d) {
+              dpos[d] = (T)o[d] - fx[d];
+              weight *= w[o[d]][d];
+            }
+            const int64_t I = ((base[0] - S.off[0] + ox) * ry + (base[1] - S.off[1] + oy)) * rz + (base[2] - S.off[2] + oz);
+            for (int r = 0; r < 3; ++r) {
+              const T g = gv[I * 3 + r];
+              nv[r] += weight * g;
+              for (int c = 0; c < 3; ++c) nC(r, c) += 4 * S.inv_dx * weight * g * dpos[c];
+            }
+          }
+      T np[3];
+      for (int d = 0; d < 3; ++d) np[d] = pos[i * 3 + d] + S.dt * nv[d];
+      for (int d = 0; d < 3; ++d) {
+        if (np[d] >= S.hi[d] && nv[d] >= 0) nv[d] *= -S.restitution;
+        else if (np[d] <= S.lo[d] && nv[d] <= 0) nv[d] *= -S.restitution;
+        if (std::isnan(np[d])) nan = 1;
+        np[d] = std::max(std::min(np[d], S.hi[d]), S.lo[d]);
+      }
+      for (int d = 0; d < 3; ++d) {
+        pos[i * 3 + d] = np[d];
+        vel[i * 3 + d] = nv[d];
+      }
+      std::memcpy(C + i * 9, nC.a, sizeof(T) * 9);
+    }
+    if (nan) return 4;
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int oracle_substeps_f64(const oracle_scene* sc, const oracle_material* mats, int n_mats, int64_t n, double* pos,
+                        double* vel, double* C, double* F, double* Jp, const int32_t* mat, const uint8_t* active,
+                        const uint8_t* free_, const double* actu, const double* mdir, int n_substeps,
+                        double* grid_out, int64_t* n_touched, int threads) {
+  return run<double>(sc, mats, n_mats, n, pos, vel, C, F, Jp, mat, active, free_, actu, mdir, n_substeps, grid_out,
+                     n_touched, threads);
+}
+
+int oracle_substeps_f32(const oracle_scene* sc, const oracle_material* mats, int n_mats, int64_t n, float* pos,
+                        float* vel, float* C, float* F, float* Jp, const int32_t* mat, const uint8_t* active,
+                        const uint8_t* free_, const float* actu, const float* mdir, int n_substeps, float* grid_out,
+                        int64_t* n_touched, int threads) {
+  return run<float>(sc, mats, n_mats, n, pos, vel, C, F, Jp, mat, active, free_, actu, mdir, n_substeps, grid_out,
+                    n_touched, threads);
+}
+
+void oracle_svd_f64(const double* A, double* U, double* sig, double* V) {
+  M3<double> a, u, s, v;
+  std::memcpy(a.a, A, sizeof(a.a));
+  svd_hestenes(a, u, s, v);
+  std::memcpy(U, u.a, sizeof(u.a));
+  std::memcpy(V, v.a, sizeof(v.a));
+  for (int k = 0; k < 3; ++k) sig[k] = s(k, k);
+}
+
+// Material update + stress of one particle (for golden-vector checks of the material code).
+void oracle_material_f64(const oracle_material* mm, const double* F_tmp, double Jp, double actu, const double* mdir,
+                         double eps, double* F_new, double* Jp_new, double* stress) {
+  Mat<double> m = {mm->type, mm->flags, mm->mu, mm->lam, mm->rho, mm->default_Jp, mm->alpha,
+                   mm->yield_lower, mm->yield_higher, mm->vm_yield, mm->stiffness};
+  M3<double> Ft, U, S, V, Fn, Sn;
+  std::memcpy(Ft.a, F_tmp, sizeof(Ft.a));
+  svd_hestenes(Ft, U, S, V);
+  const double J = det(S);
+  double jn;
+  update_F_S_Jp(m, J, Ft, U, S, V, Jp, eps, Fn, Sn, jn);
+  M3<double> st = update_stress(m, U, Sn, V, Ft, Fn, J, Jp, actu, mdir);
+  std::memcpy(F_new, Fn.a, sizeof(Fn.a));
+  *Jp_new = jn;
+  std::memcpy(stress, st.a, sizeof(st.a));
+}
+
+int oracle_grid_res(const oracle_scene* sc, int64_t* res3) {
+  const Scene<double> S = make_scene<double>(*sc);
+  for (int d = 0; d < 3; ++d) res3[d] = S.res[d];
+  return 0;
+}
+
+}  // extern "C"
