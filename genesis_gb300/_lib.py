@@ -62,6 +62,17 @@ class MpmMaterial(ctypes.Structure):
     ]
 
 
+class MpmPoolConfig(ctypes.Structure):
+    _fields_ = [
+        ("max_scenes", c_int64),
+        ("particle_capacity", c_int64),
+        ("max_grid_res", c_int32),
+        ("max_materials_per_scene", c_int32),
+        ("with_muscle", c_int32),
+        ("reserved", c_int32),
+    ]
+
+
 class MpmSceneConfig(ctypes.Structure):
     _fields_ = [
         ("substep_dt", c_double),
@@ -101,6 +112,10 @@ _SIGNATURES = {
     "mpm_set_profiling": (c_int32, [_P, c_int32]),
     "mpm_kernel_times": (c_int32, [_P, ctypes.POINTER(c_double), ctypes.POINTER(c_int64), c_int32]),
     "mpm_version": (c_int32, []),
+    "mpm_ctx_create_pool": (c_int32, [ctypes.c_void_p, c_int32, ctypes.POINTER(c_void_p)]),
+    "mpm_scene_admit": (c_int32, [_P, c_int64, ctypes.c_void_p, ctypes.c_void_p, c_int32, c_int64, _P, _P, c_int32, _P]),
+    "mpm_scene_retire": (c_int32, [_P, c_int64, _P]),
+    "mpm_scene_steps_left": (c_int32, [_P, ctypes.POINTER(c_int32), _P]),
 }
 
 _lib = None

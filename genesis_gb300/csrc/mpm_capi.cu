@@ -41,7 +41,14 @@ struct mpm_ctx {
   std::vector<int32_t> first_mat_h;
   std::vector<int32_t> mat_count_h;
   int64_t cap = 0, n = 0, K = 0;
+  int64_t n_phys = 0;  // extent of the current particle buffer (> n after a retire, until the next substep)
   int nf = NF_BASE;
+  // pool mode (serving): slots configured and retired at run time
+  bool pool = false;
+  int64_t max_blocks = 0;
+  int32_t max_mats = 0;
+  std::vector<int64_t> slot_n;
+  std::vector<char> slot_live;
   float eps_norm = 1.1920929e-7f;
 
   // device memory
@@ -67,6 +74,7 @@ struct mpm_ctx {
   unsigned long long* d_fp64 = nullptr;
   unsigned long long* d_tmp64 = nullptr;
   uint32_t* d_pin = nullptr;
+  int32_t* d_steps = nullptr;
   int64_t max_items = 0;
   int n_tiles = 0;
   std::vector<void*> allocs;
@@ -79,7 +87,7 @@ struct mpm_ctx {
   // tuning / launch
   int p2g_threads = 256, ppt = 2;
   bool use_graph = true;
-  int p2g_blocks = 0, g2p_blocks = 0, grid_blocks = 0, io_blocks = 0;
+  int p2g_blocks = 0, g2p_blocks = 0, keys_blocks = 0, grid_blocks = 0, io_blocks = 0;
 
   // streams, graph, timing
   cudaStream_t cs = nullptr;
@@ -142,8 +150,9 @@ KParams make_params(mpm_ctx* ctx, int src, int dst, int g) {
   P.cap = ctx->cap;
   P.nf = ctx->nf;
   P.chunk = ctx->p2g_threads * ctx->ppt;
-  P.n = ctx->n;
+  P.n = ctx->n_phys;
   P.K = ctx->K;
+  P.n_scenes = (int32_t)ctx->n_scenes;
   P.grid = ctx->d_grid[g];
   P.grid_other = ctx->d_grid[1 - g];
   P.flags = ctx->d_flags[g];
@@ -206,7 +215,7 @@ int launch_sort(mpm_ctx* ctx, const KParams& P, cudaStream_t s) {
     k_scan_apply<<<ctx->n_tiles, SCAN_THREADS, 0, s>>>(P);
   }
   CKL();
-  if (ctx->n > 0) {
+  if (P.n > 0 || P.steps) {
     Timer t(ctx, s, KT_PERM);
     k_perm<<<ctx->io_blocks, 256, 0, s>>>(P);
   }
@@ -217,8 +226,8 @@ int launch_sort(mpm_ctx* ctx, const KParams& P, cudaStream_t s) {
 // Keys of the current state (after load / set_state), then the sort.
 int launch_rekey(mpm_ctx* ctx, cudaStream_t s) {
   KParams P = make_params(ctx, ctx->cur, ctx->cur, ctx->cur);
-  if (ctx->n > 0) {
-    k_keys<<<ctx->g2p_blocks, 256, 0, s>>>(P);
+  if (ctx->n_phys > 0) {
+    k_keys<<<ctx->keys_blocks, 256, 0, s>>>(P);
     CKL();
   }
   int r = launch_sort(ctx, P, s);
@@ -229,6 +238,8 @@ int launch_rekey(mpm_ctx* ctx, cudaStream_t s) {
 
 int launch_pre(mpm_ctx* ctx, int c, cudaStream_t s) {
   KParams P = make_params(ctx, c, 1 - c, c);
+  P.n = ctx->n;
+  P.steps = ctx->d_steps;
   Timer t(ctx, s, KT_P2G);
   k_p2g<<<ctx->p2g_blocks, ctx->p2g_threads, 0, s>>>(P);
   CKL();
@@ -245,6 +256,8 @@ int launch_grid(mpm_ctx* ctx, int c, cudaStream_t s) {
 
 int launch_post(mpm_ctx* ctx, int c, cudaStream_t s) {
   KParams P = make_params(ctx, c, 1 - c, c);
+  P.n = ctx->n;
+  P.steps = ctx->d_steps;
   {
     Timer t(ctx, s, KT_G2P);
     k_g2p<<<ctx->g2p_blocks, 256, 0, s>>>(P);
@@ -266,11 +279,15 @@ int compute_launch_shapes(mpm_ctx* ctx) {
   ctx->p2g_blocks = ctx->n_sm * (occ > 0 ? occ : 1);
   int occ2 = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, k_g2p, 256, 0));
-  int64_t want = (ctx->n + 255) / 256;
-  int64_t lim = (int64_t)ctx->n_sm * (occ2 > 0 ? occ2 : 1);
-  ctx->g2p_blocks = (int)(want < 1 ? 1 : (want < lim ? want : lim));
+  ctx->g2p_blocks = ctx->n_sm * (occ2 > 0 ? occ2 : 1);  // persistent over the work items
+  int occ3 = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ3, k_keys, 256, 0));
+  const int64_t ext = ctx->n_phys > ctx->n ? ctx->n_phys : ctx->n;
+  int64_t want = (ext + 255) / 256;
+  int64_t lim = (int64_t)ctx->n_sm * (occ3 > 0 ? occ3 : 1);
+  ctx->keys_blocks = (int)(want < 1 ? 1 : (want < lim ? want : lim));
   ctx->grid_blocks = ctx->n_sm * 8;
-  int64_t io = (ctx->n + 255) / 256;
+  int64_t io = (ext + 255) / 256;
   ctx->io_blocks = (int)(io < 1 ? 1 : (io < ctx->n_sm * 16 ? io : ctx->n_sm * 16));
   return MPM_OK;
 }
@@ -315,9 +332,179 @@ int leave(mpm_ctx* ctx, void* stream) {
   return MPM_OK;
 }
 
+
+// Scene constants exactly as MPMSolver.__init__ (mpm_solver.py:32-80); fills everything but
+// the block/material/particle bases.
+int derive_scene(const mpm_scene_config& c, SceneDev& S, std::string& err) {
+  std::memset(&S, 0, sizeof(S));
+  if (!(c.grid_density > 0) || !(c.particle_size > 0) || !(c.substep_dt > 0) || c.n_particles < 0) {
+    err = "invalid grid_density/particle_size/substep_dt/n_particles";
+    return MPM_ERR_BAD_ARG;
+  }
+  const double dx = 1.0 / c.grid_density;
+  const double inv_dx = c.grid_density;
+  int64_t lo_cell[3], hi_cell[3], res[3];
+  double nodes = 1.0;
+  for (int d = 0; d < 3; ++d) {
+    if (!(c.upper_bound[d] > c.lower_bound[d])) {
+      err = "Invalid pair of upper_bound and lower_bound.";
+      return MPM_ERR_BAD_ARG;
+    }
+    lo_cell[d] = (int64_t)std::nearbyint(c.grid_density * c.lower_bound[d]);
+    hi_cell[d] = (int64_t)std::nearbyint(c.grid_density * c.upper_bound[d]);
+    res[d] = hi_cell[d] - lo_cell[d] + 1;
+    nodes *= (double)res[d];
+  }
+  if (nodes > 1e9) {
+    err = "Grid size larger than 1e9 not supported by MPM solver. Please reduce 'grid_density', or set tighter "
+          "boundaries via 'lower_bound' / 'upper_bound'.";
+    return MPM_ERR_BAD_ARG;
+  }
+  const double pvol = c.particle_size * c.particle_size * c.particle_size * 1e3;
+  S.dx = (float)dx;
+  S.inv_dx = (float)inv_dx;
+  S.dt = (float)c.substep_dt;
+  S.stress_scale = (float)(-c.substep_dt * pvol * 4.0 * inv_dx * inv_dx);
+  for (int d = 0; d < 3; ++d) {
+    S.grav[d] = (float)c.gravity[d];
+    S.lo[d] = (float)(c.lower_bound[d] + 3.0 * dx);
+    S.hi[d] = (float)(c.upper_bound[d] - 3.0 * dx);
+    S.res[d] = (int32_t)res[d];
+    S.offset[d] = (int32_t)lo_cell[d];
+    S.bres[d] = (int32_t)((res[d] + BLK - 1) / BLK);
+  }
+  S.eps = (float)c.mass_eps;
+  S.restitution = (float)c.restitution;
+  S.n_particles = c.n_particles;
+  return MPM_OK;
+}
+
+// Material record with the constants the reference folds in Python before compiling its
+// kernels (sand.py:70, snow.py:60, elasto_plastic.py:56) and the fp32 particle mass
+// particle_volume * rho (mpm_solver.py:822).
+MaterialDev derive_material(const mpm_material& m, const mpm_scene_config& c) {
+  MaterialDev M;
+  std::memset(&M, 0, sizeof(M));
+  M.type = m.type;
+  M.flags = m.flags;
+  M.scene = m.scene;
+  M.mu = (float)m.mu;
+  M.lam = (float)m.lam;
+  const float pvol = (float)(c.particle_size * c.particle_size * c.particle_size * 1e3);
+  M.mass = pvol * (float)m.rho;
+  M.default_Jp = (float)m.default_Jp;
+  M.alpha = (float)m.friction_alpha;
+  M.sand_coef = m.mu != 0.0 ? (float)((3.0 * m.lam + 2.0 * m.mu) / (2.0 * m.mu)) : 0.f;
+  M.clamp_lo = (float)(1.0 - m.yield_lower);
+  M.clamp_hi = (float)(1.0 + m.yield_higher);
+  M.vm_ratio = m.mu != 0.0 ? (float)(m.von_mises_yield_stress / (2.0 * m.mu)) : 0.f;
+  M.stiffness = (float)m.stiffness;
+  return M;
+}
+
 bool scene_range_ok(mpm_ctx* ctx, int64_t s0, int64_t s1) { return s0 >= 0 && s1 <= ctx->n_scenes && s0 < s1; }
 
 }  // namespace
+
+int mpm_ctx_destroy(mpm_ctx* ctx);
+// Allocates every device buffer of a context whose host tables are filled, uploads them
+// and initialises the particle slots; on failure frees the context.
+static int ctx_alloc_init(mpm_ctx* ctx, int32_t device, const std::vector<int32_t>& block_scene_h, mpm_ctx** out) {
+  int r = MPM_OK;
+  do {
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+      r = fail(nullptr, MPM_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+      break;
+    }
+    cudaDeviceProp prop;
+    e = cudaGetDeviceProperties(&prop, device);
+    if (e != cudaSuccess) {
+      r = fail(nullptr, MPM_ERR_CUDA, std::string("cudaGetDeviceProperties: ") + cudaGetErrorString(e));
+      break;
+    }
+    ctx->n_sm = prop.multiProcessorCount;
+    ctx->max_items = ctx->cap / 32 + ctx->K + 4;
+    ctx->n_tiles = (int)((ctx->K + 2 + SCAN_TILE - 1) / SCAN_TILE);
+    if ((r = dalloc(ctx, &ctx->d_scenes, ctx->n_scenes))) break;
+    if ((r = dalloc(ctx, &ctx->d_mats, ctx->n_mats > 0 ? ctx->n_mats : 1))) break;
+    if ((r = dalloc(ctx, &ctx->d_block_scene, ctx->K))) break;
+    if ((r = dalloc(ctx, &ctx->d_pbegin, ctx->n_scenes + 1))) break;
+    if ((r = dalloc(ctx, &ctx->d_first_mat, ctx->n_scenes))) break;
+    for (int b = 0; b < 2 && !r; ++b) {
+      if ((r = dalloc(ctx, &ctx->d_pbuf[b], (size_t)ctx->nf * ctx->cap))) break;
+      if ((r = dalloc(ctx, &ctx->d_grid[b], (size_t)ctx->K * BLK_NODES))) break;
+      if ((r = dalloc(ctx, &ctx->d_flags[b], ctx->K))) break;
+      if ((r = dalloc(ctx, &ctx->d_list[b], ctx->K))) break;
+    }
+    if (r) break;
+    if ((r = dalloc(ctx, &ctx->d_nlist, 2))) break;
+    if ((r = dalloc(ctx, &ctx->d_key, ctx->cap))) break;
+    if ((r = dalloc(ctx, &ctx->d_rank, ctx->cap))) break;
+    if ((r = dalloc(ctx, &ctx->d_perm, ctx->cap))) break;
+    if ((r = dalloc(ctx, &ctx->d_count, ctx->K + 2))) break;
+    if ((r = dalloc(ctx, &ctx->d_offset, ctx->K + 2))) break;
+    if ((r = dalloc(ctx, &ctx->d_items, ctx->max_items))) break;
+    if ((r = dalloc(ctx, &ctx->d_nitems, 1))) break;
+    if ((r = dalloc(ctx, &ctx->d_partials, ctx->n_tiles))) break;
+    if ((r = dalloc(ctx, &ctx->d_status, 1))) break;
+    if ((r = dalloc(ctx, &ctx->d_fp64, 1))) break;
+    if ((r = dalloc(ctx, &ctx->d_tmp64, 1))) break;
+    if ((r = dalloc(ctx, &ctx->d_steps, ctx->n_scenes))) break;
+  } while (0);
+  if (r) {
+    if (r != MPM_OK && ctx->err.size()) fail(nullptr, r, ctx->err);
+    mpm_ctx_destroy(ctx);
+    return r;
+  }
+#define CKC(call)                                                                                   \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess) {                                                                        \
+      fail(nullptr, MPM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));              \
+      mpm_ctx_destroy(ctx);                                                                         \
+      return MPM_ERR_CUDA;                                                                          \
+    }                                                                                               \
+  } while (0)
+  CKC(cudaStreamCreateWithFlags(&ctx->cs, cudaStreamNonBlocking));
+  CKC(cudaEventCreateWithFlags(&ctx->ev_in, cudaEventDisableTiming));
+  CKC(cudaEventCreateWithFlags(&ctx->ev_out, cudaEventDisableTiming));
+  CKC(cudaMemcpyAsync(ctx->d_scenes, ctx->scenes_h.data(), sizeof(SceneDev) * ctx->n_scenes, cudaMemcpyHostToDevice, ctx->cs));
+  if (ctx->n_mats > 0)
+    CKC(cudaMemcpyAsync(ctx->d_mats, ctx->mats_h.data(), sizeof(MaterialDev) * ctx->n_mats, cudaMemcpyHostToDevice,
+                        ctx->cs));
+  if (ctx->K > 0)
+    CKC(cudaMemcpyAsync(ctx->d_block_scene, block_scene_h.data(), sizeof(int32_t) * ctx->K, cudaMemcpyHostToDevice, ctx->cs));
+  CKC(cudaMemcpyAsync(ctx->d_pbegin, ctx->pbegin_h.data(), sizeof(int64_t) * (ctx->n_scenes + 1), cudaMemcpyHostToDevice,
+                      ctx->cs));
+  CKC(cudaMemcpyAsync(ctx->d_first_mat, ctx->first_mat_h.data(), sizeof(int32_t) * ctx->n_scenes, cudaMemcpyHostToDevice,
+                      ctx->cs));
+  for (int b = 0; b < 2; ++b) {
+    CKC(cudaMemsetAsync(ctx->d_grid[b], 0, sizeof(float4) * (size_t)ctx->K * BLK_NODES, ctx->cs));
+    CKC(cudaMemsetAsync(ctx->d_flags[b], 0, sizeof(int32_t) * (size_t)(ctx->K > 0 ? ctx->K : 1), ctx->cs));
+    CKC(cudaMemsetAsync(ctx->d_pbuf[b], 0, sizeof(float) * (size_t)ctx->nf * ctx->cap, ctx->cs));
+  }
+  CKC(cudaMemsetAsync(ctx->d_nlist, 0, sizeof(int32_t) * 2, ctx->cs));
+  CKC(cudaMemsetAsync(ctx->d_count, 0, sizeof(int32_t) * (ctx->K + 2), ctx->cs));
+  CKC(cudaMemsetAsync(ctx->d_nitems, 0, sizeof(int32_t), ctx->cs));
+  CKC(cudaMemsetAsync(ctx->d_status, 0, sizeof(uint32_t), ctx->cs));
+  CKC(cudaMemsetAsync(ctx->d_fp64, 0, sizeof(unsigned long long), ctx->cs));
+  CKC(cudaMemsetAsync(ctx->d_steps, 0xff, sizeof(int32_t) * ctx->n_scenes, ctx->cs));  // -1: unlimited
+  if (compute_launch_shapes(ctx)) {
+    fail(nullptr, MPM_ERR_CUDA, ctx->err);
+    mpm_ctx_destroy(ctx);
+    return MPM_ERR_CUDA;
+  }
+  if (ctx->n > 0 && ctx->n_mats > 0) {
+    KParams Pp = make_params(ctx, 0, 0, 0);
+    k_init_particles<<<ctx->io_blocks, 256, 0, ctx->cs>>>(Pp, ctx->d_pbegin, ctx->d_first_mat, ctx->n_scenes);
+    CKC(cudaGetLastError());
+  }
+  CKC(cudaStreamSynchronize(ctx->cs));
+#undef CKC
+  *out = ctx;
+  return MPM_OK;
+}
 
 // =====================================================================================
 extern "C" {
@@ -375,42 +562,11 @@ int mpm_ctx_create(const mpm_scene_config* scenes, int64_t n_scenes, const mpm_m
       return fail(nullptr, MPM_ERR_BAD_ARG, "scene " + std::to_string(s) + ": invalid grid_density/particle_size/dt");
     }
     SceneDev S;
-    std::memset(&S, 0, sizeof(S));
-    const double dx = 1.0 / c.grid_density;
-    const double inv_dx = c.grid_density;
-    int64_t lo_cell[3], hi_cell[3], res[3];
-    double nodes = 1.0;
-    for (int d = 0; d < 3; ++d) {
-      if (!(c.upper_bound[d] > c.lower_bound[d])) {
-        delete ctx;
-        return fail(nullptr, MPM_ERR_BAD_ARG, "Invalid pair of upper_bound and lower_bound.");
-      }
-      lo_cell[d] = (int64_t)std::nearbyint(c.grid_density * c.lower_bound[d]);
-      hi_cell[d] = (int64_t)std::nearbyint(c.grid_density * c.upper_bound[d]);
-      res[d] = hi_cell[d] - lo_cell[d] + 1;
-      nodes *= (double)res[d];
-    }
-    if (nodes > 1e9) {
+    std::string derr;
+    if (int e = derive_scene(c, S, derr)) {
       delete ctx;
-      return fail(nullptr, MPM_ERR_BAD_ARG,
-                  "Grid size larger than 1e9 not supported by MPM solver. Please reduce 'grid_density', or set "
-                  "tighter boundaries via 'lower_bound' / 'upper_bound'.");
+      return fail(nullptr, e, derr);
     }
-    const double pvol = c.particle_size * c.particle_size * c.particle_size * 1e3;
-    S.dx = (float)dx;
-    S.inv_dx = (float)inv_dx;
-    S.dt = (float)c.substep_dt;
-    S.stress_scale = (float)(-c.substep_dt * pvol * 4.0 * inv_dx * inv_dx);
-    for (int d = 0; d < 3; ++d) {
-      S.grav[d] = (float)c.gravity[d];
-      S.lo[d] = (float)(c.lower_bound[d] + 3.0 * dx);
-      S.hi[d] = (float)(c.upper_bound[d] - 3.0 * dx);
-      S.res[d] = (int32_t)res[d];
-      S.offset[d] = (int32_t)lo_cell[d];
-      S.bres[d] = (int32_t)((res[d] + BLK - 1) / BLK);
-    }
-    S.eps = (float)c.mass_eps;
-    S.restitution = (float)c.restitution;
     S.mat_begin = mat_begin[s] < 0 ? 0 : mat_begin[s];
     S.block_base = K;
     S.p_begin = P;
@@ -435,123 +591,18 @@ int mpm_ctx_create(const mpm_scene_config* scenes, int64_t n_scenes, const mpm_m
   }
   ctx->K = K;
   ctx->n = P;
+  ctx->n_phys = P;
   ctx->cap = ((P + 63) / 64) * 64;
   if (ctx->cap == 0) ctx->cap = 64;
 
   for (int32_t i = 0; i < n_materials; ++i) {
     const mpm_material& m = materials[i];
     const mpm_scene_config& c = scenes[m.scene];
-    MaterialDev M;
-    std::memset(&M, 0, sizeof(M));
-    M.type = m.type;
-    M.flags = m.flags;
-    M.scene = m.scene;
-    M.mu = (float)m.mu;
-    M.lam = (float)m.lam;
-    const float pvol = (float)(c.particle_size * c.particle_size * c.particle_size * 1e3);
-    M.mass = pvol * (float)m.rho;  // mpm_solver.py:822, fp32 product
-    M.default_Jp = (float)m.default_Jp;
-    M.alpha = (float)m.friction_alpha;
-    M.sand_coef = m.mu != 0.0 ? (float)((3.0 * m.lam + 2.0 * m.mu) / (2.0 * m.mu)) : 0.f;
-    M.clamp_lo = (float)(1.0 - m.yield_lower);
-    M.clamp_hi = (float)(1.0 + m.yield_higher);
-    M.vm_ratio = m.mu != 0.0 ? (float)(m.von_mises_yield_stress / (2.0 * m.mu)) : 0.f;
-    M.stiffness = (float)m.stiffness;
+    MaterialDev M = derive_material(m, c);
     ctx->mats_h.push_back(M);
   }
 
-  int r = MPM_OK;
-  do {
-    cudaError_t e = cudaSetDevice(device);
-    if (e != cudaSuccess) {
-      r = fail(nullptr, MPM_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
-      break;
-    }
-    cudaDeviceProp prop;
-    e = cudaGetDeviceProperties(&prop, device);
-    if (e != cudaSuccess) {
-      r = fail(nullptr, MPM_ERR_CUDA, std::string("cudaGetDeviceProperties: ") + cudaGetErrorString(e));
-      break;
-    }
-    ctx->n_sm = prop.multiProcessorCount;
-    ctx->max_items = ctx->cap / 32 + K + 4;
-    ctx->n_tiles = (int)((K + 2 + SCAN_TILE - 1) / SCAN_TILE);
-    if ((r = dalloc(ctx, &ctx->d_scenes, n_scenes))) break;
-    if ((r = dalloc(ctx, &ctx->d_mats, n_materials > 0 ? n_materials : 1))) break;
-    if ((r = dalloc(ctx, &ctx->d_block_scene, K))) break;
-    if ((r = dalloc(ctx, &ctx->d_pbegin, n_scenes + 1))) break;
-    if ((r = dalloc(ctx, &ctx->d_first_mat, n_scenes))) break;
-    for (int b = 0; b < 2 && !r; ++b) {
-      if ((r = dalloc(ctx, &ctx->d_pbuf[b], (size_t)ctx->nf * ctx->cap))) break;
-      if ((r = dalloc(ctx, &ctx->d_grid[b], (size_t)K * BLK_NODES))) break;
-      if ((r = dalloc(ctx, &ctx->d_flags[b], K))) break;
-      if ((r = dalloc(ctx, &ctx->d_list[b], K))) break;
-    }
-    if (r) break;
-    if ((r = dalloc(ctx, &ctx->d_nlist, 2))) break;
-    if ((r = dalloc(ctx, &ctx->d_key, ctx->cap))) break;
-    if ((r = dalloc(ctx, &ctx->d_rank, ctx->cap))) break;
-    if ((r = dalloc(ctx, &ctx->d_perm, ctx->cap))) break;
-    if ((r = dalloc(ctx, &ctx->d_count, K + 2))) break;
-    if ((r = dalloc(ctx, &ctx->d_offset, K + 2))) break;
-    if ((r = dalloc(ctx, &ctx->d_items, ctx->max_items))) break;
-    if ((r = dalloc(ctx, &ctx->d_nitems, 1))) break;
-    if ((r = dalloc(ctx, &ctx->d_partials, ctx->n_tiles))) break;
-    if ((r = dalloc(ctx, &ctx->d_status, 1))) break;
-    if ((r = dalloc(ctx, &ctx->d_fp64, 1))) break;
-    if ((r = dalloc(ctx, &ctx->d_tmp64, 1))) break;
-  } while (0);
-  if (r) {
-    if (r != MPM_OK && ctx->err.size()) fail(nullptr, r, ctx->err);
-    mpm_ctx_destroy(ctx);
-    return r;
-  }
-#define CKC(call)                                                                                   \
-  do {                                                                                              \
-    cudaError_t e_ = (call);                                                                        \
-    if (e_ != cudaSuccess) {                                                                        \
-      fail(nullptr, MPM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));              \
-      mpm_ctx_destroy(ctx);                                                                         \
-      return MPM_ERR_CUDA;                                                                          \
-    }                                                                                               \
-  } while (0)
-  CKC(cudaStreamCreateWithFlags(&ctx->cs, cudaStreamNonBlocking));
-  CKC(cudaEventCreateWithFlags(&ctx->ev_in, cudaEventDisableTiming));
-  CKC(cudaEventCreateWithFlags(&ctx->ev_out, cudaEventDisableTiming));
-  CKC(cudaMemcpyAsync(ctx->d_scenes, ctx->scenes_h.data(), sizeof(SceneDev) * n_scenes, cudaMemcpyHostToDevice, ctx->cs));
-  if (n_materials > 0)
-    CKC(cudaMemcpyAsync(ctx->d_mats, ctx->mats_h.data(), sizeof(MaterialDev) * n_materials, cudaMemcpyHostToDevice,
-                        ctx->cs));
-  if (K > 0)
-    CKC(cudaMemcpyAsync(ctx->d_block_scene, block_scene_h.data(), sizeof(int32_t) * K, cudaMemcpyHostToDevice, ctx->cs));
-  CKC(cudaMemcpyAsync(ctx->d_pbegin, ctx->pbegin_h.data(), sizeof(int64_t) * (n_scenes + 1), cudaMemcpyHostToDevice,
-                      ctx->cs));
-  CKC(cudaMemcpyAsync(ctx->d_first_mat, ctx->first_mat_h.data(), sizeof(int32_t) * n_scenes, cudaMemcpyHostToDevice,
-                      ctx->cs));
-  for (int b = 0; b < 2; ++b) {
-    CKC(cudaMemsetAsync(ctx->d_grid[b], 0, sizeof(float4) * (size_t)K * BLK_NODES, ctx->cs));
-    CKC(cudaMemsetAsync(ctx->d_flags[b], 0, sizeof(int32_t) * (size_t)(K > 0 ? K : 1), ctx->cs));
-    CKC(cudaMemsetAsync(ctx->d_pbuf[b], 0, sizeof(float) * (size_t)ctx->nf * ctx->cap, ctx->cs));
-  }
-  CKC(cudaMemsetAsync(ctx->d_nlist, 0, sizeof(int32_t) * 2, ctx->cs));
-  CKC(cudaMemsetAsync(ctx->d_count, 0, sizeof(int32_t) * (K + 2), ctx->cs));
-  CKC(cudaMemsetAsync(ctx->d_nitems, 0, sizeof(int32_t), ctx->cs));
-  CKC(cudaMemsetAsync(ctx->d_status, 0, sizeof(uint32_t), ctx->cs));
-  CKC(cudaMemsetAsync(ctx->d_fp64, 0, sizeof(unsigned long long), ctx->cs));
-  if (compute_launch_shapes(ctx)) {
-    fail(nullptr, MPM_ERR_CUDA, ctx->err);
-    mpm_ctx_destroy(ctx);
-    return MPM_ERR_CUDA;
-  }
-  if (ctx->n > 0 && n_materials > 0) {
-    KParams Pp = make_params(ctx, 0, 0, 0);
-    k_init_particles<<<ctx->io_blocks, 256, 0, ctx->cs>>>(Pp, ctx->d_pbegin, ctx->d_first_mat, n_scenes);
-    CKC(cudaGetLastError());
-  }
-  CKC(cudaStreamSynchronize(ctx->cs));
-#undef CKC
-  *out = ctx;
-  return MPM_OK;
+  return ctx_alloc_init(ctx, device, block_scene_h, out);
 }
 
 int mpm_ctx_destroy(mpm_ctx* ctx) {
@@ -687,6 +738,7 @@ int mpm_substeps(mpm_ctx* ctx, int32_t n_substeps, void* stream) {
     if (ctx->cur == 1) {
       if ((r = launch_substep(ctx, 1, ctx->cs))) return r;
       ctx->cur = 0;
+      ctx->n_phys = ctx->n;
       --left;
     }
     if (left >= 2) {
@@ -698,7 +750,9 @@ int mpm_substeps(mpm_ctx* ctx, int32_t n_substeps, void* stream) {
   while (left-- > 0) {
     if ((r = launch_substep(ctx, ctx->cur, ctx->cs))) return r;
     ctx->cur ^= 1;
+    ctx->n_phys = ctx->n;
   }
+  ctx->n_phys = ctx->n;
   return leave(ctx, stream);
 }
 
@@ -730,6 +784,7 @@ int mpm_substep_post(mpm_ctx* ctx, void* stream) {
   if (r) return r;
   if ((r = launch_post(ctx, ctx->cur, ctx->cs))) return r;
   ctx->cur ^= 1;
+  ctx->n_phys = ctx->n;
   ctx->phase = 0;
   return leave(ctx, stream);
 }
@@ -782,9 +837,9 @@ int mpm_status_word(mpm_ctx* ctx, uint32_t* status_host, int64_t* fp64_svd_host,
 
 int mpm_set_tuning(mpm_ctx* ctx, int32_t p2g_threads, int32_t particles_per_thread, int32_t use_graph) {
   if (!ctx) return MPM_ERR_BAD_ARG;
-  if (p2g_threads < 64 || p2g_threads > 256 || p2g_threads % 32 || particles_per_thread < 1 ||
-      particles_per_thread > 16)
-    return fail(ctx, MPM_ERR_BAD_ARG, "tuning out of range (threads 64..256 step 32, ppt 1..16)");
+  if (p2g_threads < 64 || p2g_threads > P2G_MAX_THREADS || p2g_threads % 32 || particles_per_thread < 1 ||
+      p2g_threads * particles_per_thread > P2G_MAX_CHUNK)
+    return fail(ctx, MPM_ERR_BAD_ARG, "tuning out of range (threads 64..256 step 32, threads*ppt <= 2048)");
   if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "tuning inside a substep");
   const bool changed = p2g_threads != ctx->p2g_threads || particles_per_thread != ctx->ppt;
   ctx->p2g_threads = p2g_threads;
@@ -841,6 +896,149 @@ int mpm_kernel_times(mpm_ctx* ctx, double* ms_host, int64_t* counts_host, int32_
     }
   }
   return MPM_OK;
+}
+
+// ------------------------------------------------------------------ pool mode (serving)
+int mpm_ctx_create_pool(const mpm_pool_config* cfg, int32_t device, mpm_ctx** out) {
+  if (!out || !cfg) return fail(nullptr, MPM_ERR_BAD_ARG, "null argument");
+  *out = nullptr;
+  if (cfg->max_scenes <= 0 || cfg->particle_capacity <= 0 || cfg->max_grid_res < 4 || cfg->max_materials_per_scene <= 0)
+    return fail(nullptr, MPM_ERR_BAD_ARG, "invalid pool configuration");
+  const int64_t bres = (cfg->max_grid_res + BLK - 1) / BLK;
+  const int64_t max_blocks = bres * bres * bres;
+  const int64_t K = cfg->max_scenes * max_blocks;
+  const int64_t n_mats = cfg->max_scenes * (int64_t)cfg->max_materials_per_scene;
+  if (K + 2 >= (int64_t)INT32_MAX / 2 || cfg->particle_capacity >= (int64_t)INT32_MAX / 2 ||
+      n_mats > (int64_t)INFO_MAT_MASK)
+    return fail(nullptr, MPM_ERR_BAD_ARG, "pool too large for one context");
+  mpm_ctx* ctx = new mpm_ctx();
+  ctx->device = device;
+  ctx->pool = true;
+  ctx->n_scenes = cfg->max_scenes;
+  ctx->n_mats = n_mats;
+  ctx->max_blocks = max_blocks;
+  ctx->max_mats = cfg->max_materials_per_scene;
+  ctx->nf = cfg->with_muscle ? NF_MUSCLE : NF_BASE;
+  ctx->K = K;
+  ctx->cap = ((cfg->particle_capacity + 63) / 64) * 64;
+  ctx->n = ctx->n_phys = 0;
+  ctx->slot_n.assign(cfg->max_scenes, 0);
+  ctx->slot_live.assign(cfg->max_scenes, 0);
+  ctx->mat_count_h.assign(cfg->max_scenes, 0);
+  ctx->pbegin_h.assign(cfg->max_scenes + 1, 0);
+  ctx->first_mat_h.resize(cfg->max_scenes);
+  std::vector<int32_t> block_scene_h((size_t)K);
+  mpm_scene_config c0;
+  std::memset(&c0, 0, sizeof(c0));
+  c0.substep_dt = 1e-4;
+  c0.grid_density = (double)(cfg->max_grid_res - 1);
+  c0.upper_bound[0] = c0.upper_bound[1] = c0.upper_bound[2] = 1.0;
+  c0.particle_size = 1.0 / c0.grid_density;
+  c0.mass_eps = 1.1920929e-7;
+  for (int64_t s = 0; s < cfg->max_scenes; ++s) {
+    SceneDev S;
+    std::string err;
+    derive_scene(c0, S, err);
+    S.block_base = s * max_blocks;
+    S.mat_begin = (int32_t)(s * cfg->max_materials_per_scene);
+    ctx->scenes_h.push_back(S);
+    ctx->first_mat_h[s] = S.mat_begin;
+    for (int64_t b = 0; b < max_blocks; ++b) block_scene_h[(size_t)(s * max_blocks + b)] = (int32_t)s;
+    for (int32_t j = 0; j < cfg->max_materials_per_scene; ++j) {
+      mpm_material m;
+      std::memset(&m, 0, sizeof(m));
+      m.scene = (int32_t)s;
+      m.rho = 1000.0;
+      m.default_Jp = 1.0;
+      ctx->mats_h.push_back(derive_material(m, c0));
+    }
+  }
+  return ctx_alloc_init(ctx, device, block_scene_h, out);
+}
+
+int mpm_scene_admit(mpm_ctx* ctx, int64_t slot, const mpm_scene_config* scene, const mpm_material* materials,
+                    int32_t n_materials, int64_t n, const float* pos, const int32_t* mat_local, int32_t n_substeps,
+                    void* stream) {
+  if (!ctx || !scene || !materials || !pos) return MPM_ERR_BAD_ARG;
+  if (!ctx->pool) return fail(ctx, MPM_ERR_STATE, "not a pool context");
+  if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "admit inside a substep");
+  if (slot < 0 || slot >= ctx->n_scenes || ctx->slot_live[slot]) return fail(ctx, MPM_ERR_BAD_ARG, "slot busy or out of range");
+  if (n_materials <= 0 || n_materials > ctx->max_mats) return fail(ctx, MPM_ERR_BAD_ARG, "bad material count");
+  if (n <= 0 || ctx->n_phys + n > ctx->cap) return fail(ctx, MPM_ERR_OOM, "particle pool full");
+  SceneDev S;
+  std::string err;
+  if (int e = derive_scene(*scene, S, err)) return fail(ctx, e, err);
+  if ((int64_t)S.bres[0] * S.bres[1] * S.bres[2] > ctx->max_blocks)
+    return fail(ctx, MPM_ERR_BAD_ARG, "scene grid larger than the pool's per-slot grid");
+  for (int32_t j = 0; j < n_materials; ++j) {
+    if (materials[j].type < MPM_MAT_ELASTIC || materials[j].type > MPM_MAT_MUSCLE)
+      return fail(ctx, MPM_ERR_BAD_ARG, "unknown material type");
+    if (materials[j].type == MPM_MAT_MUSCLE && ctx->nf == NF_BASE)
+      return fail(ctx, MPM_ERR_BAD_ARG, "pool created without muscle fields");
+  }
+  S.block_base = slot * ctx->max_blocks;
+  S.mat_begin = (int32_t)(slot * ctx->max_mats);
+  S.p_begin = 0;
+  S.n_particles = n;
+  int r = enter(ctx, stream);
+  if (r) return r;
+  ctx->scenes_h[slot] = S;
+  for (int32_t j = 0; j < n_materials; ++j) {
+    mpm_material m = materials[j];
+    m.scene = (int32_t)slot;
+    ctx->mats_h[S.mat_begin + j] = derive_material(m, *scene);
+  }
+  CK(cudaMemcpyAsync(ctx->d_scenes + slot, &ctx->scenes_h[slot], sizeof(SceneDev), cudaMemcpyHostToDevice, ctx->cs));
+  CK(cudaMemcpyAsync(ctx->d_mats + S.mat_begin, &ctx->mats_h[S.mat_begin], sizeof(MaterialDev) * n_materials,
+                     cudaMemcpyHostToDevice, ctx->cs));
+  int32_t steps = n_substeps < 0 ? -1 : n_substeps;
+  CK(cudaMemcpyAsync(ctx->d_steps + slot, &steps, sizeof(int32_t), cudaMemcpyHostToDevice, ctx->cs));
+  KParams P = make_params(ctx, ctx->cur, ctx->cur, ctx->cur);
+  const int64_t nb = (n + 255) / 256;
+  k_admit<<<(unsigned)(nb < 65535 ? nb : 65535), 256, 0, ctx->cs>>>(P, (int32_t)slot, ctx->n_phys, n, pos, mat_local);
+  CKL();
+  CK(cudaStreamSynchronize(ctx->cs));  // the host records above must outlive the copies
+  ctx->n_phys += n;
+  ctx->n += n;
+  ctx->slot_n[slot] = n;
+  ctx->slot_live[slot] = 1;
+  ctx->mat_count_h[slot] = n_materials;
+  ctx->sorted = false;
+  drop_graph(ctx);
+  if ((r = compute_launch_shapes(ctx))) return r;
+  return leave(ctx, stream);
+}
+
+int mpm_scene_retire(mpm_ctx* ctx, int64_t slot, void* stream) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (!ctx->pool) return fail(ctx, MPM_ERR_STATE, "not a pool context");
+  if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "retire inside a substep");
+  if (slot < 0 || slot >= ctx->n_scenes || !ctx->slot_live[slot]) return fail(ctx, MPM_ERR_BAD_ARG, "slot not live");
+  int r = enter(ctx, stream);
+  if (r) return r;
+  KParams P = make_params(ctx, ctx->cur, ctx->cur, ctx->cur);
+  k_retire<<<ctx->io_blocks, 256, 0, ctx->cs>>>(P, (int32_t)slot);
+  CKL();
+  int32_t frozen = 0;
+  CK(cudaMemcpyAsync(ctx->d_steps + slot, &frozen, sizeof(int32_t), cudaMemcpyHostToDevice, ctx->cs));
+  // dead particles sort after every live one; the next P2G drops them
+  if ((r = launch_rekey(ctx, ctx->cs))) return r;
+  CK(cudaStreamSynchronize(ctx->cs));
+  ctx->n -= ctx->slot_n[slot];
+  ctx->slot_n[slot] = 0;
+  ctx->slot_live[slot] = 0;
+  drop_graph(ctx);
+  if ((r = compute_launch_shapes(ctx))) return r;
+  return leave(ctx, stream);
+}
+
+int mpm_scene_steps_left(mpm_ctx* ctx, int32_t* out_host, void* stream) {
+  if (!ctx || !out_host) return MPM_ERR_BAD_ARG;
+  int r = enter(ctx, stream);
+  if (r) return r;
+  CK(cudaMemcpyAsync(out_host, ctx->d_steps, sizeof(int32_t) * ctx->n_scenes, cudaMemcpyDeviceToHost, ctx->cs));
+  CK(cudaStreamSynchronize(ctx->cs));
+  return leave(ctx, stream);
 }
 
 int mpm_version(void) { return 1; }

@@ -1,7 +1,7 @@
 // mpm_kernels.cu - sm_103a kernels of the MLS-MPM substep (P2G, grid op, G2P) and of the
 // per-substep particle re-sort, plus the state I/O kernels.
 //
-// One substep = k_p2g -> k_grid_op -> k_g2p<true> -> k_scan_reduce -> k_scan_partials ->
+// One substep = k_p2g -> k_grid_op -> k_g2p -> k_scan_reduce -> k_scan_partials ->
 // k_scan_apply -> k_perm.  Reference semantics: genesis/engine/solvers/mpm_solver.py
 // (p2g :322-421, g2p :423-481) and genesis/engine/couplers/legacy_coupler.py
 // (mpm_grid_op :356-501); see each kernel.
@@ -47,7 +47,7 @@ __device__ __forceinline__ void write_defaults(float* D, int64_t cap, int64_t i,
 
 // FP64 re-solve for the rare particle whose FP32 factor fails its residual check; kept out
 // of line so its registers do not weigh on the P2G kernel.
-__device__ __noinline__ void svd3_fp64(const float* Ft, float* U, float* sig, float* V) {
+__device__ __forceinline__ void svd3_fp64(const float* Ft, float* U, float* sig, float* V) {
   double Ad[9], Ud[9], sd[3], Vd[9];
   for (int k = 0; k < 9; ++k) Ad[k] = Ft[k];
   svd3<double, 8>(Ad, Ud, sd, Vd);
@@ -93,6 +93,32 @@ __global__ void k_add_particles(KParams P, int64_t s0, int64_t s1, int64_t start
 #pragma unroll
     for (int d = 0; d < 3; ++d) D[(int64_t)(PF_POS + d) * P.cap + i] = pos[j * 3 + d];
     D[(int64_t)PF_INFO * P.cap + i] = __uint_as_float(gmat | INFO_FREE | (active ? INFO_ACTIVE : 0u));
+  }
+}
+
+// Pool mode: append n_add particles of scene `s` at slots [n0, n0 + n_add) of the current
+// buffer (pid 0..n_add-1, material = scene base + mat_local[i] or + 0).
+__global__ void k_admit(KParams P, int32_t s, int64_t n0, int64_t n_add, const float* pos, const int32_t* mat_local) {
+  float* D = P.dst;
+  const SceneDev& S = P.scenes[s];
+  for (int64_t j = grid_stride_begin(); j < n_add; j += grid_stride_step()) {
+    const int64_t i = n0 + j;
+    const uint32_t gmat = (uint32_t)(S.mat_begin + (mat_local ? mat_local[j] : 0));
+    write_defaults(D, P.cap, i, P.nf, P.mats[gmat].default_Jp);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) D[(int64_t)(PF_POS + d) * P.cap + i] = pos[j * 3 + d];
+    D[(int64_t)PF_INFO * P.cap + i] = __uint_as_float(gmat | INFO_FREE | INFO_ACTIVE);
+    D[(int64_t)PF_PID * P.cap + i] = __uint_as_float((uint32_t)j);
+  }
+}
+
+// Pool mode: mark every particle of scene `s` dead (dropped by the next sort).
+__global__ void k_retire(KParams P, int32_t s) {
+  float* D = P.dst;
+  for (int64_t i = grid_stride_begin(); i < P.n; i += grid_stride_step()) {
+    const uint32_t info = ld_info(D, P.cap, i);
+    if (!(info & INFO_DEAD) && scene_of(P, info) == s)
+      D[(int64_t)PF_INFO * P.cap + i] = __uint_as_float(info | INFO_DEAD);
   }
 }
 
@@ -190,110 +216,33 @@ __global__ void k_particles_field(KParams P, int field, int write, int64_t s0, i
   }
 }
 
-// ------------------------------------------------------------------ G2P (+ re-keying)
-// mpm_solver.py:423-481 (g2p) with the particle boundary of boundaries.py:22-32, followed by
-// the bucket key of the new position and a warp-aggregated rank within the bucket.
-// UPDATE=false only computes keys (after a state change).
-template <bool UPDATE>
-__device__ __forceinline__ void g2p_body(const KParams& P) {
-  if (UPDATE && blockIdx.x == 0 && threadIdx.x == 0) *P.nlist_other = 0;
-  float* D = P.dst;
+// ------------------------------------------------------------------ re-keying
+// Bucket key and warp-aggregated rank of every particle from its current position (after
+// a state change: load, set_state, set_particles).  The per-substep keys come from k_g2p.
+__global__ void __launch_bounds__(256) k_keys(KParams P) {
+  const float* D = P.dst;
   const int64_t cap = P.cap;
   const int lane = threadIdx.x & 31;
   const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const int32_t kInactive = (int32_t)P.K, kDead = (int32_t)P.K + 1;
   for (int64_t base = warp0 * 32; base < P.n; base += nwarps * 32) {
     const int64_t i = base + lane;
     const bool valid = i < P.n;
-    int32_t key = kInactive;
+    int32_t key = (int32_t)P.K;
     if (valid) {
       const uint32_t info = ld_info(D, cap, i);
       if (info & INFO_DEAD) {
-        key = kDead;
+        key = (int32_t)P.K + 1;
       } else if (info & INFO_ACTIVE) {
         const SceneDev& S = P.scenes[scene_of(P, info)];
         float x[3];
+        int b[3];
 #pragma unroll
         for (int d = 0; d < 3; ++d) x[d] = D[(int64_t)(PF_POS + d) * cap + i];
-        int b[3];
-        const bool ok = stencil_origin(S, x, b);
-        if (!ok) {
-          atomicOr(P.status, (isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2])) ? 2u : 1u);
-        } else if (!UPDATE) {
-          key = (int32_t)block_of(S, b[0], b[1], b[2]);
-        } else {
-          float fx[3], w[3][3];
-#pragma unroll
-          for (int d = 0; d < 3; ++d) {
-            const float t = __fmul_rn(x[d], S.inv_dx);
-            fx[d] = t - (float)(b[d] + S.offset[d]);
-            bspline_w(fx[d], w[d]);
-          }
-          // per-axis address terms of the 3 stencil nodes
-          int64_t ax[3];
-          int ay[3], az[3];
-#pragma unroll
-          for (int o = 0; o < 3; ++o) {
-            const int gx = b[0] + o, gy = b[1] + o, gz = b[2] + o;
-            ax[o] = (S.block_base + (int64_t)(gx >> 2) * S.bres[1] * S.bres[2]) * BLK_NODES + (gx & 3) * 16;
-            ay[o] = (gy >> 2) * S.bres[2] * BLK_NODES + (gy & 3) * 4;
-            az[o] = (gz >> 2) * BLK_NODES + (gz & 3);
-          }
-          float v[3] = {0.f, 0.f, 0.f};
-          float Cn[9];
-#pragma unroll
-          for (int k = 0; k < 9; ++k) Cn[k] = 0.f;
-#pragma unroll
-          for (int ox = 0; ox < 3; ++ox)
-#pragma unroll
-            for (int oy = 0; oy < 3; ++oy)
-#pragma unroll
-              for (int oz = 0; oz < 3; ++oz) {
-                const float4 g = __ldg(&P.grid[ax[ox] + ay[oy] + az[oz]]);
-                const float wt = w[0][ox] * w[1][oy] * w[2][oz];
-                const float dp[3] = {(float)ox - fx[0], (float)oy - fx[1], (float)oz - fx[2]};
-                const float gv[3] = {g.x, g.y, g.z};
-#pragma unroll
-                for (int r = 0; r < 3; ++r) {
-                  v[r] += wt * gv[r];
-                  const float s = 4.f * S.inv_dx * wt * gv[r];
-#pragma unroll
-                  for (int c = 0; c < 3; ++c) Cn[r * 3 + c] += s * dp[c];
-                }
-              }
-          float xn[3];
-          bool finite = true;
-#pragma unroll
-          for (int d = 0; d < 3; ++d) {
-            xn[d] = x[d] + S.dt * v[d];
-            finite = finite && isfinite(xn[d]) && isfinite(v[d]);
-          }
-          // CubeBoundary.impose_pos_vel (boundaries.py:22-32)
-#pragma unroll
-          for (int d = 0; d < 3; ++d) {
-            if (xn[d] >= S.hi[d] && v[d] >= 0.f) v[d] *= -S.restitution;
-            else if (xn[d] <= S.lo[d] && v[d] <= 0.f) v[d] *= -S.restitution;
-            xn[d] = fmaxf(fminf(xn[d], S.hi[d]), S.lo[d]);
-          }
-#pragma unroll
-          for (int d = 0; d < 3; ++d) {
-            D[(int64_t)(PF_POS + d) * cap + i] = xn[d];
-            D[(int64_t)(PF_VEL + d) * cap + i] = v[d];
-          }
-#pragma unroll
-          for (int k = 0; k < 9; ++k) D[(int64_t)(PF_C + k) * cap + i] = Cn[k];
-          if (!finite) {
-            atomicOr(P.status, 1u);
-          } else if (stencil_origin(S, xn, b)) {
-            key = (int32_t)block_of(S, b[0], b[1], b[2]);
-          } else {
-            atomicOr(P.status, 2u);
-          }
-        }
+        if (stencil_origin(S, x, b)) key = (int32_t)block_of(S, b[0], b[1], b[2]);
+        else atomicOr(P.status, (isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2])) ? 2u : 1u);
       }
     }
-    // warp-aggregated rank within the bucket
     const unsigned am = __ballot_sync(0xffffffffu, valid);
     if (valid) {
       const unsigned peers = __match_any_sync(am, key);
@@ -307,8 +256,6 @@ __device__ __forceinline__ void g2p_body(const KParams& P) {
     }
   }
 }
-__global__ void __launch_bounds__(256) k_g2p(KParams P) { g2p_body<true>(P); }
-__global__ void __launch_bounds__(256) k_keys(KParams P) { g2p_body<false>(P); }
 
 // ------------------------------------------------------------------ counting-sort scan
 namespace {
@@ -420,159 +367,267 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(KParams P) {
 __global__ void k_perm(KParams P) {
   for (int64_t i = grid_stride_begin(); i < P.n; i += grid_stride_step())
     P.perm[P.offset[P.key[i]] + P.rank[i]] = (int32_t)i;
+  if (P.steps && blockIdx.x == 0)  // end of a substep: count down per-scene substep budgets
+    for (int s = threadIdx.x; s < P.n_scenes; s += blockDim.x)
+      if (P.steps[s] > 0) P.steps[s] -= 1;
 }
 
 // ------------------------------------------------------------------ P2G
-// Per work item (one grid block's bucket, up to `chunk` particles): gather each particle
-// from the old order through perm, run compute_F_tmp + svd + material update + stress
-// (mpm_solver.py:293-307, 339-377), write the full particle to its sorted slot, and
-// scatter mass and APIC momentum (mpm_solver.py:379-418) into a 6^3-node shared-memory
-// tile.  The tile is flushed with one 16-byte vector reduction per touched node.
-__global__ void __launch_bounds__(256) k_p2g(KParams P) {
-  __shared__ float s_m[TILE_NODES], s_px[TILE_NODES], s_py[TILE_NODES], s_pz[TILE_NODES];
+namespace {
+
+// Loads one particle from the old order (planes of `S`, index si).
+struct Particle {
+  float x[3], v[3], C[9], F[9], Jp, pid, actu, mdir[3];
+  uint32_t info;
+};
+
+__device__ __forceinline__ void load_particle(const KParams& P, const float* Sx, int64_t si, Particle& q) {
+  const int64_t cap = P.cap;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    q.x[d] = Sx[(int64_t)(PF_POS + d) * cap + si];
+    q.v[d] = Sx[(int64_t)(PF_VEL + d) * cap + si];
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    q.C[k] = Sx[(int64_t)(PF_C + k) * cap + si];
+    q.F[k] = Sx[(int64_t)(PF_F + k) * cap + si];
+  }
+  q.Jp = Sx[(int64_t)PF_JP * cap + si];
+  q.info = __float_as_uint(Sx[(int64_t)PF_INFO * cap + si]);
+  q.pid = Sx[(int64_t)PF_PID * cap + si];
+  q.actu = 0.f;
+  q.mdir[0] = 0.f, q.mdir[1] = 0.f, q.mdir[2] = 1.f;
+  if (P.nf > NF_BASE) {
+    q.actu = Sx[(int64_t)PF_ACTU * cap + si];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) q.mdir[d] = Sx[(int64_t)(PF_MDIR + d) * cap + si];
+  }
+}
+
+__device__ __forceinline__ void store_particle(const KParams& P, float* Dx, int64_t slot, const Particle& q) {
+  const int64_t cap = P.cap;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    Dx[(int64_t)(PF_POS + d) * cap + slot] = q.x[d];
+    Dx[(int64_t)(PF_VEL + d) * cap + slot] = q.v[d];
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    Dx[(int64_t)(PF_C + k) * cap + slot] = q.C[k];
+    Dx[(int64_t)(PF_F + k) * cap + slot] = q.F[k];
+  }
+  Dx[(int64_t)PF_JP * cap + slot] = q.Jp;
+  Dx[(int64_t)PF_INFO * cap + slot] = __uint_as_float(q.info);
+  Dx[(int64_t)PF_PID * cap + slot] = q.pid;
+  if (P.nf > NF_BASE) {
+    Dx[(int64_t)PF_ACTU * cap + slot] = q.actu;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) Dx[(int64_t)(PF_MDIR + d) * cap + slot] = q.mdir[d];
+  }
+}
+
+// Local cell (0..63) of a particle inside the block whose node origin is `org`, or 64.
+__device__ __forceinline__ int local_cell(const SceneDev& S, const float* x, const int* org, int* tb) {
+  bool inside = true;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float t = __fmul_rn(x[d], S.inv_dx);
+    const float f = floorf(__fsub_rn(t, 0.5f));
+    const int b = (f > -1e9f && f < 1e9f) ? (int)f : -1000000;
+    tb[d] = b - S.offset[d] - org[d];
+    inside = inside && tb[d] >= 0 && tb[d] < BLK;
+  }
+  return inside ? (tb[0] * BLK + tb[1]) * BLK + tb[2] : BLK_NODES;
+}
+
+__device__ __forceinline__ void block_origin(const SceneDev& S, int64_t key, int* org) {
+  const int64_t lb = key - S.block_base;
+  org[2] = (int)(lb % S.bres[2]) * BLK;
+  org[1] = (int)((lb / S.bres[2]) % S.bres[1]) * BLK;
+  org[0] = (int)(lb / ((int64_t)S.bres[2] * S.bres[1])) * BLK;
+}
+
+}  // namespace
+
+// Per work item (one grid block's bucket, up to `chunk` <= P2G_MAX_CHUNK particles):
+//  1. counting-sort the item's particles by cell in shared memory (native integer atomics);
+//  2. each particle, gathered from the old order through perm, runs compute_F_tmp + svd +
+//     material update + stress (mpm_solver.py:293-307, 339-377) and is written to its slot;
+//  3. its APIC mass/momentum (mpm_solver.py:379-418) goes to a warp-private 6^3 shared tile
+//     with plain float4 read-modify-writes: lanes of a warp take particles from different
+//     cells (transposed walk of the cell-sorted order), and lanes that still share a cell are
+//     serialised in __match_any rounds, so no two lanes update a node at the same time;
+//  4. the warp tiles are summed and flushed with one 16-byte vector reduction per node.
+__global__ void __launch_bounds__(P2G_MAX_THREADS) k_p2g(KParams P) {
+  __shared__ float4 s_tile[P2G_MAX_WARPS * TILE_NODES];
+  __shared__ int s_cnt[BLK_NODES + 1], s_off[BLK_NODES + 1];
+  __shared__ uint32_t s_cr[P2G_MAX_CHUNK];
+  __shared__ uint16_t s_order[P2G_MAX_CHUNK];
   __shared__ int s_touch[8];
   const int n_items = *P.n_items;
+  const int T = blockDim.x, nw = T >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t cap = P.cap;
   const float* Sx = P.src;
   float* Dx = P.dst;
+  float4* my_tile = s_tile + warp * TILE_NODES;
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
     const int4 item = P.items[it];
-    const bool real = item.x < P.K;
-    int32_t sid = 0;
-    int org[3] = {0, 0, 0};
-    if (real) {
-      sid = P.block_scene[item.x];
-      const SceneDev& S = P.scenes[sid];
-      const int64_t lb = (int64_t)item.x - S.block_base;
-      org[2] = (int)(lb % S.bres[2]) * BLK;
-      org[1] = (int)((lb / S.bres[2]) % S.bres[1]) * BLK;
-      org[0] = (int)(lb / ((int64_t)S.bres[2] * S.bres[1])) * BLK;
-      for (int t = threadIdx.x; t < TILE_NODES; t += blockDim.x) {
-        s_m[t] = 0.f;
-        s_px[t] = 0.f;
-        s_py[t] = 0.f;
-        s_pz[t] = 0.f;
+    const int cnt = item.z - item.y;
+    const bool frozen = item.x < P.K && P.steps && P.steps[P.block_scene[item.x]] == 0;
+    if (item.x >= P.K || frozen) {  // inactive bucket or frozen scene: carry over unchanged (uniform)
+      for (int j = threadIdx.x; j < cnt; j += T) {
+        const int64_t si = P.perm[item.y + j];
+        for (int k = 0; k < P.nf; ++k) Dx[(int64_t)k * cap + item.y + j] = Sx[(int64_t)k * cap + si];
       }
-      if (threadIdx.x < 8) s_touch[threadIdx.x] = 0;
+      continue;
+    }
+    const int32_t sid = P.block_scene[item.x];
+    const SceneDev& S = P.scenes[sid];
+    int org[3];
+    block_origin(S, item.x, org);
+    for (int t = threadIdx.x; t < nw * TILE_NODES; t += T) s_tile[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (threadIdx.x <= BLK_NODES) s_cnt[threadIdx.x] = 0;
+    if (threadIdx.x < 8) s_touch[threadIdx.x] = 0;
+    __syncthreads();
+    // 1. cell ranks
+    for (int j = threadIdx.x; j < cnt; j += T) {
+      const int64_t si = P.perm[item.y + j];
+      float x[3];
+      int tb[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) x[d] = Sx[(int64_t)(PF_POS + d) * cap + si];
+      const int cell = local_cell(S, x, org, tb);
+      const int r = atomicAdd(&s_cnt[cell], 1);
+      s_cr[j] = ((uint32_t)cell << 16) | (uint32_t)r;
     }
     __syncthreads();
-    for (int slot = item.y + threadIdx.x; slot < item.z; slot += blockDim.x) {
-      const int64_t si = P.perm[slot];
-      const uint32_t info = __float_as_uint(Sx[(int64_t)PF_INFO * cap + si]);
-      if (!real || !(info & INFO_ACTIVE)) {
-        for (int k = 0; k < P.nf; ++k) Dx[(int64_t)k * cap + slot] = Sx[(int64_t)k * cap + si];
-        continue;
-      }
-      const SceneDev& S = P.scenes[sid];
-      const MaterialDev& M = P.mats[info & INFO_MAT_MASK];
-      float x[3], v[3], C[9], F[9];
+    if (warp == 0) {  // exclusive scan of the 65 cell counts
+      const int a = s_cnt[lane], b = s_cnt[lane + 32];
+      int ia = a, ib = b;
 #pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        x[d] = Sx[(int64_t)(PF_POS + d) * cap + si];
-        v[d] = Sx[(int64_t)(PF_VEL + d) * cap + si];
-      }
-#pragma unroll
-      for (int k = 0; k < 9; ++k) {
-        C[k] = Sx[(int64_t)(PF_C + k) * cap + si];
-        F[k] = Sx[(int64_t)(PF_F + k) * cap + si];
-      }
-      const float Jp = Sx[(int64_t)PF_JP * cap + si];
-      const float pid = Sx[(int64_t)PF_PID * cap + si];
-      float actu = 0.f, mdir[3] = {0.f, 0.f, 1.f};
-      if (P.nf > NF_BASE) {
-        actu = Sx[(int64_t)PF_ACTU * cap + si];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) mdir[d] = Sx[(int64_t)(PF_MDIR + d) * cap + si];
-      }
-      // F_tmp = (I + dt C) F   (compute_F_tmp, mpm_solver.py:293-299)
-      float A[9], Ft[9];
-#pragma unroll
-      for (int k = 0; k < 9; ++k) A[k] = ((k % 4 == 0) ? 1.f : 0.f) + S.dt * C[k];
-      mat_mul(A, F, Ft);
-      // svd (mpm_solver.py:301-307)
-      float U[9], sig[3], V[9];
-      const float res = svd3<float, SVD_SWEEPS>(Ft, U, sig, V);
-      if (!(res <= SVD_FP64_TOL)) {
-        svd3_fp64(Ft, U, sig, V);
-        atomicAdd(P.fp64_count, 1ull);
-      }
-      // material update + stress (mpm_solver.py:339-375)
-      float Fn[9], Pk[9], Jpn;
-      material_update<float>(M, Ft, U, sig, V, Jp, actu, mdir, P.eps_norm, Fn, Jpn, Pk);
-      // write the particle to its sorted slot (frame f+1: F, Jp; pos/vel/C carried)
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        Dx[(int64_t)(PF_POS + d) * cap + slot] = x[d];
-        Dx[(int64_t)(PF_VEL + d) * cap + slot] = v[d];
-      }
-#pragma unroll
-      for (int k = 0; k < 9; ++k) {
-        Dx[(int64_t)(PF_C + k) * cap + slot] = C[k];
-        Dx[(int64_t)(PF_F + k) * cap + slot] = Fn[k];
-      }
-      Dx[(int64_t)PF_JP * cap + slot] = Jpn;
-      Dx[(int64_t)PF_INFO * cap + slot] = __uint_as_float(info);
-      Dx[(int64_t)PF_PID * cap + slot] = pid;
-      if (P.nf > NF_BASE) {
-        Dx[(int64_t)PF_ACTU * cap + slot] = actu;
-#pragma unroll
-        for (int d = 0; d < 3; ++d) Dx[(int64_t)(PF_MDIR + d) * cap + slot] = mdir[d];
-      }
-      // APIC scatter (mpm_solver.py:376-418)
-      const float mass = M.mass;
-      float aff[9];
-#pragma unroll
-      for (int k = 0; k < 9; ++k) aff[k] = S.stress_scale * Pk[k] + mass * C[k];
-      int tb[3];
-      float fx[3], w[3][3];
-      bool inside = true;
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const float t = __fmul_rn(x[d], S.inv_dx);
-        const int b = (int)floorf(__fsub_rn(t, 0.5f));
-        fx[d] = t - (float)b;
-        tb[d] = b - S.offset[d] - org[d];
-        inside = inside && tb[d] >= 0 && tb[d] < BLK;
-        bspline_w(fx[d], w[d]);
-      }
-      if (!inside) {  // cannot happen for a correctly keyed particle; never touch memory
-        atomicOr(P.status, 2u);
-        continue;
-      }
-      const float mv[3] = {mass * v[0], mass * v[1], mass * v[2]};
-      const bool is_free = (info & INFO_FREE) != 0;
-#pragma unroll
-      for (int ox = 0; ox < 3; ++ox)
-#pragma unroll
-        for (int oy = 0; oy < 3; ++oy)
-#pragma unroll
-          for (int oz = 0; oz < 3; ++oz) {
-            const float wt = w[0][ox] * w[1][oy] * w[2][oz];
-            const float dp[3] = {((float)ox - fx[0]) * S.dx, ((float)oy - fx[1]) * S.dx, ((float)oz - fx[2]) * S.dx};
-            const int idx = ((tb[0] + ox) * TILE + (tb[1] + oy)) * TILE + (tb[2] + oz);
-            atomicAdd(&s_m[idx], wt * mass);
-            atomicAdd(&s_px[idx], wt * (mv[0] + aff[0] * dp[0] + aff[1] * dp[1] + aff[2] * dp[2]));
-            atomicAdd(&s_py[idx], wt * (mv[1] + aff[3] * dp[0] + aff[4] * dp[1] + aff[5] * dp[2]));
-            atomicAdd(&s_pz[idx], wt * (mv[2] + aff[6] * dp[0] + aff[7] * dp[1] + aff[8] * dp[2]));
-          }
-      if (!is_free && P.pin) {  // non-free particle: its 27 nodes lose all momentum (mpm_solver.py:420-421)
-        for (int o = 0; o < 27; ++o) {
-          const int gx = tb[0] + org[0] + o / 9, gy = tb[1] + org[1] + (o / 3) % 3, gz = tb[2] + org[2] + o % 3;
-          const int64_t a = node_addr(S, gx, gy, gz);
-          atomicOr(&P.pin[a >> 5], 1u << (a & 31));
+      for (int o = 1; o < 32; o <<= 1) {
+        const int ta = __shfl_up_sync(0xffffffffu, ia, o), tbv = __shfl_up_sync(0xffffffffu, ib, o);
+        if (lane >= o) {
+          ia += ta;
+          ib += tbv;
         }
       }
+      const int tot_a = __shfl_sync(0xffffffffu, ia, 31);
+      s_off[lane] = ia - a;
+      s_off[lane + 32] = tot_a + ib - b;
+      if (lane == 31) s_off[BLK_NODES] = tot_a + ib;
     }
-    if (!real) continue;  // uniform across the CTA
     __syncthreads();
-    const SceneDev& S = P.scenes[sid];
-    for (int t = threadIdx.x; t < TILE_NODES; t += blockDim.x) {
-      const float m = s_m[t];
-      if (m == 0.f) continue;
+    for (int j = threadIdx.x; j < cnt; j += T) {
+      const uint32_t cr = s_cr[j];
+      s_order[s_off[cr >> 16] + (cr & 0xffffu)] = (uint16_t)j;
+    }
+    __syncthreads();
+    // 2-3. per particle: material + stress + scatter into the warp tile
+    const int stride = (cnt + 31) >> 5;
+    const int total = stride << 5;
+    for (int q = threadIdx.x; q < total; q += T) {
+      const int p = (q & 31) * stride + (q >> 5);
+      bool scat = false;
+      int cell = BLK_NODES, tb[3] = {0, 0, 0};
+      float fx[3] = {0.f, 0.f, 0.f}, w[3][3], aff[9], mv[3] = {0.f, 0.f, 0.f}, mass = 0.f;
+      if (p < cnt) {
+        const int j = s_order[p];
+        const int64_t slot = item.y + j;
+        const int64_t si = P.perm[slot];
+        Particle pt;
+        load_particle(P, Sx, si, pt);
+        if (pt.info & INFO_ACTIVE) {
+          const MaterialDev& M = P.mats[pt.info & INFO_MAT_MASK];
+          // F_tmp = (I + dt C) F   (compute_F_tmp, mpm_solver.py:293-299)
+          float A[9], Ft[9];
+#pragma unroll
+          for (int k = 0; k < 9; ++k) A[k] = ((k % 4 == 0) ? 1.f : 0.f) + S.dt * pt.C[k];
+          mat_mul(A, pt.F, Ft);
+          float U[9], sig[3], V[9];
+          const float res = svd3<float, SVD_SWEEPS>(Ft, U, sig, V);
+          if (!(res <= SVD_FP64_TOL)) {
+            svd3_fp64(Ft, U, sig, V);
+            atomicAdd(P.fp64_count, 1ull);
+          }
+          float Pk[9], Jpn;
+          material_update<float>(M, Ft, U, sig, V, pt.Jp, pt.actu, pt.mdir, P.eps_norm, pt.F, Jpn, Pk);
+          pt.Jp = Jpn;
+          mass = M.mass;
+#pragma unroll
+          for (int k = 0; k < 9; ++k) aff[k] = S.stress_scale * Pk[k] + mass * pt.C[k];
+#pragma unroll
+          for (int d = 0; d < 3; ++d) mv[d] = mass * pt.v[d];
+          cell = local_cell(S, pt.x, org, tb);
+          if (cell < BLK_NODES) {
+            scat = true;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+              const float t = __fmul_rn(pt.x[d], S.inv_dx);
+              fx[d] = t - (float)(tb[d] + S.offset[d] + org[d]);
+              bspline_w(fx[d], w[d]);
+            }
+            if (!(pt.info & INFO_FREE) && P.pin) {  // its 27 nodes lose all momentum (mpm_solver.py:420-421)
+              for (int o = 0; o < 27; ++o) {
+                const int64_t a = node_addr(S, org[0] + tb[0] + o / 9, org[1] + tb[1] + (o / 3) % 3, org[2] + tb[2] + o % 3);
+                atomicOr(&P.pin[a >> 5], 1u << (a & 31));
+              }
+            }
+          } else {
+            atomicOr(P.status, 2u);  // cannot happen for a correctly keyed particle; never touches memory
+          }
+        }
+        store_particle(P, Dx, slot, pt);
+      }
+      const unsigned am = __ballot_sync(0xffffffffu, scat);
+      if (am == 0u) continue;  // warp-uniform
+      unsigned my_round = 0;
+      if (scat) {
+        const unsigned peers = __match_any_sync(am, cell);
+        my_round = __popc(peers & ((1u << lane) - 1u));
+      }
+      const unsigned rounds = __reduce_max_sync(0xffffffffu, my_round) + 1u;
+      for (unsigned rd = 0; rd < rounds; ++rd) {
+        const bool mine = scat && my_round == rd;
+#pragma unroll
+        for (int ox = 0; ox < 3; ++ox)
+#pragma unroll
+          for (int oy = 0; oy < 3; ++oy)
+#pragma unroll
+            for (int oz = 0; oz < 3; ++oz) {
+              if (mine) {
+                const float wt = w[0][ox] * w[1][oy] * w[2][oz];
+                const float dp0 = ((float)ox - fx[0]) * S.dx, dp1 = ((float)oy - fx[1]) * S.dx,
+                            dp2 = ((float)oz - fx[2]) * S.dx;
+                const int idx = ((tb[0] + ox) * TILE + (tb[1] + oy)) * TILE + (tb[2] + oz);
+                float4 g = my_tile[idx];
+                g.x += wt * (mv[0] + aff[0] * dp0 + aff[1] * dp1 + aff[2] * dp2);
+                g.y += wt * (mv[1] + aff[3] * dp0 + aff[4] * dp1 + aff[5] * dp2);
+                g.z += wt * (mv[2] + aff[6] * dp0 + aff[7] * dp1 + aff[8] * dp2);
+                g.w += wt * mass;
+                my_tile[idx] = g;
+              }
+              __syncwarp();
+            }
+      }
+    }
+    __syncthreads();
+    // 4. flush
+    for (int t = threadIdx.x; t < TILE_NODES; t += T) {
+      float4 g = s_tile[t];
+      for (int ww = 1; ww < nw; ++ww) {
+        const float4 h = s_tile[ww * TILE_NODES + t];
+        g.x += h.x;
+        g.y += h.y;
+        g.z += h.z;
+        g.w += h.w;
+      }
+      if (g.w == 0.f) continue;
       const int tx = t / (TILE * TILE), ty = (t / TILE) % TILE, tz = t % TILE;
       const int gx = org[0] + tx, gy = org[1] + ty, gz = org[2] + tz;
       if (gx >= S.res[0] || gy >= S.res[1] || gz >= S.res[2]) continue;
-      atomicAdd(reinterpret_cast<float4*>(&P.grid[node_addr(S, gx, gy, gz)]), make_float4(s_px[t], s_py[t], s_pz[t], m));
+      atomicAdd(reinterpret_cast<float4*>(&P.grid[node_addr(S, gx, gy, gz)]), g);
       s_touch[(tx >> 2) * 4 + (ty >> 2) * 2 + (tz >> 2)] = 1;
     }
     __syncthreads();
@@ -584,6 +639,142 @@ __global__ void __launch_bounds__(256) k_p2g(KParams P) {
         if (atomicExch(&P.flags[blk], 1) == 0) P.list[atomicAdd(P.nlist, 1)] = (int32_t)blk;
       }
     }
+  }
+}
+
+// ------------------------------------------------------------------ G2P
+// mpm_solver.py:423-481 (g2p) with the particle boundary of boundaries.py:22-32, over the
+// same work items as the P2G that wrote the particles (so every item's particles read one
+// 6^3 node tile, staged once in shared memory), followed by the bucket key of the new
+// position and a warp-aggregated rank within the bucket.
+__device__ __forceinline__ void add_rank(const KParams& P, bool valid, int32_t key, int64_t i, int lane) {
+  const unsigned am = __ballot_sync(0xffffffffu, valid);
+  if (valid) {
+    const unsigned peers = __match_any_sync(am, key);
+    const int leader = __ffs(peers) - 1;
+    int r = 0;
+    if (lane == leader) r = atomicAdd(&P.count[key], __popc(peers));
+    r = __shfl_sync(peers, r, leader);
+    r += __popc(peers & ((1u << lane) - 1u));
+    P.key[i] = key;
+    P.rank[i] = r;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_g2p(KParams P) {
+  __shared__ float4 s_v[TILE_NODES];
+  if (blockIdx.x == 0 && threadIdx.x == 0) *P.nlist_other = 0;
+  const int n_items = *P.n_items;
+  const int T = blockDim.x, lane = threadIdx.x & 31;
+  const int64_t cap = P.cap;
+  float* D = P.dst;
+  const int32_t kInactive = (int32_t)P.K, kDead = (int32_t)P.K + 1;
+  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const int4 item = P.items[it];
+    const int cnt = item.z - item.y;
+    const int total = (cnt + 31) & ~31;
+    const bool frozen = item.x < P.K && P.steps && P.steps[P.block_scene[item.x]] == 0;
+    if (item.x >= P.K || frozen) {  // inactive bucket or frozen scene: keys only (uniform branch)
+      for (int q = threadIdx.x; q < total; q += T) {
+        const bool valid = q < cnt;
+        const int64_t i = item.y + q;
+        int32_t key = kInactive;
+        if (valid) {
+          const uint32_t info = ld_info(D, cap, i);
+          if (info & INFO_DEAD) key = kDead;
+          else if (info & INFO_ACTIVE) {
+            const SceneDev& Sc = P.scenes[scene_of(P, info)];
+            float x[3];
+            int b[3];
+            for (int d = 0; d < 3; ++d) x[d] = D[(int64_t)(PF_POS + d) * cap + i];
+            if (stencil_origin(Sc, x, b)) key = (int32_t)block_of(Sc, b[0], b[1], b[2]);
+          }
+        }
+        add_rank(P, valid, key, i, lane);
+      }
+      continue;
+    }
+    const SceneDev& S = P.scenes[P.block_scene[item.x]];
+    int org[3];
+    block_origin(S, item.x, org);
+    for (int t = threadIdx.x; t < TILE_NODES; t += T) {
+      const int gx = org[0] + t / (TILE * TILE), gy = org[1] + (t / TILE) % TILE, gz = org[2] + t % TILE;
+      float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (gx < S.res[0] && gy < S.res[1] && gz < S.res[2]) g = P.grid[node_addr(S, gx, gy, gz)];
+      s_v[t] = g;
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < total; q += T) {
+      const bool valid = q < cnt;
+      const int64_t i = item.y + q;
+      int32_t key = kInactive;
+      if (valid) {
+        float x[3];
+        int tb[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) x[d] = D[(int64_t)(PF_POS + d) * cap + i];
+        const int cell = local_cell(S, x, org, tb);
+        if (cell < BLK_NODES) {
+          float fx[3], w[3][3];
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            const float t = __fmul_rn(x[d], S.inv_dx);
+            fx[d] = t - (float)(tb[d] + S.offset[d] + org[d]);
+            bspline_w(fx[d], w[d]);
+          }
+          float v[3] = {0.f, 0.f, 0.f}, Cn[9];
+#pragma unroll
+          for (int k = 0; k < 9; ++k) Cn[k] = 0.f;
+#pragma unroll
+          for (int ox = 0; ox < 3; ++ox)
+#pragma unroll
+            for (int oy = 0; oy < 3; ++oy)
+#pragma unroll
+              for (int oz = 0; oz < 3; ++oz) {
+                const float4 g = s_v[((tb[0] + ox) * TILE + (tb[1] + oy)) * TILE + (tb[2] + oz)];
+                const float wt = w[0][ox] * w[1][oy] * w[2][oz];
+                const float dp[3] = {(float)ox - fx[0], (float)oy - fx[1], (float)oz - fx[2]};
+                const float gv[3] = {g.x, g.y, g.z};
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                  v[r] += wt * gv[r];
+                  const float s = 4.f * S.inv_dx * wt * gv[r];
+#pragma unroll
+                  for (int c = 0; c < 3; ++c) Cn[r * 3 + c] += s * dp[c];
+                }
+              }
+          float xn[3];
+          bool finite = true;
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            xn[d] = x[d] + S.dt * v[d];
+            finite = finite && isfinite(xn[d]) && isfinite(v[d]);
+          }
+          // CubeBoundary.impose_pos_vel (boundaries.py:22-32)
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            if (xn[d] >= S.hi[d] && v[d] >= 0.f) v[d] *= -S.restitution;
+            else if (xn[d] <= S.lo[d] && v[d] <= 0.f) v[d] *= -S.restitution;
+            xn[d] = fmaxf(fminf(xn[d], S.hi[d]), S.lo[d]);
+          }
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            D[(int64_t)(PF_POS + d) * cap + i] = xn[d];
+            D[(int64_t)(PF_VEL + d) * cap + i] = v[d];
+          }
+#pragma unroll
+          for (int k = 0; k < 9; ++k) D[(int64_t)(PF_C + k) * cap + i] = Cn[k];
+          int b[3];
+          if (!finite) atomicOr(P.status, 1u);
+          else if (stencil_origin(S, xn, b)) key = (int32_t)block_of(S, b[0], b[1], b[2]);
+          else atomicOr(P.status, 2u);
+        } else {
+          atomicOr(P.status, 2u);
+        }
+      }
+      add_rank(P, valid, key, i, lane);
+    }
+    __syncthreads();
   }
 }
 

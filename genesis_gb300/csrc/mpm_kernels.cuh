@@ -31,6 +31,9 @@ constexpr int TILE_NODES = TILE * TILE * TILE;  // 216
 constexpr int SCAN_TILE = 2048;              // buckets per scan CTA (256 threads x 8)
 constexpr int SCAN_THREADS = 256;
 constexpr int SVD_SWEEPS = 4;
+constexpr int P2G_MAX_THREADS = 256;         // P2G CTA size limit (warp-private tiles)
+constexpr int P2G_MAX_WARPS = P2G_MAX_THREADS / 32;
+constexpr int P2G_MAX_CHUNK = 2048;          // particles per P2G work item
 constexpr float SVD_FP64_TOL = 1e-5f;        // residual above which the SVD is redone in FP64
 
 enum : int {
@@ -92,6 +95,8 @@ struct KParams {
   int32_t* n_items;
   int2* partials;              // scan tile partials
   uint32_t* pin;               // per-node bitmap of nodes touched by non-free particles (or null)
+  int32_t* steps;              // per-scene substeps left (-1 unlimited, 0 frozen); null outside a substep
+  int32_t n_scenes;
   float eps_norm;              // gs.EPS for Matrix.norm(eps)
   uint32_t* status;
   unsigned long long* fp64_count;
@@ -124,13 +129,15 @@ __global__ void k_init_particles(KParams P, const int64_t* scene_pbegin, const i
                                  int64_t n_scenes);
 __global__ void k_add_particles(KParams P, int64_t s0, int64_t s1, int64_t start, int64_t n_add, int32_t mat_local,
                                 int32_t active, const float* pos);
+__global__ void k_admit(KParams P, int32_t s, int64_t n0, int64_t n_add, const float* pos, const int32_t* mat_local);
+__global__ void k_retire(KParams P, int32_t s);
 __global__ void k_get_state(KParams P, int64_t s0, int64_t s1, float* pos, float* vel, float* C, float* F,
                             float* Jp, uint8_t* active);
 __global__ void k_set_state(KParams P, int64_t s0, int64_t s1, const float* pos, const float* vel, const float* C,
                             const float* F, const float* Jp, const uint8_t* active);
 __global__ void k_particles_field(KParams P, int field, int write, int64_t s0, int64_t s1, int64_t start,
                                   int64_t n_sel, float* data);
-__global__ void k_g2p(KParams P);   // G2P + re-keying
+__global__ void k_g2p(KParams P);   // G2P + re-keying, over the P2G work items
 __global__ void k_keys(KParams P);  // re-keying only (after a state change)
 __global__ void k_scan_reduce(KParams P);
 __global__ void k_scan_partials(KParams P, int n_tiles);

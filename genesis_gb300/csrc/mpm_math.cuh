@@ -44,10 +44,17 @@ template <typename T> GB_HD T gmax(T a, T b) { return a > b ? a : b; }
 // sort of B = A V by norm, then Givens QR of B giving U and the singular values.
 // ------------------------------------------------------------------------------------
 
-// One Jacobi rotation zeroing the symmetric entry (p,q); r is the third index.
+template <typename T> struct Eps;
+template <> struct Eps<float> { static constexpr float v = 1.1920929e-7f; };
+template <> struct Eps<double> { static constexpr double v = 2.220446049250313e-16; };
+
+// One Jacobi rotation zeroing the symmetric entry (p,q); r is the third index.  An entry
+// already below the rounding level of its diagonal pair is left alone (the classical
+// Jacobi threshold): rotating it would swap exact degeneracies (F = I) for rounding noise
+// in U and V, which the corotated stress 2 mu (F - U V^T) F^T amplifies by mu.
 template <typename T>
 GB_HD void jacobi_rotate(T& app, T& aqq, T& apq, T& arp, T& arq, T* V, int p, int q) {
-  if (apq == T(0)) return;
+  if (!(gabs(apq) > Eps<T>::v * gsqrt(gabs(app * aqq)))) return;
   const T theta = (aqq - app) / (T(2) * apq);
   const T at = gabs(theta);
   T t = (at < T(1e18)) ? T(1) / (at + gsqrt(theta * theta + T(1))) : T(0.5) / at;

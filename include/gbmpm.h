@@ -201,6 +201,37 @@ int mpm_set_tuning(mpm_ctx* ctx, int32_t p2g_threads, int32_t particles_per_thre
 int mpm_set_profiling(mpm_ctx* ctx, int32_t enable);
 int mpm_kernel_times(mpm_ctx* ctx, double* ms_host /*[5]*/, int64_t* counts_host /*[5]*/, int32_t reset);
 
+/* ---------------------------------------------------------------- pool mode (serving)
+ * A context whose scene slots are configured and retired while it runs, for a request
+ * loop that keeps every live scene in one set of launches (continuous batching).  There is
+ * no reference counterpart: Genesis builds one fixed scene per process (scene.py:841-905).
+ * Slot s owns grid blocks [s*B, (s+1)*B) with B = ceil(max_grid_res/4)^3 and materials
+ * [s*M, (s+1)*M) with M = max_materials_per_scene; particles of all slots share one pool. */
+typedef struct mpm_pool_config {
+  int64_t max_scenes;
+  int64_t particle_capacity;
+  int32_t max_grid_res;            /* largest grid nodes per axis of any admitted scene */
+  int32_t max_materials_per_scene;
+  int32_t with_muscle;             /* allocate actuation fields */
+  int32_t reserved;
+} mpm_pool_config;
+int mpm_ctx_create_pool(const mpm_pool_config* cfg, int32_t device, mpm_ctx** out);
+
+/* Configure free slot `slot` as `scene` with its materials and append its n particles
+ * (device pos [n,3], per-particle material index among `materials` or NULL for 0).  The
+ * scene advances for n_substeps substeps (-1: unlimited) and then stays frozen (its
+ * particles are carried unchanged) until retired.  Synchronises `stream`. */
+int mpm_scene_admit(mpm_ctx* ctx, int64_t slot, const mpm_scene_config* scene, const mpm_material* materials,
+                    int32_t n_materials, int64_t n, const float* pos, const int32_t* mat_local,
+                    int32_t n_substeps, void* stream);
+
+/* Drop every particle of `slot` (they sort after all live particles and the next P2G does
+ * not carry them) and free the slot.  Read its state first with mpm_get_state(slot, slot+1). */
+int mpm_scene_retire(mpm_ctx* ctx, int64_t slot, void* stream);
+
+/* Substeps left per slot ([max_scenes] host ints; 0 = finished/frozen, -1 = unlimited). */
+int mpm_scene_steps_left(mpm_ctx* ctx, int32_t* out_host, void* stream);
+
 /* ABI version of this header (1). */
 int mpm_version(void);
 

@@ -116,3 +116,24 @@ def test_device_material_matches_oracle(shim, oracle, name, kw):
         assert np.allclose(Fn.reshape(3, 3), Fo, atol=2e-5 * max(1, np.abs(Fo).max())), (name, i)
         assert abs(jn[0] - jo) <= 2e-5 * max(1.0, abs(jo)), (name, i, jn[0], jo)
         assert np.abs(P.reshape(3, 3) - Po).max() <= 1e-5 * moduli * max(hard, 1.0) + 1e-4 * np.abs(Po).max(), (name, i)
+
+
+def test_corotated_stress_has_no_rounding_noise_near_identity(shim):
+    """F_tmp = I + tiny off-diagonals (as after a free-fall substep): the FP32 stress must be
+    of the order of 2 mu |E|, not 2 mu * eps_f32 (noise from degenerate Jacobi rotations)."""
+    import genesis_gb300 as gs
+
+    mat = gs.materials.MPM.Elastic(E=3e5, nu=0.2)
+    cm = mat.to_c(0)
+    rng = np.random.default_rng(5)
+    eps = float(np.finfo(np.float32).eps)
+    worst = 0.0
+    for _ in range(200):
+        E = rng.normal(scale=4e-11, size=(3, 3))
+        Ft = (np.eye(3) + E).astype(np.float32)
+        Fn, jn, P = np.zeros(9, np.float32), np.zeros(1, np.float32), np.zeros(9, np.float32)
+        md = np.array([0, 0, 1], np.float32)
+        shim.shim_material_f32(*_mat_args(cm), Ft.ctypes.data, 1.0, 0.0, md.ctypes.data, eps, Fn.ctypes.data,
+                               jn.ctypes.data, P.ctypes.data)
+        worst = max(worst, np.abs(P).max())
+    assert worst <= 2 * cm.mu * 1e-9, worst
