@@ -116,6 +116,8 @@ _SIGNATURES = {
     "mpm_scene_admit": (c_int32, [_P, c_int64, ctypes.c_void_p, ctypes.c_void_p, c_int32, c_int64, _P, _P, c_int32, _P]),
     "mpm_scene_retire": (c_int32, [_P, c_int64, _P]),
     "mpm_scene_steps_left": (c_int32, [_P, ctypes.POINTER(c_int32), _P]),
+    "mpm_substeps_noalloc": (c_int32, [_P, _P, c_int32, c_int64, _P, _P, _P, _P, _P, _P, _P, c_int32, _P]),
+    "mpm_noalloc_last_error": (ctypes.c_char_p, []),
 }
 
 _lib = None

@@ -333,6 +333,9 @@ int leave(mpm_ctx* ctx, void* stream) {
 }
 
 
+}  // namespace
+
+namespace gbmpm {
 // Scene constants exactly as MPMSolver.__init__ (mpm_solver.py:32-80); fills everything but
 // the block/material/particle bases.
 int derive_scene(const mpm_scene_config& c, SceneDev& S, std::string& err) {
@@ -401,6 +404,10 @@ MaterialDev derive_material(const mpm_material& m, const mpm_scene_config& c) {
   M.stiffness = (float)m.stiffness;
   return M;
 }
+
+}  // namespace gbmpm
+
+namespace {
 
 bool scene_range_ok(mpm_ctx* ctx, int64_t s0, int64_t s1) { return s0 >= 0 && s1 <= ctx->n_scenes && s0 < s1; }
 
