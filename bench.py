@@ -202,7 +202,10 @@ def run_ours(args, rank, world):
     lib = _lib.load()
     stream = torch.cuda.current_stream()
 
-    # warm-up (also captures the CUDA graph)
+    # launch-shape autotuning (P2G threads x particles per thread), then warm-up (captures the graph)
+    from genesis_gb300.autotune import autotune
+
+    tuning, tune_ms = autotune(solver.ctx, substeps=4, repeats=1, use_cache=False)
     for _ in range(args.warmup):
         scene.step()
     torch.cuda.synchronize()
@@ -328,6 +331,8 @@ def run_ours(args, rank, world):
             "parallelism": "replicas only" if world > 1 else "single GPU",
             "l2": "inputs larger than L2 (particle state double buffer 2 x 108 MB)",
             "path": "CUDA graph of 2 substeps",
+            "p2g_tuning": {"threads": tuning[0], "particles_per_thread": tuning[1],
+                           "ms_per_substep": {k: round(v, 4) for k, v in tune_ms.items()}},
         },
         "roofline": roofline,
         "kernels": per_kernel,
@@ -335,9 +340,127 @@ def run_ours(args, rank, world):
         "gpu_launches": 7 * SUBSTEPS_PER_STEP * args.steps,
         "clocks": clk,
     }
+    if rank == 0 and not args.skip_forms:
+        result["forms"] = run_forms()
+        result["forms"]["differentiation"] = run_diff()
     if rank == 0 and not args.skip_cpu:
         result["cpu_baseline"] = cpu_baseline()
     return result
+
+
+def _timed(fn):
+    import torch
+
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def run_forms(batched_substeps=200, n_requests=48):
+    """Batched (256 uneven scenes, one context) and served (continuous batching) forms, each
+    against the plain form run scene by scene (one context per scene) on the same workload."""
+    from genesis_gb300.batched import BatchedMPM, batched_workload
+    from genesis_gb300.serve import MPMServer, serving_workload
+
+    out = {}
+    specs = batched_workload(n_scenes=256, seed=1234)
+    b = BatchedMPM(specs, tune=True)
+    b.step(2)
+    t = _timed(lambda: b.step(batched_substeps))
+    st = b.check()
+    n_b = b.n_particles
+    tuning = b.tuning[0] if b.tuning else None
+    b.close()
+    t_plain = 0.0
+    for sp in specs:
+        one = BatchedMPM([sp], tune=False)
+        one.step(2)
+        t_plain += _timed(lambda: one.step(batched_substeps))
+        one.close()
+    out["batched"] = {
+        "workload": "256 scenes, 65^3 grids each, N ~ logU[2k,64k], Elastic/Liquid/Sand/Snow, extent U[0.1,0.3], "
+                    f"dt 2e-4, {batched_substeps} substeps",
+        "n_scenes": len(specs), "n_particles": n_b, "value": n_b * batched_substeps / t,
+        "plain_scene_by_scene": n_b * batched_substeps / t_plain, "speedup_vs_plain": t_plain / t,
+        "p2g_tuning": tuning, "status": st, "unit": "particle-substeps/s",
+    }
+    # served: the same request set (a) saturated (all arrive at once) for throughput, against each
+    # request run alone in turn; (b) Poisson arrivals at half the saturated rate for p50/p99 latency
+    reqs = serving_workload(n_requests=n_requests, rate_hz=0, seed=77)
+    work = sum(r.work for r in reqs)
+    srv = MPMServer(max_slots=64, particle_capacity=40_000_000, max_grid_res=129, chunk=10)
+    sat = srv.run(reqs, realtime=False)
+    t_alone = 0.0
+    for r in reqs:
+        one = BatchedMPM([r.spec], tune=False)
+        one.step(2)
+        t_alone += _timed(lambda: one.step(r.spec.substeps))
+        one.close()
+    mean_work = work / len(reqs)
+    rate = 0.5 * sat["throughput"] / mean_work
+    reqs2 = serving_workload(n_requests=n_requests, rate_hz=rate, seed=77)
+    live = srv.run(reqs2, realtime=True)
+    srv.close()
+    out["served"] = {
+        "workload": f"{n_requests} requests, N ~ logU[1k,500k], grid 33^3/65^3/129^3, substeps U[50,500], "
+                    "4 materials; continuous batching in one pool context",
+        "throughput_saturated": sat["throughput"], "plain_alone_sequential": work / t_alone,
+        "speedup_vs_plain": sat["throughput"] / (work / t_alone),
+        "poisson_rate_hz": rate, "throughput_poisson": live["throughput"],
+        "p50_latency_s": live["p50_s"], "p99_latency_s": live["p99_s"], "status": sat["status"] | live["status"],
+        "unit": "particle-substeps/s",
+    }
+    return out
+
+
+def run_diff(steps=64, substeps_per_step=10, ckpt_steps=16, seed=99):
+    """Differentiation config: ~216k-particle elastic cube (per-particle E ~ LogNormal(ln 3e5, 0.2)) on
+    a 97^3 grid, 64 steps x 10 substeps, checkpoint every 16 steps; loss = ||COM - target||^2;
+    gradients w.r.t. the initial velocity and every particle's E.  Reports forward+backward
+    particle-substeps/s (forward substeps counted once)."""
+    import torch
+
+    from genesis_gb300 import _lib
+    from genesis_gb300.diff import DifferentiableMPM
+
+    rng = np.random.default_rng(seed)
+    cfg = _lib.MpmSceneConfig()
+    cfg.substep_dt = 1e-4
+    for d in range(3):
+        cfg.gravity[d] = (0.0, 0.0, -9.81)[d]
+        cfg.lower_bound[d], cfg.upper_bound[d] = 0.0, 1.0
+    cfg.grid_density = 96.0
+    cfg.particle_size = 1.0 / 240
+    cfg.mass_eps = float(np.finfo(np.float32).eps)
+    side = 60
+    ax = 0.5 + (np.arange(side) - (side - 1) / 2) / 240.0
+    x0 = np.stack(np.meshgrid(ax, ax, ax, indexing="ij"), -1).reshape(-1, 3)
+    x0 = x0 + rng.uniform(-0.25 / 240, 0.25 / 240, size=x0.shape)
+    n = len(x0)
+    E = torch.tensor(3e5 * np.exp(0.2 * rng.normal(size=n)), dtype=torch.float32, device="cuda", requires_grad=True)
+    v0 = torch.tensor([0.1, 0.0, 0.0], device="cuda", requires_grad=True)
+    target = torch.tensor(rng.uniform(0.3, 0.7, size=3), dtype=torch.float32, device="cuda")
+    sim = DifferentiableMPM(cfg, nu=0.2, rho=1000.0, ckpt_every=ckpt_steps * substeps_per_step)
+    x = torch.tensor(x0, dtype=torch.float32, device="cuda")
+    n_sub = steps * substeps_per_step
+
+    def fwd_bwd():
+        loss = ((sim.rollout(x, v0, E, n_sub).mean(0) - target) ** 2).sum()
+        loss.backward()
+        return loss
+
+    sim.rollout(x, v0.detach(), E.detach(), 20)  # warm-up
+    t = _timed(fwd_bwd)
+    return {
+        "workload": f"elastic cube {n} particles, 97^3 grid, {steps} steps x {substeps_per_step} substeps, "
+                    f"checkpoint every {ckpt_steps} steps, grads w.r.t. v0 and per-particle E",
+        "n_particles": n, "seconds_fwd_bwd": t, "value": n * n_sub / t, "unit": "particle-substeps/s (fwd+bwd)",
+        "grad_v0": v0.grad.tolist(), "grad_E_norm": float(E.grad.norm()),
+    }
 
 
 def run_reference(args):
@@ -383,6 +506,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-forms", action="store_true", help="skip the batched/served form measurements")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -118,6 +118,8 @@ _SIGNATURES = {
     "mpm_scene_steps_left": (c_int32, [_P, ctypes.POINTER(c_int32), _P]),
     "mpm_substeps_noalloc": (c_int32, [_P, _P, c_int32, c_int64, _P, _P, _P, _P, _P, _P, _P, c_int32, _P]),
     "mpm_noalloc_last_error": (ctypes.c_char_p, []),
+    "mpm_diff_forward": (c_int32, [_P, c_double, c_int32, c_int64] + [_P] * 14),
+    "mpm_diff_backward": (c_int32, [_P, c_double, c_int32, c_int64] + [_P] * 22),
 }
 
 _lib = None

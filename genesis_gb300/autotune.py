@@ -19,7 +19,7 @@ import torch
 
 from . import _lib
 
-CANDIDATES = ((64, 1), (64, 2), (128, 1), (128, 2), (128, 4), (256, 1), (256, 2), (256, 4))
+CANDIDATES = ((64, 1), (64, 2), (128, 1), (128, 2), (128, 4), (256, 1), (256, 2), (256, 4))  # threads*ppt <= 1024
 CACHE_PATH = os.environ.get(
     "GBMPM_AUTOTUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "genesis_gb300", "autotune.json")
 )

@@ -20,7 +20,7 @@ INCLUDE = os.path.join(REPO_DIR, "include")
 LIB_PATH = os.path.join(PKG_DIR, "libgbmpm.so")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 
-SOURCES = ["mpm_kernels.cu", "mpm_capi.cu", "mpm_noalloc.cu"]
+SOURCES = ["mpm_kernels.cu", "mpm_capi.cu", "mpm_noalloc.cu", "mpm_grad.cu"]
 GENCODE = "arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [
     "-gencode",

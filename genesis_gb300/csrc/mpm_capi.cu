@@ -75,6 +75,7 @@ struct mpm_ctx {
   unsigned long long* d_tmp64 = nullptr;
   uint32_t* d_pin = nullptr;
   int32_t* d_steps = nullptr;
+  int64_t* d_n = nullptr;  // live particle count, read by k_perm inside captured substeps
   int64_t max_items = 0;
   int n_tiles = 0;
   std::vector<void*> allocs;
@@ -210,9 +211,13 @@ struct Timer {
 int launch_sort(mpm_ctx* ctx, const KParams& P, cudaStream_t s) {
   {
     Timer t(ctx, s, KT_SCAN);
-    k_scan_reduce<<<ctx->n_tiles, SCAN_THREADS, 0, s>>>(P);
-    k_scan_partials<<<1, SCAN_THREADS, 0, s>>>(P, ctx->n_tiles);
-    k_scan_apply<<<ctx->n_tiles, SCAN_THREADS, 0, s>>>(P);
+    if (ctx->K + 2 <= SCAN_SINGLE_MAX) {
+      k_scan_single<<<1, 1024, 0, s>>>(P);
+    } else {
+      k_scan_reduce<<<ctx->n_tiles, SCAN_THREADS, 0, s>>>(P);
+      k_scan_partials<<<1, SCAN_THREADS, 0, s>>>(P, ctx->n_tiles);
+      k_scan_apply<<<ctx->n_tiles, SCAN_THREADS, 0, s>>>(P);
+    }
   }
   CKL();
   if (P.n > 0 || P.steps) {
@@ -241,7 +246,7 @@ int launch_pre(mpm_ctx* ctx, int c, cudaStream_t s) {
   P.n = ctx->n;
   P.steps = ctx->d_steps;
   Timer t(ctx, s, KT_P2G);
-  k_p2g<<<ctx->p2g_blocks, ctx->p2g_threads, 0, s>>>(P);
+  k_p2g<<<ctx->p2g_blocks, ctx->p2g_threads, p2g_dyn_smem(ctx->p2g_threads, P.chunk), s>>>(P);
   CKL();
   return MPM_OK;
 }
@@ -257,6 +262,7 @@ int launch_grid(mpm_ctx* ctx, int c, cudaStream_t s) {
 int launch_post(mpm_ctx* ctx, int c, cudaStream_t s) {
   KParams P = make_params(ctx, c, 1 - c, c);
   P.n = ctx->n;
+  P.n_dev = ctx->d_n;
   P.steps = ctx->d_steps;
   {
     Timer t(ctx, s, KT_G2P);
@@ -275,7 +281,10 @@ int launch_substep(mpm_ctx* ctx, int c, cudaStream_t s) {
 
 int compute_launch_shapes(mpm_ctx* ctx) {
   int occ = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_p2g, ctx->p2g_threads, 0));
+  CK(cudaFuncSetAttribute(k_p2g, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)p2g_dyn_smem(P2G_MAX_THREADS, P2G_MAX_CHUNK)));
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_p2g, ctx->p2g_threads,
+                                                   p2g_dyn_smem(ctx->p2g_threads, ctx->p2g_threads * ctx->ppt)));
   ctx->p2g_blocks = ctx->n_sm * (occ > 0 ? occ : 1);
   int occ2 = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, k_g2p, 256, 0));
@@ -287,8 +296,8 @@ int compute_launch_shapes(mpm_ctx* ctx) {
   int64_t lim = (int64_t)ctx->n_sm * (occ3 > 0 ? occ3 : 1);
   ctx->keys_blocks = (int)(want < 1 ? 1 : (want < lim ? want : lim));
   ctx->grid_blocks = ctx->n_sm * 8;
-  int64_t io = (ext + 255) / 256;
-  ctx->io_blocks = (int)(io < 1 ? 1 : (io < ctx->n_sm * 16 ? io : ctx->n_sm * 16));
+  (void)ext;
+  ctx->io_blocks = ctx->n_sm * 16;  // grid-stride; independent of n so captured graphs stay valid
   return MPM_OK;
 }
 
@@ -458,6 +467,7 @@ static int ctx_alloc_init(mpm_ctx* ctx, int32_t device, const std::vector<int32_
     if ((r = dalloc(ctx, &ctx->d_fp64, 1))) break;
     if ((r = dalloc(ctx, &ctx->d_tmp64, 1))) break;
     if ((r = dalloc(ctx, &ctx->d_steps, ctx->n_scenes))) break;
+    if ((r = dalloc(ctx, &ctx->d_n, 1))) break;
   } while (0);
   if (r) {
     if (r != MPM_OK && ctx->err.size()) fail(nullptr, r, ctx->err);
@@ -497,6 +507,7 @@ static int ctx_alloc_init(mpm_ctx* ctx, int32_t device, const std::vector<int32_
   CKC(cudaMemsetAsync(ctx->d_status, 0, sizeof(uint32_t), ctx->cs));
   CKC(cudaMemsetAsync(ctx->d_fp64, 0, sizeof(unsigned long long), ctx->cs));
   CKC(cudaMemsetAsync(ctx->d_steps, 0xff, sizeof(int32_t) * ctx->n_scenes, ctx->cs));  // -1: unlimited
+  CKC(cudaMemcpyAsync(ctx->d_n, &ctx->n, sizeof(int64_t), cudaMemcpyHostToDevice, ctx->cs));
   if (compute_launch_shapes(ctx)) {
     fail(nullptr, MPM_ERR_CUDA, ctx->err);
     mpm_ctx_destroy(ctx);
@@ -846,7 +857,7 @@ int mpm_set_tuning(mpm_ctx* ctx, int32_t p2g_threads, int32_t particles_per_thre
   if (!ctx) return MPM_ERR_BAD_ARG;
   if (p2g_threads < 64 || p2g_threads > P2G_MAX_THREADS || p2g_threads % 32 || particles_per_thread < 1 ||
       p2g_threads * particles_per_thread > P2G_MAX_CHUNK)
-    return fail(ctx, MPM_ERR_BAD_ARG, "tuning out of range (threads 64..256 step 32, threads*ppt <= 2048)");
+    return fail(ctx, MPM_ERR_BAD_ARG, "tuning out of range (threads 64..256 step 32, threads*ppt <= 1024)");
   if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "tuning inside a substep");
   const bool changed = p2g_threads != ctx->p2g_threads || particles_per_thread != ctx->ppt;
   ctx->p2g_threads = p2g_threads;
@@ -1011,7 +1022,8 @@ int mpm_scene_admit(mpm_ctx* ctx, int64_t slot, const mpm_scene_config* scene, c
   ctx->slot_live[slot] = 1;
   ctx->mat_count_h[slot] = n_materials;
   ctx->sorted = false;
-  drop_graph(ctx);
+  CK(cudaMemcpyAsync(ctx->d_n, &ctx->n, sizeof(int64_t), cudaMemcpyHostToDevice, ctx->cs));
+  CK(cudaStreamSynchronize(ctx->cs));
   if ((r = compute_launch_shapes(ctx))) return r;
   return leave(ctx, stream);
 }
@@ -1034,7 +1046,8 @@ int mpm_scene_retire(mpm_ctx* ctx, int64_t slot, void* stream) {
   ctx->n -= ctx->slot_n[slot];
   ctx->slot_n[slot] = 0;
   ctx->slot_live[slot] = 0;
-  drop_graph(ctx);
+  CK(cudaMemcpyAsync(ctx->d_n, &ctx->n, sizeof(int64_t), cudaMemcpyHostToDevice, ctx->cs));
+  CK(cudaStreamSynchronize(ctx->cs));
   if ((r = compute_launch_shapes(ctx))) return r;
   return leave(ctx, stream);
 }

@@ -364,8 +364,63 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(KParams P) {
   }
 }
 
+// The whole scan in one CTA (1024 threads) when the bucket count is small: counts -> offsets,
+// work items and count reset, in three passes over the buckets with block-wide scans.
+__global__ void __launch_bounds__(1024) k_scan_single(KParams P) {
+  __shared__ int2 s_warp[32];
+  __shared__ int2 s_carry;
+  const int64_t nb = P.K + 2;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  if (threadIdx.x == 0) s_carry = make_int2(0, 0);
+  __syncthreads();
+  for (int64_t k0 = 0; k0 < nb; k0 += blockDim.x) {
+    const int64_t k = k0 + threadIdx.x;
+    const int c = k < nb ? P.count[k] : 0;
+    const int ic = (k <= P.K) ? items_of(c, P.chunk) : 0;
+    int a = c, b = ic;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int ta = __shfl_up_sync(0xffffffffu, a, o), tb = __shfl_up_sync(0xffffffffu, b, o);
+      if (lane >= o) {
+        a += ta;
+        b += tb;
+      }
+    }
+    if (lane == 31) s_warp[wid] = make_int2(a, b);
+    __syncthreads();
+    if (wid == 0) {
+      int2 v = lane < nwarp ? s_warp[lane] : make_int2(0, 0);
+      int x = v.x, y = v.y;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int tx = __shfl_up_sync(0xffffffffu, x, o), ty = __shfl_up_sync(0xffffffffu, y, o);
+        if (lane >= o) {
+          x += tx;
+          y += ty;
+        }
+      }
+      if (lane < nwarp) s_warp[lane] = make_int2(x - v.x, y - v.y);
+    }
+    __syncthreads();
+    const int2 base = s_carry;
+    const int2 wo = s_warp[wid];
+    const int off = base.x + wo.x + a - c, it0 = base.y + wo.y + b - ic;
+    if (k < nb) {
+      P.offset[k] = off;
+      for (int s = 0, j = 0; s < c && k <= P.K; s += P.chunk, ++j)
+        P.items[it0 + j] = make_int4((int)k, off + s, off + min(s + P.chunk, c), 0);
+      P.count[k] = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) s_carry = make_int2(off + c, it0 + ic);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *P.n_items = s_carry.y;
+}
+
 __global__ void k_perm(KParams P) {
-  for (int64_t i = grid_stride_begin(); i < P.n; i += grid_stride_step())
+  const int64_t n = P.n_dev ? *P.n_dev : P.n;
+  for (int64_t i = grid_stride_begin(); i < n; i += grid_stride_step())
     P.perm[P.offset[P.key[i]] + P.rank[i]] = (int32_t)i;
   if (P.steps && blockIdx.x == 0)  // end of a substep: count down per-scene substep budgets
     for (int s = threadIdx.x; s < P.n_scenes; s += blockDim.x)
@@ -452,21 +507,26 @@ __device__ __forceinline__ void block_origin(const SceneDev& S, int64_t key, int
 
 // Per work item (one grid block's bucket, up to `chunk` <= P2G_MAX_CHUNK particles):
 //  1. counting-sort the item's particles by cell in shared memory (native integer atomics);
-//  2. each particle, gathered from the old order through perm, runs compute_F_tmp + svd +
-//     material update + stress (mpm_solver.py:293-307, 339-377) and is written to its slot;
-//  3. its APIC mass/momentum (mpm_solver.py:379-418) goes to a warp-private 6^3 shared tile
-//     with plain float4 read-modify-writes: lanes of a warp take particles from different
-//     cells (transposed walk of the cell-sorted order), and lanes that still share a cell are
-//     serialised in __match_any rounds, so no two lanes update a node at the same time;
-//  4. the warp tiles are summed and flushed with one 16-byte vector reduction per node.
-__global__ void __launch_bounds__(P2G_MAX_THREADS) k_p2g(KParams P) {
-  __shared__ float4 s_tile[P2G_MAX_WARPS * TILE_NODES];
+//  2. in slot order (coalesced gathers through perm): compute_F_tmp + svd + material update
+//     + stress (mpm_solver.py:293-307, 339-377), write the particle to its slot, and leave its
+//     scatter parameters (fx, mass, q = m v - sum_k a_k fx_k, a_k = dx * affine[:,k]) in a
+//     shared record at its cell-sorted position;
+//  3. walk the cell-sorted records transposed (lanes of a warp take records `stride` apart, so
+//     different cells) and add the APIC mass/momentum w_o (q + sum_k o_k a_k), w_o m
+//     (mpm_solver.py:379-418) to a warp-private 6^3 shared tile with plain float4
+//     read-modify-writes; lanes that still share a cell are serialised in __match_any rounds;
+//  4. sum the warp tiles and flush with one 16-byte vector reduction per node.
+__global__ void __launch_bounds__(P2G_MAX_THREADS, 2) k_p2g(KParams P) {
+  extern __shared__ __align__(16) unsigned char p2g_smem[];
   __shared__ int s_cnt[BLK_NODES + 1], s_off[BLK_NODES + 1];
-  __shared__ uint32_t s_cr[P2G_MAX_CHUNK];
-  __shared__ uint16_t s_order[P2G_MAX_CHUNK];
   __shared__ int s_touch[8];
   const int n_items = *P.n_items;
   const int T = blockDim.x, nw = T >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int RS = p2g_record_stride(P.chunk);
+  float4* s_tile = reinterpret_cast<float4*>(p2g_smem);
+  float* s_rec = reinterpret_cast<float*>(s_tile + nw * TILE_NODES);
+  uint32_t* s_cr = reinterpret_cast<uint32_t*>(s_rec + 16 * RS);
+  uint8_t* s_cellp = reinterpret_cast<uint8_t*>(s_cr + P.chunk);
   const int64_t cap = P.cap;
   const float* Sx = P.src;
   float* Dx = P.dst;
@@ -519,66 +579,108 @@ __global__ void __launch_bounds__(P2G_MAX_THREADS) k_p2g(KParams P) {
       if (lane == 31) s_off[BLK_NODES] = tot_a + ib;
     }
     __syncthreads();
+    // 2. material + stress in slot order; scatter parameters to the sorted record
     for (int j = threadIdx.x; j < cnt; j += T) {
       const uint32_t cr = s_cr[j];
-      s_order[s_off[cr >> 16] + (cr & 0xffffu)] = (uint16_t)j;
-    }
-    __syncthreads();
-    // 2-3. per particle: material + stress + scatter into the warp tile
-    const int stride = (cnt + 31) >> 5;
-    const int total = stride << 5;
-    for (int q = threadIdx.x; q < total; q += T) {
-      const int p = (q & 31) * stride + (q >> 5);
-      bool scat = false;
-      int cell = BLK_NODES, tb[3] = {0, 0, 0};
-      float fx[3] = {0.f, 0.f, 0.f}, w[3][3], aff[9], mv[3] = {0.f, 0.f, 0.f}, mass = 0.f;
-      if (p < cnt) {
-        const int j = s_order[p];
-        const int64_t slot = item.y + j;
-        const int64_t si = P.perm[slot];
-        Particle pt;
-        load_particle(P, Sx, si, pt);
-        if (pt.info & INFO_ACTIVE) {
-          const MaterialDev& M = P.mats[pt.info & INFO_MAT_MASK];
-          // F_tmp = (I + dt C) F   (compute_F_tmp, mpm_solver.py:293-299)
-          float A[9], Ft[9];
+      const int cell = (int)(cr >> 16);
+      const int p = s_off[cell] + (int)(cr & 0xffffu);
+      const int64_t slot = item.y + j;
+      const int64_t si = P.perm[slot];
+      Particle pt;
+      load_particle(P, Sx, si, pt);
+      uint8_t cp = 255;
+      if (pt.info & INFO_ACTIVE) {
+        const MaterialDev& M = P.mats[pt.info & INFO_MAT_MASK];
+        // F_tmp = (I + dt C) F   (compute_F_tmp, mpm_solver.py:293-299)
+        float A[9], Ft[9];
 #pragma unroll
-          for (int k = 0; k < 9; ++k) A[k] = ((k % 4 == 0) ? 1.f : 0.f) + S.dt * pt.C[k];
-          mat_mul(A, pt.F, Ft);
+        for (int k = 0; k < 9; ++k) A[k] = ((k % 4 == 0) ? 1.f : 0.f) + S.dt * pt.C[k];
+        mat_mul(A, pt.F, Ft);
+        float Pk[9], Jpn = pt.Jp;
+        if (M.type == MT_LIQUID && M.mu == 0.f) {
+          // Non-viscous liquid (liquid.py:36-49 with mu = 0) uses only J = sigma0 sigma1 sigma2 of the
+          // SVD, which equals det F_tmp (det U = det V = 1): F_new = J^(1/3) I, stress = lam J (J-1) I.
+          const float J = Ft[0] * (Ft[4] * Ft[8] - Ft[5] * Ft[7]) - Ft[1] * (Ft[3] * Ft[8] - Ft[5] * Ft[6]) +
+                          Ft[2] * (Ft[3] * Ft[7] - Ft[4] * Ft[6]);
+          const float j3 = powf(J, 1.f / 3.f);
+          const float pr = M.lam * J * (J - 1.f);
+#pragma unroll
+          for (int k = 0; k < 9; ++k) {
+            pt.F[k] = (k % 4 == 0) ? j3 : 0.f;
+            Pk[k] = (k % 4 == 0) ? pr : 0.f;
+          }
+        } else {
           float U[9], sig[3], V[9];
           const float res = svd3<float, SVD_SWEEPS>(Ft, U, sig, V);
           if (!(res <= SVD_FP64_TOL)) {
             svd3_fp64(Ft, U, sig, V);
             atomicAdd(P.fp64_count, 1ull);
           }
-          float Pk[9], Jpn;
           material_update<float>(M, Ft, U, sig, V, pt.Jp, pt.actu, pt.mdir, P.eps_norm, pt.F, Jpn, Pk);
-          pt.Jp = Jpn;
-          mass = M.mass;
-#pragma unroll
-          for (int k = 0; k < 9; ++k) aff[k] = S.stress_scale * Pk[k] + mass * pt.C[k];
-#pragma unroll
-          for (int d = 0; d < 3; ++d) mv[d] = mass * pt.v[d];
-          cell = local_cell(S, pt.x, org, tb);
-          if (cell < BLK_NODES) {
-            scat = true;
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-              const float t = __fmul_rn(pt.x[d], S.inv_dx);
-              fx[d] = t - (float)(tb[d] + S.offset[d] + org[d]);
-              bspline_w(fx[d], w[d]);
-            }
-            if (!(pt.info & INFO_FREE) && P.pin) {  // its 27 nodes lose all momentum (mpm_solver.py:420-421)
-              for (int o = 0; o < 27; ++o) {
-                const int64_t a = node_addr(S, org[0] + tb[0] + o / 9, org[1] + tb[1] + (o / 3) % 3, org[2] + tb[2] + o % 3);
-                atomicOr(&P.pin[a >> 5], 1u << (a & 31));
-              }
-            }
-          } else {
-            atomicOr(P.status, 2u);  // cannot happen for a correctly keyed particle; never touches memory
-          }
         }
-        store_particle(P, Dx, slot, pt);
+        pt.Jp = Jpn;
+        if (cell < BLK_NODES) {
+          const int tb0 = cell >> 4, tb1 = (cell >> 2) & 3, tb2 = cell & 3;
+          const float mass = M.mass;
+          float fx[3];
+          const int tbv[3] = {tb0, tb1, tb2};
+#pragma unroll
+          for (int d = 0; d < 3; ++d) fx[d] = __fmul_rn(pt.x[d], S.inv_dx) - (float)(tbv[d] + S.offset[d] + org[d]);
+          float a[9];  // a[k*3 + r] = dx * affine[r][k]
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) a[k * 3 + r] = S.dx * (S.stress_scale * Pk[r * 3 + k] + mass * pt.C[r * 3 + k]);
+          float* rec = s_rec + p;
+          rec[0 * RS] = fx[0];
+          rec[1 * RS] = fx[1];
+          rec[2 * RS] = fx[2];
+          rec[3 * RS] = mass;
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+            rec[(4 + r) * RS] = mass * pt.v[r] - (a[r] * fx[0] + a[3 + r] * fx[1] + a[6 + r] * fx[2]);
+#pragma unroll
+          for (int k = 0; k < 9; ++k) rec[(7 + k) * RS] = a[k];
+          cp = (uint8_t)cell;
+          if (!(pt.info & INFO_FREE) && P.pin) {  // its 27 nodes lose all momentum (mpm_solver.py:420-421)
+            for (int o = 0; o < 27; ++o) {
+              const int64_t ad = node_addr(S, org[0] + tb0 + o / 9, org[1] + tb1 + (o / 3) % 3, org[2] + tb2 + o % 3);
+              atomicOr(&P.pin[ad >> 5], 1u << (ad & 31));
+            }
+          }
+        } else {
+          atomicOr(P.status, 2u);  // cannot happen for a correctly keyed particle; never touches memory
+        }
+      }
+      s_cellp[p] = cp;
+      store_particle(P, Dx, slot, pt);
+    }
+    __syncthreads();
+    // 3. transposed scatter into the warp tile
+    const int stride = ((cnt + 31) >> 5) | 1;
+    const int total = stride << 5;
+    for (int q = threadIdx.x; q < total; q += T) {
+      const int p = (q & 31) * stride + (q >> 5);
+      const int cell = p < cnt ? (int)s_cellp[p] : 255;
+      const bool scat = cell < BLK_NODES;
+      float w[3][3], mass = 0.f, qv[3] = {0.f, 0.f, 0.f}, a[9];
+      int tb[3] = {0, 0, 0};
+      if (scat) {
+        const float* rec = s_rec + p;
+        float fx[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          fx[d] = rec[d * RS];
+          bspline_w(fx[d], w[d]);
+        }
+        mass = rec[3 * RS];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) qv[r] = rec[(4 + r) * RS];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) a[k] = rec[(7 + k) * RS];
+        tb[0] = cell >> 4;
+        tb[1] = (cell >> 2) & 3;
+        tb[2] = cell & 3;
       }
       const unsigned am = __ballot_sync(0xffffffffu, scat);
       if (am == 0u) continue;  // warp-uniform
@@ -591,25 +693,28 @@ __global__ void __launch_bounds__(P2G_MAX_THREADS) k_p2g(KParams P) {
       for (unsigned rd = 0; rd < rounds; ++rd) {
         const bool mine = scat && my_round == rd;
 #pragma unroll
-        for (int ox = 0; ox < 3; ++ox)
+        for (int ox = 0; ox < 3; ++ox) {
+          const float t0x = qv[0] + (float)ox * a[0], t0y = qv[1] + (float)ox * a[1], t0z = qv[2] + (float)ox * a[2];
 #pragma unroll
-          for (int oy = 0; oy < 3; ++oy)
+          for (int oy = 0; oy < 3; ++oy) {
+            const float t1x = t0x + (float)oy * a[3], t1y = t0y + (float)oy * a[4], t1z = t0z + (float)oy * a[5];
+            const float w01 = w[0][ox] * w[1][oy];
 #pragma unroll
             for (int oz = 0; oz < 3; ++oz) {
               if (mine) {
-                const float wt = w[0][ox] * w[1][oy] * w[2][oz];
-                const float dp0 = ((float)ox - fx[0]) * S.dx, dp1 = ((float)oy - fx[1]) * S.dx,
-                            dp2 = ((float)oz - fx[2]) * S.dx;
+                const float wt = w01 * w[2][oz];
                 const int idx = ((tb[0] + ox) * TILE + (tb[1] + oy)) * TILE + (tb[2] + oz);
                 float4 g = my_tile[idx];
-                g.x += wt * (mv[0] + aff[0] * dp0 + aff[1] * dp1 + aff[2] * dp2);
-                g.y += wt * (mv[1] + aff[3] * dp0 + aff[4] * dp1 + aff[5] * dp2);
-                g.z += wt * (mv[2] + aff[6] * dp0 + aff[7] * dp1 + aff[8] * dp2);
+                g.x += wt * (t1x + (float)oz * a[6]);
+                g.y += wt * (t1y + (float)oz * a[7]);
+                g.z += wt * (t1z + (float)oz * a[8]);
                 g.w += wt * mass;
                 my_tile[idx] = g;
               }
               __syncwarp();
             }
+          }
+        }
       }
     }
     __syncthreads();
@@ -722,27 +827,45 @@ __global__ void __launch_bounds__(256) k_g2p(KParams P) {
             fx[d] = t - (float)(tb[d] + S.offset[d] + org[d]);
             bspline_w(fx[d], w[d]);
           }
-          float v[3] = {0.f, 0.f, 0.f}, Cn[9];
+          // v = sum w v_i;  C = 4 inv_dx sum w v_i (o - fx)^T = 4 inv_dx (M - v fx^T), M = sum w v_i o^T,
+          // accumulated along the separable stencil (z innermost)
+          float v[3] = {0.f, 0.f, 0.f}, M[9];
 #pragma unroll
-          for (int k = 0; k < 9; ++k) Cn[k] = 0.f;
+          for (int k = 0; k < 9; ++k) M[k] = 0.f;
 #pragma unroll
           for (int ox = 0; ox < 3; ++ox)
 #pragma unroll
-            for (int oy = 0; oy < 3; ++oy)
+            for (int oy = 0; oy < 3; ++oy) {
+              float a[3] = {0.f, 0.f, 0.f}, bz[3] = {0.f, 0.f, 0.f};
 #pragma unroll
               for (int oz = 0; oz < 3; ++oz) {
                 const float4 g = s_v[((tb[0] + ox) * TILE + (tb[1] + oy)) * TILE + (tb[2] + oz)];
-                const float wt = w[0][ox] * w[1][oy] * w[2][oz];
-                const float dp[3] = {(float)ox - fx[0], (float)oy - fx[1], (float)oz - fx[2]};
-                const float gv[3] = {g.x, g.y, g.z};
-#pragma unroll
-                for (int r = 0; r < 3; ++r) {
-                  v[r] += wt * gv[r];
-                  const float s = 4.f * S.inv_dx * wt * gv[r];
-#pragma unroll
-                  for (int c = 0; c < 3; ++c) Cn[r * 3 + c] += s * dp[c];
+                const float wz = w[2][oz];
+                a[0] += wz * g.x;
+                a[1] += wz * g.y;
+                a[2] += wz * g.z;
+                if (oz > 0) {
+                  const float wo = wz * (float)oz;
+                  bz[0] += wo * g.x;
+                  bz[1] += wo * g.y;
+                  bz[2] += wo * g.z;
                 }
               }
+              const float wxy = w[0][ox] * w[1][oy];
+#pragma unroll
+              for (int r = 0; r < 3; ++r) {
+                const float t = wxy * a[r];
+                v[r] += t;
+                M[r * 3 + 0] += (float)ox * t;
+                M[r * 3 + 1] += (float)oy * t;
+                M[r * 3 + 2] += wxy * bz[r];
+              }
+            }
+          float Cn[9];
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) Cn[r * 3 + c] = 4.f * S.inv_dx * (M[r * 3 + c] - v[r] * fx[c]);
           float xn[3];
           bool finite = true;
 #pragma unroll

@@ -30,10 +30,20 @@ constexpr int TILE = BLK + 2;                // P2G shared tile edge: block + st
 constexpr int TILE_NODES = TILE * TILE * TILE;  // 216
 constexpr int SCAN_TILE = 2048;              // buckets per scan CTA (256 threads x 8)
 constexpr int SCAN_THREADS = 256;
+constexpr int64_t SCAN_SINGLE_MAX = 4096;     // bucket count up to which one CTA scans
 constexpr int SVD_SWEEPS = 4;
 constexpr int P2G_MAX_THREADS = 256;         // P2G CTA size limit (warp-private tiles)
 constexpr int P2G_MAX_WARPS = P2G_MAX_THREADS / 32;
-constexpr int P2G_MAX_CHUNK = 2048;          // particles per P2G work item
+constexpr int P2G_MAX_CHUNK = 1024;          // particles per P2G work item
+
+// Shared-memory layout of k_p2g (dynamic part): warp tiles, then 16 SoA record planes of
+// `stride` floats (a multiple of 32 holding 32 * odd rows, so transposed reads hit distinct
+// banks), then the item's (cell, rank) words, then one cell byte per sorted position.
+__host__ __device__ __forceinline__ int p2g_record_stride(int chunk) { return 32 * (((chunk + 31) / 32) | 1); }
+__host__ __device__ __forceinline__ size_t p2g_dyn_smem(int threads, int chunk) {
+  const int rs = p2g_record_stride(chunk);
+  return (size_t)(threads / 32) * TILE_NODES * 16 + (size_t)16 * rs * 4 + (size_t)chunk * 4 + (size_t)rs;
+}
 constexpr float SVD_FP64_TOL = 1e-5f;        // residual above which the SVD is redone in FP64
 
 enum : int {
@@ -76,7 +86,8 @@ struct KParams {
   int64_t cap;
   int32_t nf;
   int32_t chunk;               // particles per P2G work item
-  int64_t n;                   // particles in use
+  int64_t n;                   // particles in use (flat kernels outside a substep)
+  const int64_t* n_dev;        // particles in use, read on the device by k_perm inside a substep
   int64_t K;                   // grid blocks (real buckets)
   float4* grid;                // grid buffer of this substep
   float4* grid_other;          // the other grid buffer (cleared by the grid op)
@@ -142,6 +153,7 @@ __global__ void k_keys(KParams P);  // re-keying only (after a state change)
 __global__ void k_scan_reduce(KParams P);
 __global__ void k_scan_partials(KParams P, int n_tiles);
 __global__ void k_scan_apply(KParams P);
+__global__ void k_scan_single(KParams P);
 __global__ void k_perm(KParams P);
 __global__ void k_p2g(KParams P);
 __global__ void k_grid_op(KParams P);

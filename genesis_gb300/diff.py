@@ -1,0 +1,137 @@
+"""Differentiation form: MPM rollouts with hand-written adjoints behind torch.autograd.
+
+`DifferentiableMPM.rollout(x0, v0, E)` runs `n_substeps` substeps of one Elastic scene with
+per-particle Young's modulus E (Lame parameters from E and nu as in base.py:77-83) and returns
+the final particle positions; its backward runs the adjoint substeps of libgbmpm
+(mpm_diff_backward) in reverse.  Memory follows checkpoint-and-recompute like Genesis's
+differentiable mode (simulator.py:372-404): the forward keeps the particle state only every
+`ckpt_every` substeps; the backward re-simulates each segment from its checkpoint, keeping
+that segment's states, and then walks it backwards.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .exceptions import GenesisException
+
+
+def lame(E: torch.Tensor, nu: float):
+    mu = E / (2.0 * (1.0 + nu))
+    lam = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu))
+    return mu, lam
+
+
+class DifferentiableMPM:
+    def __init__(self, scene_cfg: "_lib.MpmSceneConfig", nu: float = 0.2, rho: float = 1000.0,
+                 neohookean: bool = False, ckpt_every: int = 160):
+        self.lib = _lib.load()
+        self.cfg = scene_cfg
+        self.nu = float(nu)
+        self.rho = float(rho)
+        self.neo = int(bool(neohookean))
+        self.ckpt_every = int(ckpt_every)
+        d = scene_cfg.grid_density
+        res = [int(round(d * scene_cfg.upper_bound[k]) - round(d * scene_cfg.lower_bound[k]) + 1) for k in range(3)]
+        self.nodes = res[0] * res[1] * res[2]
+        dev = "cuda"
+        self.grid_pm = torch.zeros((self.nodes, 4), device=dev)
+        self.grid_v = torch.zeros((self.nodes, 4), device=dev)
+        self.g_grid_v = torch.zeros((self.nodes, 4), device=dev)
+        self.g_grid_pm = torch.zeros((self.nodes, 4), device=dev)
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+
+    @staticmethod
+    def _s():
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def forward_substep(self, st, mu, lam):
+        """(x, v, C, F) -> next state (new tensors)."""
+        x, v, C, F = st
+        n = x.shape[0]
+        out = (torch.empty_like(x), torch.empty_like(v), torch.empty_like(C), torch.empty_like(F))
+        r = self.lib.mpm_diff_forward(ctypes.byref(self.cfg), self.rho, self.neo, n, x.data_ptr(), v.data_ptr(),
+                                      C.data_ptr(), F.data_ptr(), mu.data_ptr(), lam.data_ptr(), out[0].data_ptr(),
+                                      out[1].data_ptr(), out[2].data_ptr(), out[3].data_ptr(),
+                                      self.grid_pm.data_ptr(), self.grid_v.data_ptr(), self.status.data_ptr(),
+                                      self._s())
+        _lib.check(r, None, "mpm_diff_forward")
+        return out
+
+    def backward_substep(self, st, mu, lam, g_out, gmu, glam):
+        """Adjoint of forward_substep at state `st` given dL/d(next state); returns dL/d(state)."""
+        x, v, C, F = st
+        n = x.shape[0]
+        self.forward_substep(st, mu, lam)  # rebuild this substep's grid
+        gx1, gv1, gC1, gF1 = g_out
+        gin = (torch.empty_like(x), torch.empty_like(v), torch.empty_like(C), torch.empty_like(F))
+        r = self.lib.mpm_diff_backward(ctypes.byref(self.cfg), self.rho, self.neo, n, x.data_ptr(), v.data_ptr(),
+                                       C.data_ptr(), F.data_ptr(), mu.data_ptr(), lam.data_ptr(), gx1.data_ptr(),
+                                       gv1.data_ptr(), gC1.data_ptr(), gF1.data_ptr(), gin[0].data_ptr(),
+                                       gin[1].data_ptr(), gin[2].data_ptr(), gin[3].data_ptr(), gmu.data_ptr(),
+                                       glam.data_ptr(), self.grid_pm.data_ptr(), self.grid_v.data_ptr(),
+                                       self.g_grid_v.data_ptr(), self.g_grid_pm.data_ptr(), self.status.data_ptr(),
+                                       self._s())
+        _lib.check(r, None, "mpm_diff_backward")
+        return gin
+
+    def check(self):
+        st = int(self.status.item())
+        if st & _lib.STATUS_NAN:
+            raise GenesisException("NaN detected in MPM states.")
+        if st & _lib.STATUS_OOB:
+            raise GenesisException("MPM particles left the simulation grid (stencil out of bounds).")
+
+    def rollout(self, x0: torch.Tensor, v0: torch.Tensor, E: torch.Tensor, n_substeps: int) -> torch.Tensor:
+        """Final positions after n_substeps from positions x0 [n,3], velocities v0 ([3] or [n,3]) and
+        per-particle Young's modulus E [n]; differentiable w.r.t. x0, v0 and E."""
+        n = x0.shape[0]
+        v0 = v0.expand(n, 3) if v0.dim() == 1 else v0
+        mu, lam = lame(E, self.nu)
+        return _Rollout.apply(self, int(n_substeps), x0, v0, mu, lam)
+
+
+class _Rollout(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, sim: DifferentiableMPM, n_substeps, x0, v0, mu, lam):
+        n = x0.shape[0]
+        x = x0.detach().float().contiguous()
+        v = v0.detach().float().contiguous()
+        C = torch.zeros((n, 3, 3), device=x.device)
+        F = torch.eye(3, device=x.device).repeat(n, 1, 1).contiguous()
+        mu_d, lam_d = mu.detach().float().contiguous(), lam.detach().float().contiguous()
+        st = (x, v, C, F)
+        ckpts = {}
+        for s in range(n_substeps):
+            if s % sim.ckpt_every == 0:
+                ckpts[s] = tuple(t.clone() for t in st)
+            st = sim.forward_substep(st, mu_d, lam_d)
+        sim.check()
+        ctx.sim, ctx.n_substeps, ctx.ckpts = sim, n_substeps, ckpts
+        ctx.save_for_backward(mu_d, lam_d)
+        return st[0]
+
+    @staticmethod
+    def backward(ctx, g_x):
+        sim, n_sub = ctx.sim, ctx.n_substeps
+        mu, lam = ctx.saved_tensors
+        n = g_x.shape[0]
+        g = (g_x.contiguous().float(), torch.zeros((n, 3), device=g_x.device),
+             torch.zeros((n, 3, 3), device=g_x.device), torch.zeros((n, 3, 3), device=g_x.device))
+        gmu = torch.zeros_like(mu)
+        glam = torch.zeros_like(lam)
+        starts = sorted(ctx.ckpts)
+        for seg_i in range(len(starts) - 1, -1, -1):
+            s0 = starts[seg_i]
+            s1 = starts[seg_i + 1] if seg_i + 1 < len(starts) else n_sub
+            states = [ctx.ckpts[s0]]
+            for _ in range(s0, s1 - 1):  # re-simulate the segment (checkpoint-and-recompute)
+                states.append(sim.forward_substep(states[-1], mu, lam))
+            for st in reversed(states):
+                g = sim.backward_substep(st, mu, lam, g, gmu, glam)
+        sim.check()
+        return None, None, g[0], g[1], gmu, glam

@@ -76,7 +76,7 @@ def serving_workload(n_requests=64, rate_hz=200.0, seed=7, n_range=(1000, 500000
 
 
 class MPMServer:
-    def __init__(self, max_slots=64, particle_capacity=None, max_grid_res=129, mem_fraction=0.8, chunk=10,
+    def __init__(self, max_slots=64, particle_capacity=None, max_grid_res=129, mem_fraction=0.8, chunk=20,
                  device=None):
         self.lib = _lib.load()
         dev = torch.cuda.current_device() if device is None else device

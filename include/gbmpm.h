@@ -249,6 +249,27 @@ int mpm_substeps_noalloc(const mpm_scene_config* scene, const mpm_material* mate
                          const int32_t* mat, const uint8_t* active, int32_t n_substeps, void* stream);
 const char* mpm_noalloc_last_error(void);
 
+/* ---------------------------------------------------------------- differentiation
+ * One differentiable substep of one Elastic scene (corotated, or neo-Hookean when
+ * neohookean != 0) with per-particle Lame parameters mu[n], lam[n], and its adjoint.
+ * Replace the reference's Quadrants autodiff of the substep (p2g.grad, mpm_grid_op.grad,
+ * g2p.grad, compute_F_tmp.grad: mpm_solver.py:517-554, legacy_coupler.py:998-1019) and its SVD
+ * backward (mpm_solver.py:1229-1252).  Particle arrays use the reference layout; grid_pm,
+ * grid_v, g_grid_v, g_grid_pm are caller buffers of res^3 float4 (res = the scene's grid);
+ * status is a device uint32 (MPM_STATUS_* bits, or-ed).  mpm_diff_backward needs the grid of
+ * the same substep in grid_pm/grid_v (run mpm_diff_forward on the same state first); it
+ * writes dL/d(x, v, C, F) and adds into dL/d(mu, lam).  gF1 may be NULL. */
+int mpm_diff_forward(const mpm_scene_config* scene, double rho, int32_t neohookean, int64_t n,
+                     const float* x, const float* v, const float* C, const float* F,
+                     const float* mu, const float* lam, float* x1, float* v1, float* C1, float* F1,
+                     void* grid_pm, void* grid_v, uint32_t* status, void* stream);
+int mpm_diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean, int64_t n,
+                      const float* x, const float* v, const float* C, const float* F,
+                      const float* mu, const float* lam, const float* gx1, const float* gv1,
+                      const float* gC1, const float* gF1, float* gx, float* gv, float* gC, float* gF,
+                      float* gmu, float* glam, void* grid_pm, void* grid_v, void* g_grid_v,
+                      void* g_grid_pm, uint32_t* status, void* stream);
+
 /* ABI version of this header (1). */
 int mpm_version(void);
 
