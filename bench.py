@@ -175,6 +175,18 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
+def reduce_over_ranks(ms: float, units: float, device) -> tuple[float, float]:
+    """Replicas: job time = max over ranks, work = sum over ranks (no collective on the data path)."""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    u = torch.tensor([units], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return t.item(), u.item()
+
+
 def load_traffic(kernel):
     p = os.path.join(ROOT, "profiles", f"{kernel}_traffic.json")
     if os.path.exists(p):
@@ -226,11 +238,9 @@ def run_ours(args, rank, world):
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
     solver.check_state()
+    total_units = n * SUBSTEPS_PER_STEP * args.steps
     if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = t.item()
-    total_units = n * SUBSTEPS_PER_STEP * args.steps * world
+        ms, total_units = reduce_over_ranks(ms, total_units, "cuda")
     value = total_units / (ms / 1e3)
 
     # --- per-kernel durations over a second timed region of the same K steps (events per kernel)
@@ -331,7 +341,7 @@ def run_ours(args, rank, world):
             "parallelism": "replicas only" if world > 1 else "single GPU",
             "l2": "inputs larger than L2 (particle state double buffer 2 x 108 MB)",
             "path": "CUDA graph of 2 substeps",
-            "p2g_tuning": {"threads": tuning[0], "particles_per_thread": tuning[1],
+            "p2g_tuning": {"threads": tuning[0], "particles_per_thread": tuning[1], "g2p_threads": tuning[2],
                            "ms_per_substep": {k: round(v, 4) for k, v in tune_ms.items()}},
         },
         "roofline": roofline,
@@ -439,10 +449,11 @@ def run_diff(steps=64, substeps_per_step=10, ckpt_steps=16, seed=99):
     side = 60
     ax = 0.5 + (np.arange(side) - (side - 1) / 2) / 240.0
     x0 = np.stack(np.meshgrid(ax, ax, ax, indexing="ij"), -1).reshape(-1, 3)
+    x0[:, 2] += 0.18 - 0.5  # 2 cm above the floor boundary: the fall ends in contact, so E shapes the COM
     x0 = x0 + rng.uniform(-0.25 / 240, 0.25 / 240, size=x0.shape)
     n = len(x0)
     E = torch.tensor(3e5 * np.exp(0.2 * rng.normal(size=n)), dtype=torch.float32, device="cuda", requires_grad=True)
-    v0 = torch.tensor([0.1, 0.0, 0.0], device="cuda", requires_grad=True)
+    v0 = torch.tensor([0.1, 0.0, -1.0], device="cuda", requires_grad=True)
     target = torch.tensor(rng.uniform(0.3, 0.7, size=3), dtype=torch.float32, device="cuda")
     sim = DifferentiableMPM(cfg, nu=0.2, rho=1000.0, ckpt_every=ckpt_steps * substeps_per_step)
     x = torch.tensor(x0, dtype=torch.float32, device="cuda")

@@ -106,7 +106,7 @@ _SIGNATURES = {
     "mpm_get_grid": (c_int32, [_P, c_int64, _P, _P]),
     "mpm_count_touched_nodes": (c_int32, [_P, ctypes.POINTER(c_int64), _P]),
     "mpm_status_word": (c_int32, [_P, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(c_int64), c_int32, _P]),
-    "mpm_set_tuning": (c_int32, [_P, c_int32, c_int32, c_int32]),
+    "mpm_set_tuning": (c_int32, [_P, c_int32, c_int32, c_int32, c_int32]),
     "mpm_get_info": (c_int32, [_P, ctypes.POINTER(c_int64), ctypes.POINTER(c_int64), ctypes.POINTER(c_int64)]),
     "mpm_scene_grid_res": (c_int32, [_P, c_int64, ctypes.POINTER(c_int32)]),
     "mpm_set_profiling": (c_int32, [_P, c_int32]),

@@ -1,4 +1,4 @@
-"""Autotuner of the P2G launch shape (threads per CTA x particles per thread).
+"""Autotuner of the launch shapes (P2G threads per CTA x particles per thread, G2P threads).
 
 The work chunk of one P2G CTA is threads * particles_per_thread particles of one grid
 block's bucket.  Larger chunks amortise the shared-tile clear/flush over more particles;
@@ -19,7 +19,9 @@ import torch
 
 from . import _lib
 
-CANDIDATES = ((64, 1), (64, 2), (128, 1), (128, 2), (128, 4), (256, 1), (256, 2), (256, 4))  # threads*ppt <= 1024
+# (P2G threads, particles per thread, G2P threads); P2G threads * ppt <= 1024
+CANDIDATES = ((64, 2, 128), (128, 1, 128), (128, 2, 128), (128, 4, 128), (256, 1, 128), (256, 2, 128),
+              (256, 4, 128), (128, 2, 64), (128, 2, 256))
 CACHE_PATH = os.environ.get(
     "GBMPM_AUTOTUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "genesis_gb300", "autotune.json")
 )
@@ -58,15 +60,15 @@ def autotune(ctx, substeps: int = 10, repeats: int = 2, use_cache: bool = True, 
     lib = _lib.load()
     sig = signature(ctx)
     cache = _load_cache() if use_cache else {}
-    if sig in cache:
-        t, p = cache[sig]["choice"]
-        _lib.check(lib.mpm_set_tuning(ctx, t, p, 1), ctx, "mpm_set_tuning")
-        return (t, p), cache[sig].get("timings", {})
+    if sig in cache and len(cache[sig]["choice"]) == 3:
+        t, p, g = cache[sig]["choice"]
+        _lib.check(lib.mpm_set_tuning(ctx, t, p, 1, g), ctx, "mpm_set_tuning")
+        return (t, p, g), cache[sig].get("timings", {})
     stream = torch.cuda.current_stream()
     h = ctypes.c_void_p(stream.cuda_stream)
     timings = {}
-    for t, p in candidates:
-        _lib.check(lib.mpm_set_tuning(ctx, t, p, 1), ctx, "mpm_set_tuning")
+    for t, p, g in candidates:
+        _lib.check(lib.mpm_set_tuning(ctx, t, p, 1, g), ctx, "mpm_set_tuning")
         _lib.check(lib.mpm_substeps(ctx, 2, h), ctx, "mpm_substeps")  # warm-up + graph capture
         best = float("inf")
         for _ in range(repeats):
@@ -76,9 +78,9 @@ def autotune(ctx, substeps: int = 10, repeats: int = 2, use_cache: bool = True, 
             e1.record(stream)
             e1.synchronize()
             best = min(best, e0.elapsed_time(e1) / substeps)
-        timings[f"{t}x{p}"] = best
-    choice = min(candidates, key=lambda c: timings[f"{c[0]}x{c[1]}"])
-    _lib.check(lib.mpm_set_tuning(ctx, choice[0], choice[1], 1), ctx, "mpm_set_tuning")
+        timings[f"{t}x{p}/{g}"] = best
+    choice = min(candidates, key=lambda c: timings[f"{c[0]}x{c[1]}/{c[2]}"])
+    _lib.check(lib.mpm_set_tuning(ctx, choice[0], choice[1], 1, choice[2]), ctx, "mpm_set_tuning")
     cache[sig] = {"choice": list(choice), "timings": timings}
     if use_cache:
         _save_cache(cache)

@@ -86,7 +86,7 @@ struct mpm_ctx {
   int phase = 0;        // 0 ready, 1 after P2G, 2 after grid op
 
   // tuning / launch
-  int p2g_threads = 256, ppt = 2;
+  int p2g_threads = 256, ppt = 2, g2p_threads = 128;
   bool use_graph = true;
   int p2g_blocks = 0, g2p_blocks = 0, keys_blocks = 0, grid_blocks = 0, io_blocks = 0;
 
@@ -266,7 +266,7 @@ int launch_post(mpm_ctx* ctx, int c, cudaStream_t s) {
   P.steps = ctx->d_steps;
   {
     Timer t(ctx, s, KT_G2P);
-    k_g2p<<<ctx->g2p_blocks, 256, 0, s>>>(P);
+    k_g2p<<<ctx->g2p_blocks, ctx->g2p_threads, 0, s>>>(P);
   }
   CKL();
   return launch_sort(ctx, P, s);
@@ -287,7 +287,7 @@ int compute_launch_shapes(mpm_ctx* ctx) {
                                                    p2g_dyn_smem(ctx->p2g_threads, ctx->p2g_threads * ctx->ppt)));
   ctx->p2g_blocks = ctx->n_sm * (occ > 0 ? occ : 1);
   int occ2 = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, k_g2p, 256, 0));
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, k_g2p, ctx->g2p_threads, 0));
   ctx->g2p_blocks = ctx->n_sm * (occ2 > 0 ? occ2 : 1);  // persistent over the work items
   int occ3 = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ3, k_keys, 256, 0));
@@ -853,13 +853,18 @@ int mpm_status_word(mpm_ctx* ctx, uint32_t* status_host, int64_t* fp64_svd_host,
   return leave(ctx, stream);
 }
 
-int mpm_set_tuning(mpm_ctx* ctx, int32_t p2g_threads, int32_t particles_per_thread, int32_t use_graph) {
+int mpm_set_tuning(mpm_ctx* ctx, int32_t p2g_threads, int32_t particles_per_thread, int32_t use_graph,
+                   int32_t g2p_threads) {
   if (!ctx) return MPM_ERR_BAD_ARG;
   if (p2g_threads < 64 || p2g_threads > P2G_MAX_THREADS || p2g_threads % 32 || particles_per_thread < 1 ||
       p2g_threads * particles_per_thread > P2G_MAX_CHUNK)
     return fail(ctx, MPM_ERR_BAD_ARG, "tuning out of range (threads 64..256 step 32, threads*ppt <= 1024)");
   if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "tuning inside a substep");
-  const bool changed = p2g_threads != ctx->p2g_threads || particles_per_thread != ctx->ppt;
+  if (g2p_threads != 0 && (g2p_threads < 64 || g2p_threads > 256 || g2p_threads % 32))
+    return fail(ctx, MPM_ERR_BAD_ARG, "g2p threads out of range (64..256 step 32)");
+  const int g2p_t = g2p_threads ? g2p_threads : ctx->g2p_threads;
+  const bool changed = p2g_threads != ctx->p2g_threads || particles_per_thread != ctx->ppt || g2p_t != ctx->g2p_threads;
+  ctx->g2p_threads = g2p_t;
   ctx->p2g_threads = p2g_threads;
   ctx->ppt = particles_per_thread;
   ctx->use_graph = use_graph != 0;

@@ -28,6 +28,27 @@ GB_HD double gexp(double x) { return exp(x); }
 GB_HD float gpow(float x, float y) { return powf(x, y); }
 GB_HD double gpow(double x, double y) { return pow(x, y); }
 template <typename T> GB_HD T gmin(T a, T b) { return a < b ? a : b; }
+
+// Rotation helpers: the angle of a Jacobi rotation only has to shrink the off-diagonal, so
+// float uses the fast reciprocal-based division; what must stay accurate is c^2 + s^2 = 1,
+// so the float cosine is rsqrt refined by one Newton step.  double keeps exact operations.
+GB_HD float gdiv_fast(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fdividef(a, b);
+#else
+  return a / b;
+#endif
+}
+GB_HD double gdiv_fast(double a, double b) { return a / b; }
+GB_HD float grsqrt_acc(float x) {
+#ifdef __CUDA_ARCH__
+  const float r = rsqrtf(x);
+  return r * (1.5f - 0.5f * x * r * r);
+#else
+  return 1.f / sqrtf(x);
+#endif
+}
+GB_HD double grsqrt_acc(double x) { return 1.0 / sqrt(x); }
 template <typename T> GB_HD T gmax(T a, T b) { return a > b ? a : b; }
 
 // ------------------------------------------------------------------------------------
@@ -55,11 +76,11 @@ template <> struct Eps<double> { static constexpr double v = 2.220446049250313e-
 template <typename T>
 GB_HD void jacobi_rotate(T& app, T& aqq, T& apq, T& arp, T& arq, T* V, int p, int q) {
   if (!(gabs(apq) > Eps<T>::v * gsqrt(gabs(app * aqq)))) return;
-  const T theta = (aqq - app) / (T(2) * apq);
+  const T theta = gdiv_fast(aqq - app, T(2) * apq);
   const T at = gabs(theta);
-  T t = (at < T(1e18)) ? T(1) / (at + gsqrt(theta * theta + T(1))) : T(0.5) / at;
+  T t = (at < T(1e18)) ? gdiv_fast(T(1), at + gsqrt(theta * theta + T(1))) : gdiv_fast(T(0.5), at);
   if (theta < T(0)) t = -t;
-  const T c = T(1) / gsqrt(t * t + T(1));
+  const T c = grsqrt_acc(t * t + T(1));
   const T s = t * c;
   app -= t * apq;
   aqq += t * apq;

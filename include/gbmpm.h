@@ -190,10 +190,11 @@ int mpm_count_touched_nodes(mpm_ctx* ctx, int64_t* out_host, void* stream);
 int mpm_status_word(mpm_ctx* ctx, uint32_t* status_host, int64_t* fp64_svd_host,
                     int32_t clear, void* stream);
 
-/* Tuning knobs (the autotuner sets these): P2G threads per CTA (64..512, multiple of 32)
- * and particles per thread (1..16); the P2G work chunk is their product. */
+/* Tuning knobs (the autotuner sets these): P2G threads per CTA (64..256, multiple of 32) and
+ * particles per thread (threads * ppt <= 1024; the P2G work chunk is their product), G2P
+ * threads per CTA (64..256, multiple of 32; 0 keeps the current value), CUDA graphs on/off. */
 int mpm_set_tuning(mpm_ctx* ctx, int32_t p2g_threads, int32_t particles_per_thread,
-                   int32_t use_graph);
+                   int32_t use_graph, int32_t g2p_threads);
 
 /* Per-kernel timing: when enabled, mpm_substeps runs without a graph and brackets every
  * kernel with CUDA events on its launch stream; mpm_kernel_times synchronises and returns

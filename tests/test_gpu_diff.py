@@ -1,10 +1,12 @@
 """Differentiation form: hand-written adjoint substeps checked against FP64 central differences
 of the CPU oracle (eps = 1e-4), for d loss / d v0 and a directional derivative d loss / d E.
 
-loss = ||centre of mass of the final positions - target||^2 (the differentiation config).
-The reference's own (Quadrants autodiff) gradient cannot run here; the FP64 finite
-differences of the reference algorithm are the ground truth.  Tolerance: 2e-2 relative
-(float32 adjoint against float64 differences of a float64 rollout)."""
+d/dv0 uses the differentiation config's loss ||centre of mass - target||^2.  Without contact a
+centre of mass does not depend on E (internal stresses exert no net force), so the E checks
+use a loss that sees the deformation: a fixed random projection of every final position, with
+an initial shear velocity so the elastic forces matter.  The reference's own (Quadrants
+autodiff) gradient cannot run here; FP64 finite differences of the reference algorithm are the
+ground truth.  Tolerance: 2e-2 relative (float32 adjoint against float64 differences)."""
 
 import numpy as np
 import pytest
@@ -32,7 +34,17 @@ def _setup(seed=4, n_side=8):
     return x0, v0, E, target
 
 
-def _oracle_loss(O, x0, v0, E, target, n_sub, nu=0.2, dt=2e-4):
+def _shear(x0):
+    """Fixed initial velocity field (shear + stretch), added to the uniform v0."""
+    d = x0 - x0.mean(0)
+    return np.stack([20.0 * d[:, 2], -15.0 * d[:, 0], 25.0 * d[:, 1]], -1)
+
+
+def _proj(n, seed=12):
+    return np.random.default_rng(seed).normal(size=(n, 3))
+
+
+def _oracle_loss(O, x0, v0, E, target, n_sub, nu=0.2, dt=2e-4, vfield=None, proj=None):
     n = len(x0)
     sc = O.make_scene(dt, grid_density=32.0, particle_size=1.0 / 64)
     mats = []
@@ -40,9 +52,12 @@ def _oracle_loss(O, x0, v0, E, target, n_sub, nu=0.2, dt=2e-4):
         mu = e / (2 * (1 + nu))
         lam = e * nu / ((1 + nu) * (1 - 2 * nu))
         mats.append(O.make_material(0, mu, lam, 1000.0))
-    st = dict(pos=x0, vel=np.tile(v0, (n, 1)), C=np.zeros((n, 3, 3)), F=np.tile(np.eye(3), (n, 1, 1)),
+    vel = np.tile(v0, (n, 1)) + (0.0 if vfield is None else vfield)
+    st = dict(pos=x0, vel=vel, C=np.zeros((n, 3, 3)), F=np.tile(np.eye(3), (n, 1, 1)),
               Jp=np.ones(n), mat=np.arange(n, dtype=np.int32), active=np.ones(n, bool))
     out, _, _ = O.run(sc, mats, st, n_sub)
+    if proj is not None:
+        return float((out["pos"] * proj).sum() / n), out["pos"]
     com = out["pos"].mean(0)
     return float(((com - target) ** 2).sum()), out["pos"]
 
@@ -57,12 +72,18 @@ def sim():
     return DifferentiableMPM(_scene(), nu=0.2, rho=1000.0, ckpt_every=16)
 
 
-def _gpu_loss_and_grads(sim, x0, v0, E, target, n_sub):
+def _gpu_loss_and_grads(sim, x0, v0, E, target, n_sub, vfield=None, proj=None):
     x = torch.tensor(x0, dtype=torch.float32, device="cuda")
     v = torch.tensor(v0, dtype=torch.float32, device="cuda", requires_grad=True)
     e = torch.tensor(E, dtype=torch.float32, device="cuda", requires_grad=True)
-    xf = sim.rollout(x, v, e, n_sub)
-    loss = ((xf.mean(0) - torch.tensor(target, dtype=torch.float32, device="cuda")) ** 2).sum()
+    vv = v.expand(len(x0), 3)
+    if vfield is not None:
+        vv = vv + torch.tensor(vfield, dtype=torch.float32, device="cuda")
+    xf = sim.rollout(x, vv, e, n_sub)
+    if proj is not None:
+        loss = (xf * torch.tensor(proj, dtype=torch.float32, device="cuda")).sum() / len(x0)
+    else:
+        loss = ((xf.mean(0) - torch.tensor(target, dtype=torch.float32, device="cuda")) ** 2).sum()
     loss.backward()
     return loss.item(), xf.detach().cpu().numpy(), v.grad.cpu().numpy().astype(np.float64), e.grad.cpu().numpy().astype(np.float64)
 
@@ -86,14 +107,25 @@ def test_grad_v0_and_E_match_fp64_central_differences(sim, oracle):
         fd_v[k] = (_oracle_loss(oracle, x0, v0 + dv, E, target, n_sub)[0] -
                    _oracle_loss(oracle, x0, v0 - dv, E, target, n_sub)[0]) / (2 * eps)
     assert np.linalg.norm(gv - fd_v) <= GRAD_RTOL * np.linalg.norm(fd_v), (gv, fd_v)
+
+
+def test_grad_E_matches_fp64_central_differences(sim, oracle):
+    x0, v0, E, target = _setup()
+    n_sub = 40
+    vf, pj = _shear(x0), _proj(len(x0))
+    _, _, _, gE = _gpu_loss_and_grads(sim, x0, v0, E, target, n_sub, vfield=vf, proj=pj)
+    assert np.abs(gE).max() > 0
     rng = np.random.default_rng(8)
-    d = rng.normal(size=len(E))
-    d /= np.linalg.norm(d)
-    h = eps * E  # relative step per particle: E (1 +- eps d)
-    fd_E = (_oracle_loss(oracle, x0, v0, E + h * d, target, n_sub)[0] -
-            _oracle_loss(oracle, x0, v0, E - h * d, target, n_sub)[0]) / (2 * eps)
-    ad_E = float(np.dot(gE, h * d)) / eps
-    assert abs(ad_E - fd_E) <= GRAD_RTOL * max(abs(fd_E), 1e-12) + 1e-9, (ad_E, fd_E)
+    for trial in range(2):
+        d = rng.normal(size=len(E))
+        d /= np.linalg.norm(d)
+        eps = 1e-4
+        h = eps * E  # relative step per particle: E (1 +- eps d)
+        fd_E = (_oracle_loss(oracle, x0, v0, E + h * d, target, n_sub, vfield=vf, proj=pj)[0] -
+                _oracle_loss(oracle, x0, v0, E - h * d, target, n_sub, vfield=vf, proj=pj)[0]) / (2 * eps)
+        ad_E = float(np.dot(gE, E * d))
+        assert abs(fd_E) > 1e-8, fd_E
+        assert abs(ad_E - fd_E) <= GRAD_RTOL * abs(fd_E), (trial, ad_E, fd_E)
 
 
 def test_checkpointing_does_not_change_gradients(oracle):
@@ -105,7 +137,8 @@ def test_checkpointing_does_not_change_gradients(oracle):
     x0, v0, E, target = _setup(seed=6)
     a = DifferentiableMPM(_scene(), ckpt_every=8)
     b = DifferentiableMPM(_scene(), ckpt_every=1000)
-    _, _, gva, gEa = _gpu_loss_and_grads(a, x0, v0, E, target, 32)
-    _, _, gvb, gEb = _gpu_loss_and_grads(b, x0, v0, E, target, 32)
-    assert np.allclose(gva, gvb, rtol=1e-3, atol=1e-9)
-    assert np.allclose(gEa, gEb, rtol=1e-2, atol=1e-3 * np.abs(gEb).max())
+    vf, pj = _shear(x0), _proj(len(x0))
+    _, _, gva, gEa = _gpu_loss_and_grads(a, x0, v0, E, target, 32, vfield=vf, proj=pj)
+    _, _, gvb, gEb = _gpu_loss_and_grads(b, x0, v0, E, target, 32, vfield=vf, proj=pj)
+    assert np.allclose(gva, gvb, rtol=1e-3, atol=1e-9 + 1e-4 * np.abs(gvb).max())
+    assert np.linalg.norm(gEa - gEb) <= 1e-2 * np.linalg.norm(gEb)
