@@ -1,0 +1,118 @@
+"""Host-side logic of the Genesis-style facade (no GPU): options, materials, morph sampling,
+derived solver constants, workload generators and the serving admission arithmetic."""
+
+import math
+
+import numpy as np
+import pytest
+
+import genesis_gb300 as gs
+from genesis_gb300 import morphs
+from genesis_gb300.exceptions import GenesisException
+
+
+def test_sim_and_mpm_options_defaults_and_validation():
+    so = gs.options.SimOptions()
+    assert so.dt == 1e-2 and so.substeps == 1 and so.substeps_local == 1 and so.gravity == (0.0, 0.0, -9.81)
+    mo = gs.options.MPMOptions()
+    assert mo.grid_density == 64 and mo.particle_size == pytest.approx(0.01)
+    assert gs.options.MPMOptions(grid_density=128).particle_size == pytest.approx(0.005)
+    with pytest.raises(GenesisException, match="upper_bound"):
+        gs.options.MPMOptions(lower_bound=(0, 0, 1), upper_bound=(1, 1, 0))
+    with pytest.raises(GenesisException):
+        gs.options.SimOptions(nonsense=1)
+    with pytest.raises(GenesisException, match="divisible"):
+        gs.options.SimOptions(requires_grad=True, substeps=3, substeps_local=4)
+    # MPMOptions inherits dt and gravity from SimOptions (scene.py:157)
+    merged = gs.options.MPMOptions().model_copy_from(gs.options.SimOptions(dt=3e-4, gravity=(0, 0, -1)))
+    assert merged.dt == 3e-4 and merged.gravity == (0, 0, -1)
+
+
+def test_material_defaults_match_reference_formulas():
+    e = gs.materials.MPM.Elastic()
+    assert e.E == 3e5 and e.nu == 0.2 and e.rho == 1000.0
+    assert e.mu == pytest.approx(3e5 / (2 * 1.2)) and e.lam == pytest.approx(3e5 * 0.2 / (1.2 * 0.6))
+    assert gs.materials.MPM.Liquid().mu == 0.0
+    assert gs.materials.MPM.Liquid(viscous=True).mu > 0
+    s = gs.materials.MPM.Sand()
+    sp = math.sin(math.radians(45.0))
+    assert s.alpha == pytest.approx(math.sqrt(2 / 3) * 2 * sp / (3 - sp)) and s._default_Jp == 0.0
+    sn = gs.materials.MPM.Snow()
+    assert sn.yield_lower == 2.5e-2 and sn.yield_higher == 4.5e-3 and not sn.use_von_mises
+    with pytest.raises(GenesisException):
+        gs.materials.MPM.Snow(use_von_mises=True)
+    m = gs.materials.MPM.Muscle()
+    assert m.E == 1e6 and m.model == "neohooken" and m.stiffness == 1e6
+    ep = gs.materials.MPM.ElastoPlastic()
+    assert ep.use_von_mises and ep.von_mises_yield_stress == 10000.0
+    with pytest.raises(GenesisException):
+        gs.materials.MPM.Elastic(nu=0.5)
+    with pytest.raises(GenesisException):
+        gs.materials.MPM.Elastic(sampler="bogus")
+
+
+def test_material_c_records():
+    from genesis_gb300 import _lib
+
+    r = gs.materials.MPM.ElastoPlastic().to_c(3)
+    assert r.type == _lib.MAT_ELASTOPLASTIC and r.flags == _lib.MATF_VON_MISES and r.scene == 3
+    assert gs.materials.MPM.Elastic(model="neohooken").to_c(0).flags == _lib.MATF_NEOHOOKEAN
+    assert gs.materials.MPM.Sand().to_c(0).default_Jp == 0.0
+
+
+def test_box_regular_sampler_matches_reference_count_and_layout():
+    p = morphs.box_to_particles(1 / 128, (0.5, 0.5, 0.4), (0.2, 0.2, 0.2), "regular")
+    assert len(p) == 26**3  # n_particles_1D = round(0.2 * 128) = 26 per axis
+    assert p.min(0) == pytest.approx(np.array([0.4, 0.4, 0.3]) + 0.5 / 128)
+    assert morphs.n_particles_3D(0.01, (0.3, 0.2, 0.1)) == 30 * 20 * 10
+    np.random.seed(0)
+    r = morphs.box_to_particles(0.01, (0, 0, 0), (0.1, 0.1, 0.1), "random")
+    assert len(r) == 1000 and np.all(np.abs(r) <= 0.05)
+
+
+def test_sphere_and_rotation():
+    s = morphs.Sphere(pos=(0.5, 0.5, 0.5), radius=0.1).sample(0.01, "regular")
+    assert np.all(np.linalg.norm(s - 0.5, axis=1) <= 0.1 + 1e-12)
+    b = morphs.Box(pos=(0, 0, 0), size=(0.2, 0.1, 0.1), euler=(0, 0, 90)).sample(0.01, "regular")
+    ext = b.max(0) - b.min(0)
+    assert ext[1] == pytest.approx(0.19, abs=1e-9) and ext[0] == pytest.approx(0.09, abs=1e-9)
+
+
+def test_solver_derived_constants_without_gpu():
+    from genesis_gb300.solver import MPMSolver
+
+    class _Sim:
+        substeps = 1
+
+    gs.EPS = float(np.finfo(np.float32).eps)
+    opts = gs.options.MPMOptions(lower_bound=(0, 0, 0), upper_bound=(1, 1, 1)).model_copy_from(
+        gs.options.SimOptions(dt=2e-4))
+    s = MPMSolver(None, _Sim(), opts)
+    assert tuple(s.grid_res) == (65, 65, 65)
+    assert s.dx == 1 / 64 and s.particle_volume == pytest.approx((0.01**3) * 1e3)
+    assert s.boundary.lower == pytest.approx(np.float32(3 / 64)) and s.boundary.upper[0] == pytest.approx(61 / 64)
+    s.add_material(gs.materials.MPM.Elastic())
+    m2 = gs.materials.MPM.Elastic()
+    s.add_material(m2)
+    s.add_material(gs.materials.MPM.Sand())
+    assert m2.idx == 0 and len(s._unique_materials()) == 2
+    with pytest.raises(GenesisException, match="1e9"):
+        MPMSolver(None, _Sim(), gs.options.MPMOptions(grid_density=2000, lower_bound=(-1, -1, -1),
+                                                        upper_bound=(1, 1, 1)).model_copy_from(gs.options.SimOptions()))
+
+
+def test_workload_generators_are_seeded_and_in_range():
+    from genesis_gb300.batched import batched_workload
+    from genesis_gb300.serve import grid_blocks, serving_workload
+
+    a = batched_workload(n_scenes=64, seed=1)
+    b = batched_workload(n_scenes=64, seed=1)
+    assert [s.n_particles for s in a] == [s.n_particles for s in b]
+    assert all(2000 <= s.n_particles <= 64000 and 0.1 <= s.extent <= 0.3 for s in a)
+    assert len({type(s.material).__name__ for s in a}) == 4
+    reqs = serving_workload(n_requests=200, rate_hz=100.0, seed=3)
+    arr = np.array([r.arrival for r in reqs])
+    assert np.all(np.diff(arr) >= 0) and 0.5 < arr[-1] / 2.0 < 2.0  # ~200 arrivals at 100/s
+    assert all(1000 <= r.spec.n_particles <= 500000 and 50 <= r.spec.substeps <= 500 for r in reqs)
+    assert {int(r.spec.grid_density) + 1 for r in reqs} == {33, 65, 129}
+    assert grid_blocks(129) == 33**3 and grid_blocks(65) == 17**3
