@@ -138,26 +138,39 @@ class ClockSampler:
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, device_index=0):
-        self.samples = []
+    def __init__(self, device_index=0, period_ms=20):
+        self.samples = []  # (host time when read, fields)
         self.proc = None
         self.dev = device_index
+        self.period_ms = period_ms
+        self.t_begin = self.t_end = None
 
-    def start(self):
+    def start(self, wait_s=10.0):
+        """Start nvidia-smi and wait for its first sample, so the timed region is covered."""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", str(self.period_ms)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        t0 = time.perf_counter()
+        while not self.samples and time.perf_counter() - t0 < wait_s and self.proc.poll() is None:
+            time.sleep(0.01)
+
+    def begin(self):
+        self.t_begin = time.perf_counter()
+
+    def end(self):
+        self.t_end = time.perf_counter()
 
     def _read(self):
         for line in self.proc.stdout:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) >= 9:
-                self.samples.append(parts)
+                self.samples.append((time.perf_counter(), parts))
 
     def stop(self):
         if self.proc is None:
@@ -167,12 +180,18 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
-        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        inside = [p for t, p in self.samples
+                  if self.t_begin is not None and self.t_end is not None and self.t_begin <= t <= self.t_end]
+        # a sample is read up to one period after it was taken: also keep the one read just after the end
+        after = [p for t, p in self.samples if self.t_end is not None and self.t_end < t <= self.t_end + self.period_ms / 1e3]
+        use = inside + after[:1] if inside or after else [p for _, p in self.samples]
+        sm = [float(s[1]) for s in use if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in use if s[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[5 + i].lower() == "active"})
+        reasons = sorted({names[i] for s in use for i in range(4) if s[5 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "reasons": reasons, "samples": len(use), "period_ms": self.period_ms,
+                "window": "timed region" if inside or after else "whole run (no sample inside the timed region)"}
 
 
 def reduce_over_ranks(ms: float, units: float, device) -> tuple[float, float]:
@@ -225,17 +244,19 @@ def run_ours(args, rank, world):
     # --- timed region: K steps of 10 substeps, CUDA graph path, inputs resident in HBM
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
-    time.sleep(0.3)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks.begin()
     e0.record(stream)
     for _ in range(args.steps):
         solver.substeps(SUBSTEPS_PER_STEP)
     e1.record(stream)
     torch.cuda.synchronize()
+    clocks.end()
     ms = e0.elapsed_time(e1)
+    time.sleep(0.05)
     clk = clocks.stop()
     solver.check_state()
     total_units = n * SUBSTEPS_PER_STEP * args.steps
@@ -400,7 +421,7 @@ def run_forms(batched_substeps=200, n_requests=48):
     }
     # served: the same request set (a) saturated (all arrive at once) for throughput, against each
     # request run alone in turn; (b) Poisson arrivals at half the saturated rate for p50/p99 latency
-    reqs = serving_workload(n_requests=n_requests, rate_hz=0, seed=77)
+    reqs = serving_workload(n_requests=n_requests, rate_hz=0, seed=77, with_payload=True)
     work = sum(r.work for r in reqs)
     srv = MPMServer(max_slots=64, particle_capacity=40_000_000, max_grid_res=129, chunk=10)
     sat = srv.run(reqs, realtime=False)
@@ -412,7 +433,7 @@ def run_forms(batched_substeps=200, n_requests=48):
         one.close()
     mean_work = work / len(reqs)
     rate = 0.5 * sat["throughput"] / mean_work
-    reqs2 = serving_workload(n_requests=n_requests, rate_hz=rate, seed=77)
+    reqs2 = serving_workload(n_requests=n_requests, rate_hz=rate, seed=77, with_payload=True)
     live = srv.run(reqs2, realtime=True)
     srv.close()
     out["served"] = {
@@ -513,7 +534,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-cpu", action="store_true")

@@ -95,6 +95,7 @@ struct mpm_ctx {
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
   cudaGraphExec_t gexec = nullptr;
   bool graph_valid = false;
+  bool grid_momentum[2] = {false, false};  // grid buffer holds P2G momentum (grid op fused into G2P)
   bool profiling = false;
   std::vector<TimedPair> pending;
   std::vector<cudaEvent_t> ev_pool;
@@ -220,7 +221,7 @@ int launch_sort(mpm_ctx* ctx, const KParams& P, cudaStream_t s) {
     }
   }
   CKL();
-  if (P.n > 0 || P.steps) {
+  if (P.n > 0 || P.steps || P.nlist_reset) {
     Timer t(ctx, s, KT_PERM);
     k_perm<<<ctx->io_blocks, 256, 0, s>>>(P);
   }
@@ -253,17 +254,21 @@ int launch_pre(mpm_ctx* ctx, int c, cudaStream_t s) {
 
 int launch_grid(mpm_ctx* ctx, int c, cudaStream_t s) {
   KParams P = make_params(ctx, c, 1 - c, c);
+  ctx->grid_momentum[c] = false;
   Timer t(ctx, s, KT_GRID);
   k_grid_op<<<ctx->grid_blocks, 256, 0, s>>>(P);
   CKL();
   return MPM_OK;
 }
 
-int launch_post(mpm_ctx* ctx, int c, cudaStream_t s) {
+int launch_post(mpm_ctx* ctx, int c, cudaStream_t s, bool fuse_grid = false) {
   KParams P = make_params(ctx, c, 1 - c, c);
   P.n = ctx->n;
   P.n_dev = ctx->d_n;
   P.steps = ctx->d_steps;
+  P.fuse_grid = fuse_grid ? 1 : 0;
+  P.nlist_reset = fuse_grid ? P.nlist_other : nullptr;
+  ctx->grid_momentum[c] = fuse_grid;
   {
     Timer t(ctx, s, KT_G2P);
     k_g2p<<<ctx->g2p_blocks, ctx->g2p_threads, 0, s>>>(P);
@@ -272,10 +277,13 @@ int launch_post(mpm_ctx* ctx, int c, cudaStream_t s) {
   return launch_sort(ctx, P, s);
 }
 
+// Without pinned particles the grid op is folded into G2P (k_grid_op is not launched); the
+// split-phase entry points keep it separate so a coupler can act on the velocity grid.
 int launch_substep(mpm_ctx* ctx, int c, cudaStream_t s) {
+  const bool fuse = ctx->d_pin == nullptr;
   int r = launch_pre(ctx, c, s);
-  if (!r) r = launch_grid(ctx, c, s);
-  if (!r) r = launch_post(ctx, c, s);
+  if (!r && !fuse) r = launch_grid(ctx, c, s);
+  if (!r) r = launch_post(ctx, c, s, fuse);
   return r;
 }
 
@@ -814,6 +822,7 @@ int mpm_get_grid(mpm_ctx* ctx, int64_t scene, float* out, void* stream) {
   int r = enter(ctx, stream);
   if (r) return r;
   KParams P = make_params(ctx, ctx->cur, ctx->cur, g);
+  P.fuse_grid = (ctx->phase == 0 && ctx->grid_momentum[g]) ? 1 : 0;
   k_get_grid<<<ctx->n_sm * 8, 256, 0, ctx->cs>>>(P, scene, out);
   CKL();
   return leave(ctx, stream);

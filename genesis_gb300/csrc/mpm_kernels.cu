@@ -2,8 +2,10 @@
 // per-substep particle re-sort, plus the state I/O kernels.
 //
 // One substep = k_p2g -> k_grid_op -> k_g2p -> k_scan_reduce -> k_scan_partials ->
-// k_scan_apply -> k_perm.  Reference semantics: genesis/engine/solvers/mpm_solver.py
-// (p2g :322-421, g2p :423-481) and genesis/engine/couplers/legacy_coupler.py
+// k_scan_apply -> k_perm; without particles pinned to their nodes the grid op runs inside
+// k_g2p (per staged node) and k_grid_op is not launched.  Reference semantics:
+// genesis/engine/solvers/mpm_solver.py (p2g :322-421, g2p :423-481) and
+// genesis/engine/couplers/legacy_coupler.py
 // (mpm_grid_op :356-501); see each kernel.
 #include "mpm_kernels.cuh"
 
@@ -422,6 +424,7 @@ __global__ void k_perm(KParams P) {
   const int64_t n = P.n_dev ? *P.n_dev : P.n;
   for (int64_t i = grid_stride_begin(); i < n; i += grid_stride_step())
     P.perm[P.offset[P.key[i]] + P.rank[i]] = (int32_t)i;
+  if (P.nlist_reset && blockIdx.x == 0 && threadIdx.x == 0) *P.nlist_reset = 0;  // cleared by the fused G2P
   if (P.steps && blockIdx.x == 0)  // end of a substep: count down per-scene substep budgets
     for (int s = threadIdx.x; s < P.n_scenes; s += blockDim.x)
       if (P.steps[s] > 0) P.steps[s] -= 1;
@@ -460,18 +463,14 @@ __device__ __forceinline__ void load_particle(const KParams& P, const float* Sx,
   }
 }
 
+// Writes a particle to its sorted slot.  Velocity and C are left out: G2P of the same substep
+// overwrites both for every particle of an active bucket before anything reads them.
 __device__ __forceinline__ void store_particle(const KParams& P, float* Dx, int64_t slot, const Particle& q) {
   const int64_t cap = P.cap;
 #pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    Dx[(int64_t)(PF_POS + d) * cap + slot] = q.x[d];
-    Dx[(int64_t)(PF_VEL + d) * cap + slot] = q.v[d];
-  }
+  for (int d = 0; d < 3; ++d) Dx[(int64_t)(PF_POS + d) * cap + slot] = q.x[d];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) {
-    Dx[(int64_t)(PF_C + k) * cap + slot] = q.C[k];
-    Dx[(int64_t)(PF_F + k) * cap + slot] = q.F[k];
-  }
+  for (int k = 0; k < 9; ++k) Dx[(int64_t)(PF_F + k) * cap + slot] = q.F[k];
   Dx[(int64_t)PF_JP * cap + slot] = q.Jp;
   Dx[(int64_t)PF_INFO * cap + slot] = __uint_as_float(q.info);
   Dx[(int64_t)PF_PID * cap + slot] = q.pid;
@@ -511,10 +510,11 @@ __device__ __forceinline__ void block_origin(const SceneDev& S, int64_t key, int
 //     + stress (mpm_solver.py:293-307, 339-377), write the particle to its slot, and leave its
 //     scatter parameters (fx, mass, q = m v - sum_k a_k fx_k, a_k = dx * affine[:,k]) in a
 //     shared record at its cell-sorted position;
-//  3. walk the cell-sorted records transposed (lanes of a warp take records `stride` apart, so
-//     different cells) and add the APIC mass/momentum w_o (q + sum_k o_k a_k), w_o m
-//     (mpm_solver.py:379-418) to a warp-private 6^3 shared tile with plain float4
-//     read-modify-writes; lanes that still share a cell are serialised in __match_any rounds;
+//  3. one thread per (cell, ox) walks its cell's records and sums the APIC mass/momentum
+//     w_o (q + sum_k o_k a_k), w_o m (mpm_solver.py:379-418) of the 9 nodes (ox, *, *) in
+//     registers, then adds them to its warp's private 6^3 shared tile (plain float4
+//     read-modify-writes; no two lanes of a warp share a node): one tile update per cell and
+//     node instead of one per particle and node;
 //  4. sum the warp tiles and flush with one 16-byte vector reduction per node.
 __global__ void __launch_bounds__(P2G_MAX_THREADS, 2) k_p2g(KParams P) {
   extern __shared__ __align__(16) unsigned char p2g_smem[];
@@ -522,11 +522,9 @@ __global__ void __launch_bounds__(P2G_MAX_THREADS, 2) k_p2g(KParams P) {
   __shared__ int s_touch[8];
   const int n_items = *P.n_items;
   const int T = blockDim.x, nw = T >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int RS = p2g_record_stride(P.chunk);
   float4* s_tile = reinterpret_cast<float4*>(p2g_smem);
-  float* s_rec = reinterpret_cast<float*>(s_tile + nw * TILE_NODES);
-  uint32_t* s_cr = reinterpret_cast<uint32_t*>(s_rec + 16 * RS);
-  uint8_t* s_cellp = reinterpret_cast<uint8_t*>(s_cr + P.chunk);
+  float4* s_rec = s_tile + nw * TILE_NODES;
+  uint32_t* s_cr = reinterpret_cast<uint32_t*>(s_rec + P2G_REC * P.chunk);
   const int64_t cap = P.cap;
   const float* Sx = P.src;
   float* Dx = P.dst;
@@ -588,7 +586,7 @@ __global__ void __launch_bounds__(P2G_MAX_THREADS, 2) k_p2g(KParams P) {
       const int64_t si = P.perm[slot];
       Particle pt;
       load_particle(P, Sx, si, pt);
-      uint8_t cp = 255;
+      bool scattered = false;
       if (pt.info & INFO_ACTIVE) {
         const MaterialDev& M = P.mats[pt.info & INFO_MAT_MASK];
         // F_tmp = (I + dt C) F   (compute_F_tmp, mpm_solver.py:293-299)
@@ -631,17 +629,15 @@ __global__ void __launch_bounds__(P2G_MAX_THREADS, 2) k_p2g(KParams P) {
           for (int r = 0; r < 3; ++r)
 #pragma unroll
             for (int k = 0; k < 3; ++k) a[k * 3 + r] = S.dx * (S.stress_scale * Pk[r * 3 + k] + mass * pt.C[r * 3 + k]);
-          float* rec = s_rec + p;
-          rec[0 * RS] = fx[0];
-          rec[1 * RS] = fx[1];
-          rec[2 * RS] = fx[2];
-          rec[3 * RS] = mass;
+          float qv[3];
 #pragma unroll
-          for (int r = 0; r < 3; ++r)
-            rec[(4 + r) * RS] = mass * pt.v[r] - (a[r] * fx[0] + a[3 + r] * fx[1] + a[6 + r] * fx[2]);
-#pragma unroll
-          for (int k = 0; k < 9; ++k) rec[(7 + k) * RS] = a[k];
-          cp = (uint8_t)cell;
+          for (int r = 0; r < 3; ++r) qv[r] = mass * pt.v[r] - (a[r] * fx[0] + a[3 + r] * fx[1] + a[6 + r] * fx[2]);
+          float4* rec = s_rec + P2G_REC * p;
+          rec[0] = make_float4(fx[0], fx[1], fx[2], mass);
+          rec[1] = make_float4(qv[0], qv[1], qv[2], a[0]);
+          rec[2] = make_float4(a[1], a[2], a[3], a[4]);
+          rec[3] = make_float4(a[5], a[6], a[7], a[8]);
+          scattered = true;
           if (!(pt.info & INFO_FREE) && P.pin) {  // its 27 nodes lose all momentum (mpm_solver.py:420-421)
             for (int o = 0; o < 27; ++o) {
               const int64_t ad = node_addr(S, org[0] + tb0 + o / 9, org[1] + tb1 + (o / 3) % 3, org[2] + tb2 + o % 3);
@@ -652,70 +648,75 @@ __global__ void __launch_bounds__(P2G_MAX_THREADS, 2) k_p2g(KParams P) {
           atomicOr(P.status, 2u);  // cannot happen for a correctly keyed particle; never touches memory
         }
       }
-      s_cellp[p] = cp;
+      if (!scattered && cell < BLK_NODES) {  // holds a place in its cell's run: contributes nothing
+        float4* rec = s_rec + P2G_REC * p;
+        rec[0] = make_float4(0.5f, 0.5f, 0.5f, 0.f);
+        rec[1] = rec[2] = rec[3] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
       store_particle(P, Dx, slot, pt);
     }
     __syncthreads();
-    // 3. transposed scatter into the warp tile
-    const int stride = ((cnt + 31) >> 5) | 1;
-    const int total = stride << 5;
-    for (int q = threadIdx.x; q < total; q += T) {
-      const int p = (q & 31) * stride + (q >> 5);
-      const int cell = p < cnt ? (int)s_cellp[p] : 255;
-      const bool scat = cell < BLK_NODES;
-      float w[3][3], mass = 0.f, qv[3] = {0.f, 0.f, 0.f}, a[9];
-      int tb[3] = {0, 0, 0};
-      if (scat) {
-        const float* rec = s_rec + p;
-        float fx[3];
+    // 3. cell-major scatter: unit u = (cell, ox) sums the 9 nodes (ox, *, *) of the stencils of
+    //    all particles of its cell in registers and adds them to the warp tile once.  A warp's
+    //    32 units span fewer than 16 consecutive cells, so no two of its lanes share a node.
+    for (int u0 = 0; u0 < 3 * BLK_NODES; u0 += T) {
+      const int u = u0 + threadIdx.x;
+      const bool has = u < 3 * BLK_NODES;
+      const int cell = has ? u / 3 : 0, ox = has ? u - 3 * (u / 3) : 0;
+      const int beg = has ? s_off[cell] : 0;
+      const int len = has ? s_off[cell + 1] - beg : 0;
+      const int nmax = __reduce_max_sync(0xffffffffu, len);
+      if (nmax == 0) continue;  // warp-uniform
+      float4 acc[3][3];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          fx[d] = rec[d * RS];
-          bspline_w(fx[d], w[d]);
-        }
-        mass = rec[3 * RS];
+      for (int oy = 0; oy < 3; ++oy)
 #pragma unroll
-        for (int r = 0; r < 3; ++r) qv[r] = rec[(4 + r) * RS];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) a[k] = rec[(7 + k) * RS];
-        tb[0] = cell >> 4;
-        tb[1] = (cell >> 2) & 3;
-        tb[2] = cell & 3;
-      }
-      const unsigned am = __ballot_sync(0xffffffffu, scat);
-      if (am == 0u) continue;  // warp-uniform
-      unsigned my_round = 0;
-      if (scat) {
-        const unsigned peers = __match_any_sync(am, cell);
-        my_round = __popc(peers & ((1u << lane) - 1u));
-      }
-      const unsigned rounds = __reduce_max_sync(0xffffffffu, my_round) + 1u;
-      for (unsigned rd = 0; rd < rounds; ++rd) {
-        const bool mine = scat && my_round == rd;
-#pragma unroll
-        for (int ox = 0; ox < 3; ++ox) {
-          const float t0x = qv[0] + (float)ox * a[0], t0y = qv[1] + (float)ox * a[1], t0z = qv[2] + (float)ox * a[2];
+        for (int oz = 0; oz < 3; ++oz) acc[oy][oz] = make_float4(0.f, 0.f, 0.f, 0.f);
+      const float fo = (float)ox;
+      for (int j = 0; j < nmax; ++j) {
+        if (j < len) {
+          const float4* rec = s_rec + P2G_REC * (beg + j);
+          const float4 r0 = rec[0], r1 = rec[1], r2 = rec[2], r3 = rec[3];
+          float wxv[3], wy[3], wz[3];
+          bspline_w(r0.x, wxv);
+          bspline_w(r0.y, wy);
+          bspline_w(r0.z, wz);
+          const float wx = ox == 0 ? wxv[0] : (ox == 1 ? wxv[1] : wxv[2]);
+          // a (k-major, a[k*3 + r]) = r1.w, r2.x, r2.y | r2.z, r2.w, r3.x | r3.y, r3.z, r3.w
+          const float t0x = r1.x + fo * r1.w, t0y = r1.y + fo * r2.x, t0z = r1.z + fo * r2.y;
 #pragma unroll
           for (int oy = 0; oy < 3; ++oy) {
-            const float t1x = t0x + (float)oy * a[3], t1y = t0y + (float)oy * a[4], t1z = t0z + (float)oy * a[5];
-            const float w01 = w[0][ox] * w[1][oy];
+            const float t1x = t0x + (float)oy * r2.z, t1y = t0y + (float)oy * r2.w, t1z = t0z + (float)oy * r3.x;
+            const float w01 = wx * wy[oy];
 #pragma unroll
             for (int oz = 0; oz < 3; ++oz) {
-              if (mine) {
-                const float wt = w01 * w[2][oz];
-                const int idx = ((tb[0] + ox) * TILE + (tb[1] + oy)) * TILE + (tb[2] + oz);
-                float4 g = my_tile[idx];
-                g.x += wt * (t1x + (float)oz * a[6]);
-                g.y += wt * (t1y + (float)oz * a[7]);
-                g.z += wt * (t1z + (float)oz * a[8]);
-                g.w += wt * mass;
-                my_tile[idx] = g;
-              }
-              __syncwarp();
+              const float wt = w01 * wz[oz];
+              acc[oy][oz].x += wt * (t1x + (float)oz * r3.y);
+              acc[oy][oz].y += wt * (t1y + (float)oz * r3.z);
+              acc[oy][oz].z += wt * (t1z + (float)oz * r3.w);
+              acc[oy][oz].w += wt * r0.w;
             }
           }
         }
       }
+      // Lanes of neighbouring cells reach the same node at different (oy, oz) steps: a
+      // __syncwarp between steps orders those read-modify-writes.
+      const int tb0 = cell >> 4, tb1 = (cell >> 2) & 3, tb2 = cell & 3;
+#pragma unroll
+      for (int oy = 0; oy < 3; ++oy)
+#pragma unroll
+        for (int oz = 0; oz < 3; ++oz) {
+          if (len > 0) {
+            float4* g = my_tile + ((tb0 + ox) * TILE + (tb1 + oy)) * TILE + (tb2 + oz);
+            float4 h = *g;
+            h.x += acc[oy][oz].x;
+            h.y += acc[oy][oz].y;
+            h.z += acc[oy][oz].z;
+            h.w += acc[oy][oz].w;
+            *g = h;
+          }
+          __syncwarp();
+        }
     }
     __syncthreads();
     // 4. flush
@@ -768,7 +769,18 @@ __device__ __forceinline__ void add_rank(const KParams& P, bool valid, int32_t k
 
 __global__ void __launch_bounds__(256) k_g2p(KParams P) {
   __shared__ float4 s_v[TILE_NODES];
-  if (blockIdx.x == 0 && threadIdx.x == 0) *P.nlist_other = 0;
+  if (P.fuse_grid) {
+    // the grid op's other duty: zero the blocks the previous substep left in the other buffer
+    // (the next P2G adds into it); k_perm resets that list's length after this kernel
+    const int64_t n_other = (int64_t)*P.nlist_other * BLK_NODES;
+    for (int64_t i = grid_stride_begin(); i < n_other; i += grid_stride_step()) {
+      const int32_t blk = P.list_other[i / BLK_NODES];
+      P.grid_other[(int64_t)blk * BLK_NODES + (i % BLK_NODES)] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (i % BLK_NODES == 0) P.flags_other[blk] = 0;
+    }
+  } else if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *P.nlist_other = 0;
+  }
   const int n_items = *P.n_items;
   const int T = blockDim.x, lane = threadIdx.x & 31;
   const int64_t cap = P.cap;
@@ -805,7 +817,10 @@ __global__ void __launch_bounds__(256) k_g2p(KParams P) {
     for (int t = threadIdx.x; t < TILE_NODES; t += T) {
       const int gx = org[0] + t / (TILE * TILE), gy = org[1] + (t / TILE) % TILE, gz = org[2] + t % TILE;
       float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (gx < S.res[0] && gy < S.res[1] && gz < S.res[2]) g = P.grid[node_addr(S, gx, gy, gz)];
+      if (gx < S.res[0] && gy < S.res[1] && gz < S.res[2]) {
+        g = P.grid[node_addr(S, gx, gy, gz)];
+        if (P.fuse_grid) g = grid_velocity(S, g, gx, gy, gz);
+      }
       s_v[t] = g;
     }
     __syncthreads();
@@ -932,20 +947,7 @@ __global__ void __launch_bounds__(256) k_grid_op(KParams P) {
         atomicAnd(&P.pin[a >> 5], ~bit);
       }
     }
-    float v[3] = {0.f, 0.f, 0.f};
-    if (q.w > S.eps) {
-      const float inv = 1.f / q.w;
-      v[0] = inv * q.x + S.dt * S.grav[0];
-      v[1] = inv * q.y + S.dt * S.grav[1];
-      v[2] = inv * q.z + S.dt * S.grav[2];
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const float pos = (float)(g[d] + S.offset[d]) * S.dx;
-        if (pos >= S.hi[d] && v[d] >= 0.f) v[d] *= -S.restitution;
-        else if (pos <= S.lo[d] && v[d] <= 0.f) v[d] *= -S.restitution;
-      }
-    }
-    *node = make_float4(v[0], v[1], v[2], q.w);
+    *node = grid_velocity(S, q, g[0], g[1], g[2]);
   }
 }
 
@@ -957,7 +959,8 @@ __global__ void k_get_grid(KParams P, int64_t scene, float* out) {
     const int gz = (int)(i % S.res[2]);
     const int gy = (int)((i / S.res[2]) % S.res[1]);
     const int gx = (int)(i / ((int64_t)S.res[2] * S.res[1]));
-    const float4 q = P.grid[node_addr(S, gx, gy, gz)];
+    float4 q = P.grid[node_addr(S, gx, gy, gz)];
+    if (P.fuse_grid) q = grid_velocity(S, q, gx, gy, gz);  // the buffer holds P2G momentum
     out[i * 4 + 0] = q.x;
     out[i * 4 + 1] = q.y;
     out[i * 4 + 2] = q.z;

@@ -36,13 +36,13 @@ constexpr int P2G_MAX_THREADS = 256;         // P2G CTA size limit (warp-private
 constexpr int P2G_MAX_WARPS = P2G_MAX_THREADS / 32;
 constexpr int P2G_MAX_CHUNK = 1024;          // particles per P2G work item
 
-// Shared-memory layout of k_p2g (dynamic part): warp tiles, then 16 SoA record planes of
-// `stride` floats (a multiple of 32 holding 32 * odd rows, so transposed reads hit distinct
-// banks), then the item's (cell, rank) words, then one cell byte per sorted position.
-__host__ __device__ __forceinline__ int p2g_record_stride(int chunk) { return 32 * (((chunk + 31) / 32) | 1); }
+// Shared-memory layout of k_p2g (dynamic part): warp tiles, then one scatter record per particle
+// at its cell-sorted position (P2G_REC float4 each: fx | mass, q | a0, a1..a4, a5..a8, pad; the
+// odd stride of 5 float4 puts consecutive records in different bank groups), then the item's
+// (cell, rank) words.
+constexpr int P2G_REC = 5;
 __host__ __device__ __forceinline__ size_t p2g_dyn_smem(int threads, int chunk) {
-  const int rs = p2g_record_stride(chunk);
-  return (size_t)(threads / 32) * TILE_NODES * 16 + (size_t)16 * rs * 4 + (size_t)chunk * 4 + (size_t)rs;
+  return (size_t)(threads / 32) * TILE_NODES * 16 + (size_t)chunk * P2G_REC * 16 + (size_t)chunk * 4;
 }
 constexpr float SVD_FP64_TOL = 1e-5f;        // residual above which the SVD is redone in FP64
 
@@ -111,6 +111,8 @@ struct KParams {
   float eps_norm;              // gs.EPS for Matrix.norm(eps)
   uint32_t* status;
   unsigned long long* fp64_count;
+  int32_t fuse_grid;           // G2P applies the grid op while staging its tile and clears the other buffer
+  int32_t* nlist_reset;        // active-list length that k_perm resets at the end of a fused substep
 };
 
 // Block key of a world position; returns false if the stencil would leave the grid.
@@ -125,6 +127,27 @@ __device__ __forceinline__ bool stencil_origin(const SceneDev& S, const float* x
     if (b[d] < 0 || b[d] > S.res[d] - 3) return false;
   }
   return true;
+}
+
+// Grid op of one node (legacy_coupler.py:356-501 with MPM alone): v = p/m + dt g where the node
+// holds mass, then the free-slip separating boundary on node positions (boundaries.py:22-32).
+// (gx, gy, gz) is the node index within its scene's grid.
+__device__ __forceinline__ float4 grid_velocity(const SceneDev& S, float4 q, int gx, int gy, int gz) {
+  float v[3] = {0.f, 0.f, 0.f};
+  if (q.w > S.eps) {
+    const float inv = 1.f / q.w;
+    v[0] = inv * q.x + S.dt * S.grav[0];
+    v[1] = inv * q.y + S.dt * S.grav[1];
+    v[2] = inv * q.z + S.dt * S.grav[2];
+    const int g[3] = {gx, gy, gz};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float pos = (float)(g[d] + S.offset[d]) * S.dx;
+      if (pos >= S.hi[d] && v[d] >= 0.f) v[d] *= -S.restitution;
+      else if (pos <= S.lo[d] && v[d] <= 0.f) v[d] *= -S.restitution;
+    }
+  }
+  return make_float4(v[0], v[1], v[2], q.w);
 }
 
 __device__ __forceinline__ int64_t block_of(const SceneDev& S, int gx, int gy, int gz) {
