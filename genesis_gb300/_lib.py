@@ -33,6 +33,7 @@ STATUS_NAMES = {
 }
 STATUS_NAN = 0x1
 STATUS_OOB = 0x2
+STATUS_WAIT = 0x4
 
 # material types / flags (mpm_material_type, MPM_MATF_*)
 MAT_ELASTIC, MAT_LIQUID, MAT_SAND, MAT_SNOW, MAT_ELASTOPLASTIC, MAT_MUSCLE = range(6)

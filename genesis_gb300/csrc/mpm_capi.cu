@@ -70,6 +70,8 @@ struct mpm_ctx {
   int4* d_items = nullptr;
   int32_t* d_nitems = nullptr;
   int2* d_partials = nullptr;
+  unsigned long long* d_scan_state = nullptr;  // one-pass scan: per-tile (flag, count, items) words
+  int32_t* d_scan_sync = nullptr;              // one-pass scan: tile ticket, finished tiles
   uint32_t* d_status = nullptr;
   unsigned long long* d_fp64 = nullptr;
   unsigned long long* d_tmp64 = nullptr;
@@ -171,6 +173,9 @@ KParams make_params(mpm_ctx* ctx, int src, int dst, int g) {
   P.items = ctx->d_items;
   P.n_items = ctx->d_nitems;
   P.partials = ctx->d_partials;
+  P.scan_state = ctx->d_scan_state;
+  P.scan_sync = ctx->d_scan_sync;
+  P.n_tiles = ctx->n_tiles;
   P.pin = ctx->d_pin;
   P.eps_norm = ctx->eps_norm;
   P.status = ctx->d_status;
@@ -215,9 +220,7 @@ int launch_sort(mpm_ctx* ctx, const KParams& P, cudaStream_t s) {
     if (ctx->K + 2 <= SCAN_SINGLE_MAX) {
       k_scan_single<<<1, 1024, 0, s>>>(P);
     } else {
-      k_scan_reduce<<<ctx->n_tiles, SCAN_THREADS, 0, s>>>(P);
-      k_scan_partials<<<1, SCAN_THREADS, 0, s>>>(P, ctx->n_tiles);
-      k_scan_apply<<<ctx->n_tiles, SCAN_THREADS, 0, s>>>(P);
+      k_scan_onepass<<<ctx->n_tiles, SCAN_THREADS, 0, s>>>(P);
     }
   }
   CKL();
@@ -471,6 +474,8 @@ static int ctx_alloc_init(mpm_ctx* ctx, int32_t device, const std::vector<int32_
     if ((r = dalloc(ctx, &ctx->d_items, ctx->max_items))) break;
     if ((r = dalloc(ctx, &ctx->d_nitems, 1))) break;
     if ((r = dalloc(ctx, &ctx->d_partials, ctx->n_tiles))) break;
+    if ((r = dalloc(ctx, &ctx->d_scan_state, ctx->n_tiles))) break;
+    if ((r = dalloc(ctx, &ctx->d_scan_sync, 2))) break;
     if ((r = dalloc(ctx, &ctx->d_status, 1))) break;
     if ((r = dalloc(ctx, &ctx->d_fp64, 1))) break;
     if ((r = dalloc(ctx, &ctx->d_tmp64, 1))) break;
@@ -512,6 +517,8 @@ static int ctx_alloc_init(mpm_ctx* ctx, int32_t device, const std::vector<int32_
   CKC(cudaMemsetAsync(ctx->d_nlist, 0, sizeof(int32_t) * 2, ctx->cs));
   CKC(cudaMemsetAsync(ctx->d_count, 0, sizeof(int32_t) * (ctx->K + 2), ctx->cs));
   CKC(cudaMemsetAsync(ctx->d_nitems, 0, sizeof(int32_t), ctx->cs));
+  CKC(cudaMemsetAsync(ctx->d_scan_state, 0, sizeof(unsigned long long) * ctx->n_tiles, ctx->cs));
+  CKC(cudaMemsetAsync(ctx->d_scan_sync, 0, sizeof(int32_t) * 2, ctx->cs));
   CKC(cudaMemsetAsync(ctx->d_status, 0, sizeof(uint32_t), ctx->cs));
   CKC(cudaMemsetAsync(ctx->d_fp64, 0, sizeof(unsigned long long), ctx->cs));
   CKC(cudaMemsetAsync(ctx->d_steps, 0xff, sizeof(int32_t) * ctx->n_scenes, ctx->cs));  // -1: unlimited

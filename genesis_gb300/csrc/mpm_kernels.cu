@@ -1,9 +1,9 @@
 // mpm_kernels.cu - sm_103a kernels of the MLS-MPM substep (P2G, grid op, G2P) and of the
 // per-substep particle re-sort, plus the state I/O kernels.
 //
-// One substep = k_p2g -> k_grid_op -> k_g2p -> k_scan_reduce -> k_scan_partials ->
-// k_scan_apply -> k_perm; without particles pinned to their nodes the grid op runs inside
-// k_g2p (per staged node) and k_grid_op is not launched.  Reference semantics:
+// One substep = k_p2g -> k_grid_op -> k_g2p -> k_scan_onepass (or k_scan_single) -> k_perm;
+// without particles pinned to their nodes the grid op runs inside k_g2p (per staged node) and
+// k_grid_op is not launched.  Reference semantics:
 // genesis/engine/solvers/mpm_solver.py (p2g :322-421, g2p :423-481) and
 // genesis/engine/couplers/legacy_coupler.py
 // (mpm_grid_op :356-501); see each kernel.
@@ -302,41 +302,31 @@ __device__ __forceinline__ int2 block_exclusive_scan2(int a, int b, int2& total)
 }
 }  // namespace
 
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(KParams P) {
-  const int64_t nb = P.K + 2;
-  const int64_t t0 = (int64_t)blockIdx.x * SCAN_TILE;
-  int cs = 0, is = 0;
-  for (int64_t k = t0 + threadIdx.x; k < t0 + SCAN_TILE && k < nb; k += blockDim.x) {
-    const int c = P.count[k];
-    cs += c;
-    if (k <= P.K) is += items_of(c, P.chunk);
-  }
-  int2 total;
-  block_exclusive_scan2(cs, is, total);
-  if (threadIdx.x == 0) P.partials[blockIdx.x] = total;
+// One-pass scan of the bucket counts with decoupled look-back (Merrill & Garland, "Single-pass
+// Parallel Prefix Scan with Decoupled Look-back", 2016): a CTA takes the next tile by ticket,
+// publishes its tile aggregate, sums its predecessors' words back to the nearest inclusive
+// prefix (a warp reads 32 words per round), publishes its own inclusive prefix, then writes
+// its tile's bucket offsets, P2G work items and count reset.  A predecessor holds an earlier
+// ticket, so it is already running and publishes without waiting; the wait is still bounded
+// (MPM_STATUS_WAIT on exhaustion).  The CTA that finishes last resets the tile words and the
+// ticket for the next scan.
+namespace {
+constexpr unsigned long long SCAN_AGG = 1ull << 62, SCAN_PRE = 2ull << 62;
+constexpr unsigned SCAN_SPIN_LIMIT = 1u << 20;
+__device__ __forceinline__ unsigned long long scan_word(unsigned long long flag, int c, int i) {
+  return flag | ((unsigned long long)(uint32_t)c << 31) | (unsigned long long)(uint32_t)i;
 }
+}  // namespace
 
-// One CTA: exclusive scan of the tile partials in place; writes the P2G item count.
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_partials(KParams P, int n_tiles) {
-  int2 carry = make_int2(0, 0);
-  for (int t0 = 0; t0 < n_tiles; t0 += SCAN_THREADS) {
-    const int t = t0 + threadIdx.x;
-    const int2 v = t < n_tiles ? P.partials[t] : make_int2(0, 0);
-    int2 total;
-    const int2 ex = block_exclusive_scan2(v.x, v.y, total);
-    if (t < n_tiles) P.partials[t] = make_int2(carry.x + ex.x, carry.y + ex.y);
-    carry.x += total.x;
-    carry.y += total.y;
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) *P.n_items = carry.y;
-}
-
-// Bucket offsets, P2G work items, and count reset for the next histogram.
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(KParams P) {
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_onepass(KParams P) {
   constexpr int PER = SCAN_TILE / SCAN_THREADS;
+  __shared__ int s_tile, s_last;
+  __shared__ int2 s_prefix;
+  if (threadIdx.x == 0) s_tile = atomicAdd(&P.scan_sync[0], 1);
+  __syncthreads();
+  const int tile = s_tile;
   const int64_t nb = P.K + 2;
-  const int64_t k0 = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * PER;
+  const int64_t k0 = (int64_t)tile * SCAN_TILE + (int64_t)threadIdx.x * PER;
   int c[PER];
   int cs = 0, is = 0;
 #pragma unroll
@@ -348,7 +338,44 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(KParams P) {
   }
   int2 total;
   const int2 ex = block_exclusive_scan2(cs, is, total);
-  const int2 base = P.partials[blockIdx.x];
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    if (lane == 0) atomicExch(&P.scan_state[tile], scan_word(tile == 0 ? SCAN_PRE : SCAN_AGG, total.x, total.y));
+    int pc = 0, pi = 0;
+    int j = tile - 1;
+    unsigned spins = 0;
+    while (j >= 0) {
+      const int idx = j - lane;
+      const unsigned long long w = idx >= 0 ? atomicAdd(&P.scan_state[idx], 0ull) : SCAN_PRE;
+      const unsigned long long flag = w & (3ull << 62);
+      if (__any_sync(0xffffffffu, flag == 0ull)) {  // a predecessor has not published yet
+        if (++spins > SCAN_SPIN_LIMIT) {
+          if (lane == 0) atomicOr(P.status, MPM_STATUS_WAIT);
+          break;
+        }
+        continue;
+      }
+      const unsigned pre = __ballot_sync(0xffffffffu, flag == SCAN_PRE);
+      const int stop = pre ? __ffs(pre) - 1 : 31;  // lanes 0..stop are summed
+      int vc = lane <= stop ? (int)((w >> 31) & 0x7fffffffull) : 0;
+      int vi = lane <= stop ? (int)(w & 0x7fffffffull) : 0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        vc += __shfl_xor_sync(0xffffffffu, vc, o);
+        vi += __shfl_xor_sync(0xffffffffu, vi, o);
+      }
+      pc += vc;
+      pi += vi;
+      if (pre) break;
+      j -= 32;
+    }
+    if (lane == 0) {
+      if (tile > 0) atomicExch(&P.scan_state[tile], scan_word(SCAN_PRE, pc + total.x, pi + total.y));
+      s_prefix = make_int2(pc, pi);
+    }
+  }
+  __syncthreads();
+  const int2 base = s_prefix;
   int off = base.x + ex.x, it = base.y + ex.y;
 #pragma unroll
   for (int j = 0; j < PER; ++j) {
@@ -363,6 +390,19 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(KParams P) {
     }
     off += c[j];
     P.count[k] = 0;
+  }
+  if (tile == P.n_tiles - 1 && threadIdx.x == 0) *P.n_items = base.y + total.y;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(&P.scan_sync[1], 1) == P.n_tiles - 1;
+  }
+  __syncthreads();
+  if (s_last) {  // every CTA is past its look-back: reset for the next scan
+    for (int t = threadIdx.x; t < P.n_tiles; t += blockDim.x) P.scan_state[t] = 0ull;
+    if (threadIdx.x == 0) {
+      P.scan_sync[0] = 0;
+      P.scan_sync[1] = 0;
+    }
   }
 }
 
@@ -814,6 +854,12 @@ __global__ void __launch_bounds__(256) k_g2p(KParams P) {
     const SceneDev& S = P.scenes[P.block_scene[item.x]];
     int org[3];
     block_origin(S, item.x, org);
+    // positions are software-pipelined one particle ahead; the first load overlaps the staging
+    float xn[3] = {0.f, 0.f, 0.f};
+    if ((int)threadIdx.x < cnt) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) xn[d] = D[(int64_t)(PF_POS + d) * cap + item.y + threadIdx.x];
+    }
     for (int t = threadIdx.x; t < TILE_NODES; t += T) {
       const int gx = org[0] + t / (TILE * TILE), gy = org[1] + (t / TILE) % TILE, gz = org[2] + t % TILE;
       float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -828,11 +874,13 @@ __global__ void __launch_bounds__(256) k_g2p(KParams P) {
       const bool valid = q < cnt;
       const int64_t i = item.y + q;
       int32_t key = kInactive;
-      if (valid) {
-        float x[3];
-        int tb[3];
+      float x[3] = {xn[0], xn[1], xn[2]};
+      if (q + T < cnt) {
 #pragma unroll
-        for (int d = 0; d < 3; ++d) x[d] = D[(int64_t)(PF_POS + d) * cap + i];
+        for (int d = 0; d < 3; ++d) xn[d] = D[(int64_t)(PF_POS + d) * cap + i + T];
+      }
+      if (valid) {
+        int tb[3];
         const int cell = local_cell(S, x, org, tb);
         if (cell < BLK_NODES) {
           float fx[3], w[3][3];

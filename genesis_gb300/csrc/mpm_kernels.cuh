@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "gbmpm.h"
 #include "mpm_math.cuh"
 
 namespace gbmpm {
@@ -105,6 +106,9 @@ struct KParams {
   int4* items;                 // P2G work items (bucket, begin, end, 0)
   int32_t* n_items;
   int2* partials;              // scan tile partials
+  unsigned long long* scan_state;  // one-pass scan: per tile, flag (2 bits) | count (31) | items (31)
+  int32_t* scan_sync;          // one-pass scan: [0] tile ticket, [1] finished tiles
+  int32_t n_tiles;
   uint32_t* pin;               // per-node bitmap of nodes touched by non-free particles (or null)
   int32_t* steps;              // per-scene substeps left (-1 unlimited, 0 frozen); null outside a substep
   int32_t n_scenes;
@@ -173,9 +177,7 @@ __global__ void k_particles_field(KParams P, int field, int write, int64_t s0, i
                                   int64_t n_sel, float* data);
 __global__ void k_g2p(KParams P);   // G2P + re-keying, over the P2G work items
 __global__ void k_keys(KParams P);  // re-keying only (after a state change)
-__global__ void k_scan_reduce(KParams P);
-__global__ void k_scan_partials(KParams P, int n_tiles);
-__global__ void k_scan_apply(KParams P);
+__global__ void k_scan_onepass(KParams P);
 __global__ void k_scan_single(KParams P);
 __global__ void k_perm(KParams P);
 __global__ void k_p2g(KParams P);

@@ -219,6 +219,8 @@ class MPMSolver:
             )
         if st.value & _lib.STATUS_OOB:
             raise GenesisException("MPM particles left the simulation grid (stencil out of bounds).")
+        if st.value & _lib.STATUS_WAIT:
+            raise GenesisException("MPM internal error: a bounded device-side wait ran out; the state is invalid.")
 
     def fp64_svd_count(self, reset: bool = False) -> int:
         st = ctypes.c_uint32()

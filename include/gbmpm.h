@@ -42,6 +42,7 @@ typedef enum mpm_status {
 /* Bits of the device status word returned by mpm_status_word(). */
 #define MPM_STATUS_NAN 0x1u
 #define MPM_STATUS_OOB 0x2u
+#define MPM_STATUS_WAIT 0x4u /* a bounded device-side wait ran out (internal error; results invalid) */
 
 /* ---------------------------------------------------------------- materials */
 /* Material models of genesis/engine/materials/MPM/*.py */
