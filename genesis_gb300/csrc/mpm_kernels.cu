@@ -558,7 +558,7 @@ __device__ __forceinline__ void block_origin(const SceneDev& S, int64_t key, int
 //  4. sum the warp tiles and flush with one 16-byte vector reduction per node.
 __global__ void __launch_bounds__(P2G_MAX_THREADS, 2) k_p2g(KParams P) {
   extern __shared__ __align__(16) unsigned char p2g_smem[];
-  __shared__ int s_cnt[BLK_NODES + 1], s_off[BLK_NODES + 1];
+  __shared__ int s_cnt[BLK_NODES + 1];
   __shared__ int s_touch[8];
   const int n_items = *P.n_items;
   const int T = blockDim.x, nw = T >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -569,6 +569,11 @@ __global__ void __launch_bounds__(P2G_MAX_THREADS, 2) k_p2g(KParams P) {
   const float* Sx = P.src;
   float* Dx = P.dst;
   float4* my_tile = s_tile + warp * TILE_NODES;
+  // tiles, cell counts and touch flags start zeroed; each item leaves them zeroed again
+  for (int t = threadIdx.x; t < nw * TILE_NODES; t += T) s_tile[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (threadIdx.x <= BLK_NODES) s_cnt[threadIdx.x] = 0;
+  if (threadIdx.x < 8) s_touch[threadIdx.x] = 0;
+  __syncthreads();
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
     const int4 item = P.items[it];
     const int cnt = item.z - item.y;
@@ -584,10 +589,6 @@ __global__ void __launch_bounds__(P2G_MAX_THREADS, 2) k_p2g(KParams P) {
     const SceneDev& S = P.scenes[sid];
     int org[3];
     block_origin(S, item.x, org);
-    for (int t = threadIdx.x; t < nw * TILE_NODES; t += T) s_tile[t] = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (threadIdx.x <= BLK_NODES) s_cnt[threadIdx.x] = 0;
-    if (threadIdx.x < 8) s_touch[threadIdx.x] = 0;
-    __syncthreads();
     // 1. cell ranks
     for (int j = threadIdx.x; j < cnt; j += T) {
       const int64_t si = P.perm[item.y + j];
@@ -600,7 +601,10 @@ __global__ void __launch_bounds__(P2G_MAX_THREADS, 2) k_p2g(KParams P) {
       s_cr[j] = ((uint32_t)cell << 16) | (uint32_t)r;
     }
     __syncthreads();
-    if (warp == 0) {  // exclusive scan of the 65 cell counts
+    // every warp scans the 64 cell counts into registers: lane l holds the start of cells l and
+    // l + 32 (no extra barrier; starts are fetched by shuffles, a cell ends where the next starts)
+    int offA, offB, tot_in;
+    {
       const int a = s_cnt[lane], b = s_cnt[lane + 32];
       int ia = a, ib = b;
 #pragma unroll
@@ -612,16 +616,19 @@ __global__ void __launch_bounds__(P2G_MAX_THREADS, 2) k_p2g(KParams P) {
         }
       }
       const int tot_a = __shfl_sync(0xffffffffu, ia, 31);
-      s_off[lane] = ia - a;
-      s_off[lane + 32] = tot_a + ib - b;
-      if (lane == 31) s_off[BLK_NODES] = tot_a + ib;
+      offA = ia - a;
+      offB = tot_a + ib - b;
+      tot_in = __shfl_sync(0xffffffffu, tot_a + ib, 31);  // start of the particles outside the block's cells
     }
-    __syncthreads();
-    // 2. material + stress in slot order; scatter parameters to the sorted record
-    for (int j = threadIdx.x; j < cnt; j += T) {
-      const uint32_t cr = s_cr[j];
+    // 2. material + stress in slot order; scatter parameters to the sorted record (lanes of a warp
+    //    iterate together so the offset shuffles see the whole warp)
+    for (int jb = threadIdx.x - lane; jb < cnt; jb += T) {
+      const int j = jb + lane;
+      const uint32_t cr = j < cnt ? s_cr[j] : 0u;
       const int cell = (int)(cr >> 16);
-      const int p = s_off[cell] + (int)(cr & 0xffffu);
+      const int oa = __shfl_sync(0xffffffffu, offA, cell & 31), ob = __shfl_sync(0xffffffffu, offB, cell & 31);
+      if (j >= cnt) continue;
+      const int p = (cell < 32 ? oa : (cell < BLK_NODES ? ob : tot_in)) + (int)(cr & 0xffffu);
       const int64_t slot = item.y + j;
       const int64_t si = P.perm[slot];
       Particle pt;
@@ -703,8 +710,12 @@ __global__ void __launch_bounds__(P2G_MAX_THREADS, 2) k_p2g(KParams P) {
       const int u = u0 + threadIdx.x;
       const bool has = u < 3 * BLK_NODES;
       const int cell = has ? u / 3 : 0, ox = has ? u - 3 * (u / 3) : 0;
-      const int beg = has ? s_off[cell] : 0;
-      const int len = has ? s_off[cell + 1] - beg : 0;
+      const int nx = (cell + 1) & 31;
+      const int oa = __shfl_sync(0xffffffffu, offA, cell & 31), ob = __shfl_sync(0xffffffffu, offB, cell & 31);
+      const int na = __shfl_sync(0xffffffffu, offA, nx), nb = __shfl_sync(0xffffffffu, offB, nx);
+      const int beg = cell < 32 ? oa : ob;
+      const int end = cell + 1 < 32 ? na : (cell + 1 < BLK_NODES ? nb : tot_in);
+      const int len = has ? end - beg : 0;
       const int nmax = __reduce_max_sync(0xffffffffu, len);
       if (nmax == 0) continue;  // warp-uniform
       float4 acc[3][3];
@@ -760,10 +771,13 @@ __global__ void __launch_bounds__(P2G_MAX_THREADS, 2) k_p2g(KParams P) {
     }
     __syncthreads();
     // 4. flush
+    if (threadIdx.x <= BLK_NODES) s_cnt[threadIdx.x] = 0;  // every warp's scan read it before phase 2 ended
     for (int t = threadIdx.x; t < TILE_NODES; t += T) {
       float4 g = s_tile[t];
+      s_tile[t] = make_float4(0.f, 0.f, 0.f, 0.f);
       for (int ww = 1; ww < nw; ++ww) {
         const float4 h = s_tile[ww * TILE_NODES + t];
+        s_tile[ww * TILE_NODES + t] = make_float4(0.f, 0.f, 0.f, 0.f);
         g.x += h.x;
         g.y += h.y;
         g.z += h.z;
@@ -778,6 +792,7 @@ __global__ void __launch_bounds__(P2G_MAX_THREADS, 2) k_p2g(KParams P) {
     }
     __syncthreads();
     if (threadIdx.x < 8 && s_touch[threadIdx.x]) {
+      s_touch[threadIdx.x] = 0;
       const int bx = org[0] / BLK + (threadIdx.x >> 2), by = org[1] / BLK + ((threadIdx.x >> 1) & 1),
                 bz = org[2] / BLK + (threadIdx.x & 1);
       if (bx < S.bres[0] && by < S.bres[1] && bz < S.bres[2]) {
