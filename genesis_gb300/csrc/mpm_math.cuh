@@ -74,8 +74,8 @@ template <> struct Eps<double> { static constexpr double v = 2.220446049250313e-
 // Jacobi threshold): rotating it would swap exact degeneracies (F = I) for rounding noise
 // in U and V, which the corotated stress 2 mu (F - U V^T) F^T amplifies by mu.
 template <typename T>
-GB_HD void jacobi_rotate(T& app, T& aqq, T& apq, T& arp, T& arq, T* V, int p, int q) {
-  if (!(gabs(apq) > Eps<T>::v * gsqrt(gabs(app * aqq)))) return;
+GB_HD bool jacobi_rotate(T& app, T& aqq, T& apq, T& arp, T& arq, T* V, int p, int q) {
+  if (!(gabs(apq) > Eps<T>::v * gsqrt(gabs(app * aqq)))) return false;
   const T theta = gdiv_fast(aqq - app, T(2) * apq);
   const T at = gabs(theta);
   T t = (at < T(1e18)) ? gdiv_fast(T(1), at + gsqrt(theta * theta + T(1))) : gdiv_fast(T(0.5), at);
@@ -95,6 +95,7 @@ GB_HD void jacobi_rotate(T& app, T& aqq, T& apq, T& arp, T& arq, T* V, int p, in
     V[r * 3 + p] = c * vp - s * vq;
     V[r * 3 + q] = s * vp + c * vq;
   }
+  return true;
 }
 
 // Swap columns i and j of B and V and negate the new column j (keeps det V = +1).
@@ -156,9 +157,11 @@ GB_HD T svd3(const T* A, T* U, T* sig, T* V) {
   for (int k = 0; k < 9; ++k) V[k] = (k % 4 == 0) ? T(1) : T(0);
 #pragma unroll
   for (int sweep = 0; sweep < SWEEPS; ++sweep) {
-    jacobi_rotate(s00, s11, s01, s02, s12, V, 0, 1);
-    jacobi_rotate(s00, s22, s02, s01, s12, V, 0, 2);
-    jacobi_rotate(s11, s22, s12, s01, s02, V, 1, 2);
+    // a sweep that rotates nothing leaves S unchanged, so every later sweep would skip too
+    bool any = jacobi_rotate(s00, s11, s01, s02, s12, V, 0, 1);
+    any = jacobi_rotate(s00, s22, s02, s01, s12, V, 0, 2) || any;
+    any = jacobi_rotate(s11, s22, s12, s01, s02, V, 1, 2) || any;
+    if (!any) break;
   }
   // B = A V
   T B[9];
