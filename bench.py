@@ -123,6 +123,10 @@ def cpu_baseline(target_s=10.0):
     t0 = time.perf_counter()
     O.run(sc, oms, st, k, dtype=np.float32, threads=cores)
     dt = time.perf_counter() - t0
+    # the same restatement on one thread (one substep of the full scene)
+    t0 = time.perf_counter()
+    O.run(sc, oms, st, 1, dtype=np.float32, threads=1)
+    dt1 = time.perf_counter() - t0
     return {
         "value": n * k / dt,
         "unit": "particle-substeps/s",
@@ -130,6 +134,7 @@ def cpu_baseline(target_s=10.0):
         "kind": "port",
         "sample": f"full workload ({n} particles), {k} substeps after 1 warm-up substep, fp32 oracle, "
         f"OpenMP {cores} threads, {dt:.1f} s",
+        "single_thread": {"value": n / dt1, "cores": 1, "sample": f"1 substep of the full workload, {dt1:.1f} s"},
     }
 
 
@@ -391,13 +396,40 @@ def _timed(fn):
     return e0.elapsed_time(e1) / 1e3
 
 
+def run_c1(substeps=100, repeats=5):
+    """The small plain case: 17,576-particle elastic cube (side 0.2 at (0.5, 0.5, 0.4), regular
+    sampler at particle size 1/128, jitter +-0.25 dx) on a 65^3 grid, dt = 2e-4, 100 substeps.
+    Its particle state (~4 MB) is L2-resident and the substep is launch-bound."""
+    import torch
+
+    import genesis_gb300 as gs
+
+    scene = gs.Scene(sim_options=gs.options.SimOptions(dt=2e-4, substeps=1),
+                     mpm_options=gs.options.MPMOptions(lower_bound=(0, 0, 0), upper_bound=(1, 1, 1), grid_density=64,
+                                                       particle_size=1.0 / 128))
+    cube = scene.add_entity(material=gs.materials.MPM.Elastic(sampler="regular"),
+                            morph=gs.morphs.Box(pos=(0.5, 0.5, 0.4), size=(0.2, 0.2, 0.2)))
+    scene.build()
+    rng = np.random.default_rng(SEED)
+    p = cube.init_particles + rng.uniform(-0.25 / 64, 0.25 / 64, size=cube.init_particles.shape)
+    cube.set_particles_pos(torch.tensor(p, dtype=torch.float32, device="cuda"))
+    solver = scene.sim.mpm_solver
+    n = solver.n_particles
+    solver.substeps(substeps)
+    t = min(_timed(lambda: solver.substeps(substeps)) for _ in range(repeats))
+    solver.check_state()
+    return {"workload": "17,576-particle elastic cube, 65^3 grid, dt 2e-4, 100 substeps (L2-resident)",
+            "n_particles": n, "value": n * substeps / t, "us_per_substep": t / substeps * 1e6,
+            "unit": "particle-substeps/s"}
+
+
 def run_forms(batched_substeps=200, n_requests=48):
     """Batched (256 uneven scenes, one context) and served (continuous batching) forms, each
     against the plain form run scene by scene (one context per scene) on the same workload."""
     from genesis_gb300.batched import BatchedMPM, batched_workload
     from genesis_gb300.serve import MPMServer, serving_workload
 
-    out = {}
+    out = {"plain_small": run_c1()}
     specs = batched_workload(n_scenes=256, seed=1234)
     b = BatchedMPM(specs, tune=True)
     b.step(2)

@@ -41,4 +41,6 @@ void shim_material_f32(int type, int flags, double mu, double lam, double alpha,
   material_update<float>(M, Ft, U, s, V, Jp, actu, mdir, eps, F_new, jn, P);
   *Jp_new = jn;
 }
+
+void shim_bspline_w(float fx, float* w) { bspline_w<float>(fx, w); }
 }

@@ -6,6 +6,8 @@ import subprocess
 import tempfile
 
 import numpy as np
+
+import genesis_gb300 as gs
 import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -26,6 +28,8 @@ def shim():
     lib.shim_material_f32.restype = None
     lib.shim_material_f32.argtypes = [ctypes.c_int, ctypes.c_int, d, d, d, d, d, d, d, d, P, ctypes.c_float,
                                       ctypes.c_float, P, ctypes.c_float, P, P, P]
+    lib.shim_bspline_w.restype = None
+    lib.shim_bspline_w.argtypes = [ctypes.c_float, P]
     return lib
 
 
@@ -137,3 +141,68 @@ def test_corotated_stress_has_no_rounding_noise_near_identity(shim):
                                jn.ctypes.data, P.ctypes.data)
         worst = max(worst, np.abs(P).max())
     assert worst <= 2 * cm.mu * 1e-9, worst
+
+
+# ---- known-answer tests from the mathematics of the method (no reference output needed)
+
+def _run_material(shim, cm, Ft, Jp=1.0):
+    eps = np.float32(np.finfo(np.float32).eps)
+    Ft = np.ascontiguousarray(Ft, np.float32).reshape(9)
+    Fn, jn, P = np.zeros(9, np.float32), np.zeros(1, np.float32), np.zeros(9, np.float32)
+    md = np.array([0, 0, 1], np.float32)
+    shim.shim_material_f32(*_mat_args(cm), Ft.ctypes.data, float(Jp), 0.0, md.ctypes.data, eps, Fn.ctypes.data,
+                           jn.ctypes.data, P.ctypes.data)
+    return Fn.reshape(3, 3).astype(np.float64), float(jn[0]), P.reshape(3, 3).astype(np.float64)
+
+
+def test_bspline_partition_of_unity_and_zero_first_moment(shim):
+    """Quadratic B-spline weights sum to 1 and sum_o w_o (o - fx) = 0 for fx in [0.5, 1.5)."""
+    w = np.zeros(3, np.float32)
+    for fx in np.linspace(0.5, 1.5, 41, endpoint=False):
+        shim.shim_bspline_w(float(fx), w.ctypes.data)
+        assert abs(w.sum() - 1.0) < 1e-6
+        assert abs(float(np.dot(w, np.arange(3) - np.float32(fx)))) < 1e-6
+        assert np.all(w >= 0)
+
+
+@pytest.mark.parametrize("name", ["Elastic", "Liquid", "Snow"])
+def test_rest_state_has_zero_stress(shim, oracle, name):
+    """F = I gives exactly zero stress (corotated: F - UV^T = 0 and J(J - 1) = 0)."""
+    cm = getattr(gs.materials.MPM, name)().to_c(0)
+    Fn, jn, P = _run_material(shim, cm, np.eye(3))
+    assert np.abs(P).max() == 0.0, P
+    assert np.allclose(Fn, np.eye(3), atol=1e-7)
+
+
+def test_sand_expansion_returns_to_identity(shim):
+    """Drucker-Prager: a state whose log-strain trace (+ Jp) is non-negative maps to Sigma_new = I
+    and Jp_new = trace (sand.py:58-61)."""
+    cm = gs.materials.MPM.Sand().to_c(0)
+    rng = np.random.default_rng(3)
+    for _ in range(20):
+        Q1, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        Q2, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        Q1 *= np.sign(np.linalg.det(Q1))
+        Q2 *= np.sign(np.linalg.det(Q2))
+        sig = rng.uniform(1.01, 1.2, size=3)  # stretched: log strains > 0
+        Fn, jn, _ = _run_material(shim, cm, Q1 @ np.diag(sig) @ Q2.T, Jp=0.0)
+        R = Q1 @ Q2.T  # U I V^T
+        assert np.allclose(Fn, R, atol=2e-5), (Fn, R)
+        assert abs(jn - np.log(sig).sum()) < 2e-5
+
+
+def test_snow_clamps_singular_values(shim):
+    """Snow keeps the singular values of F_new inside [1 - 2.5e-2, 1 + 4.5e-3] (snow.py:49-57)."""
+    cm = gs.materials.MPM.Snow().to_c(0)
+    rng = np.random.default_rng(4)
+    for _ in range(20):
+        Q1, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        Q2, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        Q1 *= np.sign(np.linalg.det(Q1))
+        Q2 *= np.sign(np.linalg.det(Q2))
+        sig = rng.uniform(0.9, 1.1, size=3)
+        Fn, jn, _ = _run_material(shim, cm, Q1 @ np.diag(sig) @ Q2.T, Jp=1.0)
+        s = np.linalg.svd(Fn, compute_uv=False)
+        assert s.min() >= 1 - 2.5e-2 - 1e-5 and s.max() <= 1 + 4.5e-3 + 1e-5, s
+        clamped = np.clip(sig, 1 - 2.5e-2, 1 + 4.5e-3)
+        assert abs(jn - np.prod(sig / clamped)) < 1e-5

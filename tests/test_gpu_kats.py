@@ -1,0 +1,192 @@
+"""Known-answer tests of the CUDA substep that follow from the mathematics of MLS-MPM with
+quadratic B-splines (no reference output needed), plus edge cases: an empty context, a single
+particle, particles exactly on cell faces.  Each drives libgbmpm through the C ABI, using the
+split-phase entry points to read the grid after P2G (momentum, mass) and after the grid op
+(velocity, mass)."""
+
+import numpy as np
+import pytest
+import torch
+
+from capi_helpers import Ctx, material_record, scene_record
+
+pytestmark = pytest.mark.gpu
+
+DT = 2e-4
+DENSITY = 32.0  # dx = 1/32, 33^3 nodes over the unit cube
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _build():
+    import __graft_entry__ as g
+
+    g.build()
+
+
+def _ctx(n, gravity=(0.0, 0.0, 0.0), mu=0.0, lam=0.0):
+    from genesis_gb300 import _lib
+
+    sc = scene_record(_lib, DT, n, density=DENSITY, gravity=gravity)
+    return Ctx([sc], [material_record(_lib, 0, 0, 0, mu, lam)])
+
+
+def _cloud(n, lo=0.35, hi=0.65, seed=0):
+    return np.random.default_rng(seed).uniform(lo, hi, size=(n, 3))
+
+
+def _split_substep(c):
+    """One substep through the split phases; returns (P2G grid, velocity grid)."""
+    c.call("mpm_substep_pre", c.stream)
+    g1 = c.grid(0)
+    c.call("mpm_substep_grid_op", c.stream)
+    g2 = c.grid(0)
+    c.call("mpm_substep_post", c.stream)
+    torch.cuda.synchronize()
+    return g1, g2
+
+
+def test_p2g_conserves_mass_and_momentum_with_affine_and_stress():
+    """sum_i m_i = N m_p and sum_i p_i = m_p sum_p v_p for any C and stress, because
+    sum_o w_o = 1 and sum_o w_o (x_o - x_p) = 0."""
+    n = 4000
+    c = _ctx(n, mu=1e5, lam=2e5)
+    rng = np.random.default_rng(1)
+    x = _cloud(n)
+    c.add(0, 1, 0, x, 0)
+    v = rng.normal(size=(n, 3))
+    C = rng.normal(size=(n, 3, 3)) * 5.0
+    F = np.eye(3) + 0.05 * rng.normal(size=(n, 3, 3))
+    c.set_state(0, 1, pos=x, vel=v, C=C, F=F, Jp=np.ones(n), active=np.ones(n, bool))
+    g1, _ = _split_substep(c)
+    m_total = g1[..., 3].sum()
+    m_p = m_total / n
+    p_sum = g1[..., :3].reshape(-1, 3).sum(0)
+    want = m_p * v.sum(0)
+    assert np.linalg.norm(p_sum - want) <= 1e-5 * m_p * np.abs(v).sum()
+    c.close()
+
+
+def test_grid_op_adds_gravity_and_boundary_zeroes_only_outward_components():
+    """v_o = p_o / m_o + dt g away from walls; at nodes beyond a wall only the outward velocity
+    component is zeroed (boundaries.py:22-32 with restitution 0)."""
+    n = 3000
+    g = (0.3, -0.2, -9.81)
+    c = _ctx(n, gravity=g)
+    x = _cloud(n, 0.05, 0.95, seed=2)  # reaches the boundary band [0, 3dx] and [1 - 3dx, 1]
+    c.add(0, 1, 0, x, 0)
+    rng = np.random.default_rng(5)
+    v = rng.normal(size=(n, 3))
+    c.set_state(0, 1, pos=x, vel=v, C=np.zeros((n, 3, 3)), F=np.tile(np.eye(3), (n, 1, 1)), Jp=np.ones(n),
+                active=np.ones(n, bool))
+    g1, g2 = _split_substep(c)
+    mass = g1[..., 3]
+    has = mass > np.finfo(np.float32).eps
+    free = g1[..., :3] / np.where(has, mass, 1.0)[..., None] + DT * np.array(g)
+    dx = 1.0 / DENSITY
+    idx = np.stack(np.meshgrid(*[np.arange(s) for s in mass.shape], indexing="ij"), -1)
+    pos = idx * dx
+    lo, hi = 3 * dx, 1.0 - 3 * dx
+    for d in range(3):
+        clear = np.abs(free[..., d]) > 1e-5  # the sign test is unambiguous in float32
+        out_hi = has & clear & (pos[..., d] >= np.float32(hi)) & (free[..., d] >= 0)
+        out_lo = has & clear & (pos[..., d] <= np.float32(lo)) & (free[..., d] <= 0)
+        inside = has & clear & ~out_hi & ~out_lo
+        assert np.all(g2[..., d][out_hi | out_lo] == 0.0)
+        err = np.abs(g2[..., d][inside] - free[..., d][inside])
+        assert err.max() <= 1e-5 * (1 + np.abs(free[..., d][inside]).max())
+    assert (has & ((pos <= lo) | (pos >= hi)).any(-1)).any(), "the cloud must reach the wall band"
+    assert np.all(g2[..., 3] == mass)
+    c.close()
+
+
+def test_uniform_velocity_is_reproduced_with_zero_affine():
+    """A rigid translation u (C = 0, no stress, no gravity) comes back from G2P as v = u, C = 0
+    and x' = x + dt u."""
+    n = 5000
+    c = _ctx(n)
+    x = _cloud(n, seed=3)
+    u = np.array([0.7, -0.4, 0.25])
+    c.add(0, 1, 0, x, 0)
+    c.set_state(0, 1, pos=x, vel=np.tile(u, (n, 1)), C=np.zeros((n, 3, 3)), F=np.tile(np.eye(3), (n, 1, 1)),
+                Jp=np.ones(n), active=np.ones(n, bool))
+    _split_substep(c)
+    st = c.get_state(0, 1, n)
+    assert np.abs(st["vel"] - u).max() <= 1e-5 * np.abs(u).max()
+    assert np.abs(st["C"]).max() <= 1e-3 * np.abs(u).max()
+    assert np.abs(st["pos"] - (x + DT * u)).max() <= 2e-6
+    c.close()
+
+
+def test_apic_reproduces_an_affine_velocity_field():
+    """With v_p = A x_p + b and C_p = A (no stress, no gravity), APIC transfers the linear field
+    exactly: G2P returns v = A x_p + b and C = A (quadratic B-splines reproduce linear fields and
+    D_p = dx^2/4 I)."""
+    n = 6000
+    c = _ctx(n)
+    rng = np.random.default_rng(4)
+    x = _cloud(n, seed=4)
+    A = rng.normal(size=(3, 3)) * 2.0
+    b = rng.normal(size=3)
+    v = x @ A.T + b
+    c.add(0, 1, 0, x, 0)
+    c.set_state(0, 1, pos=x, vel=v, C=np.tile(A, (n, 1, 1)), F=np.tile(np.eye(3), (n, 1, 1)), Jp=np.ones(n),
+                active=np.ones(n, bool))
+    _split_substep(c)
+    st = c.get_state(0, 1, n)
+    scale = np.abs(v).max()
+    assert np.abs(st["vel"] - v).max() <= 2e-5 * scale
+    assert np.abs(st["C"] - A).max() <= 2e-4 * np.abs(A).max()
+    c.close()
+
+
+def test_empty_context_runs():
+    c = _ctx(0)
+    c.substeps(4)
+    torch.cuda.synchronize()
+    assert c.status() == (0, 0)
+    c.close()
+
+
+def test_single_particle_conserves_mass_and_falls_freely():
+    c = _ctx(1, gravity=(0.0, 0.0, -9.81), mu=1e4, lam=1e4)
+    x = np.array([[0.503, 0.511, 0.52]])  # generic offsets: all 27 stencil weights non-zero
+    c.add(0, 1, 0, x, 0)
+    c.substeps(10)
+    st = c.get_state(0, 1, 1)
+    # free fall: v_z = -9.81 * 10 dt, exact to float rounding (no stress at F = I, C stays 0)
+    assert abs(st["vel"][0, 2] + 9.81 * 10 * DT) <= 1e-6
+    assert np.abs(st["vel"][0, :2]).max() <= 1e-7
+    g1, _ = _split_substep(c)
+    m = g1[..., 3]
+    assert np.count_nonzero(m) == 27
+    c.close()
+
+
+def test_particles_on_cell_faces_match_oracle(oracle):
+    """Positions with x * inv_dx - 0.5 exactly integral (fx = 0.5, the stencil's lower edge) and
+    exactly on node planes (fx = 1.0)."""
+    from genesis_gb300 import _lib
+
+    k = np.arange(10, 22, dtype=np.float64)
+    pts = []
+    for i in k:
+        pts.append(((i + 0.5) / DENSITY, (i + 1.0) / DENSITY, 0.5 + (i - 16) / DENSITY))
+    x = np.array(pts)
+    n = len(x)
+    c = _ctx(n, gravity=(0.0, 0.0, -9.81), mu=3e4, lam=2e4)
+    c.add(0, 1, 0, x, 0)
+    rng = np.random.default_rng(9)
+    v = rng.normal(size=(n, 3)) * 0.1
+    c.set_state(0, 1, pos=x, vel=v, C=np.zeros((n, 3, 3)), F=np.tile(np.eye(3), (n, 1, 1)), Jp=np.ones(n),
+                active=np.ones(n, bool))
+    g1, _ = _split_substep(c)
+    sc = oracle.make_scene(DT, grid_density=DENSITY, particle_size=0.01 * 64.0 / DENSITY, gravity=(0.0, 0.0, -9.81))
+    mat = oracle.make_material(0, 3e4, 2e4, 1000.0)
+    st = dict(pos=x, vel=v, C=np.zeros((n, 3, 3)), F=np.tile(np.eye(3), (n, 1, 1)), Jp=np.ones(n),
+              mat=np.zeros(n, np.int32), active=np.ones(n, bool))
+    out, grid, _ = oracle.run(sc, [mat], st, 1, want_grid=True)
+    ref_m = grid[..., 3]
+    assert np.abs(g1[..., 3] - ref_m).max() <= 1e-6 * ref_m.max()
+    got = c.get_state(0, 1, n)
+    assert np.abs(got["pos"] - out["pos"]).max() <= 1e-6
+    c.close()
