@@ -245,6 +245,7 @@ def run_ours(args, rank, world):
     for _ in range(args.warmup):
         scene.step()
     torch.cuda.synchronize()
+    start_state = solver.get_state()  # the per-kernel region below replays the same trajectory
 
     # --- timed region: K steps of 10 substeps, CUDA graph path, inputs resident in HBM
     clocks = ClockSampler(torch.cuda.current_device())
@@ -269,7 +270,11 @@ def run_ours(args, rank, world):
         ms, total_units = reduce_over_ranks(ms, total_units, "cuda")
     value = total_units / (ms / 1e3)
 
-    # --- per-kernel durations over a second timed region of the same K steps (events per kernel)
+    # --- per-kernel durations over a second timed region: the same K steps from the same state
+    # (events around every kernel, no graph)
+    solver.set_state(0, start_state)
+    solver.substeps(2)
+    torch.cuda.synchronize()
     lib.mpm_set_profiling(solver.ctx, 1)
     lib.mpm_kernel_times(solver.ctx, None, None, 1)
     for _ in range(args.steps):

@@ -34,6 +34,7 @@ STATUS_NAMES = {
 STATUS_NAN = 0x1
 STATUS_OOB = 0x2
 STATUS_WAIT = 0x4
+STATUS_BAD_INDEX = 0x8
 
 # material types / flags (mpm_material_type, MPM_MATF_*)
 MAT_ELASTIC, MAT_LIQUID, MAT_SAND, MAT_SNOW, MAT_ELASTOPLASTIC, MAT_MUSCLE = range(6)
@@ -112,6 +113,7 @@ _SIGNATURES = {
     "mpm_scene_grid_res": (c_int32, [_P, c_int64, ctypes.POINTER(c_int32)]),
     "mpm_set_profiling": (c_int32, [_P, c_int32]),
     "mpm_kernel_times": (c_int32, [_P, ctypes.POINTER(c_double), ctypes.POINTER(c_int64), c_int32]),
+    "mpm_render_fields": (c_int32, [_P, c_int64, c_int64, _P, _P, _P, c_int64, c_int32, _P, _P, _P, _P, _P]),
     "mpm_version": (c_int32, []),
     "mpm_ctx_create_pool": (c_int32, [ctypes.c_void_p, c_int32, ctypes.POINTER(c_void_p)]),
     "mpm_scene_admit": (c_int32, [_P, c_int64, ctypes.c_void_p, ctypes.c_void_p, c_int32, c_int64, _P, _P, c_int32, _P]),

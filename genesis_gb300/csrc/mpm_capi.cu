@@ -835,6 +835,36 @@ int mpm_get_grid(mpm_ctx* ctx, int64_t scene, float* out, void* stream) {
   return leave(ctx, stream);
 }
 
+int mpm_render_fields(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end, float* pos_out, float* vel_out,
+                      uint8_t* active_out, int64_t n_vverts, int32_t n_supports, const int32_t* support_idx,
+                      const float* support_w, float* vvert_pos_out, uint8_t* vvert_active_out, void* stream) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (!scene_range_ok(ctx, scene_begin, scene_end)) return fail(ctx, MPM_ERR_BAD_ARG, "bad scene range");
+  if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "render fields inside a substep");
+  if (!pos_out || !active_out) return fail(ctx, MPM_ERR_BAD_ARG, "pos_out and active_out are required");
+  if (n_vverts < 0 || (n_vverts > 0 && (n_supports <= 0 || !support_idx || !support_w || !vvert_pos_out)))
+    return fail(ctx, MPM_ERR_BAD_ARG, "bad visual-vertex arguments");
+  int r = enter(ctx, stream);
+  if (r) return r;
+  KParams P = make_params(ctx, ctx->cur, ctx->cur, ctx->cur);
+  k_get_state<<<ctx->io_blocks, 256, 0, ctx->cs>>>(P, scene_begin, scene_end, pos_out, vel_out, nullptr, nullptr,
+                                                    nullptr, active_out);
+  CKL();
+  const SceneDev& last = ctx->scenes_h[scene_end - 1];
+  const int64_t rows = last.p_begin + last.n_particles - ctx->scenes_h[scene_begin].p_begin;
+  if (n_vverts > 0) {
+    k_render_vverts<<<ctx->io_blocks, 256, 0, ctx->cs>>>(P, scene_begin, scene_end, pos_out, active_out, n_vverts,
+                                                        n_supports, support_idx, support_w, vvert_pos_out,
+                                                        vvert_active_out);
+    CKL();
+  }
+  if (rows > 0) {
+    k_render_nowhere<<<ctx->io_blocks, 256, 0, ctx->cs>>>(rows, active_out, pos_out);
+    CKL();
+  }
+  return leave(ctx, stream);
+}
+
 int mpm_count_touched_nodes(mpm_ctx* ctx, int64_t* out_host, void* stream) {
   if (!ctx || !out_host) return MPM_ERR_BAD_ARG;
   const int g = ctx->phase == 0 ? (ctx->cur ^ 1) : ctx->cur;

@@ -1033,6 +1033,44 @@ __global__ void k_get_grid(KParams P, int64_t scene, float* out) {
   }
 }
 
+// Visual vertices of _kernel_update_render_fields (mpm_solver.py:795-803): support-weighted sum
+// of the particles' positions (`pos` holds the rows of scenes [s0, s1) in get_state order).
+__global__ void k_render_vverts(KParams P, int64_t s0, int64_t s1, const float* pos, const uint8_t* active,
+                                int64_t n_vverts, int32_t n_supports, const int32_t* support_idx,
+                                const float* support_w, float* vpos, uint8_t* vactive) {
+  const int64_t total = (s1 - s0) * n_vverts;
+  for (int64_t i = grid_stride_begin(); i < total; i += grid_stride_step()) {
+    const int64_t b = i / n_vverts, v = i % n_vverts;
+    const SceneDev& S = P.scenes[s0 + b];
+    const int64_t base = S.p_begin - P.scenes[s0].p_begin, n_s = S.n_particles;
+    float acc[3] = {0.f, 0.f, 0.f};
+    for (int j = 0; j < n_supports; ++j) {
+      const int64_t k = support_idx[v * n_supports + j];
+      if (k < 0 || k >= n_s) {
+        atomicOr(P.status, MPM_STATUS_BAD_INDEX);
+        continue;
+      }
+      const float w = support_w[v * n_supports + j];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) acc[d] += pos[(base + k) * 3 + d] * w;
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) vpos[i * 3 + d] = acc[d];
+    const int64_t k0 = n_supports > 0 ? support_idx[v * n_supports] : -1;
+    if (vactive) vactive[i] = (k0 >= 0 && k0 < n_s) ? active[base + k0] : 0;
+  }
+}
+
+// particles_render.pos of an inactive particle is gu.qd_nowhere() (utils/geom.py:355-357).
+__global__ void k_render_nowhere(int64_t rows, const uint8_t* active, float* pos) {
+  for (int64_t r = grid_stride_begin(); r < rows; r += grid_stride_step()) {
+    if (active[r]) continue;
+    pos[r * 3 + 0] = -2333333.f;
+    pos[r * 3 + 1] = -6666666.f;
+    pos[r * 3 + 2] = -5201314.f;
+  }
+}
+
 __global__ void k_count_touched(KParams P, unsigned long long* out) {
   const int n_cur = *P.nlist;
   unsigned long long c = 0;

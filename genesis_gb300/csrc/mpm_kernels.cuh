@@ -183,6 +183,10 @@ __global__ void k_perm(KParams P);
 __global__ void k_p2g(KParams P);
 __global__ void k_grid_op(KParams P);
 __global__ void k_get_grid(KParams P, int64_t scene, float* out);
+__global__ void k_render_vverts(KParams P, int64_t s0, int64_t s1, const float* pos, const uint8_t* active,
+                                int64_t n_vverts, int32_t n_supports, const int32_t* support_idx,
+                                const float* support_w, float* vpos, uint8_t* vactive);
+__global__ void k_render_nowhere(int64_t rows, const uint8_t* active, float* pos);
 __global__ void k_count_touched(KParams P, unsigned long long* out);
 
 }  // namespace gbmpm

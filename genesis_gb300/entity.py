@@ -53,6 +53,36 @@ class MPMEntity:
         self._n_particles = len(self._particles)
         self.active = not isinstance(morph, Nowhere)
         self._tgt = {"pos": None, "vel": None, "act": None}
+        self._vverts = np.zeros((0, 3), dtype=np.float64)
+        self._vvert_support_idx = np.zeros((0, 0), dtype=np.int32)
+        self._vvert_support_w = np.zeros((0, 0), dtype=np.float32)
+
+    # ------------------------------------------------------------------ visual vertices
+    def set_vverts(self, verts) -> None:
+        """Attach visual-mesh vertices [V, 3] (the reference takes them from the entity's visual
+        mesh) and compute each vertex's support particles and weights from the sampled particles as
+        particle_entity.py:193-232 does: the n_support_neighbors nearest particles ordered by
+        (distance, index); with P the supports' positions relative to the last one, b = pinv(P) (v -
+        p_last), weights (b, 1 - sum b).  Indices are solver-level (entity particle start + local)."""
+        v = np.ascontiguousarray(np.asarray(verts, dtype=np.float64).reshape(-1, 3))
+        k = min(self._solver.n_vvert_supports, self._n_particles)
+        dist2 = np.sum(np.square(v[:, None, :] - self._particles[None, :, :]), axis=2)
+        idx = np.argpartition(dist2, k - 1, axis=1)[:, :k]
+        rows = np.arange(len(v))[:, None]
+        order = np.lexsort((idx, dist2[rows, idx]))
+        idx = np.clip(idx[rows, order], 0, self._n_particles - 1)
+        ps = self._particles[idx]
+        Ps = ps[:, :-1].swapaxes(-2, -1) - np.expand_dims(ps[:, -1], axis=-1)
+        b = np.einsum("vij,vj->vi", np.linalg.pinv(Ps), v - ps[:, -1])
+        w = np.concatenate([b, 1.0 - b.sum(axis=1, keepdims=True)], axis=1)
+        self._vverts = v
+        self._vvert_support_idx = (idx + self._particle_start).astype(np.int32)
+        self._vvert_support_w = w.astype(np.float32)
+        self._solver._vverts_changed()
+
+    @property
+    def n_vverts(self) -> int:
+        return len(self._vverts)
 
     # ------------------------------------------------------------------ solver plumbing
     def _add_to_solver(self):

@@ -264,6 +264,54 @@ class MPMSolver:
         _lib.check(self._lib.mpm_get_grid(self._ctx, scene, _lib.ptr(out), _stream_handle()), self._ctx, "mpm_get_grid")
         return out
 
+    # ------------------------------------------------------------------ render fields
+    @property
+    def n_vvert_supports(self) -> int:
+        vis = getattr(self._scene, "vis_options", None)
+        return int(vis.n_support_neighbors) if vis is not None else 12  # VisOptions default (options/vis.py:157)
+
+    def _vverts_changed(self) -> None:
+        self._vvert_dev = None
+
+    def update_render_fields(self) -> None:
+        """mpm_solver.py:780-803: fills `particles_render` ({pos, vel, active}, [B, N, ...]; inactive
+        particles at the reference's nowhere point) and `vverts_render` ({pos, active}, [B, V, ...])
+        from the current state, on the device."""
+        B, N = self._B, self.n_particles
+        if getattr(self, "_render", None) is None or self._render["pos"].shape[:2] != (B, N):
+            self._render = {"pos": torch.empty((B, N, 3), device="cuda"), "vel": torch.empty((B, N, 3), device="cuda"),
+                            "active": torch.empty((B, N), dtype=torch.bool, device="cuda")}
+        ents = [e for e in self._entities if e.n_vverts > 0]
+        if getattr(self, "_vvert_dev", None) is None:
+            if ents:
+                k = max(e._vvert_support_idx.shape[1] for e in ents)
+                idx = np.concatenate([np.pad(e._vvert_support_idx, ((0, 0), (0, k - e._vvert_support_idx.shape[1])),
+                                             mode="edge") for e in ents])
+                w = np.concatenate([np.pad(e._vvert_support_w, ((0, 0), (0, k - e._vvert_support_w.shape[1])))
+                                    for e in ents])
+                self._vvert_dev = (torch.as_tensor(idx, device="cuda").contiguous(),
+                                   torch.as_tensor(w, device="cuda").contiguous())
+            else:
+                self._vvert_dev = (None, None)
+        sidx, sw = self._vvert_dev
+        V = 0 if sidx is None else sidx.shape[0]
+        vpos = torch.empty((B, V, 3), device="cuda")
+        vact = torch.empty((B, V), dtype=torch.bool, device="cuda")
+        _lib.check(self._lib.mpm_render_fields(
+            self._ctx, 0, B, _lib.ptr(self._render["pos"]), _lib.ptr(self._render["vel"]), _lib.ptr(self._render["active"]),
+            V, 0 if sidx is None else sidx.shape[1], None if sidx is None else _lib.ptr(sidx),
+            None if sw is None else _lib.ptr(sw), _lib.ptr(vpos) if V else None, _lib.ptr(vact) if V else None,
+            _stream_handle()), self._ctx, "mpm_render_fields")
+        self._vverts_render = {"pos": vpos, "active": vact}
+
+    @property
+    def particles_render(self):
+        return self._render
+
+    @property
+    def vverts_render(self):
+        return self._vverts_render
+
     def set_gravity(self, gravity, envs_idx=None) -> None:
         g = np.asarray(gravity, dtype=np.float64).reshape(-1, 3)
         envs = list(range(self._B)) if envs_idx is None else [int(e) for e in np.atleast_1d(envs_idx)]

@@ -43,6 +43,7 @@ typedef enum mpm_status {
 #define MPM_STATUS_NAN 0x1u
 #define MPM_STATUS_OOB 0x2u
 #define MPM_STATUS_WAIT 0x4u /* a bounded device-side wait ran out (internal error; results invalid) */
+#define MPM_STATUS_BAD_INDEX 0x8u /* an index array passed to a kernel held an out-of-range entry (skipped) */
 
 /* ---------------------------------------------------------------- materials */
 /* Material models of genesis/engine/materials/MPM/*.py */
@@ -180,6 +181,21 @@ int mpm_substep_post(mpm_ctx* ctx, void* stream);
  * after mpm_substep_pre it holds (momentum xyz, mass); after mpm_substep_grid_op it
  * holds (vel_out xyz, mass).  Replaces reading MPMSolver.grid (mpm_solver.py:137-148). */
 int mpm_get_grid(mpm_ctx* ctx, int64_t scene, float* out, void* stream);
+
+/* Render fields (mpm_solver.py:780-803, _kernel_update_render_fields) of scenes
+ * [scene_begin, scene_end), in the reference [B, N] row order of mpm_get_state:
+ *   pos_out [B,N,3]: the particle position, or the reference's "nowhere" point
+ *     (-2333333, -6666666, -5201314) for an inactive particle; vel_out [B,N,3]; active_out [B,N];
+ *   vvert_pos_out [B,V,3]: for each of n_vverts visual vertices, sum_j w[v,j] * x[support[v,j]]
+ *     over its n_supports support particles (indices within the scene, weights from
+ *     particle_entity.py:193-232), using the particles' actual positions; vvert_active_out [B,V]:
+ *     the active flag of the first support.  support_idx [V, n_supports] int32 and
+ *     support_w [V, n_supports] float are device arrays; an out-of-range support index is skipped
+ *     and sets MPM_STATUS_BAD_INDEX.  n_vverts may be 0 (vvert pointers may then be NULL).
+ * All pointers are device memory; outputs are written on `stream`. */
+int mpm_render_fields(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end, float* pos_out, float* vel_out,
+                      uint8_t* active_out, int64_t n_vverts, int32_t n_supports, const int32_t* support_idx,
+                      const float* support_w, float* vvert_pos_out, uint8_t* vvert_active_out, void* stream);
 
 /* Number of grid nodes with mass > mass_eps in the current grid buffer of all scenes
  * (device reduction; synchronises `stream`). */

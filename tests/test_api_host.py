@@ -116,3 +116,32 @@ def test_workload_generators_are_seeded_and_in_range():
     assert all(1000 <= r.spec.n_particles <= 500000 and 50 <= r.spec.substeps <= 500 for r in reqs)
     assert {int(r.spec.grid_density) + 1 for r in reqs} == {33, 65, 129}
     assert grid_blocks(129) == 33**3 and grid_blocks(65) == 17**3
+
+
+def test_vvert_supports_reconstruct_the_vertex_at_rest():
+    """particle_entity.py:193-232: the support weights reproduce each visual vertex from the sampled
+    particles (affine combination, weights summing to 1), supports ordered by distance."""
+    from genesis_gb300.entity import MPMEntity
+    from genesis_gb300.solver import MPMSolver
+
+    class _Sim:
+        substeps = 1
+
+    class _Scene:
+        vis_options = gs.options.VisOptions(n_support_neighbors=8)
+
+    gs.EPS = float(np.finfo(np.float32).eps)
+    opts = gs.options.MPMOptions(lower_bound=(0, 0, 0), upper_bound=(1, 1, 1)).model_copy_from(gs.options.SimOptions())
+    solver = MPMSolver(_Scene(), _Sim(), opts)
+    mat = gs.materials.MPM.Elastic()
+    solver.add_material(mat)
+    ent = MPMEntity(None, solver, mat, morphs.Box(pos=(0.5, 0.5, 0.5), size=(0.1, 0.1, 0.1)), None, 0.01, 0, 40)
+    rng = np.random.default_rng(0)
+    verts = 0.5 + rng.uniform(-0.05, 0.05, size=(30, 3))
+    ent.set_vverts(verts)
+    idx, w = ent._vvert_support_idx - 40, ent._vvert_support_w.astype(np.float64)
+    assert idx.shape == (30, 8) and np.allclose(w.sum(1), 1.0, atol=1e-6)
+    rec = np.einsum("vj,vjd->vd", w, ent._particles[idx])
+    assert np.abs(rec - verts).max() < 1e-5
+    d = np.linalg.norm(ent._particles[idx] - verts[:, None], axis=2)
+    assert np.all(np.diff(d, axis=1) >= -1e-12)

@@ -223,3 +223,43 @@ def test_mass_conservation_and_touched_nodes(gs):
     assert abs(g[..., 3].double().sum().item() - m_expected) <= 1e-5 * m_expected
     solver.couple()
     solver.substep_post_coupling()
+
+
+def test_render_fields_and_visual_vertices(gs):
+    """update_render_fields (mpm_solver.py:780-803): positions / velocities / active flags in the
+    reference order, the nowhere point for inactive particles, and visual vertices as the
+    support-weighted sum of the current particle positions."""
+    scene = gs.Scene(
+        sim_options=gs.options.SimOptions(dt=2e-4),
+        mpm_options=gs.options.MPMOptions(lower_bound=(0, 0, 0), upper_bound=(1, 1, 1)),
+        vis_options=gs.options.VisOptions(n_support_neighbors=6),
+    )
+    a = scene.add_entity(material=gs.materials.MPM.Elastic(), morph=gs.morphs.Box(pos=(0.3, 0.5, 0.5), size=(0.1,) * 3))
+    b = scene.add_entity(material=gs.materials.MPM.Elastic(), morph=gs.morphs.Box(pos=(0.7, 0.5, 0.5), size=(0.1,) * 3))
+    rng = np.random.default_rng(1)
+    va = 0.3 + rng.uniform(-0.04, 0.04, size=(50, 3)) + np.array([0.0, 0.2, 0.2])
+    a.set_vverts(va)
+    b.set_vverts(np.array([0.7, 0.5, 0.5]) + rng.uniform(-0.04, 0.04, size=(20, 3)))
+    scene.build()
+    solver = scene.sim.mpm_solver
+    solver.update_render_fields()
+    vr = solver.vverts_render["pos"][0].cpu().numpy()
+    assert np.abs(vr[:50] - va).max() < 1e-5  # at rest the supports reproduce the vertices
+    b.deactivate()
+    for _ in range(5):
+        scene.step()
+    solver.update_render_fields()
+    st = solver.get_state()
+    pr = solver.particles_render
+    na = a.n_particles
+    assert torch.equal(pr["pos"][0, :na], st.pos[0, :na])
+    assert torch.equal(pr["vel"][0], st.vel[0])
+    assert torch.equal(pr["active"][0], st.active[0])
+    nowhere = torch.tensor([-2333333.0, -6666666.0, -5201314.0], device="cuda")
+    assert torch.equal(pr["pos"][0, na:], nowhere.expand(b.n_particles, 3))
+    idx = torch.as_tensor(np.concatenate([a._vvert_support_idx, b._vvert_support_idx]), device="cuda").long()
+    w = torch.as_tensor(np.concatenate([a._vvert_support_w, b._vvert_support_w]), device="cuda")
+    want = (st.pos[0][idx] * w[..., None]).sum(1)
+    assert torch.allclose(solver.vverts_render["pos"][0], want, atol=1e-6)
+    act = solver.vverts_render["active"][0]
+    assert act[:50].all() and not act[50:].any()
