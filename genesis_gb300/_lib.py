@@ -114,6 +114,10 @@ _SIGNATURES = {
     "mpm_set_profiling": (c_int32, [_P, c_int32]),
     "mpm_kernel_times": (c_int32, [_P, ctypes.POINTER(c_double), ctypes.POINTER(c_int64), c_int32]),
     "mpm_render_fields": (c_int32, [_P, c_int64, c_int64, _P, _P, _P, c_int64, c_int32, _P, _P, _P, _P, _P]),
+    "mpm_set_particle_constraints": (c_int32, [_P, c_int64, c_int64, c_int64, c_int64, _P, c_double, c_int32, _P, _P,
+                                               _P]),
+    "mpm_remove_particle_constraints": (c_int32, [_P, c_int64, c_int64, c_int64, c_int64, _P, _P]),
+    "mpm_set_link_poses": (c_int32, [_P, c_int32, _P]),
     "mpm_version": (c_int32, []),
     "mpm_ctx_create_pool": (c_int32, [ctypes.c_void_p, c_int32, ctypes.POINTER(c_void_p)]),
     "mpm_scene_admit": (c_int32, [_P, c_int64, ctypes.c_void_p, ctypes.c_void_p, c_int32, c_int64, _P, _P, c_int32, _P]),

@@ -76,6 +76,9 @@ struct mpm_ctx {
   unsigned long long* d_fp64 = nullptr;
   unsigned long long* d_tmp64 = nullptr;
   uint32_t* d_pin = nullptr;
+  ConstraintDev* d_cons = nullptr;  // particle constraints by reference row (allocated on first use)
+  float* d_links = nullptr;         // kinematic link poses [scene][link] (pos xyz, quat wxyz)
+  int32_t n_links = 0;
   int32_t* d_steps = nullptr;
   int64_t* d_n = nullptr;  // live particle count, read by k_perm inside captured substeps
   int64_t max_items = 0;
@@ -277,6 +280,10 @@ int launch_post(mpm_ctx* ctx, int c, cudaStream_t s, bool fuse_grid = false) {
     k_g2p<<<ctx->g2p_blocks, ctx->g2p_threads, 0, s>>>(P);
   }
   CKL();
+  if (ctx->d_cons) {  // after g2p, as substep_post_coupling does (mpm_solver.py:538-540)
+    k_constraints<<<ctx->io_blocks, 256, 0, s>>>(P, ctx->d_cons, ctx->d_links, ctx->n_links);
+    CKL();
+  }
   return launch_sort(ctx, P, s);
 }
 
@@ -650,6 +657,8 @@ int mpm_ctx_destroy(mpm_ctx* ctx) {
   for (auto e : ctx->ev_pool) cudaEventDestroy(e);
   for (void* p : ctx->allocs) cudaFree(p);
   if (ctx->d_pin) cudaFree(ctx->d_pin);
+  if (ctx->d_cons) cudaFree(ctx->d_cons);
+  if (ctx->d_links) cudaFree(ctx->d_links);
   if (ctx->ev_in) cudaEventDestroy(ctx->ev_in);
   if (ctx->ev_out) cudaEventDestroy(ctx->ev_out);
   if (ctx->cs) cudaStreamDestroy(ctx->cs);
@@ -833,6 +842,81 @@ int mpm_get_grid(mpm_ctx* ctx, int64_t scene, float* out, void* stream) {
   k_get_grid<<<ctx->n_sm * 8, 256, 0, ctx->cs>>>(P, scene, out);
   CKL();
   return leave(ctx, stream);
+}
+
+static int ensure_constraints(mpm_ctx* ctx) {
+  if (ctx->d_cons) return MPM_OK;
+  if (ctx->pool) return fail(ctx, MPM_ERR_BAD_ARG, "particle constraints are not available in pool mode");
+  cudaError_t e = cudaMalloc((void**)&ctx->d_cons, sizeof(ConstraintDev) * (size_t)ctx->cap);
+  if (e != cudaSuccess) {
+    ctx->d_cons = nullptr;
+    return fail(ctx, MPM_ERR_OOM, "constraint table allocation failed");
+  }
+  CK(cudaMemsetAsync(ctx->d_cons, 0, sizeof(ConstraintDev) * (size_t)ctx->cap, ctx->cs));
+  drop_graph(ctx);  // substeps now launch the constraint kernel
+  return MPM_OK;
+}
+
+int mpm_set_particle_constraints(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end, int64_t particle_start,
+                                 int64_t n, const uint8_t* mask, double stiffness, int32_t link_idx,
+                                 const float* link_pos, const float* link_quat, void* stream) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (!scene_range_ok(ctx, scene_begin, scene_end)) return fail(ctx, MPM_ERR_BAD_ARG, "bad scene range");
+  if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "constraints inside a substep");
+  if (n <= 0) return MPM_OK;
+  if (!mask || !link_pos || !link_quat || particle_start < 0) return fail(ctx, MPM_ERR_BAD_ARG, "bad arguments");
+  int r = enter(ctx, stream);
+  if (r) return r;
+  if ((r = ensure_constraints(ctx))) return r;
+  KParams P = make_params(ctx, ctx->cur, ctx->cur, ctx->cur);
+  k_set_constraints<<<ctx->io_blocks, 256, 0, ctx->cs>>>(P, scene_begin, scene_end, particle_start, n, mask,
+                                                          (float)stiffness, link_idx, link_pos, link_quat,
+                                                          ctx->d_cons);
+  CKL();
+  return leave(ctx, stream);
+}
+
+int mpm_remove_particle_constraints(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end, int64_t particle_start,
+                                    int64_t n, const uint8_t* mask, void* stream) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (!scene_range_ok(ctx, scene_begin, scene_end)) return fail(ctx, MPM_ERR_BAD_ARG, "bad scene range");
+  if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "constraints inside a substep");
+  if (!ctx->d_cons || n <= 0) return MPM_OK;
+  if (!mask || particle_start < 0) return fail(ctx, MPM_ERR_BAD_ARG, "bad arguments");
+  int r = enter(ctx, stream);
+  if (r) return r;
+  KParams P = make_params(ctx, ctx->cur, ctx->cur, ctx->cur);
+  k_remove_constraints<<<ctx->io_blocks, 256, 0, ctx->cs>>>(P, scene_begin, scene_end, particle_start, n, mask,
+                                                             ctx->d_cons);
+  CKL();
+  return leave(ctx, stream);
+}
+
+int mpm_set_link_poses(mpm_ctx* ctx, int32_t n_links, const float* poses_host) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (n_links < 0 || (n_links > 0 && !poses_host)) return fail(ctx, MPM_ERR_BAD_ARG, "bad arguments");
+  CK(cudaSetDevice(ctx->device));
+  const size_t count = (size_t)ctx->n_scenes * n_links * 7;
+  if (n_links != ctx->n_links) {
+    if (ctx->d_links) CK(cudaFree(ctx->d_links));
+    ctx->d_links = nullptr;
+    if (count > 0) {
+      cudaError_t e = cudaMalloc((void**)&ctx->d_links, count * sizeof(float));
+      if (e != cudaSuccess) {
+        ctx->d_links = nullptr;
+        ctx->n_links = 0;
+        drop_graph(ctx);
+        return fail(ctx, MPM_ERR_OOM, "link table allocation failed");
+      }
+    }
+    ctx->n_links = n_links;
+    drop_graph(ctx);  // the captured constraint launch holds the table pointer
+  }
+  if (count > 0) {
+    CK(cudaMemcpyAsync(ctx->d_links, poses_host, count * sizeof(float), cudaMemcpyHostToDevice, ctx->cs));
+    CK(cudaStreamSynchronize(ctx->cs));
+  }
+  return MPM_OK;
 }
 
 int mpm_render_fields(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end, float* pos_out, float* vel_out,

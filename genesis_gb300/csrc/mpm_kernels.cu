@@ -1033,6 +1033,108 @@ __global__ void k_get_grid(KParams P, int64_t scene, float* out) {
   }
 }
 
+// ------------------------------------------------------------------ particle constraints
+namespace {
+// gu.qd_transform_by_quat (utils/geom.py:256-271) for q = (w, x, y, z), unnormalised as there.
+__device__ __forceinline__ void quat_rotate(const float* q, const float* v, float* o) {
+  const float w = q[0], x = q[1], y = q[2], z = q[3];
+  const float xx = x * x, xy = x * y, xz = x * z, wx = x * w, yy = y * y, yz = y * z, wy = y * w, zz = z * z,
+              wz = z * w, ww = w * w;
+  o[0] = v[0] * (xx + ww - yy - zz) + v[1] * (2.f * xy - 2.f * wz) + v[2] * (2.f * xz + 2.f * wy);
+  o[1] = v[0] * (2.f * wz + 2.f * xy) + v[1] * (ww - xx + yy - zz) + v[2] * (-2.f * wx + 2.f * yz);
+  o[2] = v[0] * (-2.f * wy + 2.f * xz) + v[1] * (2.f * wx + 2.f * yz) + v[2] * (ww - xx - yy + zz);
+}
+
+// Reference row of a particle slot of scenes [s0, s1) that lies in [start, start + n) of its
+// scene, or -1.
+__device__ __forceinline__ int64_t masked_local(const KParams& P, int64_t i, int64_t s0, int64_t s1, int64_t start,
+                                                int64_t n, int32_t& s, uint32_t& pid) {
+  const uint32_t info = ld_info(P.dst, P.cap, i);
+  if (info & INFO_DEAD) return -1;
+  s = scene_of(P, info);
+  if (s < s0 || s >= s1) return -1;
+  pid = __float_as_uint(P.dst[(int64_t)PF_PID * P.cap + i]);
+  const int64_t l = (int64_t)pid - start;
+  return (l >= 0 && l < n) ? l : -1;
+}
+}  // namespace
+
+// _kernel_set_particle_constraints (mpm_solver.py:1052-1084): the target is the particle's
+// current position; its offset in the link frame is kept for later link poses.
+__global__ void k_set_constraints(KParams P, int64_t s0, int64_t s1, int64_t start, int64_t n, const uint8_t* mask,
+                                  float stiffness, int32_t link, const float* link_pos, const float* link_quat,
+                                  ConstraintDev* cons) {
+  for (int64_t i = grid_stride_begin(); i < P.n; i += grid_stride_step()) {
+    int32_t s;
+    uint32_t pid;
+    const int64_t l = masked_local(P, i, s0, s1, start, n, s, pid);
+    if (l < 0 || !mask[(s - s0) * n + l]) continue;
+    float x[3], d[3], loc[3];
+    const float* lp = link_pos + (s - s0) * 3;
+    const float* lq = link_quat + (s - s0) * 4;
+    for (int k = 0; k < 3; ++k) {
+      x[k] = P.dst[(int64_t)(PF_POS + k) * P.cap + i];
+      d[k] = x[k] - lp[k];
+    }
+    const float qi[4] = {lq[0], -lq[1], -lq[2], -lq[3]};
+    quat_rotate(qi, d, loc);
+    ConstraintDev& c = cons[P.scenes[s].p_begin + pid];
+    for (int k = 0; k < 3; ++k) {
+      c.local[k] = loc[k];
+      c.target[k] = x[k];
+    }
+    c.stiffness = stiffness;
+    c.link = link;
+    c.on = 1;
+  }
+}
+
+// _kernel_remove_particle_constraints (mpm_solver.py:1086-1097)
+__global__ void k_remove_constraints(KParams P, int64_t s0, int64_t s1, int64_t start, int64_t n,
+                                     const uint8_t* mask, ConstraintDev* cons) {
+  for (int64_t i = grid_stride_begin(); i < P.n; i += grid_stride_step()) {
+    int32_t s;
+    uint32_t pid;
+    const int64_t l = masked_local(P, i, s0, s1, start, n, s, pid);
+    if (l < 0 || !mask[(s - s0) * n + l]) continue;
+    ConstraintDev& c = cons[P.scenes[s].p_begin + pid];
+    c.on = 0;
+    c.link = -1;
+  }
+}
+
+// apply_particle_constraints (mpm_solver.py:1099-1128), after G2P: the target follows its link's
+// pose; a critically damped spring changes the velocity,
+// dv = dt (-k (x - target) - 2 sqrt(k m) v) / m with m the particle's real mass.
+__global__ void k_constraints(KParams P, ConstraintDev* cons, const float* links, int32_t n_links) {
+  const int64_t n = P.n_dev ? *P.n_dev : P.n;
+  for (int64_t i = grid_stride_begin(); i < n; i += grid_stride_step()) {
+    const uint32_t info = ld_info(P.dst, P.cap, i);
+    if (info & INFO_DEAD) continue;
+    const MaterialDev& M = P.mats[info & INFO_MAT_MASK];
+    const int32_t s = M.scene;
+    if (P.steps && P.steps[s] == 0) continue;  // frozen scene
+    const uint32_t pid = __float_as_uint(P.dst[(int64_t)PF_PID * P.cap + i]);
+    ConstraintDev& c = cons[P.scenes[s].p_begin + pid];
+    if (!c.on) continue;
+    if (c.link >= 0 && c.link < n_links) {
+      const float* L = links + ((int64_t)s * n_links + c.link) * 7;
+      float t[3];
+      quat_rotate(L + 3, c.local, t);
+      for (int k = 0; k < 3; ++k) c.target[k] = t[k] + L[k];
+    }
+    const float m = M.mass / 1e3f;  // particles_info.mass / particle_volume_scale
+    const float k = c.stiffness;
+    const float damp = 2.f * sqrtf(k * m);
+    for (int d = 0; d < 3; ++d) {
+      const float x = P.dst[(int64_t)(PF_POS + d) * P.cap + i];
+      float& v = P.dst[(int64_t)(PF_VEL + d) * P.cap + i];
+      const float f = -k * (x - c.target[d]) - damp * v;
+      v = v + P.scenes[s].dt * f / m;
+    }
+  }
+}
+
 // Visual vertices of _kernel_update_render_fields (mpm_solver.py:795-803): support-weighted sum
 // of the particles' positions (`pos` holds the rows of scenes [s0, s1) in get_state order).
 __global__ void k_render_vverts(KParams P, int64_t s0, int64_t s1, const float* pos, const uint8_t* active,

@@ -183,6 +183,21 @@ __global__ void k_perm(KParams P);
 __global__ void k_p2g(KParams P);
 __global__ void k_grid_op(KParams P);
 __global__ void k_get_grid(KParams P, int64_t scene, float* out);
+// Soft particle-to-link constraint of one reference particle row (mpm_solver.py:1052-1128).
+struct ConstraintDev {
+  float local[3];   // offset in the link frame at attachment
+  float target[3];  // current target position
+  float stiffness;
+  int32_t link;     // kinematic link index, or -1 (target stays where it was set)
+  int32_t on;
+  int32_t pad;
+};
+__global__ void k_set_constraints(KParams P, int64_t s0, int64_t s1, int64_t start, int64_t n, const uint8_t* mask,
+                                  float stiffness, int32_t link, const float* link_pos, const float* link_quat,
+                                  ConstraintDev* cons);
+__global__ void k_remove_constraints(KParams P, int64_t s0, int64_t s1, int64_t start, int64_t n,
+                                     const uint8_t* mask, ConstraintDev* cons);
+__global__ void k_constraints(KParams P, ConstraintDev* cons, const float* links, int32_t n_links);
 __global__ void k_render_vverts(KParams P, int64_t s0, int64_t s1, const float* pos, const uint8_t* active,
                                 int64_t n_vverts, int32_t n_supports, const int32_t* support_idx,
                                 const float* support_w, float* vpos, uint8_t* vactive);

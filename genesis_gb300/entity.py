@@ -15,6 +15,10 @@ from . import _lib
 from .exceptions import GenesisException
 from .states import MPMEntityState
 
+
+def _stream_ptr():
+    return torch.cuda.current_stream().cuda_stream
+
 ACTIVE = 1
 INACTIVE = 0
 
@@ -56,6 +60,44 @@ class MPMEntity:
         self._vverts = np.zeros((0, 3), dtype=np.float64)
         self._vvert_support_idx = np.zeros((0, 0), dtype=np.int32)
         self._vvert_support_w = np.zeros((0, 0), dtype=np.float32)
+
+    # ------------------------------------------------------------------ particle constraints
+    def _mask(self, particles_mask):
+        B = self._solver._B
+        if particles_mask is None:
+            m = torch.ones((B, self._n_particles), dtype=torch.uint8, device="cuda")
+        else:
+            m = torch.as_tensor(particles_mask, device="cuda").to(torch.uint8)
+            if m.ndim == 1:
+                m = m.unsqueeze(0).expand(B, -1)
+            if tuple(m.shape) != (B, self._n_particles):
+                raise GenesisException(f"particles_mask must have shape ({B}, {self._n_particles}).")
+        return m.contiguous()
+
+    def set_particle_constraints(self, particles_mask, link_idx, stiffness):
+        """mpm_entity.py:631-671: attach the masked particles to kinematic link `link_idx` (its
+        pose from MPMSolver.set_link_poses) with a critically damped spring of `stiffness`."""
+        if not isinstance(link_idx, int):
+            raise GenesisException("link_idx must be an integer.")
+        lp, lq = self._solver.get_link_pose(link_idx)
+        m = self._mask(particles_mask)
+        pos = torch.as_tensor(np.ascontiguousarray(lp), device="cuda")
+        quat = torch.as_tensor(np.ascontiguousarray(lq), device="cuda")
+        lib = self._solver._lib
+        _lib.check(lib.mpm_set_particle_constraints(self._solver._ctx, 0, self._solver._B, self._particle_start,
+                                                    self._n_particles, m.data_ptr(), float(stiffness), link_idx,
+                                                    pos.data_ptr(), quat.data_ptr(), _stream_ptr()),
+                   self._solver._ctx, "mpm_set_particle_constraints")
+        torch.cuda.current_stream().synchronize()
+
+    def remove_particle_constraints(self, particles_mask=None):
+        """mpm_entity.py:674-690: remove the constraints of the masked particles (all if None)."""
+        m = self._mask(particles_mask)
+        lib = self._solver._lib
+        _lib.check(lib.mpm_remove_particle_constraints(self._solver._ctx, 0, self._solver._B, self._particle_start,
+                                                       self._n_particles, m.data_ptr(), _stream_ptr()),
+                   self._solver._ctx, "mpm_remove_particle_constraints")
+        torch.cuda.current_stream().synchronize()
 
     # ------------------------------------------------------------------ visual vertices
     def set_vverts(self, verts) -> None:

@@ -129,6 +129,7 @@ class Scene:
         self.show_viewer = False
         self._sim = Simulator(self, self.sim_options, self.mpm_options)
         self._entities = []
+        self._emitters = []
         self._is_built = False
         self._n_envs = 0
         self._envs_idx = None
@@ -147,6 +148,25 @@ class Scene:
         entity = self._sim.mpm_solver.add_entity(len(self._entities), material, morph, surface, name=name)
         self._entities.append(entity)
         return entity
+
+    def add_emitter(self, material, max_particles=20000, surface=None):
+        """scene.py:765-818: an MPM entity of `max_particles` inactive particles driven by an Emitter."""
+        from .emitter import Emitter
+        from .materials import _MPMBase
+
+        if self.requires_grad:
+            raise GenesisException("Emitter is not supported in differentiable mode.")
+        if not isinstance(material, _MPMBase):
+            raise GenesisException("Non-supported material for emitter. Supported materials are: `gs.materials.MPM.Base`.")
+        emitter = Emitter(max_particles)
+        entity = self.add_entity(morph=_morphs.Nowhere(n_particles=max_particles), material=material, surface=surface)
+        emitter.set_entity(entity)
+        self._emitters.append(emitter)
+        return emitter
+
+    @property
+    def emitters(self):
+        return self._emitters
 
     def build(self, n_envs: int = 0, env_spacing=(0.0, 0.0), n_envs_per_row=None, center_envs_at_origin=True,
               compile_kernels=None):

@@ -35,6 +35,10 @@ class CubeBoundary:
         return f"CubeBoundary(lower={self.lower.tolist()}, upper={self.upper.tolist()})"
 
 
+def gs_exc(msg: str):
+    raise GenesisException(msg)
+
+
 def _stream_handle():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
@@ -263,6 +267,28 @@ class MPMSolver:
         out = torch.empty((res[0], res[1], res[2], 4), dtype=torch.float32, device="cuda")
         _lib.check(self._lib.mpm_get_grid(self._ctx, scene, _lib.ptr(out), _stream_handle()), self._ctx, "mpm_get_grid")
         return out
+
+    # ------------------------------------------------------------------ kinematic links
+    def set_link_poses(self, pos, quat) -> None:
+        """Poses of the links that particle constraints follow (the reference reads them from the
+        rigid solver's links_state): pos [B, L, 3] or [L, 3], quat (w, x, y, z) [B, L, 4] or [L, 4]."""
+        p = np.asarray(pos, dtype=np.float32)
+        q = np.asarray(quat, dtype=np.float32)
+        if p.ndim == 2:
+            p = np.broadcast_to(p, (self._B,) + p.shape)
+            q = np.broadcast_to(q, (self._B,) + q.shape)
+        if p.shape[0] != self._B or q.shape[:2] != p.shape[:2] or p.shape[2] != 3 or q.shape[2] != 4:
+            gs_exc("link poses must be [B, L, 3] and [B, L, 4]")
+        self._link_pos, self._link_quat = np.ascontiguousarray(p), np.ascontiguousarray(q)
+        table = np.ascontiguousarray(np.concatenate([p, q], axis=2), dtype=np.float32)
+        _lib.check(self._lib.mpm_set_link_poses(self._ctx, p.shape[1], table.ctypes.data), self._ctx,
+                   "mpm_set_link_poses")
+
+    def get_link_pose(self, link_idx: int):
+        lp = getattr(self, "_link_pos", None)
+        if lp is None or not 0 <= link_idx < lp.shape[1]:
+            gs_exc(f"link {link_idx} has no pose; call set_link_poses first")
+        return self._link_pos[:, link_idx], self._link_quat[:, link_idx]
 
     # ------------------------------------------------------------------ render fields
     @property

@@ -182,6 +182,27 @@ int mpm_substep_post(mpm_ctx* ctx, void* stream);
  * holds (vel_out xyz, mass).  Replaces reading MPMSolver.grid (mpm_solver.py:137-148). */
 int mpm_get_grid(mpm_ctx* ctx, int64_t scene, float* out, void* stream);
 
+/* Soft particle-to-link constraints (mpm_solver.py:1052-1128; mpm_entity.py:631-690).
+ * mpm_set_particle_constraints: for each scene b of [scene_begin, scene_end) and each particle
+ * [particle_start, particle_start + n) of it with mask[b * n + i] != 0, attach the particle to
+ * kinematic link `link_idx` (or to its current position if link_idx < 0): the target is the
+ * current position, its offset in the link frame is kept.  link_pos [B,3] and link_quat [B,4]
+ * (w, x, y, z) are the link poses at attachment, per scene.  After every G2P the target follows
+ * the link's current pose (mpm_set_link_poses) and the velocity gets
+ * dv = dt (-k (x - target) - 2 sqrt(k m) v) / m (m = the particle's real mass).
+ * mpm_remove_particle_constraints clears the masked particles.  mask, link_pos and link_quat are
+ * device arrays.  Not available in pool mode. */
+int mpm_set_particle_constraints(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end, int64_t particle_start,
+                                 int64_t n, const uint8_t* mask, double stiffness, int32_t link_idx,
+                                 const float* link_pos, const float* link_quat, void* stream);
+int mpm_remove_particle_constraints(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end, int64_t particle_start,
+                                    int64_t n, const uint8_t* mask, void* stream);
+
+/* Poses of the kinematic links that constraints follow, replacing the rigid solver's
+ * links_state: poses_host [n_scenes][n_links][7] = (pos xyz, quat wxyz), host memory, copied
+ * before returning.  Call whenever the links move (e.g. once per scene.step()). */
+int mpm_set_link_poses(mpm_ctx* ctx, int32_t n_links, const float* poses_host);
+
 /* Render fields (mpm_solver.py:780-803, _kernel_update_render_fields) of scenes
  * [scene_begin, scene_end), in the reference [B, N] row order of mpm_get_state:
  *   pos_out [B,N,3]: the particle position, or the reference's "nowhere" point

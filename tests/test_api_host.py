@@ -145,3 +145,21 @@ def test_vvert_supports_reconstruct_the_vertex_at_rest():
     assert np.abs(rec - verts).max() < 1e-5
     d = np.linalg.norm(ent._particles[idx] - verts[:, None], axis=2)
     assert np.all(np.diff(d, axis=1) >= -1e-12)
+
+
+def test_emitter_geometry_helpers_follow_reference_conventions():
+    from genesis_gb300.emitter import axis_angle_R, shell_to_particles, z_up_frame
+
+    eps = float(np.finfo(np.float32).eps)
+    for d in ([0, 0, -1], [1, 0, 0], [0.3, -0.4, 0.8], [0, 0, 1]):
+        R = z_up_frame(np.array(d, float), eps)
+        assert np.allclose(R @ R.T, np.eye(3), atol=1e-12) and np.isclose(np.linalg.det(R), 1.0)
+        assert np.allclose(R[:, 2], np.array(d) / np.linalg.norm(d))
+    R = z_up_frame(np.array([0.3, -0.4, 0.8]), eps)
+    assert abs(R[2, 0]) < 1e-12  # first axis horizontal for a non-vertical direction
+    Rz = axis_angle_R([0, 0, 1], 0.5)
+    assert np.allclose(Rz, [[np.cos(0.5), -np.sin(0.5), 0], [np.sin(0.5), np.cos(0.5), 0], [0, 0, 1]])
+    assert np.allclose(axis_angle_R([0, 0, 1], -0.5), Rz)  # sin from sqrt(1 - cos^2), as the reference
+    p = shell_to_particles(0.01, (0, 0, 0), 0.04, 0.1, "regular")
+    r = np.linalg.norm(p, axis=1)
+    assert len(p) > 0 and r.min() >= 0.04 and r.max() <= 0.1

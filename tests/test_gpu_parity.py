@@ -263,3 +263,94 @@ def test_render_fields_and_visual_vertices(gs):
     assert torch.allclose(solver.vverts_render["pos"][0], want, atol=1e-6)
     act = solver.vverts_render["active"][0]
     assert act[:50].all() and not act[50:].any()
+
+
+def _quat_rotate(q, v):
+    w, x, y, z = q
+    R = np.array([[x * x + w * w - y * y - z * z, 2 * x * y - 2 * w * z, 2 * x * z + 2 * w * y],
+                  [2 * w * z + 2 * x * y, w * w - x * x + y * y - z * z, -2 * w * x + 2 * y * z],
+                  [-2 * w * y + 2 * x * z, 2 * w * x + 2 * y * z, w * w - x * x - y * y + z * z]])
+    return v @ R.T
+
+
+def test_particle_constraints_match_spring_update(gs, oracle):
+    """apply_particle_constraints (mpm_solver.py:1099-1128) after G2P: the target follows the link
+    (attachment offset in the link frame), dv = dt (-k (x - target) - 2 sqrt(k m) v) / m."""
+    scene, cube, mat = c1_scene(gs, size=0.1)
+    solver = scene.sim.mpm_solver
+    n = cube.n_particles
+    q0 = np.array([np.cos(0.2), 0.0, 0.0, np.sin(0.2)])  # rotation about z
+    p0 = np.array([0.5, 0.5, 0.4])
+    solver.set_link_poses(p0[None], q0[None])
+    mask = torch.zeros(n, dtype=torch.bool)
+    mask[::3] = True
+    k = 2e3
+    cube.set_particle_constraints(mask, 0, k)
+    st0 = solver.get_state()
+    x0 = st0.pos[0].double().cpu().numpy()
+    local = _quat_rotate(q0 * np.array([1, -1, -1, -1]), x0 - p0)
+    # move the link, then one substep
+    q1 = np.array([np.cos(0.25), 0.0, np.sin(0.25) * 0.6, np.sin(0.25) * 0.8])
+    p1 = np.array([0.52, 0.49, 0.41])
+    solver.set_link_poses(p1[None], q1[None])
+    scene.step()
+    st1 = solver.get_state()
+    ref, _, _ = oracle.run(oracle_scene_for(oracle, solver), [oracle.from_c_material(mat.to_c(0))], oracle_state(st0), 1)
+    m_real = np.float32(np.float32(solver.particle_volume) * np.float32(mat.rho)) / 1e3
+    target = _quat_rotate(q1, local) + p1
+    v = ref["vel"].copy()
+    sel = mask.numpy()
+    dv = 2e-4 * (-k * (ref["pos"][sel] - target[sel]) - 2 * np.sqrt(k * m_real) * v[sel]) / m_real
+    v[sel] += dv
+    got = st1.vel[0].double().cpu().numpy()
+    assert np.abs(got - v).max() <= 1e-4 * max(1.0, np.abs(v).max()), np.abs(got - v).max()
+    assert np.abs(dv).max() > 1e-3  # the spring acted
+    cube.remove_particle_constraints()
+    st1b = solver.get_state()
+    scene.step()
+    st2 = solver.get_state()
+    ref2, _, _ = oracle.run(oracle_scene_for(oracle, solver), [oracle.from_c_material(mat.to_c(0))],
+                            oracle_state(st1b), 1)
+    assert np.abs(st2.vel[0].double().cpu().numpy() - ref2["vel"]).max() <= 1e-4
+
+
+def test_emitter_activates_droplets_and_recycles(gs):
+    """Emitter.emit (emitter.py:56-194): the next pool particles take the droplet's positions and
+    the emission velocity and become active; the pool index wraps when it would overflow."""
+    from genesis_gb300.emitter import z_up_frame
+
+    scene = gs.Scene(
+        sim_options=gs.options.SimOptions(dt=4e-3, substeps=10),
+        mpm_options=gs.options.MPMOptions(lower_bound=(0, 0, 0), upper_bound=(1, 1, 1)),
+    )
+    em = scene.add_emitter(material=gs.materials.MPM.Liquid(), max_particles=3000)
+    scene.build()
+    ent = em.entity
+    assert not ent.get_particles_active().any()
+    # the droplet length from speed * dt (1.5 * 4e-3 = 6 mm) is below the particle size: the first
+    # call only accumulates it (emitter.py:110-116), the second emits
+    em.emit("sphere", 0.08, pos=(0.5, 0.5, 0.6), direction=(0.0, 0.0, -1.0), speed=1.5)
+    assert not ent.get_particles_active().any()
+    em.emit("sphere", 0.08, pos=(0.5, 0.5, 0.6), direction=(0.0, 0.0, -1.0), speed=1.5)
+    act = ent.get_particles_active()
+    n1 = int(act.sum())
+    assert n1 > 100 and act[:n1].all()
+    vel = ent.get_particles_vel()[:n1]
+    assert torch.allclose(vel, torch.tensor([0.0, 0.0, -1.5], device="cuda").expand(n1, 3))
+    pos = ent.get_particles_pos()[:n1].cpu().numpy()
+    assert np.linalg.norm(pos - np.array([0.5, 0.5, 0.6]), axis=1).max() <= 0.04 + 1e-6
+    for _ in range(3):
+        scene.step()
+    assert (ent.get_particles_pos()[:n1, 2] < 0.6 - 0.04).any()
+    # square nozzle along +x with a rotation: positions sit in the rotated frame
+    em.emit("square", 0.05, droplet_length=0.03, pos=(0.3, 0.5, 0.5), direction=(1.0, 0.0, 0.0), theta=0.3,
+            speed=0.5)
+    n2 = int(ent.get_particles_active().sum()) - n1
+    assert n2 > 0
+    p2 = ent.get_particles_pos()[n1:n1 + n2].double().cpu().numpy()
+    R = z_up_frame(np.array([1.0, 0.0, 0.0]), gs.EPS)
+    local = (p2 - np.array([0.3, 0.5, 0.5])) @ R
+    assert np.abs(local[:, 2]).max() <= 0.015 + 1e-6  # droplet length along the direction
+    while em._next_particle != 0:  # keep emitting until the pool wraps
+        em.emit("sphere", 0.08, droplet_length=0.05, pos=(0.5, 0.5, 0.6), direction=(0.0, 0.0, -1.0), speed=1.5)
+    assert int(ent.get_particles_active().sum()) <= 3000
