@@ -75,6 +75,27 @@ class MpmPoolConfig(ctypes.Structure):
     ]
 
 
+class MpmCollider(ctypes.Structure):
+    """mpm_collider (include/gbmpm.h)."""
+
+    _fields_ = [
+        ("type", c_int32),
+        ("scene", c_int32),
+        ("pos", c_double * 3),
+        ("quat", c_double * 4),
+        ("size", c_double * 3),
+        ("com", c_double * 3),
+        ("lin_vel", c_double * 3),
+        ("ang_vel", c_double * 3),
+        ("friction", c_double),
+        ("softness", c_double),
+        ("restitution", c_double),
+    ]
+
+
+COLLIDER_SPHERE, COLLIDER_PLANE, COLLIDER_BOX = 0, 1, 2
+
+
 class MpmSceneConfig(ctypes.Structure):
     _fields_ = [
         ("substep_dt", c_double),
@@ -118,6 +139,8 @@ _SIGNATURES = {
                                                _P]),
     "mpm_remove_particle_constraints": (c_int32, [_P, c_int64, c_int64, c_int64, c_int64, _P, _P]),
     "mpm_set_link_poses": (c_int32, [_P, c_int32, _P]),
+    "mpm_set_colliders": (c_int32, [_P, c_int32, _P]),
+    "mpm_get_collider_forces": (c_int32, [_P, _P, c_int32, _P]),
     "mpm_version": (c_int32, []),
     "mpm_ctx_create_pool": (c_int32, [ctypes.c_void_p, c_int32, ctypes.POINTER(c_void_p)]),
     "mpm_scene_admit": (c_int32, [_P, c_int64, ctypes.c_void_p, ctypes.c_void_p, c_int32, c_int64, _P, _P, c_int32, _P]),

@@ -77,6 +77,9 @@ struct mpm_ctx {
   unsigned long long* d_tmp64 = nullptr;
   uint32_t* d_pin = nullptr;
   ConstraintDev* d_cons = nullptr;  // particle constraints by reference row (allocated on first use)
+  ColliderDev* d_colliders = nullptr;  // kinematic colliders (capacity MAX_COLLIDERS once allocated)
+  double* d_collider_acc = nullptr;    // [MAX_COLLIDERS][6]
+  int32_t n_colliders = 0;
   float* d_links = nullptr;         // kinematic link poses [scene][link] (pos xyz, quat wxyz)
   int32_t n_links = 0;
   int32_t* d_steps = nullptr;
@@ -177,6 +180,9 @@ KParams make_params(mpm_ctx* ctx, int src, int dst, int g) {
   P.n_items = ctx->d_nitems;
   P.partials = ctx->d_partials;
   P.scan_state = ctx->d_scan_state;
+  P.colliders = ctx->d_colliders;
+  P.n_colliders = ctx->n_colliders;
+  P.collider_acc = ctx->d_collider_acc;
   P.scan_sync = ctx->d_scan_sync;
   P.n_tiles = ctx->n_tiles;
   P.pin = ctx->d_pin;
@@ -290,7 +296,7 @@ int launch_post(mpm_ctx* ctx, int c, cudaStream_t s, bool fuse_grid = false) {
 // Without pinned particles the grid op is folded into G2P (k_grid_op is not launched); the
 // split-phase entry points keep it separate so a coupler can act on the velocity grid.
 int launch_substep(mpm_ctx* ctx, int c, cudaStream_t s) {
-  const bool fuse = ctx->d_pin == nullptr;
+  const bool fuse = ctx->d_pin == nullptr && ctx->n_colliders == 0;
   int r = launch_pre(ctx, c, s);
   if (!r && !fuse) r = launch_grid(ctx, c, s);
   if (!r) r = launch_post(ctx, c, s, fuse);
@@ -658,6 +664,8 @@ int mpm_ctx_destroy(mpm_ctx* ctx) {
   for (void* p : ctx->allocs) cudaFree(p);
   if (ctx->d_pin) cudaFree(ctx->d_pin);
   if (ctx->d_cons) cudaFree(ctx->d_cons);
+  if (ctx->d_colliders) cudaFree(ctx->d_colliders);
+  if (ctx->d_collider_acc) cudaFree(ctx->d_collider_acc);
   if (ctx->d_links) cudaFree(ctx->d_links);
   if (ctx->ev_in) cudaEventDestroy(ctx->ev_in);
   if (ctx->ev_out) cudaEventDestroy(ctx->ev_out);
@@ -841,6 +849,62 @@ int mpm_get_grid(mpm_ctx* ctx, int64_t scene, float* out, void* stream) {
   P.fuse_grid = (ctx->phase == 0 && ctx->grid_momentum[g]) ? 1 : 0;
   k_get_grid<<<ctx->n_sm * 8, 256, 0, ctx->cs>>>(P, scene, out);
   CKL();
+  return leave(ctx, stream);
+}
+
+constexpr int32_t MAX_COLLIDERS = 256;
+
+int mpm_set_colliders(mpm_ctx* ctx, int32_t n, const mpm_collider* colliders) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (n < 0 || n > MAX_COLLIDERS || (n > 0 && !colliders)) return fail(ctx, MPM_ERR_BAD_ARG, "bad collider arguments");
+  if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "colliders inside a substep");
+  std::vector<ColliderDev> h((size_t)n);
+  for (int32_t i = 0; i < n; ++i) {
+    const mpm_collider& c = colliders[i];
+    if (c.type < MPM_COLLIDER_SPHERE || c.type > MPM_COLLIDER_BOX)
+      return fail(ctx, MPM_ERR_BAD_ARG, "unknown collider type");
+    if (c.scene < -1 || c.scene >= ctx->n_scenes) return fail(ctx, MPM_ERR_BAD_ARG, "collider scene out of range");
+    ColliderDev& d = h[(size_t)i];
+    std::memset(&d, 0, sizeof(d));
+    d.type = c.type;
+    d.scene = c.scene;
+    for (int k = 0; k < 3; ++k) {
+      d.pos[k] = (float)c.pos[k];
+      d.size[k] = (float)c.size[k];
+      d.com[k] = (float)c.com[k];
+      d.lin[k] = (float)c.lin_vel[k];
+      d.ang[k] = (float)c.ang_vel[k];
+    }
+    for (int k = 0; k < 4; ++k) d.quat[k] = (float)c.quat[k];
+    d.friction = (float)c.friction;
+    d.softness = (float)c.softness;
+    d.restitution = (float)c.restitution;
+  }
+  CK(cudaSetDevice(ctx->device));
+  if (!ctx->d_colliders && n > 0) {
+    cudaError_t e = cudaMalloc((void**)&ctx->d_colliders, sizeof(ColliderDev) * MAX_COLLIDERS);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&ctx->d_collider_acc, sizeof(double) * 6 * MAX_COLLIDERS);
+    if (e != cudaSuccess) return fail(ctx, MPM_ERR_OOM, "collider table allocation failed");
+  }
+  if (n > 0) {
+    CK(cudaMemcpyAsync(ctx->d_colliders, h.data(), sizeof(ColliderDev) * n, cudaMemcpyHostToDevice, ctx->cs));
+    CK(cudaMemsetAsync(ctx->d_collider_acc, 0, sizeof(double) * 6 * MAX_COLLIDERS, ctx->cs));
+    CK(cudaStreamSynchronize(ctx->cs));
+  }
+  if (n != ctx->n_colliders) drop_graph(ctx);  // the count is a captured kernel argument
+  ctx->n_colliders = n;
+  return MPM_OK;
+}
+
+int mpm_get_collider_forces(mpm_ctx* ctx, double* out_host, int32_t reset, void* stream) {
+  if (!ctx || !out_host) return MPM_ERR_BAD_ARG;
+  if (ctx->n_colliders == 0) return MPM_OK;
+  int r = enter(ctx, stream);
+  if (r) return r;
+  CK(cudaMemcpyAsync(out_host, ctx->d_collider_acc, sizeof(double) * 6 * ctx->n_colliders, cudaMemcpyDeviceToHost,
+                     ctx->cs));
+  if (reset) CK(cudaMemsetAsync(ctx->d_collider_acc, 0, sizeof(double) * 6 * MAX_COLLIDERS, ctx->cs));
+  CK(cudaStreamSynchronize(ctx->cs));
   return leave(ctx, stream);
 }
 

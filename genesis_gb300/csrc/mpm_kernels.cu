@@ -981,6 +981,95 @@ __global__ void __launch_bounds__(256) k_g2p(KParams P) {
   }
 }
 
+// ------------------------------------------------------------------ kinematic colliders
+namespace {
+__device__ __forceinline__ void rot(const float* q, const float* v, float* o) {  // gu.qd_transform_by_quat
+  const float w = q[0], x = q[1], y = q[2], z = q[3];
+  o[0] = v[0] * (x * x + w * w - y * y - z * z) + v[1] * (2.f * x * y - 2.f * w * z) + v[2] * (2.f * x * z + 2.f * w * y);
+  o[1] = v[0] * (2.f * w * z + 2.f * x * y) + v[1] * (w * w - x * x + y * y - z * z) + v[2] * (-2.f * w * x + 2.f * y * z);
+  o[2] = v[0] * (-2.f * w * y + 2.f * x * z) + v[1] * (2.f * w * x + 2.f * y * z) + v[2] * (w * w - x * x - y * y + z * z);
+}
+
+// Signed distance and outward unit normal of a collider at world point x
+// (utils/sdf.py:119-126 and 372-378 for sphere and plane; analytic box).
+__device__ __forceinline__ float collider_sdf(const ColliderDev& c, const float* x, float eps, float* n) {
+  float d[3] = {x[0] - c.pos[0], x[1] - c.pos[1], x[2] - c.pos[2]};
+  if (c.type == MPM_COLLIDER_SPHERE) {
+    const float len = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const float ln = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2] + eps);  // norm(EPS)
+    for (int k = 0; k < 3; ++k) n[k] = d[k] / ln;
+    return len - c.size[0];
+  }
+  const float qi[4] = {c.quat[0], -c.quat[1], -c.quat[2], -c.quat[3]};
+  float l[3];
+  rot(qi, d, l);  // position in the collider frame
+  float gl[3];
+  float sd;
+  if (c.type == MPM_COLLIDER_PLANE) {
+    sd = l[0] * c.size[0] + l[1] * c.size[1] + l[2] * c.size[2];
+    gl[0] = c.size[0], gl[1] = c.size[1], gl[2] = c.size[2];
+  } else {  // box
+    float q[3], outside = 0.f;
+    int ax = 0;
+    for (int k = 0; k < 3; ++k) {
+      q[k] = fabsf(l[k]) - c.size[k];
+      const float o = fmaxf(q[k], 0.f);
+      outside += o * o;
+      if (q[k] > q[ax]) ax = k;
+    }
+    const float inside = fminf(fmaxf(q[0], fmaxf(q[1], q[2])), 0.f);
+    sd = sqrtf(outside) + inside;
+    for (int k = 0; k < 3; ++k) {
+      const float sg = l[k] < 0.f ? -1.f : 1.f;
+      gl[k] = outside > 0.f ? sg * fmaxf(q[k], 0.f) : (k == ax ? sg : 0.f);
+    }
+  }
+  float g[3];
+  rot(c.quat, gl, g);
+  const float gn = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2] + eps);
+  for (int k = 0; k < 3; ++k) n[k] = g[k] / gn;
+  return sd;
+}
+
+// _func_collide_with_rigid_geom + _func_collide_in_rigid_geom (legacy_coupler.py:166-218, 284-347)
+// for every collider of the node's scene; reaction force and torque go to collider_acc.
+__device__ void collide_node(const KParams& P, const SceneDev& S, int32_t scene, const float* x, float* v, float m) {
+  for (int ci = 0; ci < P.n_colliders; ++ci) {
+    const ColliderDev& c = P.colliders[ci];
+    if (c.scene >= 0 && c.scene != scene) continue;
+    float n[3];
+    const float sd = collider_sdf(c, x, S.eps, n);
+    const float influence = fminf(expf(-sd / fmaxf(1e-10f, c.softness)), 1.f);
+    if (!(influence > 0.1f)) continue;
+    const float r[3] = {x[0] - c.com[0], x[1] - c.com[1], x[2] - c.com[2]};
+    const float vr[3] = {c.ang[1] * r[2] - c.ang[2] * r[1] + c.lin[0], c.ang[2] * r[0] - c.ang[0] * r[2] + c.lin[1],
+                         c.ang[0] * r[1] - c.ang[1] * r[0] + c.lin[2]};
+    const float rv[3] = {v[0] - vr[0], v[1] - vr[1], v[2] - vr[2]};
+    const float rvn = rv[0] * n[0] + rv[1] * n[1] + rv[2] * n[2];
+    if (!(rvn < 0.f)) continue;
+    float rt[3];
+    for (int k = 0; k < 3; ++k) rt[k] = rv[k] - rvn * n[k];
+    const float rtn = sqrtf(rt[0] * rt[0] + rt[1] * rt[1] + rt[2] * rt[2] + S.eps);  // norm(gs.EPS)
+    const float scale = fmaxf(0.f, rtn + rvn * c.friction) / rtn;
+    float dv[3];
+    for (int k = 0; k < 3; ++k) {
+      const float nv = vr[k] + (rt[k] * scale - n[k] * rvn * c.restitution) * influence + rv[k] * (1.f - influence);
+      dv[k] = nv - v[k];
+      v[k] = nv;
+    }
+    // particle -> rigid: force = -m dv / dt at x, torque (x - com) x force
+    const float f[3] = {-m * dv[0] / S.dt, -m * dv[1] / S.dt, -m * dv[2] / S.dt};
+    double* acc = P.collider_acc + (int64_t)ci * 6;
+    atomicAdd(acc + 0, (double)f[0]);
+    atomicAdd(acc + 1, (double)f[1]);
+    atomicAdd(acc + 2, (double)f[2]);
+    atomicAdd(acc + 3, (double)(r[1] * f[2] - r[2] * f[1]));
+    atomicAdd(acc + 4, (double)(r[2] * f[0] - r[0] * f[2]));
+    atomicAdd(acc + 5, (double)(r[0] * f[1] - r[1] * f[0]));
+  }
+}
+}  // namespace
+
 // ------------------------------------------------------------------ grid op
 // legacy_coupler.py:356-501 without coupling partners: for nodes with mass > eps,
 // v = (1/m) p + dt g, then CubeBoundary.impose_pos_vel at the node position; 0 otherwise.
@@ -1012,7 +1101,18 @@ __global__ void __launch_bounds__(256) k_grid_op(KParams P) {
         atomicAnd(&P.pin[a >> 5], ~bit);
       }
     }
-    *node = grid_velocity(S, q, g[0], g[1], g[2]);
+    if (P.n_colliders == 0) {
+      *node = grid_velocity(S, q, g[0], g[1], g[2]);
+    } else {  // gravity, then the colliders (legacy_coupler.py:389-403), then the boundary
+      float v[3];
+      if (grid_free_velocity(S, q, v)) {
+        const float x[3] = {(float)(g[0] + S.offset[0]) * S.dx, (float)(g[1] + S.offset[1]) * S.dx,
+                            (float)(g[2] + S.offset[2]) * S.dx};
+        collide_node(P, S, P.block_scene[blk], x, v, q.w / 1e3f);
+        grid_boundary(S, v, g[0], g[1], g[2]);
+      }
+      *node = make_float4(v[0], v[1], v[2], q.w);
+    }
   }
 }
 

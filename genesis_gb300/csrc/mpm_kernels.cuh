@@ -78,6 +78,13 @@ struct SceneDev {
   int64_t n_particles;
 };
 
+// Kinematic rigid collider of the grid op (mpm_collider in float).
+struct ColliderDev {
+  int32_t type, scene, pad0, pad1;
+  float pos[3], quat[4], size[3], com[3], lin[3], ang[3];
+  float friction, softness, restitution, pad2;
+};
+
 struct KParams {
   const SceneDev* scenes;
   const MaterialDev* mats;
@@ -115,6 +122,9 @@ struct KParams {
   float eps_norm;              // gs.EPS for Matrix.norm(eps)
   uint32_t* status;
   unsigned long long* fp64_count;
+  const ColliderDev* colliders;  // kinematic colliders applied by k_grid_op (n_colliders > 0)
+  int32_t n_colliders;
+  double* collider_acc;        // [n_colliders][6] reaction force and torque
   int32_t fuse_grid;           // G2P applies the grid op while staging its tile and clears the other buffer
   int32_t* nlist_reset;        // active-list length that k_perm resets at the end of a fused substep
 };
@@ -136,21 +146,29 @@ __device__ __forceinline__ bool stencil_origin(const SceneDev& S, const float* x
 // Grid op of one node (legacy_coupler.py:356-501 with MPM alone): v = p/m + dt g where the node
 // holds mass, then the free-slip separating boundary on node positions (boundaries.py:22-32).
 // (gx, gy, gz) is the node index within its scene's grid.
-__device__ __forceinline__ float4 grid_velocity(const SceneDev& S, float4 q, int gx, int gy, int gz) {
-  float v[3] = {0.f, 0.f, 0.f};
-  if (q.w > S.eps) {
-    const float inv = 1.f / q.w;
-    v[0] = inv * q.x + S.dt * S.grav[0];
-    v[1] = inv * q.y + S.dt * S.grav[1];
-    v[2] = inv * q.z + S.dt * S.grav[2];
-    const int g[3] = {gx, gy, gz};
+__device__ __forceinline__ bool grid_free_velocity(const SceneDev& S, float4 q, float* v) {
+  v[0] = v[1] = v[2] = 0.f;
+  if (!(q.w > S.eps)) return false;
+  const float inv = 1.f / q.w;
+  v[0] = inv * q.x + S.dt * S.grav[0];
+  v[1] = inv * q.y + S.dt * S.grav[1];
+  v[2] = inv * q.z + S.dt * S.grav[2];
+  return true;
+}
+
+__device__ __forceinline__ void grid_boundary(const SceneDev& S, float* v, int gx, int gy, int gz) {
+  const int g[3] = {gx, gy, gz};
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const float pos = (float)(g[d] + S.offset[d]) * S.dx;
-      if (pos >= S.hi[d] && v[d] >= 0.f) v[d] *= -S.restitution;
-      else if (pos <= S.lo[d] && v[d] <= 0.f) v[d] *= -S.restitution;
-    }
+  for (int d = 0; d < 3; ++d) {
+    const float pos = (float)(g[d] + S.offset[d]) * S.dx;
+    if (pos >= S.hi[d] && v[d] >= 0.f) v[d] *= -S.restitution;
+    else if (pos <= S.lo[d] && v[d] <= 0.f) v[d] *= -S.restitution;
   }
+}
+
+__device__ __forceinline__ float4 grid_velocity(const SceneDev& S, float4 q, int gx, int gy, int gz) {
+  float v[3];
+  if (grid_free_velocity(S, q, v)) grid_boundary(S, v, gx, gy, gz);
   return make_float4(v[0], v[1], v[2], q.w);
 }
 

@@ -268,6 +268,24 @@ class MPMSolver:
         _lib.check(self._lib.mpm_get_grid(self._ctx, scene, _lib.ptr(out), _stream_handle()), self._ctx, "mpm_get_grid")
         return out
 
+    # ------------------------------------------------------------------ rigid coupling
+    def set_colliders(self, colliders) -> None:
+        """Kinematic rigid colliders coupled in the grid op (genesis_gb300.coupling.Collider list;
+        call again whenever they move)."""
+        recs = [c.to_c() for c in colliders]
+        arr = (_lib.MpmCollider * max(1, len(recs)))(*recs)
+        _lib.check(self._lib.mpm_set_colliders(self._ctx, len(recs), arr), self._ctx, "mpm_set_colliders")
+        self._n_colliders = len(recs)
+
+    def get_collider_forces(self, reset: bool = True) -> np.ndarray:
+        """[n_colliders, 6]: force (xyz) and torque about each collider's com exerted by the
+        particles, summed over the substeps since the last reset."""
+        n = getattr(self, "_n_colliders", 0)
+        out = np.zeros((max(1, n), 6), dtype=np.float64)
+        _lib.check(self._lib.mpm_get_collider_forces(self._ctx, out.ctypes.data, int(reset), _stream_handle()),
+                   self._ctx, "mpm_get_collider_forces")
+        return out[:n]
+
     # ------------------------------------------------------------------ kinematic links
     def set_link_poses(self, pos, quat) -> None:
         """Poses of the links that particle constraints follow (the reference reads them from the

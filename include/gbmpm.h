@@ -182,6 +182,42 @@ int mpm_substep_post(mpm_ctx* ctx, void* stream);
  * holds (vel_out xyz, mass).  Replaces reading MPMSolver.grid (mpm_solver.py:137-148). */
 int mpm_get_grid(mpm_ctx* ctx, int64_t scene, float* out, void* stream);
 
+/* Kinematic rigid colliders coupled in the grid op (legacy_coupler.py:134-218, 284-347, called
+ * from mpm_grid_op :389-403).  For every grid node with mass, after gravity and before the domain
+ * boundary, each collider of the node's scene (in array order) with
+ * influence = min(exp(-sdf / max(1e-10, softness)), 1) > 0.1 and an approaching relative velocity
+ * (v - v_rigid) . n < 0 gets: tangential part reduced by friction * |normal part| (never
+ * reversed), normal part scaled by -restitution, blended with the old relative velocity by the
+ * influence; v_rigid = lin_vel + ang_vel x (x - com).  The reaction force -m dv / dt on the
+ * collider (m = node mass / 1e3, the particle_volume_scale) and its torque about `com` are
+ * accumulated on the device.  Sphere and plane SDFs are the reference's analytic ones
+ * (utils/sdf.py:119-126, 372-378); the box SDF is analytic here (the reference samples a
+ * precomputed SDF grid for boxes).  With colliders set, the grid op runs as its own kernel. */
+#define MPM_COLLIDER_SPHERE 0 /* size[0] = radius */
+#define MPM_COLLIDER_PLANE 1  /* size = plane normal in the collider frame; sdf = n . x_local */
+#define MPM_COLLIDER_BOX 2    /* size = half extents */
+typedef struct mpm_collider {
+  int32_t type;
+  int32_t scene;        /* scene index, or -1: every scene */
+  double pos[3];        /* collider position (world) */
+  double quat[4];       /* orientation (w, x, y, z) */
+  double size[3];
+  double com[3];        /* point the angular velocity turns about (the link's root COM) */
+  double lin_vel[3];
+  double ang_vel[3];
+  double friction;      /* coup_friction */
+  double softness;      /* coup_softness */
+  double restitution;   /* coup_restitution */
+} mpm_collider;
+
+/* Replace the collider set (n may be 0); host array, copied before returning.  Resets the force
+ * accumulators. */
+int mpm_set_colliders(mpm_ctx* ctx, int32_t n, const mpm_collider* colliders);
+
+/* Force (xyz) and torque about com (xyz) exerted by the particles on each collider, summed over
+ * the substeps since the last reset: out_host [n][6].  Synchronises `stream`. */
+int mpm_get_collider_forces(mpm_ctx* ctx, double* out_host, int32_t reset, void* stream);
+
 /* Soft particle-to-link constraints (mpm_solver.py:1052-1128; mpm_entity.py:631-690).
  * mpm_set_particle_constraints: for each scene b of [scene_begin, scene_end) and each particle
  * [particle_start, particle_start + n) of it with mask[b * n + i] != 0, attach the particle to

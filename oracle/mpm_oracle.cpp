@@ -12,7 +12,9 @@
 //   MPMSolver.__init__ constants      genesis/engine/solvers/mpm_solver.py:32-80
 //   compute_F_tmp / svd               mpm_solver.py:293-307
 //   p2g (material, stress, scatter)   mpm_solver.py:322-421
-//   grid op (no coupling partners)    genesis/engine/couplers/legacy_coupler.py:356-501
+//   grid op                           genesis/engine/couplers/legacy_coupler.py:356-501
+//   rigid coupling (kinematic         legacy_coupler.py:166-218, 284-347; SDFs utils/sdf.py:119-126,
+//     colliders)                      372-378 (sphere, plane); boxes use their exact distance
 //   g2p + particle boundary           mpm_solver.py:423-481, engine/boundaries/boundaries.py:22-32
 //   materials                         genesis/engine/materials/MPM/{base,elastic,liquid,sand,snow,
 //                                     elasto_plastic,muscle}.py
@@ -45,6 +47,14 @@ typedef struct oracle_scene {
   double eps;          // gs.EPS (grid-op mass threshold and Matrix.norm eps)
   double restitution;  // CubeBoundary restitution (0)
 } oracle_scene;
+
+// Kinematic rigid collider: same layout as mpm_collider of the library header.
+typedef struct oracle_collider {
+  int32_t type;  // 0 sphere (size[0] radius), 1 plane (size = normal, collider frame), 2 box (half extents)
+  int32_t scene;
+  double pos[3], quat[4], size[3], com[3], lin_vel[3], ang_vel[3];
+  double friction, softness, restitution;
+} oracle_collider;
 
 typedef struct oracle_material {
   int32_t type;   // 0 elastic, 1 liquid, 2 sand, 3 snow, 4 elastoplastic, 5 muscle
@@ -339,6 +349,99 @@ M3<T> update_stress(const Mat<T>& m, const M3<T>& U, const M3<T>& S, const M3<T>
   }
 }
 
+// Colliders applied in the grid op of every run (set by oracle_set_colliders) and the reaction
+// force / torque they accumulated.
+std::vector<oracle_collider> g_colliders;
+std::vector<double> g_collider_acc;
+
+// gu.transform_by_quat with q = (w, x, y, z) (utils/geom.py:256-271).
+template <typename T>
+void quat_rot(const double* q, const T* v, T* o) {
+  const T w = (T)q[0], x = (T)q[1], y = (T)q[2], z = (T)q[3];
+  o[0] = v[0] * (x * x + w * w - y * y - z * z) + v[1] * (2 * x * y - 2 * w * z) + v[2] * (2 * x * z + 2 * w * y);
+  o[1] = v[0] * (2 * w * z + 2 * x * y) + v[1] * (w * w - x * x + y * y - z * z) + v[2] * (-2 * w * x + 2 * y * z);
+  o[2] = v[0] * (-2 * w * y + 2 * x * z) + v[1] * (2 * w * x + 2 * y * z) + v[2] * (w * w - x * x - y * y + z * z);
+}
+
+// Signed distance and unit normal: sphere and plane as utils/sdf.py:119-126, 372-378; a box by
+// its exact distance function (outside: the clamped offset; inside: the nearest face).
+template <typename T>
+T collider_sdf(const oracle_collider& c, const T* x, T eps, T* n) {
+  T d[3] = {x[0] - (T)c.pos[0], x[1] - (T)c.pos[1], x[2] - (T)c.pos[2]};
+  if (c.type == 0) {
+    const T ln = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2] + eps);
+    for (int k = 0; k < 3; ++k) n[k] = d[k] / ln;
+    return std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) - (T)c.size[0];
+  }
+  const double qi[4] = {c.quat[0], -c.quat[1], -c.quat[2], -c.quat[3]};
+  T l[3], gl[3], g[3], sd;
+  quat_rot(qi, d, l);
+  if (c.type == 1) {
+    sd = l[0] * (T)c.size[0] + l[1] * (T)c.size[1] + l[2] * (T)c.size[2];
+    for (int k = 0; k < 3; ++k) gl[k] = (T)c.size[k];
+  } else {
+    T q[3], out2 = 0;
+    int ax = 0;
+    for (int k = 0; k < 3; ++k) {
+      q[k] = std::fabs(l[k]) - (T)c.size[k];
+      const T o = std::max(q[k], (T)0);
+      out2 += o * o;
+      if (q[k] > q[ax]) ax = k;
+    }
+    sd = std::sqrt(out2) + std::min(std::max(q[0], std::max(q[1], q[2])), (T)0);
+    for (int k = 0; k < 3; ++k) {
+      const T sg = l[k] < 0 ? (T)-1 : (T)1;
+      gl[k] = out2 > 0 ? sg * std::max(q[k], (T)0) : (k == ax ? sg : (T)0);
+    }
+  }
+  quat_rot(c.quat, gl, g);
+  const T gn = std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2] + eps);
+  for (int k = 0; k < 3; ++k) n[k] = g[k] / gn;
+  return sd;
+}
+
+// legacy_coupler.py:166-218 and 284-347: relative-velocity projection with friction,
+// restitution and the SDF influence; returns the reaction on the collider in acc[6].
+template <typename T>
+void collide_node(int scene, const T* x, T* v, T mass, T dt, T eps) {
+  for (size_t ci = 0; ci < g_colliders.size(); ++ci) {
+    const oracle_collider& c = g_colliders[ci];
+    if (c.scene >= 0 && c.scene != scene) continue;
+    T n[3];
+    const T sd = collider_sdf(c, x, eps, n);
+    const T influence = std::min(std::exp(-sd / std::max((T)1e-10, (T)c.softness)), (T)1);
+    if (!(influence > (T)0.1)) continue;
+    const T r[3] = {x[0] - (T)c.com[0], x[1] - (T)c.com[1], x[2] - (T)c.com[2]};
+    const T w[3] = {(T)c.ang_vel[0], (T)c.ang_vel[1], (T)c.ang_vel[2]};
+    const T vr[3] = {w[1] * r[2] - w[2] * r[1] + (T)c.lin_vel[0], w[2] * r[0] - w[0] * r[2] + (T)c.lin_vel[1],
+                     w[0] * r[1] - w[1] * r[0] + (T)c.lin_vel[2]};
+    T rv[3];
+    for (int k = 0; k < 3; ++k) rv[k] = v[k] - vr[k];
+    const T rvn = rv[0] * n[0] + rv[1] * n[1] + rv[2] * n[2];
+    if (!(rvn < 0)) continue;
+    T rt[3];
+    for (int k = 0; k < 3; ++k) rt[k] = rv[k] - rvn * n[k];
+    const T rtn = std::sqrt(rt[0] * rt[0] + rt[1] * rt[1] + rt[2] * rt[2] + eps);
+    const T mag = std::max((T)0, rtn + rvn * (T)c.friction);
+    T f[3];
+    for (int k = 0; k < 3; ++k) {
+      const T rnew = rt[k] / rtn * mag - n[k] * rvn * (T)c.restitution;
+      const T nv = vr[k] + rnew * influence + rv[k] * (1 - influence);
+      f[k] = -mass * (nv - v[k]) / dt;
+      v[k] = nv;
+    }
+    double* acc = g_collider_acc.data() + ci * 6;
+    const double tq[3] = {(double)(r[1] * f[2] - r[2] * f[1]), (double)(r[2] * f[0] - r[0] * f[2]),
+                          (double)(r[0] * f[1] - r[1] * f[0])};
+    for (int k = 0; k < 3; ++k) {
+#pragma omp atomic
+      acc[k] += (double)f[k];
+#pragma omp atomic
+      acc[3 + k] += tq[k];
+    }
+  }
+}
+
 template <typename T>
 struct Scene {
   T dt, dx, inv_dx, p_vol, eps, restitution;
@@ -485,6 +588,11 @@ int run(const oracle_scene* sc, const oracle_material* mats, int n_mats, int64_t
       const int64_t idx[3] = {I / (ry * rz), (I / rz) % ry, I % rz};
       T v[3];
       for (int d = 0; d < 3; ++d) v[d] = (1 / gm[I]) * gp[I * 3 + d] + S.dt * S.g[d];
+      if (!g_colliders.empty()) {  // rigid coupling before the boundary (legacy_coupler.py:389-403)
+        T x[3];
+        for (int d = 0; d < 3; ++d) x[d] = (T)(idx[d] + S.off[d]) * S.dx;
+        collide_node<T>(0, x, v, gm[I] / (T)1e3, S.dt, S.eps);
+      }
       for (int d = 0; d < 3; ++d) {
         const T p = (T)(idx[d] + S.off[d]) * S.dx;
         if (p >= S.hi[d] && v[d] >= 0) v[d] *= -S.restitution;
@@ -590,6 +698,17 @@ void oracle_material_f64(const oracle_material* mm, const double* F_tmp, double 
   std::memcpy(F_new, Fn.a, sizeof(Fn.a));
   *Jp_new = jn;
   std::memcpy(stress, st.a, sizeof(st.a));
+}
+
+// Colliders for the following runs (n = 0 removes them); resets the force accumulators.
+void oracle_set_colliders(int n, const oracle_collider* c) {
+  g_colliders.assign(c, c + n);
+  g_collider_acc.assign((size_t)n * 6, 0.0);
+}
+
+// Reaction force and torque accumulated on each collider: out [n][6].
+void oracle_collider_forces(double* out) {
+  for (size_t i = 0; i < g_collider_acc.size(); ++i) out[i] = g_collider_acc[i];
 }
 
 int oracle_grid_res(const oracle_scene* sc, int64_t* res3) {

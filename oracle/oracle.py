@@ -53,6 +53,22 @@ class OracleMaterial(ctypes.Structure):
     ]
 
 
+class _Collider(ctypes.Structure):
+    _fields_ = [
+        ("type", ctypes.c_int32),
+        ("scene", ctypes.c_int32),
+        ("pos", ctypes.c_double * 3),
+        ("quat", ctypes.c_double * 4),
+        ("size", ctypes.c_double * 3),
+        ("com", ctypes.c_double * 3),
+        ("lin_vel", ctypes.c_double * 3),
+        ("ang_vel", ctypes.c_double * 3),
+        ("friction", ctypes.c_double),
+        ("softness", ctypes.c_double),
+        ("restitution", ctypes.c_double),
+    ]
+
+
 MAT_TYPES = {"elastic": 0, "liquid": 1, "sand": 2, "snow": 3, "elastoplastic": 4, "muscle": 5}
 FP32_EPS = float(np.finfo(np.float32).eps)
 
@@ -77,6 +93,10 @@ def load():
         lib.oracle_material_f64.restype = None
         lib.oracle_grid_res.argtypes = [ctypes.POINTER(OracleScene), P]
         lib.oracle_grid_res.restype = ctypes.c_int
+        lib.oracle_set_colliders.argtypes = [ctypes.c_int, P]
+        lib.oracle_set_colliders.restype = None
+        lib.oracle_collider_forces.argtypes = [P]
+        lib.oracle_collider_forces.restype = None
         _lib = lib
     return _lib
 
@@ -155,6 +175,21 @@ def run(scene: OracleScene, materials, state: dict, n_substeps: int, dtype=np.fl
     out = dict(state)
     out.update(st)
     return out, grid, touched.value
+
+
+def set_colliders(colliders) -> None:
+    """Kinematic colliders (list of genesis_gb300._lib.MpmCollider, same layout) for the following
+    runs; an empty list removes them.  Resets the accumulated reaction forces."""
+    lib = load()
+    n = len(colliders)
+    arr = (_Collider * max(1, n))(*[_Collider.from_buffer_copy(bytes(c)) for c in colliders])
+    lib.oracle_set_colliders(n, arr)
+
+
+def collider_forces(n: int) -> np.ndarray:
+    out = np.zeros((max(1, n), 6))
+    load().oracle_collider_forces(out.ctypes.data)
+    return out[:n]
 
 
 def svd(A):

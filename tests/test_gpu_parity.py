@@ -354,3 +354,45 @@ def test_emitter_activates_droplets_and_recycles(gs):
     while em._next_particle != 0:  # keep emitting until the pool wraps
         em.emit("sphere", 0.08, droplet_length=0.05, pos=(0.5, 0.5, 0.6), direction=(0.0, 0.0, -1.0), speed=1.5)
     assert int(ent.get_particles_active().sum()) <= 3000
+
+
+def test_rigid_colliders_match_oracle(gs, oracle):
+    """MPM <-> rigid coupling in the grid op (legacy_coupler.py:166-218, 284-347) with kinematic
+    sphere / rotated box / tilted plane colliders, one of them moving and spinning: particle state
+    and the reaction force on each collider against the FP64 oracle."""
+    from genesis_gb300.coupling import Collider
+
+    scene, cube, mat = c1_scene(gs, size=0.12)
+    solver = scene.sim.mpm_solver
+    st = solver.get_state()
+    vel = st.vel.clone()
+    vel[..., 2] = -2.0
+    st.vel = vel
+    solver.set_state(0, st)
+    cols = [
+        Collider("sphere", pos=(0.46, 0.5, 0.30), radius=0.04, lin_vel=(0.2, 0.0, 0.1), ang_vel=(0.0, 3.0, 0.0),
+                 coup_friction=0.4),
+        Collider("box", pos=(0.55, 0.52, 0.30), quat=(np.cos(0.3), 0.0, np.sin(0.3), 0.0),
+                 half_extents=(0.03, 0.04, 0.015), coup_restitution=0.3, coup_softness=0.004),
+        Collider("plane", pos=(0.5, 0.5, 0.325), quat=(np.cos(0.1), np.sin(0.1), 0.0, 0.0), normal=(0.0, 0.0, 1.0)),
+    ]
+    solver.set_colliders(cols)
+    st0 = solver.get_state()
+    n_sub = 60
+    for _ in range(n_sub):
+        scene.step()
+    st1 = solver.get_state()
+    f_gpu = solver.get_collider_forces()
+    oracle.set_colliders([c.to_c() for c in cols])
+    try:
+        ref, _, _ = oracle.run(oracle_scene_for(oracle, solver), [oracle.from_c_material(mat.to_c(0))],
+                               oracle_state(st0), n_sub)
+        f_ref = oracle.collider_forces(len(cols))
+    finally:
+        oracle.set_colliders([])
+    assert np.abs(f_ref[:, :3]).max(axis=1).min() > 1.0, f_ref  # every collider was hit
+    err = np.abs(st1.pos[0].double().cpu().numpy() - ref["pos"]).max()
+    assert err <= POS_TOL, err
+    assert np.abs(st1.vel[0].double().cpu().numpy() - ref["vel"]).max() < 5e-3
+    assert np.allclose(f_gpu, f_ref, rtol=2e-3, atol=2e-3 * np.abs(f_ref).max()), (f_gpu, f_ref)
+    solver.set_colliders([])
