@@ -21,7 +21,7 @@ import types as _types
 import numpy as np
 
 from . import materials as _materials_mod
-from . import morphs
+from . import force_fields, morphs
 from . import options as _options_mod
 from .entity import ACTIVE, INACTIVE
 from .exceptions import GenesisException

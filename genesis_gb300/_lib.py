@@ -96,6 +96,31 @@ class MpmCollider(ctypes.Structure):
 COLLIDER_SPHERE, COLLIDER_PLANE, COLLIDER_BOX = 0, 1, 2
 
 
+class MpmForceField(ctypes.Structure):
+    """mpm_force_field (include/gbmpm.h)."""
+
+    _fields_ = [
+        ("type", c_int32),
+        ("active", c_int32),
+        ("direction", c_double * 3),
+        ("center", c_double * 3),
+        ("strength", c_double),
+        ("radius", c_double),
+        ("falloff_pow", c_double),
+        ("flow", c_double),
+        ("linear", c_double),
+        ("quadratic", c_double),
+        ("strength_perpendicular", c_double),
+        ("strength_radial", c_double),
+        ("falloff_min", c_double),
+        ("falloff_max", c_double),
+        ("damping", c_double),
+    ]
+
+
+FF_CONSTANT, FF_WIND, FF_POINT, FF_DRAG, FF_VORTEX = 0, 1, 2, 3, 4
+
+
 class MpmSceneConfig(ctypes.Structure):
     _fields_ = [
         ("substep_dt", c_double),
@@ -140,6 +165,7 @@ _SIGNATURES = {
     "mpm_remove_particle_constraints": (c_int32, [_P, c_int64, c_int64, c_int64, c_int64, _P, _P]),
     "mpm_set_link_poses": (c_int32, [_P, c_int32, _P]),
     "mpm_set_colliders": (c_int32, [_P, c_int32, _P]),
+    "mpm_set_force_fields": (c_int32, [_P, c_int32, _P]),
     "mpm_get_collider_forces": (c_int32, [_P, _P, c_int32, _P]),
     "mpm_version": (c_int32, []),
     "mpm_ctx_create_pool": (c_int32, [ctypes.c_void_p, c_int32, ctypes.POINTER(c_void_p)]),

@@ -77,6 +77,8 @@ struct mpm_ctx {
   unsigned long long* d_tmp64 = nullptr;
   uint32_t* d_pin = nullptr;
   ConstraintDev* d_cons = nullptr;  // particle constraints by reference row (allocated on first use)
+  ForceFieldDev* d_ffs = nullptr;      // force fields (capacity MAX_FORCE_FIELDS once allocated)
+  int32_t n_ffs = 0;
   ColliderDev* d_colliders = nullptr;  // kinematic colliders (capacity MAX_COLLIDERS once allocated)
   double* d_collider_acc = nullptr;    // [MAX_COLLIDERS][6]
   int32_t n_colliders = 0;
@@ -180,6 +182,8 @@ KParams make_params(mpm_ctx* ctx, int src, int dst, int g) {
   P.n_items = ctx->d_nitems;
   P.partials = ctx->d_partials;
   P.scan_state = ctx->d_scan_state;
+  P.ffs = ctx->d_ffs;
+  P.n_ffs = ctx->n_ffs;
   P.colliders = ctx->d_colliders;
   P.n_colliders = ctx->n_colliders;
   P.collider_acc = ctx->d_collider_acc;
@@ -296,7 +300,7 @@ int launch_post(mpm_ctx* ctx, int c, cudaStream_t s, bool fuse_grid = false) {
 // Without pinned particles the grid op is folded into G2P (k_grid_op is not launched); the
 // split-phase entry points keep it separate so a coupler can act on the velocity grid.
 int launch_substep(mpm_ctx* ctx, int c, cudaStream_t s) {
-  const bool fuse = ctx->d_pin == nullptr && ctx->n_colliders == 0;
+  const bool fuse = ctx->d_pin == nullptr && ctx->n_colliders == 0 && ctx->n_ffs == 0;
   int r = launch_pre(ctx, c, s);
   if (!r && !fuse) r = launch_grid(ctx, c, s);
   if (!r) r = launch_post(ctx, c, s, fuse);
@@ -665,6 +669,7 @@ int mpm_ctx_destroy(mpm_ctx* ctx) {
   if (ctx->d_pin) cudaFree(ctx->d_pin);
   if (ctx->d_cons) cudaFree(ctx->d_cons);
   if (ctx->d_colliders) cudaFree(ctx->d_colliders);
+  if (ctx->d_ffs) cudaFree(ctx->d_ffs);
   if (ctx->d_collider_acc) cudaFree(ctx->d_collider_acc);
   if (ctx->d_links) cudaFree(ctx->d_links);
   if (ctx->ev_in) cudaEventDestroy(ctx->ev_in);
@@ -853,6 +858,52 @@ int mpm_get_grid(mpm_ctx* ctx, int64_t scene, float* out, void* stream) {
 }
 
 constexpr int32_t MAX_COLLIDERS = 256;
+constexpr int32_t MAX_FORCE_FIELDS = 64;
+
+int mpm_set_force_fields(mpm_ctx* ctx, int32_t n, const mpm_force_field* fields) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (n < 0 || n > MAX_FORCE_FIELDS || (n > 0 && !fields)) return fail(ctx, MPM_ERR_BAD_ARG, "bad force-field arguments");
+  if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "force fields inside a substep");
+  std::vector<ForceFieldDev> h((size_t)n);
+  for (int32_t i = 0; i < n; ++i) {
+    const mpm_force_field& f = fields[i];
+    if (f.type < MPM_FF_CONSTANT || f.type > MPM_FF_VORTEX) return fail(ctx, MPM_ERR_BAD_ARG, "unknown force field");
+    ForceFieldDev& d = h[(size_t)i];
+    std::memset(&d, 0, sizeof(d));
+    d.type = f.type;
+    d.active = f.active ? 1 : 0;
+    for (int k = 0; k < 3; ++k) {
+      d.dir[k] = (float)f.direction[k];
+      d.center[k] = (float)f.center[k];
+    }
+    d.strength = (float)f.strength;
+    d.radius = (float)f.radius;
+    d.falloff_pow = (float)f.falloff_pow;
+    d.flow = (float)f.flow;
+    d.linear = (float)f.linear;
+    d.quadratic = (float)f.quadratic;
+    d.s_perp = (float)f.strength_perpendicular;
+    d.s_radial = (float)f.strength_radial;
+    d.falloff_min = (float)f.falloff_min;
+    d.falloff_max = (float)f.falloff_max;  // +inf stays +inf
+    d.damping = (float)f.damping;
+  }
+  CK(cudaSetDevice(ctx->device));
+  if (!ctx->d_ffs && n > 0) {
+    cudaError_t e = cudaMalloc((void**)&ctx->d_ffs, sizeof(ForceFieldDev) * MAX_FORCE_FIELDS);
+    if (e != cudaSuccess) {
+      ctx->d_ffs = nullptr;
+      return fail(ctx, MPM_ERR_OOM, "force-field table allocation failed");
+    }
+  }
+  if (n > 0) {
+    CK(cudaMemcpyAsync(ctx->d_ffs, h.data(), sizeof(ForceFieldDev) * n, cudaMemcpyHostToDevice, ctx->cs));
+    CK(cudaStreamSynchronize(ctx->cs));
+  }
+  if (n != ctx->n_ffs) drop_graph(ctx);  // the count is a captured kernel argument
+  ctx->n_ffs = n;
+  return MPM_OK;
+}
 
 int mpm_set_colliders(mpm_ctx* ctx, int32_t n, const mpm_collider* colliders) {
   if (!ctx) return MPM_ERR_BAD_ARG;

@@ -990,6 +990,42 @@ __device__ __forceinline__ void rot(const float* q, const float* v, float* o) { 
   o[2] = v[0] * (-2.f * w * y + 2.f * x * z) + v[1] * (2.f * w * x + 2.f * y * z) + v[2] * (w * w - x * x - y * y + z * z);
 }
 
+// engine/force_fields.py _get_acc of each field type (Constant :73, Wind :122, Point :178,
+// Drag :220, Vortex :319) at node position x with the current node velocity v.
+__device__ __forceinline__ void ff_acc(const ForceFieldDev& f, const float* x, const float* v, float eps, float* a) {
+  a[0] = a[1] = a[2] = 0.f;
+  if (f.type == MPM_FF_CONSTANT) {
+    for (int k = 0; k < 3; ++k) a[k] = f.dir[k] * f.strength;
+  } else if (f.type == MPM_FF_WIND) {
+    const float r[3] = {x[0] - f.center[0], x[1] - f.center[1], x[2] - f.center[2]};
+    const float c[3] = {r[1] * f.dir[2] - r[2] * f.dir[1], r[2] * f.dir[0] - r[0] * f.dir[2],
+                        r[0] * f.dir[1] - r[1] * f.dir[0]};
+    if (!(sqrtf(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]) > f.radius))
+      for (int k = 0; k < 3; ++k) a[k] = f.dir[k] * f.strength;
+  } else if (f.type == MPM_FF_POINT) {
+    const float r[3] = {x[0] - f.center[0], x[1] - f.center[1], x[2] - f.center[2]};
+    const float rad = sqrtf(r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + eps);  // norm(gs.EPS)
+    const float fall = 1.f / powf(rad + 1.f, f.falloff_pow);
+    for (int k = 0; k < 3; ++k) {
+      float ak = f.strength * (r[k] / rad);
+      ak += (ak - v[k]) * f.flow;
+      a[k] = ak * fall;
+    }
+  } else if (f.type == MPM_FF_DRAG) {
+    const float vn = sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    for (int k = 0; k < 3; ++k) a[k] = -f.linear * v[k] - f.quadratic * vn * v[k];
+  } else if (f.type == MPM_FF_VORTEX) {
+    const float rx = x[0] - f.center[0], ry = x[1] - f.center[1];
+    const float rad = sqrtf(rx * rx + ry * ry);
+    float fall = 0.f;
+    if (rad < f.falloff_min) fall = 1.f;
+    else if (rad < f.falloff_max) fall = 1.f / powf(rad - f.falloff_min + 1.f, f.falloff_pow);
+    a[0] = fall * (f.s_perp * -ry + f.s_radial * -rx) - f.damping * v[0];
+    a[1] = fall * (f.s_perp * rx + f.s_radial * -ry) - f.damping * v[1];
+    a[2] = fall * 0.f - f.damping * v[2];
+  }
+}
+
 // Signed distance and outward unit normal of a collider at world point x
 // (utils/sdf.py:119-126 and 372-378 for sphere and plane; analytic box).
 __device__ __forceinline__ float collider_sdf(const ColliderDev& c, const float* x, float eps, float* n) {
@@ -1101,13 +1137,19 @@ __global__ void __launch_bounds__(256) k_grid_op(KParams P) {
         atomicAnd(&P.pin[a >> 5], ~bit);
       }
     }
-    if (P.n_colliders == 0) {
+    if (P.n_colliders == 0 && P.n_ffs == 0) {
       *node = grid_velocity(S, q, g[0], g[1], g[2]);
-    } else {  // gravity, then the colliders (legacy_coupler.py:389-403), then the boundary
+    } else {  // gravity, force fields (:381-383), colliders (:389-403), then the boundary
       float v[3];
       if (grid_free_velocity(S, q, v)) {
         const float x[3] = {(float)(g[0] + S.offset[0]) * S.dx, (float)(g[1] + S.offset[1]) * S.dx,
                             (float)(g[2] + S.offset[2]) * S.dx};
+        for (int fi = 0; fi < P.n_ffs; ++fi) {
+          if (!P.ffs[fi].active) continue;
+          float a[3];
+          ff_acc(P.ffs[fi], x, v, S.eps, a);
+          for (int k = 0; k < 3; ++k) v[k] += a[k] * S.dt;
+        }
         collide_node(P, S, P.block_scene[blk], x, v, q.w / 1e3f);
         grid_boundary(S, v, g[0], g[1], g[2]);
       }

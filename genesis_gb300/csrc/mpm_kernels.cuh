@@ -85,6 +85,14 @@ struct ColliderDev {
   float friction, softness, restitution, pad2;
 };
 
+// External acceleration field of the grid op (mpm_force_field in float).
+struct ForceFieldDev {
+  int32_t type, active, pad0, pad1;
+  float dir[3], center[3];
+  float strength, radius, falloff_pow, flow, linear, quadratic;
+  float s_perp, s_radial, falloff_min, falloff_max, damping, pad2;
+};
+
 struct KParams {
   const SceneDev* scenes;
   const MaterialDev* mats;
@@ -122,6 +130,8 @@ struct KParams {
   float eps_norm;              // gs.EPS for Matrix.norm(eps)
   uint32_t* status;
   unsigned long long* fp64_count;
+  const ForceFieldDev* ffs;    // external acceleration fields applied by k_grid_op (n_ffs > 0)
+  int32_t n_ffs;
   const ColliderDev* colliders;  // kinematic colliders applied by k_grid_op (n_colliders > 0)
   int32_t n_colliders;
   double* collider_acc;        // [n_colliders][6] reaction force and torque

@@ -1,0 +1,184 @@
+"""External acceleration fields (genesis/engine/force_fields.py) applied in the MPM grid op.
+
+`scene.add_force_field(ff)` registers a field; it acts on grid velocities as
+v += acc(x, v) * dt after gravity (legacy_coupler.py:381-383), on the device.  Fields start
+inactive, as in the reference; `activate()` / `deactivate()` take effect at the next substep.
+Noise, Turbulence and Custom (a user Quadrants function) are not provided.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from . import _lib
+
+
+class ForceField:
+    _type = -1
+
+    def __init__(self):
+        self._active = False
+        self._solver = None
+
+    def activate(self):
+        self._active = True
+        self._sync()
+
+    def deactivate(self):
+        self._active = False
+        self._sync()
+
+    @property
+    def active(self):
+        return self._active
+
+    def _sync(self):
+        if self._solver is not None:
+            self._solver._upload_force_fields()
+
+    def to_c(self) -> "_lib.MpmForceField":
+        f = _lib.MpmForceField()
+        f.type = self._type
+        f.active = int(self._active)
+        f.falloff_max = float("inf")
+        self._fill(f)
+        return f
+
+    def _fill(self, f):
+        raise NotImplementedError
+
+
+def _dir(direction):
+    d = np.array(direction, dtype=np.float64)
+    if d.shape != (3,):
+        raise ValueError("direction must have shape (3,)")
+    return d / np.linalg.norm(d)
+
+
+def _vec3(v, name):
+    a = np.array(v, dtype=np.float64)
+    if a.shape != (3,):
+        raise ValueError(f"{name} must have shape (3,)")
+    return a
+
+
+class Constant(ForceField):
+    """force_fields.py:49-82: acc = direction * strength everywhere."""
+
+    _type = _lib.FF_CONSTANT
+
+    def __init__(self, direction=(1, 0, 0), strength=1.0):
+        super().__init__()
+        self._direction = _dir(direction)
+        self._strength = strength
+
+    def _fill(self, f):
+        f.direction[:] = tuple(self._direction)
+        f.strength = float(self._strength)
+
+    @property
+    def direction(self):
+        return self._direction
+
+    @property
+    def strength(self):
+        return self._strength
+
+
+class Wind(ForceField):
+    """force_fields.py:85-144: constant acceleration inside a cylinder about `center` along
+    `direction`."""
+
+    _type = _lib.FF_WIND
+
+    def __init__(self, direction=(1, 0, 0), strength=1.0, radius=1, center=(0, 0, 0)):
+        super().__init__()
+        self._direction = _dir(direction)
+        self._center = _vec3(center, "center")
+        self._strength = strength
+        self._radius = radius
+
+    def _fill(self, f):
+        f.direction[:] = tuple(self._direction)
+        f.center[:] = tuple(self._center)
+        f.strength = float(self._strength)
+        f.radius = float(self._radius)
+
+    @property
+    def radius(self):
+        return self._radius
+
+    @property
+    def center(self):
+        return self._center
+
+
+class Point(ForceField):
+    """force_fields.py:147-198: towards (strength > 0) or away from a point, with flow and falloff."""
+
+    _type = _lib.FF_POINT
+
+    def __init__(self, strength=1.0, position=(0, 0, 0), falloff_pow=0.0, flow=1.0):
+        super().__init__()
+        self._strength = strength
+        self._position = _vec3(position, "position")
+        self._falloff_pow = falloff_pow
+        self._flow = flow
+
+    def _fill(self, f):
+        f.center[:] = tuple(self._position)
+        f.strength = float(self._strength)
+        f.falloff_pow = float(self._falloff_pow)
+        f.flow = float(self._flow)
+
+    @property
+    def position(self):
+        return self._position
+
+
+class Drag(ForceField):
+    """force_fields.py:201-229: -linear v - quadratic |v| v."""
+
+    _type = _lib.FF_DRAG
+
+    def __init__(self, linear=0.0, quadratic=0.0):
+        super().__init__()
+        self._linear = linear
+        self._quadratic = quadratic
+
+    def _fill(self, f):
+        f.linear = float(self._linear)
+        f.quadratic = float(self._quadratic)
+
+
+class Vortex(ForceField):
+    """force_fields.py:263-369: swirl about the z axis through `center` with radial pull, falloff
+    and damping."""
+
+    _type = _lib.FF_VORTEX
+
+    def __init__(self, direction=(0.0, 0.0, 1.0), center=(0.0, 0.0, 0.0), strength_perpendicular=20.0,
+                 strength_radial=0.0, falloff_pow=2.0, falloff_min=0.01, falloff_max=np.inf, damping=0.0):
+        super().__init__()
+        self._direction = _dir(direction)
+        self._center = _vec3(center, "center")
+        self._strength_perpendicular = strength_perpendicular
+        self._strength_radial = strength_radial
+        self._falloff_pow = falloff_pow
+        self._falloff_min = falloff_min
+        self._falloff_max = falloff_max
+        self._damping = damping
+
+    def _fill(self, f):
+        f.direction[:] = tuple(self._direction)
+        f.center[:] = tuple(self._center)
+        f.strength_perpendicular = float(self._strength_perpendicular)
+        f.strength_radial = float(self._strength_radial)
+        f.falloff_pow = float(self._falloff_pow)
+        f.falloff_min = float(self._falloff_min)
+        f.falloff_max = float(self._falloff_max)
+        f.damping = float(self._damping)
+
+    @property
+    def center(self):
+        return self._center

@@ -149,6 +149,14 @@ class Scene:
         self._entities.append(entity)
         return entity
 
+    def add_force_field(self, force_field):
+        """scene.py:820-836: an external acceleration field acting on the MPM grid."""
+        if self._is_built:
+            raise GenesisException("Scene is already built.")
+        force_field.scene = self
+        self._sim.mpm_solver._add_force_field(force_field)
+        return force_field
+
     def add_emitter(self, material, max_particles=20000, surface=None):
         """scene.py:765-818: an MPM entity of `max_particles` inactive particles driven by an Emitter."""
         from .emitter import Emitter

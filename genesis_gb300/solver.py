@@ -169,6 +169,8 @@ class MPMSolver:
             )
         for entity in self._entities:
             entity._add_to_solver()
+        if getattr(self, "_ffs", None):
+            self._upload_force_fields()
 
     def _add_particles(self, particle_start, n, material_idx, active, pos_np):
         pos = torch.as_tensor(np.ascontiguousarray(pos_np, dtype=np.float32), device="cuda")
@@ -267,6 +269,23 @@ class MPMSolver:
         out = torch.empty((res[0], res[1], res[2], 4), dtype=torch.float32, device="cuda")
         _lib.check(self._lib.mpm_get_grid(self._ctx, scene, _lib.ptr(out), _stream_handle()), self._ctx, "mpm_get_grid")
         return out
+
+    # ------------------------------------------------------------------ force fields
+    def _add_force_field(self, ff) -> None:
+        if not hasattr(self, "_ffs"):
+            self._ffs = []
+        self._ffs.append(ff)
+        ff._solver = self
+        if self._ctx is not None:
+            self._upload_force_fields()
+
+    def _upload_force_fields(self) -> None:
+        ffs = getattr(self, "_ffs", [])
+        if self._ctx is None:
+            return
+        recs = [f.to_c() for f in ffs]
+        arr = (_lib.MpmForceField * max(1, len(recs)))(*recs)
+        _lib.check(self._lib.mpm_set_force_fields(self._ctx, len(recs), arr), self._ctx, "mpm_set_force_fields")
 
     # ------------------------------------------------------------------ rigid coupling
     def set_colliders(self, colliders) -> None:

@@ -182,6 +182,38 @@ int mpm_substep_post(mpm_ctx* ctx, void* stream);
  * holds (vel_out xyz, mass).  Replaces reading MPMSolver.grid (mpm_solver.py:137-148). */
 int mpm_get_grid(mpm_ctx* ctx, int64_t scene, float* out, void* stream);
 
+/* External acceleration fields of the grid op (engine/force_fields.py; applied at
+ * legacy_coupler.py:381-383 as v += acc(x, v) dt for each field in order, after gravity and before
+ * rigid coupling).  direction is normalised by the caller as the reference's constructors do.
+ *   CONSTANT: acc = direction * strength
+ *   WIND:     direction * strength inside the infinite cylinder of `radius` about the axis through
+ *             center along direction, 0 outside
+ *   POINT:    r = x - center, d = r / norm(r, eps); acc = strength d; acc += (acc - v) flow;
+ *             acc *= 1 / (|r|_eps + 1)^falloff_pow
+ *   DRAG:     -linear v - quadratic |v| v
+ *   VORTEX:   about the z axis through center: falloff 1 below falloff_min, 1/(r - falloff_min + 1)^
+ *             falloff_pow below falloff_max, 0 beyond; acc = falloff (strength_perpendicular
+ *             (-ry, rx, 0) + strength_radial (-rx, -ry, 0)) - damping v
+ * Inactive fields (active = 0) are skipped.  With any field set, the grid op runs as its own
+ * kernel. */
+#define MPM_FF_CONSTANT 0
+#define MPM_FF_WIND 1
+#define MPM_FF_POINT 2
+#define MPM_FF_DRAG 3
+#define MPM_FF_VORTEX 4
+typedef struct mpm_force_field {
+  int32_t type;
+  int32_t active;
+  double direction[3];
+  double center[3];
+  double strength, radius, falloff_pow, flow;
+  double linear, quadratic;
+  double strength_perpendicular, strength_radial, falloff_min, falloff_max, damping;
+} mpm_force_field;
+
+/* Replace the force-field set (n may be 0); host array, copied before returning. */
+int mpm_set_force_fields(mpm_ctx* ctx, int32_t n, const mpm_force_field* fields);
+
 /* Kinematic rigid colliders coupled in the grid op (legacy_coupler.py:134-218, 284-347, called
  * from mpm_grid_op :389-403).  For every grid node with mass, after gravity and before the domain
  * boundary, each collider of the node's scene (in array order) with

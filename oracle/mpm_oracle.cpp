@@ -13,6 +13,7 @@
 //   compute_F_tmp / svd               mpm_solver.py:293-307
 //   p2g (material, stress, scatter)   mpm_solver.py:322-421
 //   grid op                           genesis/engine/couplers/legacy_coupler.py:356-501
+//   force fields                      genesis/engine/force_fields.py (constant, wind, point, drag, vortex)
 //   rigid coupling (kinematic         legacy_coupler.py:166-218, 284-347; SDFs utils/sdf.py:119-126,
 //     colliders)                      372-378 (sphere, plane); boxes use their exact distance
 //   g2p + particle boundary           mpm_solver.py:423-481, engine/boundaries/boundaries.py:22-32
@@ -55,6 +56,15 @@ typedef struct oracle_collider {
   double pos[3], quat[4], size[3], com[3], lin_vel[3], ang_vel[3];
   double friction, softness, restitution;
 } oracle_collider;
+
+// External acceleration field: same layout as mpm_force_field of the library header.
+typedef struct oracle_force_field {
+  int32_t type;  // 0 constant, 1 wind, 2 point, 3 drag, 4 vortex
+  int32_t active;
+  double direction[3], center[3];
+  double strength, radius, falloff_pow, flow, linear, quadratic;
+  double strength_perpendicular, strength_radial, falloff_min, falloff_max, damping;
+} oracle_force_field;
 
 typedef struct oracle_material {
   int32_t type;   // 0 elastic, 1 liquid, 2 sand, 3 snow, 4 elastoplastic, 5 muscle
@@ -354,6 +364,43 @@ M3<T> update_stress(const Mat<T>& m, const M3<T>& U, const M3<T>& S, const M3<T>
 std::vector<oracle_collider> g_colliders;
 std::vector<double> g_collider_acc;
 
+std::vector<oracle_force_field> g_ffs;
+
+// engine/force_fields.py _get_acc: Constant :73, Wind :122, Point :178, Drag :220, Vortex :319.
+template <typename T>
+void ff_acc(const oracle_force_field& f, const T* x, const T* v, T eps, T* a) {
+  a[0] = a[1] = a[2] = 0;
+  const T dir[3] = {(T)f.direction[0], (T)f.direction[1], (T)f.direction[2]};
+  const T r[3] = {x[0] - (T)f.center[0], x[1] - (T)f.center[1], x[2] - (T)f.center[2]};
+  if (f.type == 0) {
+    for (int k = 0; k < 3; ++k) a[k] = dir[k] * (T)f.strength;
+  } else if (f.type == 1) {
+    const T c[3] = {r[1] * dir[2] - r[2] * dir[1], r[2] * dir[0] - r[0] * dir[2], r[0] * dir[1] - r[1] * dir[0]};
+    if (!(std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]) > (T)f.radius))
+      for (int k = 0; k < 3; ++k) a[k] = dir[k] * (T)f.strength;
+  } else if (f.type == 2) {
+    const T rad = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + eps);
+    const T fall = 1 / std::pow(rad + 1, (T)f.falloff_pow);
+    for (int k = 0; k < 3; ++k) {
+      T ak = (T)f.strength * (r[k] / rad);
+      ak += (ak - v[k]) * (T)f.flow;
+      a[k] = ak * fall;
+    }
+  } else if (f.type == 3) {
+    const T vn = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    for (int k = 0; k < 3; ++k) a[k] = -(T)f.linear * v[k] - (T)f.quadratic * vn * v[k];
+  } else if (f.type == 4) {
+    const T rad = std::sqrt(r[0] * r[0] + r[1] * r[1]);
+    T fall = 0;
+    if (rad < (T)f.falloff_min) fall = 1;
+    else if (rad < (T)f.falloff_max) fall = 1 / std::pow(rad - (T)f.falloff_min + 1, (T)f.falloff_pow);
+    const T sp = (T)f.strength_perpendicular, sr = (T)f.strength_radial, dm = (T)f.damping;
+    a[0] = fall * (sp * -r[1] + sr * -r[0]) - dm * v[0];
+    a[1] = fall * (sp * r[0] + sr * -r[1]) - dm * v[1];
+    a[2] = -dm * v[2];
+  }
+}
+
 // gu.transform_by_quat with q = (w, x, y, z) (utils/geom.py:256-271).
 template <typename T>
 void quat_rot(const double* q, const T* v, T* o) {
@@ -588,10 +635,16 @@ int run(const oracle_scene* sc, const oracle_material* mats, int n_mats, int64_t
       const int64_t idx[3] = {I / (ry * rz), (I / rz) % ry, I % rz};
       T v[3];
       for (int d = 0; d < 3; ++d) v[d] = (1 / gm[I]) * gp[I * 3 + d] + S.dt * S.g[d];
-      if (!g_colliders.empty()) {  // rigid coupling before the boundary (legacy_coupler.py:389-403)
+      if (!g_colliders.empty() || !g_ffs.empty()) {
         T x[3];
         for (int d = 0; d < 3; ++d) x[d] = (T)(idx[d] + S.off[d]) * S.dx;
-        collide_node<T>(0, x, v, gm[I] / (T)1e3, S.dt, S.eps);
+        for (const oracle_force_field& f : g_ffs) {  // force fields (legacy_coupler.py:381-383)
+          if (!f.active) continue;
+          T a[3];
+          ff_acc<T>(f, x, v, S.eps, a);
+          for (int d = 0; d < 3; ++d) v[d] += a[d] * S.dt;
+        }
+        collide_node<T>(0, x, v, gm[I] / (T)1e3, S.dt, S.eps);  // rigid coupling (:389-403)
       }
       for (int d = 0; d < 3; ++d) {
         const T p = (T)(idx[d] + S.off[d]) * S.dx;
@@ -705,6 +758,9 @@ void oracle_set_colliders(int n, const oracle_collider* c) {
   g_colliders.assign(c, c + n);
   g_collider_acc.assign((size_t)n * 6, 0.0);
 }
+
+// Force fields for the following runs (n = 0 removes them).
+void oracle_set_force_fields(int n, const oracle_force_field* f) { g_ffs.assign(f, f + n); }
 
 // Reaction force and torque accumulated on each collider: out [n][6].
 void oracle_collider_forces(double* out) {

@@ -95,6 +95,8 @@ def load():
         lib.oracle_grid_res.restype = ctypes.c_int
         lib.oracle_set_colliders.argtypes = [ctypes.c_int, P]
         lib.oracle_set_colliders.restype = None
+        lib.oracle_set_force_fields.argtypes = [ctypes.c_int, P]
+        lib.oracle_set_force_fields.restype = None
         lib.oracle_collider_forces.argtypes = [P]
         lib.oracle_collider_forces.restype = None
         _lib = lib
@@ -184,6 +186,14 @@ def set_colliders(colliders) -> None:
     n = len(colliders)
     arr = (_Collider * max(1, n))(*[_Collider.from_buffer_copy(bytes(c)) for c in colliders])
     lib.oracle_set_colliders(n, arr)
+
+
+def set_force_fields(fields) -> None:
+    """Force fields (list of genesis_gb300._lib.MpmForceField, same layout) for the following runs."""
+    n = len(fields)
+    buf = b"".join(bytes(f) for f in fields) or b"\0" * 8
+    arr = ctypes.create_string_buffer(buf, len(buf))
+    load().oracle_set_force_fields(n, arr)
 
 
 def collider_forces(n: int) -> np.ndarray:

@@ -16,6 +16,7 @@ STRUCTS = {
     "mpm_scene_config": "MpmSceneConfig",
     "mpm_pool_config": "MpmPoolConfig",
     "mpm_collider": "MpmCollider",
+    "mpm_force_field": "MpmForceField",
 }
 
 

@@ -396,3 +396,54 @@ def test_rigid_colliders_match_oracle(gs, oracle):
     assert np.abs(st1.vel[0].double().cpu().numpy() - ref["vel"]).max() < 5e-3
     assert np.allclose(f_gpu, f_ref, rtol=2e-3, atol=2e-3 * np.abs(f_ref).max()), (f_gpu, f_ref)
     solver.set_colliders([])
+
+
+def test_force_fields_match_oracle(gs, oracle):
+    """Force fields in the grid op (legacy_coupler.py:381-383, engine/force_fields.py): constant,
+    wind, point, drag and vortex fields (one left inactive) against the FP64 oracle."""
+    ff = gs.force_fields
+    scene = gs.Scene(
+        sim_options=gs.options.SimOptions(dt=2e-4, substeps=1),
+        mpm_options=gs.options.MPMOptions(lower_bound=(0, 0, 0), upper_bound=(1, 1, 1), grid_density=64,
+                                          particle_size=1 / 128),
+    )
+    mat = gs.materials.MPM.Elastic(E=3e5, nu=0.2, rho=1000, sampler="regular")
+    cube = scene.add_entity(material=mat, morph=gs.morphs.Box(pos=(0.5, 0.5, 0.4), size=(0.12,) * 3))
+    fields = [
+        ff.Constant(direction=(1.0, 0.5, 0.0), strength=3.0),
+        ff.Wind(direction=(0.0, 1.0, 0.0), strength=4.0, radius=0.04, center=(0.5, 0.5, 0.4)),
+        ff.Point(strength=-2.0, position=(0.45, 0.55, 0.35), falloff_pow=1.0, flow=0.5),
+        ff.Drag(linear=0.8, quadratic=0.3),
+        ff.Vortex(center=(0.52, 0.48, 0.0), strength_perpendicular=6.0, strength_radial=1.0, falloff_min=0.02,
+                  falloff_max=0.3, damping=0.2),
+        ff.Constant(direction=(0.0, 0.0, 1.0), strength=50.0),  # stays inactive
+    ]
+    for f in fields:
+        scene.add_force_field(f)
+    scene.build()
+    for f in fields[:5]:
+        f.activate()
+    solver = scene.sim.mpm_solver
+    st0 = solver.get_state()
+    n_sub = 40
+    for _ in range(n_sub):
+        scene.step()
+    st1 = solver.get_state()
+    oracle.set_force_fields([f.to_c() for f in fields])
+    try:
+        ref, _, _ = oracle.run(oracle_scene_for(oracle, solver), [oracle.from_c_material(mat.to_c(0))],
+                               oracle_state(st0), n_sub)
+    finally:
+        oracle.set_force_fields([])
+    ref_plain, _, _ = oracle.run(oracle_scene_for(oracle, solver), [oracle.from_c_material(mat.to_c(0))],
+                                 oracle_state(st0), n_sub)
+    assert np.abs(ref["vel"] - ref_plain["vel"]).max() > 1e-2  # the fields act
+    assert np.abs(st1.pos[0].double().cpu().numpy() - ref["pos"]).max() <= POS_TOL
+    assert np.abs(st1.vel[0].double().cpu().numpy() - ref["vel"]).max() <= 1e-3
+    fields[0].deactivate()
+    for f in fields[1:5]:
+        f.deactivate()
+    st2 = solver.get_state()
+    scene.step()
+    ref2, _, _ = oracle.run(oracle_scene_for(oracle, solver), [oracle.from_c_material(mat.to_c(0))], oracle_state(st2), 1)
+    assert np.abs(solver.get_state().vel[0].double().cpu().numpy() - ref2["vel"]).max() <= 1e-4
