@@ -45,35 +45,47 @@ class DifferentiableMPM:
         self.g_grid_pm = torch.zeros((self.nodes, 4), device=dev)
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
 
+    def grid_budget_bytes(self) -> int:
+        """Device memory the backward may spend on one segment's grids (a quarter of what is free)."""
+        free, _ = torch.cuda.mem_get_info()
+        return free // 4
+
     @staticmethod
     def _s():
         return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
-    def forward_substep(self, st, mu, lam):
-        """(x, v, C, F) -> next state (new tensors)."""
+    def forward_substep(self, st, mu, lam, grids=None):
+        """(x, v, C, F) -> next state (new tensors).  `grids` = (grid_pm, grid_v) buffers that keep
+        this substep's grid (default: the shared scratch grid)."""
         x, v, C, F = st
         n = x.shape[0]
+        gpm, gv = grids if grids is not None else (self.grid_pm, self.grid_v)
         out = (torch.empty_like(x), torch.empty_like(v), torch.empty_like(C), torch.empty_like(F))
         r = self.lib.mpm_diff_forward(ctypes.byref(self.cfg), self.rho, self.neo, n, x.data_ptr(), v.data_ptr(),
                                       C.data_ptr(), F.data_ptr(), mu.data_ptr(), lam.data_ptr(), out[0].data_ptr(),
                                       out[1].data_ptr(), out[2].data_ptr(), out[3].data_ptr(),
-                                      self.grid_pm.data_ptr(), self.grid_v.data_ptr(), self.status.data_ptr(),
-                                      self._s())
+                                      gpm.data_ptr(), gv.data_ptr(), self.status.data_ptr(), self._s())
         _lib.check(r, None, "mpm_diff_forward")
         return out
 
-    def backward_substep(self, st, mu, lam, g_out, gmu, glam):
-        """Adjoint of forward_substep at state `st` given dL/d(next state); returns dL/d(state)."""
+    def new_grids(self):
+        return (torch.empty((self.nodes, 4), device="cuda"), torch.empty((self.nodes, 4), device="cuda"))
+
+    def backward_substep(self, st, mu, lam, g_out, gmu, glam, grids=None):
+        """Adjoint of forward_substep at state `st` given dL/d(next state); returns dL/d(state).
+        `grids` holds this substep's grid from a kept forward; without it the forward is re-run."""
         x, v, C, F = st
         n = x.shape[0]
-        self.forward_substep(st, mu, lam)  # rebuild this substep's grid
+        if grids is None:
+            self.forward_substep(st, mu, lam)  # rebuild this substep's grid
+            grids = (self.grid_pm, self.grid_v)
         gx1, gv1, gC1, gF1 = g_out
         gin = (torch.empty_like(x), torch.empty_like(v), torch.empty_like(C), torch.empty_like(F))
         r = self.lib.mpm_diff_backward(ctypes.byref(self.cfg), self.rho, self.neo, n, x.data_ptr(), v.data_ptr(),
                                        C.data_ptr(), F.data_ptr(), mu.data_ptr(), lam.data_ptr(), gx1.data_ptr(),
                                        gv1.data_ptr(), gC1.data_ptr(), gF1.data_ptr(), gin[0].data_ptr(),
                                        gin[1].data_ptr(), gin[2].data_ptr(), gin[3].data_ptr(), gmu.data_ptr(),
-                                       glam.data_ptr(), self.grid_pm.data_ptr(), self.grid_v.data_ptr(),
+                                       glam.data_ptr(), grids[0].data_ptr(), grids[1].data_ptr(),
                                        self.g_grid_v.data_ptr(), self.g_grid_pm.data_ptr(), self.status.data_ptr(),
                                        self._s())
         _lib.check(r, None, "mpm_diff_backward")
@@ -125,13 +137,23 @@ class _Rollout(torch.autograd.Function):
         gmu = torch.zeros_like(mu)
         glam = torch.zeros_like(lam)
         starts = sorted(ctx.ckpts)
+        seg_max = max((starts[i + 1] if i + 1 < len(starts) else n_sub) - starts[i] for i in range(len(starts)))
+        keep = sim.nodes * 32 * seg_max <= sim.grid_budget_bytes()  # keep every substep's grid of a segment
         for seg_i in range(len(starts) - 1, -1, -1):
             s0 = starts[seg_i]
             s1 = starts[seg_i + 1] if seg_i + 1 < len(starts) else n_sub
             states = [ctx.ckpts[s0]]
-            for _ in range(s0, s1 - 1):  # re-simulate the segment (checkpoint-and-recompute)
-                states.append(sim.forward_substep(states[-1], mu, lam))
-            for st in reversed(states):
-                g = sim.backward_substep(st, mu, lam, g, gmu, glam)
+            grids = []
+            for k in range(s0, s1):  # re-simulate the segment (checkpoint-and-recompute)
+                if keep:
+                    grids.append(sim.new_grids())
+                    nxt = sim.forward_substep(states[-1], mu, lam, grids[-1])
+                    if k < s1 - 1:
+                        states.append(nxt)
+                elif k < s1 - 1:
+                    states.append(sim.forward_substep(states[-1], mu, lam))
+            for i in range(len(states) - 1, -1, -1):
+                g = sim.backward_substep(states[i], mu, lam, g, gmu, glam, grids[i] if keep else None)
+            del grids
         sim.check()
         return None, None, g[0], g[1], gmu, glam

@@ -81,8 +81,8 @@ class MPMEntity:
             raise GenesisException("link_idx must be an integer.")
         lp, lq = self._solver.get_link_pose(link_idx)
         m = self._mask(particles_mask)
-        pos = torch.as_tensor(np.ascontiguousarray(lp), device="cuda")
-        quat = torch.as_tensor(np.ascontiguousarray(lq), device="cuda")
+        pos = torch.as_tensor(np.array(lp, dtype=np.float32), device="cuda")
+        quat = torch.as_tensor(np.array(lq, dtype=np.float32), device="cuda")
         lib = self._solver._lib
         _lib.check(lib.mpm_set_particle_constraints(self._solver._ctx, 0, self._solver._B, self._particle_start,
                                                     self._n_particles, m.data_ptr(), float(stiffness), link_idx,

@@ -270,6 +270,77 @@ class MPMSolver:
         _lib.check(self._lib.mpm_get_grid(self._ctx, scene, _lib.ptr(out), _stream_handle()), self._ctx, "mpm_get_grid")
         return out
 
+    # ------------------------------------------------------------------ Solver protocol members
+    def init_ckpt(self):
+        """mpm_solver.py:165-166."""
+        self._ckpt = dict()
+
+    def save_ckpt(self, ckpt_name):
+        """mpm_solver.py:676-701: keep a copy of the current state under `ckpt_name`.  The
+        reference keeps it only in differentiable mode (its frames hold the state otherwise);
+        here it is always kept, so load_ckpt restores it."""
+        if not hasattr(self, "_ckpt"):
+            self.init_ckpt()
+        st = self.get_state()
+        if st is not None:
+            self._ckpt[ckpt_name] = st
+
+    def load_ckpt(self, ckpt_name):
+        """mpm_solver.py:703-721."""
+        ck = getattr(self, "_ckpt", {}).get(ckpt_name)
+        if ck is not None:
+            self.set_state(0, ck)
+
+    def _is_state_valid(self, f=0) -> bool:
+        """mpm_solver.py:484-489 (one host sync on the device status word)."""
+        st = ctypes.c_uint32()
+        _lib.check(self._lib.mpm_status_word(self._ctx, ctypes.byref(st), None, 0, _stream_handle()), self._ctx,
+                   "mpm_status_word")
+        return not (st.value & _lib.STATUS_NAN)
+
+    # The reference's per-kernel launch methods map onto the fused split phases: p2g runs
+    # compute_F_tmp + svd + material update + scatter in one kernel, g2p the gather and re-sort.
+    def p2g(self, f=0):
+        self.substep_pre_coupling(f)
+
+    def g2p(self, f=0):
+        self.substep_post_coupling(f)
+
+    def setup_boundary(self):
+        pad = 3 * self._dx
+        self.boundary_padding = pad
+        self.boundary = CubeBoundary(np.asarray(self._lower_bound) + pad, np.asarray(self._upper_bound) - pad)
+
+    @property
+    def stencil_range(self):
+        return [(i, j, k) for i in range(3) for j in range(3) for k in range(3)]
+
+    @property
+    def is_built(self):
+        return self._ctx is not None
+
+    @property
+    def n_vverts(self):
+        return sum(e.n_vverts for e in self._entities)
+
+    @property
+    def n_vfaces(self):
+        return 0  # visual faces come from meshes, which this path does not load
+
+    @property
+    def enable_particle_constraints(self):
+        return getattr(self, "_constraints_used", False)
+
+    # Differentiable mode: gradients come from genesis_gb300.diff.DifferentiableMPM (hand-written
+    # adjoint kernels); the autodiff entry points of the reference are not available here.
+    def _no_grad(self, *args, **kwargs):
+        raise GenesisException(
+            "Differentiable mode runs through genesis_gb300.diff.DifferentiableMPM (hand-written adjoints)."
+        )
+
+    substep_pre_coupling_grad = substep_post_coupling_grad = process_input_grad = _no_grad
+    add_grad_from_state = collect_output_grads = reset_grad = reset_grad_till_frame = _no_grad
+
     # ------------------------------------------------------------------ force fields
     def _add_force_field(self, ff) -> None:
         if not hasattr(self, "_ffs"):
