@@ -165,6 +165,10 @@ _SIGNATURES = {
     "mpm_remove_particle_constraints": (c_int32, [_P, c_int64, c_int64, c_int64, c_int64, _P, _P]),
     "mpm_set_link_poses": (c_int32, [_P, c_int32, _P]),
     "mpm_set_colliders": (c_int32, [_P, c_int32, _P]),
+    "mpm_diff_forward_seq": (c_int32, [_P, c_double, c_int32, c_int64, c_int32, _P, _P, _P, _P, c_int32, _P, _P,
+                                       _P, _P, c_int32, _P, _P]),
+    "mpm_diff_backward_seq": (c_int32, [_P, c_double, c_int32, c_int64, c_int32, _P, _P, _P, _P, _P, _P, _P,
+                                        _P, _P, _P, _P, _P, _P, _P, _P]),
     "mpm_set_force_fields": (c_int32, [_P, c_int32, _P]),
     "mpm_get_collider_forces": (c_int32, [_P, _P, c_int32, _P]),
     "mpm_version": (c_int32, []),

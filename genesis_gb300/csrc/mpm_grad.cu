@@ -551,4 +551,61 @@ int mpm_diff_backward(const mpm_scene_config* scene, double rho, int32_t neohook
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_ERR_CUDA;
 }
 
+// n_sub forward substeps in one call (no host round trip per substep).  State k (k = 0..n_sub)
+// lives in slot k % ring of x_seq [ring, n, 3], v_seq [ring, n, 3], C_seq [ring, n, 9] and
+// F_seq [ring, n, 9]; slot 0 holds the input.  ring = 2 ping-pongs; ring > n_sub keeps every
+// state.  With grids_per_substep, substep k leaves its grid in grid_pm + k * nodes and
+// grid_v + k * nodes (n_sub grids each); otherwise every substep uses the one grid given.
+int mpm_diff_forward_seq(const mpm_scene_config* scene, double rho, int32_t neohookean, int64_t n, int32_t n_sub,
+                         float* x_seq, float* v_seq, float* C_seq, float* F_seq, int32_t ring, const float* mu,
+                         const float* lam, void* grid_pm, void* grid_v, int32_t grids_per_substep, uint32_t* status,
+                         void* stream) {
+  if (!scene || n < 0 || n_sub < 0 || ring < 2 || !x_seq || !v_seq || !C_seq || !F_seq) return MPM_ERR_BAD_ARG;
+  SceneDev S;
+  std::string err;
+  if (derive_scene(*scene, S, err)) return MPM_ERR_BAD_ARG;
+  const int64_t nodes = (int64_t)S.res[0] * S.res[1] * S.res[2];
+  for (int32_t k = 0; k < n_sub; ++k) {
+    const int64_t a = k % ring, b = (k + 1) % ring;
+    const int64_t go = grids_per_substep ? (int64_t)k * nodes : 0;
+    const int r = mpm_diff_forward(scene, rho, neohookean, n, x_seq + a * n * 3, v_seq + a * n * 3, C_seq + a * n * 9,
+                                   F_seq + a * n * 9, mu, lam, x_seq + b * n * 3, v_seq + b * n * 3, C_seq + b * n * 9,
+                                   F_seq + b * n * 9, (float4*)grid_pm + go, (float4*)grid_v + go, status, stream);
+    if (r) return r;
+  }
+  return MPM_OK;
+}
+
+// Adjoint of n_sub substeps whose states 0..n_sub-1 and grids were kept by mpm_diff_forward_seq
+// (ring > n_sub - 1, grids_per_substep).  g_seq [2, 24 n] holds two packed gradient buffers
+// (dx [n,3], dv [n,3], dC [n,9], dF [n,9]); buffer 0 holds dL/d(state n_sub) on entry and
+// dL/d(state 0) on return.  dL/d(mu, lam) accumulate into gmu, glam.
+int mpm_diff_backward_seq(const mpm_scene_config* scene, double rho, int32_t neohookean, int64_t n, int32_t n_sub,
+                          const float* x_seq, const float* v_seq, const float* C_seq, const float* F_seq,
+                          const float* mu, const float* lam, float* g_seq, float* gmu, float* glam, void* grid_pm,
+                          void* grid_v, void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream) {
+  if (!scene || n < 0 || n_sub < 0 || !g_seq) return MPM_ERR_BAD_ARG;
+  SceneDev S;
+  std::string err;
+  if (derive_scene(*scene, S, err)) return MPM_ERR_BAD_ARG;
+  const int64_t nodes = (int64_t)S.res[0] * S.res[1] * S.res[2];
+  const int64_t gs = 24 * n;
+  int cur = 0;
+  for (int32_t k = n_sub - 1; k >= 0; --k) {
+    float* gi = g_seq + cur * gs;
+    float* go = g_seq + (1 - cur) * gs;
+    const int r = mpm_diff_backward(scene, rho, neohookean, n, x_seq + (int64_t)k * n * 3, v_seq + (int64_t)k * n * 3,
+                                    C_seq + (int64_t)k * n * 9, F_seq + (int64_t)k * n * 9, mu, lam, gi, gi + 3 * n,
+                                    gi + 6 * n, gi + 15 * n, go, go + 3 * n, go + 6 * n, go + 15 * n, gmu, glam,
+                                    (float4*)grid_pm + (int64_t)k * nodes, (float4*)grid_v + (int64_t)k * nodes,
+                                    g_grid_v, g_grid_pm, status, stream);
+    if (r) return r;
+    cur = 1 - cur;
+  }
+  if (cur == 1 && cudaMemcpyAsync(g_seq, g_seq + gs, sizeof(float) * gs, cudaMemcpyDeviceToDevice,
+                                  (cudaStream_t)stream) != cudaSuccess)
+    return MPM_ERR_CUDA;
+  return MPM_OK;
+}
+
 }  // extern "C"

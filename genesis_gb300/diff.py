@@ -45,6 +45,47 @@ class DifferentiableMPM:
         self.g_grid_pm = torch.zeros((self.nodes, 4), device=dev)
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
 
+    # ---- segment calls: n substeps per library call (no host round trip per substep)
+    def forward_segment(self, st, mu, lam, n_sub, keep=False):
+        """Run n_sub substeps from state st.  keep=False: returns the final state.  keep=True: returns
+        (states [n_sub+1] as (x, v, C, F) stacked tensors, grids (pm, v) [n_sub, nodes, 4])."""
+        x, v, C, F = st
+        n = x.shape[0]
+        ring = n_sub + 1 if keep else 2
+        xs = torch.empty((ring, n, 3), device="cuda")
+        vs = torch.empty((ring, n, 3), device="cuda")
+        Cs = torch.empty((ring, n, 3, 3), device="cuda")
+        Fs = torch.empty((ring, n, 3, 3), device="cuda")
+        xs[0], vs[0], Cs[0], Fs[0] = x, v, C, F
+        if keep:
+            gpm = torch.empty((max(1, n_sub), self.nodes, 4), device="cuda")
+            gv = torch.empty((max(1, n_sub), self.nodes, 4), device="cuda")
+        else:
+            gpm, gv = self.grid_pm, self.grid_v
+        r = self.lib.mpm_diff_forward_seq(ctypes.byref(self.cfg), self.rho, self.neo, n, int(n_sub), xs.data_ptr(),
+                                          vs.data_ptr(), Cs.data_ptr(), Fs.data_ptr(), ring, mu.data_ptr(),
+                                          lam.data_ptr(), gpm.data_ptr(), gv.data_ptr(), int(keep),
+                                          self.status.data_ptr(), self._s())
+        _lib.check(r, None, "mpm_diff_forward_seq")
+        if keep:
+            return (xs, vs, Cs, Fs), (gpm, gv)
+        last = n_sub % 2
+        return xs[last].clone(), vs[last].clone(), Cs[last].clone(), Fs[last].clone()
+
+    def backward_segment(self, states, grids, mu, lam, g_packed, gmu, glam, n_sub):
+        """Adjoint of a kept segment; g_packed [2, 24 n]: row 0 in = dL/d(last state), out = dL/d(first)."""
+        xs, vs, Cs, Fs = states
+        n = xs.shape[1]
+        r = self.lib.mpm_diff_backward_seq(ctypes.byref(self.cfg), self.rho, self.neo, n, int(n_sub), xs.data_ptr(),
+                                           vs.data_ptr(), Cs.data_ptr(), Fs.data_ptr(), mu.data_ptr(), lam.data_ptr(),
+                                           g_packed.data_ptr(), gmu.data_ptr(), glam.data_ptr(), grids[0].data_ptr(),
+                                           grids[1].data_ptr(), self.g_grid_v.data_ptr(), self.g_grid_pm.data_ptr(),
+                                           self.status.data_ptr(), self._s())
+        _lib.check(r, None, "mpm_diff_backward_seq")
+
+    def segment_bytes(self, n, n_sub) -> int:
+        return (n_sub + 1) * 24 * 4 * n + 2 * n_sub * self.nodes * 16
+
     def grid_budget_bytes(self) -> int:
         """Device memory the backward may spend on one segment's grids (a quarter of what is free)."""
         free, _ = torch.cuda.mem_get_info()
@@ -118,10 +159,12 @@ class _Rollout(torch.autograd.Function):
         mu_d, lam_d = mu.detach().float().contiguous(), lam.detach().float().contiguous()
         st = (x, v, C, F)
         ckpts = {}
-        for s in range(n_substeps):
-            if s % sim.ckpt_every == 0:
-                ckpts[s] = tuple(t.clone() for t in st)
-            st = sim.forward_substep(st, mu_d, lam_d)
+        s = 0
+        while s < n_substeps:
+            seg = min(sim.ckpt_every, n_substeps - s)
+            ckpts[s] = tuple(t.clone() for t in st)
+            st = sim.forward_segment(st, mu_d, lam_d, seg)
+            s += seg
         sim.check()
         ctx.sim, ctx.n_substeps, ctx.ckpts = sim, n_substeps, ckpts
         ctx.save_for_backward(mu_d, lam_d)
@@ -138,6 +181,18 @@ class _Rollout(torch.autograd.Function):
         glam = torch.zeros_like(lam)
         starts = sorted(ctx.ckpts)
         seg_max = max((starts[i + 1] if i + 1 < len(starts) else n_sub) - starts[i] for i in range(len(starts)))
+        if sim.segment_bytes(n, seg_max) <= sim.grid_budget_bytes():
+            # whole segments per library call: re-simulate keeping states and grids, then walk back
+            gp = torch.zeros((2, 24 * n), device=g_x.device)
+            gp[0, : 3 * n] = g[0].reshape(-1)
+            for seg_i in range(len(starts) - 1, -1, -1):
+                s0 = starts[seg_i]
+                s1 = starts[seg_i + 1] if seg_i + 1 < len(starts) else n_sub
+                states, grids = sim.forward_segment(ctx.ckpts[s0], mu, lam, s1 - s0, keep=True)
+                sim.backward_segment(states, grids, mu, lam, gp, gmu, glam, s1 - s0)
+                del states, grids
+            sim.check()
+            return None, None, gp[0, : 3 * n].view(n, 3).clone(), gp[0, 3 * n: 6 * n].view(n, 3).clone(), gmu, glam
         keep = sim.nodes * 32 * seg_max <= sim.grid_budget_bytes()  # keep every substep's grid of a segment
         for seg_i in range(len(starts) - 1, -1, -1):
             s0 = starts[seg_i]

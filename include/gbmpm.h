@@ -377,6 +377,22 @@ int mpm_diff_backward(const mpm_scene_config* scene, double rho, int32_t neohook
                       float* gmu, float* glam, void* grid_pm, void* grid_v, void* g_grid_v,
                       void* g_grid_pm, uint32_t* status, void* stream);
 
+/* n_sub forward substeps in one call: state k in slot k % ring of x_seq [ring,n,3],
+ * v_seq [ring,n,3], C_seq [ring,n,9], F_seq [ring,n,9] (slot 0 = input); with grids_per_substep
+ * substep k leaves its grid at grid_pm/grid_v + k * res^3 float4, else one grid is reused. */
+int mpm_diff_forward_seq(const mpm_scene_config* scene, double rho, int32_t neohookean, int64_t n, int32_t n_sub,
+                         float* x_seq, float* v_seq, float* C_seq, float* F_seq, int32_t ring, const float* mu,
+                         const float* lam, void* grid_pm, void* grid_v, int32_t grids_per_substep, uint32_t* status,
+                         void* stream);
+
+/* Adjoint of n_sub substeps kept by mpm_diff_forward_seq (all states and grids): g_seq holds two
+ * packed gradient buffers of 24 n floats (dx, dv, dC, dF); buffer 0 carries dL/d(state n_sub) in
+ * and dL/d(state 0) out; dL/d(mu, lam) accumulate into gmu, glam. */
+int mpm_diff_backward_seq(const mpm_scene_config* scene, double rho, int32_t neohookean, int64_t n, int32_t n_sub,
+                          const float* x_seq, const float* v_seq, const float* C_seq, const float* F_seq,
+                          const float* mu, const float* lam, float* g_seq, float* gmu, float* glam, void* grid_pm,
+                          void* grid_v, void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream);
+
 /* ABI version of this header (1). */
 int mpm_version(void);
 
