@@ -241,7 +241,12 @@ def run_ours(args, rank, world):
     # launch-shape autotuning (P2G threads x particles per thread), then warm-up (captures the graph)
     from genesis_gb300.autotune import autotune
 
-    tuning, tune_ms = autotune(solver.ctx, substeps=4, repeats=1, use_cache=False)
+    if args.tuning:  # fixed launch shapes (profiling captures, where timings under the profiler mislead)
+        t, pp, gt = (int(v) for v in args.tuning.split(","))
+        _lib.check(lib.mpm_set_tuning(solver.ctx, t, pp, 1, gt), solver.ctx, "mpm_set_tuning")
+        tuning, tune_ms = (t, pp, gt), {}
+    else:
+        tuning, tune_ms = autotune(solver.ctx, substeps=4, repeats=1, use_cache=False)
     for _ in range(args.warmup):
         scene.step()
     torch.cuda.synchronize()
@@ -576,6 +581,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-forms", action="store_true", help="skip the batched/served form measurements")
+    ap.add_argument("--tuning", default="", help="fixed P2G threads,particles per thread,G2P threads (no autotune)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
