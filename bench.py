@@ -324,32 +324,56 @@ def run_ours(args, rank, world):
                     "frac": sub_alg / (substep_ms / 1e3) / 1e9 / peak},
     }
 
-    # --- e2e: through the public API with host buffers: H2D state from pinned memory, 10 substeps,
-    # D2H of positions, every step
+    # --- e2e: through the public C API with host buffers: every step uploads the full particle
+    # state from pinned host memory (mpm_set_state), runs 10 substeps (mpm_substeps) and reads the
+    # positions back (mpm_get_state); the copies run on their own streams with double-buffered
+    # device staging, so step k's uploads overlap step k-1's substeps and its read-back overlaps
+    # step k+1's
     st = solver.get_state()
-    host = {k: getattr(st, k).cpu().pin_memory() for k in ("pos", "vel", "C", "F", "Jp", "active")}
+    keys = ("pos", "vel", "C", "F", "Jp", "active")
+    host = {k: (getattr(st, k).to(torch.uint8) if k == "active" else getattr(st, k)).cpu().pin_memory() for k in keys}
     h2d = sum(t.numel() * t.element_size() for t in host.values())
-    out_host = torch.empty_like(host["pos"]).pin_memory()
-    d2h = out_host.numel() * out_host.element_size()
+    stage = [{k: torch.empty_like(v, device="cuda") for k, v in host.items()} for _ in range(2)]
+    dev_out = [torch.empty_like(host["pos"], device="cuda") for _ in range(2)]
+    out_host = [torch.empty_like(host["pos"]).pin_memory() for _ in range(2)]
+    d2h = out_host[0].numel() * out_host[0].element_size()
+    up, down = torch.cuda.Stream(), torch.cuda.Stream()
+    staged = [torch.cuda.Event() for _ in range(2)]
+    consumed = [torch.cuda.Event() for _ in range(2)]
+    produced = [torch.cuda.Event() for _ in range(2)]
+    read = [torch.cuda.Event() for _ in range(2)]
+    h = ctypes.c_void_p(stream.cuda_stream)
+    B = solver._B
 
-    class _S:
-        pass
+    def e2e_step(k):
+        b = k % 2
+        with torch.cuda.stream(up):  # upload step k's state once step k-2 has consumed the buffer
+            up.wait_event(consumed[b])
+            for key in keys:
+                stage[b][key].copy_(host[key], non_blocking=True)
+            staged[b].record(up)
+        stream.wait_event(staged[b])
+        stream.wait_event(read[b])  # step k-2's positions have left dev_out[b]
+        sb = stage[b]
+        _lib.check(lib.mpm_set_state(solver.ctx, 0, B, sb["pos"].data_ptr(), sb["vel"].data_ptr(), sb["C"].data_ptr(),
+                                     sb["F"].data_ptr(), sb["Jp"].data_ptr(), sb["active"].data_ptr(), h), solver.ctx,
+                   "mpm_set_state")
+        consumed[b].record(stream)
+        _lib.check(lib.mpm_substeps(solver.ctx, SUBSTEPS_PER_STEP, h), solver.ctx, "mpm_substeps")
+        _lib.check(lib.mpm_get_state(solver.ctx, 0, B, dev_out[b].data_ptr(), None, None, None, None, None, h),
+                   solver.ctx, "mpm_get_state")
+        produced[b].record(stream)
+        with torch.cuda.stream(down):
+            down.wait_event(produced[b])
+            out_host[b].copy_(dev_out[b], non_blocking=True)
+            read[b].record(down)
 
-    def e2e_step():
-        s = _S()
-        for k, v in host.items():
-            setattr(s, k, v.to("cuda", non_blocking=True))
-        solver.set_state(0, s)
-        solver.substeps(SUBSTEPS_PER_STEP)
-        dst = ents[0].solver.get_state()
-        out_host.copy_(dst.pos, non_blocking=True)
-
-    for _ in range(2):
-        e2e_step()
+    for k in range(2):
+        e2e_step(k)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_step()
+    for k in range(args.steps):
+        e2e_step(k)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e = {"value": n * SUBSTEPS_PER_STEP * args.steps * world / e2e_s, "unit": "particle-substeps/s",
