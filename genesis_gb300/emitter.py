@@ -133,7 +133,7 @@ class Emitter:
         positions = positions @ R.T + np.asarray(pos, dtype=np.float64)
         if not self._solver.boundary.is_inside(positions):
             raise GenesisException("Emitted particles are outside the boundary.")
-        self._activate(positions, np.broadcast_to(speed * direction, positions.shape))
+        self._activate(positions, np.tile(speed * direction, (len(positions), 1)))
 
     def emit_omni(self, source_radius=0.1, pos=(0.5, 0.5, 1.0), speed=1.0, particle_size=None):
         import genesis_gb300 as gs
