@@ -57,11 +57,13 @@ def jitter(pos, spacing, rng):
     return pos + rng.uniform(-0.25 * spacing, 0.25 * spacing, size=pos.shape)
 
 
-def build_c2_scene(gs, n_envs=0):
-    """The ~1M-particle three-material scene through the Genesis-style API."""
+def build_c2_scene(gs, n_envs=0, spacing=None):
+    """The ~1M-particle three-material scene through the Genesis-style API (or the same boxes at
+    another particle spacing)."""
     import torch
 
-    liquid, sand, sphere, spacing = workload_boxes()
+    liquid, sand, sphere, sp = workload_boxes()
+    spacing = sp if spacing is None else spacing
     scene = gs.Scene(
         sim_options=gs.options.SimOptions(dt=SUBSTEP_DT * SUBSTEPS_PER_STEP, substeps=SUBSTEPS_PER_STEP),
         mpm_options=gs.options.MPMOptions(lower_bound=(0, 0, 0), upper_bound=(1, 1, 1), grid_density=GRID_DENSITY,
@@ -468,13 +470,31 @@ def run_c1(substeps=100, repeats=5):
             "unit": "particle-substeps/s"}
 
 
+def run_dense(steps=20):
+    """The same three-material scene at 4 particles per cell per axis (spacing dx / 4, ~5.3M
+    particles, the density the config names literally), graph path, 10 substeps per step."""
+    import genesis_gb300 as gs
+
+    scene, ents, spacing = build_c2_scene(gs, spacing=1.0 / (4 * GRID_DENSITY))
+    solver = scene.sim.mpm_solver
+    n = solver.n_particles
+    solver.substeps(2 * SUBSTEPS_PER_STEP)
+    t = _timed(lambda: [solver.substeps(SUBSTEPS_PER_STEP) for _ in range(steps)])
+    solver.check_state()
+    out = {"workload": f"three-material scene at 4 particles per cell per axis ({n} particles), 129^3, "
+                       f"{steps} steps x {SUBSTEPS_PER_STEP} substeps", "n_particles": n,
+           "value": n * SUBSTEPS_PER_STEP * steps / t, "unit": "particle-substeps/s"}
+    solver.destroy()
+    return out
+
+
 def run_forms(batched_substeps=200, n_requests=48):
     """Batched (256 uneven scenes, one context) and served (continuous batching) forms, each
     against the plain form run scene by scene (one context per scene) on the same workload."""
     from genesis_gb300.batched import BatchedMPM, batched_workload
     from genesis_gb300.serve import MPMServer, serving_workload
 
-    out = {"plain_small": run_c1()}
+    out = {"plain_small": run_c1(), "plain_dense": run_dense()}
     specs = batched_workload(n_scenes=256, seed=1234)
     b = BatchedMPM(specs, tune=True)
     b.step(2)

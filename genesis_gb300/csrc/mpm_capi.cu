@@ -1034,6 +1034,58 @@ int mpm_set_link_poses(mpm_ctx* ctx, int32_t n_links, const float* poses_host) {
   return MPM_OK;
 }
 
+int mpm_sample_regular(int32_t shape, const double* pos, const double* size, double p_size, float* out,
+                       int64_t capacity, int64_t* n_out, void* stream) {
+  if (!pos || !size || !n_out || !(p_size > 0) || shape < 0 || shape > 2) return MPM_ERR_BAD_ARG;
+  LatticeDev L;
+  std::memset(&L, 0, sizeof(L));
+  L.shape = shape;
+  double ext[3];
+  if (shape == 0) ext[0] = size[0], ext[1] = size[1], ext[2] = size[2];
+  else if (shape == 1) ext[0] = ext[1] = ext[2] = 2 * size[0];
+  else ext[0] = ext[1] = 2 * size[0], ext[2] = size[1];
+  int64_t total_rows = 1;
+  for (int d = 0; d < 3; ++d) {
+    const double n = std::nearbyint(ext[d] / p_size);  // Python round(): half to even
+    L.n[d] = n < 1 ? 1 : (int64_t)n;
+    const double lower = pos[d] - ext[d] / 2, upper = pos[d] + ext[d] / 2;
+    L.lo[d] = lower + 0.5 * p_size;
+    L.hi[d] = upper - 0.5 * p_size;
+    L.step[d] = L.n[d] > 1 ? (L.hi[d] - L.lo[d]) / (double)(L.n[d] - 1) : 0.0;
+    L.center[d] = pos[d];
+  }
+  L.radius = shape == 0 ? 0.0 : size[0];
+  total_rows = L.n[0] * L.n[1];
+  if (L.n[0] * L.n[1] * L.n[2] > ((int64_t)1 << 40)) return MPM_ERR_BAD_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  int64_t* d_rows = nullptr;
+  if (cudaMalloc((void**)&d_rows, sizeof(int64_t) * (size_t)total_rows) != cudaSuccess) {
+    cudaGetLastError();
+    return MPM_ERR_OOM;
+  }
+  const int blocks = (int)std::min<int64_t>((total_rows + 255) / 256, 4096);
+  k_lattice_rows<<<blocks, 256, 0, s>>>(L, d_rows);
+  std::vector<int64_t> rows((size_t)total_rows);
+  cudaError_t e = cudaMemcpyAsync(rows.data(), d_rows, sizeof(int64_t) * (size_t)total_rows, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  int64_t total = 0;
+  for (auto& c : rows) {  // exclusive scan
+    const int64_t v = c;
+    c = total;
+    total += v;
+  }
+  *n_out = total;
+  if (e == cudaSuccess && out && capacity >= total && total > 0) {
+    e = cudaMemcpyAsync(d_rows, rows.data(), sizeof(int64_t) * (size_t)total_rows, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) k_lattice_fill<<<blocks, 256, 0, s>>>(L, d_rows, out);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  cudaFree(d_rows);
+  if (e != cudaSuccess) return MPM_ERR_CUDA;
+  return (out && capacity < total) ? MPM_ERR_BAD_ARG : MPM_OK;
+}
+
 int mpm_render_fields(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end, float* pos_out, float* vel_out,
                       uint8_t* active_out, int64_t n_vverts, int32_t n_supports, const int32_t* support_idx,
                       const float* support_w, float* vvert_pos_out, uint8_t* vvert_active_out, void* stream) {

@@ -1277,6 +1277,52 @@ __global__ void k_constraints(KParams P, ConstraintDev* cons, const float* links
   }
 }
 
+// ------------------------------------------------------------------ lattice sampling
+namespace {
+// np.linspace(lo, hi, n)[i]: i * step + lo, the last point exactly hi.
+__device__ __forceinline__ double lattice_coord(const LatticeDev& L, int d, int64_t i) {
+  return (L.n[d] > 1 && i == L.n[d] - 1) ? L.hi[d] : (double)i * L.step[d] + L.lo[d];
+}
+
+// The reference's rejection tests (particle.py:249-250, 273-274): numpy norm in float64.
+__device__ __forceinline__ bool lattice_keep(const LatticeDev& L, double x, double y, double z) {
+  if (L.shape == 0) return true;
+  const double dx = x - L.center[0], dy = y - L.center[1];
+  if (L.shape == 2) return sqrt(dx * dx + dy * dy) <= L.radius;
+  const double dz = z - L.center[2];
+  return sqrt(dx * dx + dy * dy + dz * dz) <= L.radius;
+}
+}  // namespace
+
+// Kept points of each (ix, iy) row of the lattice.
+__global__ void k_lattice_rows(LatticeDev L, int64_t* row_count) {
+  const int64_t rows = L.n[0] * L.n[1];
+  for (int64_t r = grid_stride_begin(); r < rows; r += grid_stride_step()) {
+    const double x = lattice_coord(L, 0, r / L.n[1]), y = lattice_coord(L, 1, r % L.n[1]);
+    int64_t c = 0;
+    for (int64_t iz = 0; iz < L.n[2]; ++iz) c += lattice_keep(L, x, y, lattice_coord(L, 2, iz)) ? 1 : 0;
+    row_count[r] = c;
+  }
+}
+
+// Kept points in row-major (ix, iy, iz) order, as np.meshgrid(..., indexing='ij').reshape(-1, 3)
+// followed by the boolean mask; row_offset is the exclusive scan of k_lattice_rows.
+__global__ void k_lattice_fill(LatticeDev L, const int64_t* row_offset, float* out) {
+  const int64_t rows = L.n[0] * L.n[1];
+  for (int64_t r = grid_stride_begin(); r < rows; r += grid_stride_step()) {
+    const double x = lattice_coord(L, 0, r / L.n[1]), y = lattice_coord(L, 1, r % L.n[1]);
+    int64_t o = row_offset[r];
+    for (int64_t iz = 0; iz < L.n[2]; ++iz) {
+      const double z = lattice_coord(L, 2, iz);
+      if (!lattice_keep(L, x, y, z)) continue;
+      out[o * 3 + 0] = (float)x;
+      out[o * 3 + 1] = (float)y;
+      out[o * 3 + 2] = (float)z;
+      ++o;
+    }
+  }
+}
+
 // Visual vertices of _kernel_update_render_fields (mpm_solver.py:795-803): support-weighted sum
 // of the particles' positions (`pos` holds the rows of scenes [s0, s1) in get_state order).
 __global__ void k_render_vverts(KParams P, int64_t s0, int64_t s1, const float* pos, const uint8_t* active,

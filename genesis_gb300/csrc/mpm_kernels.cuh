@@ -226,6 +226,16 @@ __global__ void k_set_constraints(KParams P, int64_t s0, int64_t s1, int64_t sta
 __global__ void k_remove_constraints(KParams P, int64_t s0, int64_t s1, int64_t start, int64_t n,
                                      const uint8_t* mask, ConstraintDev* cons);
 __global__ void k_constraints(KParams P, ConstraintDev* cons, const float* links, int32_t n_links);
+// Regular-lattice particle sampling on the device (utils/particle.py:180-278, 'regular' sampler).
+struct LatticeDev {
+  double lo[3], step[3], hi[3];  // per axis: first point, spacing, last point (np.linspace)
+  int64_t n[3];
+  int32_t shape;                 // 0 box, 1 sphere, 2 cylinder (z axis)
+  int32_t pad;
+  double center[3], radius;
+};
+__global__ void k_lattice_rows(LatticeDev L, int64_t* row_count);
+__global__ void k_lattice_fill(LatticeDev L, const int64_t* row_offset, float* out);
 __global__ void k_render_vverts(KParams P, int64_t s0, int64_t s1, const float* pos, const uint8_t* active,
                                 int64_t n_vverts, int32_t n_supports, const int32_t* support_idx,
                                 const float* support_w, float* vpos, uint8_t* vactive);

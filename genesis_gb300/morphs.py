@@ -175,3 +175,32 @@ class Nowhere(Morph):
 
     def sample(self, p_size, sampler):
         return np.zeros((int(self.n_particles), 3))
+
+
+def sample_regular_on_device(shape: str, pos, size, p_size, stream=None):
+    """The 'regular' samplers above computed on the GPU (libgbmpm mpm_sample_regular): returns a
+    float32 CUDA tensor [n, 3] equal to box/sphere/cylinder_to_particles(..., 'regular') rounded to
+    float32.  shape: 'box' (size = extents), 'sphere' (size = radius), 'cylinder' (size =
+    (radius, height))."""
+    import ctypes
+
+    import torch
+
+    from . import _lib
+
+    kinds = {"box": 0, "sphere": 1, "cylinder": 2}
+    if shape not in kinds:
+        raise GenesisException(f"Unsupported shape: {shape}.")
+    sz = np.zeros(3)
+    sz[: np.size(size)] = np.atleast_1d(np.asarray(size, dtype=np.float64))
+    p = (ctypes.c_double * 3)(*np.asarray(pos, dtype=np.float64))
+    s = (ctypes.c_double * 3)(*sz)
+    lib = _lib.load()
+    h = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream if stream is None else stream)
+    n = ctypes.c_int64()
+    _lib.check(lib.mpm_sample_regular(kinds[shape], p, s, float(p_size), None, 0, ctypes.byref(n), h), None,
+               "mpm_sample_regular")
+    out = torch.empty((max(1, n.value), 3), dtype=torch.float32, device="cuda")
+    _lib.check(lib.mpm_sample_regular(kinds[shape], p, s, float(p_size), out.data_ptr(), n.value, ctypes.byref(n), h),
+               None, "mpm_sample_regular")
+    return out[: n.value]

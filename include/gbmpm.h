@@ -271,6 +271,16 @@ int mpm_remove_particle_constraints(mpm_ctx* ctx, int64_t scene_begin, int64_t s
  * before returning.  Call whenever the links move (e.g. once per scene.step()). */
 int mpm_set_link_poses(mpm_ctx* ctx, int32_t n_links, const float* poses_host);
 
+/* Device-side 'regular' particle sampling (utils/particle.py:180-278): the lattice of
+ * np.linspace(lower + p/2, upper - p/2, max(1, round(extent / p))) per axis in row-major order,
+ * kept by the reference's rejection test; positions as float32 (x, y, z) into out (device).
+ * shape 0 box (size = extents), 1 sphere (size[0] = radius), 2 cylinder along z (size[0] =
+ * radius, size[1] = height); pos = centre.  *n_out receives the count; with out == NULL only the
+ * count is computed, and a too small capacity returns MPM_ERR_BAD_ARG after setting *n_out.
+ * Synchronises `stream`. */
+int mpm_sample_regular(int32_t shape, const double* pos, const double* size, double p_size, float* out,
+                       int64_t capacity, int64_t* n_out, void* stream);
+
 /* Render fields (mpm_solver.py:780-803, _kernel_update_render_fields) of scenes
  * [scene_begin, scene_end), in the reference [B, N] row order of mpm_get_state:
  *   pos_out [B,N,3]: the particle position, or the reference's "nowhere" point

@@ -483,3 +483,23 @@ def test_full_size_conservation_properties(gs):
     solver.substep_post_coupling()
     s = solver.get_state()
     assert s.active[0].all() and torch.isfinite(s.pos).all()
+
+
+@pytest.mark.parametrize("shape,size,p_size", [
+    ("box", (0.2, 0.13, 0.07), 0.01), ("box", (0.3, 0.3, 0.3), 1.0 / 128), ("sphere", 0.1, 0.0034),
+    ("sphere", 0.045, 0.01), ("cylinder", (0.05, 0.2), 0.0071)])
+def test_device_regular_sampling_equals_host(gs, shape, size, p_size):
+    """mpm_sample_regular reproduces the host 'regular' samplers (utils/particle.py:180-278)
+    bit for bit after the float32 rounding every particle position goes through."""
+    from genesis_gb300 import morphs
+
+    pos = (0.5, 0.47, 0.52)
+    if shape == "box":
+        host = morphs.box_to_particles(p_size, pos, size, "regular")
+    elif shape == "sphere":
+        host = morphs.sphere_to_particles(p_size, pos, size, "regular")
+    else:
+        host = morphs.cylinder_to_particles(p_size, pos, size[0], size[1], "regular")
+    dev = morphs.sample_regular_on_device(shape, pos, size, p_size).cpu().numpy()
+    assert dev.shape == host.shape
+    assert np.array_equal(dev, host.astype(np.float32))
