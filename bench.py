@@ -491,6 +491,7 @@ def run_dense(steps=20):
 def run_forms(batched_substeps=200, n_requests=48):
     """Batched (256 uneven scenes, one context) and served (continuous batching) forms, each
     against the plain form run scene by scene (one context per scene) on the same workload."""
+    from genesis_gb300 import _lib
     from genesis_gb300.batched import BatchedMPM, batched_workload
     from genesis_gb300.serve import MPMServer, serving_workload
 
@@ -523,11 +524,27 @@ def run_forms(batched_substeps=200, n_requests=48):
     srv = MPMServer(max_slots=64, particle_capacity=40_000_000, max_grid_res=129, chunk=10)
     sat = srv.run(reqs, realtime=False)
     t_alone = 0.0
-    for r in reqs:
-        one = BatchedMPM([r.spec], tune=False)
+    for r in reqs:  # GPU time of each request's substeps alone (the plain form, setup excluded)
+        one = BatchedMPM([r.spec], tune=False, positions=[r.payload])
         one.step(2)
         t_alone += _timed(lambda: one.step(r.spec.substeps))
         one.close()
+    # each request end to end through the plain form, one after another: context creation, upload
+    # of its payload, its substeps, read-back of its positions, teardown (wall clock, as the served
+    # run is timed)
+    import torch
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for r in reqs:
+        one = BatchedMPM([r.spec], tune=False, positions=[r.payload])
+        one.step(r.spec.substeps)
+        pos = torch.empty((r.spec.n_particles, 3), device="cuda")
+        _lib.check(one.lib.mpm_get_state(one.ctx, 0, 1, pos.data_ptr(), None, None, None, None, None,
+                                         one._stream()), one.ctx, "mpm_get_state")
+        pos.cpu()
+        one.close()
+    t_alone_wall = time.perf_counter() - t0
     mean_work = work / len(reqs)
     rate = 0.5 * sat["throughput"] / mean_work
     reqs2 = serving_workload(n_requests=n_requests, rate_hz=rate, seed=77, with_payload=True)
@@ -538,6 +555,8 @@ def run_forms(batched_substeps=200, n_requests=48):
                     "4 materials; continuous batching in one pool context",
         "throughput_saturated": sat["throughput"], "plain_alone_sequential": work / t_alone,
         "speedup_vs_plain": sat["throughput"] / (work / t_alone),
+        "plain_alone_end_to_end": work / t_alone_wall,
+        "speedup_vs_plain_end_to_end": sat["throughput"] / (work / t_alone_wall),
         "poisson_rate_hz": rate, "throughput_poisson": live["throughput"],
         "p50_latency_s": live["p50_s"], "p99_latency_s": live["p99_s"], "status": sat["status"] | live["status"],
         "unit": "particle-substeps/s",

@@ -86,7 +86,7 @@ def scene_config(spec: SceneSpec, eps: float) -> _lib.MpmSceneConfig:
 class BatchedMPM:
     """One libgbmpm context holding every scene of `specs`."""
 
-    def __init__(self, specs, tune: bool = True, device=None):
+    def __init__(self, specs, tune: bool = True, device=None, positions=None):
         self.specs = list(specs)
         self.lib = _lib.load()
         eps = float(np.finfo(np.float32).eps)
@@ -99,7 +99,8 @@ class BatchedMPM:
         self.offsets = np.concatenate([[0], np.cumsum([s.n_particles for s in specs])]).astype(np.int64)
         h = self._stream()
         for i, s in enumerate(specs):
-            p = torch.as_tensor(s.positions(), dtype=torch.float32, device="cuda")
+            host = s.positions() if positions is None or positions[i] is None else positions[i]
+            p = torch.as_tensor(host, dtype=torch.float32, device="cuda")
             _lib.check(self.lib.mpm_add_particles(self.ctx, i, i + 1, 0, s.n_particles, 0, 1, p.data_ptr(), h),
                        self.ctx, "mpm_add_particles")
         torch.cuda.current_stream().synchronize()
