@@ -33,7 +33,7 @@ SUBSTEP_DT = 1e-4
 GRID_DENSITY = 128
 SEED = 2024
 METRIC = "particle-substeps/s on 1 GB300 (plain, batched, served p50/p99) at stated tol"
-# per-kernel algorithmic bytes (per particle, per touched node); see the design doc
+# per-kernel algorithmic bytes (per particle, per touched node): what each kernel must move at least
 ALG_BYTES = {
     "p2g": (144, 16),   # read pos,vel,C,F,Jp,material (104 B) + write F,Jp (40 B); grid write 16 B/node
     "grid_op": (0, 32),  # read (momentum,mass) 16 B + write velocity 16 B per touched node

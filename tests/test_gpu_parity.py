@@ -1,6 +1,6 @@
 """GPU parity: the CUDA substep (through the Genesis-style API / C ABI) against the FP64 CPU oracle.
 
-Tolerances (BASELINE the benchmark spec): grid mass and momentum per substep within 1e-5 relative
+Tolerances: grid mass and momentum per substep within 1e-5 relative
 (L2 over the grid) of the FP64 oracle started from the same state; particle positions within
 1e-4 * domain (domain = 1 m) after 100 substeps.
 """
