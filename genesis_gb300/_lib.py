@@ -171,6 +171,7 @@ _SIGNATURES = {
                                         _P, _P, _P, _P, _P, _P, _P, _P]),
     "mpm_set_force_fields": (c_int32, [_P, c_int32, _P]),
     "mpm_sample_regular": (c_int32, [c_int32, _P, _P, c_double, _P, c_int64, _P, _P]),
+    "mpm_test_wait_timeout": (c_int32, [_P, _P]),
     "mpm_get_collider_forces": (c_int32, [_P, _P, c_int32, _P]),
     "mpm_version": (c_int32, []),
     "mpm_ctx_create_pool": (c_int32, [ctypes.c_void_p, c_int32, ctypes.POINTER(c_void_p)]),

@@ -1034,6 +1034,21 @@ int mpm_set_link_poses(mpm_ctx* ctx, int32_t n_links, const float* poses_host) {
   return MPM_OK;
 }
 
+int mpm_test_wait_timeout(mpm_ctx* ctx, void* stream) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "wait test inside a substep");
+  if (ctx->K + 2 <= SCAN_SINGLE_MAX) return fail(ctx, MPM_ERR_BAD_ARG, "context too small for the one-pass scan");
+  int r = enter(ctx, stream);
+  if (r) return r;
+  KParams P = make_params(ctx, ctx->cur, ctx->cur, ctx->cur);
+  P.scan_hold_tile0 = 1;
+  P.scan_spin_limit = 1u << 12;
+  k_scan_onepass<<<ctx->n_tiles, SCAN_THREADS, 0, ctx->cs>>>(P);
+  CKL();
+  ctx->sorted = false;  // offsets and work items are rebuilt before the next substep
+  return leave(ctx, stream);
+}
+
 int mpm_sample_regular(int32_t shape, const double* pos, const double* size, double p_size, float* out,
                        int64_t capacity, int64_t* n_out, void* stream) {
   if (!pos || !size || !n_out || !(p_size > 0) || shape < 0 || shape > 2) return MPM_ERR_BAD_ARG;

@@ -340,7 +340,11 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_onepass(KParams P) {
   const int2 ex = block_exclusive_scan2(cs, is, total);
   if (threadIdx.x < 32) {
     const int lane = threadIdx.x;
-    if (lane == 0) atomicExch(&P.scan_state[tile], scan_word(tile == 0 ? SCAN_PRE : SCAN_AGG, total.x, total.y));
+    // (scan_hold_tile0: a failure-detection test keeps tile 0 from publishing, so its successor's
+    // wait runs out)
+    const bool hold = P.scan_hold_tile0 && tile == 0;
+    if (lane == 0 && !hold)
+      atomicExch(&P.scan_state[tile], scan_word(tile == 0 ? SCAN_PRE : SCAN_AGG, total.x, total.y));
     int pc = 0, pi = 0;
     int j = tile - 1;
     unsigned spins = 0;
@@ -349,7 +353,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_onepass(KParams P) {
       const unsigned long long w = idx >= 0 ? atomicAdd(&P.scan_state[idx], 0ull) : SCAN_PRE;
       const unsigned long long flag = w & (3ull << 62);
       if (__any_sync(0xffffffffu, flag == 0ull)) {  // a predecessor has not published yet
-        if (++spins > SCAN_SPIN_LIMIT) {
+        if (++spins > (P.scan_spin_limit ? P.scan_spin_limit : SCAN_SPIN_LIMIT)) {
           if (lane == 0) atomicOr(P.status, MPM_STATUS_WAIT);
           break;
         }

@@ -124,6 +124,8 @@ struct KParams {
   unsigned long long* scan_state;  // one-pass scan: per tile, flag (2 bits) | count (31) | items (31)
   int32_t* scan_sync;          // one-pass scan: [0] tile ticket, [1] finished tiles
   int32_t n_tiles;
+  int32_t scan_hold_tile0;     // failure-detection test only: tile 0 never publishes
+  uint32_t scan_spin_limit;    // look-back wait limit (0: the default)
   uint32_t* pin;               // per-node bitmap of nodes touched by non-free particles (or null)
   int32_t* steps;              // per-scene substeps left (-1 unlimited, 0 frozen); null outside a substep
   int32_t n_scenes;

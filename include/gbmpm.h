@@ -271,6 +271,12 @@ int mpm_remove_particle_constraints(mpm_ctx* ctx, int64_t scene_begin, int64_t s
  * before returning.  Call whenever the links move (e.g. once per scene.step()). */
 int mpm_set_link_poses(mpm_ctx* ctx, int32_t n_links, const float* poses_host);
 
+/* Failure-detection test of the bounded device waits: runs the one-pass bucket scan with tile 0
+ * withheld, so the next tile's look-back wait runs out (after 4096 polls) and sets
+ * MPM_STATUS_WAIT in the status word; the kernel still completes and the context stays usable
+ * (the sort is rebuilt before the next substep).  Needs a context with more than 4096 buckets. */
+int mpm_test_wait_timeout(mpm_ctx* ctx, void* stream);
+
 /* Device-side 'regular' particle sampling (utils/particle.py:180-278): the lattice of
  * np.linspace(lower + p/2, upper - p/2, max(1, round(extent / p))) per axis in row-major order,
  * kept by the reference's rejection test; positions as float32 (x, y, z) into out (device).

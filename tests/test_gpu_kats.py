@@ -190,3 +190,36 @@ def test_particles_on_cell_faces_match_oracle(oracle):
     got = c.get_state(0, 1, n)
     assert np.abs(got["pos"] - out["pos"]).max() <= 1e-6
     c.close()
+
+
+def test_bounded_wait_times_out_and_context_recovers():
+    """Failure detection without a GPU fault: the one-pass scan's look-back wait is bounded.  With
+    tile 0 withheld (mpm_test_wait_timeout) the wait runs out, MPM_STATUS_WAIT is reported through
+    the status word, and the context keeps working: the next substeps rebuild the sort and match
+    a context that never saw the failure."""
+    from genesis_gb300 import _lib
+
+    n = 3000
+    x = _cloud(n, seed=8)
+
+    def make():
+        sc = scene_record(_lib, DT, n, density=64.0, gravity=(0.0, 0.0, -9.81))
+        c = Ctx([sc], [material_record(_lib, 0, 0, 0, 1e4, 1e4)])
+        c.add(0, 1, 0, x, 0)
+        return c
+
+    a, b = make(), make()
+    a.substeps(2)
+    b.substeps(2)
+    a.call("mpm_test_wait_timeout", a.stream)
+    torch.cuda.synchronize()
+    st, _ = a.status()
+    assert st & _lib.STATUS_WAIT, st
+    assert a.status() == (0, 0)  # the read cleared it
+    a.substeps(6)
+    b.substeps(6)
+    sa, sb = a.get_state(0, 1, n), b.get_state(0, 1, n)
+    assert a.status() == (0, 0)
+    assert np.abs(sa["pos"] - sb["pos"]).max() <= 1e-6
+    a.close()
+    b.close()
