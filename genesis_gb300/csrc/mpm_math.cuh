@@ -49,6 +49,15 @@ GB_HD float grsqrt_acc(float x) {
 #endif
 }
 GB_HD double grsqrt_acc(double x) { return 1.0 / sqrt(x); }
+// sqrt of a positive argument for a rotation angle (only the convergence rate depends on it)
+GB_HD float gsqrt_fast(float x) {
+#ifdef __CUDA_ARCH__
+  return x * rsqrtf(x);
+#else
+  return sqrtf(x);
+#endif
+}
+GB_HD double gsqrt_fast(double x) { return sqrt(x); }
 template <typename T> GB_HD T gmax(T a, T b) { return a > b ? a : b; }
 
 // ------------------------------------------------------------------------------------
@@ -75,10 +84,10 @@ template <> struct Eps<double> { static constexpr double v = 2.220446049250313e-
 // in U and V, which the corotated stress 2 mu (F - U V^T) F^T amplifies by mu.
 template <typename T>
 GB_HD bool jacobi_rotate(T& app, T& aqq, T& apq, T& arp, T& arq, T* V, int p, int q) {
-  if (!(gabs(apq) > Eps<T>::v * gsqrt(gabs(app * aqq)))) return false;
+  if (!(apq * apq > Eps<T>::v * Eps<T>::v * gabs(app * aqq))) return false;  // |apq| > eps sqrt|app aqq|
   const T theta = gdiv_fast(aqq - app, T(2) * apq);
   const T at = gabs(theta);
-  T t = (at < T(1e18)) ? gdiv_fast(T(1), at + gsqrt(theta * theta + T(1))) : gdiv_fast(T(0.5), at);
+  T t = (at < T(1e18)) ? gdiv_fast(T(1), at + gsqrt_fast(theta * theta + T(1))) : gdiv_fast(T(0.5), at);
   if (theta < T(0)) t = -t;
   const T c = grsqrt_acc(t * t + T(1));
   const T s = t * c;
@@ -122,7 +131,7 @@ GB_HD void givens_qr_step(T* B, T* Q, int j, int i) {
   const T r2 = a * a + b * b;
   T c = T(1), s = T(0);
   if (r2 > T(0)) {
-    const T inv = T(1) / gsqrt(r2);
+    const T inv = grsqrt_acc(r2);  // c^2 + s^2 = 1 to rounding
     c = a * inv;
     s = b * inv;
   }
