@@ -82,6 +82,8 @@ struct mpm_ctx {
   ColliderDev* d_colliders = nullptr;  // kinematic colliders (capacity MAX_COLLIDERS once allocated)
   double* d_collider_acc = nullptr;    // [MAX_COLLIDERS][6]
   int32_t n_colliders = 0;
+  int32_t cpic_slots = 0;            // CPIC collider slots (normal planes); 0: CPIC off
+  uint32_t* d_cpic_mask = nullptr;   // CPIC: per particle slot, the stencil nodes behind a collider
   float* d_links = nullptr;         // kinematic link poses [scene][link] (pos xyz, quat wxyz)
   int32_t n_links = 0;
   int32_t* d_steps = nullptr;
@@ -99,6 +101,7 @@ struct mpm_ctx {
   int p2g_threads = 256, ppt = 2, g2p_threads = 128;
   bool use_graph = true;
   int p2g_blocks = 0, g2p_blocks = 0, keys_blocks = 0, grid_blocks = 0, io_blocks = 0;
+  int p2g_cpic_blocks = 0, g2p_cpic_blocks = 0;
 
   // streams, graph, timing
   cudaStream_t cs = nullptr;
@@ -187,6 +190,8 @@ KParams make_params(mpm_ctx* ctx, int src, int dst, int g) {
   P.colliders = ctx->d_colliders;
   P.n_colliders = ctx->n_colliders;
   P.collider_acc = ctx->d_collider_acc;
+  P.cpic_slots = ctx->cpic_slots;
+  P.cpic_mask = ctx->d_cpic_mask;
   P.scan_sync = ctx->d_scan_sync;
   P.n_tiles = ctx->n_tiles;
   P.pin = ctx->d_pin;
@@ -263,7 +268,10 @@ int launch_pre(mpm_ctx* ctx, int c, cudaStream_t s) {
   P.n = ctx->n;
   P.steps = ctx->d_steps;
   Timer t(ctx, s, KT_P2G);
-  k_p2g<<<ctx->p2g_blocks, ctx->p2g_threads, p2g_dyn_smem(ctx->p2g_threads, P.chunk), s>>>(P);
+  if (ctx->cpic_slots > 0 && ctx->n_colliders > 0)
+    k_p2g_cpic<<<ctx->p2g_cpic_blocks, ctx->p2g_threads, p2g_dyn_smem(ctx->p2g_threads, P.chunk), s>>>(P);
+  else
+    k_p2g<<<ctx->p2g_blocks, ctx->p2g_threads, p2g_dyn_smem(ctx->p2g_threads, P.chunk), s>>>(P);
   CKL();
   return MPM_OK;
 }
@@ -287,7 +295,10 @@ int launch_post(mpm_ctx* ctx, int c, cudaStream_t s, bool fuse_grid = false) {
   ctx->grid_momentum[c] = fuse_grid;
   {
     Timer t(ctx, s, KT_G2P);
-    k_g2p<<<ctx->g2p_blocks, ctx->g2p_threads, 0, s>>>(P);
+    if (ctx->cpic_slots > 0 && ctx->n_colliders > 0)
+      k_g2p_cpic<<<ctx->g2p_cpic_blocks, ctx->g2p_threads, 0, s>>>(P);
+    else
+      k_g2p<<<ctx->g2p_blocks, ctx->g2p_threads, 0, s>>>(P);
   }
   CKL();
   if (ctx->d_cons) {  // after g2p, as substep_post_coupling does (mpm_solver.py:538-540)
@@ -317,6 +328,17 @@ int compute_launch_shapes(mpm_ctx* ctx) {
   int occ2 = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, k_g2p, ctx->g2p_threads, 0));
   ctx->g2p_blocks = ctx->n_sm * (occ2 > 0 ? occ2 : 1);  // persistent over the work items
+  if (ctx->cpic_slots > 0) {
+    CK(cudaFuncSetAttribute(k_p2g_cpic, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)p2g_dyn_smem(P2G_MAX_THREADS, P2G_MAX_CHUNK)));
+    int oc = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&oc, k_p2g_cpic, ctx->p2g_threads,
+                                                     p2g_dyn_smem(ctx->p2g_threads, ctx->p2g_threads * ctx->ppt)));
+    ctx->p2g_cpic_blocks = ctx->n_sm * (oc > 0 ? oc : 1);
+    oc = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&oc, k_g2p_cpic, ctx->g2p_threads, 0));
+    ctx->g2p_cpic_blocks = ctx->n_sm * (oc > 0 ? oc : 1);
+  }
   int occ3 = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ3, k_keys, 256, 0));
   const int64_t ext = ctx->n_phys > ctx->n ? ctx->n_phys : ctx->n;
@@ -671,6 +693,7 @@ int mpm_ctx_destroy(mpm_ctx* ctx) {
   if (ctx->d_colliders) cudaFree(ctx->d_colliders);
   if (ctx->d_ffs) cudaFree(ctx->d_ffs);
   if (ctx->d_collider_acc) cudaFree(ctx->d_collider_acc);
+  if (ctx->d_cpic_mask) cudaFree(ctx->d_cpic_mask);
   if (ctx->d_links) cudaFree(ctx->d_links);
   if (ctx->ev_in) cudaEventDestroy(ctx->ev_in);
   if (ctx->ev_out) cudaEventDestroy(ctx->ev_out);
@@ -915,6 +938,8 @@ int mpm_set_colliders(mpm_ctx* ctx, int32_t n, const mpm_collider* colliders) {
     if (c.type < MPM_COLLIDER_SPHERE || c.type > MPM_COLLIDER_BOX)
       return fail(ctx, MPM_ERR_BAD_ARG, "unknown collider type");
     if (c.scene < -1 || c.scene >= ctx->n_scenes) return fail(ctx, MPM_ERR_BAD_ARG, "collider scene out of range");
+    if (ctx->cpic_slots > 0 && i >= ctx->cpic_slots)
+      return fail(ctx, MPM_ERR_BAD_ARG, "more colliders than CPIC slots (mpm_enable_cpic)");
     ColliderDev& d = h[(size_t)i];
     std::memset(&d, 0, sizeof(d));
     d.type = c.type;
@@ -945,6 +970,62 @@ int mpm_set_colliders(mpm_ctx* ctx, int32_t n, const mpm_collider* colliders) {
   if (n != ctx->n_colliders) drop_graph(ctx);  // the count is a captured kernel argument
   ctx->n_colliders = n;
   return MPM_OK;
+}
+
+int mpm_enable_cpic(mpm_ctx* ctx, int32_t n_slots, void* stream) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (n_slots < 0 || n_slots > MAX_COLLIDERS) return fail(ctx, MPM_ERR_BAD_ARG, "bad CPIC slot count");
+  if (ctx->pool) return fail(ctx, MPM_ERR_BAD_ARG, "CPIC is not available in pool mode");
+  if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "CPIC set-up inside a substep");
+  if (n_slots > 0 && ctx->n_colliders > n_slots)
+    return fail(ctx, MPM_ERR_BAD_ARG, "fewer CPIC slots than colliders");
+  int r = enter(ctx, stream);
+  if (r) return r;
+  const size_t cap = (size_t)ctx->cap;
+  const int nf_new = n_slots > 0 ? NF_MUSCLE + 3 * n_slots : ctx->nf;
+  if (nf_new > ctx->nf) {  // grow both particle buffers; the current one keeps its planes
+    float* nb[2] = {nullptr, nullptr};
+    for (int b = 0; b < 2; ++b) {
+      cudaError_t e = cudaMalloc((void**)&nb[b], sizeof(float) * (size_t)nf_new * cap);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        if (nb[0]) cudaFree(nb[0]);
+        return fail(ctx, MPM_ERR_OOM, "CPIC particle planes: " + std::string(cudaGetErrorString(e)));
+      }
+    }
+    float* cur = nb[ctx->cur];
+    CK(cudaMemcpyAsync(cur, ctx->d_pbuf[ctx->cur], sizeof(float) * (size_t)ctx->nf * cap, cudaMemcpyDeviceToDevice,
+                       ctx->cs));
+    if (ctx->nf == NF_BASE) {  // muscle planes at their defaults: actu 0, direction (0, 0, 1)
+      k_fill_plane<<<ctx->io_blocks, 256, 0, ctx->cs>>>(cur + (size_t)PF_ACTU * cap, (int64_t)(3 * cap), 0.f);
+      k_fill_plane<<<ctx->io_blocks, 256, 0, ctx->cs>>>(cur + (size_t)(PF_MDIR + 2) * cap, (int64_t)cap, 1.f);
+      CKL();
+    }
+    CK(cudaStreamSynchronize(ctx->cs));
+    for (int b = 0; b < 2; ++b) {
+      for (void*& a : ctx->allocs)
+        if (a == (void*)ctx->d_pbuf[b]) a = (void*)nb[b];
+      cudaFree(ctx->d_pbuf[b]);
+      ctx->d_pbuf[b] = nb[b];
+    }
+    ctx->nf = nf_new;
+  }
+  if (n_slots > 0) {  // the normals start at zero (LegacyCoupler.reset, legacy_coupler.py:114)
+    CK(cudaMemsetAsync(ctx->d_pbuf[ctx->cur] + (size_t)PF_CPIC * cap, 0, sizeof(float) * 3 * (size_t)n_slots * cap,
+                       ctx->cs));
+    if (!ctx->d_cpic_mask) {
+      cudaError_t e = cudaMalloc((void**)&ctx->d_cpic_mask, sizeof(uint32_t) * cap);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        ctx->d_cpic_mask = nullptr;
+        return fail(ctx, MPM_ERR_OOM, "CPIC mask allocation failed");
+      }
+    }
+  }
+  ctx->cpic_slots = n_slots;
+  drop_graph(ctx);  // kernel choice and plane count are captured
+  if ((r = compute_launch_shapes(ctx))) return r;
+  return leave(ctx, stream);
 }
 
 int mpm_get_collider_forces(mpm_ctx* ctx, double* out_host, int32_t reset, void* stream) {

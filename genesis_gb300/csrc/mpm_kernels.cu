@@ -45,6 +45,7 @@ __device__ __forceinline__ void write_defaults(float* D, int64_t cap, int64_t i,
     D[(int64_t)(PF_MDIR + 1) * cap + i] = 0.f;
     D[(int64_t)(PF_MDIR + 2) * cap + i] = 1.f;
   }
+  for (int k = NF_MUSCLE; k < nf; ++k) D[(int64_t)k * cap + i] = 0.f;  // CPIC normals
 }
 
 // FP64 re-solve for the rare particle whose FP32 factor fails its residual check; kept out
@@ -474,517 +475,6 @@ __global__ void k_perm(KParams P) {
       if (P.steps[s] > 0) P.steps[s] -= 1;
 }
 
-// ------------------------------------------------------------------ P2G
-namespace {
-
-// Loads one particle from the old order (planes of `S`, index si).
-struct Particle {
-  float x[3], v[3], C[9], F[9], Jp, pid, actu, mdir[3];
-  uint32_t info;
-};
-
-__device__ __forceinline__ void load_particle(const KParams& P, const float* Sx, int64_t si, Particle& q) {
-  const int64_t cap = P.cap;
-#pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    q.x[d] = Sx[(int64_t)(PF_POS + d) * cap + si];
-    q.v[d] = Sx[(int64_t)(PF_VEL + d) * cap + si];
-  }
-#pragma unroll
-  for (int k = 0; k < 9; ++k) {
-    q.C[k] = Sx[(int64_t)(PF_C + k) * cap + si];
-    q.F[k] = Sx[(int64_t)(PF_F + k) * cap + si];
-  }
-  q.Jp = Sx[(int64_t)PF_JP * cap + si];
-  q.info = __float_as_uint(Sx[(int64_t)PF_INFO * cap + si]);
-  q.pid = Sx[(int64_t)PF_PID * cap + si];
-  q.actu = 0.f;
-  q.mdir[0] = 0.f, q.mdir[1] = 0.f, q.mdir[2] = 1.f;
-  if (P.nf > NF_BASE) {
-    q.actu = Sx[(int64_t)PF_ACTU * cap + si];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) q.mdir[d] = Sx[(int64_t)(PF_MDIR + d) * cap + si];
-  }
-}
-
-// Writes a particle to its sorted slot.  Velocity and C are left out: G2P of the same substep
-// overwrites both for every particle of an active bucket before anything reads them.
-__device__ __forceinline__ void store_particle(const KParams& P, float* Dx, int64_t slot, const Particle& q) {
-  const int64_t cap = P.cap;
-#pragma unroll
-  for (int d = 0; d < 3; ++d) Dx[(int64_t)(PF_POS + d) * cap + slot] = q.x[d];
-#pragma unroll
-  for (int k = 0; k < 9; ++k) Dx[(int64_t)(PF_F + k) * cap + slot] = q.F[k];
-  Dx[(int64_t)PF_JP * cap + slot] = q.Jp;
-  Dx[(int64_t)PF_INFO * cap + slot] = __uint_as_float(q.info);
-  Dx[(int64_t)PF_PID * cap + slot] = q.pid;
-  if (P.nf > NF_BASE) {
-    Dx[(int64_t)PF_ACTU * cap + slot] = q.actu;
-#pragma unroll
-    for (int d = 0; d < 3; ++d) Dx[(int64_t)(PF_MDIR + d) * cap + slot] = q.mdir[d];
-  }
-}
-
-// Local cell (0..63) of a particle inside the block whose node origin is `org`, or 64.
-__device__ __forceinline__ int local_cell(const SceneDev& S, const float* x, const int* org, int* tb) {
-  bool inside = true;
-#pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    const float t = __fmul_rn(x[d], S.inv_dx);
-    const float f = floorf(__fsub_rn(t, 0.5f));
-    const int b = (f > -1e9f && f < 1e9f) ? (int)f : -1000000;
-    tb[d] = b - S.offset[d] - org[d];
-    inside = inside && tb[d] >= 0 && tb[d] < BLK;
-  }
-  return inside ? (tb[0] * BLK + tb[1]) * BLK + tb[2] : BLK_NODES;
-}
-
-__device__ __forceinline__ void block_origin(const SceneDev& S, int64_t key, int* org) {
-  const int64_t lb = key - S.block_base;
-  org[2] = (int)(lb % S.bres[2]) * BLK;
-  org[1] = (int)((lb / S.bres[2]) % S.bres[1]) * BLK;
-  org[0] = (int)(lb / ((int64_t)S.bres[2] * S.bres[1])) * BLK;
-}
-
-}  // namespace
-
-// Per work item (one grid block's bucket, up to `chunk` <= P2G_MAX_CHUNK particles):
-//  1. counting-sort the item's particles by cell in shared memory (native integer atomics);
-//  2. in slot order (coalesced gathers through perm): compute_F_tmp + svd + material update
-//     + stress (mpm_solver.py:293-307, 339-377), write the particle to its slot, and leave its
-//     scatter parameters (fx, mass, q = m v - sum_k a_k fx_k, a_k = dx * affine[:,k]) in a
-//     shared record at its cell-sorted position;
-//  3. one thread per (cell, ox) walks its cell's records and sums the APIC mass/momentum
-//     w_o (q + sum_k o_k a_k), w_o m (mpm_solver.py:379-418) of the 9 nodes (ox, *, *) in
-//     registers, then adds them to its warp's private 6^3 shared tile (plain float4
-//     read-modify-writes; no two lanes of a warp share a node): one tile update per cell and
-//     node instead of one per particle and node;
-//  4. sum the warp tiles and flush with one 16-byte vector reduction per node.
-// Capped at 96 registers: five 128-thread CTAs per SM instead of four at 128 registers, which
-// measured 5% faster despite a small spill.
-__global__ void __maxnreg__(96) k_p2g(KParams P) {
-  extern __shared__ __align__(16) unsigned char p2g_smem[];
-  __shared__ int s_cnt[BLK_NODES + 1];
-  __shared__ int s_touch[8];
-  const int n_items = *P.n_items;
-  const int T = blockDim.x, nw = T >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float4* s_tile = reinterpret_cast<float4*>(p2g_smem);
-  float4* s_rec = s_tile + nw * TILE_NODES;
-  uint32_t* s_cr = reinterpret_cast<uint32_t*>(s_rec + P2G_REC * P.chunk);
-  const int64_t cap = P.cap;
-  const float* Sx = P.src;
-  float* Dx = P.dst;
-  float4* my_tile = s_tile + warp * TILE_NODES;
-  // tiles, cell counts and touch flags start zeroed; each item leaves them zeroed again
-  for (int t = threadIdx.x; t < nw * TILE_NODES; t += T) s_tile[t] = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (threadIdx.x <= BLK_NODES) s_cnt[threadIdx.x] = 0;
-  if (threadIdx.x < 8) s_touch[threadIdx.x] = 0;
-  __syncthreads();
-  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
-    const int4 item = P.items[it];
-    const int cnt = item.z - item.y;
-    const bool frozen = item.x < P.K && P.steps && P.steps[P.block_scene[item.x]] == 0;
-    if (item.x >= P.K || frozen) {  // inactive bucket or frozen scene: carry over unchanged (uniform)
-      for (int j = threadIdx.x; j < cnt; j += T) {
-        const int64_t si = P.perm[item.y + j];
-        for (int k = 0; k < P.nf; ++k) Dx[(int64_t)k * cap + item.y + j] = Sx[(int64_t)k * cap + si];
-      }
-      continue;
-    }
-    const int32_t sid = P.block_scene[item.x];
-    const SceneDev& S = P.scenes[sid];
-    int org[3];
-    block_origin(S, item.x, org);
-    // 1. cell ranks
-    for (int j = threadIdx.x; j < cnt; j += T) {
-      const int64_t si = P.perm[item.y + j];
-      float x[3];
-      int tb[3];
-#pragma unroll
-      for (int d = 0; d < 3; ++d) x[d] = Sx[(int64_t)(PF_POS + d) * cap + si];
-      const int cell = local_cell(S, x, org, tb);
-      const int r = atomicAdd(&s_cnt[cell], 1);
-      s_cr[j] = ((uint32_t)cell << 16) | (uint32_t)r;
-    }
-    __syncthreads();
-    // every warp scans the 64 cell counts into registers: lane l holds the start of cells l and
-    // l + 32 (no extra barrier; starts are fetched by shuffles, a cell ends where the next starts)
-    int offA, offB, tot_in;
-    {
-      const int a = s_cnt[lane], b = s_cnt[lane + 32];
-      int ia = a, ib = b;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int ta = __shfl_up_sync(0xffffffffu, ia, o), tbv = __shfl_up_sync(0xffffffffu, ib, o);
-        if (lane >= o) {
-          ia += ta;
-          ib += tbv;
-        }
-      }
-      const int tot_a = __shfl_sync(0xffffffffu, ia, 31);
-      offA = ia - a;
-      offB = tot_a + ib - b;
-      tot_in = __shfl_sync(0xffffffffu, tot_a + ib, 31);  // start of the particles outside the block's cells
-    }
-    // 2. material + stress in slot order; scatter parameters to the sorted record (lanes of a warp
-    //    iterate together so the offset shuffles see the whole warp)
-    for (int jb = threadIdx.x - lane; jb < cnt; jb += T) {
-      const int j = jb + lane;
-      const uint32_t cr = j < cnt ? s_cr[j] : 0u;
-      const int cell = (int)(cr >> 16);
-      const int oa = __shfl_sync(0xffffffffu, offA, cell & 31), ob = __shfl_sync(0xffffffffu, offB, cell & 31);
-      if (j >= cnt) continue;
-      const int p = (cell < 32 ? oa : (cell < BLK_NODES ? ob : tot_in)) + (int)(cr & 0xffffu);
-      const int64_t slot = item.y + j;
-      const int64_t si = P.perm[slot];
-      Particle pt;
-      load_particle(P, Sx, si, pt);
-      bool scattered = false;
-      if (pt.info & INFO_ACTIVE) {
-        const MaterialDev& M = P.mats[pt.info & INFO_MAT_MASK];
-        // F_tmp = (I + dt C) F   (compute_F_tmp, mpm_solver.py:293-299)
-        float A[9], Ft[9];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) A[k] = ((k % 4 == 0) ? 1.f : 0.f) + S.dt * pt.C[k];
-        mat_mul(A, pt.F, Ft);
-        float Pk[9], Jpn = pt.Jp;
-        if (M.type == MT_LIQUID && M.mu == 0.f) {
-          // Non-viscous liquid (liquid.py:36-49 with mu = 0) uses only J = sigma0 sigma1 sigma2 of the
-          // SVD, which equals det F_tmp (det U = det V = 1): F_new = J^(1/3) I, stress = lam J (J-1) I.
-          const float J = Ft[0] * (Ft[4] * Ft[8] - Ft[5] * Ft[7]) - Ft[1] * (Ft[3] * Ft[8] - Ft[5] * Ft[6]) +
-                          Ft[2] * (Ft[3] * Ft[7] - Ft[4] * Ft[6]);
-          const float j3 = powf(J, 1.f / 3.f);
-          const float pr = M.lam * J * (J - 1.f);
-#pragma unroll
-          for (int k = 0; k < 9; ++k) {
-            pt.F[k] = (k % 4 == 0) ? j3 : 0.f;
-            Pk[k] = (k % 4 == 0) ? pr : 0.f;
-          }
-        } else {
-          float U[9], sig[3], V[9];
-          const float res = svd3<float, SVD_SWEEPS>(Ft, U, sig, V);
-          if (!(res <= SVD_FP64_TOL)) {
-            svd3_fp64(Ft, U, sig, V);
-            atomicAdd(P.fp64_count, 1ull);
-          }
-          material_update<float>(M, Ft, U, sig, V, pt.Jp, pt.actu, pt.mdir, P.eps_norm, pt.F, Jpn, Pk);
-        }
-        pt.Jp = Jpn;
-        if (cell < BLK_NODES) {
-          const int tb0 = cell >> 4, tb1 = (cell >> 2) & 3, tb2 = cell & 3;
-          const float mass = M.mass;
-          float fx[3];
-          const int tbv[3] = {tb0, tb1, tb2};
-#pragma unroll
-          for (int d = 0; d < 3; ++d) fx[d] = __fmul_rn(pt.x[d], S.inv_dx) - (float)(tbv[d] + S.offset[d] + org[d]);
-          float a[9];  // a[k*3 + r] = dx * affine[r][k]
-#pragma unroll
-          for (int r = 0; r < 3; ++r)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) a[k * 3 + r] = S.dx * (S.stress_scale * Pk[r * 3 + k] + mass * pt.C[r * 3 + k]);
-          float qv[3];
-#pragma unroll
-          for (int r = 0; r < 3; ++r) qv[r] = mass * pt.v[r] - (a[r] * fx[0] + a[3 + r] * fx[1] + a[6 + r] * fx[2]);
-          float4* rec = s_rec + P2G_REC * p;
-          rec[0] = make_float4(fx[0], fx[1], fx[2], mass);
-          rec[1] = make_float4(qv[0], qv[1], qv[2], a[0]);
-          rec[2] = make_float4(a[1], a[2], a[3], a[4]);
-          rec[3] = make_float4(a[5], a[6], a[7], a[8]);
-          scattered = true;
-          if (!(pt.info & INFO_FREE) && P.pin) {  // its 27 nodes lose all momentum (mpm_solver.py:420-421)
-            for (int o = 0; o < 27; ++o) {
-              const int64_t ad = node_addr(S, org[0] + tb0 + o / 9, org[1] + tb1 + (o / 3) % 3, org[2] + tb2 + o % 3);
-              atomicOr(&P.pin[ad >> 5], 1u << (ad & 31));
-            }
-          }
-        } else {
-          atomicOr(P.status, 2u);  // cannot happen for a correctly keyed particle; never touches memory
-        }
-      }
-      if (!scattered && cell < BLK_NODES) {  // holds a place in its cell's run: contributes nothing
-        float4* rec = s_rec + P2G_REC * p;
-        rec[0] = make_float4(0.5f, 0.5f, 0.5f, 0.f);
-        rec[1] = rec[2] = rec[3] = make_float4(0.f, 0.f, 0.f, 0.f);
-      }
-      store_particle(P, Dx, slot, pt);
-    }
-    __syncthreads();
-    // 3. cell-major scatter: unit u = (cell, ox) sums the 9 nodes (ox, *, *) of the stencils of
-    //    all particles of its cell in registers and adds them to the warp tile once.  A warp's
-    //    32 units span fewer than 16 consecutive cells, so no two of its lanes share a node.
-    for (int u0 = 0; u0 < 3 * BLK_NODES; u0 += T) {
-      const int u = u0 + threadIdx.x;
-      const bool has = u < 3 * BLK_NODES;
-      const int cell = has ? u / 3 : 0, ox = has ? u - 3 * (u / 3) : 0;
-      const int nx = (cell + 1) & 31;
-      const int oa = __shfl_sync(0xffffffffu, offA, cell & 31), ob = __shfl_sync(0xffffffffu, offB, cell & 31);
-      const int na = __shfl_sync(0xffffffffu, offA, nx), nb = __shfl_sync(0xffffffffu, offB, nx);
-      const int beg = cell < 32 ? oa : ob;
-      const int end = cell + 1 < 32 ? na : (cell + 1 < BLK_NODES ? nb : tot_in);
-      const int len = has ? end - beg : 0;
-      const int nmax = __reduce_max_sync(0xffffffffu, len);
-      if (nmax == 0) continue;  // warp-uniform
-      float4 acc[3][3];
-#pragma unroll
-      for (int oy = 0; oy < 3; ++oy)
-#pragma unroll
-        for (int oz = 0; oz < 3; ++oz) acc[oy][oz] = make_float4(0.f, 0.f, 0.f, 0.f);
-      const float fo = (float)ox;
-      for (int j = 0; j < nmax; ++j) {
-        if (j < len) {
-          const float4* rec = s_rec + P2G_REC * (beg + j);
-          const float4 r0 = rec[0], r1 = rec[1], r2 = rec[2], r3 = rec[3];
-          float wxv[3], wy[3], wz[3];
-          bspline_w(r0.x, wxv);
-          bspline_w(r0.y, wy);
-          bspline_w(r0.z, wz);
-          const float wx = ox == 0 ? wxv[0] : (ox == 1 ? wxv[1] : wxv[2]);
-          // a (k-major, a[k*3 + r]) = r1.w, r2.x, r2.y | r2.z, r2.w, r3.x | r3.y, r3.z, r3.w
-          const float t0x = r1.x + fo * r1.w, t0y = r1.y + fo * r2.x, t0z = r1.z + fo * r2.y;
-#pragma unroll
-          for (int oy = 0; oy < 3; ++oy) {
-            const float t1x = t0x + (float)oy * r2.z, t1y = t0y + (float)oy * r2.w, t1z = t0z + (float)oy * r3.x;
-            const float w01 = wx * wy[oy];
-#pragma unroll
-            for (int oz = 0; oz < 3; ++oz) {
-              const float wt = w01 * wz[oz];
-              acc[oy][oz].x += wt * (t1x + (float)oz * r3.y);
-              acc[oy][oz].y += wt * (t1y + (float)oz * r3.z);
-              acc[oy][oz].z += wt * (t1z + (float)oz * r3.w);
-              acc[oy][oz].w += wt * r0.w;
-            }
-          }
-        }
-      }
-      // Lanes of neighbouring cells reach the same node at different (oy, oz) steps: a
-      // __syncwarp between steps orders those read-modify-writes.
-      const int tb0 = cell >> 4, tb1 = (cell >> 2) & 3, tb2 = cell & 3;
-#pragma unroll
-      for (int oy = 0; oy < 3; ++oy)
-#pragma unroll
-        for (int oz = 0; oz < 3; ++oz) {
-          if (len > 0) {
-            float4* g = my_tile + ((tb0 + ox) * TILE + (tb1 + oy)) * TILE + (tb2 + oz);
-            float4 h = *g;
-            h.x += acc[oy][oz].x;
-            h.y += acc[oy][oz].y;
-            h.z += acc[oy][oz].z;
-            h.w += acc[oy][oz].w;
-            *g = h;
-          }
-          __syncwarp();
-        }
-    }
-    __syncthreads();
-    // 4. flush
-    if (threadIdx.x <= BLK_NODES) s_cnt[threadIdx.x] = 0;  // every warp's scan read it before phase 2 ended
-    for (int t = threadIdx.x; t < TILE_NODES; t += T) {
-      float4 g = s_tile[t];
-      s_tile[t] = make_float4(0.f, 0.f, 0.f, 0.f);
-      for (int ww = 1; ww < nw; ++ww) {
-        const float4 h = s_tile[ww * TILE_NODES + t];
-        s_tile[ww * TILE_NODES + t] = make_float4(0.f, 0.f, 0.f, 0.f);
-        g.x += h.x;
-        g.y += h.y;
-        g.z += h.z;
-        g.w += h.w;
-      }
-      if (g.w == 0.f) continue;
-      const int tx = t / (TILE * TILE), ty = (t / TILE) % TILE, tz = t % TILE;
-      const int gx = org[0] + tx, gy = org[1] + ty, gz = org[2] + tz;
-      if (gx >= S.res[0] || gy >= S.res[1] || gz >= S.res[2]) continue;
-      atomicAdd(reinterpret_cast<float4*>(&P.grid[node_addr(S, gx, gy, gz)]), g);
-      s_touch[(tx >> 2) * 4 + (ty >> 2) * 2 + (tz >> 2)] = 1;
-    }
-    __syncthreads();
-    if (threadIdx.x < 8 && s_touch[threadIdx.x]) {
-      s_touch[threadIdx.x] = 0;
-      const int bx = org[0] / BLK + (threadIdx.x >> 2), by = org[1] / BLK + ((threadIdx.x >> 1) & 1),
-                bz = org[2] / BLK + (threadIdx.x & 1);
-      if (bx < S.bres[0] && by < S.bres[1] && bz < S.bres[2]) {
-        const int64_t blk = S.block_base + ((int64_t)bx * S.bres[1] + by) * S.bres[2] + bz;
-        if (atomicExch(&P.flags[blk], 1) == 0) P.list[atomicAdd(P.nlist, 1)] = (int32_t)blk;
-      }
-    }
-  }
-}
-
-// ------------------------------------------------------------------ G2P
-// mpm_solver.py:423-481 (g2p) with the particle boundary of boundaries.py:22-32, over the
-// same work items as the P2G that wrote the particles (so every item's particles read one
-// 6^3 node tile, staged once in shared memory), followed by the bucket key of the new
-// position and a warp-aggregated rank within the bucket.
-__device__ __forceinline__ void add_rank(const KParams& P, bool valid, int32_t key, int64_t i, int lane) {
-  const unsigned am = __ballot_sync(0xffffffffu, valid);
-  if (valid) {
-    const unsigned peers = __match_any_sync(am, key);
-    const int leader = __ffs(peers) - 1;
-    int r = 0;
-    if (lane == leader) r = atomicAdd(&P.count[key], __popc(peers));
-    r = __shfl_sync(peers, r, leader);
-    r += __popc(peers & ((1u << lane) - 1u));
-    P.key[i] = key;
-    P.rank[i] = r;
-  }
-}
-
-__global__ void __launch_bounds__(256) k_g2p(KParams P) {
-  __shared__ float4 s_v[TILE_NODES];
-  if (P.fuse_grid) {
-    // the grid op's other duty: zero the blocks the previous substep left in the other buffer
-    // (the next P2G adds into it); k_perm resets that list's length after this kernel
-    const int64_t n_other = (int64_t)*P.nlist_other * BLK_NODES;
-    for (int64_t i = grid_stride_begin(); i < n_other; i += grid_stride_step()) {
-      const int32_t blk = P.list_other[i / BLK_NODES];
-      P.grid_other[(int64_t)blk * BLK_NODES + (i % BLK_NODES)] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (i % BLK_NODES == 0) P.flags_other[blk] = 0;
-    }
-  } else if (blockIdx.x == 0 && threadIdx.x == 0) {
-    *P.nlist_other = 0;
-  }
-  const int n_items = *P.n_items;
-  const int T = blockDim.x, lane = threadIdx.x & 31;
-  const int64_t cap = P.cap;
-  float* D = P.dst;
-  const int32_t kInactive = (int32_t)P.K, kDead = (int32_t)P.K + 1;
-  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
-    const int4 item = P.items[it];
-    const int cnt = item.z - item.y;
-    const int total = (cnt + 31) & ~31;
-    const bool frozen = item.x < P.K && P.steps && P.steps[P.block_scene[item.x]] == 0;
-    if (item.x >= P.K || frozen) {  // inactive bucket or frozen scene: keys only (uniform branch)
-      for (int q = threadIdx.x; q < total; q += T) {
-        const bool valid = q < cnt;
-        const int64_t i = item.y + q;
-        int32_t key = kInactive;
-        if (valid) {
-          const uint32_t info = ld_info(D, cap, i);
-          if (info & INFO_DEAD) key = kDead;
-          else if (info & INFO_ACTIVE) {
-            const SceneDev& Sc = P.scenes[scene_of(P, info)];
-            float x[3];
-            int b[3];
-            for (int d = 0; d < 3; ++d) x[d] = D[(int64_t)(PF_POS + d) * cap + i];
-            if (stencil_origin(Sc, x, b)) key = (int32_t)block_of(Sc, b[0], b[1], b[2]);
-          }
-        }
-        add_rank(P, valid, key, i, lane);
-      }
-      continue;
-    }
-    const SceneDev& S = P.scenes[P.block_scene[item.x]];
-    int org[3];
-    block_origin(S, item.x, org);
-    // positions are software-pipelined one particle ahead; the first load overlaps the staging
-    float xn[3] = {0.f, 0.f, 0.f};
-    if ((int)threadIdx.x < cnt) {
-#pragma unroll
-      for (int d = 0; d < 3; ++d) xn[d] = D[(int64_t)(PF_POS + d) * cap + item.y + threadIdx.x];
-    }
-    for (int t = threadIdx.x; t < TILE_NODES; t += T) {
-      const int gx = org[0] + t / (TILE * TILE), gy = org[1] + (t / TILE) % TILE, gz = org[2] + t % TILE;
-      float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (gx < S.res[0] && gy < S.res[1] && gz < S.res[2]) {
-        g = P.grid[node_addr(S, gx, gy, gz)];
-        if (P.fuse_grid) g = grid_velocity(S, g, gx, gy, gz);
-      }
-      s_v[t] = g;
-    }
-    __syncthreads();
-    for (int q = threadIdx.x; q < total; q += T) {
-      const bool valid = q < cnt;
-      const int64_t i = item.y + q;
-      int32_t key = kInactive;
-      float x[3] = {xn[0], xn[1], xn[2]};
-      if (q + T < cnt) {
-#pragma unroll
-        for (int d = 0; d < 3; ++d) xn[d] = D[(int64_t)(PF_POS + d) * cap + i + T];
-      }
-      if (valid) {
-        int tb[3];
-        const int cell = local_cell(S, x, org, tb);
-        if (cell < BLK_NODES) {
-          float fx[3], w[3][3];
-#pragma unroll
-          for (int d = 0; d < 3; ++d) {
-            const float t = __fmul_rn(x[d], S.inv_dx);
-            fx[d] = t - (float)(tb[d] + S.offset[d] + org[d]);
-            bspline_w(fx[d], w[d]);
-          }
-          // v = sum w v_i;  C = 4 inv_dx sum w v_i (o - fx)^T = 4 inv_dx (M - v fx^T), M = sum w v_i o^T,
-          // accumulated along the separable stencil (z innermost)
-          float v[3] = {0.f, 0.f, 0.f}, M[9];
-#pragma unroll
-          for (int k = 0; k < 9; ++k) M[k] = 0.f;
-#pragma unroll
-          for (int ox = 0; ox < 3; ++ox)
-#pragma unroll
-            for (int oy = 0; oy < 3; ++oy) {
-              float a[3] = {0.f, 0.f, 0.f}, bz[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-              for (int oz = 0; oz < 3; ++oz) {
-                const float4 g = s_v[((tb[0] + ox) * TILE + (tb[1] + oy)) * TILE + (tb[2] + oz)];
-                const float wz = w[2][oz];
-                a[0] += wz * g.x;
-                a[1] += wz * g.y;
-                a[2] += wz * g.z;
-                if (oz > 0) {
-                  const float wo = wz * (float)oz;
-                  bz[0] += wo * g.x;
-                  bz[1] += wo * g.y;
-                  bz[2] += wo * g.z;
-                }
-              }
-              const float wxy = w[0][ox] * w[1][oy];
-#pragma unroll
-              for (int r = 0; r < 3; ++r) {
-                const float t = wxy * a[r];
-                v[r] += t;
-                M[r * 3 + 0] += (float)ox * t;
-                M[r * 3 + 1] += (float)oy * t;
-                M[r * 3 + 2] += wxy * bz[r];
-              }
-            }
-          float Cn[9];
-#pragma unroll
-          for (int r = 0; r < 3; ++r)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) Cn[r * 3 + c] = 4.f * S.inv_dx * (M[r * 3 + c] - v[r] * fx[c]);
-          float xn[3];
-          bool finite = true;
-#pragma unroll
-          for (int d = 0; d < 3; ++d) {
-            xn[d] = x[d] + S.dt * v[d];
-            finite = finite && isfinite(xn[d]) && isfinite(v[d]);
-          }
-          // CubeBoundary.impose_pos_vel (boundaries.py:22-32)
-#pragma unroll
-          for (int d = 0; d < 3; ++d) {
-            if (xn[d] >= S.hi[d] && v[d] >= 0.f) v[d] *= -S.restitution;
-            else if (xn[d] <= S.lo[d] && v[d] <= 0.f) v[d] *= -S.restitution;
-            xn[d] = fmaxf(fminf(xn[d], S.hi[d]), S.lo[d]);
-          }
-#pragma unroll
-          for (int d = 0; d < 3; ++d) {
-            D[(int64_t)(PF_POS + d) * cap + i] = xn[d];
-            D[(int64_t)(PF_VEL + d) * cap + i] = v[d];
-          }
-#pragma unroll
-          for (int k = 0; k < 9; ++k) D[(int64_t)(PF_C + k) * cap + i] = Cn[k];
-          int b[3];
-          if (!finite) atomicOr(P.status, 1u);
-          else if (stencil_origin(S, xn, b)) key = (int32_t)block_of(S, b[0], b[1], b[2]);
-          else atomicOr(P.status, 2u);
-        } else {
-          atomicOr(P.status, 2u);
-        }
-      }
-      add_rank(P, valid, key, i, lane);
-    }
-    __syncthreads();
-  }
-}
-
 // ------------------------------------------------------------------ kinematic colliders
 namespace {
 __device__ __forceinline__ void rot(const float* q, const float* v, float* o) {  // gu.qd_transform_by_quat
@@ -1071,8 +561,41 @@ __device__ __forceinline__ float collider_sdf(const ColliderDev& c, const float*
   return sd;
 }
 
-// _func_collide_with_rigid_geom + _func_collide_in_rigid_geom (legacy_coupler.py:166-218, 284-347)
-// for every collider of the node's scene; reaction force and torque go to collider_acc.
+// _func_collide_in_rigid_geom (legacy_coupler.py:284-347): velocity v of mass m at x, relative to
+// collider ci, loses its inward normal part (restitution) and tangential speed (friction), blended
+// by `influence`; the reaction force and torque go to collider_acc.
+__device__ void collide_in(const KParams& P, const SceneDev& S, int ci, const float* x, float* v, float m,
+                           const float* n, float influence) {
+  const ColliderDev& c = P.colliders[ci];
+  const float r[3] = {x[0] - c.com[0], x[1] - c.com[1], x[2] - c.com[2]};
+  const float vr[3] = {c.ang[1] * r[2] - c.ang[2] * r[1] + c.lin[0], c.ang[2] * r[0] - c.ang[0] * r[2] + c.lin[1],
+                       c.ang[0] * r[1] - c.ang[1] * r[0] + c.lin[2]};
+  const float rv[3] = {v[0] - vr[0], v[1] - vr[1], v[2] - vr[2]};
+  const float rvn = rv[0] * n[0] + rv[1] * n[1] + rv[2] * n[2];
+  if (!(rvn < 0.f)) return;
+  float rt[3];
+  for (int k = 0; k < 3; ++k) rt[k] = rv[k] - rvn * n[k];
+  const float rtn = sqrtf(rt[0] * rt[0] + rt[1] * rt[1] + rt[2] * rt[2] + S.eps);  // norm(gs.EPS)
+  const float scale = fmaxf(0.f, rtn + rvn * c.friction) / rtn;
+  float dv[3];
+  for (int k = 0; k < 3; ++k) {
+    const float nv = vr[k] + (rt[k] * scale - n[k] * rvn * c.restitution) * influence + rv[k] * (1.f - influence);
+    dv[k] = nv - v[k];
+    v[k] = nv;
+  }
+  // particle -> rigid: force = -m dv / dt at x, torque (x - com) x force
+  const float f[3] = {-m * dv[0] / S.dt, -m * dv[1] / S.dt, -m * dv[2] / S.dt};
+  double* acc = P.collider_acc + (int64_t)ci * 6;
+  atomicAdd(acc + 0, (double)f[0]);
+  atomicAdd(acc + 1, (double)f[1]);
+  atomicAdd(acc + 2, (double)f[2]);
+  atomicAdd(acc + 3, (double)(r[1] * f[2] - r[2] * f[1]));
+  atomicAdd(acc + 4, (double)(r[2] * f[0] - r[0] * f[2]));
+  atomicAdd(acc + 5, (double)(r[0] * f[1] - r[1] * f[0]));
+}
+
+// _func_collide_with_rigid (legacy_coupler.py:134-218): every collider of the node's scene whose
+// SDF influence exceeds 0.1 at x, in order.
 __device__ void collide_node(const KParams& P, const SceneDev& S, int32_t scene, const float* x, float* v, float m) {
   for (int ci = 0; ci < P.n_colliders; ++ci) {
     const ColliderDev& c = P.colliders[ci];
@@ -1081,34 +604,633 @@ __device__ void collide_node(const KParams& P, const SceneDev& S, int32_t scene,
     const float sd = collider_sdf(c, x, S.eps, n);
     const float influence = fminf(expf(-sd / fmaxf(1e-10f, c.softness)), 1.f);
     if (!(influence > 0.1f)) continue;
-    const float r[3] = {x[0] - c.com[0], x[1] - c.com[1], x[2] - c.com[2]};
-    const float vr[3] = {c.ang[1] * r[2] - c.ang[2] * r[1] + c.lin[0], c.ang[2] * r[0] - c.ang[0] * r[2] + c.lin[1],
-                         c.ang[0] * r[1] - c.ang[1] * r[0] + c.lin[2]};
-    const float rv[3] = {v[0] - vr[0], v[1] - vr[1], v[2] - vr[2]};
-    const float rvn = rv[0] * n[0] + rv[1] * n[1] + rv[2] * n[2];
-    if (!(rvn < 0.f)) continue;
-    float rt[3];
-    for (int k = 0; k < 3; ++k) rt[k] = rv[k] - rvn * n[k];
-    const float rtn = sqrtf(rt[0] * rt[0] + rt[1] * rt[1] + rt[2] * rt[2] + S.eps);  // norm(gs.EPS)
-    const float scale = fmaxf(0.f, rtn + rvn * c.friction) / rtn;
-    float dv[3];
-    for (int k = 0; k < 3; ++k) {
-      const float nv = vr[k] + (rt[k] * scale - n[k] * rvn * c.restitution) * influence + rv[k] * (1.f - influence);
-      dv[k] = nv - v[k];
-      v[k] = nv;
-    }
-    // particle -> rigid: force = -m dv / dt at x, torque (x - com) x force
-    const float f[3] = {-m * dv[0] / S.dt, -m * dv[1] / S.dt, -m * dv[2] / S.dt};
-    double* acc = P.collider_acc + (int64_t)ci * 6;
-    atomicAdd(acc + 0, (double)f[0]);
-    atomicAdd(acc + 1, (double)f[1]);
-    atomicAdd(acc + 2, (double)f[2]);
-    atomicAdd(acc + 3, (double)(r[1] * f[2] - r[2] * f[1]));
-    atomicAdd(acc + 4, (double)(r[2] * f[0] - r[0] * f[2]));
-    atomicAdd(acc + 5, (double)(r[0] * f[1] - r[1] * f[0]));
+    collide_in(P, S, ci, x, v, m, n, influence);
   }
 }
+
+// CPIC (MPMOptions.enable_CPIC) for thin colliders.  Particle side, mpm_surface_to_particle
+// (legacy_coupler.py:513-529): per collider the particle keeps the SDF normal at its position
+// unless that normal turned against the stored one, so the stored normal remembers the side the
+// particle is on; the normals ride with the particle in planes PF_CPIC + 3 * collider.  Node
+// side (mpm_solver.py:389-411): a stencil node lies behind collider ci when the collider's
+// normal at the node points against the particle's; the first such collider, in order, counts.
+__device__ __forceinline__ bool collider_in_scene(const ColliderDev& c, int32_t scene) {
+  return c.scene < 0 || c.scene == scene;
+}
+
+__device__ int cpic_separating(const KParams& P, const SceneDev& S, int32_t scene, const float* D, int64_t i,
+                               const float* xc) {
+  const int64_t cap = P.cap;
+  const int nc = P.n_colliders < P.cpic_slots ? P.n_colliders : P.cpic_slots;
+  for (int ci = 0; ci < nc; ++ci) {
+    const ColliderDev& c = P.colliders[ci];
+    if (!collider_in_scene(c, scene)) continue;
+    float n[3];
+    collider_sdf(c, xc, S.eps, n);
+    const float* pn = D + (int64_t)(PF_CPIC + 3 * ci) * cap + i;
+    if (pn[0] * n[0] + pn[cap] * n[1] + pn[2 * cap] * n[2] < 0.f) return ci;
+  }
+  return -1;
+}
+
+// World position of stencil node o (= ox*9 + oy*3 + oz) of a particle in local cell tb of the
+// block with node origin org: (base + offset) * dx as the reference computes it.
+__device__ __forceinline__ void cpic_node_pos(const SceneDev& S, const int* org, const int* tb, int o, float* xc) {
+  const int oo[3] = {o / 9, (o / 3) % 3, o % 3};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) xc[d] = (float)(org[d] + tb[d] + oo[d] + S.offset[d]) * S.dx;
+}
+
+// P2G side: moves the particle's normals from its old slot (src) to its new one (dst), updating
+// them when it is active, and returns the mask of its stencil nodes behind a collider
+// (bit ox*9 + oy*3 + oz); 0 when inactive or outside the block.
+__device__ __noinline__ uint32_t cpic_p2g(const KParams& P, const SceneDev& S, int32_t scene, const float* x,
+                                          bool active, int64_t si, int64_t slot, const int* org, int cell) {
+  const int64_t cap = P.cap;
+  for (int ci = 0; ci < P.cpic_slots; ++ci) {
+    float pn[3];
+    for (int d = 0; d < 3; ++d) pn[d] = P.src[(int64_t)(PF_CPIC + 3 * ci + d) * cap + si];
+    if (active && ci < P.n_colliders && collider_in_scene(P.colliders[ci], scene)) {
+      float n[3];
+      collider_sdf(P.colliders[ci], x, S.eps, n);
+      if (n[0] * pn[0] + n[1] * pn[1] + n[2] * pn[2] >= 0.f)
+        for (int d = 0; d < 3; ++d) pn[d] = n[d];
+    }
+    for (int d = 0; d < 3; ++d) P.dst[(int64_t)(PF_CPIC + 3 * ci + d) * cap + slot] = pn[d];
+  }
+  if (!active || cell >= BLK_NODES) return 0u;
+  const int tb[3] = {cell >> 4, (cell >> 2) & 3, cell & 3};
+  uint32_t mask = 0u;
+  for (int o = 0; o < 27; ++o) {
+    float xc[3];
+    cpic_node_pos(S, org, tb, o, xc);
+    if (cpic_separating(P, S, scene, P.dst, slot, xc) >= 0) mask |= 1u << o;
+  }
+  return mask;
+}
+
+// G2P side (mpm_solver.py:445-459): a node behind collider ci contributes, instead of its grid
+// velocity, the particle's own velocity collided with ci (_func_collide_in_rigid_geom with the
+// particle's stored normal, influence 1 and mass m_p w / 1e3), the reaction going to ci.
+__device__ __noinline__ float4 cpic_g2p_node(const KParams& P, const SceneDev& S, int32_t scene, const float* D,
+                                             int64_t i, const float* x, const int* org, const int* tb, int o,
+                                             float weight, float4 g) {
+  const int64_t cap = P.cap;
+  float xc[3];
+  cpic_node_pos(S, org, tb, o, xc);
+  const int ci = cpic_separating(P, S, scene, D, i, xc);
+  if (ci < 0) return g;
+  float v[3], pn[3];
+  for (int d = 0; d < 3; ++d) {
+    v[d] = D[(int64_t)(PF_VEL + d) * cap + i];
+    pn[d] = D[(int64_t)(PF_CPIC + 3 * ci + d) * cap + i];
+  }
+  const float m = P.mats[ld_info(D, cap, i) & INFO_MAT_MASK].mass * weight / 1e3f;
+  collide_in(P, S, ci, x, v, m, pn, 1.f);
+  return make_float4(v[0], v[1], v[2], g.w);
+}
 }  // namespace
+
+// ------------------------------------------------------------------ P2G
+namespace {
+
+// Loads one particle from the old order (planes of `S`, index si).
+struct Particle {
+  float x[3], v[3], C[9], F[9], Jp, pid, actu, mdir[3];
+  uint32_t info;
+};
+
+__device__ __forceinline__ void load_particle(const KParams& P, const float* Sx, int64_t si, Particle& q) {
+  const int64_t cap = P.cap;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    q.x[d] = Sx[(int64_t)(PF_POS + d) * cap + si];
+    q.v[d] = Sx[(int64_t)(PF_VEL + d) * cap + si];
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    q.C[k] = Sx[(int64_t)(PF_C + k) * cap + si];
+    q.F[k] = Sx[(int64_t)(PF_F + k) * cap + si];
+  }
+  q.Jp = Sx[(int64_t)PF_JP * cap + si];
+  q.info = __float_as_uint(Sx[(int64_t)PF_INFO * cap + si]);
+  q.pid = Sx[(int64_t)PF_PID * cap + si];
+  q.actu = 0.f;
+  q.mdir[0] = 0.f, q.mdir[1] = 0.f, q.mdir[2] = 1.f;
+  if (P.nf > NF_BASE) {
+    q.actu = Sx[(int64_t)PF_ACTU * cap + si];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) q.mdir[d] = Sx[(int64_t)(PF_MDIR + d) * cap + si];
+  }
+}
+
+// Writes a particle to its sorted slot.  Velocity and C are left out: G2P of the same substep
+// overwrites both for every particle of an active bucket before anything reads them.
+__device__ __forceinline__ void store_particle(const KParams& P, float* Dx, int64_t slot, const Particle& q) {
+  const int64_t cap = P.cap;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) Dx[(int64_t)(PF_POS + d) * cap + slot] = q.x[d];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) Dx[(int64_t)(PF_F + k) * cap + slot] = q.F[k];
+  Dx[(int64_t)PF_JP * cap + slot] = q.Jp;
+  Dx[(int64_t)PF_INFO * cap + slot] = __uint_as_float(q.info);
+  Dx[(int64_t)PF_PID * cap + slot] = q.pid;
+  if (P.nf > NF_BASE) {
+    Dx[(int64_t)PF_ACTU * cap + slot] = q.actu;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) Dx[(int64_t)(PF_MDIR + d) * cap + slot] = q.mdir[d];
+  }
+}
+
+// Local cell (0..63) of a particle inside the block whose node origin is `org`, or 64.
+__device__ __forceinline__ int local_cell(const SceneDev& S, const float* x, const int* org, int* tb) {
+  bool inside = true;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float t = __fmul_rn(x[d], S.inv_dx);
+    const float f = floorf(__fsub_rn(t, 0.5f));
+    const int b = (f > -1e9f && f < 1e9f) ? (int)f : -1000000;
+    tb[d] = b - S.offset[d] - org[d];
+    inside = inside && tb[d] >= 0 && tb[d] < BLK;
+  }
+  return inside ? (tb[0] * BLK + tb[1]) * BLK + tb[2] : BLK_NODES;
+}
+
+__device__ __forceinline__ void block_origin(const SceneDev& S, int64_t key, int* org) {
+  const int64_t lb = key - S.block_base;
+  org[2] = (int)(lb % S.bres[2]) * BLK;
+  org[1] = (int)((lb / S.bres[2]) % S.bres[1]) * BLK;
+  org[0] = (int)(lb / ((int64_t)S.bres[2] * S.bres[1])) * BLK;
+}
+
+}  // namespace
+
+// Per work item (one grid block's bucket, up to `chunk` <= P2G_MAX_CHUNK particles):
+//  1. counting-sort the item's particles by cell in shared memory (native integer atomics);
+//  2. in slot order (coalesced gathers through perm): compute_F_tmp + svd + material update
+//     + stress (mpm_solver.py:293-307, 339-377), write the particle to its slot, and leave its
+//     scatter parameters (fx, mass, q = m v - sum_k a_k fx_k, a_k = dx * affine[:,k]) in a
+//     shared record at its cell-sorted position;
+//  3. one thread per (cell, ox) walks its cell's records and sums the APIC mass/momentum
+//     w_o (q + sum_k o_k a_k), w_o m (mpm_solver.py:379-418) of the 9 nodes (ox, *, *) in
+//     registers, then adds them to its warp's private 6^3 shared tile (plain float4
+//     read-modify-writes; no two lanes of a warp share a node): one tile update per cell and
+//     node instead of one per particle and node;
+//  4. sum the warp tiles and flush with one 16-byte vector reduction per node.
+// With CPIC the nodes behind a thin collider get nothing from the particle (weight 0 in step 3).
+template <bool CPIC>
+__device__ __forceinline__ void p2g_body(const KParams& P) {
+  extern __shared__ __align__(16) unsigned char p2g_smem[];
+  __shared__ int s_cnt[BLK_NODES + 1];
+  __shared__ int s_touch[8];
+  const int n_items = *P.n_items;
+  const int T = blockDim.x, nw = T >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float4* s_tile = reinterpret_cast<float4*>(p2g_smem);
+  float4* s_rec = s_tile + nw * TILE_NODES;
+  uint32_t* s_cr = reinterpret_cast<uint32_t*>(s_rec + P2G_REC * P.chunk);
+  const int64_t cap = P.cap;
+  const float* Sx = P.src;
+  float* Dx = P.dst;
+  float4* my_tile = s_tile + warp * TILE_NODES;
+  // tiles, cell counts and touch flags start zeroed; each item leaves them zeroed again
+  for (int t = threadIdx.x; t < nw * TILE_NODES; t += T) s_tile[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (threadIdx.x <= BLK_NODES) s_cnt[threadIdx.x] = 0;
+  if (threadIdx.x < 8) s_touch[threadIdx.x] = 0;
+  __syncthreads();
+  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const int4 item = P.items[it];
+    const int cnt = item.z - item.y;
+    const bool frozen = item.x < P.K && P.steps && P.steps[P.block_scene[item.x]] == 0;
+    if (item.x >= P.K || frozen) {  // inactive bucket or frozen scene: carry over unchanged (uniform)
+      for (int j = threadIdx.x; j < cnt; j += T) {
+        const int64_t si = P.perm[item.y + j];
+        for (int k = 0; k < P.nf; ++k) Dx[(int64_t)k * cap + item.y + j] = Sx[(int64_t)k * cap + si];
+      }
+      continue;
+    }
+    const int32_t sid = P.block_scene[item.x];
+    const SceneDev& S = P.scenes[sid];
+    int org[3];
+    block_origin(S, item.x, org);
+    // 1. cell ranks
+    for (int j = threadIdx.x; j < cnt; j += T) {
+      const int64_t si = P.perm[item.y + j];
+      float x[3];
+      int tb[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) x[d] = Sx[(int64_t)(PF_POS + d) * cap + si];
+      const int cell = local_cell(S, x, org, tb);
+      const int r = atomicAdd(&s_cnt[cell], 1);
+      s_cr[j] = ((uint32_t)cell << 16) | (uint32_t)r;
+    }
+    __syncthreads();
+    // every warp scans the 64 cell counts into registers: lane l holds the start of cells l and
+    // l + 32 (no extra barrier; starts are fetched by shuffles, a cell ends where the next starts)
+    int offA, offB, tot_in;
+    {
+      const int a = s_cnt[lane], b = s_cnt[lane + 32];
+      int ia = a, ib = b;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int ta = __shfl_up_sync(0xffffffffu, ia, o), tbv = __shfl_up_sync(0xffffffffu, ib, o);
+        if (lane >= o) {
+          ia += ta;
+          ib += tbv;
+        }
+      }
+      const int tot_a = __shfl_sync(0xffffffffu, ia, 31);
+      offA = ia - a;
+      offB = tot_a + ib - b;
+      tot_in = __shfl_sync(0xffffffffu, tot_a + ib, 31);  // start of the particles outside the block's cells
+    }
+    // 2. material + stress in slot order; scatter parameters to the sorted record (lanes of a warp
+    //    iterate together so the offset shuffles see the whole warp)
+    for (int jb = threadIdx.x - lane; jb < cnt; jb += T) {
+      const int j = jb + lane;
+      const uint32_t cr = j < cnt ? s_cr[j] : 0u;
+      const int cell = (int)(cr >> 16);
+      const int oa = __shfl_sync(0xffffffffu, offA, cell & 31), ob = __shfl_sync(0xffffffffu, offB, cell & 31);
+      if (j >= cnt) continue;
+      const int p = (cell < 32 ? oa : (cell < BLK_NODES ? ob : tot_in)) + (int)(cr & 0xffffu);
+      const int64_t slot = item.y + j;
+      const int64_t si = P.perm[slot];
+      Particle pt;
+      load_particle(P, Sx, si, pt);
+      bool scattered = false;
+      uint32_t cmask = 0u;
+      if constexpr (CPIC) {
+        cmask = cpic_p2g(P, S, sid, pt.x, (pt.info & INFO_ACTIVE) != 0, si, slot, org, cell);
+        P.cpic_mask[slot] = cmask;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) Dx[(int64_t)(PF_VEL + d) * cap + slot] = pt.v[d];  // G2P collides it
+      }
+      if (pt.info & INFO_ACTIVE) {
+        const MaterialDev& M = P.mats[pt.info & INFO_MAT_MASK];
+        // F_tmp = (I + dt C) F   (compute_F_tmp, mpm_solver.py:293-299)
+        float A[9], Ft[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) A[k] = ((k % 4 == 0) ? 1.f : 0.f) + S.dt * pt.C[k];
+        mat_mul(A, pt.F, Ft);
+        float Pk[9], Jpn = pt.Jp;
+        if (M.type == MT_LIQUID && M.mu == 0.f) {
+          // Non-viscous liquid (liquid.py:36-49 with mu = 0) uses only J = sigma0 sigma1 sigma2 of the
+          // SVD, which equals det F_tmp (det U = det V = 1): F_new = J^(1/3) I, stress = lam J (J-1) I.
+          const float J = Ft[0] * (Ft[4] * Ft[8] - Ft[5] * Ft[7]) - Ft[1] * (Ft[3] * Ft[8] - Ft[5] * Ft[6]) +
+                          Ft[2] * (Ft[3] * Ft[7] - Ft[4] * Ft[6]);
+          const float j3 = powf(J, 1.f / 3.f);
+          const float pr = M.lam * J * (J - 1.f);
+#pragma unroll
+          for (int k = 0; k < 9; ++k) {
+            pt.F[k] = (k % 4 == 0) ? j3 : 0.f;
+            Pk[k] = (k % 4 == 0) ? pr : 0.f;
+          }
+        } else {
+          float U[9], sig[3], V[9];
+          const float res = svd3<float, SVD_SWEEPS>(Ft, U, sig, V);
+          if (!(res <= SVD_FP64_TOL)) {
+            svd3_fp64(Ft, U, sig, V);
+            atomicAdd(P.fp64_count, 1ull);
+          }
+          material_update<float>(M, Ft, U, sig, V, pt.Jp, pt.actu, pt.mdir, P.eps_norm, pt.F, Jpn, Pk);
+        }
+        pt.Jp = Jpn;
+        if (cell < BLK_NODES) {
+          const int tb0 = cell >> 4, tb1 = (cell >> 2) & 3, tb2 = cell & 3;
+          const float mass = M.mass;
+          float fx[3];
+          const int tbv[3] = {tb0, tb1, tb2};
+#pragma unroll
+          for (int d = 0; d < 3; ++d) fx[d] = __fmul_rn(pt.x[d], S.inv_dx) - (float)(tbv[d] + S.offset[d] + org[d]);
+          float a[9];  // a[k*3 + r] = dx * affine[r][k]
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) a[k * 3 + r] = S.dx * (S.stress_scale * Pk[r * 3 + k] + mass * pt.C[r * 3 + k]);
+          float qv[3];
+#pragma unroll
+          for (int r = 0; r < 3; ++r) qv[r] = mass * pt.v[r] - (a[r] * fx[0] + a[3 + r] * fx[1] + a[6 + r] * fx[2]);
+          float4* rec = s_rec + P2G_REC * p;
+          rec[0] = make_float4(fx[0], fx[1], fx[2], mass);
+          rec[1] = make_float4(qv[0], qv[1], qv[2], a[0]);
+          rec[2] = make_float4(a[1], a[2], a[3], a[4]);
+          rec[3] = make_float4(a[5], a[6], a[7], a[8]);
+          if constexpr (CPIC) rec[4] = make_float4(__uint_as_float(cmask), 0.f, 0.f, 0.f);
+          scattered = true;
+          if (!(pt.info & INFO_FREE) && P.pin) {  // its 27 nodes lose all momentum (mpm_solver.py:420-421)
+            for (int o = 0; o < 27; ++o) {
+              const int64_t ad = node_addr(S, org[0] + tb0 + o / 9, org[1] + tb1 + (o / 3) % 3, org[2] + tb2 + o % 3);
+              atomicOr(&P.pin[ad >> 5], 1u << (ad & 31));
+            }
+          }
+        } else {
+          atomicOr(P.status, 2u);  // cannot happen for a correctly keyed particle; never touches memory
+        }
+      }
+      if (!scattered && cell < BLK_NODES) {  // holds a place in its cell's run: contributes nothing
+        float4* rec = s_rec + P2G_REC * p;
+        rec[0] = make_float4(0.5f, 0.5f, 0.5f, 0.f);
+        rec[1] = rec[2] = rec[3] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if constexpr (CPIC) rec[4] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      store_particle(P, Dx, slot, pt);
+    }
+    __syncthreads();
+    // 3. cell-major scatter: unit u = (cell, ox) sums the 9 nodes (ox, *, *) of the stencils of
+    //    all particles of its cell in registers and adds them to the warp tile once.  A warp's
+    //    32 units span fewer than 16 consecutive cells, so no two of its lanes share a node.
+    for (int u0 = 0; u0 < 3 * BLK_NODES; u0 += T) {
+      const int u = u0 + threadIdx.x;
+      const bool has = u < 3 * BLK_NODES;
+      const int cell = has ? u / 3 : 0, ox = has ? u - 3 * (u / 3) : 0;
+      const int nx = (cell + 1) & 31;
+      const int oa = __shfl_sync(0xffffffffu, offA, cell & 31), ob = __shfl_sync(0xffffffffu, offB, cell & 31);
+      const int na = __shfl_sync(0xffffffffu, offA, nx), nb = __shfl_sync(0xffffffffu, offB, nx);
+      const int beg = cell < 32 ? oa : ob;
+      const int end = cell + 1 < 32 ? na : (cell + 1 < BLK_NODES ? nb : tot_in);
+      const int len = has ? end - beg : 0;
+      const int nmax = __reduce_max_sync(0xffffffffu, len);
+      if (nmax == 0) continue;  // warp-uniform
+      float4 acc[3][3];
+#pragma unroll
+      for (int oy = 0; oy < 3; ++oy)
+#pragma unroll
+        for (int oz = 0; oz < 3; ++oz) acc[oy][oz] = make_float4(0.f, 0.f, 0.f, 0.f);
+      const float fo = (float)ox;
+      for (int j = 0; j < nmax; ++j) {
+        if (j < len) {
+          const float4* rec = s_rec + P2G_REC * (beg + j);
+          const float4 r0 = rec[0], r1 = rec[1], r2 = rec[2], r3 = rec[3];
+          uint32_t m9 = 0u;  // CPIC: the record's separated nodes of this ox
+          if constexpr (CPIC) m9 = __float_as_uint(rec[4].x) >> (9 * ox);
+          float wxv[3], wy[3], wz[3];
+          bspline_w(r0.x, wxv);
+          bspline_w(r0.y, wy);
+          bspline_w(r0.z, wz);
+          const float wx = ox == 0 ? wxv[0] : (ox == 1 ? wxv[1] : wxv[2]);
+          // a (k-major, a[k*3 + r]) = r1.w, r2.x, r2.y | r2.z, r2.w, r3.x | r3.y, r3.z, r3.w
+          const float t0x = r1.x + fo * r1.w, t0y = r1.y + fo * r2.x, t0z = r1.z + fo * r2.y;
+#pragma unroll
+          for (int oy = 0; oy < 3; ++oy) {
+            const float t1x = t0x + (float)oy * r2.z, t1y = t0y + (float)oy * r2.w, t1z = t0z + (float)oy * r3.x;
+            const float w01 = wx * wy[oy];
+#pragma unroll
+            for (int oz = 0; oz < 3; ++oz) {
+              float wt = w01 * wz[oz];
+              if constexpr (CPIC) {
+                if ((m9 >> (oy * 3 + oz)) & 1u) wt = 0.f;
+              }
+              acc[oy][oz].x += wt * (t1x + (float)oz * r3.y);
+              acc[oy][oz].y += wt * (t1y + (float)oz * r3.z);
+              acc[oy][oz].z += wt * (t1z + (float)oz * r3.w);
+              acc[oy][oz].w += wt * r0.w;
+            }
+          }
+        }
+      }
+      // Lanes of neighbouring cells reach the same node at different (oy, oz) steps: a
+      // __syncwarp between steps orders those read-modify-writes.
+      const int tb0 = cell >> 4, tb1 = (cell >> 2) & 3, tb2 = cell & 3;
+#pragma unroll
+      for (int oy = 0; oy < 3; ++oy)
+#pragma unroll
+        for (int oz = 0; oz < 3; ++oz) {
+          if (len > 0) {
+            float4* g = my_tile + ((tb0 + ox) * TILE + (tb1 + oy)) * TILE + (tb2 + oz);
+            float4 h = *g;
+            h.x += acc[oy][oz].x;
+            h.y += acc[oy][oz].y;
+            h.z += acc[oy][oz].z;
+            h.w += acc[oy][oz].w;
+            *g = h;
+          }
+          __syncwarp();
+        }
+    }
+    __syncthreads();
+    // 4. flush
+    if (threadIdx.x <= BLK_NODES) s_cnt[threadIdx.x] = 0;  // every warp's scan read it before phase 2 ended
+    for (int t = threadIdx.x; t < TILE_NODES; t += T) {
+      float4 g = s_tile[t];
+      s_tile[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int ww = 1; ww < nw; ++ww) {
+        const float4 h = s_tile[ww * TILE_NODES + t];
+        s_tile[ww * TILE_NODES + t] = make_float4(0.f, 0.f, 0.f, 0.f);
+        g.x += h.x;
+        g.y += h.y;
+        g.z += h.z;
+        g.w += h.w;
+      }
+      if (g.w == 0.f) continue;
+      const int tx = t / (TILE * TILE), ty = (t / TILE) % TILE, tz = t % TILE;
+      const int gx = org[0] + tx, gy = org[1] + ty, gz = org[2] + tz;
+      if (gx >= S.res[0] || gy >= S.res[1] || gz >= S.res[2]) continue;
+      atomicAdd(reinterpret_cast<float4*>(&P.grid[node_addr(S, gx, gy, gz)]), g);
+      s_touch[(tx >> 2) * 4 + (ty >> 2) * 2 + (tz >> 2)] = 1;
+    }
+    __syncthreads();
+    if (threadIdx.x < 8 && s_touch[threadIdx.x]) {
+      s_touch[threadIdx.x] = 0;
+      const int bx = org[0] / BLK + (threadIdx.x >> 2), by = org[1] / BLK + ((threadIdx.x >> 1) & 1),
+                bz = org[2] / BLK + (threadIdx.x & 1);
+      if (bx < S.bres[0] && by < S.bres[1] && bz < S.bres[2]) {
+        const int64_t blk = S.block_base + ((int64_t)bx * S.bres[1] + by) * S.bres[2] + bz;
+        if (atomicExch(&P.flags[blk], 1) == 0) P.list[atomicAdd(P.nlist, 1)] = (int32_t)blk;
+      }
+    }
+  }
+}
+
+// Capped at 96 registers: five 128-thread CTAs per SM instead of four at 128 registers, which
+// measured 5% faster despite a small spill.
+__global__ void __maxnreg__(96) k_p2g(KParams P) { p2g_body<false>(P); }
+__global__ void __launch_bounds__(P2G_MAX_THREADS) k_p2g_cpic(KParams P) { p2g_body<true>(P); }
+
+// ------------------------------------------------------------------ G2P
+// mpm_solver.py:423-481 (g2p) with the particle boundary of boundaries.py:22-32, over the
+// same work items as the P2G that wrote the particles (so every item's particles read one
+// 6^3 node tile, staged once in shared memory), followed by the bucket key of the new
+// position and a warp-aggregated rank within the bucket.
+__device__ __forceinline__ void add_rank(const KParams& P, bool valid, int32_t key, int64_t i, int lane) {
+  const unsigned am = __ballot_sync(0xffffffffu, valid);
+  if (valid) {
+    const unsigned peers = __match_any_sync(am, key);
+    const int leader = __ffs(peers) - 1;
+    int r = 0;
+    if (lane == leader) r = atomicAdd(&P.count[key], __popc(peers));
+    r = __shfl_sync(peers, r, leader);
+    r += __popc(peers & ((1u << lane) - 1u));
+    P.key[i] = key;
+    P.rank[i] = r;
+  }
+}
+
+template <bool CPIC>
+__device__ __forceinline__ void g2p_body(const KParams& P) {
+  __shared__ float4 s_v[TILE_NODES];
+  if (P.fuse_grid) {
+    // the grid op's other duty: zero the blocks the previous substep left in the other buffer
+    // (the next P2G adds into it); k_perm resets that list's length after this kernel
+    const int64_t n_other = (int64_t)*P.nlist_other * BLK_NODES;
+    for (int64_t i = grid_stride_begin(); i < n_other; i += grid_stride_step()) {
+      const int32_t blk = P.list_other[i / BLK_NODES];
+      P.grid_other[(int64_t)blk * BLK_NODES + (i % BLK_NODES)] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (i % BLK_NODES == 0) P.flags_other[blk] = 0;
+    }
+  } else if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *P.nlist_other = 0;
+  }
+  const int n_items = *P.n_items;
+  const int T = blockDim.x, lane = threadIdx.x & 31;
+  const int64_t cap = P.cap;
+  float* D = P.dst;
+  const int32_t kInactive = (int32_t)P.K, kDead = (int32_t)P.K + 1;
+  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const int4 item = P.items[it];
+    const int cnt = item.z - item.y;
+    const int total = (cnt + 31) & ~31;
+    const bool frozen = item.x < P.K && P.steps && P.steps[P.block_scene[item.x]] == 0;
+    if (item.x >= P.K || frozen) {  // inactive bucket or frozen scene: keys only (uniform branch)
+      for (int q = threadIdx.x; q < total; q += T) {
+        const bool valid = q < cnt;
+        const int64_t i = item.y + q;
+        int32_t key = kInactive;
+        if (valid) {
+          const uint32_t info = ld_info(D, cap, i);
+          if (info & INFO_DEAD) key = kDead;
+          else if (info & INFO_ACTIVE) {
+            const SceneDev& Sc = P.scenes[scene_of(P, info)];
+            float x[3];
+            int b[3];
+            for (int d = 0; d < 3; ++d) x[d] = D[(int64_t)(PF_POS + d) * cap + i];
+            if (stencil_origin(Sc, x, b)) key = (int32_t)block_of(Sc, b[0], b[1], b[2]);
+          }
+        }
+        add_rank(P, valid, key, i, lane);
+      }
+      continue;
+    }
+    const SceneDev& S = P.scenes[P.block_scene[item.x]];
+    int org[3];
+    block_origin(S, item.x, org);
+    // positions are software-pipelined one particle ahead; the first load overlaps the staging
+    float xn[3] = {0.f, 0.f, 0.f};
+    if ((int)threadIdx.x < cnt) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) xn[d] = D[(int64_t)(PF_POS + d) * cap + item.y + threadIdx.x];
+    }
+    for (int t = threadIdx.x; t < TILE_NODES; t += T) {
+      const int gx = org[0] + t / (TILE * TILE), gy = org[1] + (t / TILE) % TILE, gz = org[2] + t % TILE;
+      float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (gx < S.res[0] && gy < S.res[1] && gz < S.res[2]) {
+        g = P.grid[node_addr(S, gx, gy, gz)];
+        if (P.fuse_grid) g = grid_velocity(S, g, gx, gy, gz);
+      }
+      s_v[t] = g;
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < total; q += T) {
+      const bool valid = q < cnt;
+      const int64_t i = item.y + q;
+      int32_t key = kInactive;
+      float x[3] = {xn[0], xn[1], xn[2]};
+      if (q + T < cnt) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) xn[d] = D[(int64_t)(PF_POS + d) * cap + i + T];
+      }
+      if (valid) {
+        int tb[3];
+        const int cell = local_cell(S, x, org, tb);
+        if (cell < BLK_NODES) {
+          float fx[3], w[3][3];
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            const float t = __fmul_rn(x[d], S.inv_dx);
+            fx[d] = t - (float)(tb[d] + S.offset[d] + org[d]);
+            bspline_w(fx[d], w[d]);
+          }
+          // v = sum w v_i;  C = 4 inv_dx sum w v_i (o - fx)^T = 4 inv_dx (M - v fx^T), M = sum w v_i o^T,
+          // accumulated along the separable stencil (z innermost)
+          uint32_t cm = 0u;  // CPIC: nodes behind a collider, from this substep's P2G
+          if constexpr (CPIC) cm = P.cpic_mask[i];
+          float v[3] = {0.f, 0.f, 0.f}, M[9];
+#pragma unroll
+          for (int k = 0; k < 9; ++k) M[k] = 0.f;
+#pragma unroll
+          for (int ox = 0; ox < 3; ++ox)
+#pragma unroll
+            for (int oy = 0; oy < 3; ++oy) {
+              float a[3] = {0.f, 0.f, 0.f}, bz[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+              for (int oz = 0; oz < 3; ++oz) {
+                float4 g = s_v[((tb[0] + ox) * TILE + (tb[1] + oy)) * TILE + (tb[2] + oz)];
+                if constexpr (CPIC) {
+                  if ((cm >> (ox * 9 + oy * 3 + oz)) & 1u)
+                    g = cpic_g2p_node(P, S, P.block_scene[item.x], D, i, x, org, tb, ox * 9 + oy * 3 + oz,
+                                      w[0][ox] * w[1][oy] * w[2][oz], g);
+                }
+                const float wz = w[2][oz];
+                a[0] += wz * g.x;
+                a[1] += wz * g.y;
+                a[2] += wz * g.z;
+                if (oz > 0) {
+                  const float wo = wz * (float)oz;
+                  bz[0] += wo * g.x;
+                  bz[1] += wo * g.y;
+                  bz[2] += wo * g.z;
+                }
+              }
+              const float wxy = w[0][ox] * w[1][oy];
+#pragma unroll
+              for (int r = 0; r < 3; ++r) {
+                const float t = wxy * a[r];
+                v[r] += t;
+                M[r * 3 + 0] += (float)ox * t;
+                M[r * 3 + 1] += (float)oy * t;
+                M[r * 3 + 2] += wxy * bz[r];
+              }
+            }
+          float Cn[9];
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) Cn[r * 3 + c] = 4.f * S.inv_dx * (M[r * 3 + c] - v[r] * fx[c]);
+          float xn[3];
+          bool finite = true;
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            xn[d] = x[d] + S.dt * v[d];
+            finite = finite && isfinite(xn[d]) && isfinite(v[d]);
+          }
+          // CubeBoundary.impose_pos_vel (boundaries.py:22-32)
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            if (xn[d] >= S.hi[d] && v[d] >= 0.f) v[d] *= -S.restitution;
+            else if (xn[d] <= S.lo[d] && v[d] <= 0.f) v[d] *= -S.restitution;
+            xn[d] = fmaxf(fminf(xn[d], S.hi[d]), S.lo[d]);
+          }
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            D[(int64_t)(PF_POS + d) * cap + i] = xn[d];
+            D[(int64_t)(PF_VEL + d) * cap + i] = v[d];
+          }
+#pragma unroll
+          for (int k = 0; k < 9; ++k) D[(int64_t)(PF_C + k) * cap + i] = Cn[k];
+          int b[3];
+          if (!finite) atomicOr(P.status, 1u);
+          else if (stencil_origin(S, xn, b)) key = (int32_t)block_of(S, b[0], b[1], b[2]);
+          else atomicOr(P.status, 2u);
+        } else {
+          atomicOr(P.status, 2u);
+        }
+      }
+      add_rank(P, valid, key, i, lane);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(256) k_g2p(KParams P) { g2p_body<false>(P); }
+__global__ void __launch_bounds__(256) k_g2p_cpic(KParams P) { g2p_body<true>(P); }
 
 // ------------------------------------------------------------------ grid op
 // legacy_coupler.py:356-501 without coupling partners: for nodes with mass > eps,
@@ -1375,6 +1497,11 @@ __global__ void k_count_touched(KParams P, unsigned long long* out) {
   }
   for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
   if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+// Sets n floats of one particle plane to v (planes added to a live context).
+__global__ void k_fill_plane(float* p, int64_t n, float v) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
 }
 
 }  // namespace gbmpm

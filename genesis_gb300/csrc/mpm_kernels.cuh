@@ -38,8 +38,8 @@ constexpr int P2G_MAX_WARPS = P2G_MAX_THREADS / 32;
 constexpr int P2G_MAX_CHUNK = 1024;          // particles per P2G work item
 
 // Shared-memory layout of k_p2g (dynamic part): warp tiles, then one scatter record per particle
-// at its cell-sorted position (P2G_REC float4 each: fx | mass, q | a0, a1..a4, a5..a8, pad; the
-// odd stride of 5 float4 puts consecutive records in different bank groups), then the item's
+// at its cell-sorted position (P2G_REC float4 each: fx | mass, q | a0, a1..a4, a5..a8, then the
+// CPIC node mask in .x of the fifth, unused without CPIC; the odd stride of 5 float4 puts consecutive records in different bank groups), then the item's
 // (cell, rank) words.
 constexpr int P2G_REC = 5;
 __host__ __device__ __forceinline__ size_t p2g_dyn_smem(int threads, int chunk) {
@@ -59,6 +59,7 @@ enum : int {
   PF_MDIR = 28,
   NF_BASE = 27,
   NF_MUSCLE = 31,
+  PF_CPIC = 31,  // CPIC: 3 planes (the particle-side normal) per collider slot after the muscle planes
 };
 
 constexpr uint32_t INFO_MAT_MASK = 0x00FFFFFFu;
@@ -139,6 +140,8 @@ struct KParams {
   double* collider_acc;        // [n_colliders][6] reaction force and torque
   int32_t fuse_grid;           // G2P applies the grid op while staging its tile and clears the other buffer
   int32_t* nlist_reset;        // active-list length that k_perm resets at the end of a fused substep
+  int32_t cpic_slots;          // CPIC collider slots (normal planes PF_CPIC + 3 * slot); 0: CPIC off
+  uint32_t* cpic_mask;         // CPIC: per slot, the particle's nodes behind a collider (bit ox*9+oy*3+oz)
 };
 
 // Block key of a world position; returns false if the stencil would leave the grid.
@@ -211,7 +214,10 @@ __global__ void k_scan_onepass(KParams P);
 __global__ void k_scan_single(KParams P);
 __global__ void k_perm(KParams P);
 __global__ void k_p2g(KParams P);
+__global__ void k_p2g_cpic(KParams P);  // k_p2g with CPIC (thin-collider separation)
+__global__ void k_g2p_cpic(KParams P);  // k_g2p with CPIC
 __global__ void k_grid_op(KParams P);
+__global__ void k_fill_plane(float* p, int64_t n, float v);
 __global__ void k_get_grid(KParams P, int64_t scene, float* out);
 // Soft particle-to-link constraint of one reference particle row (mpm_solver.py:1052-1128).
 struct ConstraintDev {

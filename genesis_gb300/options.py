@@ -110,8 +110,6 @@ class MPMOptions(Options):
         self.upper_bound = _vec3(self.upper_bound, "upper_bound")
         if not np.all(np.array(self.upper_bound) > np.array(self.lower_bound)):
             raise GenesisException("Invalid pair of upper_bound and lower_bound.")
-        if self.enable_CPIC:
-            raise GenesisException("CPIC coupling with rigid bodies is not part of this MPM path.")
 
 
 class LegacyCouplerOptions(Options):

@@ -364,6 +364,12 @@ class MPMSolver:
         call again whenever they move)."""
         recs = [c.to_c() for c in colliders]
         arr = (_lib.MpmCollider * max(1, len(recs)))(*recs)
+        if self._enable_CPIC and len(recs) > getattr(self, "_cpic_slots", 0):
+            # CPIC (mpm_solver.py:389-411, 445-459): one slot of particle-side normals per collider;
+            # growing the slots starts every particle's normals afresh, as the coupler's build does
+            _lib.check(self._lib.mpm_enable_cpic(self._ctx, len(recs), _stream_handle()), self._ctx,
+                       "mpm_enable_cpic")
+            self._cpic_slots = len(recs)
         _lib.check(self._lib.mpm_set_colliders(self._ctx, len(recs), arr), self._ctx, "mpm_set_colliders")
         self._n_colliders = len(recs)
 

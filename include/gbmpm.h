@@ -250,6 +250,17 @@ int mpm_set_colliders(mpm_ctx* ctx, int32_t n, const mpm_collider* colliders);
  * the substeps since the last reset: out_host [n][6].  Synchronises `stream`. */
 int mpm_get_collider_forces(mpm_ctx* ctx, double* out_host, int32_t reset, void* stream);
 
+/* CPIC for thin colliders (MPMOptions.enable_CPIC; mpm_solver.py:389-411, 445-459,
+ * legacy_coupler.py:62-66, 503-529): reserves n_slots collider slots of particle-side SDF normals
+ * (3 floats per particle and slot, carried with the particle) and sets them to zero, as the
+ * coupler's reset does; call again to reset them.  While colliders are set, P2G gives nothing
+ * to a stencil node that a collider separates from the particle (its SDF normal at the node
+ * points against the particle's stored one), and G2P takes there the particle's own velocity
+ * collided with that collider (influence 1), the reaction going to the collider's accumulator.
+ * Colliders beyond n_slots are rejected by mpm_set_colliders.  n_slots = 0 turns CPIC off.
+ * Not available in pool mode. */
+int mpm_enable_cpic(mpm_ctx* ctx, int32_t n_slots, void* stream);
+
 /* Soft particle-to-link constraints (mpm_solver.py:1052-1128; mpm_entity.py:631-690).
  * mpm_set_particle_constraints: for each scene b of [scene_begin, scene_end) and each particle
  * [particle_start, particle_start + n) of it with mask[b * n + i] != 0, attach the particle to

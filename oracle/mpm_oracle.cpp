@@ -16,6 +16,9 @@
 //   force fields                      genesis/engine/force_fields.py (constant, wind, point, drag, vortex)
 //   rigid coupling (kinematic         legacy_coupler.py:166-218, 284-347; SDFs utils/sdf.py:119-126,
 //     colliders)                      372-378 (sphere, plane); boxes use their exact distance
+//   CPIC (thin colliders)             legacy_coupler.py:503-529 (particle-side normals),
+//                                     mpm_solver.py:389-411 (P2G skips separated nodes), :445-459
+//                                     (G2P takes the collided particle velocity there)
 //   g2p + particle boundary           mpm_solver.py:423-481, engine/boundaries/boundaries.py:22-32
 //   materials                         genesis/engine/materials/MPM/{base,elastic,liquid,sand,snow,
 //                                     elasto_plastic,muscle}.py
@@ -447,8 +450,44 @@ T collider_sdf(const oracle_collider& c, const T* x, T eps, T* n) {
   return sd;
 }
 
-// legacy_coupler.py:166-218 and 284-347: relative-velocity projection with friction,
-// restitution and the SDF influence; returns the reaction on the collider in acc[6].
+// _func_collide_in_rigid_geom (legacy_coupler.py:284-347): relative-velocity projection with
+// friction and restitution along the normal n, blended by `influence`; the reaction on collider
+// ci goes to its accumulator.
+template <typename T>
+void collide_in(size_t ci, const T* x, T* v, T mass, const T* n, T influence, T dt, T eps) {
+  const oracle_collider& c = g_colliders[ci];
+  const T r[3] = {x[0] - (T)c.com[0], x[1] - (T)c.com[1], x[2] - (T)c.com[2]};
+  const T w[3] = {(T)c.ang_vel[0], (T)c.ang_vel[1], (T)c.ang_vel[2]};
+  const T vr[3] = {w[1] * r[2] - w[2] * r[1] + (T)c.lin_vel[0], w[2] * r[0] - w[0] * r[2] + (T)c.lin_vel[1],
+                   w[0] * r[1] - w[1] * r[0] + (T)c.lin_vel[2]};
+  T rv[3];
+  for (int k = 0; k < 3; ++k) rv[k] = v[k] - vr[k];
+  const T rvn = rv[0] * n[0] + rv[1] * n[1] + rv[2] * n[2];
+  if (!(rvn < 0)) return;
+  T rt[3];
+  for (int k = 0; k < 3; ++k) rt[k] = rv[k] - rvn * n[k];
+  const T rtn = std::sqrt(rt[0] * rt[0] + rt[1] * rt[1] + rt[2] * rt[2] + eps);
+  const T mag = std::max((T)0, rtn + rvn * (T)c.friction);
+  T f[3];
+  for (int k = 0; k < 3; ++k) {
+    const T rnew = rt[k] / rtn * mag - n[k] * rvn * (T)c.restitution;
+    const T nv = vr[k] + rnew * influence + rv[k] * (1 - influence);
+    f[k] = -mass * (nv - v[k]) / dt;
+    v[k] = nv;
+  }
+  double* acc = g_collider_acc.data() + ci * 6;
+  const double tq[3] = {(double)(r[1] * f[2] - r[2] * f[1]), (double)(r[2] * f[0] - r[0] * f[2]),
+                        (double)(r[0] * f[1] - r[1] * f[0])};
+  for (int k = 0; k < 3; ++k) {
+#pragma omp atomic
+    acc[k] += (double)f[k];
+#pragma omp atomic
+    acc[3 + k] += tq[k];
+  }
+}
+
+// _func_collide_with_rigid (legacy_coupler.py:134-218): every collider of the scene whose SDF
+// influence exceeds 0.1 at x, in order.
 template <typename T>
 void collide_node(int scene, const T* x, T* v, T mass, T dt, T eps) {
   for (size_t ci = 0; ci < g_colliders.size(); ++ci) {
@@ -458,35 +497,28 @@ void collide_node(int scene, const T* x, T* v, T mass, T dt, T eps) {
     const T sd = collider_sdf(c, x, eps, n);
     const T influence = std::min(std::exp(-sd / std::max((T)1e-10, (T)c.softness)), (T)1);
     if (!(influence > (T)0.1)) continue;
-    const T r[3] = {x[0] - (T)c.com[0], x[1] - (T)c.com[1], x[2] - (T)c.com[2]};
-    const T w[3] = {(T)c.ang_vel[0], (T)c.ang_vel[1], (T)c.ang_vel[2]};
-    const T vr[3] = {w[1] * r[2] - w[2] * r[1] + (T)c.lin_vel[0], w[2] * r[0] - w[0] * r[2] + (T)c.lin_vel[1],
-                     w[0] * r[1] - w[1] * r[0] + (T)c.lin_vel[2]};
-    T rv[3];
-    for (int k = 0; k < 3; ++k) rv[k] = v[k] - vr[k];
-    const T rvn = rv[0] * n[0] + rv[1] * n[1] + rv[2] * n[2];
-    if (!(rvn < 0)) continue;
-    T rt[3];
-    for (int k = 0; k < 3; ++k) rt[k] = rv[k] - rvn * n[k];
-    const T rtn = std::sqrt(rt[0] * rt[0] + rt[1] * rt[1] + rt[2] * rt[2] + eps);
-    const T mag = std::max((T)0, rtn + rvn * (T)c.friction);
-    T f[3];
-    for (int k = 0; k < 3; ++k) {
-      const T rnew = rt[k] / rtn * mag - n[k] * rvn * (T)c.restitution;
-      const T nv = vr[k] + rnew * influence + rv[k] * (1 - influence);
-      f[k] = -mass * (nv - v[k]) / dt;
-      v[k] = nv;
-    }
-    double* acc = g_collider_acc.data() + ci * 6;
-    const double tq[3] = {(double)(r[1] * f[2] - r[2] * f[1]), (double)(r[2] * f[0] - r[0] * f[2]),
-                          (double)(r[0] * f[1] - r[1] * f[0])};
-    for (int k = 0; k < 3; ++k) {
-#pragma omp atomic
-      acc[k] += (double)f[k];
-#pragma omp atomic
-      acc[3 + k] += tq[k];
-    }
+    collide_in<T>(ci, x, v, mass, n, influence, dt, eps);
   }
+}
+
+// CPIC state: per particle and collider, the last SDF normal seen on the particle's side
+// (mpm_rigid_normal, legacy_coupler.py:65), zero until the first substep.
+bool g_cpic = false;
+std::vector<double> g_cpic_normal;
+
+// First collider of the scene (in order) whose normal at world point xc points against the
+// particle's stored normal (mpm_solver.py:392-409), or -1.
+template <typename T>
+int cpic_separating(int scene, const double* pn, const T* xc, T eps) {
+  const size_t nc = g_colliders.size();
+  for (size_t ci = 0; ci < nc; ++ci) {
+    const oracle_collider& c = g_colliders[ci];
+    if (c.scene >= 0 && c.scene != scene) continue;
+    T n[3];
+    collider_sdf(c, xc, eps, n);
+    if ((T)pn[ci * 3] * n[0] + (T)pn[ci * 3 + 1] * n[1] + (T)pn[ci * 3 + 2] * n[2] < 0) return (int)ci;
+  }
+  return -1;
 }
 
 template <typename T>
@@ -551,7 +583,29 @@ int run(const oracle_scene* sc, const oracle_material* mats, int n_mats, int64_t
 #endif
   const bool par = threads > 1;
   const T stress_scale = (T)(-(double)S.dt * (double)S.p_vol * 4.0 * (double)S.inv_dx * (double)S.inv_dx);
+  const size_t ncol = g_colliders.size();
+  const bool cpic = g_cpic && ncol > 0;
+  std::vector<int16_t> cflag;  // cpic_flag: separating collider of each particle's 27 nodes, or -1
+  if (cpic) {
+    if (g_cpic_normal.size() != (size_t)n * ncol * 3) g_cpic_normal.assign((size_t)n * ncol * 3, 0.0);
+    cflag.assign((size_t)n * 27, -1);
+  }
   for (int step = 0; step < n_substeps; ++step) {
+    if (cpic) {  // mpm_surface_to_particle (legacy_coupler.py:513-529): keep the particle's side
+#pragma omp parallel for schedule(static) if (par)
+      for (int64_t i = 0; i < n; ++i) {
+        if (!active[i]) continue;
+        for (size_t ci = 0; ci < ncol; ++ci) {
+          const oracle_collider& c = g_colliders[ci];
+          if (c.scene >= 0 && c.scene != 0) continue;
+          T nr[3];
+          collider_sdf(c, pos + i * 3, S.eps, nr);
+          double* pn = g_cpic_normal.data() + ((size_t)i * ncol + ci) * 3;
+          if ((T)pn[0] * nr[0] + (T)pn[1] * nr[1] + (T)pn[2] * nr[2] >= 0)
+            for (int k = 0; k < 3; ++k) pn[k] = (double)nr[k];
+        }
+      }
+    }
     // reset_grid_and_grad (mpm_solver.py:577-587)
     std::fill(gm.begin(), gm.end(), T(0));
     std::fill(gp.begin(), gp.end(), T(0));
@@ -604,12 +658,18 @@ int run(const oracle_scene* sc, const oracle_material* mats, int n_mats, int64_t
               weight *= w[o[d]][d];
             }
             const int64_t I = ((base[0] - S.off[0] + ox) * ry + (base[1] - S.off[1] + oy)) * rz + (base[2] - S.off[2] + oz);
+            if (!is_free) pin[I] = 1;
+            if (cpic) {  // a node behind a thin collider gets nothing from this particle (:389-412)
+              const T xc[3] = {(T)(base[0] + ox) * S.dx, (T)(base[1] + oy) * S.dx, (T)(base[2] + oz) * S.dx};
+              const int sep = cpic_separating<T>(0, g_cpic_normal.data() + (size_t)i * ncol * 3, xc, S.eps);
+              cflag[(size_t)i * 27 + ox * 9 + oy * 3 + oz] = (int16_t)sep;
+              if (sep >= 0) continue;
+            }
             for (int r = 0; r < 3; ++r) {
               const T a = affine(r, 0) * dpos[0] + affine(r, 1) * dpos[1] + affine(r, 2) * dpos[2];
               atomic_add(gp[I * 3 + r], weight * (mass * vel[i * 3 + r] + a), par);
             }
             atomic_add(gm[I], weight * mass, par);
-            if (!is_free) pin[I] = 1;
           }
     }
     if (bad) return 5;
@@ -682,8 +742,17 @@ int run(const oracle_scene* sc, const oracle_material* mats, int n_mats, int64_t
               weight *= w[o[d]][d];
             }
             const int64_t I = ((base[0] - S.off[0] + ox) * ry + (base[1] - S.off[1] + oy)) * rz + (base[2] - S.off[2] + oz);
+            T gvel[3] = {gv[I * 3], gv[I * 3 + 1], gv[I * 3 + 2]};
+            const int sep = cpic ? cflag[(size_t)i * 27 + ox * 9 + oy * 3 + oz] : -1;
+            if (sep >= 0) {  // the particle's own velocity, collided with that collider (:445-459)
+              for (int r = 0; r < 3; ++r) gvel[r] = vel[i * 3 + r];
+              T pn[3];
+              for (int k = 0; k < 3; ++k) pn[k] = (T)g_cpic_normal[((size_t)i * ncol + sep) * 3 + k];
+              collide_in<T>((size_t)sep, pos + i * 3, gvel, M[mat[i]].rho * S.p_vol * weight / (T)1e3, pn, (T)1,
+                            S.dt, S.eps);
+            }
             for (int r = 0; r < 3; ++r) {
-              const T g = gv[I * 3 + r];
+              const T g = gvel[r];
               nv[r] += weight * g;
               for (int c = 0; c < 3; ++c) nC(r, c) += 4 * S.inv_dx * weight * g * dpos[c];
             }
@@ -757,6 +826,12 @@ void oracle_material_f64(const oracle_material* mm, const double* F_tmp, double 
 void oracle_set_colliders(int n, const oracle_collider* c) {
   g_colliders.assign(c, c + n);
   g_collider_acc.assign((size_t)n * 6, 0.0);
+}
+
+// CPIC for the following runs (MPMOptions.enable_CPIC); clears the particle-side normals.
+void oracle_set_cpic(int enable) {
+  g_cpic = enable != 0;
+  g_cpic_normal.clear();
 }
 
 // Force fields for the following runs (n = 0 removes them).

@@ -99,6 +99,8 @@ def load():
         lib.oracle_set_force_fields.restype = None
         lib.oracle_collider_forces.argtypes = [P]
         lib.oracle_collider_forces.restype = None
+        lib.oracle_set_cpic.argtypes = [ctypes.c_int]
+        lib.oracle_set_cpic.restype = None
         _lib = lib
     return _lib
 
@@ -194,6 +196,12 @@ def set_force_fields(fields) -> None:
     buf = b"".join(bytes(f) for f in fields) or b"\0" * 8
     arr = ctypes.create_string_buffer(buf, len(buf))
     load().oracle_set_force_fields(n, arr)
+
+
+def set_cpic(enable: bool) -> None:
+    """CPIC (MPMOptions.enable_CPIC) for the following runs; clears the particle-side collider
+    normals, which otherwise persist from run to run like the particle state."""
+    load().oracle_set_cpic(1 if enable else 0)
 
 
 def collider_forces(n: int) -> np.ndarray:

@@ -35,14 +35,14 @@ def jittered_lattice(center, size, spacing, dx, seed):
     return p + rng.uniform(-0.25 * dx, 0.25 * dx, size=p.shape)
 
 
-def c1_scene(gs, n_envs=0, seed=7, size=0.2):
+def c1_scene(gs, n_envs=0, seed=7, size=0.2, cpic=False):
     """Config 1: grid 64^3 over the unit cube, elastic cube of side 0.2 at (0.5,0.5,0.4),
     2 particles per cell per axis, jitter +-0.25 dx, E=3e5 nu=0.2 rho=1000, dt=2e-4."""
     dx = 1 / 64
     scene = gs.Scene(
         sim_options=gs.options.SimOptions(dt=2e-4, substeps=1),
         mpm_options=gs.options.MPMOptions(lower_bound=(0, 0, 0), upper_bound=(1, 1, 1), grid_density=64,
-                                          particle_size=1 / 128),
+                                          particle_size=1 / 128, enable_CPIC=cpic),
     )
     mat = gs.materials.MPM.Elastic(E=3e5, nu=0.2, rho=1000, sampler="regular")
     cube = scene.add_entity(material=mat, morph=gs.morphs.Box(pos=(0.5, 0.5, 0.4), size=(size,) * 3))
@@ -391,6 +391,53 @@ def test_rigid_colliders_match_oracle(gs, oracle):
     finally:
         oracle.set_colliders([])
     assert np.abs(f_ref[:, :3]).max(axis=1).min() > 1.0, f_ref  # every collider was hit
+    err = np.abs(st1.pos[0].double().cpu().numpy() - ref["pos"]).max()
+    assert err <= POS_TOL, err
+    assert np.abs(st1.vel[0].double().cpu().numpy() - ref["vel"]).max() < 5e-3
+    assert np.allclose(f_gpu, f_ref, rtol=2e-3, atol=2e-3 * np.abs(f_ref).max()), (f_gpu, f_ref)
+    solver.set_colliders([])
+
+
+def test_cpic_thin_blade_matches_oracle(gs, oracle):
+    """CPIC (mpm_solver.py:389-411, 445-459; legacy_coupler.py:503-529): a thin static blade through
+    an elastic cube that moves into it.  Nodes behind the blade take nothing from a particle in
+    P2G and give it its own collided velocity in G2P.  Particle state and the blade's reaction
+    against the FP64 oracle; the oracle without CPIC must end elsewhere (CPIC did something)."""
+    from genesis_gb300.coupling import Collider
+
+    scene, cube, mat = c1_scene(gs, size=0.12, cpic=True)
+    solver = scene.sim.mpm_solver
+    st = solver.get_state()
+    vel = st.vel.clone()
+    vel[..., 0] = 1.0
+    vel[..., 2] = -0.5
+    st.vel = vel
+    solver.set_state(0, st)
+    # mid-plane exact in fp32 and 4.9 mm from the nearest node column: every side test is clear-cut
+    bx = 0.5 + 5 / 1024
+    blade = Collider("box", pos=(bx, 0.5, 0.4), half_extents=(0.0015, 0.15, 0.15), coup_friction=0.3)
+    solver.set_colliders([blade])
+    st0 = solver.get_state()
+    n_sub = 40
+    for _ in range(n_sub):
+        scene.step()
+    st1 = solver.get_state()
+    f_gpu = solver.get_collider_forces()
+    sc = oracle_scene_for(oracle, solver)
+    om = [oracle.from_c_material(mat.to_c(0))]
+    try:
+        oracle.set_cpic(True)
+        oracle.set_colliders([blade.to_c()])
+        ref, _, _ = oracle.run(sc, om, oracle_state(st0), n_sub)
+        f_ref = oracle.collider_forces(1)
+        oracle.set_cpic(False)
+        oracle.set_colliders([blade.to_c()])
+        plain, _, _ = oracle.run(sc, om, oracle_state(st0), n_sub)
+    finally:
+        oracle.set_cpic(False)
+        oracle.set_colliders([])
+    assert f_ref[0, 0] > 100.0, f_ref  # the cube pushes the blade along +x
+    assert np.abs(plain["pos"] - ref["pos"]).max() > 20 * POS_TOL
     err = np.abs(st1.pos[0].double().cpu().numpy() - ref["pos"]).max()
     assert err <= POS_TOL, err
     assert np.abs(st1.vel[0].double().cpu().numpy() - ref["vel"]).max() < 5e-3
