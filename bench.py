@@ -29,6 +29,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 SUBSTEPS_PER_STEP = 10
+# kernels one substep of the benchmark launches (fused grid op: no pinned particles, colliders or
+# force fields): k_p2g, k_g2p, k_scan_onepass, k_perm
+KERNELS_PER_SUBSTEP = 4
 SUBSTEP_DT = 1e-4
 GRID_DENSITY = 128
 SEED = 2024
@@ -330,8 +333,8 @@ def run_ours(args, rank, world):
         # (ncu count per particle x particles / event-timed duration) against the SM issue peak
         # (4 schedulers x SMs x SM clock under load)
         props = torch.cuda.get_device_properties(torch.cuda.current_device())
-        clk = (clk.get("sm_mhz") or 2070.0) * 1e6
-        issue_peak = 4 * props.multi_processor_count * clk
+        sm_hz = (clk.get("sm_mhz") or 2070.0) * 1e6
+        issue_peak = 4 * props.multi_processor_count * sm_hz
         inst = tr["warp_instructions_per_particle"] * n
         rate = inst / (per_kernel[dom]["ms_avg"] / 1e3)
         roofline["issue"] = {"kernel": dom, "warp_instructions": inst, "achieved": rate / 1e9,
@@ -420,7 +423,7 @@ def run_ours(args, rank, world):
         "roofline": roofline,
         "kernels": per_kernel,
         "e2e": e2e,
-        "gpu_launches": 7 * SUBSTEPS_PER_STEP * args.steps,
+        "gpu_launches": KERNELS_PER_SUBSTEP * SUBSTEPS_PER_STEP * args.steps,
         "clocks": clk,
     }
     if rank == 0 and not args.skip_forms:
@@ -429,6 +432,46 @@ def run_ours(args, rank, world):
     if rank == 0 and not args.skip_cpu:
         result["cpu_baseline"] = cpu_baseline()
     return result
+
+
+def validate_line(d: dict) -> None:
+    """Checks the shape of the JSON line (keys and types the consumers read); raises ValueError
+    naming the first key that is missing or of the wrong type."""
+    num = (int, float)
+
+    def need(obj, key, typ, where):
+        if key not in obj or isinstance(obj[key], bool) != (typ is bool) or not isinstance(obj[key], typ):
+            raise ValueError(f"{where}{key}: expected {typ}, got {obj.get(key)!r}")
+
+    if d.get("impl") == "reference":
+        if "unavailable" in d:
+            need(d, "unavailable", str, "")
+            return
+        for k, t in (("metric", str), ("value", num), ("unit", str), ("cpu_baseline", dict), ("e2e", dict)):
+            need(d, k, t, "")
+    else:
+        for k, t in (("metric", str), ("value", num), ("unit", str), ("n_gpus", int), ("steps", int),
+                     ("warmup", int), ("ms_per_step", num), ("higher_is_better", bool), ("scaling", str),
+                     ("dtype", str), ("data", str), ("config", dict), ("roofline", dict), ("e2e", dict),
+                     ("gpu_launches", int), ("clocks", dict)):
+            need(d, k, t, "")
+        need(d["config"], "workload", str, "config.")
+        for k, t in (("bound", str), ("achieved", num), ("peak", num), ("unit", str), ("frac", num)):
+            need(d["roofline"], k, t, "roofline.")
+        if "traffic" not in d["roofline"] or not (d["roofline"]["traffic"] is None
+                                                   or isinstance(d["roofline"]["traffic"], num)):
+            raise ValueError("roofline.traffic: expected a number or null")
+        need(d["clocks"], "reasons", list, "clocks.")
+        for k in ("sm_mhz", "sm_max_mhz"):
+            if k not in d["clocks"] or not (d["clocks"][k] is None or isinstance(d["clocks"][k], num)):
+                raise ValueError(f"clocks.{k}: expected a number or null")
+    for k, t in (("value", num), ("unit", str), ("h2d_bytes_per_step", int), ("d2h_bytes_per_step", int)):
+        need(d["e2e"], k, t, "e2e.")
+    if "cpu_baseline" in d:
+        for k, t in (("value", num), ("unit", str), ("cores", int), ("kind", str), ("sample", str)):
+            need(d["cpu_baseline"], k, t, "cpu_baseline.")
+        if d["cpu_baseline"]["kind"] not in ("reference", "port"):
+            raise ValueError("cpu_baseline.kind: expected 'reference' or 'port'")
 
 
 def _timed(fn):
@@ -663,7 +706,9 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
         if rank == 0:
-            print(json.dumps(run_reference(args)))
+            line = run_reference(args)
+            validate_line(line)
+            print(json.dumps(line))
         return
     if world > 1:
         import torch
@@ -672,6 +717,7 @@ def main():
         torch.distributed.init_process_group("nccl")
     res = run_ours(args, rank, world)
     if rank == 0:
+        validate_line(res)
         print(json.dumps(res))
     if world > 1:
         import torch
