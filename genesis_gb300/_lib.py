@@ -174,6 +174,7 @@ _SIGNATURES = {
     "mpm_test_wait_timeout": (c_int32, [_P, _P]),
     "mpm_get_collider_forces": (c_int32, [_P, _P, c_int32, _P]),
     "mpm_enable_cpic": (c_int32, [_P, c_int32, _P]),
+    "mpm_set_coupled_particles": (c_int32, [_P, c_int32, c_int64, _P, _P, _P, _P, _P]),
     "mpm_version": (c_int32, []),
     "mpm_ctx_create_pool": (c_int32, [ctypes.c_void_p, c_int32, ctypes.POINTER(c_void_p)]),
     "mpm_scene_admit": (c_int32, [_P, c_int64, ctypes.c_void_p, ctypes.c_void_p, c_int32, c_int64, _P, _P, c_int32, _P]),

@@ -84,6 +84,8 @@ struct mpm_ctx {
   int32_t n_colliders = 0;
   int32_t cpic_slots = 0;            // CPIC collider slots (normal planes); 0: CPIC off
   uint32_t* d_cpic_mask = nullptr;   // CPIC: per particle slot, the stencil nodes behind a collider
+  ExtSetDev ext[2] = {};             // coupled SPH / PBD particle sets (caller-owned arrays, own bins)
+  int64_t ext_cap[2] = {0, 0};       // particles the bin arrays of each set hold
   float* d_links = nullptr;         // kinematic link poses [scene][link] (pos xyz, quat wxyz)
   int32_t n_links = 0;
   int32_t* d_steps = nullptr;
@@ -192,6 +194,8 @@ KParams make_params(mpm_ctx* ctx, int src, int dst, int g) {
   P.collider_acc = ctx->d_collider_acc;
   P.cpic_slots = ctx->cpic_slots;
   P.cpic_mask = ctx->d_cpic_mask;
+  P.ext[0] = ctx->ext[0];
+  P.ext[1] = ctx->ext[1];
   P.scan_sync = ctx->d_scan_sync;
   P.n_tiles = ctx->n_tiles;
   P.pin = ctx->d_pin;
@@ -279,8 +283,14 @@ int launch_pre(mpm_ctx* ctx, int c, cudaStream_t s) {
 int launch_grid(mpm_ctx* ctx, int c, cudaStream_t s) {
   KParams P = make_params(ctx, c, 1 - c, c);
   ctx->grid_momentum[c] = false;
-  Timer t(ctx, s, KT_GRID);
-  k_grid_op<<<ctx->grid_blocks, 256, 0, s>>>(P);
+  for (int k = 0; k < 2; ++k)
+    if (ctx->ext[k].n > 0) k_ext_bin<<<ctx->io_blocks, 256, 0, s>>>(P, k, 0);
+  {
+    Timer t(ctx, s, KT_GRID);
+    k_grid_op<<<ctx->grid_blocks, 256, 0, s>>>(P);
+  }
+  for (int k = 0; k < 2; ++k)
+    if (ctx->ext[k].n > 0) k_ext_bin<<<ctx->io_blocks, 256, 0, s>>>(P, k, 1);
   CKL();
   return MPM_OK;
 }
@@ -311,7 +321,8 @@ int launch_post(mpm_ctx* ctx, int c, cudaStream_t s, bool fuse_grid = false) {
 // Without pinned particles the grid op is folded into G2P (k_grid_op is not launched); the
 // split-phase entry points keep it separate so a coupler can act on the velocity grid.
 int launch_substep(mpm_ctx* ctx, int c, cudaStream_t s) {
-  const bool fuse = ctx->d_pin == nullptr && ctx->n_colliders == 0 && ctx->n_ffs == 0;
+  const bool fuse = ctx->d_pin == nullptr && ctx->n_colliders == 0 && ctx->n_ffs == 0 && ctx->ext[0].n == 0 &&
+                    ctx->ext[1].n == 0;
   int r = launch_pre(ctx, c, s);
   if (!r && !fuse) r = launch_grid(ctx, c, s);
   if (!r) r = launch_post(ctx, c, s, fuse);
@@ -694,6 +705,11 @@ int mpm_ctx_destroy(mpm_ctx* ctx) {
   if (ctx->d_ffs) cudaFree(ctx->d_ffs);
   if (ctx->d_collider_acc) cudaFree(ctx->d_collider_acc);
   if (ctx->d_cpic_mask) cudaFree(ctx->d_cpic_mask);
+  for (int k = 0; k < 2; ++k) {
+    if (ctx->ext[k].head) cudaFree(ctx->ext[k].head);
+    if (ctx->ext[k].next) cudaFree(ctx->ext[k].next);
+    if (ctx->ext[k].node) cudaFree(ctx->ext[k].node);
+  }
   if (ctx->d_links) cudaFree(ctx->d_links);
   if (ctx->ev_in) cudaEventDestroy(ctx->ev_in);
   if (ctx->ev_out) cudaEventDestroy(ctx->ev_out);
@@ -1025,6 +1041,53 @@ int mpm_enable_cpic(mpm_ctx* ctx, int32_t n_slots, void* stream) {
   ctx->cpic_slots = n_slots;
   drop_graph(ctx);  // kernel choice and plane count are captured
   if ((r = compute_launch_shapes(ctx))) return r;
+  return leave(ctx, stream);
+}
+
+int mpm_set_coupled_particles(mpm_ctx* ctx, int32_t kind, int64_t n, const float* pos, float* vel, const float* mass,
+                              const uint8_t* free_, void* stream) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (kind != MPM_COUPLED_SPH && kind != MPM_COUPLED_PBD) return fail(ctx, MPM_ERR_BAD_ARG, "unknown coupled set");
+  if (n < 0 || (n > 0 && (!pos || !vel || !mass))) return fail(ctx, MPM_ERR_BAD_ARG, "bad coupled particle arrays");
+  if (n > 0 && n * ctx->n_scenes >= (int64_t)INT32_MAX) return fail(ctx, MPM_ERR_BAD_ARG, "too many coupled particles");
+  if (ctx->pool) return fail(ctx, MPM_ERR_BAD_ARG, "particle coupling is not available in pool mode");
+  if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "coupling set-up inside a substep");
+  int r = enter(ctx, stream);
+  if (r) return r;
+  ExtSetDev& E = ctx->ext[kind];
+  const int64_t total = n * ctx->n_scenes;
+  if (n > 0 && !E.head) {
+    const size_t nodes = (size_t)ctx->K * BLK_NODES;
+    cudaError_t e = cudaMalloc((void**)&E.head, sizeof(int32_t) * nodes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      E.head = nullptr;
+      return fail(ctx, MPM_ERR_OOM, "coupling bins: " + std::string(cudaGetErrorString(e)));
+    }
+    CK(cudaMemsetAsync(E.head, 0xff, sizeof(int32_t) * nodes, ctx->cs));  // every list empty (-1)
+  }
+  if (total > ctx->ext_cap[kind]) {
+    if (E.next) cudaFree(E.next);
+    if (E.node) cudaFree(E.node);
+    E.next = nullptr;
+    E.node = nullptr;
+    ctx->ext_cap[kind] = 0;
+    cudaError_t e = cudaMalloc((void**)&E.next, sizeof(int32_t) * (size_t)total);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&E.node, sizeof(int64_t) * (size_t)total);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ctx, MPM_ERR_OOM, "coupling lists: " + std::string(cudaGetErrorString(e)));
+    }
+    ctx->ext_cap[kind] = total;
+  }
+  const uint8_t* fr = kind == MPM_COUPLED_PBD ? free_ : nullptr;
+  const bool changed = E.n != n || E.pos != pos || E.vel != vel || E.mass != mass || E.free_ != fr;
+  E.pos = pos;
+  E.vel = vel;
+  E.mass = mass;
+  E.free_ = fr;
+  E.n = n;
+  if (changed) drop_graph(ctx);  // the arrays are captured kernel arguments
   return leave(ctx, stream);
 }
 

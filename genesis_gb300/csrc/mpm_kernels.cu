@@ -608,6 +608,41 @@ __device__ void collide_node(const KParams& P, const SceneDev& S, int32_t scene,
   }
 }
 
+// MPM <-> SPH, then MPM <-> PBD (legacy_coupler.py:404-498) at node address a with MPM mass m:
+// when the set has particles in the node's cell, the node takes their mean velocity and each of
+// them loses delta_mv / m_i, delta_mv = m (v_new - v_old) (PBD: only free particles).  The lists
+// are acyclic by construction; a walk longer than the set still stops and flags the status.
+__device__ void couple_ext(const KParams& P, int64_t a, float* v, float m) {
+  for (int k = 0; k < 2; ++k) {
+    const ExtSetDev& E = P.ext[k];
+    if (E.n == 0) continue;
+    const int64_t total = E.n * (int64_t)P.n_scenes;
+    const int32_t h = E.head[a];
+    if (h < 0) continue;
+    float sv[3] = {0.f, 0.f, 0.f};
+    int64_t cnt = 0;
+    for (int32_t j = h; j >= 0 && j < total; j = E.next[j]) {
+      if (++cnt > total) {
+        atomicOr(P.status, MPM_STATUS_BAD_INDEX);
+        return;
+      }
+      for (int d = 0; d < 3; ++d) sv[d] += E.vel[(int64_t)j * 3 + d];
+    }
+    float dmv[3];
+    for (int d = 0; d < 3; ++d) {
+      const float vn = sv[d] / (float)cnt;
+      dmv[d] = m * (vn - v[d]);
+      v[d] = vn;
+    }
+    int64_t left = cnt;
+    for (int32_t j = h; j >= 0 && j < total && left > 0; j = E.next[j], --left) {
+      if (k == 1 && E.free_ && !E.free_[j]) continue;
+      const float mi = E.mass[j];
+      for (int d = 0; d < 3; ++d) E.vel[(int64_t)j * 3 + d] -= dmv[d] / mi;
+    }
+  }
+}
+
 // CPIC (MPMOptions.enable_CPIC) for thin colliders.  Particle side, mpm_surface_to_particle
 // (legacy_coupler.py:513-529): per collider the particle keeps the SDF normal at its position
 // unless that normal turned against the stored one, so the stored normal remembers the side the
@@ -1263,9 +1298,9 @@ __global__ void __launch_bounds__(256) k_grid_op(KParams P) {
         atomicAnd(&P.pin[a >> 5], ~bit);
       }
     }
-    if (P.n_colliders == 0 && P.n_ffs == 0) {
+    if (P.n_colliders == 0 && P.n_ffs == 0 && P.ext[0].n == 0 && P.ext[1].n == 0) {
       *node = grid_velocity(S, q, g[0], g[1], g[2]);
-    } else {  // gravity, force fields (:381-383), colliders (:389-403), then the boundary
+    } else {  // gravity, force fields (:381-383), colliders (:389-403), SPH / PBD (:404-498), boundary
       float v[3];
       if (grid_free_velocity(S, q, v)) {
         const float x[3] = {(float)(g[0] + S.offset[0]) * S.dx, (float)(g[1] + S.offset[1]) * S.dx,
@@ -1277,6 +1312,7 @@ __global__ void __launch_bounds__(256) k_grid_op(KParams P) {
           for (int k = 0; k < 3; ++k) v[k] += a[k] * S.dt;
         }
         collide_node(P, S, P.block_scene[blk], x, v, q.w / 1e3f);
+        couple_ext(P, (int64_t)blk * BLK_NODES + ln, v, q.w / 1e3f);
         grid_boundary(S, v, g[0], g[1], g[2]);
       }
       *node = make_float4(v[0], v[1], v[2], q.w);
@@ -1502,6 +1538,42 @@ __global__ void k_count_touched(KParams P, unsigned long long* out) {
 // Sets n floats of one particle plane to v (planes added to a live context).
 __global__ void k_fill_plane(float* p, int64_t n, float v) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+// Bins coupled set k by grid node before the grid op (unbin = 0) and empties those lists after it
+// (unbin = 1).  A particle belongs to the node whose cell holds it, |x_node - p|_inf < dx / 2
+// (legacy_coupler.py:417-420); only the nearest node can pass that test, so it alone is tried.
+__global__ void k_ext_bin(KParams P, int k, int unbin) {
+  const ExtSetDev& E = P.ext[k];
+  const int64_t total = E.n * (int64_t)P.n_scenes;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    if (unbin) {
+      const int64_t a = E.node[i];
+      if (a >= 0) E.head[a] = -1;
+      continue;
+    }
+    const SceneDev& S = P.scenes[i / E.n];
+    int g[3];
+    bool ok = true;
+    for (int d = 0; d < 3 && ok; ++d) {
+      const float p = E.pos[i * 3 + d];
+      const float t = floorf(__fadd_rn(__fmul_rn(p, S.inv_dx), 0.5f));
+      if (!(t > -1e9f && t < 1e9f)) {
+        ok = false;
+        break;
+      }
+      const int gi = (int)t;
+      ok = fabsf(__fsub_rn(__fmul_rn((float)gi, S.dx), p)) < __fmul_rn(0.5f, S.dx);
+      g[d] = gi - S.offset[d];
+      ok = ok && g[d] >= 0 && g[d] < S.res[d];
+    }
+    int64_t a = -1;
+    if (ok) {
+      a = node_addr(S, g[0], g[1], g[2]);
+      E.next[i] = atomicExch(&E.head[a], (int32_t)i);
+    }
+    E.node[i] = a;
+  }
 }
 
 }  // namespace gbmpm

@@ -3,7 +3,8 @@
 // Layout in HBM (all scenes of a context share one set of buffers):
 //  * particles: two buffers (ping-pong), each NF float planes of `cap` entries (SoA):
 //      0-2 pos, 3-5 vel, 6-14 C (row-major), 15-23 F, 24 Jp, 25 info (bits), 26 pid (bits),
-//      27 actu, 28-30 muscle direction (only when a muscle material exists).
+//      27 actu, 28-30 muscle direction (when a muscle material exists or CPIC is on),
+//      31 + 3c .. 33 + 3c the CPIC normal of collider slot c (CPIC only).
 //    info = global material index (bits 0-23) | ACTIVE | FREE | DEAD.
 //    pid = particle index within its scene (reference particle order for get/set state).
 //  * grid: two buffers of float4 nodes grouped in blocks of 4x4x4 nodes (1 KiB each).
@@ -39,8 +40,8 @@ constexpr int P2G_MAX_CHUNK = 1024;          // particles per P2G work item
 
 // Shared-memory layout of k_p2g (dynamic part): warp tiles, then one scatter record per particle
 // at its cell-sorted position (P2G_REC float4 each: fx | mass, q | a0, a1..a4, a5..a8, then the
-// CPIC node mask in .x of the fifth, unused without CPIC; the odd stride of 5 float4 puts consecutive records in different bank groups), then the item's
-// (cell, rank) words.
+// CPIC node mask in .x of the fifth, unused without CPIC; the odd stride of 5 float4 puts
+// consecutive records in different bank groups), then the item's (cell, rank) words.
 constexpr int P2G_REC = 5;
 __host__ __device__ __forceinline__ size_t p2g_dyn_smem(int threads, int chunk) {
   return (size_t)(threads / 32) * TILE_NODES * 16 + (size_t)chunk * P2G_REC * 16 + (size_t)chunk * 4;
@@ -94,6 +95,18 @@ struct ForceFieldDev {
   float s_perp, s_radial, falloff_min, falloff_max, damping, pad2;
 };
 
+// Another solver's particles coupled through the grid op (SPH or PBD), caller-owned device arrays.
+struct ExtSetDev {
+  const float* pos;      // [n_scenes][n][3]
+  float* vel;            // [n_scenes][n][3], updated in place
+  const float* mass;     // [n_scenes][n]
+  const uint8_t* free_;  // [n_scenes][n] (PBD) or null: every particle takes momentum
+  int64_t n;             // particles per scene; 0: set unused
+  int32_t* head;         // per grid node: first binned particle, -1 when empty
+  int32_t* next;         // per particle: next particle of its node's list
+  int64_t* node;         // per particle: node it was binned to, -1 if none
+};
+
 struct KParams {
   const SceneDev* scenes;
   const MaterialDev* mats;
@@ -142,6 +155,7 @@ struct KParams {
   int32_t* nlist_reset;        // active-list length that k_perm resets at the end of a fused substep
   int32_t cpic_slots;          // CPIC collider slots (normal planes PF_CPIC + 3 * slot); 0: CPIC off
   uint32_t* cpic_mask;         // CPIC: per slot, the particle's nodes behind a collider (bit ox*9+oy*3+oz)
+  ExtSetDev ext[2];            // coupled particle sets: [0] SPH, [1] PBD (applied in that order)
 };
 
 // Block key of a world position; returns false if the stencil would leave the grid.
@@ -218,6 +232,7 @@ __global__ void k_p2g_cpic(KParams P);  // k_p2g with CPIC (thin-collider separa
 __global__ void k_g2p_cpic(KParams P);  // k_g2p with CPIC
 __global__ void k_grid_op(KParams P);
 __global__ void k_fill_plane(float* p, int64_t n, float v);
+__global__ void k_ext_bin(KParams P, int k, int unbin);
 __global__ void k_get_grid(KParams P, int64_t scene, float* out);
 // Soft particle-to-link constraint of one reference particle row (mpm_solver.py:1052-1128).
 struct ConstraintDev {

@@ -382,6 +382,50 @@ class MPMSolver:
                    self._ctx, "mpm_get_collider_forces")
         return out[:n]
 
+    # ------------------------------------------------------------------ SPH / PBD coupling
+    def set_coupled_particles(self, kind: str, pos=None, vel=None, mass=None, free=None) -> None:
+        """Couple another solver's particles through the grid op (legacy_coupler.py:404-498).
+
+        kind 'sph' or 'pbd'; pos and vel float32 CUDA tensors [B, n, 3] ([n, 3] with one env),
+        mass float32 [B, n] ([n]), free uint8 [B, n] ([n]; PBD only, None: all free).  A node with
+        MPM mass takes the mean velocity of the set's particles in its cell and gives each of them
+        back the momentum change; vel is updated in place by every grid op.  The tensors stay
+        referenced here (and must not be reallocated) until the set is replaced or removed with
+        pos=None."""
+        k = {"sph": 0, "pbd": 1}.get(kind)
+        if k is None:
+            gs_exc(f"Unsupported coupled particle kind: {kind!r} (expected 'sph' or 'pbd').")
+        if not hasattr(self, "_coupled"):
+            self._coupled = [None, None]
+        if pos is None:
+            _lib.check(self._lib.mpm_set_coupled_particles(self._ctx, k, 0, None, None, None, None, _stream_handle()),
+                       self._ctx, "mpm_set_coupled_particles")
+            self._coupled[k] = None
+            return
+        B = self._B
+
+        def arr(t, name, width, dtype):
+            if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == dtype and t.is_contiguous()):
+                gs_exc(f"{name} must be a contiguous {dtype} CUDA tensor")
+            shape = tuple(t.shape)
+            tail = (width,) if width else ()
+            if len(shape) == 1 + len(tail) and B == 1:
+                shape = (1,) + shape
+            if len(shape) != 2 + len(tail) or shape[0] != B or shape[2:] != tail:
+                gs_exc(f"{name} must be [B, n{', %d' % width if width else ''}] with B = {B}")
+            return shape[1]
+
+        n = arr(pos, "pos", 3, torch.float32)
+        if arr(vel, "vel", 3, torch.float32) != n or arr(mass, "mass", 0, torch.float32) != n:
+            gs_exc("pos, vel and mass must hold the same particles")
+        if free is not None and arr(free, "free", 0, torch.uint8) != n:
+            gs_exc("free must hold the same particles as pos")
+        _lib.check(self._lib.mpm_set_coupled_particles(
+            self._ctx, k, n, pos.data_ptr(), vel.data_ptr(), mass.data_ptr(),
+            None if free is None or k == 0 else free.data_ptr(), _stream_handle()), self._ctx,
+            "mpm_set_coupled_particles")
+        self._coupled[k] = (pos, vel, mass, free)
+
     # ------------------------------------------------------------------ kinematic links
     def set_link_poses(self, pos, quat) -> None:
         """Poses of the links that particle constraints follow (the reference reads them from the

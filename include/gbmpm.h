@@ -16,7 +16,8 @@
  *    per-scene particle count.  Ragged scenes are laid out back to back in scene order.
  *  - `stream` is a cudaStream_t passed as void*; NULL means the legacy default stream.
  *    Work is enqueued on it; no entry point synchronises the host unless it says so.
- *  - No pointer passed in is retained after the call returns.
+ *  - No pointer passed in is retained after the call returns, except the coupled particle
+ *    arrays of mpm_set_coupled_particles (the other solver's live state, read every grid op).
  */
 #ifndef GBMPM_H
 #define GBMPM_H
@@ -260,6 +261,21 @@ int mpm_get_collider_forces(mpm_ctx* ctx, double* out_host, int32_t reset, void*
  * Colliders beyond n_slots are rejected by mpm_set_colliders.  n_slots = 0 turns CPIC off.
  * Not available in pool mode. */
 int mpm_enable_cpic(mpm_ctx* ctx, int32_t n_slots, void* stream);
+
+/* MPM <-> SPH and MPM <-> PBD coupling in the grid op (legacy_coupler.py:404-498) with another
+ * solver's particles.  In every grid op, after the colliders and before the domain boundary, a node
+ * with MPM mass whose cell (|x_node - p|_inf < dx/2) holds particles of the set takes their mean
+ * velocity, and each of those particles loses delta_mv / m_i, delta_mv = m_node (v_new - v_old)
+ * (PBD: only particles with free != 0); the SPH set acts before the PBD set.
+ * pos and vel [n_scenes][n][3], mass [n_scenes][n] and free [n_scenes][n] (PBD only; NULL: all
+ * free) are device arrays that the caller keeps owning: they must stay valid until the set is
+ * replaced or removed (n = 0).  Every grid op reads pos, mass and free and updates vel in place
+ * (the caller's solver advances pos between substeps, e.g. through the split-phase entry points).
+ * Not available in pool mode. */
+#define MPM_COUPLED_SPH 0
+#define MPM_COUPLED_PBD 1
+int mpm_set_coupled_particles(mpm_ctx* ctx, int32_t kind, int64_t n, const float* pos, float* vel,
+                              const float* mass, const uint8_t* free_, void* stream);
 
 /* Soft particle-to-link constraints (mpm_solver.py:1052-1128; mpm_entity.py:631-690).
  * mpm_set_particle_constraints: for each scene b of [scene_begin, scene_end) and each particle

@@ -16,6 +16,7 @@
 //   force fields                      genesis/engine/force_fields.py (constant, wind, point, drag, vortex)
 //   rigid coupling (kinematic         legacy_coupler.py:166-218, 284-347; SDFs utils/sdf.py:119-126,
 //     colliders)                      372-378 (sphere, plane); boxes use their exact distance
+//   SPH / PBD grid coupling           legacy_coupler.py:404-498 (another solver's particles, by cell)
 //   CPIC (thin colliders)             legacy_coupler.py:503-529 (particle-side normals),
 //                                     mpm_solver.py:389-411 (P2G skips separated nodes), :445-459
 //                                     (G2P takes the collided particle velocity there)
@@ -501,6 +502,47 @@ void collide_node(int scene, const T* x, T* v, T mass, T dt, T eps) {
   }
 }
 
+// Another solver's particles coupled in the grid op, [0] SPH and [1] PBD (set by
+// oracle_set_coupled); velocities are updated in place across runs.
+struct ExtSet {
+  std::vector<double> pos, vel, mass;
+  std::vector<uint8_t> free_;
+  int64_t n = 0;
+};
+ExtSet g_ext[2];
+
+// legacy_coupler.py:404-498: the node at x (MPM mass m) takes the mean velocity of the set's
+// particles with |x - p|_inf < dx/2; each of them loses m (v_new - v_old) / m_i (PBD: free only).
+template <typename T>
+void couple_ext(const T* x, T* v, T m, T dx) {
+  for (int k = 0; k < 2; ++k) {
+    ExtSet& E = g_ext[k];
+    if (E.n == 0) continue;
+    auto inside = [&](int64_t i) {
+      for (int d = 0; d < 3; ++d)
+        if (!(std::fabs(x[d] - (T)E.pos[i * 3 + d]) < (T)0.5 * dx)) return false;
+      return true;
+    };
+    T sv[3] = {0, 0, 0};
+    int64_t cnt = 0;
+    for (int64_t i = 0; i < E.n; ++i)
+      if (inside(i)) {
+        for (int d = 0; d < 3; ++d) sv[d] += (T)E.vel[i * 3 + d];
+        ++cnt;
+      }
+    if (cnt == 0) continue;
+    T dmv[3];
+    for (int d = 0; d < 3; ++d) {
+      const T vn = sv[d] / (T)cnt;
+      dmv[d] = m * (vn - v[d]);
+      v[d] = vn;
+    }
+    for (int64_t i = 0; i < E.n; ++i)
+      if (inside(i) && (k == 0 || E.free_.empty() || E.free_[i]))
+        for (int d = 0; d < 3; ++d) E.vel[i * 3 + d] -= (double)(dmv[d] / (T)E.mass[i]);
+  }
+}
+
 // CPIC state: per particle and collider, the last SDF normal seen on the particle's side
 // (mpm_rigid_normal, legacy_coupler.py:65), zero until the first substep.
 bool g_cpic = false;
@@ -695,7 +737,7 @@ int run(const oracle_scene* sc, const oracle_material* mats, int n_mats, int64_t
       const int64_t idx[3] = {I / (ry * rz), (I / rz) % ry, I % rz};
       T v[3];
       for (int d = 0; d < 3; ++d) v[d] = (1 / gm[I]) * gp[I * 3 + d] + S.dt * S.g[d];
-      if (!g_colliders.empty() || !g_ffs.empty()) {
+      if (!g_colliders.empty() || !g_ffs.empty() || g_ext[0].n > 0 || g_ext[1].n > 0) {
         T x[3];
         for (int d = 0; d < 3; ++d) x[d] = (T)(idx[d] + S.off[d]) * S.dx;
         for (const oracle_force_field& f : g_ffs) {  // force fields (legacy_coupler.py:381-383)
@@ -705,6 +747,7 @@ int run(const oracle_scene* sc, const oracle_material* mats, int n_mats, int64_t
           for (int d = 0; d < 3; ++d) v[d] += a[d] * S.dt;
         }
         collide_node<T>(0, x, v, gm[I] / (T)1e3, S.dt, S.eps);  // rigid coupling (:389-403)
+        couple_ext<T>(x, v, gm[I] / (T)1e3, S.dx);               // SPH, then PBD (:404-498)
       }
       for (int d = 0; d < 3; ++d) {
         const T p = (T)(idx[d] + S.off[d]) * S.dx;
@@ -832,6 +875,25 @@ void oracle_set_colliders(int n, const oracle_collider* c) {
 void oracle_set_cpic(int enable) {
   g_cpic = enable != 0;
   g_cpic_normal.clear();
+}
+
+// Coupled particle set `kind` (0 SPH, 1 PBD) for the following runs: pos/vel [n][3], mass [n],
+// free [n] or NULL (PBD); n = 0 removes it.
+void oracle_set_coupled(int kind, int64_t n, const double* pos, const double* vel, const double* mass,
+                        const uint8_t* free_) {
+  ExtSet& E = g_ext[kind & 1];
+  E.n = n;
+  E.pos.assign(pos, pos + (n > 0 ? n * 3 : 0));
+  E.vel.assign(vel, vel + (n > 0 ? n * 3 : 0));
+  E.mass.assign(mass, mass + (n > 0 ? n : 0));
+  if (free_ && n > 0) E.free_.assign(free_, free_ + n);
+  else E.free_.clear();
+}
+
+// Current velocities of coupled set `kind`: out [n][3].
+void oracle_coupled_vel(int kind, double* out) {
+  const ExtSet& E = g_ext[kind & 1];
+  for (size_t i = 0; i < E.vel.size(); ++i) out[i] = E.vel[i];
 }
 
 // Force fields for the following runs (n = 0 removes them).

@@ -101,6 +101,10 @@ def load():
         lib.oracle_collider_forces.restype = None
         lib.oracle_set_cpic.argtypes = [ctypes.c_int]
         lib.oracle_set_cpic.restype = None
+        lib.oracle_set_coupled.argtypes = [ctypes.c_int, ctypes.c_int64, P, P, P, P]
+        lib.oracle_set_coupled.restype = None
+        lib.oracle_coupled_vel.argtypes = [ctypes.c_int, P]
+        lib.oracle_coupled_vel.restype = None
         _lib = lib
     return _lib
 
@@ -202,6 +206,34 @@ def set_cpic(enable: bool) -> None:
     """CPIC (MPMOptions.enable_CPIC) for the following runs; clears the particle-side collider
     normals, which otherwise persist from run to run like the particle state."""
     load().oracle_set_cpic(1 if enable else 0)
+
+
+_coupled_n = [0, 0]
+
+
+def set_coupled(kind: int, pos=None, vel=None, mass=None, free=None) -> None:
+    """Coupled particle set `kind` (0 SPH, 1 PBD) for the following runs: pos, vel [n, 3],
+    mass [n], free [n] (PBD; None: all free).  pos=None removes the set.  Their velocities are
+    updated in place by every grid op, run after run, until the set is replaced."""
+    lib = load()
+    if pos is None:
+        z = np.zeros(3)
+        lib.oracle_set_coupled(kind, 0, z.ctypes.data, z.ctypes.data, z.ctypes.data, None)
+        _coupled_n[kind] = 0
+        return
+    p = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+    v = np.ascontiguousarray(vel, dtype=np.float64).reshape(-1, 3)
+    m = np.ascontiguousarray(mass, dtype=np.float64).reshape(-1)
+    f = None if free is None else np.ascontiguousarray(free, dtype=np.uint8).reshape(-1)
+    lib.oracle_set_coupled(kind, len(p), p.ctypes.data, v.ctypes.data, m.ctypes.data,
+                           None if f is None else f.ctypes.data)
+    _coupled_n[kind] = len(p)
+
+
+def coupled_velocities(kind: int) -> np.ndarray:
+    out = np.zeros((max(1, _coupled_n[kind]), 3))
+    load().oracle_coupled_vel(kind, out.ctypes.data)
+    return out[:_coupled_n[kind]]
 
 
 def collider_forces(n: int) -> np.ndarray:

@@ -445,6 +445,67 @@ def test_cpic_thin_blade_matches_oracle(gs, oracle):
     solver.set_colliders([])
 
 
+def test_sph_pbd_grid_coupling_matches_oracle(gs, oracle):
+    """MPM <-> SPH and MPM <-> PBD coupling in the grid op (legacy_coupler.py:404-498) with two
+    caller-held particle sets: an SPH slab under an elastic cube moving down and left, a PBD slab
+    beside it with every other particle not free.  MPM particle state and both sets' velocities
+    after 40 substeps against the FP64 oracle (which finds each node's particles by the cell test
+    itself); not-free PBD particles keep their velocity; the uncoupled oracle ends elsewhere."""
+    scene, cube, mat = c1_scene(gs, size=0.12)
+    solver = scene.sim.mpm_solver
+    st = solver.get_state()
+    vel = st.vel.clone()
+    vel[..., 0] = -0.5
+    vel[..., 2] = -1.0
+    st.vel = vel
+    solver.set_state(0, st)
+    dx = 1 / 64
+    rng = np.random.default_rng(3)
+
+    def slab(ix, iy, iz, dup_every):  # one particle per node cell (some two), 0.35 dx from the node at most
+        g = np.stack(np.meshgrid(ix, iy, iz, indexing="ij"), -1).reshape(-1, 3).astype(np.float64)
+        g = np.concatenate([g, g[::dup_every]])
+        return ((g + rng.uniform(-0.35, 0.35, g.shape)) * dx).astype(np.float32)
+
+    sph = slab(np.arange(28, 37), np.arange(28, 37), np.arange(20, 22), 2)
+    pbd = slab(np.arange(26, 28), np.arange(28, 37), np.arange(22, 30), 3)
+    free = (np.arange(len(pbd)) % 2).astype(np.uint8)
+    dev = lambda a, dt=torch.float32: torch.tensor(a, dtype=dt, device="cuda").contiguous()  # noqa: E731
+    sph_pos, sph_vel, sph_m = dev(sph), dev(np.zeros_like(sph)), dev(np.full(len(sph), 2e-3))
+    pbd_pos, pbd_vel, pbd_m = dev(pbd), dev(np.tile([0.2, 0.0, 0.0], (len(pbd), 1))), dev(np.full(len(pbd), 1e-3))
+    pbd_free = dev(free, torch.uint8)
+    solver.set_coupled_particles("sph", sph_pos, sph_vel, sph_m)
+    solver.set_coupled_particles("pbd", pbd_pos, pbd_vel, pbd_m, pbd_free)
+    st0 = solver.get_state()
+    n_sub = 40
+    for _ in range(n_sub):
+        scene.step()
+    st1 = solver.get_state()
+    v_sph, v_pbd = sph_vel.double().cpu().numpy(), pbd_vel.double().cpu().numpy()
+    solver.set_coupled_particles("sph")
+    solver.set_coupled_particles("pbd")
+    sc = oracle_scene_for(oracle, solver)
+    om = [oracle.from_c_material(mat.to_c(0))]
+    try:
+        oracle.set_coupled(0, sph.astype(np.float64), np.zeros((len(sph), 3)), np.full(len(sph), np.float32(2e-3)))
+        oracle.set_coupled(1, pbd.astype(np.float64), np.tile([0.2, 0.0, 0.0], (len(pbd), 1)),
+                           np.full(len(pbd), np.float32(1e-3)), free)
+        ref, _, _ = oracle.run(sc, om, oracle_state(st0), n_sub)
+        r_sph, r_pbd = oracle.coupled_velocities(0), oracle.coupled_velocities(1)
+    finally:
+        oracle.set_coupled(0)
+        oracle.set_coupled(1)
+    plain, _, _ = oracle.run(sc, om, oracle_state(st0), n_sub)
+    assert np.abs(plain["pos"] - ref["pos"]).max() > 10 * POS_TOL
+    assert np.abs(r_sph).max() > 0.5 and np.abs(r_pbd[free == 1] - [0.2, 0.0, 0.0]).max() > 0.5
+    err = np.abs(st1.pos[0].double().cpu().numpy() - ref["pos"]).max()
+    assert err <= POS_TOL, err
+    assert np.abs(st1.vel[0].double().cpu().numpy() - ref["vel"]).max() < 5e-3
+    assert np.abs(v_sph - r_sph).max() < 5e-3, np.abs(v_sph - r_sph).max()
+    assert np.abs(v_pbd - r_pbd).max() < 5e-3, np.abs(v_pbd - r_pbd).max()
+    assert np.array_equal(v_pbd[free == 0], np.tile([0.2, 0.0, 0.0], ((free == 0).sum(), 1)).astype(np.float32))
+
+
 def test_force_fields_match_oracle(gs, oracle):
     """Force fields in the grid op (legacy_coupler.py:381-383, engine/force_fields.py): constant,
     wind, point, drag and vortex fields (one left inactive) against the FP64 oracle."""
