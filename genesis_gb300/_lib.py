@@ -115,10 +115,13 @@ class MpmForceField(ctypes.Structure):
         ("falloff_min", c_double),
         ("falloff_max", c_double),
         ("damping", c_double),
+        ("frequency", c_double),
+        ("seed", ctypes.c_uint64),
+        ("perm", (ctypes.c_uint8 * 256) * 3),
     ]
 
 
-FF_CONSTANT, FF_WIND, FF_POINT, FF_DRAG, FF_VORTEX = 0, 1, 2, 3, 4
+FF_CONSTANT, FF_WIND, FF_POINT, FF_DRAG, FF_VORTEX, FF_NOISE, FF_TURBULENCE = 0, 1, 2, 3, 4, 5, 6
 
 
 class MpmSceneConfig(ctypes.Structure):

@@ -78,6 +78,7 @@ struct mpm_ctx {
   uint32_t* d_pin = nullptr;
   ConstraintDev* d_cons = nullptr;  // particle constraints by reference row (allocated on first use)
   ForceFieldDev* d_ffs = nullptr;      // force fields (capacity MAX_FORCE_FIELDS once allocated)
+  unsigned long long* d_ff_step = nullptr;  // substeps since the force fields were set
   int32_t n_ffs = 0;
   ColliderDev* d_colliders = nullptr;  // kinematic colliders (capacity MAX_COLLIDERS once allocated)
   double* d_collider_acc = nullptr;    // [MAX_COLLIDERS][6]
@@ -196,6 +197,7 @@ KParams make_params(mpm_ctx* ctx, int src, int dst, int g) {
   P.cpic_mask = ctx->d_cpic_mask;
   P.ext[0] = ctx->ext[0];
   P.ext[1] = ctx->ext[1];
+  P.ff_step = ctx->d_ff_step;
   P.scan_sync = ctx->d_scan_sync;
   P.n_tiles = ctx->n_tiles;
   P.pin = ctx->d_pin;
@@ -302,6 +304,7 @@ int launch_post(mpm_ctx* ctx, int c, cudaStream_t s, bool fuse_grid = false) {
   P.steps = ctx->d_steps;
   P.fuse_grid = fuse_grid ? 1 : 0;
   P.nlist_reset = fuse_grid ? P.nlist_other : nullptr;
+  P.ff_step_advance = 1;
   ctx->grid_momentum[c] = fuse_grid;
   {
     Timer t(ctx, s, KT_G2P);
@@ -703,6 +706,7 @@ int mpm_ctx_destroy(mpm_ctx* ctx) {
   if (ctx->d_cons) cudaFree(ctx->d_cons);
   if (ctx->d_colliders) cudaFree(ctx->d_colliders);
   if (ctx->d_ffs) cudaFree(ctx->d_ffs);
+  if (ctx->d_ff_step) cudaFree(ctx->d_ff_step);
   if (ctx->d_collider_acc) cudaFree(ctx->d_collider_acc);
   if (ctx->d_cpic_mask) cudaFree(ctx->d_cpic_mask);
   for (int k = 0; k < 2; ++k) {
@@ -906,7 +910,7 @@ int mpm_set_force_fields(mpm_ctx* ctx, int32_t n, const mpm_force_field* fields)
   std::vector<ForceFieldDev> h((size_t)n);
   for (int32_t i = 0; i < n; ++i) {
     const mpm_force_field& f = fields[i];
-    if (f.type < MPM_FF_CONSTANT || f.type > MPM_FF_VORTEX) return fail(ctx, MPM_ERR_BAD_ARG, "unknown force field");
+    if (f.type < MPM_FF_CONSTANT || f.type > MPM_FF_TURBULENCE) return fail(ctx, MPM_ERR_BAD_ARG, "unknown force field");
     ForceFieldDev& d = h[(size_t)i];
     std::memset(&d, 0, sizeof(d));
     d.type = f.type;
@@ -926,15 +930,21 @@ int mpm_set_force_fields(mpm_ctx* ctx, int32_t n, const mpm_force_field* fields)
     d.falloff_min = (float)f.falloff_min;
     d.falloff_max = (float)f.falloff_max;  // +inf stays +inf
     d.damping = (float)f.damping;
+    d.frequency = (float)f.frequency;
+    d.seed = (unsigned long long)f.seed;
+    std::memcpy(d.perm, f.perm, sizeof(d.perm));
   }
   CK(cudaSetDevice(ctx->device));
   if (!ctx->d_ffs && n > 0) {
     cudaError_t e = cudaMalloc((void**)&ctx->d_ffs, sizeof(ForceFieldDev) * MAX_FORCE_FIELDS);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&ctx->d_ff_step, sizeof(unsigned long long));
     if (e != cudaSuccess) {
-      ctx->d_ffs = nullptr;
+      cudaGetLastError();
       return fail(ctx, MPM_ERR_OOM, "force-field table allocation failed");
     }
+    drop_graph(ctx);  // captured substeps now advance the noise counter
   }
+  if (ctx->d_ff_step) CK(cudaMemsetAsync(ctx->d_ff_step, 0, sizeof(unsigned long long), ctx->cs));
   if (n > 0) {
     CK(cudaMemcpyAsync(ctx->d_ffs, h.data(), sizeof(ForceFieldDev) * n, cudaMemcpyHostToDevice, ctx->cs));
     CK(cudaStreamSynchronize(ctx->cs));

@@ -470,6 +470,7 @@ __global__ void k_perm(KParams P) {
   for (int64_t i = grid_stride_begin(); i < n; i += grid_stride_step())
     P.perm[P.offset[P.key[i]] + P.rank[i]] = (int32_t)i;
   if (P.nlist_reset && blockIdx.x == 0 && threadIdx.x == 0) *P.nlist_reset = 0;  // cleared by the fused G2P
+  if (P.ff_step && P.ff_step_advance && blockIdx.x == 0 && threadIdx.x == 0) *P.ff_step += 1;  // end of a substep
   if (P.steps && blockIdx.x == 0)  // end of a substep: count down per-scene substep budgets
     for (int s = threadIdx.x; s < P.n_scenes; s += blockDim.x)
       if (P.steps[s] > 0) P.steps[s] -= 1;
@@ -484,9 +485,53 @@ __device__ __forceinline__ void rot(const float* q, const float* v, float* o) { 
   o[2] = v[0] * (-2.f * w * y + 2.f * x * z) + v[1] * (2.f * w * x + 2.f * y * z) + v[2] * (w * w - x * x - y * y + z * z);
 }
 
+// splitmix64 (Steele, Lea and Flood 2014): one step of the generator as a 64-bit mixing function.
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+// Perlin's improved noise (force_fields.py:441-544) over a 256-entry permutation p, at frequency f.
+__device__ __forceinline__ float perlin_fade(float t) { return t * t * t * (t * (t * 6.f - 15.f) + 10.f); }
+__device__ __forceinline__ float perlin_lerp(float t, float a, float b) { return a + t * (b - a); }
+__device__ __forceinline__ float perlin_grad(int h, float x, float y, float z) {
+  h &= 15;
+  const float u = h < 8 ? x : y;
+  float v = y;
+  if (h >= 4) v = (h == 12 || h == 14) ? x : z;
+  return ((h & 1) == 0 ? u : -u) + ((h & 2) == 0 ? v : -v);
+}
+__device__ float perlin(const uint8_t* p, float f, float x, float y, float z) {
+  x *= f;
+  y *= f;
+  z *= f;
+  const float fx = floorf(x), fy = floorf(y), fz = floorf(z);
+  const int X = (int)fx & 255, Y = (int)fy & 255, Z = (int)fz & 255;
+  x -= fx;
+  y -= fy;
+  z -= fz;
+  const float u = perlin_fade(x), v = perlin_fade(y), w = perlin_fade(z);
+  // the reference's table is the permutation written twice (512 entries): index & 255
+  const int A = p[X] + Y, AA = p[A & 255] + Z, AB = p[(A + 1) & 255] + Z;
+  const int B = p[(X + 1) & 255] + Y, BA = p[B & 255] + Z, BB = p[(B + 1) & 255] + Z;
+  return perlin_lerp(
+      w,
+      perlin_lerp(v, perlin_lerp(u, perlin_grad(p[AA & 255], x, y, z), perlin_grad(p[BA & 255], x - 1.f, y, z)),
+                  perlin_lerp(u, perlin_grad(p[AB & 255], x, y - 1.f, z), perlin_grad(p[BB & 255], x - 1.f, y - 1.f, z))),
+      perlin_lerp(v,
+                  perlin_lerp(u, perlin_grad(p[(AA + 1) & 255], x, y, z - 1.f),
+                              perlin_grad(p[(BA + 1) & 255], x - 1.f, y, z - 1.f)),
+                  perlin_lerp(u, perlin_grad(p[(AB + 1) & 255], x, y - 1.f, z - 1.f),
+                              perlin_grad(p[(BB + 1) & 255], x - 1.f, y - 1.f, z - 1.f))));
+}
+
 // engine/force_fields.py _get_acc of each field type (Constant :73, Wind :122, Point :178,
-// Drag :220, Vortex :319) at node position x with the current node velocity v.
-__device__ __forceinline__ void ff_acc(const ForceFieldDev& f, const float* x, const float* v, float eps, float* a) {
+// Drag :220, Noise :243, Vortex :319, Turbulence :400) at node position x (world node index gw of
+// scene `scene`) with the current node velocity v; `step` counts substeps for the noise draws.
+__device__ __forceinline__ void ff_acc(const ForceFieldDev& f, const float* x, const float* v, float eps, float* a,
+                                       int32_t scene, const int* gw, unsigned long long step) {
   a[0] = a[1] = a[2] = 0.f;
   if (f.type == MPM_FF_CONSTANT) {
     for (int k = 0; k < 3; ++k) a[k] = f.dir[k] * f.strength;
@@ -517,6 +562,19 @@ __device__ __forceinline__ void ff_acc(const ForceFieldDev& f, const float* x, c
     a[0] = fall * (f.s_perp * -ry + f.s_radial * -rx) - f.damping * v[0];
     a[1] = fall * (f.s_perp * rx + f.s_radial * -ry) - f.damping * v[1];
     a[2] = fall * 0.f - f.damping * v[2];
+  } else if (f.type == MPM_FF_NOISE) {
+    const unsigned long long node = ((unsigned long long)((uint32_t)gw[0] & 0x1fffffu)) |
+                                    ((unsigned long long)((uint32_t)gw[1] & 0x1fffffu) << 21) |
+                                    ((unsigned long long)((uint32_t)gw[2] & 0x1fffffu) << 42);
+    const unsigned long long h =
+        splitmix64(splitmix64(splitmix64(splitmix64(f.seed) ^ step) ^ (unsigned long long)(uint32_t)scene) ^ node);
+    for (int k = 0; k < 3; ++k) {
+      const float u = (float)(splitmix64(h + (unsigned long long)k) >> 40) * 0x1p-24f;
+      a[k] = (u * 2.f - 1.f) * f.strength;
+    }
+  } else if (f.type == MPM_FF_TURBULENCE) {
+    for (int k = 0; k < 3; ++k) a[k] = perlin(f.perm[k], f.frequency, x[0], x[1], x[2]) * f.strength;
+    for (int k = 0; k < 3; ++k) a[k] += (a[k] - v[k]) * f.flow;
   }
 }
 
@@ -1281,6 +1339,7 @@ __global__ void __launch_bounds__(256) k_grid_op(KParams P) {
     if (ln == 0) P.flags_other[blk] = 0;
   }
   const int n_cur = *P.nlist;
+  const unsigned long long step = P.ff_step ? *P.ff_step : 0ull;
   for (int i = blockIdx.x * (blockDim.x >> 6) + sub; i < n_cur; i += per_iter) {
     const int32_t blk = P.list[i];
     const SceneDev& S = P.scenes[P.block_scene[blk]];
@@ -1308,7 +1367,8 @@ __global__ void __launch_bounds__(256) k_grid_op(KParams P) {
         for (int fi = 0; fi < P.n_ffs; ++fi) {
           if (!P.ffs[fi].active) continue;
           float a[3];
-          ff_acc(P.ffs[fi], x, v, S.eps, a);
+          const int gw[3] = {g[0] + S.offset[0], g[1] + S.offset[1], g[2] + S.offset[2]};
+          ff_acc(P.ffs[fi], x, v, S.eps, a, P.block_scene[blk], gw, step);
           for (int k = 0; k < 3; ++k) v[k] += a[k] * S.dt;
         }
         collide_node(P, S, P.block_scene[blk], x, v, q.w / 1e3f);

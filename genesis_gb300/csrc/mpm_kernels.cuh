@@ -92,7 +92,9 @@ struct ForceFieldDev {
   int32_t type, active, pad0, pad1;
   float dir[3], center[3];
   float strength, radius, falloff_pow, flow, linear, quadratic;
-  float s_perp, s_radial, falloff_min, falloff_max, damping, pad2;
+  float s_perp, s_radial, falloff_min, falloff_max, damping, frequency;
+  unsigned long long seed;  // NOISE
+  uint8_t perm[3][256];     // TURBULENCE
 };
 
 // Another solver's particles coupled through the grid op (SPH or PBD), caller-owned device arrays.
@@ -156,6 +158,8 @@ struct KParams {
   int32_t cpic_slots;          // CPIC collider slots (normal planes PF_CPIC + 3 * slot); 0: CPIC off
   uint32_t* cpic_mask;         // CPIC: per slot, the particle's nodes behind a collider (bit ox*9+oy*3+oz)
   ExtSetDev ext[2];            // coupled particle sets: [0] SPH, [1] PBD (applied in that order)
+  unsigned long long* ff_step; // substeps since the force fields were set (NOISE draws), or null
+  int32_t ff_step_advance;     // k_perm counts the substep (set only for the end of a substep)
 };
 
 // Block key of a world position; returns false if the stencil would leave the grid.

@@ -3,7 +3,7 @@
 `scene.add_force_field(ff)` registers a field; it acts on grid velocities as
 v += acc(x, v) * dt after gravity (legacy_coupler.py:381-383), on the device.  Fields start
 inactive, as in the reference; `activate()` / `deactivate()` take effect at the next substep.
-Noise, Turbulence and Custom (a user Quadrants function) are not provided.
+Custom (a user Quadrants function) is not provided: it needs a device-code compiler at run time.
 """
 
 from __future__ import annotations
@@ -182,3 +182,66 @@ class Vortex(ForceField):
     @property
     def center(self):
         return self._center
+
+
+class Noise(ForceField):
+    """force_fields.py:232-259: acc = strength * (2u - 1) per node, component and substep, u uniform
+    in [0, 1).  The draws come from a counter-based hash (splitmix64 over seed, substep, scene, node
+    and component) instead of the reference's generator state: the same distribution, repeatable
+    for a given seed, not the reference's numbers."""
+
+    _type = _lib.FF_NOISE
+
+    def __init__(self, strength=1.0, seed=0):
+        super().__init__()
+        self._strength = strength
+        self._seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+
+    def _fill(self, f):
+        f.strength = float(self._strength)
+        f.seed = self._seed
+
+    @property
+    def strength(self):
+        return self._strength
+
+
+def perlin_permutation(seed, seed_offset, wrap_size=256):
+    """PerlinNoiseField's table (force_fields.py:448-460): the identity, shuffled by numpy's global
+    generator seeded with seed + seed_offset when a seed is given (the global state is restored)."""
+    perm = np.arange(wrap_size, dtype=np.int32)
+    if seed is not None:
+        state = np.random.get_state()
+        np.random.seed(seed + seed_offset)
+        np.random.shuffle(perm)
+        np.random.set_state(state)
+    return perm
+
+
+class Turbulence(ForceField):
+    """force_fields.py:372-421: acc_k = strength * perlin_k(frequency * x) for three Perlin noise
+    fields (seed offsets 0, 1, 2), then acc += (acc - v) * flow."""
+
+    _type = _lib.FF_TURBULENCE
+
+    def __init__(self, strength=1.0, frequency=3, flow=0.0, seed=None):
+        super().__init__()
+        self._strength = strength
+        self._frequency = frequency
+        self._flow = flow
+        self._perms = [perlin_permutation(seed, k) for k in range(3)]
+
+    def _fill(self, f):
+        f.strength = float(self._strength)
+        f.frequency = float(self._frequency)
+        f.flow = float(self._flow)
+        for k in range(3):
+            f.perm[k][:] = [int(v) for v in self._perms[k]]
+
+    @property
+    def strength(self):
+        return self._strength
+
+    @property
+    def frequency(self):
+        return self._frequency

@@ -195,6 +195,15 @@ int mpm_get_grid(mpm_ctx* ctx, int64_t scene, float* out, void* stream);
  *   VORTEX:   about the z axis through center: falloff 1 below falloff_min, 1/(r - falloff_min + 1)^
  *             falloff_pow below falloff_max, 0 beyond; acc = falloff (strength_perpendicular
  *             (-ry, rx, 0) + strength_radial (-rx, -ry, 0)) - damping v
+ *   NOISE:    (force_fields.py:232-259) acc_k = strength (2 u_k - 1), u_k uniform in [0, 1) drawn per
+ *             node, component and substep: the top 24 bits of splitmix64 chained over (seed, substep
+ *             counter, scene, world node index, component).  The counter counts substeps since the
+ *             last mpm_set_force_fields.  Same distribution as the reference's qd.random, not the
+ *             same numbers.
+ *   TURBULENCE: (force_fields.py:372-421, 441-544) acc_k = strength perlin(perm[k], frequency, x),
+ *             Perlin's improved noise over the 256-entry permutation perm[k] (the field's three
+ *             PerlinNoiseField tables, built by the caller as the reference builds them);
+ *             acc += (acc - v) flow
  * Inactive fields (active = 0) are skipped.  With any field set, the grid op runs as its own
  * kernel. */
 #define MPM_FF_CONSTANT 0
@@ -202,6 +211,8 @@ int mpm_get_grid(mpm_ctx* ctx, int64_t scene, float* out, void* stream);
 #define MPM_FF_POINT 2
 #define MPM_FF_DRAG 3
 #define MPM_FF_VORTEX 4
+#define MPM_FF_NOISE 5
+#define MPM_FF_TURBULENCE 6
 typedef struct mpm_force_field {
   int32_t type;
   int32_t active;
@@ -210,6 +221,9 @@ typedef struct mpm_force_field {
   double strength, radius, falloff_pow, flow;
   double linear, quadratic;
   double strength_perpendicular, strength_radial, falloff_min, falloff_max, damping;
+  double frequency;      /* TURBULENCE */
+  uint64_t seed;         /* NOISE */
+  uint8_t perm[3][256];  /* TURBULENCE: permutation tables of the x, y, z noise fields */
 } mpm_force_field;
 
 /* Replace the force-field set (n may be 0); host array, copied before returning. */

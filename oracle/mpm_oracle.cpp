@@ -63,11 +63,14 @@ typedef struct oracle_collider {
 
 // External acceleration field: same layout as mpm_force_field of the library header.
 typedef struct oracle_force_field {
-  int32_t type;  // 0 constant, 1 wind, 2 point, 3 drag, 4 vortex
+  int32_t type;  // 0 constant, 1 wind, 2 point, 3 drag, 4 vortex, 5 noise, 6 turbulence
   int32_t active;
   double direction[3], center[3];
   double strength, radius, falloff_pow, flow, linear, quadratic;
   double strength_perpendicular, strength_radial, falloff_min, falloff_max, damping;
+  double frequency;      // 6 turbulence
+  uint64_t seed;         // 5 noise
+  uint8_t perm[3][256];  // 6 turbulence: the x, y, z noise fields' permutations
 } oracle_force_field;
 
 typedef struct oracle_material {
@@ -370,9 +373,51 @@ std::vector<double> g_collider_acc;
 
 std::vector<oracle_force_field> g_ffs;
 
-// engine/force_fields.py _get_acc: Constant :73, Wind :122, Point :178, Drag :220, Vortex :319.
+// Substeps since the force fields were set: the noise field's draw counter.
+uint64_t g_ff_step = 0;
+
+// splitmix64 (Steele, Lea and Flood 2014) as a mixing function: the noise field's draws.
+inline uint64_t splitmix64(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+// Perlin's improved noise over a 256-entry permutation (force_fields.py:441-544; the reference's
+// 512-entry table is the permutation twice).
 template <typename T>
-void ff_acc(const oracle_force_field& f, const T* x, const T* v, T eps, T* a) {
+T perlin(const uint8_t* p, T f, T x, T y, T z) {
+  auto fade = [](T t) { return t * t * t * (t * (t * 6 - 15) + 10); };
+  auto lerp = [](T t, T a, T b) { return a + t * (b - a); };
+  auto grad = [](int h, T gx, T gy, T gz) {
+    h &= 15;
+    const T u = h < 8 ? gx : gy;
+    const T w = h < 4 ? gy : ((h == 12 || h == 14) ? gx : gz);
+    return ((h & 1) == 0 ? u : -u) + ((h & 2) == 0 ? w : -w);
+  };
+  x *= f;
+  y *= f;
+  z *= f;
+  const T fx = std::floor(x), fy = std::floor(y), fz = std::floor(z);
+  const int X = (int)fx & 255, Y = (int)fy & 255, Z = (int)fz & 255;
+  x -= fx;
+  y -= fy;
+  z -= fz;
+  const T u = fade(x), v = fade(y), w = fade(z);
+  auto P = [&](int i) { return (int)p[i & 255]; };
+  const int A = P(X) + Y, AA = P(A) + Z, AB = P(A + 1) + Z, B = P(X + 1) + Y, BA = P(B) + Z, BB = P(B + 1) + Z;
+  return lerp(w,
+              lerp(v, lerp(u, grad(P(AA), x, y, z), grad(P(BA), x - 1, y, z)),
+                   lerp(u, grad(P(AB), x, y - 1, z), grad(P(BB), x - 1, y - 1, z))),
+              lerp(v, lerp(u, grad(P(AA + 1), x, y, z - 1), grad(P(BA + 1), x - 1, y, z - 1)),
+                   lerp(u, grad(P(AB + 1), x, y - 1, z - 1), grad(P(BB + 1), x - 1, y - 1, z - 1))));
+}
+
+// engine/force_fields.py _get_acc: Constant :73, Wind :122, Point :178, Drag :220, Noise :243,
+// Vortex :319, Turbulence :400; gw is the node's world index (noise draws).
+template <typename T>
+void ff_acc(const oracle_force_field& f, const T* x, const T* v, T eps, T* a, const int64_t* gw) {
   a[0] = a[1] = a[2] = 0;
   const T dir[3] = {(T)f.direction[0], (T)f.direction[1], (T)f.direction[2]};
   const T r[3] = {x[0] - (T)f.center[0], x[1] - (T)f.center[1], x[2] - (T)f.center[2]};
@@ -402,6 +447,17 @@ void ff_acc(const oracle_force_field& f, const T* x, const T* v, T eps, T* a) {
     a[0] = fall * (sp * -r[1] + sr * -r[0]) - dm * v[0];
     a[1] = fall * (sp * r[0] + sr * -r[1]) - dm * v[1];
     a[2] = -dm * v[2];
+  } else if (f.type == 5) {  // uniform in [-strength, strength) per node, component and substep
+    const uint64_t node = ((uint64_t)((uint32_t)gw[0] & 0x1fffffu)) | ((uint64_t)((uint32_t)gw[1] & 0x1fffffu) << 21) |
+                          ((uint64_t)((uint32_t)gw[2] & 0x1fffffu) << 42);
+    const uint64_t h = splitmix64(splitmix64(splitmix64(splitmix64(f.seed) ^ g_ff_step) ^ 0ull) ^ node);
+    for (int k = 0; k < 3; ++k) {
+      const T u = (T)(splitmix64(h + (uint64_t)k) >> 40) * (T)(1.0 / 16777216.0);
+      a[k] = (u * 2 - 1) * (T)f.strength;
+    }
+  } else if (f.type == 6) {
+    for (int k = 0; k < 3; ++k) a[k] = perlin<T>(f.perm[k], (T)f.frequency, x[0], x[1], x[2]) * (T)f.strength;
+    for (int k = 0; k < 3; ++k) a[k] += (a[k] - v[k]) * (T)f.flow;
   }
 }
 
@@ -743,7 +799,8 @@ int run(const oracle_scene* sc, const oracle_material* mats, int n_mats, int64_t
         for (const oracle_force_field& f : g_ffs) {  // force fields (legacy_coupler.py:381-383)
           if (!f.active) continue;
           T a[3];
-          ff_acc<T>(f, x, v, S.eps, a);
+          const int64_t gw[3] = {idx[0] + S.off[0], idx[1] + S.off[1], idx[2] + S.off[2]};
+          ff_acc<T>(f, x, v, S.eps, a, gw);
           for (int d = 0; d < 3; ++d) v[d] += a[d] * S.dt;
         }
         collide_node<T>(0, x, v, gm[I] / (T)1e3, S.dt, S.eps);  // rigid coupling (:389-403)
@@ -815,6 +872,7 @@ int run(const oracle_scene* sc, const oracle_material* mats, int n_mats, int64_t
       std::memcpy(C + i * 9, nC.a, sizeof(T) * 9);
     }
     if (nan) return 4;
+    ++g_ff_step;  // the noise field draws anew every substep
   }
   return 0;
 }
@@ -897,7 +955,10 @@ void oracle_coupled_vel(int kind, double* out) {
 }
 
 // Force fields for the following runs (n = 0 removes them).
-void oracle_set_force_fields(int n, const oracle_force_field* f) { g_ffs.assign(f, f + n); }
+void oracle_set_force_fields(int n, const oracle_force_field* f) {
+  g_ffs.assign(f, f + n);
+  g_ff_step = 0;
+}
 
 // Reaction force and torque accumulated on each collider: out [n][6].
 void oracle_collider_forces(double* out) {

@@ -557,6 +557,49 @@ def test_force_fields_match_oracle(gs, oracle):
     assert np.abs(solver.get_state().vel[0].double().cpu().numpy() - ref2["vel"]).max() <= 1e-4
 
 
+def test_noise_and_turbulence_fields_match_oracle(gs, oracle):
+    """Turbulence (Perlin noise over numpy-shuffled permutations, force_fields.py:372-421,
+    441-544) and Noise (uniform draws per node, component and substep from a counter-based hash,
+    force_fields.py:232-259) in the grid op against the FP64 oracle, which restates both (the same
+    draws); the fields change the motion, and two noise seeds give different motion."""
+    ff = gs.force_fields
+    scene = gs.Scene(
+        sim_options=gs.options.SimOptions(dt=2e-4, substeps=1),
+        mpm_options=gs.options.MPMOptions(lower_bound=(0, 0, 0), upper_bound=(1, 1, 1), grid_density=64,
+                                          particle_size=1 / 128),
+    )
+    mat = gs.materials.MPM.Elastic(E=3e5, nu=0.2, rho=1000, sampler="regular")
+    scene.add_entity(material=mat, morph=gs.morphs.Box(pos=(0.5, 0.5, 0.4), size=(0.12,) * 3))
+    fields = [ff.Turbulence(strength=30.0, frequency=5, flow=0.3, seed=11), ff.Noise(strength=20.0, seed=7)]
+    for f in fields:
+        scene.add_force_field(f)
+    scene.build()
+    for f in fields:
+        f.activate()
+    solver = scene.sim.mpm_solver
+    st0 = solver.get_state()
+    n_sub = 40
+    for _ in range(n_sub):
+        scene.step()
+    st1 = solver.get_state()
+    sc = oracle_scene_for(oracle, solver)
+    om = [oracle.from_c_material(mat.to_c(0))]
+    other = [fields[0].to_c(), ff.Noise(strength=20.0, seed=8).to_c()]
+    other[1].active = 1
+    try:
+        oracle.set_force_fields([f.to_c() for f in fields])
+        ref, _, _ = oracle.run(sc, om, oracle_state(st0), n_sub)
+        oracle.set_force_fields(other)
+        ref_seed, _, _ = oracle.run(sc, om, oracle_state(st0), n_sub)
+    finally:
+        oracle.set_force_fields([])
+    ref_plain, _, _ = oracle.run(sc, om, oracle_state(st0), n_sub)
+    assert np.abs(ref["vel"] - ref_plain["vel"]).max() > 1e-2  # the fields act
+    assert np.abs(ref["vel"] - ref_seed["vel"]).max() > 1e-3   # the noise seed matters
+    assert np.abs(st1.pos[0].double().cpu().numpy() - ref["pos"]).max() <= POS_TOL
+    assert np.abs(st1.vel[0].double().cpu().numpy() - ref["vel"]).max() <= 1e-3
+
+
 def test_full_size_conservation_properties(gs):
     """The ~1M-particle three-material scene of the benchmark (too large for the oracle in a test):
     size-independent properties.  Without gravity and away from the walls, total mass on the grid
