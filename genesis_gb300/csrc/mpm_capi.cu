@@ -67,6 +67,8 @@ struct mpm_ctx {
   int32_t* d_count = nullptr;
   int32_t* d_offset = nullptr;
   int32_t* d_perm = nullptr;
+  uint8_t* d_cell8 = nullptr;
+  uint8_t* d_slot_cell = nullptr;
   int4* d_items = nullptr;
   int32_t* d_nitems = nullptr;
   int2* d_partials = nullptr;
@@ -184,6 +186,8 @@ KParams make_params(mpm_ctx* ctx, int src, int dst, int g) {
   P.count = ctx->d_count;
   P.offset = ctx->d_offset;
   P.perm = ctx->d_perm;
+  P.cell8 = ctx->d_cell8;
+  P.slot_cell = ctx->d_slot_cell;
   P.items = ctx->d_items;
   P.n_items = ctx->d_nitems;
   P.partials = ctx->d_partials;
@@ -522,6 +526,8 @@ static int ctx_alloc_init(mpm_ctx* ctx, int32_t device, const std::vector<int32_
     if ((r = dalloc(ctx, &ctx->d_key, ctx->cap))) break;
     if ((r = dalloc(ctx, &ctx->d_rank, ctx->cap))) break;
     if ((r = dalloc(ctx, &ctx->d_perm, ctx->cap))) break;
+    if ((r = dalloc(ctx, &ctx->d_cell8, ctx->cap))) break;
+    if ((r = dalloc(ctx, &ctx->d_slot_cell, ctx->cap))) break;
     if ((r = dalloc(ctx, &ctx->d_count, ctx->K + 2))) break;
     if ((r = dalloc(ctx, &ctx->d_offset, ctx->K + 2))) break;
     if ((r = dalloc(ctx, &ctx->d_items, ctx->max_items))) break;

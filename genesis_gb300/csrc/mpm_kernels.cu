@@ -232,6 +232,7 @@ __global__ void __launch_bounds__(256) k_keys(KParams P) {
     const int64_t i = base + lane;
     const bool valid = i < P.n;
     int32_t key = (int32_t)P.K;
+    int cell = BLK_NODES;
     if (valid) {
       const uint32_t info = ld_info(D, cap, i);
       if (info & INFO_DEAD) {
@@ -242,8 +243,12 @@ __global__ void __launch_bounds__(256) k_keys(KParams P) {
         int b[3];
 #pragma unroll
         for (int d = 0; d < 3; ++d) x[d] = D[(int64_t)(PF_POS + d) * cap + i];
-        if (stencil_origin(S, x, b)) key = (int32_t)block_of(S, b[0], b[1], b[2]);
-        else atomicOr(P.status, (isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2])) ? 2u : 1u);
+        if (stencil_origin(S, x, b)) {
+          key = (int32_t)block_of(S, b[0], b[1], b[2]);
+          cell = ((b[0] & 3) * 4 + (b[1] & 3)) * 4 + (b[2] & 3);
+        } else {
+          atomicOr(P.status, (isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2])) ? 2u : 1u);
+        }
       }
     }
     const unsigned am = __ballot_sync(0xffffffffu, valid);
@@ -256,6 +261,7 @@ __global__ void __launch_bounds__(256) k_keys(KParams P) {
       r += __popc(peers & ((1u << lane) - 1u));
       P.key[i] = key;
       P.rank[i] = r;
+      P.cell8[i] = (uint8_t)cell;
     }
   }
 }
@@ -467,8 +473,11 @@ __global__ void __launch_bounds__(1024) k_scan_single(KParams P) {
 
 __global__ void k_perm(KParams P) {
   const int64_t n = P.n_dev ? *P.n_dev : P.n;
-  for (int64_t i = grid_stride_begin(); i < n; i += grid_stride_step())
-    P.perm[P.offset[P.key[i]] + P.rank[i]] = (int32_t)i;
+  for (int64_t i = grid_stride_begin(); i < n; i += grid_stride_step()) {
+    const int64_t dst = P.offset[P.key[i]] + P.rank[i];
+    P.perm[dst] = (int32_t)i;
+    P.slot_cell[dst] = P.cell8[i];  // P2G reads each slot's cell without gathering its position
+  }
   if (P.nlist_reset && blockIdx.x == 0 && threadIdx.x == 0) *P.nlist_reset = 0;  // cleared by the fused G2P
   if (P.ff_step && P.ff_step_advance && blockIdx.x == 0 && threadIdx.x == 0) *P.ff_step += 1;  // end of a substep
   if (P.steps && blockIdx.x == 0)  // end of a substep: count down per-scene substep budgets
@@ -859,7 +868,9 @@ __device__ __forceinline__ void block_origin(const SceneDev& S, int64_t key, int
 }  // namespace
 
 // Per work item (one grid block's bucket, up to `chunk` <= P2G_MAX_CHUNK particles):
-//  1. counting-sort the item's particles by cell in shared memory (native integer atomics);
+//  1. counting-sort the item's particles by cell in shared memory (native integer atomics); the
+//     cell of each slot comes from the G2P (or re-keying) that keyed the particle, in slot order
+//     (k_perm), and its old slot is kept in shared memory for step 2;
 //  2. in slot order (coalesced gathers through perm): compute_F_tmp + svd + material update
 //     + stress (mpm_solver.py:293-307, 339-377), write the particle to its slot, and leave its
 //     scatter parameters (fx, mass, q = m v - sum_k a_k fx_k, a_k = dx * affine[:,k]) in a
@@ -881,6 +892,7 @@ __device__ __forceinline__ void p2g_body(const KParams& P) {
   float4* s_tile = reinterpret_cast<float4*>(p2g_smem);
   float4* s_rec = s_tile + nw * TILE_NODES;
   uint32_t* s_cr = reinterpret_cast<uint32_t*>(s_rec + P2G_REC * P.chunk);
+  int32_t* s_si = reinterpret_cast<int32_t*>(s_cr + P.chunk);  // old slot of each item particle
   const int64_t cap = P.cap;
   const float* Sx = P.src;
   float* Dx = P.dst;
@@ -907,12 +919,8 @@ __device__ __forceinline__ void p2g_body(const KParams& P) {
     block_origin(S, item.x, org);
     // 1. cell ranks
     for (int j = threadIdx.x; j < cnt; j += T) {
-      const int64_t si = P.perm[item.y + j];
-      float x[3];
-      int tb[3];
-#pragma unroll
-      for (int d = 0; d < 3; ++d) x[d] = Sx[(int64_t)(PF_POS + d) * cap + si];
-      const int cell = local_cell(S, x, org, tb);
+      s_si[j] = P.perm[item.y + j];
+      const int cell = P.slot_cell[item.y + j];  // from the G2P (or re-keying) that keyed it
       const int r = atomicAdd(&s_cnt[cell], 1);
       s_cr[j] = ((uint32_t)cell << 16) | (uint32_t)r;
     }
@@ -946,7 +954,7 @@ __device__ __forceinline__ void p2g_body(const KParams& P) {
       if (j >= cnt) continue;
       const int p = (cell < 32 ? oa : (cell < BLK_NODES ? ob : tot_in)) + (int)(cr & 0xffffu);
       const int64_t slot = item.y + j;
-      const int64_t si = P.perm[slot];
+      const int64_t si = s_si[j];
       Particle pt;
       load_particle(P, Sx, si, pt);
       bool scattered = false;
@@ -1143,7 +1151,7 @@ __global__ void __launch_bounds__(P2G_MAX_THREADS) k_p2g_cpic(KParams P) { p2g_b
 // same work items as the P2G that wrote the particles (so every item's particles read one
 // 6^3 node tile, staged once in shared memory), followed by the bucket key of the new
 // position and a warp-aggregated rank within the bucket.
-__device__ __forceinline__ void add_rank(const KParams& P, bool valid, int32_t key, int64_t i, int lane) {
+__device__ __forceinline__ void add_rank(const KParams& P, bool valid, int32_t key, int64_t i, int lane, int cell) {
   const unsigned am = __ballot_sync(0xffffffffu, valid);
   if (valid) {
     const unsigned peers = __match_any_sync(am, key);
@@ -1154,6 +1162,7 @@ __device__ __forceinline__ void add_rank(const KParams& P, bool valid, int32_t k
     r += __popc(peers & ((1u << lane) - 1u));
     P.key[i] = key;
     P.rank[i] = r;
+    P.cell8[i] = (uint8_t)cell;
   }
 }
 
@@ -1187,6 +1196,7 @@ __device__ __forceinline__ void g2p_body(const KParams& P) {
         const bool valid = q < cnt;
         const int64_t i = item.y + q;
         int32_t key = kInactive;
+        int cellk = BLK_NODES;
         if (valid) {
           const uint32_t info = ld_info(D, cap, i);
           if (info & INFO_DEAD) key = kDead;
@@ -1195,10 +1205,13 @@ __device__ __forceinline__ void g2p_body(const KParams& P) {
             float x[3];
             int b[3];
             for (int d = 0; d < 3; ++d) x[d] = D[(int64_t)(PF_POS + d) * cap + i];
-            if (stencil_origin(Sc, x, b)) key = (int32_t)block_of(Sc, b[0], b[1], b[2]);
+            if (stencil_origin(Sc, x, b)) {
+              key = (int32_t)block_of(Sc, b[0], b[1], b[2]);
+              cellk = ((b[0] & 3) * 4 + (b[1] & 3)) * 4 + (b[2] & 3);
+            }
           }
         }
-        add_rank(P, valid, key, i, lane);
+        add_rank(P, valid, key, i, lane, cellk);
       }
       continue;
     }
@@ -1225,6 +1238,7 @@ __device__ __forceinline__ void g2p_body(const KParams& P) {
       const bool valid = q < cnt;
       const int64_t i = item.y + q;
       int32_t key = kInactive;
+      int cellk = BLK_NODES;
       float x[3] = {xn[0], xn[1], xn[2]};
       if (q + T < cnt) {
 #pragma unroll
@@ -1310,13 +1324,17 @@ __device__ __forceinline__ void g2p_body(const KParams& P) {
           for (int k = 0; k < 9; ++k) D[(int64_t)(PF_C + k) * cap + i] = Cn[k];
           int b[3];
           if (!finite) atomicOr(P.status, 1u);
-          else if (stencil_origin(S, xn, b)) key = (int32_t)block_of(S, b[0], b[1], b[2]);
-          else atomicOr(P.status, 2u);
+          else if (stencil_origin(S, xn, b)) {
+            key = (int32_t)block_of(S, b[0], b[1], b[2]);
+            cellk = ((b[0] & 3) * 4 + (b[1] & 3)) * 4 + (b[2] & 3);
+          } else {
+            atomicOr(P.status, 2u);
+          }
         } else {
           atomicOr(P.status, 2u);
         }
       }
-      add_rank(P, valid, key, i, lane);
+      add_rank(P, valid, key, i, lane, cellk);
     }
     __syncthreads();
   }

@@ -14,8 +14,9 @@
 //  * sort: particles are bucketed by the grid block that holds their stencil origin (the
 //    cell index at 4^3 granularity).  Buckets [0,K) are grid blocks, K holds inactive
 //    particles, K+1 particles of removed scenes.  key/rank come from G2P (warp-aggregated
-//    atomics on count[]); an exclusive scan gives bucket offsets and P2G work items;
-//    perm[new slot] = old slot drives the gather in the next P2G.
+//    atomics on count[]), with the particle's cell inside its block; an exclusive scan gives
+//    bucket offsets and P2G work items; perm[new slot] = old slot drives the gather in the next
+//    P2G and slot_cell[new slot] its per-cell counting sort.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -41,10 +42,11 @@ constexpr int P2G_MAX_CHUNK = 1024;          // particles per P2G work item
 // Shared-memory layout of k_p2g (dynamic part): warp tiles, then one scatter record per particle
 // at its cell-sorted position (P2G_REC float4 each: fx | mass, q | a0, a1..a4, a5..a8, then the
 // CPIC node mask in .x of the fifth, unused without CPIC; the odd stride of 5 float4 puts
-// consecutive records in different bank groups), then the item's (cell, rank) words.
+// consecutive records in different bank groups), then the item's (cell, rank) words and the old
+// slots of its particles.
 constexpr int P2G_REC = 5;
 __host__ __device__ __forceinline__ size_t p2g_dyn_smem(int threads, int chunk) {
-  return (size_t)(threads / 32) * TILE_NODES * 16 + (size_t)chunk * P2G_REC * 16 + (size_t)chunk * 4;
+  return (size_t)(threads / 32) * TILE_NODES * 16 + (size_t)chunk * P2G_REC * 16 + (size_t)chunk * 8;
 }
 constexpr float SVD_FP64_TOL = 1e-5f;        // residual above which the SVD is redone in FP64
 
@@ -134,6 +136,8 @@ struct KParams {
   int32_t* count;              // [K+2]
   int32_t* offset;             // [K+2]
   int32_t* perm;               // [cap]
+  uint8_t* cell8;              // [cap] cell of each particle in its block (old order; 64: none)
+  uint8_t* slot_cell;          // [cap] the same in sorted-slot order (written by k_perm)
   int4* items;                 // P2G work items (bucket, begin, end, 0)
   int32_t* n_items;
   int2* partials;              // scan tile partials
