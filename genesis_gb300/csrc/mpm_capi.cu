@@ -759,7 +759,14 @@ int mpm_get_state(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end, float* p
   int r = enter(ctx, stream);
   if (r) return r;
   KParams P = make_params(ctx, ctx->cur, ctx->cur, ctx->cur);
-  k_get_state<<<ctx->io_blocks, 256, 0, ctx->cs>>>(P, scene_begin, scene_end, pos, vel, C, F, Jp, active);
+  if (!ctx->pool && ctx->n_phys == ctx->n) {  // every row holds one particle: gather in row order
+    const int64_t rows = ctx->pbegin_h[scene_end] - ctx->pbegin_h[scene_begin];
+    uint32_t* row_info = reinterpret_cast<uint32_t*>(ctx->d_rank);
+    k_row_slots<<<ctx->io_blocks, 256, 0, ctx->cs>>>(P, scene_begin, scene_end, ctx->d_key, row_info);
+    k_get_state_rows<<<ctx->io_blocks, 256, 0, ctx->cs>>>(P, rows, ctx->d_key, row_info, pos, vel, C, F, Jp, active);
+  } else {
+    k_get_state<<<ctx->io_blocks, 256, 0, ctx->cs>>>(P, scene_begin, scene_end, pos, vel, C, F, Jp, active);
+  }
   CKL();
   return leave(ctx, stream);
 }
@@ -772,7 +779,15 @@ int mpm_set_state(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end, const fl
   int r = enter(ctx, stream);
   if (r) return r;
   KParams P = make_params(ctx, ctx->cur, ctx->cur, ctx->cur);
-  k_set_state<<<ctx->io_blocks, 256, 0, ctx->cs>>>(P, scene_begin, scene_end, pos, vel, C, F, Jp, active);
+  const bool whole = !ctx->pool && ctx->n_phys == ctx->n && scene_begin == 0 && scene_end == ctx->n_scenes &&
+                     ctx->nf == NF_BASE && pos && vel && C && F && Jp;
+  if (whole) {  // a full state of every scene: rewrite it in row order
+    uint32_t* row_info = reinterpret_cast<uint32_t*>(ctx->d_rank);
+    k_row_slots<<<ctx->io_blocks, 256, 0, ctx->cs>>>(P, 0, ctx->n_scenes, ctx->d_key, row_info);
+    k_set_state_rows<<<ctx->io_blocks, 256, 0, ctx->cs>>>(P, ctx->n, row_info, pos, vel, C, F, Jp, active);
+  } else {
+    k_set_state<<<ctx->io_blocks, 256, 0, ctx->cs>>>(P, scene_begin, scene_end, pos, vel, C, F, Jp, active);
+  }
   CKL();
   ctx->sorted = false;
   return leave(ctx, stream);

@@ -174,6 +174,72 @@ __global__ void k_set_state(KParams P, int64_t s0, int64_t s1, const float* pos,
   }
 }
 
+// Row-ordered state I/O (outside pool mode, where every row of scenes [s0, s1) holds exactly
+// one particle).  k_row_slots inverts the sorted layout once: for each particle slot it stores
+// the slot and the particle's info word at the particle's output row (4-byte writes into two
+// cap-sized arrays that stay in L2).  The gather and the row-order rewrite then read and write
+// the [B, N] rows coalesced.  The two arrays are the sort's key and rank arrays, which only
+// k_perm reads, right after they are written within a substep or a re-keying; between substeps
+// they are free.
+__global__ void k_row_slots(KParams P, int64_t s0, int64_t s1, int32_t* row_slot, uint32_t* row_info) {
+  const float* D = P.dst;
+  for (int64_t i = grid_stride_begin(); i < P.n; i += grid_stride_step()) {
+    const uint32_t info = ld_info(D, P.cap, i);
+    const int32_t s = scene_of(P, info);
+    if (s < s0 || s >= s1) continue;
+    const int64_t r = out_row(P, s, s0, __float_as_uint(D[(int64_t)PF_PID * P.cap + i]));
+    row_slot[r] = (int32_t)i;
+    row_info[r] = info;
+  }
+}
+
+// mpm_solver.py:759-778 (_kernel_get_state) in row order: gathers each row's particle through
+// row_slot.
+__global__ void k_get_state_rows(KParams P, int64_t rows, const int32_t* row_slot, const uint32_t* row_info,
+                                 float* pos, float* vel, float* C, float* F, float* Jp, uint8_t* active) {
+  const float* D = P.dst;
+  for (int64_t r = grid_stride_begin(); r < rows; r += grid_stride_step()) {
+    const int64_t i = row_slot[r];
+    if (pos)
+      for (int d = 0; d < 3; ++d) pos[r * 3 + d] = D[(int64_t)(PF_POS + d) * P.cap + i];
+    if (vel)
+      for (int d = 0; d < 3; ++d) vel[r * 3 + d] = D[(int64_t)(PF_VEL + d) * P.cap + i];
+    if (C)
+      for (int d = 0; d < 9; ++d) C[r * 9 + d] = D[(int64_t)(PF_C + d) * P.cap + i];
+    if (F)
+      for (int d = 0; d < 9; ++d) F[r * 9 + d] = D[(int64_t)(PF_F + d) * P.cap + i];
+    if (Jp) Jp[r] = D[(int64_t)PF_JP * P.cap + i];
+    if (active) active[r] = (row_info[r] & INFO_ACTIVE) ? 1 : 0;
+  }
+}
+
+// mpm_solver.py:729-749 (_kernel_set_state) for a full state of every scene: particle r is
+// rewritten into slot r (the layout the context starts with), so the new state is read and
+// written coalesced; only its info word comes from its old slot (row_info).  The particle
+// order no longer matches the last sort, which the caller marks stale (re-keying follows).
+// Requires the base planes only (no muscle or CPIC planes to carry along).
+__global__ void k_set_state_rows(KParams P, int64_t rows, const uint32_t* row_info, const float* pos,
+                                 const float* vel, const float* C, const float* F, const float* Jp,
+                                 const uint8_t* active) {
+  float* D = P.dst;
+  for (int64_t r = grid_stride_begin(); r < rows; r += grid_stride_step()) {
+    uint32_t info = row_info[r];
+    if (active) info = active[r] ? (info | INFO_ACTIVE) : (info & ~INFO_ACTIVE);
+    const int32_t s = scene_of(P, info);
+    for (int d = 0; d < 3; ++d) {
+      D[(int64_t)(PF_POS + d) * P.cap + r] = pos[r * 3 + d];
+      D[(int64_t)(PF_VEL + d) * P.cap + r] = vel[r * 3 + d];
+    }
+    for (int d = 0; d < 9; ++d) {
+      D[(int64_t)(PF_C + d) * P.cap + r] = C[r * 9 + d];
+      D[(int64_t)(PF_F + d) * P.cap + r] = F[r * 9 + d];
+    }
+    D[(int64_t)PF_JP * P.cap + r] = Jp[r];
+    D[(int64_t)PF_INFO * P.cap + r] = __uint_as_float(info);
+    D[(int64_t)PF_PID * P.cap + r] = __uint_as_float((uint32_t)(r - P.scenes[s].p_begin));
+  }
+}
+
 // Per-field access to a contiguous per-scene particle range (mpm_solver.py:840-1026).
 __global__ void k_particles_field(KParams P, int field, int write, int64_t s0, int64_t s1, int64_t start,
                                   int64_t n_sel, float* data) {

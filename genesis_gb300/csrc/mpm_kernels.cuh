@@ -228,6 +228,12 @@ __global__ void k_get_state(KParams P, int64_t s0, int64_t s1, float* pos, float
                             float* Jp, uint8_t* active);
 __global__ void k_set_state(KParams P, int64_t s0, int64_t s1, const float* pos, const float* vel, const float* C,
                             const float* F, const float* Jp, const uint8_t* active);
+__global__ void k_row_slots(KParams P, int64_t s0, int64_t s1, int32_t* row_slot, uint32_t* row_info);
+__global__ void k_get_state_rows(KParams P, int64_t rows, const int32_t* row_slot, const uint32_t* row_info,
+                                 float* pos, float* vel, float* C, float* F, float* Jp, uint8_t* active);
+__global__ void k_set_state_rows(KParams P, int64_t rows, const uint32_t* row_info, const float* pos,
+                                 const float* vel, const float* C, const float* F, const float* Jp,
+                                 const uint8_t* active);
 __global__ void k_particles_field(KParams P, int field, int write, int64_t s0, int64_t s1, int64_t start,
                                   int64_t n_sel, float* data);
 __global__ void k_g2p(KParams P);   // G2P + re-keying, over the P2G work items
