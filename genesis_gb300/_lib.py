@@ -90,10 +90,13 @@ class MpmCollider(ctypes.Structure):
         ("friction", c_double),
         ("softness", c_double),
         ("restitution", c_double),
+        ("sdf_grid", c_int32),
+        ("pad", c_int32),
+        ("floor_height", c_double),
     ]
 
 
-COLLIDER_SPHERE, COLLIDER_PLANE, COLLIDER_BOX = 0, 1, 2
+COLLIDER_SPHERE, COLLIDER_PLANE, COLLIDER_BOX, COLLIDER_SDF, COLLIDER_TOOL = 0, 1, 2, 3, 4
 
 
 class MpmForceField(ctypes.Structure):
@@ -176,6 +179,8 @@ _SIGNATURES = {
     "mpm_sample_regular": (c_int32, [c_int32, _P, _P, c_double, _P, c_int64, _P, _P]),
     "mpm_test_wait_timeout": (c_int32, [_P, _P]),
     "mpm_get_collider_forces": (c_int32, [_P, _P, c_int32, _P]),
+    "mpm_add_sdf_grid": (c_int32, [_P, _P, _P, _P, _P, c_double, c_double, ctypes.POINTER(c_int32)]),
+    "mpm_get_collider_poses": (c_int32, [_P, _P, _P]),
     "mpm_enable_cpic": (c_int32, [_P, c_int32, _P]),
     "mpm_set_coupled_particles": (c_int32, [_P, c_int32, c_int64, _P, _P, _P, _P, _P]),
     "mpm_version": (c_int32, []),

@@ -85,6 +85,15 @@ struct mpm_ctx {
   ColliderDev* d_colliders = nullptr;  // kinematic colliders (capacity MAX_COLLIDERS once allocated)
   double* d_collider_acc = nullptr;    // [MAX_COLLIDERS][6]
   int32_t n_colliders = 0;
+  int32_t n_tools = 0;               // MPM_COLLIDER_TOOL colliders among them (k_perm moves them)
+  struct SdfGrid {                   // voxel SDF grids of MPM_COLLIDER_SDF / MPM_COLLIDER_TOOL colliders
+    float* val = nullptr;
+    float* grad = nullptr;
+    int32_t res[3] = {0, 0, 0};
+    double T[16] = {};
+    double cell_size = 0, sdf_max = 0;
+  };
+  std::vector<SdfGrid> sdf_grids;
   int32_t cpic_slots = 0;            // CPIC collider slots (normal planes); 0: CPIC off
   uint32_t* d_cpic_mask = nullptr;   // CPIC: per particle slot, the stencil nodes behind a collider
   ExtSetDev ext[2] = {};             // coupled SPH / PBD particle sets (caller-owned arrays, own bins)
@@ -252,7 +261,7 @@ int launch_sort(mpm_ctx* ctx, const KParams& P, cudaStream_t s) {
     }
   }
   CKL();
-  if (P.n > 0 || P.steps || P.nlist_reset) {
+  if (P.n > 0 || P.steps || P.nlist_reset || P.colliders_rw) {
     Timer t(ctx, s, KT_PERM);
     k_perm<<<ctx->io_blocks, 256, 0, s>>>(P);
   }
@@ -309,6 +318,7 @@ int launch_post(mpm_ctx* ctx, int c, cudaStream_t s, bool fuse_grid = false) {
   P.fuse_grid = fuse_grid ? 1 : 0;
   P.nlist_reset = fuse_grid ? P.nlist_other : nullptr;
   P.ff_step_advance = 1;
+  P.colliders_rw = ctx->n_tools > 0 ? ctx->d_colliders : nullptr;
   ctx->grid_momentum[c] = fuse_grid;
   {
     Timer t(ctx, s, KT_G2P);
@@ -711,6 +721,10 @@ int mpm_ctx_destroy(mpm_ctx* ctx) {
   if (ctx->d_pin) cudaFree(ctx->d_pin);
   if (ctx->d_cons) cudaFree(ctx->d_cons);
   if (ctx->d_colliders) cudaFree(ctx->d_colliders);
+  for (auto& g : ctx->sdf_grids) {
+    if (g.val) cudaFree(g.val);
+    if (g.grad) cudaFree(g.grad);
+  }
   if (ctx->d_ffs) cudaFree(ctx->d_ffs);
   if (ctx->d_ff_step) cudaFree(ctx->d_ff_step);
   if (ctx->d_collider_acc) cudaFree(ctx->d_collider_acc);
@@ -982,8 +996,13 @@ int mpm_set_colliders(mpm_ctx* ctx, int32_t n, const mpm_collider* colliders) {
   std::vector<ColliderDev> h((size_t)n);
   for (int32_t i = 0; i < n; ++i) {
     const mpm_collider& c = colliders[i];
-    if (c.type < MPM_COLLIDER_SPHERE || c.type > MPM_COLLIDER_BOX)
+    if (c.type < MPM_COLLIDER_SPHERE || c.type > MPM_COLLIDER_TOOL)
       return fail(ctx, MPM_ERR_BAD_ARG, "unknown collider type");
+    const bool gridded = c.type == MPM_COLLIDER_SDF || c.type == MPM_COLLIDER_TOOL;
+    if (gridded && (c.sdf_grid < 0 || c.sdf_grid >= (int32_t)ctx->sdf_grids.size()))
+      return fail(ctx, MPM_ERR_BAD_ARG, "collider SDF grid id out of range (mpm_add_sdf_grid)");
+    if (c.type == MPM_COLLIDER_SDF && !ctx->sdf_grids[(size_t)c.sdf_grid].grad)
+      return fail(ctx, MPM_ERR_BAD_ARG, "an SDF collider needs a grid with gradients");
     if (c.scene < -1 || c.scene >= ctx->n_scenes) return fail(ctx, MPM_ERR_BAD_ARG, "collider scene out of range");
     if (ctx->cpic_slots > 0 && i >= ctx->cpic_slots)
       return fail(ctx, MPM_ERR_BAD_ARG, "more colliders than CPIC slots (mpm_enable_cpic)");
@@ -1002,7 +1021,29 @@ int mpm_set_colliders(mpm_ctx* ctx, int32_t n, const mpm_collider* colliders) {
     d.friction = (float)c.friction;
     d.softness = (float)c.softness;
     d.restitution = (float)c.restitution;
+    if (gridded) {
+      const mpm_ctx::SdfGrid& g = ctx->sdf_grids[(size_t)c.sdf_grid];
+      d.pad0 = c.sdf_grid;
+      d.val = g.val;
+      d.grad = g.grad;
+      for (int k = 0; k < 3; ++k) d.res[k] = g.res[k];
+      for (int k = 0; k < 12; ++k) d.T[k] = (float)g.T[k];
+      // inverse of the 3x3 block (tool normals: voxel frame -> mesh frame), by cofactors in double
+      const double* T = g.T;
+      const double a = T[0], b = T[1], cc = T[2], e = T[4], f = T[5], gg = T[6], h = T[8], i2 = T[9], j = T[10];
+      const double det = a * (f * j - gg * i2) - b * (e * j - gg * h) + cc * (e * i2 - f * h);
+      if (!(std::fabs(det) > 0)) return fail(ctx, MPM_ERR_BAD_ARG, "T_mesh_to_sdf is singular");
+      const double inv[9] = {(f * j - gg * i2) / det, (cc * i2 - b * j) / det, (b * gg - cc * f) / det,
+                             (gg * h - e * j) / det,  (a * j - cc * h) / det,  (cc * e - a * gg) / det,
+                             (e * i2 - f * h) / det,  (b * h - a * i2) / det,  (a * f - b * e) / det};
+      for (int k = 0; k < 9; ++k) d.Rinv[k] = (float)inv[k];
+      d.cell_size = (float)g.cell_size;
+      d.sdf_max = (float)g.sdf_max;
+      d.floor_h = (float)c.floor_height;
+    }
   }
+  int32_t n_tools = 0;
+  for (int32_t i = 0; i < n; ++i) n_tools += colliders[i].type == MPM_COLLIDER_TOOL ? 1 : 0;
   CK(cudaSetDevice(ctx->device));
   if (!ctx->d_colliders && n > 0) {
     cudaError_t e = cudaMalloc((void**)&ctx->d_colliders, sizeof(ColliderDev) * MAX_COLLIDERS);
@@ -1014,9 +1055,59 @@ int mpm_set_colliders(mpm_ctx* ctx, int32_t n, const mpm_collider* colliders) {
     CK(cudaMemsetAsync(ctx->d_collider_acc, 0, sizeof(double) * 6 * MAX_COLLIDERS, ctx->cs));
     CK(cudaStreamSynchronize(ctx->cs));
   }
-  if (n != ctx->n_colliders) drop_graph(ctx);  // the count is a captured kernel argument
+  if (n != ctx->n_colliders || (n_tools > 0) != (ctx->n_tools > 0)) drop_graph(ctx);  // captured kernel arguments
   ctx->n_colliders = n;
+  ctx->n_tools = n_tools;
   return MPM_OK;
+}
+
+int mpm_add_sdf_grid(mpm_ctx* ctx, const int32_t* res, const float* values, const float* grads,
+                     const double* T_mesh_to_sdf, double cell_size, double sdf_max, int32_t* id_out) {
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (!res || !values || !T_mesh_to_sdf || !id_out) return fail(ctx, MPM_ERR_BAD_ARG, "null SDF grid argument");
+  if (res[0] < 2 || res[1] < 2 || res[2] < 2 || (int64_t)res[0] * res[1] * res[2] > (int64_t)1 << 30)
+    return fail(ctx, MPM_ERR_BAD_ARG, "SDF grid resolution must be >= 2 per axis");
+  if (!(cell_size > 0)) return fail(ctx, MPM_ERR_BAD_ARG, "SDF cell_size must be > 0");
+  if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "SDF grid inside a substep");
+  const size_t nv = (size_t)res[0] * res[1] * res[2];
+  mpm_ctx::SdfGrid g;
+  for (int k = 0; k < 3; ++k) g.res[k] = res[k];
+  for (int k = 0; k < 16; ++k) g.T[k] = T_mesh_to_sdf[k];
+  g.cell_size = cell_size;
+  g.sdf_max = sdf_max;
+  CK(cudaSetDevice(ctx->device));
+  cudaError_t e = cudaMalloc((void**)&g.val, sizeof(float) * nv);
+  if (e == cudaSuccess && grads) e = cudaMalloc((void**)&g.grad, sizeof(float) * 3 * nv);
+  if (e != cudaSuccess) {
+    if (g.val) cudaFree(g.val);
+    cudaGetLastError();
+    return fail(ctx, MPM_ERR_OOM, "SDF grid allocation failed");
+  }
+  e = cudaMemcpy(g.val, values, sizeof(float) * nv, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && grads) e = cudaMemcpy(g.grad, grads, sizeof(float) * 3 * nv, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(g.val);
+    if (g.grad) cudaFree(g.grad);
+    return fail(ctx, MPM_ERR_CUDA, std::string("SDF grid upload: ") + cudaGetErrorString(e));
+  }
+  ctx->sdf_grids.push_back(g);
+  *id_out = (int32_t)ctx->sdf_grids.size() - 1;
+  return MPM_OK;
+}
+
+int mpm_get_collider_poses(mpm_ctx* ctx, double* out_host, void* stream) {
+  if (!ctx || !out_host) return MPM_ERR_BAD_ARG;
+  if (ctx->n_colliders == 0) return MPM_OK;
+  int r = enter(ctx, stream);
+  if (r) return r;
+  std::vector<ColliderDev> h((size_t)ctx->n_colliders);
+  CK(cudaMemcpyAsync(h.data(), ctx->d_colliders, sizeof(ColliderDev) * h.size(), cudaMemcpyDeviceToHost, ctx->cs));
+  CK(cudaStreamSynchronize(ctx->cs));
+  for (size_t i = 0; i < h.size(); ++i) {
+    for (int k = 0; k < 3; ++k) out_host[i * 7 + k] = h[i].pos[k];
+    for (int k = 0; k < 4; ++k) out_host[i * 7 + 3 + k] = h[i].quat[k];
+  }
+  return leave(ctx, stream);
 }
 
 int mpm_enable_cpic(mpm_ctx* ctx, int32_t n_slots, void* stream) {

@@ -537,19 +537,6 @@ __global__ void __launch_bounds__(1024) k_scan_single(KParams P) {
   if (threadIdx.x == 0) *P.n_items = s_carry.y;
 }
 
-__global__ void k_perm(KParams P) {
-  const int64_t n = P.n_dev ? *P.n_dev : P.n;
-  for (int64_t i = grid_stride_begin(); i < n; i += grid_stride_step()) {
-    const int64_t dst = P.offset[P.key[i]] + P.rank[i];
-    P.perm[dst] = (int32_t)i;
-    P.slot_cell[dst] = P.cell8[i];  // P2G reads each slot's cell without gathering its position
-  }
-  if (P.nlist_reset && blockIdx.x == 0 && threadIdx.x == 0) *P.nlist_reset = 0;  // cleared by the fused G2P
-  if (P.ff_step && P.ff_step_advance && blockIdx.x == 0 && threadIdx.x == 0) *P.ff_step += 1;  // end of a substep
-  if (P.steps && blockIdx.x == 0)  // end of a substep: count down per-scene substep budgets
-    for (int s = threadIdx.x; s < P.n_scenes; s += blockDim.x)
-      if (P.steps[s] > 0) P.steps[s] -= 1;
-}
 
 // ------------------------------------------------------------------ kinematic colliders
 namespace {
@@ -653,10 +640,138 @@ __device__ __forceinline__ void ff_acc(const ForceFieldDev& f, const float* x, c
   }
 }
 
+// ---- voxel SDF grids (MPM_COLLIDER_SDF: utils/sdf.py; MPM_COLLIDER_TOOL: tool_entity/mesh.py)
+// World point x -> mesh frame (inverse pose) -> voxel coordinates ps (T_mesh_to_sdf).
+__device__ __forceinline__ void sdf_voxel_pos(const ColliderDev& c, const float* pos, const float* quat,
+                                              const float* x, float* pm, float* ps) {
+  const float d[3] = {x[0] - pos[0], x[1] - pos[1], x[2] - pos[2]};
+  const float qi[4] = {quat[0], -quat[1], -quat[2], -quat[3]};
+  rot(qi, d, pm);
+  for (int r = 0; r < 3; ++r) ps[r] = c.T[r * 4 + 0] * pm[0] + c.T[r * 4 + 1] * pm[1] + c.T[r * 4 + 2] * pm[2] + c.T[r * 4 + 3];
+}
+
+// Trilinear interpolation over the 8 voxels from `base` (utils/sdf.py:167-184, 283-294;
+// mesh.py:101-107), in the reference's corner order (z fastest); the gradient too when g != null.
+__device__ __forceinline__ float sdf_trilinear(const ColliderDev& c, const float* ps, const int* base, float* g) {
+  float sd = 0.f;
+  if (g) g[0] = g[1] = g[2] = 0.f;
+  for (int o = 0; o < 8; ++o) {
+    const int cx = base[0] + (o >> 2), cy = base[1] + ((o >> 1) & 1), cz = base[2] + (o & 1);
+    const float w = (1.f - fabsf(ps[0] - (float)cx)) * (1.f - fabsf(ps[1] - (float)cy)) * (1.f - fabsf(ps[2] - (float)cz));
+    const int64_t cell = ((int64_t)cx * c.res[1] + cy) * c.res[2] + cz;
+    sd = sd + w * c.val[cell];
+    if (g)
+      for (int k = 0; k < 3; ++k) g[k] = g[k] + w * c.grad[cell * 3 + k];
+  }
+  return sd;
+}
+
+// Rigid geom SDF grid (utils/sdf.py:137-184, 223-296): value and gradient in the voxel frame.
+__device__ __forceinline__ float sdf_grid_value_grad(const ColliderDev& c, const float* ps, float eps, float* g) {
+  bool outside = false;
+  for (int k = 0; k < 3; ++k) outside = outside || ps[k] >= (float)(c.res[k] - 1) || ps[k] <= 0.f;
+  if (outside) {  // proxy: distance to the grid centre (sdf_func_proxy_sdf / _proxy_grad)
+    float d[3];
+    for (int k = 0; k < 3; ++k) d[k] = ps[k] - (float)(c.res[k] - 1) / 2.f;
+    const float len2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    const float ln = sqrtf(len2 + eps);
+    for (int k = 0; k < 3; ++k) g[k] = d[k] / ln;
+    return sqrtf(len2) / c.cell_size + c.sdf_max;
+  }
+  int base[3];
+  for (int k = 0; k < 3; ++k) base[k] = min((int)floorf(ps[k]), c.res[k] - 2);
+  return sdf_trilinear(c, ps, base, g);
+}
+
+// Tool mesh SDF in voxel coordinates (mesh.py:92-107): 1 outside the grid.
+__device__ __forceinline__ float tool_sdf_vox(const ColliderDev& c, const float* ps) {
+  int base[3];
+  bool outside = false;
+  for (int k = 0; k < 3; ++k) {
+    base[k] = (int)floorf(ps[k]);
+    outside = outside || base[k] >= c.res[k] - 1 || base[k] < 0;
+  }
+  return outside ? 1.f : sdf_trilinear(c, ps, base, nullptr);
+}
+
+// The tool's pose one substep later (tool_entity.py:193-206): pos + v dt clamped to the floor,
+// quat turned by the rotation vector w dt (qd_rotvec_to_quat with its first-order normalisation,
+// then qd_transform_quat_by_quat: normalize(q_rot * quat)).
+__device__ __forceinline__ void tool_next_pose(const ColliderDev& c, float dt, float eps, float* pn, float* qn) {
+  for (int k = 0; k < 3; ++k) pn[k] = c.pos[k] + c.lin[k] * dt;
+  pn[2] = fmaxf(pn[2], c.floor_h);
+  const float rv[3] = {c.ang[0] * dt, c.ang[1] * dt, c.ang[2] * dt};
+  const float th2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+  float u[4] = {1.f, 0.f, 0.f, 0.f};
+  if (th2 > eps * eps) {
+    const float th = sqrtf(th2);
+    const float cs = cosf(0.5f * th), sn = sinf(0.5f * th);
+    u[0] = cs;
+    for (int k = 0; k < 3; ++k) u[k + 1] = sn / th * rv[k];
+    const float s = 0.5f * (3.f - (u[0] * u[0] + u[1] * u[1] + u[2] * u[2] + u[3] * u[3]));
+    for (int k = 0; k < 4; ++k) u[k] *= s;
+  }
+  const float* v = c.quat;
+  const float q[4] = {u[0] * v[0] - u[1] * v[1] - u[2] * v[2] - u[3] * v[3],
+                      u[0] * v[1] + u[1] * v[0] + u[2] * v[3] - u[3] * v[2],
+                      u[0] * v[2] - u[1] * v[3] + u[2] * v[0] + u[3] * v[1],
+                      u[0] * v[3] + u[1] * v[2] - u[2] * v[1] + u[3] * v[0]};
+  const float qn_len = sqrtf(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  for (int k = 0; k < 4; ++k) qn[k] = q[k] / qn_len;
+}
+
+// Mesh.collide (mesh.py:148-177) of a tool at node position x, node velocity v.
+__device__ void collide_tool(const ColliderDev& c, const SceneDev& S, const float* x, float* v) {
+  float pm[3], ps[3];
+  sdf_voxel_pos(c, c.pos, c.quat, x, pm, ps);
+  const float sd = tool_sdf_vox(c, ps);
+  const float influence = fminf(expf(-sd / fmaxf(S.eps, c.softness)), 1.f);
+  if (!(sd <= 0.f || influence > 0.1f)) return;
+  float pn[3], qn[4], xn[3];
+  tool_next_pose(c, S.dt, S.eps, pn, qn);
+  rot(qn, pm, xn);
+  float vc[3], rv[3];
+  for (int k = 0; k < 3; ++k) {
+    vc[k] = (xn[k] + pn[k] - x[k]) / S.dt;
+    rv[k] = v[k] - vc[k];
+  }
+  // normal: central differences in voxel space (delta 1e-2), back to the mesh frame, then world
+  float nv[3];
+  for (int i = 0; i < 3; ++i) {
+    float inc[3] = {ps[0], ps[1], ps[2]}, dec[3] = {ps[0], ps[1], ps[2]};
+    inc[i] += 1e-2f;
+    dec[i] -= 1e-2f;
+    nv[i] = (tool_sdf_vox(c, inc) - tool_sdf_vox(c, dec)) / (2.f * 1e-2f);
+  }
+  float l = sqrtf(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2] + S.eps);
+  for (int k = 0; k < 3; ++k) nv[k] /= l;
+  float nm[3], n[3];
+  for (int r = 0; r < 3; ++r) nm[r] = c.Rinv[r * 3 + 0] * nv[0] + c.Rinv[r * 3 + 1] * nv[1] + c.Rinv[r * 3 + 2] * nv[2];
+  rot(c.quat, nm, n);
+  l = sqrtf(n[0] * n[0] + n[1] * n[1] + n[2] * n[2] + S.eps);
+  for (int k = 0; k < 3; ++k) n[k] /= l;
+  const float rvn = rv[0] * n[0] + rv[1] * n[1] + rv[2] * n[2];
+  if (!(rvn < 0.f)) return;
+  float rt[3];
+  for (int k = 0; k < 3; ++k) rt[k] = rv[k] - rvn * n[k];
+  const float rtn = sqrtf(rt[0] * rt[0] + rt[1] * rt[1] + rt[2] * rt[2] + S.eps);
+  const float mag = fmaxf(0.f, rtn + rvn * c.friction);
+  for (int k = 0; k < 3; ++k) v[k] = vc[k] + rt[k] / rtn * mag * influence + rv[k] * (1.f - influence);
+}
+
 // Signed distance and outward unit normal of a collider at world point x
-// (utils/sdf.py:119-126 and 372-378 for sphere and plane; analytic box).
+// (utils/sdf.py:119-126 and 372-378 for sphere and plane; analytic box; SDF grid).
 __device__ __forceinline__ float collider_sdf(const ColliderDev& c, const float* x, float eps, float* n) {
   float d[3] = {x[0] - c.pos[0], x[1] - c.pos[1], x[2] - c.pos[2]};
+  if (c.type == MPM_COLLIDER_SDF) {
+    float pm[3], ps[3], gv[3], g[3];
+    sdf_voxel_pos(c, c.pos, c.quat, x, pm, ps);
+    const float sd = sdf_grid_value_grad(c, ps, eps, gv);
+    rot(c.quat, gv, g);  // no rotation between the mesh and SDF frames (utils/sdf.py:383)
+    const float gn = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2] + eps);
+    for (int k = 0; k < 3; ++k) n[k] = g[k] / gn;
+    return sd;
+  }
   if (c.type == MPM_COLLIDER_SPHERE) {
     const float len = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
     const float ln = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2] + eps);  // norm(EPS)
@@ -729,10 +844,15 @@ __device__ void collide_in(const KParams& P, const SceneDev& S, int ci, const fl
 
 // _func_collide_with_rigid (legacy_coupler.py:134-218): every collider of the node's scene whose
 // SDF influence exceeds 0.1 at x, in order.
+// Tools come first (legacy_coupler.py:386-387 before :389-403).
 __device__ void collide_node(const KParams& P, const SceneDev& S, int32_t scene, const float* x, float* v, float m) {
   for (int ci = 0; ci < P.n_colliders; ++ci) {
     const ColliderDev& c = P.colliders[ci];
-    if (c.scene >= 0 && c.scene != scene) continue;
+    if (c.type == MPM_COLLIDER_TOOL && (c.scene < 0 || c.scene == scene)) collide_tool(c, S, x, v);
+  }
+  for (int ci = 0; ci < P.n_colliders; ++ci) {
+    const ColliderDev& c = P.colliders[ci];
+    if (c.type == MPM_COLLIDER_TOOL || (c.scene >= 0 && c.scene != scene)) continue;
     float n[3];
     const float sd = collider_sdf(c, x, S.eps, n);
     const float influence = fminf(expf(-sd / fmaxf(1e-10f, c.softness)), 1.f);
@@ -783,7 +903,7 @@ __device__ void couple_ext(const KParams& P, int64_t a, float* v, float m) {
 // side (mpm_solver.py:389-411): a stencil node lies behind collider ci when the collider's
 // normal at the node points against the particle's; the first such collider, in order, counts.
 __device__ __forceinline__ bool collider_in_scene(const ColliderDev& c, int32_t scene) {
-  return c.scene < 0 || c.scene == scene;
+  return c.type != MPM_COLLIDER_TOOL && (c.scene < 0 || c.scene == scene);  // tools: no CPIC
 }
 
 __device__ int cpic_separating(const KParams& P, const SceneDev& S, int32_t scene, const float* D, int64_t i,
@@ -858,6 +978,31 @@ __device__ __noinline__ float4 cpic_g2p_node(const KParams& P, const SceneDev& S
   return make_float4(v[0], v[1], v[2], g.w);
 }
 }  // namespace
+
+// Bucket permutation of the sort; also the end-of-substep bookkeeping.
+__global__ void k_perm(KParams P) {
+  const int64_t n = P.n_dev ? *P.n_dev : P.n;
+  for (int64_t i = grid_stride_begin(); i < n; i += grid_stride_step()) {
+    const int64_t dst = P.offset[P.key[i]] + P.rank[i];
+    P.perm[dst] = (int32_t)i;
+    P.slot_cell[dst] = P.cell8[i];  // P2G reads each slot's cell without gathering its position
+  }
+  if (P.nlist_reset && blockIdx.x == 0 && threadIdx.x == 0) *P.nlist_reset = 0;  // cleared by the fused G2P
+  if (P.ff_step && P.ff_step_advance && blockIdx.x == 0 && threadIdx.x == 0) *P.ff_step += 1;  // end of a substep
+  if (P.colliders_rw && blockIdx.x == 0)  // end of a substep: tools move (tool_entity.py:193-206)
+    for (int ci = threadIdx.x; ci < P.n_colliders; ci += blockDim.x) {
+      ColliderDev& c = P.colliders_rw[ci];
+      if (c.type != MPM_COLLIDER_TOOL) continue;
+      const SceneDev& S = P.scenes[c.scene >= 0 ? c.scene : 0];
+      float pn[3], qn[4];
+      tool_next_pose(c, S.dt, S.eps, pn, qn);
+      for (int k = 0; k < 3; ++k) c.pos[k] = pn[k];
+      for (int k = 0; k < 4; ++k) c.quat[k] = qn[k];
+    }
+  if (P.steps && blockIdx.x == 0)  // end of a substep: count down per-scene substep budgets
+    for (int s = threadIdx.x; s < P.n_scenes; s += blockDim.x)
+      if (P.steps[s] > 0) P.steps[s] -= 1;
+}
 
 // ------------------------------------------------------------------ P2G
 namespace {

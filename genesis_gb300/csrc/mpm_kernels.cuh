@@ -87,6 +87,13 @@ struct ColliderDev {
   int32_t type, scene, pad0, pad1;
   float pos[3], quat[4], size[3], com[3], lin[3], ang[3];
   float friction, softness, restitution, pad2;
+  // MPM_COLLIDER_SDF / MPM_COLLIDER_TOOL: voxel SDF grid (device arrays owned by the context)
+  const float* val;   // [res0][res1][res2]
+  const float* grad;  // [res0][res1][res2][3] (SDF) or null (tool)
+  int32_t res[3], pad3;
+  float T[12];        // rows 0..2 of T_mesh_to_sdf
+  float Rinv[9];      // inverse of T[:3, :3] (tool normals back to the mesh frame)
+  float cell_size, sdf_max, floor_h, pad4;
 };
 
 // External acceleration field of the grid op (mpm_force_field in float).
@@ -164,6 +171,7 @@ struct KParams {
   ExtSetDev ext[2];            // coupled particle sets: [0] SPH, [1] PBD (applied in that order)
   unsigned long long* ff_step; // substeps since the force fields were set (NOISE draws), or null
   int32_t ff_step_advance;     // k_perm counts the substep (set only for the end of a substep)
+  ColliderDev* colliders_rw;   // k_perm advances the tools' poses at the end of a substep (else null)
 };
 
 // Block key of a world position; returns false if the stencil would leave the grid.

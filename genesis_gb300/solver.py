@@ -361,8 +361,32 @@ class MPMSolver:
     # ------------------------------------------------------------------ rigid coupling
     def set_colliders(self, colliders) -> None:
         """Kinematic rigid colliders coupled in the grid op (genesis_gb300.coupling.Collider list;
-        call again whenever they move)."""
-        recs = [c.to_c() for c in colliders]
+        call again whenever they move).  Shapes "sdf" and "tool" carry an SDFGrid, uploaded to the
+        device once per grid object; tools then move by themselves every substep (see
+        get_collider_poses)."""
+        if not hasattr(self, "_sdf_ids"):
+            self._sdf_ids = {}  # id(SDFGrid) -> (grid, library grid id)
+        ids = []
+        for c in colliders:
+            if c.sdf is None:
+                ids.append(-1)
+                continue
+            hit = self._sdf_ids.get(id(c.sdf))
+            if hit is None or hit[0] is not c.sdf:
+                g = c.sdf
+                vals = np.ascontiguousarray(g.values, np.float32)
+                grads = None if g.grads is None else np.ascontiguousarray(g.grads, np.float32)
+                res = np.asarray(vals.shape, np.int32)
+                T = np.ascontiguousarray(g.T_mesh_to_sdf, np.float64)
+                out = ctypes.c_int32()
+                _lib.check(self._lib.mpm_add_sdf_grid(self._ctx, res.ctypes.data, vals.ctypes.data,
+                                                      None if grads is None else grads.ctypes.data, T.ctypes.data,
+                                                      float(g.cell_size), float(g.sdf_max), ctypes.byref(out)),
+                           self._ctx, "mpm_add_sdf_grid")
+                hit = (g, out.value)
+                self._sdf_ids[id(g)] = hit
+            ids.append(hit[1])
+        recs = [c.to_c(i) for c, i in zip(colliders, ids)]
         arr = (_lib.MpmCollider * max(1, len(recs)))(*recs)
         if self._enable_CPIC and len(recs) > getattr(self, "_cpic_slots", 0):
             # CPIC (mpm_solver.py:389-411, 445-459): one slot of particle-side normals per collider;
@@ -372,6 +396,15 @@ class MPMSolver:
             self._cpic_slots = len(recs)
         _lib.check(self._lib.mpm_set_colliders(self._ctx, len(recs), arr), self._ctx, "mpm_set_colliders")
         self._n_colliders = len(recs)
+
+    def get_collider_poses(self) -> np.ndarray:
+        """[n_colliders, 7]: current position and quaternion (w, x, y, z) of each collider; tools
+        have advanced one substep per substep since set_colliders."""
+        n = getattr(self, "_n_colliders", 0)
+        out = np.zeros((max(1, n), 7), dtype=np.float64)
+        _lib.check(self._lib.mpm_get_collider_poses(self._ctx, out.ctypes.data, _stream_handle()), self._ctx,
+                   "mpm_get_collider_poses")
+        return out[:n]
 
     def get_collider_forces(self, reset: bool = True) -> np.ndarray:
         """[n_colliders, 6]: force (xyz) and torque about each collider's com exerted by the

@@ -239,10 +239,30 @@ int mpm_set_force_fields(mpm_ctx* ctx, int32_t n, const mpm_force_field* fields)
  * collider (m = node mass / 1e3, the particle_volume_scale) and its torque about `com` are
  * accumulated on the device.  Sphere and plane SDFs are the reference's analytic ones
  * (utils/sdf.py:119-126, 372-378); the box SDF is analytic here (the reference samples a
- * precomputed SDF grid for boxes).  With colliders set, the grid op runs as its own kernel. */
+ * precomputed SDF grid for boxes; MPM_COLLIDER_SDF does exactly that with a caller's grid).
+ * With colliders set, the grid op runs as its own kernel.
+ *
+ * MPM_COLLIDER_SDF: a rigid geom whose SDF is a precomputed voxel grid (mpm_add_sdf_grid, with
+ * gradients) - utils/sdf.py:105-185, 223-322: the point goes to the mesh frame (pos, quat), then
+ * to voxel coordinates by T_mesh_to_sdf; inside the grid the value and the gradient are trilinear
+ * interpolations, outside it the distance to the grid centre / cell_size + sdf_max and the
+ * direction from the centre; normal = quat . gradient, normalised.
+ *
+ * MPM_COLLIDER_TOOL: a tool entity (engine/entities/tool_entity/mesh.py:84-177,
+ * tool_entity.py:189-206), applied before the rigid colliders (legacy_coupler.py:349-354, 386-387).
+ * Its voxel SDF (a grid without gradients) reads 1 outside the grid, its normal is a central
+ * difference (delta 1e-2 voxels) taken back to the world frame; a node with sdf <= 0 or
+ * influence > 0.1 that approaches the tool loses its inward relative velocity and tangential speed
+ * by friction * |normal part|, blended by the influence (no restitution, no reaction force).  The
+ * tool moves by itself: every substep its pose advances on the device from lin_vel and ang_vel
+ * (pos += v dt, clamped to z >= floor_height; quat = rotvec(w dt) * quat, normalised), and the
+ * collider velocity at x is (pose_next(pose^-1(x)) - x) / dt; mpm_get_collider_poses reads the
+ * current poses.  Tools take no part in CPIC (the reference's CPIC sees rigid geoms only). */
 #define MPM_COLLIDER_SPHERE 0 /* size[0] = radius */
 #define MPM_COLLIDER_PLANE 1  /* size = plane normal in the collider frame; sdf = n . x_local */
 #define MPM_COLLIDER_BOX 2    /* size = half extents */
+#define MPM_COLLIDER_SDF 3    /* sdf_grid = id from mpm_add_sdf_grid (with gradients) */
+#define MPM_COLLIDER_TOOL 4   /* sdf_grid = id from mpm_add_sdf_grid; lin_vel, ang_vel move it */
 typedef struct mpm_collider {
   int32_t type;
   int32_t scene;        /* scene index, or -1: every scene */
@@ -252,14 +272,30 @@ typedef struct mpm_collider {
   double com[3];        /* point the angular velocity turns about (the link's root COM) */
   double lin_vel[3];
   double ang_vel[3];
-  double friction;      /* coup_friction */
+  double friction;      /* coup_friction (a tool's friction) */
   double softness;      /* coup_softness */
-  double restitution;   /* coup_restitution */
+  double restitution;   /* coup_restitution (unused by a tool) */
+  int32_t sdf_grid;     /* MPM_COLLIDER_SDF / MPM_COLLIDER_TOOL: SDF grid id */
+  int32_t pad;
+  double floor_height;  /* MPM_COLLIDER_TOOL: ToolOptions.floor_height (FloorBoundary of the tool solver) */
 } mpm_collider;
 
 /* Replace the collider set (n may be 0); host array, copied before returning.  Resets the force
  * accumulators. */
 int mpm_set_colliders(mpm_ctx* ctx, int32_t n, const mpm_collider* colliders);
+
+/* Copy a voxel SDF grid to the device for MPM_COLLIDER_SDF / MPM_COLLIDER_TOOL colliders; *id_out
+ * receives its id (0, 1, ... in call order).  values [res0][res1][res2] (x-major) in world
+ * distance units, grads [res0][res1][res2][3] or NULL (a tool's grid); T_mesh_to_sdf is the 4x4
+ * row-major transform from the mesh frame to voxel coordinates; cell_size and sdf_max enter the
+ * outside-grid distance (utils/sdf.py:157-164).  Host arrays, copied before returning; grids live
+ * until the context is destroyed (the reference's SDFInfo, rigid/sdf fields). */
+int mpm_add_sdf_grid(mpm_ctx* ctx, const int32_t* res, const float* values, const float* grads,
+                     const double* T_mesh_to_sdf, double cell_size, double sdf_max, int32_t* id_out);
+
+/* Current pose of each collider: out_host [n][7] = pos (xyz), quat (wxyz); tools have advanced one
+ * substep per substep since mpm_set_colliders.  Synchronises `stream`. */
+int mpm_get_collider_poses(mpm_ctx* ctx, double* out_host, void* stream);
 
 /* Force (xyz) and torque about com (xyz) exerted by the particles on each collider, summed over
  * the substeps since the last reset: out_host [n][6].  Synchronises `stream`. */

@@ -59,6 +59,9 @@ typedef struct oracle_collider {
   int32_t scene;
   double pos[3], quat[4], size[3], com[3], lin_vel[3], ang_vel[3];
   double friction, softness, restitution;
+  int32_t sdf_grid;  // 3 (rigid geom with an SDF grid) and 4 (tool): index into the oracle's grids
+  int32_t pad;
+  double floor_height;  // tool: the tool solver's FloorBoundary height
 } oracle_collider;
 
 // External acceleration field: same layout as mpm_force_field of the library header.
@@ -470,10 +473,158 @@ void quat_rot(const double* q, const T* v, T* o) {
   o[2] = v[0] * (-2 * w * y + 2 * x * z) + v[1] * (2 * w * x + 2 * y * z) + v[2] * (w * w - x * x - y * y + z * z);
 }
 
+// Voxel SDF grids (oracle_add_sdf_grid): values [x][y][z], gradients [x][y][z][3] (rigid) or none
+// (tool), T_mesh_to_sdf (4x4 row-major), cell size and maximum (utils/sdf.py SDFInfo).
+struct SdfGridH {
+  int64_t res[3];
+  std::vector<double> val, grad;
+  double T[16];
+  double cell_size, sdf_max;
+};
+std::vector<SdfGridH> g_sdf_grids;
+
+// qd_inv_transform_by_trans_quat then qd_transform_by_T: world -> mesh frame -> voxel frame.
+template <typename T>
+void to_voxels(const oracle_collider& c, const double* cpos, const double* cquat, const T* x, T* pm, T* pv) {
+  const SdfGridH& g = g_sdf_grids[(size_t)c.sdf_grid];
+  const T d[3] = {x[0] - (T)cpos[0], x[1] - (T)cpos[1], x[2] - (T)cpos[2]};
+  const double qi[4] = {cquat[0], -cquat[1], -cquat[2], -cquat[3]};
+  quat_rot(qi, d, pm);
+  for (int r = 0; r < 3; ++r)
+    pv[r] = (T)g.T[r * 4] * pm[0] + (T)g.T[r * 4 + 1] * pm[1] + (T)g.T[r * 4 + 2] * pm[2] + (T)g.T[r * 4 + 3];
+}
+
+// Sum over the 8 corner voxels (qd.ndrange(2, 2, 2) order) of prod(1 - |p - corner|) * value.
+template <typename T>
+T trilinear(const SdfGridH& g, const std::vector<double>& f, int comps, int comp, const T* p, const int64_t* base) {
+  T acc = 0;
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b)
+      for (int e = 0; e < 2; ++e) {
+        const int64_t q[3] = {base[0] + a, base[1] + b, base[2] + e};
+        T w = 1;
+        for (int k = 0; k < 3; ++k) w *= 1 - std::fabs(p[k] - (T)q[k]);
+        acc = acc + w * (T)f[(size_t)(((q[0] * g.res[1] + q[1]) * g.res[2] + q[2]) * comps + comp)];
+      }
+  return acc;
+}
+
+// Rigid geom SDF grid (utils/sdf.py:137-184, 223-296): signed distance; gradient in `gv`.
+template <typename T>
+T rigid_grid_sdf(const oracle_collider& c, const T* pv, T eps, T* gv) {
+  const SdfGridH& g = g_sdf_grids[(size_t)c.sdf_grid];
+  bool outside = false;
+  for (int k = 0; k < 3; ++k) outside = outside || pv[k] >= (T)(g.res[k] - 1) || pv[k] <= 0;
+  if (outside) {
+    T d[3], l2 = 0;
+    for (int k = 0; k < 3; ++k) {
+      d[k] = pv[k] - (T)(g.res[k] - 1) / 2;
+      l2 += d[k] * d[k];
+    }
+    for (int k = 0; k < 3; ++k) gv[k] = d[k] / std::sqrt(l2 + eps);
+    return std::sqrt(l2) / (T)g.cell_size + (T)g.sdf_max;
+  }
+  int64_t base[3];
+  for (int k = 0; k < 3; ++k) base[k] = std::min((int64_t)std::floor(pv[k]), g.res[k] - 2);
+  for (int k = 0; k < 3; ++k) gv[k] = trilinear(g, g.grad, 3, k, pv, base);
+  return trilinear(g, g.val, 1, 0, pv, base);
+}
+
+// Mesh.sdf_ of a tool (tool_entity/mesh.py:92-107): 1 when the base voxel leaves the grid.
+template <typename T>
+T tool_grid_sdf(const SdfGridH& g, const T* pv) {
+  int64_t base[3];
+  for (int k = 0; k < 3; ++k) {
+    base[k] = (int64_t)std::floor(pv[k]);
+    if (base[k] >= g.res[k] - 1 || base[k] < 0) return 1;
+  }
+  return trilinear(g, g.val, 1, 0, pv, base);
+}
+
+// ToolEntity.advect (tool_entity.py:193-206): pose one substep later, in double.
+void tool_advance(const oracle_collider& c, double dt, double eps, double* pn, double* qn) {
+  for (int k = 0; k < 3; ++k) pn[k] = c.pos[k] + c.lin_vel[k] * dt;
+  pn[2] = std::max(pn[2], c.floor_height);  // FloorBoundary.impose_pos
+  const double rv[3] = {c.ang_vel[0] * dt, c.ang_vel[1] * dt, c.ang_vel[2] * dt};
+  const double th2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+  double u[4] = {1, 0, 0, 0};
+  if (th2 > eps * eps) {  // qd_rotvec_to_quat
+    const double th = std::sqrt(th2);
+    u[0] = std::cos(th / 2);
+    for (int k = 0; k < 3; ++k) u[k + 1] = std::sin(th / 2) / th * rv[k];
+    const double n2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2] + u[3] * u[3];
+    for (int k = 0; k < 4; ++k) u[k] *= 0.5 * (3 - n2);
+  }
+  const double* v = c.quat;  // qd_transform_quat_by_quat(quat, u) = normalize(u * quat)
+  const double q[4] = {u[0] * v[0] - u[1] * v[1] - u[2] * v[2] - u[3] * v[3],
+                       u[0] * v[1] + u[1] * v[0] + u[2] * v[3] - u[3] * v[2],
+                       u[0] * v[2] - u[1] * v[3] + u[2] * v[0] + u[3] * v[1],
+                       u[0] * v[3] + u[1] * v[2] - u[2] * v[1] + u[3] * v[0]};
+  const double len = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  for (int k = 0; k < 4; ++k) qn[k] = q[k] / len;
+}
+
+// Mesh.collide (tool_entity/mesh.py:148-177) at node position x.
+template <typename T>
+void collide_tool(const oracle_collider& c, const T* x, T* v, T dt, T eps) {
+  const SdfGridH& g = g_sdf_grids[(size_t)c.sdf_grid];
+  T pm[3], pv[3];
+  to_voxels(c, c.pos, c.quat, x, pm, pv);
+  const T sd = tool_grid_sdf(g, pv);
+  const T infl = std::min(std::exp(-sd / std::max(eps, (T)c.softness)), (T)1);
+  if (!(sd <= 0 || infl > (T)0.1)) return;
+  double pn[3], qn[4];
+  tool_advance(c, (double)dt, (double)eps, pn, qn);
+  T xn[3], vc[3];
+  quat_rot(qn, pm, xn);
+  for (int k = 0; k < 3; ++k) vc[k] = (xn[k] + (T)pn[k] - x[k]) / dt;
+  T nv[3];
+  for (int i = 0; i < 3; ++i) {  // Mesh.normal_: central differences, delta 1e-2 voxels
+    T inc[3] = {pv[0], pv[1], pv[2]}, dec[3] = {pv[0], pv[1], pv[2]};
+    inc[i] += (T)1e-2;
+    dec[i] -= (T)1e-2;
+    nv[i] = (tool_grid_sdf(g, inc) - tool_grid_sdf(g, dec)) / (2 * (T)1e-2);
+  }
+  T l = std::sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2] + eps);
+  for (int k = 0; k < 3; ++k) nv[k] /= l;
+  // R_voxels_to_mesh = inverse(T[:3, :3]) (Cramer's rule)
+  const double* M = g.T;
+  const double det = M[0] * (M[5] * M[10] - M[6] * M[9]) - M[1] * (M[4] * M[10] - M[6] * M[8]) +
+                     M[2] * (M[4] * M[9] - M[5] * M[8]);
+  const double R[9] = {(M[5] * M[10] - M[6] * M[9]) / det, (M[2] * M[9] - M[1] * M[10]) / det,
+                       (M[1] * M[6] - M[2] * M[5]) / det,  (M[6] * M[8] - M[4] * M[10]) / det,
+                       (M[0] * M[10] - M[2] * M[8]) / det, (M[2] * M[4] - M[0] * M[6]) / det,
+                       (M[4] * M[9] - M[5] * M[8]) / det,  (M[1] * M[8] - M[0] * M[9]) / det,
+                       (M[0] * M[5] - M[1] * M[4]) / det};
+  T nm[3], n[3];
+  for (int r = 0; r < 3; ++r) nm[r] = (T)R[r * 3] * nv[0] + (T)R[r * 3 + 1] * nv[1] + (T)R[r * 3 + 2] * nv[2];
+  quat_rot(c.quat, nm, n);
+  l = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2] + eps);
+  for (int k = 0; k < 3; ++k) n[k] /= l;
+  T rv[3];
+  for (int k = 0; k < 3; ++k) rv[k] = v[k] - vc[k];
+  const T nc = rv[0] * n[0] + rv[1] * n[1] + rv[2] * n[2];
+  if (!(nc < 0)) return;
+  T rt[3];
+  for (int k = 0; k < 3; ++k) rt[k] = rv[k] - nc * n[k];
+  const T rtn = std::sqrt(rt[0] * rt[0] + rt[1] * rt[1] + rt[2] * rt[2] + eps);
+  const T keep = std::max((T)0, rtn + nc * (T)c.friction);
+  for (int k = 0; k < 3; ++k) v[k] = vc[k] + rt[k] / rtn * keep * infl + rv[k] * (1 - infl);
+}
+
 // Signed distance and unit normal: sphere and plane as utils/sdf.py:119-126, 372-378; a box by
 // its exact distance function (outside: the clamped offset; inside: the nearest face).
 template <typename T>
 T collider_sdf(const oracle_collider& c, const T* x, T eps, T* n) {
+  if (c.type == 3) {  // SDF grid: utils/sdf.py sdf_func_world / sdf_func_normal_world
+    T pm[3], pv[3], gv[3], gw[3];
+    to_voxels(c, c.pos, c.quat, x, pm, pv);
+    const T sd = rigid_grid_sdf(c, pv, eps, gv);
+    quat_rot(c.quat, gv, gw);
+    const T gn = std::sqrt(gw[0] * gw[0] + gw[1] * gw[1] + gw[2] * gw[2] + eps);
+    for (int k = 0; k < 3; ++k) n[k] = gw[k] / gn;
+    return sd;
+  }
   T d[3] = {x[0] - (T)c.pos[0], x[1] - (T)c.pos[1], x[2] - (T)c.pos[2]};
   if (c.type == 0) {
     const T ln = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2] + eps);
@@ -547,9 +698,11 @@ void collide_in(size_t ci, const T* x, T* v, T mass, const T* n, T influence, T 
 // influence exceeds 0.1 at x, in order.
 template <typename T>
 void collide_node(int scene, const T* x, T* v, T mass, T dt, T eps) {
+  for (const oracle_collider& c : g_colliders)  // tools first (legacy_coupler.py:386-387)
+    if (c.type == 4 && (c.scene < 0 || c.scene == scene)) collide_tool<T>(c, x, v, dt, eps);
   for (size_t ci = 0; ci < g_colliders.size(); ++ci) {
     const oracle_collider& c = g_colliders[ci];
-    if (c.scene >= 0 && c.scene != scene) continue;
+    if (c.type == 4 || (c.scene >= 0 && c.scene != scene)) continue;
     T n[3];
     const T sd = collider_sdf(c, x, eps, n);
     const T influence = std::min(std::exp(-sd / std::max((T)1e-10, (T)c.softness)), (T)1);
@@ -611,7 +764,7 @@ int cpic_separating(int scene, const double* pn, const T* xc, T eps) {
   const size_t nc = g_colliders.size();
   for (size_t ci = 0; ci < nc; ++ci) {
     const oracle_collider& c = g_colliders[ci];
-    if (c.scene >= 0 && c.scene != scene) continue;
+    if (c.type == 4 || (c.scene >= 0 && c.scene != scene)) continue;
     T n[3];
     collider_sdf(c, xc, eps, n);
     if ((T)pn[ci * 3] * n[0] + (T)pn[ci * 3 + 1] * n[1] + (T)pn[ci * 3 + 2] * n[2] < 0) return (int)ci;
@@ -695,7 +848,7 @@ int run(const oracle_scene* sc, const oracle_material* mats, int n_mats, int64_t
         if (!active[i]) continue;
         for (size_t ci = 0; ci < ncol; ++ci) {
           const oracle_collider& c = g_colliders[ci];
-          if (c.scene >= 0 && c.scene != 0) continue;
+          if (c.type == 4 || (c.scene >= 0 && c.scene != 0)) continue;
           T nr[3];
           collider_sdf(c, pos + i * 3, S.eps, nr);
           double* pn = g_cpic_normal.data() + ((size_t)i * ncol + ci) * 3;
@@ -873,6 +1026,13 @@ int run(const oracle_scene* sc, const oracle_material* mats, int n_mats, int64_t
     }
     if (nan) return 4;
     ++g_ff_step;  // the noise field draws anew every substep
+    for (oracle_collider& c : g_colliders)  // tools move (ToolEntity.advect)
+      if (c.type == 4) {
+        double pn[3], qn[4];
+        tool_advance(c, (double)S.dt, (double)S.eps, pn, qn);
+        std::memcpy(c.pos, pn, sizeof(pn));
+        std::memcpy(c.quat, qn, sizeof(qn));
+      }
   }
   return 0;
 }
@@ -958,6 +1118,32 @@ void oracle_coupled_vel(int kind, double* out) {
 void oracle_set_force_fields(int n, const oracle_force_field* f) {
   g_ffs.assign(f, f + n);
   g_ff_step = 0;
+}
+
+// Voxel SDF grid for collider types 3 and 4; returns its index (0, 1, ... in call order).
+int oracle_add_sdf_grid(const int32_t* res, const float* values, const float* grads, const double* T_mesh_to_sdf,
+                        double cell_size, double sdf_max) {
+  SdfGridH g;
+  for (int k = 0; k < 3; ++k) g.res[k] = res[k];
+  const size_t nv = (size_t)res[0] * res[1] * res[2];
+  g.val.assign(values, values + nv);
+  if (grads) g.grad.assign(grads, grads + 3 * nv);
+  std::memcpy(g.T, T_mesh_to_sdf, sizeof(g.T));
+  g.cell_size = cell_size;
+  g.sdf_max = sdf_max;
+  g_sdf_grids.push_back(std::move(g));
+  return (int)g_sdf_grids.size() - 1;
+}
+
+// Drops every SDF grid (ids restart at 0).
+void oracle_clear_sdf_grids() { g_sdf_grids.clear(); }
+
+// Current collider poses (tools advance every substep): out [n][7] = pos, quat.
+void oracle_collider_poses(double* out) {
+  for (size_t i = 0; i < g_colliders.size(); ++i) {
+    std::memcpy(out + i * 7, g_colliders[i].pos, sizeof(double) * 3);
+    std::memcpy(out + i * 7 + 3, g_colliders[i].quat, sizeof(double) * 4);
+  }
 }
 
 // Reaction force and torque accumulated on each collider: out [n][6].

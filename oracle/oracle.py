@@ -66,6 +66,9 @@ class _Collider(ctypes.Structure):
         ("friction", ctypes.c_double),
         ("softness", ctypes.c_double),
         ("restitution", ctypes.c_double),
+        ("sdf_grid", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
+        ("floor_height", ctypes.c_double),
     ]
 
 
@@ -99,6 +102,12 @@ def load():
         lib.oracle_set_force_fields.restype = None
         lib.oracle_collider_forces.argtypes = [P]
         lib.oracle_collider_forces.restype = None
+        lib.oracle_add_sdf_grid.argtypes = [P, P, P, P, ctypes.c_double, ctypes.c_double]
+        lib.oracle_add_sdf_grid.restype = ctypes.c_int
+        lib.oracle_clear_sdf_grids.argtypes = []
+        lib.oracle_clear_sdf_grids.restype = None
+        lib.oracle_collider_poses.argtypes = [P]
+        lib.oracle_collider_poses.restype = None
         lib.oracle_set_cpic.argtypes = [ctypes.c_int]
         lib.oracle_set_cpic.restype = None
         lib.oracle_set_coupled.argtypes = [ctypes.c_int, ctypes.c_int64, P, P, P, P]
@@ -192,6 +201,29 @@ def set_colliders(colliders) -> None:
     n = len(colliders)
     arr = (_Collider * max(1, n))(*[_Collider.from_buffer_copy(bytes(c)) for c in colliders])
     lib.oracle_set_colliders(n, arr)
+
+
+def add_sdf_grid(values, grads, T_mesh_to_sdf, cell_size, sdf_max) -> int:
+    """Voxel SDF grid for colliders of type 3 (rigid, with gradients) and 4 (tool, grads None);
+    returns its id (0, 1, ... in call order, like the library's mpm_add_sdf_grid)."""
+    lib = load()
+    v = np.ascontiguousarray(values, np.float32)
+    g = None if grads is None else np.ascontiguousarray(grads, np.float32)
+    res = np.asarray(v.shape, np.int32)
+    T = np.ascontiguousarray(T_mesh_to_sdf, np.float64)
+    return lib.oracle_add_sdf_grid(res.ctypes.data, v.ctypes.data, None if g is None else g.ctypes.data, T.ctypes.data,
+                                   float(cell_size), float(sdf_max))
+
+
+def clear_sdf_grids() -> None:
+    load().oracle_clear_sdf_grids()
+
+
+def collider_poses(n) -> np.ndarray:
+    """[n, 7] current pose (pos, quat wxyz) of each collider; tools advance every substep."""
+    out = np.zeros((n, 7))
+    load().oracle_collider_poses(out.ctypes.data)
+    return out
 
 
 def set_force_fields(fields) -> None:

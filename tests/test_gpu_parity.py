@@ -398,6 +398,72 @@ def test_rigid_colliders_match_oracle(gs, oracle):
     solver.set_colliders([])
 
 
+def _box_sdf(half):
+    half = np.asarray(half)
+
+    def f(p):
+        q = np.abs(p) - half
+        return np.linalg.norm(np.maximum(q, 0.0), axis=-1) + np.minimum(q.max(axis=-1), 0.0)
+
+    return f
+
+
+def test_sdf_grid_and_tool_colliders_match_oracle(gs, oracle):
+    """A rigid geom given by an SDF grid (utils/sdf.py: trilinear value and gradient, proxy outside
+    the grid) and a moving, spinning tool entity (tool_entity/mesh.py: voxel SDF, central-difference
+    normal, friction and softness, pose advanced every substep) in the grid op: particle state,
+    the rigid geom's reaction and the tool's pose after 60 substeps against the FP64 oracle."""
+    from genesis_gb300.coupling import Collider, SDFGrid, tool
+
+    scene, cube, mat = c1_scene(gs, size=0.12)
+    solver = scene.sim.mpm_solver
+    st = solver.get_state()
+    vel = st.vel.clone()
+    vel[..., 2] = -2.0
+    st.vel = vel
+    solver.set_state(0, st)
+    box = SDFGrid.from_function(_box_sdf((0.03, 0.04, 0.015)), (-0.06,) * 3, (0.06,) * 3, 33)
+    knob = SDFGrid.from_function(lambda p: np.linalg.norm(p, axis=-1) - 0.025, (-0.05,) * 3, (0.05,) * 3, 25,
+                                 grads=False)
+    cols = [
+        tool(knob, pos=(0.45, 0.5, 0.31), vel=(0.0, 0.0, 0.5), ang=(0.0, 0.0, 4.0), friction=0.3,
+             coup_softness=0.002),
+        Collider("sdf", sdf=box, pos=(0.56, 0.52, 0.30), quat=(np.cos(0.3), 0.0, np.sin(0.3), 0.0),
+                 coup_friction=0.2, coup_restitution=0.3, coup_softness=0.004),
+    ]
+    solver.set_colliders(cols)
+    st0 = solver.get_state()
+    n_sub = 60
+    for _ in range(n_sub):
+        scene.step()
+    st1 = solver.get_state()
+    f_gpu = solver.get_collider_forces()
+    pose_gpu = solver.get_collider_poses()
+    oracle.clear_sdf_grids()
+    ids = [oracle.add_sdf_grid(g.values, g.grads, g.T_mesh_to_sdf, g.cell_size, g.sdf_max) for g in (knob, box)]
+    recs = [c.to_c(i) for c, i in zip(cols, ids)]
+    o_scene, o_mat = oracle_scene_for(oracle, solver), [oracle.from_c_material(mat.to_c(0))]
+    oracle.set_colliders(recs)
+    try:
+        ref, _, _ = oracle.run(o_scene, o_mat, oracle_state(st0), n_sub)
+        f_ref = oracle.collider_forces(len(cols))
+        pose_ref = oracle.collider_poses(len(cols))
+    finally:
+        oracle.set_colliders([])
+    free, _, _ = oracle.run(o_scene, o_mat, oracle_state(st0), n_sub)
+    oracle.clear_sdf_grids()
+    assert np.abs(free["pos"] - ref["pos"]).max() > 5e-3  # both colliders pushed particles
+    assert np.abs(f_ref[1, :3]).max() > 1.0, f_ref
+    assert np.all(f_ref[0] == 0.0)  # a tool takes no reaction
+    err = np.abs(st1.pos[0].double().cpu().numpy() - ref["pos"]).max()
+    assert err <= POS_TOL, err
+    assert np.abs(st1.vel[0].double().cpu().numpy() - ref["vel"]).max() < 5e-3
+    assert np.allclose(f_gpu, f_ref, rtol=2e-3, atol=2e-3 * np.abs(f_ref).max()), (f_gpu, f_ref)
+    assert np.abs(pose_gpu - pose_ref).max() < 1e-5, (pose_gpu, pose_ref)
+    assert abs(pose_ref[0, 2] - (0.31 + 0.5 * n_sub * solver.substep_dt)) < 1e-9
+    solver.set_colliders([])
+
+
 def test_cpic_thin_blade_matches_oracle(gs, oracle):
     """CPIC (mpm_solver.py:389-411, 445-459; legacy_coupler.py:503-529): a thin static blade through
     an elastic cube that moves into it.  Nodes behind the blade take nothing from a particle in
