@@ -251,7 +251,7 @@ def run_ours(args, rank, world):
         _lib.check(lib.mpm_set_tuning(solver.ctx, t, pp, 1, gt), solver.ctx, "mpm_set_tuning")
         tuning, tune_ms = (t, pp, gt), {}
     else:
-        tuning, tune_ms = autotune(solver.ctx, substeps=4, repeats=1, use_cache=False)
+        tuning, tune_ms = autotune(solver.ctx, substeps=10, repeats=2, use_cache=False)
     for _ in range(args.warmup):
         scene.step()
     torch.cuda.synchronize()

@@ -263,7 +263,7 @@ int launch_sort(mpm_ctx* ctx, const KParams& P, cudaStream_t s) {
   CKL();
   if (P.n > 0 || P.steps || P.nlist_reset || P.colliders_rw) {
     Timer t(ctx, s, KT_PERM);
-    k_perm<<<ctx->io_blocks, 256, 0, s>>>(P);
+    k_perm<<<ctx->n_sm * 8, 256, 0, s>>>(P);  // one wave; four particles per thread and pass
   }
   CKL();
   return MPM_OK;

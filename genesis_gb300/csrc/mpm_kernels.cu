@@ -982,10 +982,29 @@ __device__ __noinline__ float4 cpic_g2p_node(const KParams& P, const SceneDev& S
 // Bucket permutation of the sort; also the end-of-substep bookkeeping.
 __global__ void k_perm(KParams P) {
   const int64_t n = P.n_dev ? *P.n_dev : P.n;
-  for (int64_t i = grid_stride_begin(); i < n; i += grid_stride_step()) {
-    const int64_t dst = P.offset[P.key[i]] + P.rank[i];
-    P.perm[dst] = (int32_t)i;
-    P.slot_cell[dst] = P.cell8[i];  // P2G reads each slot's cell without gathering its position
+  const int64_t stride = grid_stride_step();
+  // four particles per thread and pass, their loads issued together
+  for (int64_t i0 = grid_stride_begin(); i0 < n; i0 += 4 * stride) {
+    int32_t key[4], rank[4];
+    uint8_t cell[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int64_t i = i0 + u * stride;
+      key[u] = i < n ? P.key[i] : 0;
+      rank[u] = i < n ? P.rank[i] : 0;
+      cell[u] = i < n ? P.cell8[i] : 0;
+    }
+    int32_t off[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) off[u] = i0 + u * stride < n ? P.offset[key[u]] : 0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int64_t i = i0 + u * stride;
+      if (i >= n) break;
+      const int64_t dst = (int64_t)off[u] + rank[u];
+      P.perm[dst] = (int32_t)i;
+      P.slot_cell[dst] = cell[u];  // P2G reads each slot's cell without gathering its position
+    }
   }
   if (P.nlist_reset && blockIdx.x == 0 && threadIdx.x == 0) *P.nlist_reset = 0;  // cleared by the fused G2P
   if (P.ff_step && P.ff_step_advance && blockIdx.x == 0 && threadIdx.x == 0) *P.ff_step += 1;  // end of a substep

@@ -31,7 +31,7 @@ constexpr int BLK = 4;                       // grid block edge (nodes)
 constexpr int BLK_NODES = BLK * BLK * BLK;   // 64
 constexpr int TILE = BLK + 2;                // P2G shared tile edge: block + stencil reach
 constexpr int TILE_NODES = TILE * TILE * TILE;  // 216
-constexpr int SCAN_TILE = 2048;              // buckets per scan CTA (256 threads x 8)
+constexpr int SCAN_TILE = 512;               // buckets per scan CTA (256 threads x 2)
 constexpr int SCAN_THREADS = 256;
 constexpr int64_t SCAN_SINGLE_MAX = 4096;     // bucket count up to which one CTA scans
 constexpr int SVD_SWEEPS = 4;
