@@ -163,3 +163,14 @@ def test_emitter_geometry_helpers_follow_reference_conventions():
     p = shell_to_particles(0.01, (0, 0, 0), 0.04, 0.1, "regular")
     r = np.linalg.norm(p, axis=1)
     assert len(p) > 0 and r.min() >= 0.04 and r.max() <= 0.1
+
+
+def test_autotuner_keeps_the_default_shape_within_its_margin():
+    from genesis_gb300.autotune import CANDIDATES, DEFAULT, MARGIN, choose
+
+    t = {f"{a}x{b}/{c}": 1.0 for a, b, c in CANDIDATES}
+    t["64x2/128"] = 1.0 - MARGIN / 2  # within the margin: noise
+    assert choose(t) == DEFAULT
+    t["64x2/128"] = 1.0 - 2 * MARGIN  # a clear gain
+    assert choose(t) == (64, 2, 128)
+    assert choose({"64x2/128": 2.0, "128x1/128": 1.0}, ((64, 2, 128), (128, 1, 128))) == (128, 1, 128)
