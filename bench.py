@@ -648,13 +648,20 @@ def run_diff(steps=64, substeps_per_step=10, ckpt_steps=16, seed=99):
         loss.backward()
         return loss
 
-    sim.rollout(x, v0.detach(), E.detach(), 20)  # warm-up
+    torch.cuda.empty_cache()  # the earlier forms' cached blocks: the backward sizes its segments by free memory
+    free_gb = torch.cuda.mem_get_info()[0] / 1e9
+    # warm-up: one whole forward + backward (the first one also pays the allocation of the ~8 GB of
+    # segment states and grids, several seconds on some boxes), then the timed one
+    fwd_bwd()
+    v0.grad = None
+    E.grad = None
     t = _timed(fwd_bwd)
     return {
         "workload": f"elastic cube {n} particles, 97^3 grid, {steps} steps x {substeps_per_step} substeps, "
                     f"checkpoint every {ckpt_steps} steps, grads w.r.t. v0 and per-particle E",
         "n_particles": n, "seconds_fwd_bwd": t, "value": n * n_sub / t, "unit": "particle-substeps/s (fwd+bwd)",
         "grad_v0": v0.grad.tolist(), "grad_E_norm": float(E.grad.norm()),
+        "backward_mode": getattr(sim, "last_backward", None), "free_device_gb": free_gb,
     }
 
 

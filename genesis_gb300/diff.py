@@ -181,7 +181,8 @@ class _Rollout(torch.autograd.Function):
         glam = torch.zeros_like(lam)
         starts = sorted(ctx.ckpts)
         seg_max = max((starts[i + 1] if i + 1 < len(starts) else n_sub) - starts[i] for i in range(len(starts)))
-        if sim.segment_bytes(n, seg_max) <= sim.grid_budget_bytes():
+        sim.last_backward = "segments" if sim.segment_bytes(n, seg_max) <= sim.grid_budget_bytes() else "substeps"
+        if sim.last_backward == "segments":
             # whole segments per library call: re-simulate keeping states and grids, then walk back
             gp = torch.zeros((2, 24 * n), device=g_x.device)
             gp[0, : 3 * n] = g[0].reshape(-1)
