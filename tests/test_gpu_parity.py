@@ -720,3 +720,30 @@ def test_device_regular_sampling_equals_host(gs, shape, size, p_size):
     dev = morphs.sample_regular_on_device(shape, pos, size, p_size).cpu().numpy()
     assert dev.shape == host.shape
     assert np.array_equal(dev, host.astype(np.float32))
+
+
+def test_reference_scenario_cube_settles_on_coupled_plane(gs):
+    """The MPM part of the reference's tests/test_deformable_physics.py::test_deformable_parallel,
+    through the drop-in API: an Elastic(rho=200) cube in MPMOptions(lower_bound=(0.5, -0.1, -0.05),
+    upper_bound=(0.7, 0.1, 0.3)) dropped on the coupled ground plane (Rigid needs_coup,
+    coup_friction=0; a kinematic plane collider here), 2 envs, dt 2e-3 x 10 substeps, 1500 steps:
+    the cube moved, stays above the ground (z > -1e-5) and comes to rest (|v| <= 1e-4)."""
+    from genesis_gb300.coupling import Collider
+
+    scene = gs.Scene(
+        sim_options=gs.options.SimOptions(dt=2e-3, substeps=10),
+        mpm_options=gs.options.MPMOptions(lower_bound=(0.5, -0.1, -0.05), upper_bound=(0.7, 0.1, 0.3)),
+    )
+    cube = scene.add_entity(material=gs.materials.MPM.Elastic(rho=200),
+                            morph=gs.morphs.Box(pos=(0.6, 0.0, 0.1), size=(0.1, 0.1, 0.1)))
+    scene.build(n_envs=2)
+    scene.sim.mpm_solver.set_colliders([Collider("plane", pos=(0.0, 0.0, 0.0), normal=(0.0, 0.0, 1.0),
+                                                 coup_friction=0.0)])
+    init = cube.get_particles_pos().clone()
+    for _ in range(1500):
+        scene.step()
+    final = cube.get_particles_pos()
+    assert (init - final).abs().sum().item() > 0.1
+    assert final[..., 2].min().item() > -1e-5
+    assert cube.get_particles_vel().abs().max().item() <= 1e-4
+    scene.sim.mpm_solver.set_colliders([])
