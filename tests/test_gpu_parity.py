@@ -747,3 +747,41 @@ def test_reference_scenario_cube_settles_on_coupled_plane(gs):
     assert final[..., 2].min().item() > -1e-5
     assert cube.get_particles_vel().abs().max().item() <= 1e-4
     scene.sim.mpm_solver.set_colliders([])
+
+
+def test_reference_scenario_particle_constraints_follow_link(gs):
+    """The reference's tests/test_deformable_physics.py::test_mpm_particle_constraints through the
+    drop-in API, with the fixed rigid box as a kinematic link (its pose given by set_link_poses):
+    bbox selection gives an (n_envs, n_particles) mask that selects some but not all particles; the
+    attached particles follow the link moved by +0.2 m in x over 30 steps of 20 substeps.
+
+    Stiffness 1e4 instead of the reference test's 1e5: with particle mass 1e-3 kg and substep 1e-4 s,
+    k = 1e5 gives dt * sqrt(k / m) = 1, where the explicit critically damped update of
+    apply_particle_constraints has an eigenvalue of magnitude 1.62 for a lone particle; this run then
+    diverges (NaN), so only the grid coupling of the reference's own sampling can keep it bounded.
+    At k = 1e4 (dt * sqrt(k / m) = 0.32) the update is stable."""
+    from genesis_gb300.coupling import Collider
+
+    scene = gs.Scene(
+        sim_options=gs.options.SimOptions(dt=2e-3, substeps=20),
+        mpm_options=gs.options.MPMOptions(lower_bound=(-1.0, -1.0, 0.0), upper_bound=(1.0, 1.0, 1.0),
+                                          grid_density=64),
+    )
+    cube = scene.add_entity(material=gs.materials.MPM.Elastic(E=5e4, nu=0.3, rho=1000),
+                            morph=gs.morphs.Box(pos=(0.0, 0.0, 0.35), size=(0.15, 0.15, 0.15)))
+    scene.build(n_envs=2)
+    solver = scene.sim.mpm_solver
+    solver.set_colliders([Collider("plane", normal=(0.0, 0.0, 1.0))])  # gs.morphs.Plane()
+    box_pos = np.array([0.0, 0.0, 0.55])
+    solver.set_link_poses(box_pos[None], np.array([[1.0, 0.0, 0.0, 0.0]]))
+    mask = cube.get_particles_in_bbox((-0.08, -0.08, 0.41), (0.08, 0.08, 0.44))
+    assert tuple(mask.shape) == (2, cube.n_particles)
+    assert mask.any() and not mask.all()
+    cube.set_particle_constraints(mask, 0, stiffness=1e4)
+    x0 = cube.get_particles_pos()[:, mask[0], 0].mean()
+    solver.set_link_poses((box_pos + np.array([0.2, 0.0, 0.0]))[None], np.array([[1.0, 0.0, 0.0, 0.0]]))
+    for _ in range(30):
+        scene.step()
+    moved = cube.get_particles_pos()[:, mask[0], 0].mean() - x0
+    assert moved.item() > 0.2 * 0.3, moved.item()
+    solver.set_colliders([])
