@@ -90,3 +90,24 @@ def test_pool_slot_reuse_after_retire():
         assert err <= POS_TOL, (r.rid, err)
         alone.close()
     srv.close()
+
+
+def test_served_results_equal_alone_in_a_wide_pool():
+    """A pool with many buckets (16 slots of 129^3 grids: 575k buckets, 1,123 scan tiles, several
+    waves of scan CTAs in the look-back): each request's result is still the one it gets alone."""
+    from genesis_gb300.batched import BatchedMPM
+    from genesis_gb300.serve import MPMServer, serving_workload
+
+    reqs = serving_workload(n_requests=6, rate_hz=0, seed=9, n_range=(2000, 30000), grid_res=(65, 129),
+                            substep_range=(20, 60))
+    srv = MPMServer(max_slots=16, particle_capacity=400_000, max_grid_res=129, chunk=10)
+    stats = srv.run(reqs, keep_results=True, realtime=False)
+    assert stats["requests"] == len(reqs) and stats["status"] == 0
+    for r in reqs:
+        alone = BatchedMPM([r.spec], tune=False)
+        alone.step(r.spec.substeps)
+        ref = alone.scene_state(0)
+        err = (r.result["pos"] - ref["pos"]).abs().max().item()
+        assert err <= POS_TOL, (r.rid, err)
+        alone.close()
+    srv.close()
