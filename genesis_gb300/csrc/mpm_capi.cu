@@ -10,6 +10,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "gbmpm.h"
 #include "mpm_kernels.cuh"
 
@@ -132,6 +134,12 @@ struct mpm_ctx {
 };
 
 namespace {
+
+// NVTX range over an entry point (visible in Nsight timelines; a no-op without a tool attached).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
 
 int fail(mpm_ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg;
@@ -768,6 +776,7 @@ int mpm_add_particles(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end, int6
 
 int mpm_get_state(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end, float* pos, float* vel, float* C, float* F,
                   float* Jp, uint8_t* active, void* stream) {
+  NvtxRange nvtx_range("mpm_get_state");
   if (!ctx) return MPM_ERR_BAD_ARG;
   if (!scene_range_ok(ctx, scene_begin, scene_end)) return fail(ctx, MPM_ERR_BAD_ARG, "bad scene range");
   if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "get_state inside a substep");
@@ -788,6 +797,7 @@ int mpm_get_state(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end, float* p
 
 int mpm_set_state(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end, const float* pos, const float* vel,
                   const float* C, const float* F, const float* Jp, const uint8_t* active, void* stream) {
+  NvtxRange nvtx_range("mpm_set_state");
   if (!ctx) return MPM_ERR_BAD_ARG;
   if (!scene_range_ok(ctx, scene_begin, scene_end)) return fail(ctx, MPM_ERR_BAD_ARG, "bad scene range");
   if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "set_state inside a substep");
@@ -859,6 +869,7 @@ int mpm_set_gravity(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end, const 
 }
 
 int mpm_substeps(mpm_ctx* ctx, int32_t n_substeps, void* stream) {
+  NvtxRange nvtx_range("mpm_substeps");
   if (!ctx) return MPM_ERR_BAD_ARG;
   if (n_substeps < 0) return fail(ctx, MPM_ERR_BAD_ARG, "negative substep count");
   if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "mpm_substeps inside a split substep");
@@ -891,6 +902,7 @@ int mpm_substeps(mpm_ctx* ctx, int32_t n_substeps, void* stream) {
 }
 
 int mpm_substep_pre(mpm_ctx* ctx, void* stream) {
+  NvtxRange nvtx_range("mpm_substep_pre");
   if (!ctx) return MPM_ERR_BAD_ARG;
   if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "substep_pre called twice");
   int r = enter(ctx, stream);
@@ -902,6 +914,7 @@ int mpm_substep_pre(mpm_ctx* ctx, void* stream) {
 }
 
 int mpm_substep_grid_op(mpm_ctx* ctx, void* stream) {
+  NvtxRange nvtx_range("mpm_substep_grid_op");
   if (!ctx) return MPM_ERR_BAD_ARG;
   if (ctx->phase != 1) return fail(ctx, MPM_ERR_STATE, "grid_op must follow substep_pre");
   int r = enter(ctx, stream);
@@ -912,6 +925,7 @@ int mpm_substep_grid_op(mpm_ctx* ctx, void* stream) {
 }
 
 int mpm_substep_post(mpm_ctx* ctx, void* stream) {
+  NvtxRange nvtx_range("mpm_substep_post");
   if (!ctx) return MPM_ERR_BAD_ARG;
   if (ctx->phase != 2) return fail(ctx, MPM_ERR_STATE, "substep_post must follow grid_op");
   int r = enter(ctx, stream);
@@ -924,6 +938,7 @@ int mpm_substep_post(mpm_ctx* ctx, void* stream) {
 }
 
 int mpm_get_grid(mpm_ctx* ctx, int64_t scene, float* out, void* stream) {
+  NvtxRange nvtx_range("mpm_get_grid");
   if (!ctx) return MPM_ERR_BAD_ARG;
   if (scene < 0 || scene >= ctx->n_scenes || !out) return fail(ctx, MPM_ERR_BAD_ARG, "bad args");
   const int g = ctx->phase == 0 ? (ctx->cur ^ 1) : ctx->cur;
@@ -991,6 +1006,7 @@ int mpm_set_force_fields(mpm_ctx* ctx, int32_t n, const mpm_force_field* fields)
 }
 
 int mpm_set_colliders(mpm_ctx* ctx, int32_t n, const mpm_collider* colliders) {
+  NvtxRange nvtx_range("mpm_set_colliders");
   if (!ctx) return MPM_ERR_BAD_ARG;
   if (n < 0 || n > MAX_COLLIDERS || (n > 0 && !colliders)) return fail(ctx, MPM_ERR_BAD_ARG, "bad collider arguments");
   if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "colliders inside a substep");
@@ -1371,6 +1387,7 @@ int mpm_sample_regular(int32_t shape, const double* pos, const double* size, dou
 int mpm_render_fields(mpm_ctx* ctx, int64_t scene_begin, int64_t scene_end, float* pos_out, float* vel_out,
                       uint8_t* active_out, int64_t n_vverts, int32_t n_supports, const int32_t* support_idx,
                       const float* support_w, float* vvert_pos_out, uint8_t* vvert_active_out, void* stream) {
+  NvtxRange nvtx_range("mpm_render_fields");
   if (!ctx) return MPM_ERR_BAD_ARG;
   if (!scene_range_ok(ctx, scene_begin, scene_end)) return fail(ctx, MPM_ERR_BAD_ARG, "bad scene range");
   if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "render fields inside a substep");
@@ -1561,6 +1578,7 @@ int mpm_ctx_create_pool(const mpm_pool_config* cfg, int32_t device, mpm_ctx** ou
 int mpm_scene_admit(mpm_ctx* ctx, int64_t slot, const mpm_scene_config* scene, const mpm_material* materials,
                     int32_t n_materials, int64_t n, const float* pos, const int32_t* mat_local, int32_t n_substeps,
                     void* stream) {
+  NvtxRange nvtx_range("mpm_scene_admit");
   if (!ctx || !scene || !materials || !pos) return MPM_ERR_BAD_ARG;
   if (!ctx->pool) return fail(ctx, MPM_ERR_STATE, "not a pool context");
   if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "admit inside a substep");
@@ -1613,6 +1631,7 @@ int mpm_scene_admit(mpm_ctx* ctx, int64_t slot, const mpm_scene_config* scene, c
 }
 
 int mpm_scene_retire(mpm_ctx* ctx, int64_t slot, void* stream) {
+  NvtxRange nvtx_range("mpm_scene_retire");
   if (!ctx) return MPM_ERR_BAD_ARG;
   if (!ctx->pool) return fail(ctx, MPM_ERR_STATE, "not a pool context");
   if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "retire inside a substep");

@@ -8,7 +8,8 @@ changes).  Between chunks of substeps it:
   * admits waiting requests in arrival order while a slot, pool particles and the HBM budget
     (particle + grid bytes, capped at `mem_fraction` of device memory) allow;
   * retires scenes whose substep budget reached zero (a finished scene is frozen on the
-    device, so overshooting the chunk does not change its result), after copying its state.
+    device, so overshooting the chunk does not change its result), after copying its state;
+  * drops or retires cancelled requests (`cancel`), freeing their slot and memory.
 Latency of a request = completion time - arrival time.  The reference has no serving mode;
 the loop is the GB300 form of running many Genesis scenes.
 """
@@ -41,6 +42,7 @@ class Request:
     finished: float | None = None
     result: dict | None = None
     payload: np.ndarray | None = None  # initial particle positions [n, 3] float32, sent with the request
+    cancelled: bool = False
 
     @property
     def work(self) -> int:
@@ -109,6 +111,7 @@ class MPMServer:
         self.live_bytes = 0
         self.live_particles = 0
         self.fixed_bytes = grid_bytes
+        self._cancel = set()  # request ids to drop (waiting) or retire (running) at the next check
 
     def _stream(self):
         return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
@@ -150,9 +153,17 @@ class MPMServer:
         self.live_bytes -= self.request_bytes(r)
         self.live_particles -= r.spec.n_particles
 
-    def run(self, requests, keep_results=False, realtime=True):
-        """Serve `requests` (arrival times in seconds from the start).  Returns stats."""
+    def cancel(self, rid: int) -> None:
+        """Cancel request `rid`: if it is waiting it is never admitted; if it is running it is
+        retired after the current chunk of substeps, without a result, and its slot and memory go
+        to the next admission.  Safe to call from `run`'s on_chunk callback."""
+        self._cancel.add(int(rid))
+
+    def run(self, requests, keep_results=False, realtime=True, on_chunk=None):
+        """Serve `requests` (arrival times in seconds from the start).  Returns stats.
+        on_chunk(server, chunk_index) is called after every chunk of substeps (e.g. to cancel)."""
         pending = sorted(requests, key=lambda r: r.arrival)
+        cancelled = []
         queue = []  # arrived, waiting: (arrival, rid, request)
         steps_left = (ctypes.c_int32 * self.max_slots)()
         t0 = time.perf_counter()
@@ -164,7 +175,16 @@ class MPMServer:
             while i < len(pending) and pending[i].arrival <= now:
                 heapq.heappush(queue, (pending[i].arrival, pending[i].rid, pending[i]))
                 i += 1
-            while queue and self.can_admit(queue[0][2]):
+            while queue:
+                r = queue[0][2]
+                if r.rid in self._cancel:  # cancelled while waiting: never admitted
+                    heapq.heappop(queue)
+                    self._cancel.discard(r.rid)
+                    r.cancelled, r.finished = True, time.perf_counter() - t0
+                    cancelled.append(r)
+                    continue
+                if not self.can_admit(r):
+                    break
                 self.admit(heapq.heappop(queue)[2], time.perf_counter() - t0)
             if not self.live:
                 if queue and not self.can_admit(queue[0][2]):
@@ -175,7 +195,15 @@ class MPMServer:
             _lib.check(self.lib.mpm_substeps(self.ctx, self.chunk, self._stream()), self.ctx, "mpm_substeps")
             chunks += 1
             _lib.check(self.lib.mpm_scene_steps_left(self.ctx, steps_left, self._stream()), self.ctx, "steps_left")
+            if on_chunk is not None:
+                on_chunk(self, chunks - 1)
             now = time.perf_counter() - t0
+            for slot in [s for s, r in self.live.items() if r.rid in self._cancel]:  # cancelled while running
+                r = self.live[slot]
+                self._cancel.discard(r.rid)
+                self.retire(slot, now, keep_result=False)
+                r.cancelled = True
+                cancelled.append(r)
             for slot in [s for s in self.live if steps_left[s] == 0]:
                 r = self.live[slot]
                 self.retire(slot, now, keep_results)
@@ -194,6 +222,7 @@ class MPMServer:
             "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
             "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
             "chunks": chunks,
+            "cancelled": len(cancelled),
             "status": st.value,
         }
 

@@ -111,3 +111,40 @@ def test_served_results_equal_alone_in_a_wide_pool():
         assert err <= POS_TOL, (r.rid, err)
         alone.close()
     srv.close()
+
+
+def test_served_cancellation_and_unadmittable_request():
+    """Host-side faults of the serving loop: a running request cancelled after its first chunk is
+    retired without a result and frees its slot; a request cancelled while waiting is never
+    admitted; the others still match their runs alone.  A request larger than the pool can never be
+    admitted and raises, and the server keeps serving afterwards."""
+    from genesis_gb300.batched import BatchedMPM
+    from genesis_gb300.serve import MPMServer, serving_workload
+
+    reqs = serving_workload(n_requests=6, rate_hz=0, seed=11, n_range=(1000, 8000), grid_res=(33, 65),
+                            substep_range=(30, 60))
+    srv = MPMServer(max_slots=2, particle_capacity=40_000, max_grid_res=65, chunk=10)
+    srv.cancel(reqs[5].rid)  # before it is admitted
+
+    def on_chunk(server, k):
+        if k == 0:
+            server.cancel(reqs[0].rid)  # running since the start
+
+    stats = srv.run(reqs, keep_results=True, realtime=False, on_chunk=on_chunk)
+    assert stats["cancelled"] == 2 and stats["requests"] == 4 and stats["status"] == 0
+    assert reqs[0].cancelled and reqs[0].result is None and reqs[0].admitted is not None
+    assert reqs[5].cancelled and reqs[5].admitted is None
+    for r in reqs[1:5]:
+        assert not r.cancelled
+        alone = BatchedMPM([r.spec], tune=False)
+        alone.step(r.spec.substeps)
+        err = (r.result["pos"] - alone.scene_state(0)["pos"]).abs().max().item()
+        assert err <= POS_TOL, (r.rid, err)
+        alone.close()
+    big = serving_workload(n_requests=1, rate_hz=0, seed=12, n_range=(60000, 60001), grid_res=(65,))
+    with pytest.raises(RuntimeError, match="can never be admitted"):
+        srv.run(big, realtime=False)
+    again = serving_workload(n_requests=2, rate_hz=0, seed=13, n_range=(1000, 3000), grid_res=(33,),
+                             substep_range=(20, 30))
+    assert srv.run(again, realtime=False)["requests"] == 2
+    srv.close()
