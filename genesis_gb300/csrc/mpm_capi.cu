@@ -704,6 +704,10 @@ int mpm_ctx_create(const mpm_scene_config* scenes, int64_t n_scenes, const mpm_m
   ctx->n = P;
   ctx->n_phys = P;
   ctx->cap = ((P + 63) / 64) * 64;
+  if (P < 65536) {  // small scenes are latency-bound: items of 64 particles spread them over more SMs
+    ctx->p2g_threads = 64;
+    ctx->ppt = 1;
+  }
   if (ctx->cap == 0) ctx->cap = 64;
 
   for (int32_t i = 0; i < n_materials; ++i) {

@@ -392,7 +392,8 @@ int mpm_status_word(mpm_ctx* ctx, uint32_t* status_host, int64_t* fp64_svd_host,
 /* Tuning knobs (the autotuner sets these): P2G threads per CTA (64..256, multiple of 32) and
  * particles per thread (threads * ppt <= 1024; the P2G work chunk is their product), G2P
  * threads per CTA (64..256, multiple of 32; 0 keeps the current value), CUDA graphs on/off.
- * A new context starts at 128 P2G threads x 2 particles, 128 G2P threads, graphs on. */
+ * A new context starts at 128 P2G threads x 2 particles (64 x 1 below 65,536 particles), 128 G2P
+ * threads, graphs on. */
 int mpm_set_tuning(mpm_ctx* ctx, int32_t p2g_threads, int32_t particles_per_thread,
                    int32_t use_graph, int32_t g2p_threads);
 
