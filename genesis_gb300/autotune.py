@@ -20,9 +20,11 @@ import torch
 from . import _lib
 
 # (P2G threads, particles per thread, G2P threads); P2G threads * ppt <= 1024
-CANDIDATES = ((64, 2, 128), (128, 1, 128), (128, 2, 128), (128, 4, 128), (256, 1, 128), (256, 2, 128),
-              (256, 4, 128), (128, 2, 64), (128, 2, 256))
-DEFAULT = (128, 2, 128)  # a new context's launch shapes (libgbmpm)
+CANDIDATES = ((64, 1, 128), (64, 2, 128), (128, 1, 128), (128, 2, 128), (128, 4, 128), (256, 1, 128),
+              (256, 2, 128), (256, 4, 128), (128, 2, 64), (128, 2, 256))
+DEFAULT = (128, 2, 128)  # a new context's launch shapes (libgbmpm) ...
+DEFAULT_SMALL = (64, 1, 128)  # ... below SMALL_PARTICLES particles
+SMALL_PARTICLES = 65536
 # another candidate replaces DEFAULT only when it is faster by more than this fraction: short
 # timing windows on the starting state cannot resolve smaller differences, which later states of
 # the same run can reverse
@@ -57,12 +59,12 @@ def _save_cache(c: dict) -> None:
         pass
 
 
-def choose(timings: dict, candidates=CANDIDATES) -> tuple:
-    """Fastest candidate of `timings` ({"TxP/G": ms}); DEFAULT unless beaten by more than MARGIN."""
+def choose(timings: dict, candidates=CANDIDATES, default=DEFAULT) -> tuple:
+    """Fastest candidate of `timings` ({"TxP/G": ms}); `default` unless beaten by more than MARGIN."""
     key = lambda c: timings[f"{c[0]}x{c[1]}/{c[2]}"]  # noqa: E731
     best = min(candidates, key=key)
-    if DEFAULT in candidates and key(best) > (1.0 - MARGIN) * key(DEFAULT):
-        return DEFAULT
+    if default in candidates and key(best) > (1.0 - MARGIN) * key(default):
+        return default
     return best
 
 
@@ -93,7 +95,9 @@ def autotune(ctx, substeps: int = 10, repeats: int = 2, use_cache: bool = True, 
             e1.synchronize()
             best = min(best, e0.elapsed_time(e1) / substeps)
         timings[f"{t}x{p}/{g}"] = best
-    choice = choose(timings, candidates)
+    n = ctypes.c_int64()
+    lib.mpm_get_info(ctx, ctypes.byref(n), None, None)
+    choice = choose(timings, candidates, DEFAULT_SMALL if n.value < SMALL_PARTICLES else DEFAULT)
     _lib.check(lib.mpm_set_tuning(ctx, choice[0], choice[1], 1, choice[2]), ctx, "mpm_set_tuning")
     cache[sig] = {"choice": list(choice), "timings": timings}
     if use_cache:
