@@ -141,21 +141,28 @@ class DifferentiableMPM:
 
     def rollout(self, x0: torch.Tensor, v0: torch.Tensor, E: torch.Tensor, n_substeps: int) -> torch.Tensor:
         """Final positions after n_substeps from positions x0 [n,3], velocities v0 ([3] or [n,3]) and
-        per-particle Young's modulus E [n]; differentiable w.r.t. x0, v0 and E."""
+        per-particle Young's modulus E [n] (C = 0, F = I at the start); differentiable w.r.t. x0, v0
+        and E."""
         n = x0.shape[0]
         v0 = v0.expand(n, 3) if v0.dim() == 1 else v0
+        C = torch.zeros((n, 3, 3), device=x0.device)
+        F = torch.eye(3, device=x0.device).repeat(n, 1, 1)
+        return self.advance((x0, v0, C, F), E, n_substeps)[0]
+
+    def advance(self, state, E: torch.Tensor, n_substeps: int):
+        """The state (x [n,3], v [n,3], C [n,3,3], F [n,3,3]) after n_substeps, differentiable w.r.t.
+        every part of the state and E.  Calls chain, so a loss may combine intermediate states (the
+        reference's differentiable mode takes losses at any frame of an episode)."""
+        x, v, C, F = state
         mu, lam = lame(E, self.nu)
-        return _Rollout.apply(self, int(n_substeps), x0, v0, mu, lam)
+        return _Advance.apply(self, int(n_substeps), x, v, C, F, mu, lam)
 
 
-class _Rollout(torch.autograd.Function):
+class _Advance(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, sim: DifferentiableMPM, n_substeps, x0, v0, mu, lam):
-        n = x0.shape[0]
-        x = x0.detach().float().contiguous()
-        v = v0.detach().float().contiguous()
-        C = torch.zeros((n, 3, 3), device=x.device)
-        F = torch.eye(3, device=x.device).repeat(n, 1, 1).contiguous()
+    def forward(ctx, sim: DifferentiableMPM, n_substeps, x0, v0, C0, F0, mu, lam):
+        f32 = lambda t: t.detach().float().contiguous()  # noqa: E731
+        x, v, C, F = f32(x0), f32(v0), f32(C0), f32(F0)
         mu_d, lam_d = mu.detach().float().contiguous(), lam.detach().float().contiguous()
         st = (x, v, C, F)
         ckpts = {}
@@ -168,15 +175,20 @@ class _Rollout(torch.autograd.Function):
         sim.check()
         ctx.sim, ctx.n_substeps, ctx.ckpts = sim, n_substeps, ckpts
         ctx.save_for_backward(mu_d, lam_d)
-        return st[0]
+        if n_substeps == 0:
+            st = tuple(t.clone() for t in st)
+        return st
 
     @staticmethod
-    def backward(ctx, g_x):
+    def backward(ctx, g_x, g_v, g_C, g_F):
         sim, n_sub = ctx.sim, ctx.n_substeps
         mu, lam = ctx.saved_tensors
-        n = g_x.shape[0]
-        g = (g_x.contiguous().float(), torch.zeros((n, 3), device=g_x.device),
-             torch.zeros((n, 3, 3), device=g_x.device), torch.zeros((n, 3, 3), device=g_x.device))
+        n = mu.shape[0]
+        dev = mu.device
+        z = lambda g, shape: (torch.zeros(shape, device=dev) if g is None else g.contiguous().float())  # noqa: E731
+        g = (z(g_x, (n, 3)), z(g_v, (n, 3)), z(g_C, (n, 3, 3)), z(g_F, (n, 3, 3)))
+        if n_sub == 0:
+            return None, None, g[0], g[1], g[2], g[3], torch.zeros_like(mu), torch.zeros_like(lam)
         gmu = torch.zeros_like(mu)
         glam = torch.zeros_like(lam)
         starts = sorted(ctx.ckpts)
@@ -184,8 +196,11 @@ class _Rollout(torch.autograd.Function):
         sim.last_backward = "segments" if sim.segment_bytes(n, seg_max) <= sim.grid_budget_bytes() else "substeps"
         if sim.last_backward == "segments":
             # whole segments per library call: re-simulate keeping states and grids, then walk back
-            gp = torch.zeros((2, 24 * n), device=g_x.device)
+            gp = torch.zeros((2, 24 * n), device=dev)
             gp[0, : 3 * n] = g[0].reshape(-1)
+            gp[0, 3 * n: 6 * n] = g[1].reshape(-1)
+            gp[0, 6 * n: 15 * n] = g[2].reshape(-1)
+            gp[0, 15 * n:] = g[3].reshape(-1)
             for seg_i in range(len(starts) - 1, -1, -1):
                 s0 = starts[seg_i]
                 s1 = starts[seg_i + 1] if seg_i + 1 < len(starts) else n_sub
@@ -193,7 +208,8 @@ class _Rollout(torch.autograd.Function):
                 sim.backward_segment(states, grids, mu, lam, gp, gmu, glam, s1 - s0)
                 del states, grids
             sim.check()
-            return None, None, gp[0, : 3 * n].view(n, 3).clone(), gp[0, 3 * n: 6 * n].view(n, 3).clone(), gmu, glam
+            return (None, None, gp[0, : 3 * n].view(n, 3).clone(), gp[0, 3 * n: 6 * n].view(n, 3).clone(),
+                    gp[0, 6 * n: 15 * n].view(n, 3, 3).clone(), gp[0, 15 * n:].view(n, 3, 3).clone(), gmu, glam)
         keep = sim.nodes * 32 * seg_max <= sim.grid_budget_bytes()  # keep every substep's grid of a segment
         for seg_i in range(len(starts) - 1, -1, -1):
             s0 = starts[seg_i]
@@ -212,4 +228,4 @@ class _Rollout(torch.autograd.Function):
                 g = sim.backward_substep(states[i], mu, lam, g, gmu, glam, grids[i] if keep else None)
             del grids
         sim.check()
-        return None, None, g[0], g[1], gmu, glam
+        return None, None, g[0], g[1], g[2], g[3], gmu, glam

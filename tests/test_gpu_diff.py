@@ -142,3 +142,82 @@ def test_checkpointing_does_not_change_gradients(oracle):
     _, _, gvb, gEb = _gpu_loss_and_grads(b, x0, v0, E, target, 32, vfield=vf, proj=pj)
     assert np.allclose(gva, gvb, rtol=1e-3, atol=1e-9 + 1e-4 * np.abs(gvb).max())
     assert np.linalg.norm(gEa - gEb) <= 1e-2 * np.linalg.norm(gEb)
+
+
+def _oracle_two_loss(O, x0, v0, E, target, n1, n2, nu=0.2, dt=2e-4, vfield=None, proj=None):
+    """Loss on the state after n1 substeps plus the loss on the state after n1 + n2 (the oracle
+    continues from its own intermediate state)."""
+    n = len(x0)
+    sc = O.make_scene(dt, grid_density=32.0, particle_size=1.0 / 64)
+    mats = []
+    for e in E:
+        mu = e / (2 * (1 + nu))
+        lam = e * nu / ((1 + nu) * (1 - 2 * nu))
+        mats.append(O.make_material(0, mu, lam, 1000.0))
+    vel = np.tile(v0, (n, 1)) + (0.0 if vfield is None else vfield)
+    st = dict(pos=x0, vel=vel, C=np.zeros((n, 3, 3)), F=np.tile(np.eye(3), (n, 1, 1)),
+              Jp=np.ones(n), mat=np.arange(n, dtype=np.int32), active=np.ones(n, bool))
+    mid, _, _ = O.run(sc, mats, st, n1)
+    st2 = dict(st, pos=mid["pos"], vel=mid["vel"], C=mid["C"], F=mid["F"], Jp=mid["Jp"])
+    end, _, _ = O.run(sc, mats, st2, n2)
+    f = lambda p: float((p * proj).sum() / n)  # noqa: E731
+    return f(mid["pos"]) + f(end["pos"])
+
+
+def test_intermediate_losses_through_chained_segments_match_fp64_differences(sim, oracle):
+    """advance() chains: a loss on the state after 16 substeps plus one after 40 (as the reference's
+    differentiable mode takes losses at several frames of an episode) gives dL/dv0 and dL/dE that
+    match FP64 central differences of the oracle; and chaining 16 + 24 substeps gives the same
+    gradient of a final-state loss as one 40-substep advance."""
+    x0, v0, E, target = _setup(seed=5)
+    n = len(x0)
+    vf, pj = _shear(x0), _proj(n)
+    cu = lambda a, g=False: torch.tensor(a, dtype=torch.float32, device="cuda", requires_grad=g)  # noqa: E731
+
+    def grads(split):
+        v = cu(v0, True)
+        e = cu(E, True)
+        s = (cu(x0), v.expand(n, 3) + cu(vf), torch.zeros((n, 3, 3), device="cuda"),
+             torch.eye(3, device="cuda").repeat(n, 1, 1))
+        P = cu(pj)
+        if split:
+            s1 = sim.advance(s, e, 16)
+            s2 = sim.advance(s1, e, 24)
+            loss = (s1[0] * P).sum() / n + (s2[0] * P).sum() / n
+        else:
+            s2 = sim.advance(s, e, 40)
+            loss = (s2[0] * P).sum() / n
+        loss.backward()
+        return v.grad.cpu().numpy().astype(np.float64), e.grad.cpu().numpy().astype(np.float64), s2
+
+    gv, gE, _ = grads(True)
+    eps = 1e-4
+    fd_v = np.zeros(3)
+    for k in range(3):
+        dv = np.zeros(3)
+        dv[k] = eps
+        fd_v[k] = (_oracle_two_loss(oracle, x0, v0 + dv, E, target, 16, 24, vfield=vf, proj=pj) -
+                   _oracle_two_loss(oracle, x0, v0 - dv, E, target, 16, 24, vfield=vf, proj=pj)) / (2 * eps)
+    assert np.linalg.norm(gv - fd_v) <= GRAD_RTOL * np.linalg.norm(fd_v), (gv, fd_v)
+    d = np.random.default_rng(3).normal(size=n)
+    d /= np.linalg.norm(d)
+    h = eps * E
+    fd_E = (_oracle_two_loss(oracle, x0, v0, E + h * d, target, 16, 24, vfield=vf, proj=pj) -
+            _oracle_two_loss(oracle, x0, v0, E - h * d, target, 16, 24, vfield=vf, proj=pj)) / (2 * eps)
+    ad_E = float(np.dot(gE, E * d))
+    assert abs(ad_E - fd_E) <= GRAD_RTOL * abs(fd_E), (ad_E, fd_E)
+
+    # one final-state loss: chained segments == one advance
+    def final_grad(split):
+        v = cu(v0, True)
+        e = cu(E, True)
+        s = (cu(x0), v.expand(n, 3) + cu(vf), torch.zeros((n, 3, 3), device="cuda"),
+             torch.eye(3, device="cuda").repeat(n, 1, 1))
+        out = sim.advance(sim.advance(s, e, 16), e, 24) if split else sim.advance(s, e, 40)
+        ((out[0] * cu(pj)).sum() / n).backward()
+        return v.grad.cpu().numpy(), e.grad.cpu().numpy()
+
+    ga, gEa = final_grad(True)
+    gb, gEb = final_grad(False)
+    assert np.allclose(ga, gb, rtol=1e-3, atol=1e-9 + 1e-4 * np.abs(gb).max()), (ga, gb)
+    assert np.linalg.norm(gEa - gEb) <= 1e-2 * np.linalg.norm(gEb)
