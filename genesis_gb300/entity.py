@@ -239,14 +239,66 @@ class MPMEntity:
         a = torch.as_tensor(actives, device="cuda").to(torch.float32)
         self._set_field(_lib.FIELD_ACTIVE, 1, a[..., None], envs_idx, particles_idx_local)
 
+    def _n_groups(self):
+        n = getattr(self._material, "n_groups", None)
+        if n is None:
+            raise GenesisException("This entity's material is not a muscle.")
+        return int(n)
+
+    def _muscle_groups(self):
+        g = getattr(self, "_muscle_group", None)
+        if g is None:
+            g = torch.zeros(self._n_particles, dtype=torch.long, device="cuda")
+            self._muscle_group = g
+        return g
+
     def set_particles_actu(self, actus, particles_idx_local=None, envs_idx=None):
+        """Per-particle actuation [B, n_sel] ([n_sel] with one env), or [B, n_sel, n_groups] from which
+        each particle takes its own group's value (mpm_solver.py:959-972)."""
         a = torch.as_tensor(actus, dtype=torch.float32, device="cuda")
+        if a.ndim == 3:
+            grp = self._muscle_groups()
+            if particles_idx_local is not None:
+                grp = grp[torch.as_tensor(particles_idx_local, device="cuda", dtype=torch.long).reshape(-1)]
+            a = torch.gather(a, 2, grp.reshape(1, -1, 1).expand(a.shape[0], -1, 1))[..., 0]
         self._set_field(_lib.FIELD_ACTU, 1, a[..., None], envs_idx, particles_idx_local)
 
     def set_actuation(self, actus, envs_idx=None):
-        """Muscle actuation of a single-group muscle: one value per env for all its particles."""
-        a = torch.as_tensor(actus, dtype=torch.float32, device="cuda").reshape(-1, 1, 1)
-        self._set_field(_lib.FIELD_ACTU, 1, a, envs_idx)
+        """Actuation of each muscle group (mpm_entity.py:425-440): a scalar, [n_groups], [B, n_groups]
+        or [B, n_particles, n_groups]; every particle takes the value of its group."""
+        n_groups = self._n_groups()
+        a = torch.as_tensor(actus, dtype=torch.float32, device="cuda")
+        if a.ndim == 0:
+            a = a.reshape(1).expand(n_groups)
+        if a.shape[-1] != n_groups:
+            raise GenesisException(f"actuation must end in n_groups = {n_groups} values.")
+        B = len(self._envs(envs_idx))
+        if a.ndim == 1:
+            a = a.reshape(1, 1, n_groups)
+        elif a.ndim == 2:
+            a = a.reshape(a.shape[0], 1, n_groups)
+        a = torch.broadcast_to(a, (B, self._n_particles, n_groups))
+        grp = self._muscle_groups()
+        per = torch.gather(a, 2, grp.reshape(1, -1, 1).expand(B, -1, 1))
+        self._set_field(_lib.FIELD_ACTU, 1, per, envs_idx)
+
+    def set_muscle_group(self, muscle_group):
+        """Group index of every particle (mpm_entity.py:489-506); actuation values are per group."""
+        self._n_groups()
+        g = torch.as_tensor(muscle_group, device="cuda").to(torch.long).reshape(-1)
+        if g.numel() != self._n_particles:
+            raise GenesisException(f"muscle_group must have {self._n_particles} entries.")
+        self._muscle_group = g.clone()
+
+    def get_muscle_group(self):
+        return self._muscle_groups().to(torch.int32)
+
+    def set_muscle(self, muscle_group=None, muscle_direction=None):
+        """mpm_entity.py:543-559: muscle group indices and/or fiber directions."""
+        if muscle_group is not None:
+            self.set_muscle_group(muscle_group)
+        if muscle_direction is not None:
+            self.set_muscle_direction(muscle_direction)
 
     def set_muscle_direction(self, muscle_direction):
         d = torch.as_tensor(muscle_direction, dtype=torch.float32, device="cuda").reshape(-1, 3)

@@ -817,3 +817,53 @@ def test_reference_scenario_fluid_emitter(gs, material):
     hi = torch.tensor([1.0, 1.5, 4.0], device="cuda")
     assert ((pos >= lo) & (pos <= hi)).all()
     scene.sim.mpm_solver.set_colliders([])
+
+
+@pytest.mark.parametrize("n_envs", [0, 2])
+def test_reference_scenario_muscle_groups(gs, n_envs):
+    """The MPM case of the reference's tests/test_deformable_physics.py::test_muscle through the
+    drop-in API, with a box for the worm mesh (no mesh loader on this path): Muscle(E=5e5, nu=0.45,
+    rho=1e4, n_groups=4) split into the reference's four groups (upper/lower x fore/hind), fiber
+    direction +y, a coupled ground plane with coup_friction 5, 200 steps of sinusoidal actuation of
+    group 3.  Every particle carries its group's actuation; the actuated body ends elsewhere than
+    an unactuated one; no NaN."""
+    from genesis_gb300.coupling import Collider
+
+    def run(actuate):
+        scene = gs.Scene(
+            sim_options=gs.options.SimOptions(dt=5e-4, substeps=10, gravity=(0, 0, -9.8)),
+            mpm_options=gs.options.MPMOptions(lower_bound=(-1.0, -1.0, -0.2), upper_bound=(1.0, 1.0, 1.0)),
+        )
+        worm = scene.add_entity(material=gs.materials.MPM.Muscle(E=5e5, nu=0.45, rho=10000.0, n_groups=4),
+                                morph=gs.morphs.Box(pos=(0.3, 0.3, 0.03), size=(0.06, 0.3, 0.05)))
+        scene.build(n_envs=n_envs) if n_envs > 0 else scene.build()
+        scene.sim.mpm_solver.set_colliders([Collider("plane", normal=(0.0, 0.0, 1.0), coup_friction=5.0)])
+        pos = worm.get_state().pos[0].cpu().numpy()
+        lo, hi = pos.min(0), pos.max(0)
+        rng_ = hi - lo
+        upper = pos[:, 2] > lo[2] + rng_[2] * 0.3
+        fore = pos[:, 1] < lo[1] + rng_[1] * 0.6
+        group = np.zeros(len(pos), dtype=np.int64)
+        group[upper & ~fore] = 1
+        group[~upper & fore] = 2
+        group[~upper & ~fore] = 3
+        worm.set_muscle(muscle_group=group, muscle_direction=np.tile([0.0, 1.0, 0.0], (len(pos), 1)))
+        scene.reset()
+        for i in range(200):
+            a = np.array([0.0, 0.0, 0.0, (1.0 if actuate else 0.0) * (0.5 + np.sin(0.005 * np.pi * i))])
+            worm.set_actuation(np.tile(a, (n_envs, 1)) if n_envs > 1 else a)
+            if i == 0:
+                actu = worm.get_particles_actu()
+                actu = actu[0] if n_envs > 1 else actu
+                want = np.where(group == 3, a[3], 0.0)
+                assert np.allclose(actu.cpu().numpy(), want), "each particle takes its group's actuation"
+            scene.step()
+        out = worm.get_particles_pos()
+        scene.sim.mpm_solver.set_colliders([])
+        return out[0] if n_envs > 1 else out
+
+    act = run(True)
+    rest = run(False)
+    assert torch.isfinite(act).all() and torch.isfinite(rest).all()
+    assert (act - rest).abs().max().item() > 1e-3
+    assert act[:, 2].min().item() > -1e-3
