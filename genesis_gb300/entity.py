@@ -126,6 +126,72 @@ class MPMEntity:
     def n_vverts(self) -> int:
         return len(self._vverts)
 
+    @property
+    def n_vfaces(self) -> int:
+        """Visual faces: none here (vertices come without a mesh, set_vverts)."""
+        return 0
+
+    @property
+    def vvert_start(self) -> int:
+        """First visual vertex of this entity in the solver's vertex buffer (entities in order)."""
+        start = 0
+        for e in self._solver._entities:
+            if e is self:
+                return start
+            start += e.n_vverts
+        return start
+
+    @property
+    def vvert_end(self) -> int:
+        return self.vvert_start + self.n_vverts
+
+    @property
+    def vface_start(self) -> int:
+        return 0
+
+    @property
+    def vface_end(self) -> int:
+        return self.vface_start + self.n_vfaces
+
+    def find_closest_particle(self, pos, envs_idx=None):
+        """particle_entity.py:716-743: index of the particle nearest to pos ([3] or [B, 3]) per env."""
+        p = torch.as_tensor(pos, dtype=torch.float32, device="cuda")
+        B = self._solver._B
+        if p.ndim == 1:
+            p = p.reshape(1, 3).expand(B, 3)
+        if tuple(p.shape) != (B, 3):
+            raise GenesisException(f"Invalid tensor shape {tuple(p.shape)} (expected ({B}, 3)).")
+        cur = self._get_field(_lib.FIELD_POS, 3, envs_idx)
+        if envs_idx is not None:
+            p = p[torch.as_tensor(self._envs(envs_idx), device="cuda")]
+        idx = torch.argmin(torch.linalg.norm(cur - p[:, None], dim=-1), dim=-1).to(torch.int32)
+        return idx[0] if self._scene.n_envs == 0 else idx
+
+    def get_frame(self, f, pos, vel, C, F, Jp, active):
+        """mpm_entity.py:305-352: fill the given [B, n, ...] tensors with the particles' state.  Only
+        the current frame is kept on the device (no per-substep frame ring), so `f` must name it
+        (the solver's current substep-local frame, or None)."""
+        cur = getattr(self._scene.sim, "cur_substep_local", None)
+        if f is not None and cur is not None and int(f) != int(cur):
+            raise GenesisException("Only the current frame is kept on the device.")
+        st = self.get_state()
+        for dst, src in ((pos, st.pos), (vel, st.vel), (C, st.C), (F, st.F), (Jp, st.Jp), (active, st.active)):
+            if dst is not None:
+                dst.copy_(src.reshape(dst.shape).to(dst.dtype))
+
+    # ------------------------------------------------------------------ checkpoints (particle_entity.py:371-403)
+    def init_ckpt(self):
+        self._ckpt = {}
+
+    def save_ckpt(self, ckpt_name):
+        """Keep the pending targets (set_position / set_velocity / activation at the next step)."""
+        if not hasattr(self, "_ckpt"):
+            self._ckpt = {}
+        self._ckpt[ckpt_name] = dict(self._tgt)
+
+    def load_ckpt(self, ckpt_name):
+        self._tgt = dict(self._ckpt[ckpt_name])
+
     # ------------------------------------------------------------------ solver plumbing
     def _add_to_solver(self):
         self._solver._add_particles(

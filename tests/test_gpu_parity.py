@@ -867,3 +867,31 @@ def test_reference_scenario_muscle_groups(gs, n_envs):
     assert torch.isfinite(act).all() and torch.isfinite(rest).all()
     assert (act - rest).abs().max().item() > 1e-3
     assert act[:, 2].min().item() > -1e-3
+
+
+def test_entity_queries_frame_and_checkpoints(gs):
+    """find_closest_particle (particle_entity.py:716-743), get_frame (mpm_entity.py:305-352),
+    visual index ranges and the entity checkpoints of pending targets (particle_entity.py:371-403)."""
+    scene, cube, _ = c1_scene(gs, n_envs=2, size=0.1)
+    for _ in range(3):
+        scene.step()
+    pos = cube.get_particles_pos()
+    idx = cube.find_closest_particle(pos[:, 7])
+    assert idx.shape == (2,) and (idx == 7).all()
+    B, n = 2, cube.n_particles
+    bufs = [torch.empty((B, n, 3), device="cuda"), torch.empty((B, n, 3), device="cuda"),
+            torch.empty((B, n, 3, 3), device="cuda"), torch.empty((B, n, 3, 3), device="cuda"),
+            torch.empty((B, n), device="cuda"), torch.empty((B, n), dtype=torch.int64, device="cuda")]
+    cube.get_frame(None, *bufs)
+    st = cube.get_state()
+    for got, want in zip(bufs, (st.pos, st.vel, st.C, st.F, st.Jp, st.active)):
+        assert torch.equal(got, want.reshape(got.shape).to(got.dtype))
+    assert cube.vvert_start == 0 and cube.vvert_end == cube.n_vverts and cube.n_vfaces == 0
+    cube.init_ckpt()
+    cube.set_velocity(torch.tensor([0.0, 0.0, 1.0], device="cuda"))
+    cube.save_ckpt("a")
+    scene.step()  # applies and clears the pending target
+    cube.load_ckpt("a")
+    scene.step()  # applies it again
+    v = cube.get_particles_vel()
+    assert v[..., 2].mean().item() > 0.5
