@@ -35,8 +35,11 @@ class MPMEntity:
         self._particle_size = particle_size
         self._idx = idx
         self._particle_start = particle_start
-        self._name = name
         self._uid = id(self)
+        if name is None:  # base_entity.py:40-45: morph identifier + short uid
+            kind = type(morph).__name__.lower()
+            name = f"{kind}_{format(self._uid & 0xFFFFFFF, '07x')}"
+        self._name = name
         self.sampler = material.sampler
         particles = morph.sample(particle_size, self.sampler)
         if particles.size == 0:

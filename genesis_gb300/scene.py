@@ -209,6 +209,59 @@ class Scene:
         st = SimState(self._sim.cur_step_global, self._sim.cur_substep_local, self._sim.mpm_solver.get_state())
         return st
 
+    # ------------------------------------------------------------------ checkpoints (scene.py:1381-1446)
+    def dump_ckpt_to_numpy(self) -> dict:
+        """Flat {"Class.attr[.member]": ndarray} of the physics state: the MPM solver's particle state
+        and gravity, and the simulator's substep counter."""
+        arrays = {"Simulator._cur_substep_global": np.asarray(self._sim._cur_substep_global, dtype=np.int64)}
+        if self._is_built:
+            arrays.update(self._sim.mpm_solver.dump_ckpt_to_numpy())
+        return arrays
+
+    def save_checkpoint(self, path) -> None:
+        """Pickle the full physics state to one file (scene.py:1402-1417)."""
+        import pickle
+        import time
+
+        state = {"timestamp": time.time(), "step_index": self.t, "arrays": self.dump_ckpt_to_numpy()}
+        with open(path, "wb") as f:
+            pickle.dump(state, f)
+
+    def load_checkpoint(self, path) -> None:
+        """Restore a file written by save_checkpoint (scene.py:1419-1446)."""
+        import pickle
+
+        with open(path, "rb") as f:
+            state = pickle.load(f)
+        arrays = state["arrays"]
+        self._sim.mpm_solver.load_ckpt_from_numpy(arrays)
+        if "Simulator._cur_substep_global" in arrays:
+            self._sim._cur_substep_global = int(arrays["Simulator._cur_substep_global"])
+
+    # ------------------------------------------------------------------ lookup
+    @property
+    def entity_names(self) -> tuple:
+        return tuple(e.name for e in self._entities)
+
+    def get_entity(self, name=None, *, uid=None):
+        """By exact name or by uid (scene.py:1556-1592); raises when not found."""
+        if (name is None) == (uid is None):
+            raise GenesisException("Pass exactly one of `name` or `uid`.")
+        for e in self._entities:
+            if (name is not None and e.name == name) or (uid is not None and str(e.uid).startswith(str(uid))):
+                return e
+        raise GenesisException(f"Entity not found: {name if name is not None else uid}.")
+
+    @property
+    def gravity(self):
+        return self._sim.mpm_solver.gravity
+
+    def destroy(self) -> None:
+        """Release the device state (scene.py:304-318)."""
+        if self._sim is not None and self._is_built:
+            self._sim.mpm_solver.destroy()
+        self._is_built = False
+
     # ------------------------------------------------------------------ properties
     @property
     def sim(self):

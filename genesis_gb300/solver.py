@@ -397,6 +397,83 @@ class MPMSolver:
         _lib.check(self._lib.mpm_set_colliders(self._ctx, len(recs), arr), self._ctx, "mpm_set_colliders")
         self._n_colliders = len(recs)
 
+    # ------------------------------------------------------------------ numpy checkpoints (base_solver.py:63-126)
+    def dump_ckpt_to_numpy(self) -> dict:
+        """{"MPMSolver.particles.<field>": [B, N, ...], "MPMSolver._gravity": [B, 3]} of the current state
+        (the particle state the reference's fields hold at the current frame; muscle actuation and
+        directions too when a Muscle material is present)."""
+        out = {}
+        if not self.is_active:
+            return out
+        st = self.get_state()
+        for k in ("pos", "vel", "C", "F", "Jp", "active"):
+            out[f"MPMSolver.particles.{k}"] = getattr(st, k).detach().cpu().numpy()
+        out["MPMSolver._gravity"] = np.asarray(self.gravity, dtype=np.float64)
+        from .materials import Muscle
+
+        if any(isinstance(e.material, Muscle) for e in self._entities):
+            for e in self._entities:
+                out[f"MPMSolver.entity{e.idx}.actu"] = e._get_field(_lib.FIELD_ACTU, 1, None).cpu().numpy()
+                out[f"MPMSolver.entity{e.idx}.muscle_direction"] = e._get_field(_lib.FIELD_MUSCLE_DIR, 3, None).cpu().numpy()
+        return out
+
+    def load_ckpt_from_numpy(self, arr_dict: dict) -> None:
+        if not self.is_active:
+            return
+        keys = ("pos", "vel", "C", "F", "Jp", "active")
+        if all(f"MPMSolver.particles.{k}" in arr_dict for k in keys):
+            st = MPMSolverState(self._B, self.n_particles, "cuda")
+            for k in keys:
+                v = torch.as_tensor(arr_dict[f"MPMSolver.particles.{k}"], device="cuda")
+                setattr(st, k, v.to(getattr(st, k).dtype).reshape(getattr(st, k).shape))
+            self.set_state(0, st)
+        if "MPMSolver._gravity" in arr_dict:
+            self.set_gravity(arr_dict["MPMSolver._gravity"])
+        for e in self._entities:
+            a = arr_dict.get(f"MPMSolver.entity{e.idx}.actu")
+            if a is not None:
+                e._write(_lib.FIELD_ACTU, e._envs(None), torch.as_tensor(a, device="cuda").contiguous())
+            d = arr_dict.get(f"MPMSolver.entity{e.idx}.muscle_direction")
+            if d is not None:
+                e._write(_lib.FIELD_MUSCLE_DIR, e._envs(None), torch.as_tensor(d, device="cuda").contiguous())
+
+    # ------------------------------------------------------------------ differentiable-mode protocol members
+    def _no_grad_protocol(self, *args, **kwargs):
+        raise GenesisException(
+            "The MPM solver's gradients come from genesis_gb300.diff.DifferentiableMPM (hand-written adjoints "
+            "with checkpoint-and-recompute); the Solver-protocol gradient members are not available on this path."
+        )
+
+    add_grad_from_state = _no_grad_protocol
+    collect_output_grads = _no_grad_protocol
+    process_input_grad = _no_grad_protocol
+    reset_grad = _no_grad_protocol
+    reset_grad_till_frame = _no_grad_protocol
+    substep_pre_coupling_grad = _no_grad_protocol
+    substep_post_coupling_grad = _no_grad_protocol
+
+    @property
+    def scene(self):
+        return self._scene
+
+    @property
+    def sim(self):
+        return self._sim
+
+    @property
+    def uid(self):
+        return id(self)
+
+    @property
+    def leaf_block_size(self):
+        """Deprecated in the reference (options/solvers.py: a no-op); the grid block here is 4^3 nodes."""
+        return 4
+
+    @property
+    def use_sparse_grid(self):
+        """Deprecated in the reference; only blocks touched by particles are processed here."""
+        return False
+
     def get_collider_poses(self) -> np.ndarray:
         """[n_colliders, 7]: current position and quaternion (w, x, y, z) of each collider; tools
         have advanced one substep per substep since set_colliders."""
