@@ -2,8 +2,8 @@
 
 Mirrors the 'regular' and 'random' samplers of genesis/utils/particle.py
 (n_particles_3D :36-41, _box_to_particles :180-208, sphere/cylinder rejection :231-278) and
-the morph fields of genesis/options/morphs.py (Box :186, Sphere :351, Cylinder, Nowhere
-:128).  Sampling runs on the host with numpy's global RNG (seeded by gs.init(seed=...)),
+the morph fields of genesis/options/morphs.py (Box :186, Sphere :351, Cylinder, Mesh :630,
+Nowhere :128).  Sampling runs on the host with numpy's global RNG (seeded by gs.init(seed=...)),
 like the reference; particles are then rotated by the morph's quaternion and translated
 to its position (particle_entity.py:318-329).
 
@@ -161,6 +161,94 @@ class Cylinder(Morph):
 
     def _local_particles(self, p_size, sampler):
         return cylinder_to_particles(p_size, (0, 0, 0), self.radius, self.height, sampler)
+
+
+def load_obj(path):
+    """Vertices [V, 3] and triangles [F, 3] of a Wavefront OBJ file ('v' and 'f' records; polygons
+    are split into fans; 'f' entries may carry /vt/vn indices; negative indices count from the end)."""
+    verts, faces = [], []
+    with open(path) as fh:
+        for line in fh:
+            parts = line.split()
+            if not parts:
+                continue
+            if parts[0] == "v" and len(parts) >= 4:
+                verts.append([float(parts[1]), float(parts[2]), float(parts[3])])
+            elif parts[0] == "f" and len(parts) >= 4:
+                idx = []
+                for tok in parts[1:]:
+                    i = int(tok.split("/")[0])
+                    idx.append(i - 1 if i > 0 else len(verts) + i)
+                faces.extend([idx[0], idx[k], idx[k + 1]] for k in range(1, len(idx) - 1))
+    if not verts or not faces:
+        raise GenesisException(f"No triangles in mesh file: {path}.")
+    return np.asarray(verts, dtype=np.float64), np.asarray(faces, dtype=np.int64)
+
+
+def winding_number(points, verts, faces, chunk=4096):
+    """Generalized winding number of a triangle mesh at each point (Jacobson, Kavan, Sorkine-Hornung
+    2013: the sum of the triangles' signed solid angles over 4 pi, each by the formula of van
+    Oosterom and Strackee 1983); close to 1 inside a closed, outward-oriented mesh, 0 outside.
+    Runs on the GPU through torch when one is present (set-up work, not the substep path)."""
+    try:
+        import torch
+
+        dev = "cuda" if torch.cuda.is_available() else "cpu"
+        tri = torch.as_tensor(verts[faces], dtype=torch.float64, device=dev)  # [F, 3, 3]
+        out = []
+        for k in range(0, len(points), chunk):
+            p = torch.as_tensor(points[k:k + chunk], dtype=torch.float64, device=dev)
+            a, b, c = (tri[None, :, i, :] - p[:, None, :] for i in range(3))
+            la, lb, lc = a.norm(dim=-1), b.norm(dim=-1), c.norm(dim=-1)
+            det = (a * torch.cross(b, c, dim=-1)).sum(-1)
+            den = la * lb * lc + (a * b).sum(-1) * lc + (b * c).sum(-1) * la + (c * a).sum(-1) * lb
+            out.append((2.0 * torch.atan2(det, den)).sum(-1) / (4.0 * math.pi))
+        return torch.cat(out).cpu().numpy()
+    except ImportError:
+        tri = verts[faces]
+        out = []
+        for k in range(0, len(points), chunk):
+            p = points[k:k + chunk]
+            a, b, c = (tri[None, :, i, :] - p[:, None, :] for i in range(3))
+            la, lb, lc = (np.linalg.norm(x, axis=-1) for x in (a, b, c))
+            det = np.einsum("pfi,pfi->pf", a, np.cross(b, c))
+            den = la * lb * lc + np.einsum("pfi,pfi->pf", a, b) * lc + np.einsum("pfi,pfi->pf", b, c) * la + \
+                np.einsum("pfi,pfi->pf", c, a) * lb
+            out.append((2.0 * np.arctan2(det, den)).sum(-1) / (4.0 * math.pi))
+        return np.concatenate(out)
+
+
+class Mesh(Morph):
+    """A mesh from a Wavefront OBJ `file` (or `vertices` [V, 3] and `faces` [F, 3] given directly),
+    scaled by `scale` (float or 3-tuple), then placed by pos / euler / quat (options/morphs.py:630-700).
+    Particles: the box sampler over the scaled mesh's bounds, keeping the points inside the mesh
+    (utils/particle.py:48-82, where igl's signed distance < 0 decides; here a generalized winding
+    number > 0.5, the same test for a closed mesh).  The mesh vertices become the entity's visual
+    vertices (skinned to the particles)."""
+
+    _fields = ("file", "scale", "vertices", "faces")
+    file = None
+    scale = 1.0
+    vertices = None
+    faces = None
+
+    def _post_init(self) -> None:
+        if self.vertices is None or self.faces is None:
+            if self.file is None:
+                raise GenesisException("Mesh needs `file` or `vertices` and `faces`.")
+            self.vertices, self.faces = load_obj(self.file)
+        v = np.asarray(self.vertices, dtype=np.float64).reshape(-1, 3)
+        self.faces = np.asarray(self.faces, dtype=np.int64).reshape(-1, 3)
+        self.vertices = v * np.broadcast_to(np.asarray(self.scale, dtype=np.float64), (3,))
+
+    def _local_particles(self, p_size, sampler):
+        lo, hi = self.vertices.min(0), self.vertices.max(0)
+        p = box_to_particles(p_size, (lo + hi) / 2, hi - lo, sampler)
+        return p[winding_number(p, self.vertices, self.faces) > 0.5]
+
+    def visual_vertices(self) -> np.ndarray:
+        """The mesh vertices in the world frame (the reference's vmesh after its transform)."""
+        return self.vertices @ quat_to_R(self.quat).T + np.asarray(self.pos)
 
 
 class Nowhere(Morph):

@@ -174,3 +174,69 @@ def test_autotuner_keeps_the_default_shape_within_its_margin():
     t["64x2/128"] = 1.0 - 2 * MARGIN  # a clear gain
     assert choose(t) == (64, 2, 128)
     assert choose({"64x2/128": 2.0, "128x1/128": 1.0}, ((64, 2, 128), (128, 1, 128))) == (128, 1, 128)
+
+
+def _cube_obj(path, half=0.1):
+    v = [(x, y, z) for x in (-half, half) for y in (-half, half) for z in (-half, half)]
+    # outward-oriented quads (1-based), split into fans by the loader
+    quads = [(1, 2, 4, 3), (5, 7, 8, 6), (1, 5, 6, 2), (3, 4, 8, 7), (1, 3, 7, 5), (2, 6, 8, 4)]
+    with open(path, "w") as f:
+        f.write("# cube\n")
+        for p in v:
+            f.write("v %f %f %f\n" % p)
+        for q in quads:
+            f.write("f " + " ".join(f"{i}/{i}/{i}" for i in q) + "\n")
+
+
+def test_mesh_morph_obj_winding_and_sampling(tmp_path):
+    """Mesh morph: OBJ fan triangulation, winding numbers (1 inside, 0 outside a closed mesh), and
+    'regular' sampling of a cube mesh equal to the Box morph's lattice (every lattice point lies
+    strictly inside), placed by the same pose."""
+    import numpy as np
+
+    from genesis_gb300 import morphs
+
+    obj = tmp_path / "cube.obj"
+    _cube_obj(obj)
+    v, f = morphs.load_obj(obj)
+    assert v.shape == (8, 3) and f.shape == (12, 3)
+    w = morphs.winding_number(np.array([[0.0, 0.0, 0.0], [0.05, -0.07, 0.02], [0.3, 0.0, 0.0]]), v, f)
+    assert abs(w[0] - 1.0) < 1e-9 and abs(w[1] - 1.0) < 1e-9 and abs(w[2]) < 1e-9
+    pose = dict(pos=(0.5, 0.4, 0.3), euler=(10.0, 20.0, 30.0))
+    mesh = morphs.Mesh(file=str(obj), scale=1.5, **pose)
+    box = morphs.Box(size=(0.3, 0.3, 0.3), **pose)
+    pm, pb = mesh.sample(0.02, "regular"), box.sample(0.02, "regular")
+    assert pm.shape == pb.shape and np.abs(pm - pb).max() < 1e-12
+    vv = mesh.visual_vertices()
+    assert np.allclose(vv.mean(0), pose["pos"])
+
+
+def test_mesh_morph_sphere_mesh_counts_close_to_sphere():
+    import numpy as np
+
+    from genesis_gb300 import morphs
+
+    # UV sphere of radius 0.1 (outward triangles)
+    nu, nv, r = 48, 24, 0.1
+    verts = [(0.0, 0.0, r)]
+    for i in range(1, nv):
+        th = np.pi * i / nv
+        for j in range(nu):
+            ph = 2 * np.pi * j / nu
+            verts.append((r * np.sin(th) * np.cos(ph), r * np.sin(th) * np.sin(ph), r * np.cos(th)))
+    verts.append((0.0, 0.0, -r))
+    faces = []
+    for j in range(nu):
+        faces.append((0, 1 + j, 1 + (j + 1) % nu))
+    for i in range(nv - 2):
+        for j in range(nu):
+            a, b = 1 + i * nu + j, 1 + i * nu + (j + 1) % nu
+            faces += [(a, a + nu, b), (b, a + nu, b + nu)]
+    last = len(verts) - 1
+    for j in range(nu):
+        a, b = 1 + (nv - 2) * nu + j, 1 + (nv - 2) * nu + (j + 1) % nu
+        faces.append((a, last, b))
+    mesh = morphs.Mesh(vertices=np.array(verts), faces=np.array(faces))
+    n_mesh = len(mesh.sample(0.01, "regular"))
+    n_sphere = len(morphs.Sphere(radius=0.1).sample(0.01, "regular"))
+    assert abs(n_mesh - n_sphere) <= 0.03 * n_sphere, (n_mesh, n_sphere)

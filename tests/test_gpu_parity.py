@@ -922,3 +922,25 @@ def test_scene_checkpoint_roundtrip_and_lookup(gs, tmp_path):
     assert np.allclose(scene.gravity[0], (0.0, 0.0, -9.81))
     with pytest.raises(gs.GenesisException, match="DifferentiableMPM"):
         scene.sim.mpm_solver.reset_grad()
+
+
+def test_mesh_morph_entity_steps(gs, tmp_path):
+    """An MPM entity from a mesh file (gs.morphs.Mesh) samples like the Box of the same cube, steps,
+    and takes the mesh vertices as its visual vertices."""
+    from test_api_host import _cube_obj
+
+    obj = tmp_path / "cube.obj"
+    _cube_obj(obj, half=0.05)
+    scene = gs.Scene(sim_options=gs.options.SimOptions(dt=2e-4),
+                     mpm_options=gs.options.MPMOptions(lower_bound=(0, 0, 0), upper_bound=(1, 1, 1)))
+    mat = gs.materials.MPM.Elastic(sampler="regular")
+    ent = scene.add_entity(material=mat, morph=gs.morphs.Mesh(file=str(obj), pos=(0.5, 0.5, 0.4), euler=(0, 0, 30)))
+    ref = gs.morphs.Box(size=(0.1, 0.1, 0.1), pos=(0.5, 0.5, 0.4), euler=(0, 0, 30)).sample(ent.particle_size, "regular")
+    assert ent.n_particles == len(ref)
+    ent.set_vverts(ent.morph.visual_vertices())
+    scene.build()
+    for _ in range(10):
+        scene.step()
+    p = ent.get_particles_pos()
+    assert torch.isfinite(p).all() and (p[:, 2] < 0.4).any()
+    assert ent.n_vverts == 8
