@@ -13,9 +13,10 @@ A rigid geom whose SDF the reference samples on a voxel grid (boxes, meshes) is 
 shape "sdf" with an `SDFGrid` (values and gradients).  A tool entity (engine/entities/tool_entity:
 a kinematic mesh with a voxel SDF, friction and softness, coupled before the rigid geoms) is a
 collider of shape "tool" with an `SDFGrid` of values; the library moves it every substep from its
-linear and angular velocity, as ToolEntity.advect does.  Grids come from the caller (the reference
-builds them from meshes with trimesh/igl, which are not part of this library);
-`SDFGrid.from_function` samples an analytic distance function.
+linear and angular velocity, as ToolEntity.advect does.  Grids come from the caller:
+`SDFGrid.from_mesh` bakes a tool's grid from its mesh the way the reference does (normalised mesh,
+[-0.6, 0.6]^3, signed distance; here triangle distances and winding-number signs in place of
+trimesh/igl), `SDFGrid.from_function` samples an analytic distance function.
 """
 
 from __future__ import annotations
@@ -67,6 +68,74 @@ class SDFGrid:
         return cls(values=vals.astype(np.float32), T_mesh_to_sdf=T,
                    grads=None if g is None else g.astype(np.float32), cell_size=float(cell[0]),
                    sdf_max=float(vals.max()))
+
+    @classmethod
+    def from_mesh(cls, vertices, faces, res: int = 128, scale=1.0, grads: bool = False) -> "SDFGrid":
+        """A tool entity's SDF from its mesh as the reference builds it (tool_entity/mesh.py:40-58,
+        utils/mesh.py:193-215): the mesh is centred on its bounding box and divided by its largest
+        extent, its signed distance is sampled on res^3 points spanning [-0.6, 0.6]^3 of that frame
+        (distance to the nearest triangle, negative where the generalized winding number exceeds
+        0.5, in place of igl's signed distance), and T_mesh_to_sdf maps the scaled mesh frame
+        (`scale`, the morph's) to voxel coordinates.  grads=True adds central-difference gradients
+        (for an "sdf" rigid collider)."""
+        from .morphs import winding_number
+
+        v = np.asarray(vertices, dtype=np.float64).reshape(-1, 3)
+        f = np.asarray(faces, dtype=np.int64).reshape(-1, 3)
+        lo, hi = v.min(0), v.max(0)
+        vn = (v - (lo + hi) / 2) / np.max(hi - lo)
+        r = 0.6
+        ax = np.linspace(-r, r, res)
+        pts = np.stack(np.meshgrid(ax, ax, ax, indexing="ij"), -1).reshape(-1, 3)
+        dist = triangle_distance(pts, vn, f)
+        inside = winding_number(pts, vn, f) > 0.5
+        vals = np.where(inside, -dist, dist).reshape(res, res, res)
+        T = np.eye(4)
+        T[:3, :3] *= (res - 1) / (2 * r)
+        T[:3, 3] = (res - 1) / 2
+        S = np.diag(np.append(np.broadcast_to(np.asarray(scale, dtype=np.float64), (3,)), 1.0))
+        T = T @ np.linalg.inv(S)
+        g = None
+        if grads:
+            h = 2 * r / (res - 1)
+            g = np.stack(np.gradient(vals, h), -1)
+        return cls(values=vals.astype(np.float32), T_mesh_to_sdf=T,
+                   grads=None if g is None else g.astype(np.float32), cell_size=2 * r / (res - 1),
+                   sdf_max=float(vals.max()))
+
+
+def triangle_distance(points, verts, faces, chunk=2048):
+    """Distance from each point to the nearest triangle of a mesh: the closest point on each triangle
+    by its Voronoi regions (Ericson, Real-Time Collision Detection, 5.1.5), minimised over the
+    triangles.  Through torch on the GPU when one is present (set-up work)."""
+    import torch
+
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    tri = torch.as_tensor(verts[faces], dtype=torch.float64, device=dev)
+    a, b, c = tri[None, :, 0], tri[None, :, 1], tri[None, :, 2]
+    ab, ac = b - a, c - a
+    dot = lambda x, y: (x * y).sum(-1, keepdim=True)  # noqa: E731
+    out = []
+    step = chunk if dev == "cuda" else max(1, chunk // 8)
+    for k in range(0, len(points), step):
+        p = torch.as_tensor(points[k:k + step], dtype=torch.float64, device=dev)[:, None, :]
+        ap, bp, cp = p - a, p - b, p - c
+        d1, d2, d3, d4, d5, d6 = dot(ab, ap), dot(ac, ap), dot(ab, bp), dot(ac, bp), dot(ab, cp), dot(ac, cp)
+        va, vb, vc = d3 * d6 - d5 * d4, d5 * d2 - d1 * d6, d1 * d4 - d3 * d2
+        den = va + vb + vc
+        den = torch.where(den == 0, torch.ones_like(den), den)
+        q = a + ab * (vb / den) + ac * (vc / den)  # interior
+        t_bc = (d4 - d3) / torch.where((d4 - d3) + (d5 - d6) == 0, torch.ones_like(d4), (d4 - d3) + (d5 - d6))
+        q = torch.where((va <= 0) & (d4 - d3 >= 0) & (d5 - d6 >= 0), b + (c - b) * t_bc, q)
+        t_ac = d2 / torch.where(d2 - d6 == 0, torch.ones_like(d2), d2 - d6)
+        q = torch.where((vb <= 0) & (d2 >= 0) & (d6 <= 0), a + ac * t_ac, q)
+        q = torch.where((d6 >= 0) & (d5 <= d6), c.expand_as(q), q)
+        t_ab = d1 / torch.where(d1 - d3 == 0, torch.ones_like(d1), d1 - d3)
+        q = torch.where((vc <= 0) & (d1 >= 0) & (d3 <= 0), a + ab * t_ab, q)
+        q = torch.where((d3 >= 0) & (d4 <= d3), b.expand_as(q), q)
+        q = torch.where((d1 <= 0) & (d2 <= 0), a.expand_as(q), q)
+        out.append((p - q).norm(dim=-1).min(dim=1).values)
+    return torch.cat(out).cpu().numpy()
 
 
 @dataclasses.dataclass

@@ -240,3 +240,29 @@ def test_mesh_morph_sphere_mesh_counts_close_to_sphere():
     n_mesh = len(mesh.sample(0.01, "regular"))
     n_sphere = len(morphs.Sphere(radius=0.1).sample(0.01, "regular"))
     assert abs(n_mesh - n_sphere) <= 0.03 * n_sphere, (n_mesh, n_sphere)
+
+
+def test_sdf_grid_from_mesh_matches_the_analytic_box():
+    """SDFGrid.from_mesh of a box mesh: the reference's normalised frame and [-0.6, 0.6]^3 grid,
+    distances to the triangles and winding-number signs equal the exact box SDF there, and
+    T_mesh_to_sdf takes the scaled mesh frame to voxel coordinates."""
+    import numpy as np
+
+    from genesis_gb300.coupling import SDFGrid
+
+    h = np.array([0.2, 0.1, 0.05])  # half extents; largest extent 0.4 -> normalised half (0.5, 0.25, 0.125)
+    v = np.array([(x, y, z) for x in (-h[0], h[0]) for y in (-h[1], h[1]) for z in (-h[2], h[2])]) + 0.3
+    quads = [(0, 1, 3, 2), (4, 6, 7, 5), (0, 4, 5, 1), (2, 3, 7, 6), (0, 2, 6, 4), (1, 5, 7, 3)]
+    f = np.array([t for q in quads for t in ((q[0], q[1], q[2]), (q[0], q[2], q[3]))])
+    res = 17
+    g = SDFGrid.from_mesh(v, f, res=res, scale=2.0)
+    hn = h / 0.4
+    ax = np.linspace(-0.6, 0.6, res)
+    P = np.stack(np.meshgrid(ax, ax, ax, indexing="ij"), -1)
+    q = np.abs(P) - hn
+    exact = np.linalg.norm(np.maximum(q, 0.0), axis=-1) + np.minimum(q.max(-1), 0.0)
+    assert np.abs(g.values - exact).max() < 1e-6
+    # a point of the scaled mesh frame (scale 2: normalised coordinates x 2) lands on its voxel
+    pn = np.array([0.3, -0.15, 0.6])
+    vox = g.T_mesh_to_sdf @ np.append(pn * 2.0, 1.0)
+    assert np.allclose(vox[:3], (pn + 0.6) / 1.2 * (res - 1))
