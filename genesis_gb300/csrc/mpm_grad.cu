@@ -9,7 +9,7 @@
 // dF^T R) V)_ij / (s_i + s_j); it has no 1/(s_j^2 - s_i^2) factors, so it stays finite at
 // F = I where the generic SVD backward relies on cancelling 1e6-sized terms.
 //
-// Materials: Elastic (corotated and neo-Hookean).  Grid: dense [res^3] float4 buffers owned
+// Materials: Elastic (corotated and neo-Hookean) and Liquid.  Grid: dense [res^3] float4 buffers owned
 // by the caller (torch tensors); particles: caller arrays in the reference layout.  The
 // scatter uses global vector atomics (no sort): the differentiable path favours clarity.
 #include <cuda_runtime.h>
@@ -66,7 +66,11 @@ __device__ __forceinline__ bool make_stencil(const SceneDev& S, const float* x, 
   return true;
 }
 
+// Material of the differentiable form (the `neohookean` argument of the entry points).
+constexpr int DIFF_COROTATED = 0, DIFF_NEOHOOKEAN = 1, DIFF_LIQUID = 2;
+
 // corotated / neo-Hookean stress of elastic.py:48-60 with per-particle mu, lam; F_new = F_tmp
+// (liquid: the corotated form with its mu, 0 unless viscous; F_new = J^(1/3) I)
 __device__ __forceinline__ void elastic_stress(const float* Ft, float mu, float lam, bool neo, const float* U,
                                                const float* sig, const float* V, float* P) {
   const float J = sig[0] * sig[1] * sig[2];
@@ -124,9 +128,15 @@ __global__ void __launch_bounds__(256) k_dp2g(DiffParams Q) {
     float Ft[9], U[9], sig[3], V[9], P[9];
     f_tmp(C, F, S.dt, Ft);
     svd_f32(Ft, U, sig, V);
-    elastic_stress(Ft, Q.mu[i], Q.lam[i], Q.neohookean, U, sig, V, P);
-    if (Q.F1)
-      for (int k = 0; k < 9; ++k) Q.F1[i * 9 + k] = Ft[k];
+    elastic_stress(Ft, Q.mu[i], Q.lam[i], Q.neohookean == DIFF_NEOHOOKEAN, U, sig, V, P);
+    if (Q.F1) {
+      if (Q.neohookean == DIFF_LIQUID) {  // liquid.py:36-40: F_new = J^(1/3) I
+        const float j3 = powf(sig[0] * sig[1] * sig[2], 1.f / 3.f);
+        for (int k = 0; k < 9; ++k) Q.F1[i * 9 + k] = (k % 4 == 0) ? j3 : 0.f;
+      } else {
+        for (int k = 0; k < 9; ++k) Q.F1[i * 9 + k] = Ft[k];
+      }
+    }
     float A[9];
     for (int k = 0; k < 9; ++k) A[k] = S.stress_scale * P[k] + Q.mass * C[k];
     for (int ox = 0; ox < 3; ++ox)
@@ -347,7 +357,7 @@ __global__ void __launch_bounds__(256) k_dp2g_adj(DiffParams Q) {
     float Ft[9], U[9], sig[3], V[9], P[9];
     f_tmp(C, F, S.dt, Ft);
     svd_f32(Ft, U, sig, V);
-    elastic_stress(Ft, mu, lam, Q.neohookean, U, sig, V, P);
+    elastic_stress(Ft, mu, lam, Q.neohookean == DIFF_NEOHOOKEAN, U, sig, V, P);
     float A[9];
     for (int k = 0; k < 9; ++k) A[k] = S.stress_scale * P[k] + Q.mass * C[k];
     float gv[3] = {0.f, 0.f, 0.f}, gA[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, gx[3];
@@ -376,15 +386,28 @@ __global__ void __launch_bounds__(256) k_dp2g_adj(DiffParams Q) {
         }
     // A = s P + m C
     float gP[9], gC[9], gFt[9];
+    const float J = sig[0] * sig[1] * sig[2];
     for (int k = 0; k < 9; ++k) {
       gP[k] = S.stress_scale * gA[k];
       gC[k] = Q.mass * gA[k];
-      gFt[k] = Q.gF1 ? Q.gF1[i * 9 + k] : 0.f;  // F1 = F_tmp
+      gFt[k] = (Q.gF1 && Q.neohookean != DIFF_LIQUID) ? Q.gF1[i * 9 + k] : 0.f;  // F1 = F_tmp
     }
-    const float J = sig[0] * sig[1] * sig[2];
+    if (Q.gF1 && Q.neohookean == DIFF_LIQUID) {
+      // F1 = J^(1/3) I: dL/dJ = tr(gF1) J^(-2/3) / 3, dJ/dF_tmp = cof(F_tmp)
+      const float gJ = (Q.gF1[i * 9 + 0] + Q.gF1[i * 9 + 4] + Q.gF1[i * 9 + 8]) * powf(J, -2.f / 3.f) / 3.f;
+      gFt[0] += gJ * (Ft[4] * Ft[8] - Ft[5] * Ft[7]);
+      gFt[1] += gJ * (Ft[5] * Ft[6] - Ft[3] * Ft[8]);
+      gFt[2] += gJ * (Ft[3] * Ft[7] - Ft[4] * Ft[6]);
+      gFt[3] += gJ * (Ft[2] * Ft[7] - Ft[1] * Ft[8]);
+      gFt[4] += gJ * (Ft[0] * Ft[8] - Ft[2] * Ft[6]);
+      gFt[5] += gJ * (Ft[1] * Ft[6] - Ft[0] * Ft[7]);
+      gFt[6] += gJ * (Ft[1] * Ft[5] - Ft[2] * Ft[4]);
+      gFt[7] += gJ * (Ft[2] * Ft[3] - Ft[0] * Ft[5]);
+      gFt[8] += gJ * (Ft[0] * Ft[4] - Ft[1] * Ft[3]);
+    }
     const float trP = gP[0] + gP[4] + gP[8];
     float gmu, glam;
-    if (Q.neohookean) {
+    if (Q.neohookean == DIFF_NEOHOOKEAN) {
       // P = mu F F^T + (lam log J - mu) I
       float FFt[9];
       mat_mul_bt(Ft, Ft, FFt);
@@ -412,7 +435,7 @@ __global__ void __launch_bounds__(256) k_dp2g_adj(DiffParams Q) {
       cof[8] = Ft[0] * Ft[4] - Ft[1] * Ft[3];
       for (int k = 0; k < 9; ++k) gFt[k] += lam * trP * cof[k] / J;
     } else {
-      // P = 2 mu (F - R) F^T + lam J (J - 1) I
+      // P = 2 mu (F - R) F^T + lam J (J - 1) I (corotated elastic; liquid.py:42-49 with F = F_tmp)
       float R[9], D[9], DFt[9];
       mat_mul_bt(U, V, R);
       for (int k = 0; k < 9; ++k) D[k] = Ft[k] - R[k];

@@ -26,14 +26,26 @@ def lame(E: torch.Tensor, nu: float):
     return mu, lam
 
 
+MATERIALS = {"elastic": 0, "neohookean": 1, "liquid": 2}
+
+
 class DifferentiableMPM:
     def __init__(self, scene_cfg: "_lib.MpmSceneConfig", nu: float = 0.2, rho: float = 1000.0,
-                 neohookean: bool = False, ckpt_every: int = 160):
+                 neohookean: bool = False, ckpt_every: int = 160, material: str | None = None,
+                 viscous: bool = False):
+        """material: "elastic" (corotated; "neohookean" or neohookean=True for the neo-Hookean
+        model) or "liquid" (liquid.py: mu = 0 unless viscous, F reset to J^(1/3) I every substep).
+        Young's modulus E is per particle; nu and rho are shared."""
         self.lib = _lib.load()
         self.cfg = scene_cfg
         self.nu = float(nu)
         self.rho = float(rho)
-        self.neo = int(bool(neohookean))
+        name = material if material is not None else ("neohookean" if neohookean else "elastic")
+        if name not in MATERIALS:
+            raise GenesisException(f"Unsupported differentiable material: {name}.")
+        self.material = name
+        self.viscous = bool(viscous)
+        self.neo = MATERIALS[name]
         self.ckpt_every = int(ckpt_every)
         d = scene_cfg.grid_density
         res = [int(round(d * scene_cfg.upper_bound[k]) - round(d * scene_cfg.lower_bound[k]) + 1) for k in range(3)]
@@ -155,6 +167,8 @@ class DifferentiableMPM:
         reference's differentiable mode takes losses at any frame of an episode)."""
         x, v, C, F = state
         mu, lam = lame(E, self.nu)
+        if self.material == "liquid" and not self.viscous:  # liquid.py:27-31
+            mu = mu * 0.0
         return _Advance.apply(self, int(n_substeps), x, v, C, F, mu, lam)
 
 

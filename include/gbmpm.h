@@ -452,8 +452,10 @@ int mpm_substeps_noalloc(const mpm_scene_config* scene, const mpm_material* mate
 const char* mpm_noalloc_last_error(void);
 
 /* ---------------------------------------------------------------- differentiation
- * One differentiable substep of one Elastic scene (corotated, or neo-Hookean when
- * neohookean != 0) with per-particle Lame parameters mu[n], lam[n], and its adjoint.
+ * One differentiable substep of one scene of a single material - `neohookean` 0: corotated
+ * Elastic, 1: neo-Hookean Elastic, 2: Liquid (liquid.py: the corotated stress with its mu, 0
+ * unless viscous, and F_new = J^(1/3) I) - with per-particle Lame parameters mu[n], lam[n], and
+ * its adjoint.
  * Replace the reference's Quadrants autodiff of the substep (p2g.grad, mpm_grid_op.grad,
  * g2p.grad, compute_F_tmp.grad: mpm_solver.py:517-554, legacy_coupler.py:998-1019) and its SVD
  * backward (mpm_solver.py:1229-1252).  Particle arrays use the reference layout; grid_pm,

@@ -221,3 +221,41 @@ def test_intermediate_losses_through_chained_segments_match_fp64_differences(sim
     gb, gEb = final_grad(False)
     assert np.allclose(ga, gb, rtol=1e-3, atol=1e-9 + 1e-4 * np.abs(gb).max()), (ga, gb)
     assert np.linalg.norm(gEa - gEb) <= 1e-2 * np.linalg.norm(gEb)
+
+
+def test_liquid_gradients_match_fp64_central_differences(oracle):
+    """The differentiable form with Liquid (liquid.py: mu = 0, stress lam J (J - 1) I, F reset to
+    J^(1/3) I every substep; E per particle through lam): dL/dv0 and a directional dL/dE of a
+    projection loss after 40 substeps against FP64 central differences of the oracle."""
+    import __graft_entry__ as g
+
+    g.build()
+    from genesis_gb300.diff import DifferentiableMPM
+
+    x0, v0, E, _ = _setup(seed=7)
+    n = len(x0)
+    # shear plus a uniform compression, so the pressure lam J (J - 1) shapes the motion
+    vf, pj = _shear(x0) - 5.0 * (x0 - x0.mean(0)), _proj(n)
+    nu, n_sub = 0.3, 40
+    sim = DifferentiableMPM(_scene(), nu=nu, rho=1000.0, ckpt_every=16, material="liquid")
+
+    def oracle_loss(v0_, E_):
+        sc = oracle.make_scene(2e-4, grid_density=32.0, particle_size=1.0 / 64)
+        mats = [oracle.make_material(1, 0.0, e * nu / ((1 + nu) * (1 - 2 * nu)), 1000.0) for e in E_]
+        st = dict(pos=x0, vel=np.tile(v0_, (n, 1)) + vf, C=np.zeros((n, 3, 3)), F=np.tile(np.eye(3), (n, 1, 1)),
+                  Jp=np.ones(n), mat=np.arange(n, dtype=np.int32), active=np.ones(n, bool))
+        out, _, _ = oracle.run(sc, mats, st, n_sub)
+        return float((out["pos"] * pj).sum() / n), out["pos"]
+
+    _, ref = oracle_loss(v0, E)
+    _, xf, gv, gE = _gpu_loss_and_grads(sim, x0, v0, E, None, n_sub, vfield=vf, proj=pj)
+    assert np.abs(xf - ref).max() < 1e-5
+    eps = 1e-4
+    fd_v = np.array([(oracle_loss(v0 + eps * e, E)[0] - oracle_loss(v0 - eps * e, E)[0]) / (2 * eps)
+                     for e in np.eye(3)])
+    assert np.linalg.norm(gv - fd_v) <= GRAD_RTOL * np.linalg.norm(fd_v), (gv, fd_v)
+    d = np.random.default_rng(2).normal(size=n)
+    d /= np.linalg.norm(d)
+    fd_E = (oracle_loss(v0, E * (1 + eps * d))[0] - oracle_loss(v0, E * (1 - eps * d))[0]) / (2 * eps)
+    ad_E = float(np.dot(gE, E * d))
+    assert abs(fd_E) > 1e-8 and abs(ad_E - fd_E) <= GRAD_RTOL * abs(fd_E), (ad_E, fd_E)
