@@ -3,3 +3,7 @@
 
 class GenesisException(Exception):
     pass
+
+
+class DeprecationError(GenesisException):
+    """A removed option or property (genesis/utils/misc.py DeprecationError)."""

@@ -466,13 +466,17 @@ class MPMSolver:
 
     @property
     def leaf_block_size(self):
-        """Deprecated in the reference (options/solvers.py: a no-op); the grid block here is 4^3 nodes."""
-        return 4
+        """Removed in the reference (mpm_solver.py:1172-1174), which raises."""
+        from .exceptions import DeprecationError
+
+        raise DeprecationError("This property has been removed.")
 
     @property
     def use_sparse_grid(self):
-        """Deprecated in the reference; only blocks touched by particles are processed here."""
-        return False
+        """Removed in the reference (mpm_solver.py:1176-1178), which returns the error object."""
+        from .exceptions import DeprecationError
+
+        return DeprecationError("This property has been removed.")
 
     def get_collider_poses(self) -> np.ndarray:
         """[n_colliders, 7]: current position and quaternion (w, x, y, z) of each collider; tools
