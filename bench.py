@@ -611,6 +611,22 @@ def run_forms(batched_substeps=200, n_requests=48):
     return out
 
 
+def run_served_only(n_requests=48):
+    """The served form's saturated run alone (one warm-up run, then the measured one): the
+    workload of run_forms, for profiling captures of the pool's kernels."""
+    import __graft_entry__ as g
+
+    g.build()
+    from genesis_gb300.serve import MPMServer, serving_workload
+
+    srv = MPMServer(max_slots=64, particle_capacity=40_000_000, max_grid_res=129, chunk=10)
+    srv.run(serving_workload(n_requests=n_requests, rate_hz=0, seed=77, with_payload=True), realtime=False)
+    sat = srv.run(serving_workload(n_requests=n_requests, rate_hz=0, seed=77, with_payload=True), realtime=False)
+    srv.close()
+    return {"form": "served (saturated)", "throughput": sat["throughput"], "wall_s": sat["wall_s"],
+            "chunks": sat["chunks"], "status": sat["status"]}
+
+
 def run_diff(steps=64, substeps_per_step=10, ckpt_steps=16, seed=99):
     """Differentiation config: ~216k-particle elastic cube (per-particle E ~ LogNormal(ln 3e5, 0.2)) on
     a 97^3 grid, 64 steps x 10 substeps, checkpoint every 16 steps; loss = ||COM - target||^2;
@@ -712,7 +728,12 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-forms", action="store_true", help="skip the batched/served form measurements")
     ap.add_argument("--tuning", default="", help="fixed P2G threads,particles per thread,G2P threads (no autotune)")
+    ap.add_argument("--form", default="", choices=["", "served"],
+                    help="diagnostic: run only the saturated served workload (for profiling captures)")
     args = ap.parse_args()
+    if args.form == "served":
+        print(json.dumps(run_served_only()))
+        return
     if args.warmup < 3:
         args.warmup = 3
     rank = int(os.environ.get("RANK", "0"))
