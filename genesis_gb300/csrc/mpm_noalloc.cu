@@ -1,13 +1,13 @@
 // mpm_noalloc.cu - mpm_substeps_noalloc: MPM substeps of one small scene that allocate no
 // device memory.
 //
-// Who needs it: callers that may not allocate device memory at all - code running while a
-// CUDA graph is being captured, plug-ins whose host application owns every allocation
-// through its own pool, and real-time loops that forbid allocator calls after start-up.
-// They pass their own particle arrays (updated in place) and get the substeps without a
-// context: the grid, which the other entry points keep in a context's cudaMalloc'd pool,
-// lives here in a fixed file-scope device array that the library reserves when it is
-// loaded.
+// Who needs it: callers that may not allocate device memory at all - plug-ins whose host
+// application owns every device allocation through its own budgeted pool, and real-time
+// control loops that forbid allocator calls after start-up (cudaMalloc and cudaFree may
+// synchronise the device and take unbounded time).  They pass their own particle arrays
+// (updated in place) and get the substeps without a context: the grid, which the other
+// entry points keep in a context's cudaMalloc'd pool, lives here in a fixed file-scope
+// device array that the library reserves when it is loaded.
 //
 // Limits and sharing:
 //  * the grid may have at most NOALLOC_MAX_NODES = 524288 nodes (e.g. 80^3; the unit cube at
@@ -19,7 +19,11 @@
 //  * particles are not re-sorted (a plain scatter with global vector atomics), so this path
 //    is meant for small scenes; the context entry points are the fast path.
 // The first call on a device looks up the array's device address (cudaGetSymbolAddress)
-// with that device current; make that first call before any stream capture.
+// with that device current; make that first call before any stream capture.  The address is
+// kept per device ordinal, for the device's primary context (the one the CUDA runtime and
+// PyTorch use); callers that drive the device through contexts of their own made with
+// cuCtxCreate are not supported.  Every call ends by synchronising its stream to read the
+// status word.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -207,10 +211,9 @@ __global__ void __launch_bounds__(256) k_na_g2p(NoallocParams Q) {
 std::mutex g_na_mu;
 float4* g_na_grid_ptr[NOALLOC_MAX_DEVICES] = {};
 uint32_t* g_na_status_ptr[NOALLOC_MAX_DEVICES] = {};
-std::string g_na_err;
+thread_local std::string g_na_err;  // text of the calling thread's last failed call
 
 int na_fail(int code, const std::string& msg) {
-  std::lock_guard<std::mutex> lk(g_na_mu);
   g_na_err = msg;
   return code;
 }
@@ -228,10 +231,7 @@ using namespace gbmpm;
 
 extern "C" {
 
-const char* mpm_noalloc_last_error(void) {
-  std::lock_guard<std::mutex> lk(g_na_mu);
-  return g_na_err.c_str();
-}
+const char* mpm_noalloc_last_error(void) { return g_na_err.c_str(); }
 
 int mpm_substeps_noalloc(const mpm_scene_config* scene, const mpm_material* materials, int32_t n_materials, int64_t n,
                          float* pos, float* vel, float* C, float* F, float* Jp, const int32_t* mat,
@@ -263,15 +263,9 @@ int mpm_substeps_noalloc(const mpm_scene_config* scene, const mpm_material* mate
       void* gp = nullptr;
       void* sp = nullptr;
       e = cudaGetSymbolAddress(&gp, g_noalloc_grid);
-      if (e != cudaSuccess) {
-        g_na_err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
-        return MPM_ERR_CUDA;
-      }
+      if (e != cudaSuccess) return na_fail(MPM_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
       e = cudaGetSymbolAddress(&sp, g_noalloc_status);
-      if (e != cudaSuccess) {
-        g_na_err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
-        return MPM_ERR_CUDA;
-      }
+      if (e != cudaSuccess) return na_fail(MPM_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
       g_na_grid_ptr[dev] = (float4*)gp;
       g_na_status_ptr[dev] = (uint32_t*)sp;
     }

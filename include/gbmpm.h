@@ -6,7 +6,7 @@
  * protocol that genesis/engine/simulator.py calls.  Every entry point below names the
  * reference kernel or method it replaces (file:line, paths relative to the Genesis
  * project root).  The Python package genesis_gb300 binds these with ctypes; a Genesis
- * maintainer would bind them the same way (a ctypes stub is shown in INTEGRATION.md).
+ * maintainer would bind them the same way, from genesis/engine/solvers/mpm_solver.py.
  *
  * Conventions
  *  - Every function returns an mpm_status code (0 = OK).  No C++ exception crosses the ABI.
@@ -435,20 +435,23 @@ int mpm_scene_retire(mpm_ctx* ctx, int64_t slot, void* stream);
 int mpm_scene_steps_left(mpm_ctx* ctx, int32_t* out_host, void* stream);
 
 /* ---------------------------------------------------------------- no-allocation substeps
- * No counterpart in the reference.  For callers that may not allocate device memory (code
- * running during CUDA graph capture, plug-ins whose host owns every allocation, real-time
- * loops): n_substeps substeps of one scene on the caller's particle arrays, updated in place
+ * No counterpart in the reference.  For callers that may not allocate device memory
+ * (plug-ins whose host application owns every device allocation through its own pool,
+ * real-time loops that forbid allocator calls after start-up, since cudaMalloc/cudaFree may
+ * synchronise the device): n_substeps substeps of one scene on the caller's particle arrays, updated in place
  * (device pointers, reference layout: pos/vel [n,3], C/F [n,3,3], Jp [n]; mat [n] material
  * index or NULL for 0; active [n] or NULL for all).  No cudaMalloc/cudaFree: the grid lives
  * in a file-scope device array of at most 524288 nodes (8 MiB on every GPU that loads the
  * library); at most 16 materials, no Muscle; particles are not re-sorted (small scenes).
  * Grids beyond the limit are rejected with MPM_ERR_BAD_ARG.  All calls share the array:
  * calls that overlap on the GPU race.  The first call on a device looks up the array's
- * address with that device current; make it before any stream capture.  Synchronises
- * `stream` at the end to read the status (NaN / out-of-grid). */
+ * address with that device current; make it before any stream capture.  Only the device's
+ * primary context is supported.  Synchronises `stream` at the end to read the status
+ * (NaN / out-of-grid). */
 int mpm_substeps_noalloc(const mpm_scene_config* scene, const mpm_material* materials, int32_t n_materials,
                          int64_t n, float* pos, float* vel, float* C, float* F, float* Jp,
                          const int32_t* mat, const uint8_t* active, int32_t n_substeps, void* stream);
+/* Text of the calling thread's last failed mpm_substeps_noalloc call. */
 const char* mpm_noalloc_last_error(void);
 
 /* ---------------------------------------------------------------- differentiation

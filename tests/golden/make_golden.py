@@ -419,7 +419,9 @@ def gen_substeps(F, rng):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GENESIS_REFERENCE")
+    if not ref:
+        sys.exit("usage: make_golden.py <Genesis project root>  (or set GENESIS_REFERENCE)")
     F = load_reference(ref)
     rng = np.random.default_rng(20261204)
     np.savez_compressed(os.path.join(HERE, "materials.npz"), **gen_materials(F, rng))

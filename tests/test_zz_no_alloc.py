@@ -1,11 +1,11 @@
 """mpm_substeps_noalloc: the entry point for callers that may not allocate device memory.
 
-Such callers (code running during CUDA graph capture, plug-ins whose host application owns
-every allocation, real-time loops) pass their own particle arrays; the grid the substep
-needs lives in a fixed device array inside the library.  The GPU test checks it against the
-context entry point (mpm_substeps) on the same scene, over two calls in a row, within the
-position tolerance the other GPU tests use (1e-4 of the 1 m domain).  This file is named to
-be collected last."""
+Such callers (plug-ins whose host application owns every device allocation through its own
+pool, real-time loops that forbid allocator calls after start-up) pass their own particle
+arrays; the grid the substep needs lives in a fixed device array inside the library.  The GPU
+test checks it against the context entry point (mpm_substeps) and against the FP64 CPU oracle
+on the same scene, over two calls in a row, within the position tolerance the other GPU tests
+use (1e-4 of the 1 m domain).  This file is named to be collected last."""
 
 import ctypes
 
@@ -42,7 +42,7 @@ def test_noalloc_rejects_grid_beyond_limit():
 
 
 @pytest.mark.gpu
-def test_noalloc_matches_context_entry_point_on_two_calls():
+def test_noalloc_matches_context_entry_point_on_two_calls(oracle):
     import __graft_entry__ as g
 
     g.build()
@@ -76,9 +76,14 @@ def test_noalloc_matches_context_entry_point_on_two_calls():
     mat_arr = (_lib.MpmMaterial * 2)(*mats)
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
+    host = dict(pos=pos.astype(np.float32).astype(np.float64), vel=np.zeros((n, 3)), C=np.zeros((n, 3, 3)),
+                F=np.tile(np.eye(3), (n, 1, 1)), Jp=np.where(mat == 1, 0.0, 1.0), mat=mat, active=np.ones(n, bool))
+    osc = oracle.make_scene(2e-4, grid_density=64.0, particle_size=1 / 128)
+    omats = [oracle.from_c_material(m) for m in mats]
     for call in range(2):
         c.substeps(25)
         ref = c.get_state(0, 1, n)
+        host, _, _ = oracle.run(osc, omats, host, 25)
         r = lib.mpm_substeps_noalloc(ctypes.byref(sc), mat_arr, 2, n, P.data_ptr(), V.data_ptr(), Cm.data_ptr(),
                                      F.data_ptr(), Jp.data_ptr(), M.data_ptr(), A.data_ptr(), 25, stream)
         assert r == 0, lib.mpm_noalloc_last_error()
@@ -87,4 +92,38 @@ def test_noalloc_matches_context_entry_point_on_two_calls():
         assert err <= POS_TOL, (call, err)
         assert np.abs(V.cpu().numpy() - ref["vel"]).max() <= 1e-2, call
         assert np.abs(F.cpu().numpy() - ref["F"]).max() <= 1e-4, call
+        oerr = np.abs(P.cpu().numpy() - host["pos"]).max()
+        assert oerr <= POS_TOL, (call, oerr)
+        assert np.abs(V.cpu().numpy() - host["vel"]).max() <= 1e-2, call
     c.close()
+
+
+@pytest.mark.gpu
+def test_noalloc_reports_a_particle_outside_the_grid():
+    """A particle whose stencil would leave the grid is skipped and reported as MPM_ERR_OOB (the
+    kernel range-checks it and touches no memory for it); the next call starts from a clear
+    status and succeeds on particles inside the grid."""
+    import __graft_entry__ as g
+
+    g.build()
+    from genesis_gb300 import _lib
+
+    lib = _lib.load()
+    sc, mats = _scene_and_materials(3)
+    pos = torch.tensor([[0.5, 0.5, 0.5], [0.45, 0.5, 0.5], [1.5, 0.5, 0.5]], device="cuda")
+    n = 3
+    V = torch.zeros((n, 3), device="cuda")
+    Cm = torch.zeros((n, 3, 3), device="cuda")
+    F = torch.eye(3, device="cuda").repeat(n, 1, 1).contiguous()
+    Jp = torch.ones(n, device="cuda")
+    mat_arr = (_lib.MpmMaterial * 1)(mats[0])
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    r = lib.mpm_substeps_noalloc(ctypes.byref(sc), mat_arr, 1, n, pos.data_ptr(), V.data_ptr(), Cm.data_ptr(),
+                                 F.data_ptr(), Jp.data_ptr(), None, None, 2, stream)
+    assert _lib.STATUS_NAMES.get(r) == "MPM_ERR_OOB", (r, lib.mpm_noalloc_last_error())
+    assert b"left the grid" in lib.mpm_noalloc_last_error()
+    inside = pos[:2].contiguous()
+    r = lib.mpm_substeps_noalloc(ctypes.byref(sc), mat_arr, 1, 2, inside.data_ptr(), V.data_ptr(), Cm.data_ptr(),
+                                 F.data_ptr(), Jp.data_ptr(), None, None, 2, stream)
+    assert r == 0, lib.mpm_noalloc_last_error()
+    assert torch.isfinite(inside).all()
