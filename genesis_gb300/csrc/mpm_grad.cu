@@ -29,6 +29,8 @@ struct DiffParams {
   SceneDev S;
   float mass;
   int32_t neohookean;
+  const float* pmass;     // per-particle mass (mixed scenes) or null: `mass` for all
+  const int32_t* pkind;   // per-particle material (DIFF_*) or null: `neohookean` for all
   int64_t n;
   const float *x, *v, *C, *F, *mu, *lam;
   float *x1, *v1, *C1, *F1;
@@ -68,6 +70,9 @@ __device__ __forceinline__ bool make_stencil(const SceneDev& S, const float* x, 
 
 // Material of the differentiable form (the `neohookean` argument of the entry points).
 constexpr int DIFF_COROTATED = 0, DIFF_NEOHOOKEAN = 1, DIFF_LIQUID = 2;
+
+__device__ __forceinline__ float p_mass(const DiffParams& Q, int64_t i) { return Q.pmass ? Q.pmass[i] : Q.mass; }
+__device__ __forceinline__ int p_kind(const DiffParams& Q, int64_t i) { return Q.pkind ? Q.pkind[i] : Q.neohookean; }
 
 // corotated / neo-Hookean stress of elastic.py:48-60 with per-particle mu, lam; F_new = F_tmp
 // (liquid: the corotated form with its mu, 0 unless viscous; F_new = J^(1/3) I)
@@ -125,12 +130,14 @@ __global__ void __launch_bounds__(256) k_dp2g(DiffParams Q) {
       atomicOr(Q.status, 2u);
       continue;
     }
+    const float mass = p_mass(Q, i);
+    const int kind = p_kind(Q, i);
     float Ft[9], U[9], sig[3], V[9], P[9];
     f_tmp(C, F, S.dt, Ft);
     svd_f32(Ft, U, sig, V);
-    elastic_stress(Ft, Q.mu[i], Q.lam[i], Q.neohookean == DIFF_NEOHOOKEAN, U, sig, V, P);
+    elastic_stress(Ft, Q.mu[i], Q.lam[i], kind == DIFF_NEOHOOKEAN, U, sig, V, P);
     if (Q.F1) {
-      if (Q.neohookean == DIFF_LIQUID) {  // liquid.py:36-40: F_new = J^(1/3) I
+      if (kind == DIFF_LIQUID) {  // liquid.py:36-40: F_new = J^(1/3) I
         const float j3 = powf(sig[0] * sig[1] * sig[2], 1.f / 3.f);
         for (int k = 0; k < 9; ++k) Q.F1[i * 9 + k] = (k % 4 == 0) ? j3 : 0.f;
       } else {
@@ -138,7 +145,7 @@ __global__ void __launch_bounds__(256) k_dp2g(DiffParams Q) {
       }
     }
     float A[9];
-    for (int k = 0; k < 9; ++k) A[k] = S.stress_scale * P[k] + Q.mass * C[k];
+    for (int k = 0; k < 9; ++k) A[k] = S.stress_scale * P[k] + mass * C[k];
     for (int ox = 0; ox < 3; ++ox)
       for (int oy = 0; oy < 3; ++oy)
         for (int oz = 0; oz < 3; ++oz) {
@@ -146,10 +153,10 @@ __global__ void __launch_bounds__(256) k_dp2g(DiffParams Q) {
           const float dp[3] = {((float)ox - st.fx[0]) * S.dx, ((float)oy - st.fx[1]) * S.dx,
                                ((float)oz - st.fx[2]) * S.dx};
           float4 g;
-          g.x = wt * (Q.mass * v[0] + A[0] * dp[0] + A[1] * dp[1] + A[2] * dp[2]);
-          g.y = wt * (Q.mass * v[1] + A[3] * dp[0] + A[4] * dp[1] + A[5] * dp[2]);
-          g.z = wt * (Q.mass * v[2] + A[6] * dp[0] + A[7] * dp[1] + A[8] * dp[2]);
-          g.w = wt * Q.mass;
+          g.x = wt * (mass * v[0] + A[0] * dp[0] + A[1] * dp[1] + A[2] * dp[2]);
+          g.y = wt * (mass * v[1] + A[3] * dp[0] + A[4] * dp[1] + A[5] * dp[2]);
+          g.z = wt * (mass * v[2] + A[6] * dp[0] + A[7] * dp[1] + A[8] * dp[2]);
+          g.w = wt * mass;
           atomicAdd(&Q.pm[didx(S, st.b[0] + ox, st.b[1] + oy, st.b[2] + oz)], g);
         }
   }
@@ -354,12 +361,14 @@ __global__ void __launch_bounds__(256) k_dp2g_adj(DiffParams Q) {
       continue;
     }
     const float mu = Q.mu[i], lam = Q.lam[i];
+    const float mass = p_mass(Q, i);
+    const int kind = p_kind(Q, i);
     float Ft[9], U[9], sig[3], V[9], P[9];
     f_tmp(C, F, S.dt, Ft);
     svd_f32(Ft, U, sig, V);
-    elastic_stress(Ft, mu, lam, Q.neohookean == DIFF_NEOHOOKEAN, U, sig, V, P);
+    elastic_stress(Ft, mu, lam, kind == DIFF_NEOHOOKEAN, U, sig, V, P);
     float A[9];
-    for (int k = 0; k < 9; ++k) A[k] = S.stress_scale * P[k] + Q.mass * C[k];
+    for (int k = 0; k < 9; ++k) A[k] = S.stress_scale * P[k] + mass * C[k];
     float gv[3] = {0.f, 0.f, 0.f}, gA[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, gx[3];
     for (int d = 0; d < 3; ++d) gx[d] = Q.gx[i * 3 + d];
     for (int ox = 0; ox < 3; ++ox)
@@ -372,14 +381,14 @@ __global__ void __launch_bounds__(256) k_dp2g_adj(DiffParams Q) {
           const float dp[3] = {((float)ox - st.fx[0]) * S.dx, ((float)oy - st.fx[1]) * S.dx,
                                ((float)oz - st.fx[2]) * S.dx};
           float mom[3];
-          for (int r = 0; r < 3; ++r) mom[r] = Q.mass * v[r] + A[r * 3 + 0] * dp[0] + A[r * 3 + 1] * dp[1] + A[r * 3 + 2] * dp[2];
+          for (int r = 0; r < 3; ++r) mom[r] = mass * v[r] + A[r * 3 + 0] * dp[0] + A[r * 3 + 1] * dp[1] + A[r * 3 + 2] * dp[2];
           for (int r = 0; r < 3; ++r) {
-            gv[r] += Q.mass * wt * gp[r];
+            gv[r] += mass * wt * gp[r];
             for (int c = 0; c < 3; ++c) gA[r * 3 + c] += wt * gp[r] * dp[c];
           }
           // d(dp)/dx = -I : -A^T gp
           for (int c = 0; c < 3; ++c) gx[c] += -wt * (A[0 * 3 + c] * gp[0] + A[1 * 3 + c] * gp[1] + A[2 * 3 + c] * gp[2]);
-          const float wbar = gp[0] * mom[0] + gp[1] * mom[1] + gp[2] * mom[2] + g.w * Q.mass;
+          const float wbar = gp[0] * mom[0] + gp[1] * mom[1] + gp[2] * mom[2] + g.w * mass;
           const float dw[3] = {st.dw[0][o[0]] * st.w[1][o[1]] * st.w[2][o[2]], st.w[0][o[0]] * st.dw[1][o[1]] * st.w[2][o[2]],
                                st.w[0][o[0]] * st.w[1][o[1]] * st.dw[2][o[2]]};
           for (int c = 0; c < 3; ++c) gx[c] += wbar * dw[c] * S.inv_dx;
@@ -389,10 +398,10 @@ __global__ void __launch_bounds__(256) k_dp2g_adj(DiffParams Q) {
     const float J = sig[0] * sig[1] * sig[2];
     for (int k = 0; k < 9; ++k) {
       gP[k] = S.stress_scale * gA[k];
-      gC[k] = Q.mass * gA[k];
-      gFt[k] = (Q.gF1 && Q.neohookean != DIFF_LIQUID) ? Q.gF1[i * 9 + k] : 0.f;  // F1 = F_tmp
+      gC[k] = mass * gA[k];
+      gFt[k] = (Q.gF1 && kind != DIFF_LIQUID) ? Q.gF1[i * 9 + k] : 0.f;  // F1 = F_tmp
     }
-    if (Q.gF1 && Q.neohookean == DIFF_LIQUID) {
+    if (Q.gF1 && kind == DIFF_LIQUID) {
       // F1 = J^(1/3) I: dL/dJ = tr(gF1) J^(-2/3) / 3, dJ/dF_tmp = cof(F_tmp)
       const float gJ = (Q.gF1[i * 9 + 0] + Q.gF1[i * 9 + 4] + Q.gF1[i * 9 + 8]) * powf(J, -2.f / 3.f) / 3.f;
       gFt[0] += gJ * (Ft[4] * Ft[8] - Ft[5] * Ft[7]);
@@ -407,7 +416,7 @@ __global__ void __launch_bounds__(256) k_dp2g_adj(DiffParams Q) {
     }
     const float trP = gP[0] + gP[4] + gP[8];
     float gmu, glam;
-    if (Q.neohookean == DIFF_NEOHOOKEAN) {
+    if (kind == DIFF_NEOHOOKEAN) {
       // P = mu F F^T + (lam log J - mu) I
       float FFt[9];
       mat_mul_bt(Ft, Ft, FFt);
@@ -503,15 +512,13 @@ __global__ void __launch_bounds__(256) k_dp2g_adj(DiffParams Q) {
 
 using namespace gbmpm;
 
-extern "C" {
+namespace {
 
-// One differentiable substep of one scene: (x, v, C, F) -> (x1, v1, C1, F1) with per-particle
-// Lame parameters (Elastic material, corotated or neo-Hookean), all device arrays in the
-// reference layout.  grid_pm and grid_v are caller buffers of res^3 float4 (res from the
-// scene), left holding this substep's grid (needed by mpm_diff_backward).
-int mpm_diff_forward(const mpm_scene_config* scene, double rho, int32_t neohookean, int64_t n, const float* x,
-                     const float* v, const float* C, const float* F, const float* mu, const float* lam, float* x1,
-                     float* v1, float* C1, float* F1, void* grid_pm, void* grid_v, uint32_t* status, void* stream) {
+// One forward substep; mass_pp / kind_pp (per particle) override rho / neohookean when given.
+int diff_forward(const mpm_scene_config* scene, double rho, int32_t neohookean, const float* mass_pp,
+                 const int32_t* kind_pp, int64_t n, const float* x, const float* v, const float* C, const float* F,
+                 const float* mu, const float* lam, float* x1, float* v1, float* C1, float* F1, void* grid_pm,
+                 void* grid_v, uint32_t* status, void* stream) {
   if (!scene || n < 0 || !grid_pm || !grid_v || !status) return MPM_ERR_BAD_ARG;
   DiffParams Q;
   std::memset(&Q, 0, sizeof(Q));
@@ -520,6 +527,8 @@ int mpm_diff_forward(const mpm_scene_config* scene, double rho, int32_t neohooke
   const double pvol = scene->particle_size * scene->particle_size * scene->particle_size * 1e3;
   Q.mass = (float)pvol * (float)rho;
   Q.neohookean = neohookean;
+  Q.pmass = mass_pp;
+  Q.pkind = kind_pp;
   Q.n = n;
   Q.x = x, Q.v = v, Q.C = C, Q.F = F, Q.mu = mu, Q.lam = lam;
   Q.x1 = x1, Q.v1 = v1, Q.C1 = C1, Q.F1 = F1;
@@ -537,15 +546,11 @@ int mpm_diff_forward(const mpm_scene_config* scene, double rho, int32_t neohooke
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_ERR_CUDA;
 }
 
-// Adjoint of mpm_diff_forward at state (x, v, C, F): given dL/d(x1, v1, C1, F1) (gF1 may be
-// NULL), writes dL/d(x, v, C, F) and adds dL/d(mu, lam).  grid_pm/grid_v must hold the
-// forward grid of this substep (call mpm_diff_forward on the same state first); g_grid_v and
-// g_grid_pm are res^3 float4 scratch buffers.
-int mpm_diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean, int64_t n, const float* x,
-                      const float* v, const float* C, const float* F, const float* mu, const float* lam,
-                      const float* gx1, const float* gv1, const float* gC1, const float* gF1, float* gx, float* gv,
-                      float* gC, float* gF, float* gmu, float* glam, void* grid_pm, void* grid_v, void* g_grid_v,
-                      void* g_grid_pm, uint32_t* status, void* stream) {
+int diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean, const float* mass_pp,
+                  const int32_t* kind_pp, int64_t n, const float* x, const float* v, const float* C, const float* F,
+                  const float* mu, const float* lam, const float* gx1, const float* gv1, const float* gC1,
+                  const float* gF1, float* gx, float* gv, float* gC, float* gF, float* gmu, float* glam, void* grid_pm,
+                  void* grid_v, void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream) {
   if (!scene || n < 0 || !grid_pm || !grid_v || !g_grid_v || !g_grid_pm) return MPM_ERR_BAD_ARG;
   DiffParams Q;
   std::memset(&Q, 0, sizeof(Q));
@@ -554,6 +559,8 @@ int mpm_diff_backward(const mpm_scene_config* scene, double rho, int32_t neohook
   const double pvol = scene->particle_size * scene->particle_size * scene->particle_size * 1e3;
   Q.mass = (float)pvol * (float)rho;
   Q.neohookean = neohookean;
+  Q.pmass = mass_pp;
+  Q.pkind = kind_pp;
   Q.n = n;
   Q.x = x, Q.v = v, Q.C = C, Q.F = F, Q.mu = mu, Q.lam = lam;
   Q.gx1 = gx1, Q.gv1 = gv1, Q.gC1 = gC1, Q.gF1 = gF1;
@@ -574,15 +581,10 @@ int mpm_diff_backward(const mpm_scene_config* scene, double rho, int32_t neohook
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_ERR_CUDA;
 }
 
-// n_sub forward substeps in one call (no host round trip per substep).  State k (k = 0..n_sub)
-// lives in slot k % ring of x_seq [ring, n, 3], v_seq [ring, n, 3], C_seq [ring, n, 9] and
-// F_seq [ring, n, 9]; slot 0 holds the input.  ring = 2 ping-pongs; ring > n_sub keeps every
-// state.  With grids_per_substep, substep k leaves its grid in grid_pm + k * nodes and
-// grid_v + k * nodes (n_sub grids each); otherwise every substep uses the one grid given.
-int mpm_diff_forward_seq(const mpm_scene_config* scene, double rho, int32_t neohookean, int64_t n, int32_t n_sub,
-                         float* x_seq, float* v_seq, float* C_seq, float* F_seq, int32_t ring, const float* mu,
-                         const float* lam, void* grid_pm, void* grid_v, int32_t grids_per_substep, uint32_t* status,
-                         void* stream) {
+int diff_forward_seq(const mpm_scene_config* scene, double rho, int32_t neohookean, const float* mass_pp,
+                     const int32_t* kind_pp, int64_t n, int32_t n_sub, float* x_seq, float* v_seq, float* C_seq,
+                     float* F_seq, int32_t ring, const float* mu, const float* lam, void* grid_pm, void* grid_v,
+                     int32_t grids_per_substep, uint32_t* status, void* stream) {
   if (!scene || n < 0 || n_sub < 0 || ring < 2 || !x_seq || !v_seq || !C_seq || !F_seq) return MPM_ERR_BAD_ARG;
   SceneDev S;
   std::string err;
@@ -591,22 +593,20 @@ int mpm_diff_forward_seq(const mpm_scene_config* scene, double rho, int32_t neoh
   for (int32_t k = 0; k < n_sub; ++k) {
     const int64_t a = k % ring, b = (k + 1) % ring;
     const int64_t go = grids_per_substep ? (int64_t)k * nodes : 0;
-    const int r = mpm_diff_forward(scene, rho, neohookean, n, x_seq + a * n * 3, v_seq + a * n * 3, C_seq + a * n * 9,
-                                   F_seq + a * n * 9, mu, lam, x_seq + b * n * 3, v_seq + b * n * 3, C_seq + b * n * 9,
-                                   F_seq + b * n * 9, (float4*)grid_pm + go, (float4*)grid_v + go, status, stream);
+    const int r = diff_forward(scene, rho, neohookean, mass_pp, kind_pp, n, x_seq + a * n * 3, v_seq + a * n * 3,
+                               C_seq + a * n * 9, F_seq + a * n * 9, mu, lam, x_seq + b * n * 3, v_seq + b * n * 3,
+                               C_seq + b * n * 9, F_seq + b * n * 9, (float4*)grid_pm + go, (float4*)grid_v + go, status,
+                               stream);
     if (r) return r;
   }
   return MPM_OK;
 }
 
-// Adjoint of n_sub substeps whose states 0..n_sub-1 and grids were kept by mpm_diff_forward_seq
-// (ring > n_sub - 1, grids_per_substep).  g_seq [2, 24 n] holds two packed gradient buffers
-// (dx [n,3], dv [n,3], dC [n,9], dF [n,9]); buffer 0 holds dL/d(state n_sub) on entry and
-// dL/d(state 0) on return.  dL/d(mu, lam) accumulate into gmu, glam.
-int mpm_diff_backward_seq(const mpm_scene_config* scene, double rho, int32_t neohookean, int64_t n, int32_t n_sub,
-                          const float* x_seq, const float* v_seq, const float* C_seq, const float* F_seq,
-                          const float* mu, const float* lam, float* g_seq, float* gmu, float* glam, void* grid_pm,
-                          void* grid_v, void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream) {
+int diff_backward_seq(const mpm_scene_config* scene, double rho, int32_t neohookean, const float* mass_pp,
+                      const int32_t* kind_pp, int64_t n, int32_t n_sub, const float* x_seq, const float* v_seq,
+                      const float* C_seq, const float* F_seq, const float* mu, const float* lam, float* g_seq,
+                      float* gmu, float* glam, void* grid_pm, void* grid_v, void* g_grid_v, void* g_grid_pm,
+                      uint32_t* status, void* stream) {
   if (!scene || n < 0 || n_sub < 0 || !g_seq) return MPM_ERR_BAD_ARG;
   SceneDev S;
   std::string err;
@@ -617,11 +617,11 @@ int mpm_diff_backward_seq(const mpm_scene_config* scene, double rho, int32_t neo
   for (int32_t k = n_sub - 1; k >= 0; --k) {
     float* gi = g_seq + cur * gs;
     float* go = g_seq + (1 - cur) * gs;
-    const int r = mpm_diff_backward(scene, rho, neohookean, n, x_seq + (int64_t)k * n * 3, v_seq + (int64_t)k * n * 3,
-                                    C_seq + (int64_t)k * n * 9, F_seq + (int64_t)k * n * 9, mu, lam, gi, gi + 3 * n,
-                                    gi + 6 * n, gi + 15 * n, go, go + 3 * n, go + 6 * n, go + 15 * n, gmu, glam,
-                                    (float4*)grid_pm + (int64_t)k * nodes, (float4*)grid_v + (int64_t)k * nodes,
-                                    g_grid_v, g_grid_pm, status, stream);
+    const int r = diff_backward(scene, rho, neohookean, mass_pp, kind_pp, n, x_seq + (int64_t)k * n * 3,
+                                v_seq + (int64_t)k * n * 3, C_seq + (int64_t)k * n * 9, F_seq + (int64_t)k * n * 9, mu,
+                                lam, gi, gi + 3 * n, gi + 6 * n, gi + 15 * n, go, go + 3 * n, go + 6 * n, go + 15 * n,
+                                gmu, glam, (float4*)grid_pm + (int64_t)k * nodes, (float4*)grid_v + (int64_t)k * nodes,
+                                g_grid_v, g_grid_pm, status, stream);
     if (r) return r;
     cur = 1 - cur;
   }
@@ -629,6 +629,82 @@ int mpm_diff_backward_seq(const mpm_scene_config* scene, double rho, int32_t neo
                                   (cudaStream_t)stream) != cudaSuccess)
     return MPM_ERR_CUDA;
   return MPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// One differentiable substep of one scene: (x, v, C, F) -> (x1, v1, C1, F1) with per-particle
+// Lame parameters (Elastic material, corotated or neo-Hookean), all device arrays in the
+// reference layout.  grid_pm and grid_v are caller buffers of res^3 float4 (res from the
+// scene), left holding this substep's grid (needed by mpm_diff_backward).
+int mpm_diff_forward(const mpm_scene_config* scene, double rho, int32_t neohookean, int64_t n, const float* x,
+                     const float* v, const float* C, const float* F, const float* mu, const float* lam, float* x1,
+                     float* v1, float* C1, float* F1, void* grid_pm, void* grid_v, uint32_t* status, void* stream) {
+  return diff_forward(scene, rho, neohookean, nullptr, nullptr, n, x, v, C, F, mu, lam, x1, v1, C1, F1, grid_pm,
+                      grid_v, status, stream);
+}
+
+// Adjoint of mpm_diff_forward at state (x, v, C, F): given dL/d(x1, v1, C1, F1) (gF1 may be
+// NULL), writes dL/d(x, v, C, F) and adds dL/d(mu, lam).  grid_pm/grid_v must hold the
+// forward grid of this substep (call mpm_diff_forward on the same state first); g_grid_v and
+// g_grid_pm are res^3 float4 scratch buffers.
+int mpm_diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean, int64_t n, const float* x,
+                      const float* v, const float* C, const float* F, const float* mu, const float* lam,
+                      const float* gx1, const float* gv1, const float* gC1, const float* gF1, float* gx, float* gv,
+                      float* gC, float* gF, float* gmu, float* glam, void* grid_pm, void* grid_v, void* g_grid_v,
+                      void* g_grid_pm, uint32_t* status, void* stream) {
+  return diff_backward(scene, rho, neohookean, nullptr, nullptr, n, x, v, C, F, mu, lam, gx1, gv1, gC1, gF1, gx, gv,
+                       gC, gF, gmu, glam, grid_pm, grid_v, g_grid_v, g_grid_pm, status, stream);
+}
+
+// n_sub forward substeps in one call (no host round trip per substep).  State k (k = 0..n_sub)
+// lives in slot k % ring of x_seq [ring, n, 3], v_seq [ring, n, 3], C_seq [ring, n, 9] and
+// F_seq [ring, n, 9]; slot 0 holds the input.  ring = 2 ping-pongs; ring > n_sub keeps every
+// state.  With grids_per_substep, substep k leaves its grid in grid_pm + k * nodes and
+// grid_v + k * nodes (n_sub grids each); otherwise every substep uses the one grid given.
+int mpm_diff_forward_seq(const mpm_scene_config* scene, double rho, int32_t neohookean, int64_t n, int32_t n_sub,
+                         float* x_seq, float* v_seq, float* C_seq, float* F_seq, int32_t ring, const float* mu,
+                         const float* lam, void* grid_pm, void* grid_v, int32_t grids_per_substep, uint32_t* status,
+                         void* stream) {
+  return diff_forward_seq(scene, rho, neohookean, nullptr, nullptr, n, n_sub, x_seq, v_seq, C_seq, F_seq, ring, mu,
+                          lam, grid_pm, grid_v, grids_per_substep, status, stream);
+}
+
+// Adjoint of n_sub substeps whose states 0..n_sub-1 and grids were kept by mpm_diff_forward_seq
+// (ring > n_sub - 1, grids_per_substep).  g_seq [2, 24 n] holds two packed gradient buffers
+// (dx [n,3], dv [n,3], dC [n,9], dF [n,9]); buffer 0 holds dL/d(state n_sub) on entry and
+// dL/d(state 0) on return.  dL/d(mu, lam) accumulate into gmu, glam.
+int mpm_diff_backward_seq(const mpm_scene_config* scene, double rho, int32_t neohookean, int64_t n, int32_t n_sub,
+                          const float* x_seq, const float* v_seq, const float* C_seq, const float* F_seq,
+                          const float* mu, const float* lam, float* g_seq, float* gmu, float* glam, void* grid_pm,
+                          void* grid_v, void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream) {
+  return diff_backward_seq(scene, rho, neohookean, nullptr, nullptr, n, n_sub, x_seq, v_seq, C_seq, F_seq, mu, lam,
+                           g_seq, gmu, glam, grid_pm, grid_v, g_grid_v, g_grid_pm, status, stream);
+}
+
+// mpm_diff_forward_seq / mpm_diff_backward_seq for a scene of several entities: the particle
+// mass [n] and material kind [n] (0 corotated Elastic, 1 neo-Hookean Elastic, 2 Liquid) are given
+// per particle, as the reference's differentiable MPM path reads them per particle through
+// particles_info and the material dispatch (mpm_solver.py:341-375).
+int mpm_diff_forward_seq_pp(const mpm_scene_config* scene, const float* mass, const int32_t* kind, int64_t n,
+                            int32_t n_sub, float* x_seq, float* v_seq, float* C_seq, float* F_seq, int32_t ring,
+                            const float* mu, const float* lam, void* grid_pm, void* grid_v, int32_t grids_per_substep,
+                            uint32_t* status, void* stream) {
+  if (n > 0 && (!mass || !kind)) return MPM_ERR_BAD_ARG;
+  return diff_forward_seq(scene, 0.0, 0, mass, kind, n, n_sub, x_seq, v_seq, C_seq, F_seq, ring, mu, lam, grid_pm,
+                          grid_v, grids_per_substep, status, stream);
+}
+
+int mpm_diff_backward_seq_pp(const mpm_scene_config* scene, const float* mass, const int32_t* kind, int64_t n,
+                             int32_t n_sub, const float* x_seq, const float* v_seq, const float* C_seq,
+                             const float* F_seq, const float* mu, const float* lam, float* g_seq, float* gmu,
+                             float* glam, void* grid_pm, void* grid_v, void* g_grid_v, void* g_grid_pm,
+                             uint32_t* status, void* stream) {
+  if (n > 0 && (!mass || !kind)) return MPM_ERR_BAD_ARG;
+  return diff_backward_seq(scene, 0.0, 0, mass, kind, n, n_sub, x_seq, v_seq, C_seq, F_seq, mu, lam, g_seq, gmu, glam,
+                           grid_pm, grid_v, g_grid_v, g_grid_pm, status, stream);
 }
 
 }  // extern "C"

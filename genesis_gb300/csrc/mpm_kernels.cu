@@ -1095,6 +1095,26 @@ __device__ __forceinline__ void block_origin(const SceneDev& S, int64_t key, int
   org[0] = (int)(lb / ((int64_t)S.bres[2] * S.bres[1])) * BLK;
 }
 
+// Particles per thread of a P2G item whose old slot and cell are loaded ahead (registers).
+constexpr int P2G_PF = 4;
+
+// The head of P2G work item `item`: its scene and, for the first P2G_PF particles of each thread
+// (j = thread + k * T), the old slot (perm) and the cell in the block (slot_cell).  Loaded while
+// the previous item scatters, so an item does not start with a chain of dependent global loads.
+__device__ __forceinline__ void p2g_item_head(const KParams& P, int4 item, int T, int32_t* si, int32_t* cell,
+                                              int32_t& sid) {
+  const int cnt = item.z - item.y;
+  const bool real = item.x < P.K && cnt > 0;
+  sid = real ? P.block_scene[item.x] : 0;
+#pragma unroll
+  for (int k = 0; k < P2G_PF; ++k) {
+    const int j = (int)threadIdx.x + k * T;
+    const bool ok = real && j < cnt;
+    si[k] = ok ? P.perm[item.y + j] : 0;
+    cell[k] = ok ? (int32_t)P.slot_cell[item.y + j] : 0;
+  }
+}
+
 }  // namespace
 
 // Per work item (one grid block's bucket, up to `chunk` <= P2G_MAX_CHUNK particles):
@@ -1117,6 +1137,9 @@ __device__ __forceinline__ void p2g_body(const KParams& P) {
   extern __shared__ __align__(16) unsigned char p2g_smem[];
   __shared__ int s_cnt[BLK_NODES + 1];
   __shared__ int s_touch[8];
+  // the item's scene record, read from shared memory: a reference into the global table would be
+  // re-read after every particle store (the compiler cannot rule out aliasing)
+  __shared__ SceneDev s_scene;
   const int n_items = *P.n_items;
   const int T = blockDim.x, nw = T >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float4* s_tile = reinterpret_cast<float4*>(p2g_smem);
@@ -1132,25 +1155,48 @@ __device__ __forceinline__ void p2g_body(const KParams& P) {
   if (threadIdx.x <= BLK_NODES) s_cnt[threadIdx.x] = 0;
   if (threadIdx.x < 8) s_touch[threadIdx.x] = 0;
   __syncthreads();
+  int4 nitem = (int)blockIdx.x < n_items ? P.items[blockIdx.x] : make_int4(0, 0, 0, 0);
+  int32_t nsi[P2G_PF], ncell[P2G_PF], nsid;
+  p2g_item_head(P, nitem, T, nsi, ncell, nsid);
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
-    const int4 item = P.items[it];
+    const int4 item = nitem;
+    const int32_t sid = nsid;
+    int32_t pf_si[P2G_PF], pf_cell[P2G_PF];
+#pragma unroll
+    for (int k = 0; k < P2G_PF; ++k) {
+      pf_si[k] = nsi[k];
+      pf_cell[k] = ncell[k];
+    }
+    const int nit = it + (int)gridDim.x;
     const int cnt = item.z - item.y;
-    const bool frozen = item.x < P.K && P.steps && P.steps[P.block_scene[item.x]] == 0;
+    const bool frozen = item.x < P.K && P.steps && P.steps[sid] == 0;
     if (item.x >= P.K || frozen) {  // inactive bucket or frozen scene: carry over unchanged (uniform)
       for (int j = threadIdx.x; j < cnt; j += T) {
         const int64_t si = P.perm[item.y + j];
         for (int k = 0; k < P.nf; ++k) Dx[(int64_t)k * cap + item.y + j] = Sx[(int64_t)k * cap + si];
       }
+      nitem = nit < n_items ? P.items[nit] : make_int4(0, 0, 0, 0);
+      p2g_item_head(P, nitem, T, nsi, ncell, nsid);
       continue;
     }
-    const int32_t sid = P.block_scene[item.x];
-    const SceneDev& S = P.scenes[sid];
     int org[3];
-    block_origin(S, item.x, org);
-    // 1. cell ranks
-    for (int j = threadIdx.x; j < cnt; j += T) {
+    block_origin(P.scenes[sid], item.x, org);
+    if (threadIdx.x == 0) s_scene = P.scenes[sid];  // published by the barrier after step 1
+    const SceneDev& S = s_scene;
+    // 1. cell ranks (old slot and cell of the first P2G_PF particles per thread were loaded ahead;
+    //    the cell comes from the G2P, or re-keying, that keyed the particle)
+#pragma unroll
+    for (int k = 0; k < P2G_PF; ++k) {
+      const int j = (int)threadIdx.x + k * T;
+      if (j < cnt) {
+        s_si[j] = pf_si[k];
+        const int r = atomicAdd(&s_cnt[pf_cell[k]], 1);
+        s_cr[j] = ((uint32_t)pf_cell[k] << 16) | (uint32_t)r;
+      }
+    }
+    for (int j = (int)threadIdx.x + P2G_PF * T; j < cnt; j += T) {
       s_si[j] = P.perm[item.y + j];
-      const int cell = P.slot_cell[item.y + j];  // from the G2P (or re-keying) that keyed it
+      const int cell = P.slot_cell[item.y + j];
       const int r = atomicAdd(&s_cnt[cell], 1);
       s_cr[j] = ((uint32_t)cell << 16) | (uint32_t)r;
     }
@@ -1265,7 +1311,9 @@ __device__ __forceinline__ void p2g_body(const KParams& P) {
       }
       store_particle(P, Dx, slot, pt);
     }
+    nitem = nit < n_items ? P.items[nit] : make_int4(0, 0, 0, 0);  // arrives during the barrier wait
     __syncthreads();
+    p2g_item_head(P, nitem, T, nsi, ncell, nsid);  // consumed by the next item's step 1
     // 3. cell-major scatter: unit u = (cell, ox) sums the 9 nodes (ox, *, *) of the stencils of
     //    all particles of its cell in registers and adds them to the warp tile once.  A warp's
     //    32 units span fewer than 16 consecutive cells, so no two of its lanes share a node.
@@ -1358,13 +1406,17 @@ __device__ __forceinline__ void p2g_body(const KParams& P) {
       atomicAdd(reinterpret_cast<float4*>(&P.grid[node_addr(S, gx, gy, gz)]), g);
       s_touch[(tx >> 2) * 4 + (ty >> 2) * 2 + (tz >> 2)] = 1;
     }
+    // what the block flags need of the scene, read before the barrier (the next item's thread 0
+    // rewrites s_scene after it)
+    const int bres0 = S.bres[0], bres1 = S.bres[1], bres2 = S.bres[2];
+    const int64_t bbase = S.block_base;
     __syncthreads();
     if (threadIdx.x < 8 && s_touch[threadIdx.x]) {
       s_touch[threadIdx.x] = 0;
       const int bx = org[0] / BLK + (threadIdx.x >> 2), by = org[1] / BLK + ((threadIdx.x >> 1) & 1),
                 bz = org[2] / BLK + (threadIdx.x & 1);
-      if (bx < S.bres[0] && by < S.bres[1] && bz < S.bres[2]) {
-        const int64_t blk = S.block_base + ((int64_t)bx * S.bres[1] + by) * S.bres[2] + bz;
+      if (bx < bres0 && by < bres1 && bz < bres2) {
+        const int64_t blk = bbase + ((int64_t)bx * bres1 + by) * bres2 + bz;
         if (atomicExch(&P.flags[blk], 1) == 0) P.list[atomicAdd(P.nlist, 1)] = (int32_t)blk;
       }
     }
@@ -1399,6 +1451,7 @@ __device__ __forceinline__ void add_rank(const KParams& P, bool valid, int32_t k
 template <bool CPIC>
 __device__ __forceinline__ void g2p_body(const KParams& P) {
   __shared__ float4 s_v[TILE_NODES];
+  __shared__ SceneDev s_scene;  // the item's scene record (see p2g_body)
   if (P.fuse_grid) {
     // the grid op's other duty: zero the blocks the previous substep left in the other buffer
     // (the next P2G adds into it); k_perm resets that list's length after this kernel
@@ -1445,9 +1498,10 @@ __device__ __forceinline__ void g2p_body(const KParams& P) {
       }
       continue;
     }
-    const SceneDev& S = P.scenes[P.block_scene[item.x]];
+    const SceneDev& Sg = P.scenes[P.block_scene[item.x]];
+    if (threadIdx.x == 0) s_scene = Sg;  // published by the barrier after the staging
     int org[3];
-    block_origin(S, item.x, org);
+    block_origin(Sg, item.x, org);
     // positions are software-pipelined one particle ahead; the first load overlaps the staging
     float xn[3] = {0.f, 0.f, 0.f};
     if ((int)threadIdx.x < cnt) {
@@ -1457,13 +1511,14 @@ __device__ __forceinline__ void g2p_body(const KParams& P) {
     for (int t = threadIdx.x; t < TILE_NODES; t += T) {
       const int gx = org[0] + t / (TILE * TILE), gy = org[1] + (t / TILE) % TILE, gz = org[2] + t % TILE;
       float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (gx < S.res[0] && gy < S.res[1] && gz < S.res[2]) {
-        g = P.grid[node_addr(S, gx, gy, gz)];
-        if (P.fuse_grid) g = grid_velocity(S, g, gx, gy, gz);
+      if (gx < Sg.res[0] && gy < Sg.res[1] && gz < Sg.res[2]) {
+        g = P.grid[node_addr(Sg, gx, gy, gz)];
+        if (P.fuse_grid) g = grid_velocity(Sg, g, gx, gy, gz);
       }
       s_v[t] = g;
     }
     __syncthreads();
+    const SceneDev& S = s_scene;
     for (int q = threadIdx.x; q < total; q += T) {
       const bool valid = q < cnt;
       const int64_t i = item.y + q;

@@ -287,6 +287,16 @@ class MPMEntity:
         self.set_active(INACTIVE)
 
     def process_input(self, in_backward=False):
+        diff = self._solver._diff
+        if diff is not None:  # differentiable mode: the targets enter the torch state (their grads flow back)
+            if self._tgt["act"] is not None:
+                raise GenesisException("Activation changes are not supported in differentiable mode.")
+            for key in ("pos", "vel"):  # positions first: setting positions resets velocities
+                if self._tgt[key] is not None:
+                    val, envs_idx = self._tgt[key]
+                    diff.write(key, self._particle_start, self._n_particles, val, self._envs(envs_idx))
+            self._tgt = {"pos": None, "vel": None, "act": None}
+            return
         # positions first: setting positions resets velocities (particle_entity.py:448-451)
         if self._tgt["pos"] is not None:
             self.set_particles_pos(*self._tgt["pos"][:1], envs_idx=self._tgt["pos"][1])
@@ -382,10 +392,19 @@ class MPMEntity:
     def get_free(self):
         return self._get_field(_lib.FIELD_FREE, 1, None)[0, :, 0] != 0
 
+    def _diff_slice(self, k, envs_idx):
+        x = self._solver._diff.stacked()[k]
+        envs = self._envs(envs_idx)
+        return self._squeeze(x[envs, self._particle_start: self._particle_start + self._n_particles])
+
     def get_particles_pos(self, envs_idx=None):
+        if self._solver._diff is not None:
+            return self._diff_slice(0, envs_idx)
         return self._squeeze(self._get_field(_lib.FIELD_POS, 3, envs_idx))
 
     def get_particles_vel(self, envs_idx=None):
+        if self._solver._diff is not None:
+            return self._diff_slice(1, envs_idx)
         return self._squeeze(self._get_field(_lib.FIELD_VEL, 3, envs_idx))
 
     def get_particles_active(self, envs_idx=None):
@@ -398,6 +417,15 @@ class MPMEntity:
         """mpm_entity.py:278-302 / get_frame :305-352."""
         B = self._solver._B
         st = MPMEntityState(self, self._scene.sim.cur_step_global, B, self._n_particles, "cuda")
+        diff = self._solver._diff
+        if diff is not None:  # autograd-connected slices of the differentiable state
+            a, b = self._particle_start, self._particle_start + self._n_particles
+            x, v, C, F = diff.stacked()
+            st.pos, st.vel, st.C, st.F = x[:, a:b], v[:, a:b], C[:, a:b], F[:, a:b]
+            st.Jp = diff.Jp[a:b].expand(B, -1).clone()
+            st.active = torch.ones((B, self._n_particles), dtype=torch.int64, device="cuda")
+            diff.queried.append((diff.substeps_taken, st, a))
+            return st
         st.pos = self._get_field(_lib.FIELD_POS, 3, None)
         st.vel = self._get_field(_lib.FIELD_VEL, 3, None)
         st.C = self._get_field(_lib.FIELD_C, 9, None).reshape(B, -1, 3, 3)

@@ -1,0 +1,330 @@
+"""Differentiable mode of the scene API (`SimOptions(requires_grad=True)`).
+
+The reference differentiates `scene.step()` with Quadrants autodiff: states queried with
+`get_state()` are `gs.Tensor`s whose backward hook runs `Scene._backward`, which walks the
+steps in reverse (Simulator._step_grad: load_ckpt, re-simulate the step, then
+substep_post_coupling_grad / couple_grad / substep_pre_coupling_grad per substep,
+process_input_grad), scene.py:1365-1379, simulator.py:298-404, mpm_solver.py:517-670.
+
+Here the same user-facing flow (entity.set_position / set_velocity with tensors that require
+grad, scene.step(), scene.get_state() / entity.get_state(), loss.backward()) runs on torch
+autograd: the MPM state of every env is a set of torch tensors, and every scene.step() is one
+autograd node per env whose forward runs the step's substeps with the libgbmpm differentiable
+kernels (mpm_diff_forward_seq_pp) and whose backward re-simulates the step from its input state
+(the checkpoint, as the reference's save_ckpt / load_ckpt keep one per step) and runs the
+hand-written adjoint substeps in reverse (mpm_diff_backward_seq_pp).  Entity inputs set between
+steps enter the state through differentiable torch ops, so their gradients arrive where the
+reference's process_input_grad puts them.
+
+Materials: Elastic (corotated or neo-Hookean) and Liquid, any mix of entities; particle masses
+and Lame parameters per particle.  As in the reference, CPIC and emitters are rejected in this
+mode.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .exceptions import GenesisException
+
+KIND_COROTATED, KIND_NEOHOOKEAN, KIND_LIQUID = 0, 1, 2
+
+
+def material_kind(material) -> int:
+    from .materials import Elastic, Liquid
+
+    if type(material) is Elastic:
+        return KIND_NEOHOOKEAN if material.model == "neohooken" else KIND_COROTATED
+    if type(material) is Liquid:
+        return KIND_LIQUID
+    raise GenesisException(
+        f"{type(material).__name__} is not differentiable here: requires_grad=True supports Elastic and Liquid "
+        "MPM materials."
+    )
+
+
+class _StepNode(torch.autograd.Function):
+    """One scene.step() of one env: (x, v, C, F) -> state after n_sub substeps."""
+
+    @staticmethod
+    def forward(ctx, engine, n_sub, x, v, C, F):
+        st = tuple(t.detach().float().contiguous() for t in (x, v, C, F))
+        out = engine.run_forward(st, n_sub)
+        ctx.engine, ctx.n_sub = engine, n_sub
+        ctx.save_for_backward(*st)  # the step's checkpoint
+        return out
+
+    @staticmethod
+    def backward(ctx, gx, gv, gC, gF):
+        grads = ctx.engine.run_backward(ctx.saved_tensors, ctx.n_sub, (gx, gv, gC, gF))
+        return (None, None, *grads)
+
+
+class SceneDiffEngine:
+    """The differentiable MPM state of a built scene: per env (x [N,3], v [N,3], C [N,3,3], F [N,3,3])
+    torch tensors, Jp and active fixed (Elastic and Liquid do not update Jp)."""
+
+    def __init__(self, solver, B: int):
+        self.solver = solver
+        self.lib = _lib.load()
+        self.B = B
+        ents = solver.entities
+        n = solver.n_particles
+        self.n = n
+        kinds, mass, mu, lam = [], [], [], []
+        p_vol = solver.particle_volume
+        for e in ents:
+            m = e.material
+            k = material_kind(m)
+            kinds.append(np.full(e.n_particles, k, np.int32))
+            mass.append(np.full(e.n_particles, p_vol * m.rho, np.float32))
+            mu.append(np.full(e.n_particles, m.mu, np.float32))  # Liquid: 0 unless viscous (liquid.py:27-31)
+            lam.append(np.full(e.n_particles, m.lam, np.float32))
+        cat = lambda xs, dt: torch.as_tensor(np.concatenate(xs) if xs else np.zeros(0, dt), device="cuda")  # noqa: E731
+        self.kind = cat(kinds, np.int32).contiguous()
+        self.mass = cat(mass, np.float32).contiguous()
+        self.mu = cat(mu, np.float32).contiguous()
+        self.lam = cat(lam, np.float32).contiguous()
+        self.cfg = _lib.MpmSceneConfig()
+        c = self.cfg
+        c.substep_dt = solver.substep_dt
+        g = solver.gravity[0]
+        for d in range(3):
+            c.gravity[d] = float(g[d])
+            c.lower_bound[d] = float(solver.lower_bound[d])
+            c.upper_bound[d] = float(solver.upper_bound[d])
+        c.grid_density = float(solver.grid_density)
+        c.particle_size = float(solver.particle_size)
+        c.mass_eps = float(solver._eps)
+        c.restitution = 0.0
+        c.n_particles = n
+        res = solver.grid_res
+        self.nodes = int(res[0]) * int(res[1]) * int(res[2])
+        dev = "cuda"
+        self.g_grid_v = torch.zeros((self.nodes, 4), device=dev)
+        self.g_grid_pm = torch.zeros((self.nodes, 4), device=dev)
+        self.scratch = (torch.zeros((self.nodes, 4), device=dev), torch.zeros((self.nodes, 4), device=dev))
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        x0 = torch.as_tensor(np.concatenate([e.init_particles for e in ents]) if ents else np.zeros((0, 3)),
+                             dtype=torch.float32, device=dev)
+        eye = torch.eye(3, device=dev)
+        self.states = [(x0.clone(), torch.zeros((n, 3), device=dev), torch.zeros((n, 3, 3), device=dev),
+                        eye.repeat(n, 1, 1)) for _ in range(B)]
+        self.Jp = torch.cat([torch.full((e.n_particles,), float(e.material._default_Jp), device=dev) for e in ents]) \
+            if ents else torch.zeros(0, device=dev)
+        self.steps_taken = 0
+        self.substeps_taken = 0
+        self.step_inputs = []  # per step: (per-env state at the step start, substeps)
+        self.adj = None        # imperative adjoint walk (Solver protocol members)
+        self.cursor = 0
+        self._seg = None
+        self.queried = []      # (global substep, state, first row) returned by get_state, for collect_output_grads
+        self.pending = []      # entity inputs written since the last step: (field, start, count, values, envs)
+
+    # ---------------------------------------------------------------- kernels
+    @staticmethod
+    def _s():
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def run_forward(self, st, n_sub):
+        """The state after n_sub substeps from st (new tensors)."""
+        x, v, C, F = st
+        n = self.n
+        xs = torch.empty((2, n, 3), device="cuda")
+        vs = torch.empty((2, n, 3), device="cuda")
+        Cs = torch.empty((2, n, 3, 3), device="cuda")
+        Fs = torch.empty((2, n, 3, 3), device="cuda")
+        xs[0], vs[0], Cs[0], Fs[0] = x, v, C, F
+        r = self.lib.mpm_diff_forward_seq_pp(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(), n,
+                                             int(n_sub), xs.data_ptr(), vs.data_ptr(), Cs.data_ptr(), Fs.data_ptr(),
+                                             2, self.mu.data_ptr(), self.lam.data_ptr(), self.scratch[0].data_ptr(),
+                                             self.scratch[1].data_ptr(), 0, self.status.data_ptr(), self._s())
+        _lib.check(r, None, "mpm_diff_forward_seq_pp")
+        k = n_sub % 2
+        return xs[k].clone(), vs[k].clone(), Cs[k].clone(), Fs[k].clone()
+
+    def run_backward(self, st, n_sub, grads):
+        """dL/d(step input) from dL/d(step output): re-simulates the step keeping every substep's state
+        and grid, then runs the adjoint substeps in reverse."""
+        n = self.n
+        dev = "cuda"
+        ring = n_sub + 1
+        xs = torch.empty((ring, n, 3), device=dev)
+        vs = torch.empty((ring, n, 3), device=dev)
+        Cs = torch.empty((ring, n, 3, 3), device=dev)
+        Fs = torch.empty((ring, n, 3, 3), device=dev)
+        xs[0], vs[0], Cs[0], Fs[0] = st
+        gpm = torch.empty((max(1, n_sub), self.nodes, 4), device=dev)
+        gv = torch.empty((max(1, n_sub), self.nodes, 4), device=dev)
+        r = self.lib.mpm_diff_forward_seq_pp(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(), n,
+                                             int(n_sub), xs.data_ptr(), vs.data_ptr(), Cs.data_ptr(), Fs.data_ptr(),
+                                             ring, self.mu.data_ptr(), self.lam.data_ptr(), gpm.data_ptr(),
+                                             gv.data_ptr(), 1, self.status.data_ptr(), self._s())
+        _lib.check(r, None, "mpm_diff_forward_seq_pp")
+        gp = torch.zeros((2, 24 * n), device=dev)
+        for k, (g, w) in enumerate(zip(grads, (3, 3, 9, 9))):
+            if g is not None:
+                off = (0, 3, 6, 15)[k] * n
+                gp[0, off: off + w * n] = g.reshape(-1).float()
+        gmu = torch.zeros(n, device=dev)
+        glam = torch.zeros(n, device=dev)
+        r = self.lib.mpm_diff_backward_seq_pp(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(), n,
+                                              int(n_sub), xs.data_ptr(), vs.data_ptr(), Cs.data_ptr(), Fs.data_ptr(),
+                                              self.mu.data_ptr(), self.lam.data_ptr(), gp.data_ptr(),
+                                              gmu.data_ptr(), glam.data_ptr(), gpm.data_ptr(), gv.data_ptr(),
+                                              self.g_grid_v.data_ptr(), self.g_grid_pm.data_ptr(),
+                                              self.status.data_ptr(), self._s())
+        _lib.check(r, None, "mpm_diff_backward_seq_pp")
+        self.check()
+        return (gp[0, : 3 * n].view(n, 3).clone(), gp[0, 3 * n: 6 * n].view(n, 3).clone(),
+                gp[0, 6 * n: 15 * n].view(n, 3, 3).clone(), gp[0, 15 * n:].view(n, 3, 3).clone())
+
+    def check(self):
+        st = int(self.status.item())
+        if st & _lib.STATUS_NAN:
+            raise GenesisException(
+                "NaN detected in MPM states. Try reducing the time step size or adjusting simulation parameters.")
+        if st & _lib.STATUS_OOB:
+            raise GenesisException("MPM particles left the simulation grid (stencil out of bounds).")
+
+    # ---------------------------------------------------------------- scene-level operations
+    def step(self, n_sub: int) -> None:
+        # checkpoint of the step (after its inputs) and the inputs written before it
+        self.step_inputs.append((list(self.states), int(n_sub), self.pending))
+        self.pending = []
+        self.states = [_StepNode.apply(self, int(n_sub), *st) for st in self.states]
+        self.steps_taken += 1
+        self.substeps_taken += int(n_sub)
+
+    # ---------------------------------------------------------------- imperative adjoint (Solver protocol)
+    # The reference's Scene._backward drives a solver through add_grad_from_state /
+    # collect_output_grads, then per substep substep_post_coupling_grad, the coupler's couple_grad
+    # and substep_pre_coupling_grad, then process_input_grad (simulator.py:298-370).  These do the
+    # same on the adjoint held here: `adj[b]` is dL/d(state of env b at substep `cursor`).
+    def reset_grad(self) -> None:
+        dev = "cuda"
+        n = self.n
+        self.adj = [[torch.zeros((n, 3), device=dev), torch.zeros((n, 3), device=dev),
+                     torch.zeros((n, 3, 3), device=dev), torch.zeros((n, 3, 3), device=dev)] for _ in range(self.B)]
+        self.cursor = self.substeps_taken
+        self._seg = None
+        self.queried.clear()
+
+    def add_grad(self, grads_by_field, envs=None) -> None:
+        """Add dL/d(pos, vel, C, F) ([B', N', ...] with N' = count particles from `start`) to the adjoint."""
+        if self.adj is None:
+            self.reset_grad()
+        for field, (g, start) in grads_by_field.items():
+            if g is None:
+                continue
+            k = {"pos": 0, "vel": 1, "C": 2, "F": 3}[field]
+            for i, b in enumerate(range(self.B) if envs is None else envs):
+                self.adj[b][k][start: start + g.shape[1]] += g[i].to(torch.float32)
+
+    def _locate(self, f_global):
+        """(step index, substep within the step) of the substep that ends at global substep f_global."""
+        acc = 0
+        for s_i, (_, n_sub, _) in enumerate(self.step_inputs):
+            if f_global <= acc + n_sub:
+                return s_i, f_global - acc - 1
+            acc += n_sub
+        raise GenesisException("No forward substep recorded for this gradient step.")
+
+    def substep_grad(self) -> None:
+        """Adjoint of the substep that ends at `cursor` (G2P, grid op and P2G adjoints in one library call);
+        the cursor moves one substep back."""
+        if self.adj is None:
+            self.reset_grad()
+        if self.cursor <= 0:
+            raise GenesisException("The gradient walk is already at the first substep.")
+        s_i, k = self._locate(self.cursor)
+        n = self.n
+        if self._seg is None or self._seg[0] != s_i:  # re-simulate the step from its checkpoint (load_ckpt)
+            inputs, n_sub, _ = self.step_inputs[s_i]
+            keep = []
+            for b in range(self.B):
+                ring = n_sub + 1
+                seq = [torch.empty((ring, n, 3), device="cuda"), torch.empty((ring, n, 3), device="cuda"),
+                       torch.empty((ring, n, 3, 3), device="cuda"), torch.empty((ring, n, 3, 3), device="cuda")]
+                for j in range(4):
+                    seq[j][0] = inputs[b][j].detach()
+                gpm = torch.empty((n_sub, self.nodes, 4), device="cuda")
+                gv = torch.empty((n_sub, self.nodes, 4), device="cuda")
+                r = self.lib.mpm_diff_forward_seq_pp(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(),
+                                                     n, n_sub, *[t.data_ptr() for t in seq], ring, self.mu.data_ptr(),
+                                                     self.lam.data_ptr(), gpm.data_ptr(), gv.data_ptr(), 1,
+                                                     self.status.data_ptr(), self._s())
+                _lib.check(r, None, "mpm_diff_forward_seq_pp")
+                keep.append((seq, gpm, gv))
+            self._seg = (s_i, keep)
+        gmu = torch.zeros(n, device="cuda")
+        glam = torch.zeros(n, device="cuda")
+        for b in range(self.B):
+            seq, gpm, gv = self._seg[1][b]
+            gp = torch.zeros((2, 24 * n), device="cuda")
+            for j, off, w in ((0, 0, 3), (1, 3, 3), (2, 6, 9), (3, 15, 9)):
+                gp[0, off * n: (off + w) * n] = self.adj[b][j].reshape(-1)
+            one = [t[k: k + 1].contiguous() for t in seq]
+            r = self.lib.mpm_diff_backward_seq_pp(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(), n,
+                                                  1, *[t.data_ptr() for t in one], self.mu.data_ptr(),
+                                                  self.lam.data_ptr(), gp.data_ptr(), gmu.data_ptr(), glam.data_ptr(),
+                                                  gpm[k].data_ptr(), gv[k].data_ptr(), self.g_grid_v.data_ptr(),
+                                                  self.g_grid_pm.data_ptr(), self.status.data_ptr(), self._s())
+            _lib.check(r, None, "mpm_diff_backward_seq_pp")
+            self.adj[b] = [gp[0, : 3 * n].view(n, 3).clone(), gp[0, 3 * n: 6 * n].view(n, 3).clone(),
+                           gp[0, 6 * n: 15 * n].view(n, 3, 3).clone(), gp[0, 15 * n:].view(n, 3, 3).clone()]
+        self.cursor -= 1
+
+    def input_grad(self) -> None:
+        """At a step boundary (process_input_grad): the adjoint of the rows that the step's entity inputs
+        wrote goes to those inputs (through torch autograd, into the tensors the caller passed), and
+        stops there: a written row does not depend on the state before the write."""
+        if self.adj is None:
+            return
+        s_i, k = self._locate(self.cursor + 1)
+        if k != 0:
+            raise GenesisException("process_input_grad must follow the first substep of a step.")
+        for field, start, count, values, envs in reversed(self.step_inputs[s_i][2]):
+            rows = slice(start, start + count)
+            j = 0 if field == "pos" else 1
+            if values.requires_grad:
+                vb = torch.broadcast_to(values.to(device="cuda", dtype=torch.float32), (len(envs), count, 3))
+                torch.autograd.backward([vb], [torch.stack([self.adj[b][j][rows] for b in envs])])
+            for b in envs:  # set_position also reset v, C, F of those rows
+                for jj in ((0, 1, 2, 3) if field == "pos" else (1,)):
+                    self.adj[b][jj][rows] = 0.0
+
+    def write(self, field: str, start: int, count: int, values: torch.Tensor, envs) -> None:
+        """Set one entity's particles [start, start+count) of `field` (pos / vel) in envs, through
+        differentiable torch ops (values broadcast to [len(envs), count, 3])."""
+        k = {"pos": 0, "vel": 1}[field]
+        self.pending.append((field, start, count, values, list(envs)))
+        vals = torch.broadcast_to(values.to(device="cuda", dtype=torch.float32), (len(envs), count, 3))
+        for i, b in enumerate(envs):
+            st = list(self.states[b])
+            t = st[k]
+            st[k] = torch.cat([t[:start], vals[i], t[start + count:]], 0)
+            if k == 0:  # set_position resets the deformation state like _kernel_set_particles_pos
+                st[1] = torch.cat([st[1][:start], torch.zeros((count, 3), device="cuda"), st[1][start + count:]], 0)
+                C0 = torch.zeros((count, 3, 3), device="cuda")
+                F0 = torch.eye(3, device="cuda").repeat(count, 1, 1)
+                st[2] = torch.cat([st[2][:start], C0, st[2][start + count:]], 0)
+                st[3] = torch.cat([st[3][:start], F0, st[3][start + count:]], 0)
+            self.states[b] = tuple(st)
+
+    def stacked(self):
+        """[B, N, ...] views of the current state (autograd-connected)."""
+        x = torch.stack([s[0] for s in self.states])
+        v = torch.stack([s[1] for s in self.states])
+        C = torch.stack([s[2] for s in self.states])
+        F = torch.stack([s[3] for s in self.states])
+        return x, v, C, F
+
+    def set_from_state(self, state, envs) -> None:
+        for b in envs:
+            self.states[b] = tuple(getattr(state, k)[b].to(device="cuda", dtype=torch.float32)
+                                   for k in ("pos", "vel", "C", "F"))

@@ -119,10 +119,9 @@ class Scene:
                 raise GenesisException(f"Unrecognized Scene argument: {k}")
         self.sim_options = sim_options or SimOptions()
         mpm_options = mpm_options or MPMOptions()
-        if self.sim_options.requires_grad:
-            raise GenesisException(
-                "requires_grad=True: use genesis_gb300.diff.DifferentiableMPM (hand-written adjoint) for gradients."
-            )
+        if self.sim_options.requires_grad and mpm_options.enable_CPIC:
+            raise GenesisException(  # mpm_solver.py:213-216
+                "CPIC is not supported in differentiable mode yet. Submit a feature request if you need it.")
         # MPMOptions inherits dt and gravity from SimOptions (scene.py:157)
         self.mpm_options = mpm_options.model_copy_from(self.sim_options)
         self.vis_options = vis_options or VisOptions()

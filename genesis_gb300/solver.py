@@ -57,6 +57,7 @@ class MPMSolver:
         self._materials = []
         self._materials_idx = []
         self._ctx = None
+        self._diff = None  # differentiable mode (requires_grad): genesis_gb300.grad.SceneDiffEngine
         self._B = 1
         self._eps = gs.EPS
         # mpm_solver.py:36-80
@@ -171,6 +172,12 @@ class MPMSolver:
             entity._add_to_solver()
         if getattr(self, "_ffs", None):
             self._upload_force_fields()
+        if self._sim.requires_grad:  # the state lives in torch tensors advanced by the adjoint kernels
+            from .grad import SceneDiffEngine
+
+            if getattr(self, "_ffs", None):
+                raise GenesisException("Force fields are not supported in differentiable mode.")
+            self._diff = SceneDiffEngine(self, B)
 
     def _add_particles(self, particle_start, n, material_idx, active, pos_np):
         pos = torch.as_tensor(np.ascontiguousarray(pos_np, dtype=np.float32), device="cuda")
@@ -197,7 +204,11 @@ class MPMSolver:
             e.process_input(in_backward=in_backward)
 
     def substeps(self, n: int) -> None:
-        """Run n fused substeps (no host sync)."""
+        """Run n fused substeps (no host sync).  In differentiable mode the n substeps are one autograd
+        node per env (one scene.step())."""
+        if self._diff is not None:
+            self._diff.step(n)
+            return
         if self._ctx is None:
             return
         _lib.check(self._lib.mpm_substeps(self._ctx, int(n), _stream_handle()), self._ctx, "mpm_substeps")
@@ -214,6 +225,9 @@ class MPMSolver:
 
     def check_state(self) -> None:
         """Raise like mpm_solver.py:542-546 if any substep produced NaN (one host sync)."""
+        if self._diff is not None:
+            self._diff.check()
+            return
         if self._ctx is None:
             return
         st = ctypes.c_uint32()
@@ -239,6 +253,12 @@ class MPMSolver:
         if not self.is_active:
             return None
         s = MPMSolverState(self._B, self.n_particles, "cuda")
+        if self._diff is not None:  # autograd-connected tensors (a loss on them back-propagates)
+            s.pos, s.vel, s.C, s.F = self._diff.stacked()
+            s.Jp = self._diff.Jp.expand(self._B, -1).clone()
+            s.active = torch.ones((self._B, self.n_particles), dtype=torch.bool, device="cuda")
+            self._diff.queried.append((self._diff.substeps_taken, s, 0))
+            return s
         ret = self._lib.mpm_get_state(
             self._ctx, 0, self._B, _lib.ptr(s.pos), _lib.ptr(s.vel), _lib.ptr(s.C), _lib.ptr(s.F), _lib.ptr(s.Jp),
             _lib.ptr(s.active), _stream_handle()
@@ -248,6 +268,10 @@ class MPMSolver:
 
     def set_state(self, f, state, envs_idx=None) -> None:
         if not self.is_active:
+            return
+        if self._diff is not None:
+            envs = list(range(self._B)) if envs_idx is None else [int(e) for e in np.atleast_1d(envs_idx)]
+            self._diff.set_from_state(state, envs)
             return
 
         def dev(t, dtype=torch.float32):
@@ -438,19 +462,46 @@ class MPMSolver:
                 e._write(_lib.FIELD_MUSCLE_DIR, e._envs(None), torch.as_tensor(d, device="cuda").contiguous())
 
     # ------------------------------------------------------------------ differentiable-mode protocol members
-    def _no_grad_protocol(self, *args, **kwargs):
-        raise GenesisException(
-            "The MPM solver's gradients come from genesis_gb300.diff.DifferentiableMPM (hand-written adjoints "
-            "with checkpoint-and-recompute); the Solver-protocol gradient members are not available on this path."
-        )
+    # loss.backward() on states from get_state() needs none of these: every scene.step() is a torch
+    # autograd node (genesis_gb300.grad).  They replay the reference's imperative walk
+    # (Scene._backward -> Simulator._step_grad, simulator.py:298-370) for callers that drive it.
+    def _engine(self):
+        if self._diff is None:
+            raise GenesisException("Gradient members need SimOptions(requires_grad=True).")
+        return self._diff
 
-    add_grad_from_state = _no_grad_protocol
-    collect_output_grads = _no_grad_protocol
-    process_input_grad = _no_grad_protocol
-    reset_grad = _no_grad_protocol
-    reset_grad_till_frame = _no_grad_protocol
-    substep_pre_coupling_grad = _no_grad_protocol
-    substep_post_coupling_grad = _no_grad_protocol
+    def reset_grad(self):
+        """mpm_solver.py:194-199: zero the solver's adjoint; the walk starts at the current substep."""
+        self._engine().reset_grad()
+
+    def reset_grad_till_frame(self, f=None):
+        """mpm_solver.py:589-601."""
+        self._engine().reset_grad()
+
+    def add_grad_from_state(self, state):
+        """mpm_solver.py:614-670: add state.pos/vel/C/F .grad into the adjoint of the current substep."""
+        self._engine().add_grad({k: (getattr(getattr(state, k), "grad", None), 0) for k in ("pos", "vel", "C", "F")})
+
+    def collect_output_grads(self):
+        """mpm_solver.py:607-612: the gradients of states queried (get_state) at the current substep."""
+        eng = self._engine()
+        for f_q, st, start in eng.queried:
+            if f_q == eng.cursor:
+                eng.add_grad({k: (getattr(getattr(st, k), "grad", None), start) for k in ("pos", "vel", "C", "F")})
+
+    def substep_post_coupling_grad(self, f=0):
+        """g2p.grad (mpm_solver.py:548-554); the grid-op and P2G adjoints of the same substep run in the
+        same library call (mpm_diff_backward_seq_pp), so substep_pre_coupling_grad has nothing left."""
+        self._engine().substep_grad()
+
+    def substep_pre_coupling_grad(self, f=0):
+        """p2g.grad / svd_grad / compute_F_tmp.grad (mpm_solver.py:517-528): done by the preceding
+        substep_post_coupling_grad call."""
+        self._engine()
+
+    def process_input_grad(self):
+        """mpm_solver.py:499-501: the adjoint at the step start goes back to the entity inputs."""
+        self._engine().input_grad()
 
     @property
     def scene(self):

@@ -1,0 +1,176 @@
+"""Differentiable mode through the scene API (SimOptions(requires_grad=True)): entity inputs that
+require grad, scene.step(), scene.get_state() / entity.get_state(), loss.backward().
+
+* The gradient of a loss on the final centre of mass w.r.t. the initial velocity set through
+  entity.set_velocity (a scene of an Elastic and a Liquid entity, 4 steps x 10 substeps) against
+  FP64 central differences of the CPU oracle (eps = 1e-4), tolerance 2e-2 relative.
+* The input pattern of the reference's tests/test_grad.py::test_differentiable_push (two envs, a
+  position and a velocity set before the first step, a velocity input every step, a loss on the
+  solver state at step 5 and one on the entity state at step 8): inputs that reach a loss get a
+  non-zero gradient and the last step's input gets none.  The reference scene's tool entity (a
+  stirrer mesh, whose per-step velocity is the input there) is not part of this MPM path; the
+  per-step input here is the liquid entity's velocity.
+* The forward of differentiable mode equals the product path on the same scene (1e-4 m).
+"""
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+GRAD_RTOL = 2e-2
+
+
+@pytest.fixture(scope="module")
+def gs():
+    import __graft_entry__ as g
+
+    g.build()
+    import genesis_gb300 as gs
+
+    gs.init(backend=gs.gpu, seed=0)
+    return gs
+
+
+def _scene(gs, requires_grad=True, n_envs=0, box_z=0.35):
+    scene = gs.Scene(
+        sim_options=gs.options.SimOptions(dt=2e-3, substeps=10, requires_grad=requires_grad),
+        mpm_options=gs.options.MPMOptions(lower_bound=(0, 0, 0), upper_bound=(1, 1, 1), grid_density=32,
+                                          particle_size=1.0 / 64),
+    )
+    box = scene.add_entity(material=gs.materials.MPM.Elastic(E=2e5, nu=0.25, rho=800, sampler="regular"),
+                           morph=gs.morphs.Box(pos=(0.45, 0.5, box_z), size=(0.12, 0.12, 0.12)))
+    water = scene.add_entity(material=gs.materials.MPM.Liquid(E=1e5, nu=0.3, sampler="regular"),
+                             morph=gs.morphs.Box(pos=(0.6, 0.5, 0.22), size=(0.1, 0.1, 0.1)))
+    scene.build(n_envs=n_envs)
+    return scene, box, water
+
+
+def _oracle_com_loss(O, scene, ents, v_box, target, n_sub):
+    solver = scene.sim.mpm_solver
+    mats = solver._unique_materials()
+    oms = [O.from_c_material(m.to_c(0)) for m in mats]
+    pos = np.concatenate([e.init_particles.astype(np.float32).astype(np.float64) for e in ents])
+    n = len(pos)
+    vel = np.zeros((n, 3))
+    nb = ents[0].n_particles
+    vel[:nb] = v_box
+    st = dict(pos=pos, vel=vel, C=np.zeros((n, 3, 3)), F=np.tile(np.eye(3), (n, 1, 1)), Jp=np.ones(n),
+              mat=np.concatenate([np.full(e.n_particles, e.material.idx, np.int32) for e in ents]),
+              active=np.ones(n, bool))
+    sc = O.make_scene(solver.substep_dt, gravity=tuple(solver.gravity[0]), lower_bound=tuple(solver.lower_bound),
+                      upper_bound=tuple(solver.upper_bound), grid_density=solver.grid_density,
+                      particle_size=solver.particle_size)
+    out, _, _ = O.run(sc, oms, st, n_sub)
+    com = out["pos"][:nb].mean(0)
+    return float(((com - target) ** 2).sum())
+
+
+def test_grad_of_initial_velocity_matches_fp64_central_differences(gs, oracle):
+    """The box starts 1 cm above the floor boundary moving down at 1.5 m/s, so its lower layers hit
+    the boundary during the 40 substeps: the gradient goes through the contact, not only through
+    free flight."""
+    scene, box, water = _scene(gs, box_z=0.165)
+    v0 = np.array([0.4, -0.3, -1.5])
+    target = np.array([0.52, 0.47, 0.3])
+    v = torch.tensor(v0, dtype=torch.float32, device="cuda", requires_grad=True)
+    box.set_velocity(v)
+    steps = 4
+    for _ in range(steps):
+        scene.step()
+    st = box.get_state()
+    loss = ((st.pos[0].mean(0) - torch.tensor(target, dtype=torch.float32, device="cuda")) ** 2).sum()
+    loss.backward()
+    g = v.grad.detach().cpu().numpy().astype(np.float64)
+    n_sub = steps * scene.substeps
+    ref_loss = _oracle_com_loss(oracle, scene, [box, water], v0, target, n_sub)
+    assert abs(loss.item() - ref_loss) <= 1e-4 * max(ref_loss, 1e-6) + 1e-8, (loss.item(), ref_loss)
+    eps = 1e-4
+    fd = np.zeros(3)
+    for k in range(3):
+        e = np.zeros(3)
+        e[k] = eps
+        fd[k] = (_oracle_com_loss(oracle, scene, [box, water], v0 + e, target, n_sub)
+                 - _oracle_com_loss(oracle, scene, [box, water], v0 - e, target, n_sub)) / (2 * eps)
+    assert np.linalg.norm(g - fd) <= GRAD_RTOL * np.linalg.norm(fd), (g, fd)
+
+
+def test_reference_push_pattern_gradients(gs):
+    """The inputs and losses of test_differentiable_push without its tool entity."""
+    scene, box, water = _scene(gs, n_envs=2)
+    horizon = 10
+    pos_init = torch.tensor([0.45, 0.5, 0.35], device="cuda", requires_grad=True)
+    box.set_position(pos_init)
+    v_init = torch.tensor([0.0, -1.0, 0.0], device="cuda", requires_grad=True)
+    box.set_velocity(v_init)
+    goal = torch.tensor([0.5, 0.8, 0.05], device="cuda")
+    loss = 0.0
+    v_list = []
+    for i in range(horizon):
+        v_i = torch.tensor([[0.0, 1.0, 0.0], [0.0, 1.0, 0.0]], device="cuda", requires_grad=True)
+        water.set_velocity(v_i[:, None, :])
+        v_list.append(v_i)
+        scene.step()
+        if i == horizon // 2:
+            mpm = scene.get_state().solvers_state[0]
+            loss = loss + torch.pow(mpm.pos[mpm.active == 1] - goal, 2).sum()
+        if i == horizon - 2:
+            st = box.get_state()
+            loss = loss + torch.pow(st.pos - goal, 2).sum()
+    loss.backward()
+    assert pos_init.grad is not None and (pos_init.grad.abs() > 1e-6).any()
+    assert v_init.grad is not None and (v_init.grad.abs() > 1e-6).any()
+    for v_i in v_list[: horizon // 2 + 1]:  # the liquid is part of the solver-state loss at step 5
+        assert v_i.grad is not None and (v_i.grad.abs() > 1e-7).any()
+    assert v_list[-1].grad is None or (v_list[-1].grad.abs() < 1e-7).all()
+
+
+def test_differentiable_forward_equals_product_path(gs):
+    sg, box_g, _ = _scene(gs, requires_grad=True)
+    sp, box_p, _ = _scene(gs, requires_grad=False)
+    v0 = torch.tensor([0.3, 0.1, -0.4], device="cuda")
+    box_g.set_velocity(v0)
+    box_p.set_velocity(v0)
+    for _ in range(5):
+        sg.step()
+        sp.step()
+    a = sg.get_state().solvers_state[0].pos.detach()
+    b = sp.get_state().solvers_state[0].pos
+    assert (a - b).abs().max().item() <= 1e-4
+    sp.sim.mpm_solver.destroy()
+
+
+def test_solver_protocol_gradient_walk_equals_autograd(gs):
+    """The reference's imperative walk (Scene._backward: add_grad_from_state, then per step in reverse
+    substep_post_coupling_grad / substep_pre_coupling_grad per substep and process_input_grad) through
+    the solver's protocol members gives the same input gradient as loss.backward()."""
+    target = torch.tensor([0.5, 0.5, 0.3], device="cuda")
+    steps = 3
+
+    def run(imperative):
+        scene, box, water = _scene(gs, box_z=0.165)
+        v = torch.tensor([0.2, 0.1, -1.0], device="cuda", requires_grad=True)
+        box.set_velocity(v)
+        for _ in range(steps):
+            scene.step()
+        solver = scene.sim.mpm_solver
+        st = solver.get_state()
+        if not imperative:
+            ((st.pos[0].mean(0) - target) ** 2).sum().backward()
+            return v.grad.clone()
+        leaf = type(st)(1, solver.n_particles, "cuda")
+        for k in ("pos", "vel", "C", "F"):
+            setattr(leaf, k, getattr(st, k).detach().clone().requires_grad_(True))
+        ((leaf.pos[0].mean(0) - target) ** 2).sum().backward()
+        solver.reset_grad()
+        solver.add_grad_from_state(leaf)
+        for _ in range(steps):
+            for f in range(scene.substeps - 1, -1, -1):
+                solver.substep_post_coupling_grad(f)
+                solver.substep_pre_coupling_grad(f)
+            solver.process_input_grad()
+        return v.grad.clone()
+
+    a = run(False)
+    b = run(True)
+    assert torch.allclose(a, b, rtol=1e-4, atol=1e-7), (a, b)
