@@ -175,9 +175,9 @@ _SIGNATURES = {
                                        _P, _P, c_int32, _P, _P]),
     "mpm_diff_backward_seq": (c_int32, [_P, c_double, c_int32, c_int64, c_int32, _P, _P, _P, _P, _P, _P, _P,
                                         _P, _P, _P, _P, _P, _P, _P, _P]),
-    "mpm_diff_forward_seq_pp": (c_int32, [_P, _P, _P, c_int64, c_int32, _P, _P, _P, _P, c_int32, _P, _P,
+    "mpm_diff_forward_seq_pp": (c_int32, [_P, _P, _P, _P, c_int64, c_int32, _P, _P, _P, _P, _P, c_int32, _P, _P,
                                           _P, _P, c_int32, _P, _P]),
-    "mpm_diff_backward_seq_pp": (c_int32, [_P, _P, _P, c_int64, c_int32, _P, _P, _P, _P, _P, _P, _P,
+    "mpm_diff_backward_seq_pp": (c_int32, [_P, _P, _P, _P, c_int64, c_int32, _P, _P, _P, _P, _P, _P, _P, _P,
                                            _P, _P, _P, _P, _P, _P, _P, _P]),
     "mpm_set_force_fields": (c_int32, [_P, c_int32, _P]),
     "mpm_sample_regular": (c_int32, [c_int32, _P, _P, c_double, _P, c_int64, _P, _P]),

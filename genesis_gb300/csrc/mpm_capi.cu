@@ -74,6 +74,8 @@ struct mpm_ctx {
   int4* d_items = nullptr;
   int32_t* d_nitems = nullptr;
   int2* d_partials = nullptr;
+  int2* d_scan_tiles = nullptr;                // one-pass scan: bucket range of each live tile
+  int32_t* d_n_scan_tiles = nullptr;           // live tile count
   unsigned long long* d_scan_state = nullptr;  // one-pass scan: per-tile (flag, count, items) words
   int32_t* d_scan_sync = nullptr;              // one-pass scan: tile ticket, finished tiles
   uint32_t* d_status = nullptr;
@@ -222,6 +224,8 @@ KParams make_params(mpm_ctx* ctx, int src, int dst, int g) {
   P.ff_step = ctx->d_ff_step;
   P.scan_sync = ctx->d_scan_sync;
   P.n_tiles = ctx->n_tiles;
+  P.scan_tiles = ctx->d_scan_tiles;
+  P.n_scan_tiles = ctx->d_n_scan_tiles;
   P.pin = ctx->d_pin;
   P.eps_norm = ctx->eps_norm;
   P.status = ctx->d_status;
@@ -353,6 +357,32 @@ int launch_substep(mpm_ctx* ctx, int c, cudaStream_t s) {
   if (!r && !fuse) r = launch_grid(ctx, c, s);
   if (!r) r = launch_post(ctx, c, s, fuse);
   return r;
+}
+
+// The bucket ranges the one-pass scan covers, in tiles of SCAN_TILE: every bucket of a plain
+// context; in a pool only the blocks of each live slot's own grid, then the inactive and dead
+// buckets.  Synchronises the context stream (the host table must outlive the copy).
+int upload_scan_tiles(mpm_ctx* ctx) {
+  std::vector<int2> t;
+  auto add = [&](int64_t b, int64_t e) {
+    for (int64_t k = b; k < e; k += SCAN_TILE) t.push_back(make_int2((int)k, (int)(k + SCAN_TILE < e ? k + SCAN_TILE : e)));
+  };
+  if (!ctx->pool) {
+    add(0, ctx->K + 2);
+  } else {
+    for (int64_t s = 0; s < ctx->n_scenes; ++s)
+      if (ctx->slot_live[s]) {
+        const SceneDev& S = ctx->scenes_h[s];
+        add(S.block_base, S.block_base + (int64_t)S.bres[0] * S.bres[1] * S.bres[2]);
+      }
+    add(ctx->K, ctx->K + 2);
+  }
+  if ((int64_t)t.size() > ctx->n_tiles) return fail(ctx, MPM_ERR_STATE, "scan tile table overflow");
+  const int32_t nt = (int32_t)t.size();
+  CK(cudaMemcpyAsync(ctx->d_scan_tiles, t.data(), sizeof(int2) * t.size(), cudaMemcpyHostToDevice, ctx->cs));
+  CK(cudaMemcpyAsync(ctx->d_n_scan_tiles, &nt, sizeof(int32_t), cudaMemcpyHostToDevice, ctx->cs));
+  CK(cudaStreamSynchronize(ctx->cs));
+  return MPM_OK;
 }
 
 int compute_launch_shapes(mpm_ctx* ctx) {
@@ -528,7 +558,8 @@ static int ctx_alloc_init(mpm_ctx* ctx, int32_t device, const std::vector<int32_
     }
     ctx->n_sm = prop.multiProcessorCount;
     ctx->max_items = ctx->cap / 32 + ctx->K + 4;
-    ctx->n_tiles = (int)((ctx->K + 2 + SCAN_TILE - 1) / SCAN_TILE);
+    // a pool's live ranges are rounded up to whole tiles per slot: one extra tile per slot at most
+    ctx->n_tiles = (int)((ctx->K + 2 + SCAN_TILE - 1) / SCAN_TILE) + (ctx->pool ? (int)ctx->n_scenes + 1 : 0);
     if ((r = dalloc(ctx, &ctx->d_scenes, ctx->n_scenes))) break;
     if ((r = dalloc(ctx, &ctx->d_mats, ctx->n_mats > 0 ? ctx->n_mats : 1))) break;
     if ((r = dalloc(ctx, &ctx->d_block_scene, ctx->K))) break;
@@ -554,6 +585,8 @@ static int ctx_alloc_init(mpm_ctx* ctx, int32_t device, const std::vector<int32_
     if ((r = dalloc(ctx, &ctx->d_partials, ctx->n_tiles))) break;
     if ((r = dalloc(ctx, &ctx->d_scan_state, ctx->n_tiles))) break;
     if ((r = dalloc(ctx, &ctx->d_scan_sync, 2))) break;
+    if ((r = dalloc(ctx, &ctx->d_scan_tiles, ctx->n_tiles))) break;
+    if ((r = dalloc(ctx, &ctx->d_n_scan_tiles, 1))) break;
     if ((r = dalloc(ctx, &ctx->d_status, 1))) break;
     if ((r = dalloc(ctx, &ctx->d_fp64, 1))) break;
     if ((r = dalloc(ctx, &ctx->d_tmp64, 1))) break;
@@ -601,6 +634,11 @@ static int ctx_alloc_init(mpm_ctx* ctx, int32_t device, const std::vector<int32_
   CKC(cudaMemsetAsync(ctx->d_fp64, 0, sizeof(unsigned long long), ctx->cs));
   CKC(cudaMemsetAsync(ctx->d_steps, 0xff, sizeof(int32_t) * ctx->n_scenes, ctx->cs));  // -1: unlimited
   CKC(cudaMemcpyAsync(ctx->d_n, &ctx->n, sizeof(int64_t), cudaMemcpyHostToDevice, ctx->cs));
+  if (upload_scan_tiles(ctx)) {
+    fail(nullptr, MPM_ERR_CUDA, ctx->err);
+    mpm_ctx_destroy(ctx);
+    return MPM_ERR_CUDA;
+  }
   if (compute_launch_shapes(ctx)) {
     fail(nullptr, MPM_ERR_CUDA, ctx->err);
     mpm_ctx_destroy(ctx);
@@ -1630,6 +1668,7 @@ int mpm_scene_admit(mpm_ctx* ctx, int64_t slot, const mpm_scene_config* scene, c
   ctx->sorted = false;
   CK(cudaMemcpyAsync(ctx->d_n, &ctx->n, sizeof(int64_t), cudaMemcpyHostToDevice, ctx->cs));
   CK(cudaStreamSynchronize(ctx->cs));
+  if ((r = upload_scan_tiles(ctx))) return r;
   if ((r = compute_launch_shapes(ctx))) return r;
   return leave(ctx, stream);
 }
@@ -1647,12 +1686,14 @@ int mpm_scene_retire(mpm_ctx* ctx, int64_t slot, void* stream) {
   CKL();
   int32_t frozen = 0;
   CK(cudaMemcpyAsync(ctx->d_steps + slot, &frozen, sizeof(int32_t), cudaMemcpyHostToDevice, ctx->cs));
-  // dead particles sort after every live one; the next P2G drops them
+  // dead particles sort after every live one; the next P2G drops them (the slot's blocks are still
+  // in the scan while its particles are re-keyed)
   if ((r = launch_rekey(ctx, ctx->cs))) return r;
   CK(cudaStreamSynchronize(ctx->cs));
   ctx->n -= ctx->slot_n[slot];
   ctx->slot_n[slot] = 0;
   ctx->slot_live[slot] = 0;
+  if ((r = upload_scan_tiles(ctx))) return r;
   CK(cudaMemcpyAsync(ctx->d_n, &ctx->n, sizeof(int64_t), cudaMemcpyHostToDevice, ctx->cs));
   CK(cudaStreamSynchronize(ctx->cs));
   if ((r = compute_launch_shapes(ctx))) return r;

@@ -18,6 +18,7 @@
 #include <string>
 
 #include "gbmpm.h"
+#include "mpm_adjoint.cuh"
 #include "mpm_kernels.cuh"
 
 namespace gbmpm {
@@ -31,6 +32,11 @@ struct DiffParams {
   int32_t neohookean;
   const float* pmass;     // per-particle mass (mixed scenes) or null: `mass` for all
   const int32_t* pkind;   // per-particle material (DIFF_*) or null: `neohookean` for all
+  const float* aux;       // per particle [2]: Sand alpha | Snow clamp bounds (null without them)
+  const float* Jp;        // plastic state Jp [n] (null: Elastic / Liquid only, Jp unused)
+  float* Jp1;
+  const float* gJp1;      // dL/dJp of the next state (null: zero)
+  float* gJp;
   int64_t n;
   const float *x, *v, *C, *F, *mu, *lam;
   float *x1, *v1, *C1, *F1;
@@ -69,7 +75,21 @@ __device__ __forceinline__ bool make_stencil(const SceneDev& S, const float* x, 
 }
 
 // Material of the differentiable form (the `neohookean` argument of the entry points).
-constexpr int DIFF_COROTATED = 0, DIFF_NEOHOOKEAN = 1, DIFF_LIQUID = 2;
+constexpr int DIFF_COROTATED = 0, DIFF_NEOHOOKEAN = 1, DIFF_LIQUID = 2, DIFF_SAND = 3, DIFF_SNOW = 4;
+
+// Sand / Snow of one particle as the product path's material table holds them (mpm_math.cuh)
+__device__ __forceinline__ MaterialDev plastic_material(int kind, float mu, float lam, const float* aux) {
+  MaterialDev M;
+  M.type = kind == DIFF_SAND ? MT_SAND : MT_SNOW;
+  M.flags = 0;
+  M.mu = mu;
+  M.lam = lam;
+  M.alpha = kind == DIFF_SAND ? aux[0] : 0.f;
+  M.sand_coef = (3.f * lam + 2.f * mu) / (2.f * mu);
+  M.clamp_lo = aux[0];
+  M.clamp_hi = aux[1];
+  return M;
+}
 
 __device__ __forceinline__ float p_mass(const DiffParams& Q, int64_t i) { return Q.pmass ? Q.pmass[i] : Q.mass; }
 __device__ __forceinline__ int p_kind(const DiffParams& Q, int64_t i) { return Q.pkind ? Q.pkind[i] : Q.neohookean; }
@@ -135,8 +155,19 @@ __global__ void __launch_bounds__(256) k_dp2g(DiffParams Q) {
     float Ft[9], U[9], sig[3], V[9], P[9];
     f_tmp(C, F, S.dt, Ft);
     svd_f32(Ft, U, sig, V);
-    elastic_stress(Ft, Q.mu[i], Q.lam[i], kind == DIFF_NEOHOOKEAN, U, sig, V, P);
-    if (Q.F1) {
+    if (kind == DIFF_SAND || kind == DIFF_SNOW) {  // sand.py:47-84, snow.py:56-74 (the product path's code)
+      const MaterialDev M = plastic_material(kind, Q.mu[i], Q.lam[i], Q.aux + i * 2);
+      const float mdir[3] = {0.f, 0.f, 1.f};
+      float Fn[9], Jpn;
+      material_update<float>(M, Ft, U, sig, V, Q.Jp[i], 0.f, mdir, S.eps, Fn, Jpn, P);
+      if (Q.F1)
+        for (int k = 0; k < 9; ++k) Q.F1[i * 9 + k] = Fn[k];
+      if (Q.Jp1) Q.Jp1[i] = Jpn;
+    } else {
+      elastic_stress(Ft, Q.mu[i], Q.lam[i], kind == DIFF_NEOHOOKEAN, U, sig, V, P);
+      if (Q.Jp1) Q.Jp1[i] = Q.Jp[i];
+    }
+    if (Q.F1 && kind != DIFF_SAND && kind != DIFF_SNOW) {
       if (kind == DIFF_LIQUID) {  // liquid.py:36-40: F_new = J^(1/3) I
         const float j3 = powf(sig[0] * sig[1] * sig[2], 1.f / 3.f);
         for (int k = 0; k < 9; ++k) Q.F1[i * 9 + k] = (k % 4 == 0) ? j3 : 0.f;
@@ -358,15 +389,24 @@ __global__ void __launch_bounds__(256) k_dp2g_adj(DiffParams Q) {
         Q.gC[i * 9 + k] = 0.f;
         Q.gF[i * 9 + k] = Q.gF1 ? Q.gF1[i * 9 + k] : 0.f;
       }
+      if (Q.gJp) Q.gJp[i] = Q.gJp1 ? Q.gJp1[i] : 0.f;
       continue;
     }
     const float mu = Q.mu[i], lam = Q.lam[i];
     const float mass = p_mass(Q, i);
     const int kind = p_kind(Q, i);
+    const bool plastic = kind == DIFF_SAND || kind == DIFF_SNOW;
     float Ft[9], U[9], sig[3], V[9], P[9];
     f_tmp(C, F, S.dt, Ft);
     svd_f32(Ft, U, sig, V);
-    elastic_stress(Ft, mu, lam, kind == DIFF_NEOHOOKEAN, U, sig, V, P);
+    if (plastic) {
+      const MaterialDev M = plastic_material(kind, mu, lam, Q.aux + i * 2);
+      const float mdir[3] = {0.f, 0.f, 1.f};
+      float Fn[9], Jpn;
+      material_update<float>(M, Ft, U, sig, V, Q.Jp[i], 0.f, mdir, S.eps, Fn, Jpn, P);
+    } else {
+      elastic_stress(Ft, mu, lam, kind == DIFF_NEOHOOKEAN, U, sig, V, P);
+    }
     float A[9];
     for (int k = 0; k < 9; ++k) A[k] = S.stress_scale * P[k] + mass * C[k];
     float gv[3] = {0.f, 0.f, 0.f}, gA[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, gx[3];
@@ -415,8 +455,18 @@ __global__ void __launch_bounds__(256) k_dp2g_adj(DiffParams Q) {
       gFt[8] += gJ * (Ft[0] * Ft[4] - Ft[1] * Ft[3]);
     }
     const float trP = gP[0] + gP[4] + gP[8];
-    float gmu, glam;
-    if (kind == DIFF_NEOHOOKEAN) {
+    float gmu = 0.f, glam = 0.f;
+    if (plastic) {
+      // F_new = U diag(sn) V^T and P = U diag(tau) U^T of (F_tmp, Jp): mpm_adjoint.cuh
+      const float* aux = Q.aux + i * 2;
+      float gFn[9];
+      for (int k = 0; k < 9; ++k) gFn[k] = Q.gF1 ? Q.gF1[i * 9 + k] : 0.f;
+      float gJ = 0.f;
+      plastic_adjoint<float>(kind == DIFF_SAND ? MT_SAND : MT_SNOW, U, sig, V, Q.Jp[i], mu, lam, aux[0],
+                             kind == DIFF_SAND ? 0.f : aux[1], S.eps, gFn, gP, Q.gJp1 ? Q.gJp1[i] : 0.f, gFt, gJ, gmu,
+                             glam);
+      if (Q.gJp) Q.gJp[i] = gJ;
+    } else if (kind == DIFF_NEOHOOKEAN) {
       // P = mu F F^T + (lam log J - mu) I
       float FFt[9];
       mat_mul_bt(Ft, Ft, FFt);
@@ -484,6 +534,7 @@ __global__ void __launch_bounds__(256) k_dp2g_adj(DiffParams Q) {
       cof[8] = Ft[0] * Ft[4] - Ft[1] * Ft[3];
       for (int k = 0; k < 9; ++k) gFt[k] += lam * (2.f * J - 1.f) * trP * cof[k];
     }
+    if (!plastic && Q.gJp) Q.gJp[i] = Q.gJp1 ? Q.gJp1[i] : 0.f;  // Jp passes through unchanged
     // F_tmp = (I + dt C) F
     float Am[9];
     for (int k = 0; k < 9; ++k) Am[k] = ((k % 4 == 0) ? 1.f : 0.f) + S.dt * C[k];
@@ -516,9 +567,9 @@ namespace {
 
 // One forward substep; mass_pp / kind_pp (per particle) override rho / neohookean when given.
 int diff_forward(const mpm_scene_config* scene, double rho, int32_t neohookean, const float* mass_pp,
-                 const int32_t* kind_pp, int64_t n, const float* x, const float* v, const float* C, const float* F,
-                 const float* mu, const float* lam, float* x1, float* v1, float* C1, float* F1, void* grid_pm,
-                 void* grid_v, uint32_t* status, void* stream) {
+                 const int32_t* kind_pp, const float* aux, int64_t n, const float* x, const float* v, const float* C,
+                 const float* F, const float* Jp, const float* mu, const float* lam, float* x1, float* v1, float* C1,
+                 float* F1, float* Jp1, void* grid_pm, void* grid_v, uint32_t* status, void* stream) {
   if (!scene || n < 0 || !grid_pm || !grid_v || !status) return MPM_ERR_BAD_ARG;
   DiffParams Q;
   std::memset(&Q, 0, sizeof(Q));
@@ -529,9 +580,11 @@ int diff_forward(const mpm_scene_config* scene, double rho, int32_t neohookean, 
   Q.neohookean = neohookean;
   Q.pmass = mass_pp;
   Q.pkind = kind_pp;
+  Q.aux = aux;
   Q.n = n;
   Q.x = x, Q.v = v, Q.C = C, Q.F = F, Q.mu = mu, Q.lam = lam;
   Q.x1 = x1, Q.v1 = v1, Q.C1 = C1, Q.F1 = F1;
+  Q.Jp = Jp, Q.Jp1 = Jp1;
   Q.pm = (float4*)grid_pm;
   Q.gvel = (float4*)grid_v;
   Q.status = status;
@@ -547,10 +600,11 @@ int diff_forward(const mpm_scene_config* scene, double rho, int32_t neohookean, 
 }
 
 int diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean, const float* mass_pp,
-                  const int32_t* kind_pp, int64_t n, const float* x, const float* v, const float* C, const float* F,
-                  const float* mu, const float* lam, const float* gx1, const float* gv1, const float* gC1,
-                  const float* gF1, float* gx, float* gv, float* gC, float* gF, float* gmu, float* glam, void* grid_pm,
-                  void* grid_v, void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream) {
+                  const int32_t* kind_pp, const float* aux, int64_t n, const float* x, const float* v, const float* C,
+                  const float* F, const float* Jp, const float* mu, const float* lam, const float* gx1,
+                  const float* gv1, const float* gC1, const float* gF1, const float* gJp1, float* gx, float* gv,
+                  float* gC, float* gF, float* gJp, float* gmu, float* glam, void* grid_pm, void* grid_v,
+                  void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream) {
   if (!scene || n < 0 || !grid_pm || !grid_v || !g_grid_v || !g_grid_pm) return MPM_ERR_BAD_ARG;
   DiffParams Q;
   std::memset(&Q, 0, sizeof(Q));
@@ -561,10 +615,12 @@ int diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean,
   Q.neohookean = neohookean;
   Q.pmass = mass_pp;
   Q.pkind = kind_pp;
+  Q.aux = aux;
   Q.n = n;
   Q.x = x, Q.v = v, Q.C = C, Q.F = F, Q.mu = mu, Q.lam = lam;
-  Q.gx1 = gx1, Q.gv1 = gv1, Q.gC1 = gC1, Q.gF1 = gF1;
-  Q.gx = gx, Q.gv = gv, Q.gC = gC, Q.gF = gF, Q.gmu = gmu, Q.glam = glam;
+  Q.Jp = Jp;
+  Q.gx1 = gx1, Q.gv1 = gv1, Q.gC1 = gC1, Q.gF1 = gF1, Q.gJp1 = gJp1;
+  Q.gx = gx, Q.gv = gv, Q.gC = gC, Q.gF = gF, Q.gJp = gJp, Q.gmu = gmu, Q.glam = glam;
   Q.pm = (float4*)grid_pm;
   Q.gvel = (float4*)grid_v;
   Q.g_grid_v = (float4*)g_grid_v;
@@ -582,9 +638,9 @@ int diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean,
 }
 
 int diff_forward_seq(const mpm_scene_config* scene, double rho, int32_t neohookean, const float* mass_pp,
-                     const int32_t* kind_pp, int64_t n, int32_t n_sub, float* x_seq, float* v_seq, float* C_seq,
-                     float* F_seq, int32_t ring, const float* mu, const float* lam, void* grid_pm, void* grid_v,
-                     int32_t grids_per_substep, uint32_t* status, void* stream) {
+                     const int32_t* kind_pp, const float* aux, int64_t n, int32_t n_sub, float* x_seq, float* v_seq,
+                     float* C_seq, float* F_seq, float* Jp_seq, int32_t ring, const float* mu, const float* lam,
+                     void* grid_pm, void* grid_v, int32_t grids_per_substep, uint32_t* status, void* stream) {
   if (!scene || n < 0 || n_sub < 0 || ring < 2 || !x_seq || !v_seq || !C_seq || !F_seq) return MPM_ERR_BAD_ARG;
   SceneDev S;
   std::string err;
@@ -593,35 +649,38 @@ int diff_forward_seq(const mpm_scene_config* scene, double rho, int32_t neohooke
   for (int32_t k = 0; k < n_sub; ++k) {
     const int64_t a = k % ring, b = (k + 1) % ring;
     const int64_t go = grids_per_substep ? (int64_t)k * nodes : 0;
-    const int r = diff_forward(scene, rho, neohookean, mass_pp, kind_pp, n, x_seq + a * n * 3, v_seq + a * n * 3,
-                               C_seq + a * n * 9, F_seq + a * n * 9, mu, lam, x_seq + b * n * 3, v_seq + b * n * 3,
-                               C_seq + b * n * 9, F_seq + b * n * 9, (float4*)grid_pm + go, (float4*)grid_v + go, status,
+    const int r = diff_forward(scene, rho, neohookean, mass_pp, kind_pp, aux, n, x_seq + a * n * 3,
+                               v_seq + a * n * 3, C_seq + a * n * 9, F_seq + a * n * 9, Jp_seq ? Jp_seq + a * n : nullptr,
+                               mu, lam, x_seq + b * n * 3, v_seq + b * n * 3, C_seq + b * n * 9, F_seq + b * n * 9,
+                               Jp_seq ? Jp_seq + b * n : nullptr, (float4*)grid_pm + go, (float4*)grid_v + go, status,
                                stream);
     if (r) return r;
   }
   return MPM_OK;
 }
 
+// g_seq packs (dx, dv, dC, dF) per buffer (24 n floats), followed by dJp (n) when Jp_seq is given.
 int diff_backward_seq(const mpm_scene_config* scene, double rho, int32_t neohookean, const float* mass_pp,
-                      const int32_t* kind_pp, int64_t n, int32_t n_sub, const float* x_seq, const float* v_seq,
-                      const float* C_seq, const float* F_seq, const float* mu, const float* lam, float* g_seq,
-                      float* gmu, float* glam, void* grid_pm, void* grid_v, void* g_grid_v, void* g_grid_pm,
-                      uint32_t* status, void* stream) {
+                      const int32_t* kind_pp, const float* aux, int64_t n, int32_t n_sub, const float* x_seq,
+                      const float* v_seq, const float* C_seq, const float* F_seq, const float* Jp_seq, const float* mu,
+                      const float* lam, float* g_seq, float* gmu, float* glam, void* grid_pm, void* grid_v,
+                      void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream) {
   if (!scene || n < 0 || n_sub < 0 || !g_seq) return MPM_ERR_BAD_ARG;
   SceneDev S;
   std::string err;
   if (derive_scene(*scene, S, err)) return MPM_ERR_BAD_ARG;
   const int64_t nodes = (int64_t)S.res[0] * S.res[1] * S.res[2];
-  const int64_t gs = 24 * n;
+  const int64_t gs = (Jp_seq ? 25 : 24) * n;
   int cur = 0;
   for (int32_t k = n_sub - 1; k >= 0; --k) {
     float* gi = g_seq + cur * gs;
     float* go = g_seq + (1 - cur) * gs;
-    const int r = diff_backward(scene, rho, neohookean, mass_pp, kind_pp, n, x_seq + (int64_t)k * n * 3,
-                                v_seq + (int64_t)k * n * 3, C_seq + (int64_t)k * n * 9, F_seq + (int64_t)k * n * 9, mu,
-                                lam, gi, gi + 3 * n, gi + 6 * n, gi + 15 * n, go, go + 3 * n, go + 6 * n, go + 15 * n,
-                                gmu, glam, (float4*)grid_pm + (int64_t)k * nodes, (float4*)grid_v + (int64_t)k * nodes,
-                                g_grid_v, g_grid_pm, status, stream);
+    const int r = diff_backward(scene, rho, neohookean, mass_pp, kind_pp, aux, n, x_seq + (int64_t)k * n * 3,
+                                v_seq + (int64_t)k * n * 3, C_seq + (int64_t)k * n * 9, F_seq + (int64_t)k * n * 9,
+                                Jp_seq ? Jp_seq + (int64_t)k * n : nullptr, mu, lam, gi, gi + 3 * n, gi + 6 * n,
+                                gi + 15 * n, Jp_seq ? gi + 24 * n : nullptr, go, go + 3 * n, go + 6 * n, go + 15 * n,
+                                Jp_seq ? go + 24 * n : nullptr, gmu, glam, (float4*)grid_pm + (int64_t)k * nodes,
+                                (float4*)grid_v + (int64_t)k * nodes, g_grid_v, g_grid_pm, status, stream);
     if (r) return r;
     cur = 1 - cur;
   }
@@ -642,8 +701,8 @@ extern "C" {
 int mpm_diff_forward(const mpm_scene_config* scene, double rho, int32_t neohookean, int64_t n, const float* x,
                      const float* v, const float* C, const float* F, const float* mu, const float* lam, float* x1,
                      float* v1, float* C1, float* F1, void* grid_pm, void* grid_v, uint32_t* status, void* stream) {
-  return diff_forward(scene, rho, neohookean, nullptr, nullptr, n, x, v, C, F, mu, lam, x1, v1, C1, F1, grid_pm,
-                      grid_v, status, stream);
+  return diff_forward(scene, rho, neohookean, nullptr, nullptr, nullptr, n, x, v, C, F, nullptr, mu, lam, x1, v1, C1,
+                      F1, nullptr, grid_pm, grid_v, status, stream);
 }
 
 // Adjoint of mpm_diff_forward at state (x, v, C, F): given dL/d(x1, v1, C1, F1) (gF1 may be
@@ -655,8 +714,9 @@ int mpm_diff_backward(const mpm_scene_config* scene, double rho, int32_t neohook
                       const float* gx1, const float* gv1, const float* gC1, const float* gF1, float* gx, float* gv,
                       float* gC, float* gF, float* gmu, float* glam, void* grid_pm, void* grid_v, void* g_grid_v,
                       void* g_grid_pm, uint32_t* status, void* stream) {
-  return diff_backward(scene, rho, neohookean, nullptr, nullptr, n, x, v, C, F, mu, lam, gx1, gv1, gC1, gF1, gx, gv,
-                       gC, gF, gmu, glam, grid_pm, grid_v, g_grid_v, g_grid_pm, status, stream);
+  return diff_backward(scene, rho, neohookean, nullptr, nullptr, nullptr, n, x, v, C, F, nullptr, mu, lam, gx1, gv1,
+                       gC1, gF1, nullptr, gx, gv, gC, gF, nullptr, gmu, glam, grid_pm, grid_v, g_grid_v, g_grid_pm,
+                       status, stream);
 }
 
 // n_sub forward substeps in one call (no host round trip per substep).  State k (k = 0..n_sub)
@@ -668,8 +728,8 @@ int mpm_diff_forward_seq(const mpm_scene_config* scene, double rho, int32_t neoh
                          float* x_seq, float* v_seq, float* C_seq, float* F_seq, int32_t ring, const float* mu,
                          const float* lam, void* grid_pm, void* grid_v, int32_t grids_per_substep, uint32_t* status,
                          void* stream) {
-  return diff_forward_seq(scene, rho, neohookean, nullptr, nullptr, n, n_sub, x_seq, v_seq, C_seq, F_seq, ring, mu,
-                          lam, grid_pm, grid_v, grids_per_substep, status, stream);
+  return diff_forward_seq(scene, rho, neohookean, nullptr, nullptr, nullptr, n, n_sub, x_seq, v_seq, C_seq, F_seq,
+                          nullptr, ring, mu, lam, grid_pm, grid_v, grids_per_substep, status, stream);
 }
 
 // Adjoint of n_sub substeps whose states 0..n_sub-1 and grids were kept by mpm_diff_forward_seq
@@ -680,31 +740,33 @@ int mpm_diff_backward_seq(const mpm_scene_config* scene, double rho, int32_t neo
                           const float* x_seq, const float* v_seq, const float* C_seq, const float* F_seq,
                           const float* mu, const float* lam, float* g_seq, float* gmu, float* glam, void* grid_pm,
                           void* grid_v, void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream) {
-  return diff_backward_seq(scene, rho, neohookean, nullptr, nullptr, n, n_sub, x_seq, v_seq, C_seq, F_seq, mu, lam,
-                           g_seq, gmu, glam, grid_pm, grid_v, g_grid_v, g_grid_pm, status, stream);
+  return diff_backward_seq(scene, rho, neohookean, nullptr, nullptr, nullptr, n, n_sub, x_seq, v_seq, C_seq, F_seq,
+                           nullptr, mu, lam, g_seq, gmu, glam, grid_pm, grid_v, g_grid_v, g_grid_pm, status, stream);
 }
 
 // mpm_diff_forward_seq / mpm_diff_backward_seq for a scene of several entities: the particle
-// mass [n] and material kind [n] (0 corotated Elastic, 1 neo-Hookean Elastic, 2 Liquid) are given
+// mass [n], material kind [n] (0 corotated Elastic, 1 neo-Hookean Elastic, 2 Liquid, 3 Sand, 4 Snow)
+// and aux [n, 2] (Sand: friction alpha; Snow: clamp bounds 1 - yield_lower, 1 + yield_higher) are given
 // per particle, as the reference's differentiable MPM path reads them per particle through
-// particles_info and the material dispatch (mpm_solver.py:341-375).
-int mpm_diff_forward_seq_pp(const mpm_scene_config* scene, const float* mass, const int32_t* kind, int64_t n,
-                            int32_t n_sub, float* x_seq, float* v_seq, float* C_seq, float* F_seq, int32_t ring,
-                            const float* mu, const float* lam, void* grid_pm, void* grid_v, int32_t grids_per_substep,
-                            uint32_t* status, void* stream) {
-  if (n > 0 && (!mass || !kind)) return MPM_ERR_BAD_ARG;
-  return diff_forward_seq(scene, 0.0, 0, mass, kind, n, n_sub, x_seq, v_seq, C_seq, F_seq, ring, mu, lam, grid_pm,
-                          grid_v, grids_per_substep, status, stream);
+// particles_info and the material dispatch (mpm_solver.py:341-375); the state includes Jp
+// (Jp_seq [ring, n]) and g_seq packs dJp after (dx, dv, dC, dF): [2, 25 n].
+int mpm_diff_forward_seq_pp(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
+                            int64_t n, int32_t n_sub, float* x_seq, float* v_seq, float* C_seq, float* F_seq,
+                            float* Jp_seq, int32_t ring, const float* mu, const float* lam, void* grid_pm, void* grid_v,
+                            int32_t grids_per_substep, uint32_t* status, void* stream) {
+  if (n > 0 && (!mass || !kind || !aux || !Jp_seq)) return MPM_ERR_BAD_ARG;
+  return diff_forward_seq(scene, 0.0, 0, mass, kind, aux, n, n_sub, x_seq, v_seq, C_seq, F_seq, Jp_seq, ring, mu, lam,
+                          grid_pm, grid_v, grids_per_substep, status, stream);
 }
 
-int mpm_diff_backward_seq_pp(const mpm_scene_config* scene, const float* mass, const int32_t* kind, int64_t n,
-                             int32_t n_sub, const float* x_seq, const float* v_seq, const float* C_seq,
-                             const float* F_seq, const float* mu, const float* lam, float* g_seq, float* gmu,
-                             float* glam, void* grid_pm, void* grid_v, void* g_grid_v, void* g_grid_pm,
+int mpm_diff_backward_seq_pp(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
+                             int64_t n, int32_t n_sub, const float* x_seq, const float* v_seq, const float* C_seq,
+                             const float* F_seq, const float* Jp_seq, const float* mu, const float* lam, float* g_seq,
+                             float* gmu, float* glam, void* grid_pm, void* grid_v, void* g_grid_v, void* g_grid_pm,
                              uint32_t* status, void* stream) {
-  if (n > 0 && (!mass || !kind)) return MPM_ERR_BAD_ARG;
-  return diff_backward_seq(scene, 0.0, 0, mass, kind, n, n_sub, x_seq, v_seq, C_seq, F_seq, mu, lam, g_seq, gmu, glam,
-                           grid_pm, grid_v, g_grid_v, g_grid_pm, status, stream);
+  if (n > 0 && (!mass || !kind || !aux || !Jp_seq)) return MPM_ERR_BAD_ARG;
+  return diff_backward_seq(scene, 0.0, 0, mass, kind, aux, n, n_sub, x_seq, v_seq, C_seq, F_seq, Jp_seq, mu, lam,
+                           g_seq, gmu, glam, grid_pm, grid_v, g_grid_v, g_grid_pm, status, stream);
 }
 
 }  // extern "C"

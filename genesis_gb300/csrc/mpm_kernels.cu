@@ -395,11 +395,17 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_onepass(KParams P) {
   constexpr int PER = SCAN_TILE / SCAN_THREADS;
   __shared__ int s_tile, s_last;
   __shared__ int2 s_prefix;
+  // Only the live tiles take part (a pool's empty slots and the unused blocks of small grids hold
+  // no particle, so their buckets are skipped; the captured launch keeps its full CTA count and the
+  // extra CTAs return here, before any ticket).
+  const int n_live = *P.n_scan_tiles;
+  if ((int)blockIdx.x >= n_live) return;
   if (threadIdx.x == 0) s_tile = atomicAdd(&P.scan_sync[0], 1);
   __syncthreads();
   const int tile = s_tile;
-  const int64_t nb = P.K + 2;
-  const int64_t k0 = (int64_t)tile * SCAN_TILE + (int64_t)threadIdx.x * PER;
+  const int2 range = P.scan_tiles[tile];
+  const int64_t nb = range.y;
+  const int64_t k0 = (int64_t)range.x + (int64_t)threadIdx.x * PER;
   int c[PER];
   int cs = 0, is = 0;
 #pragma unroll
@@ -468,14 +474,14 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_onepass(KParams P) {
     off += c[j];
     P.count[k] = 0;
   }
-  if (tile == P.n_tiles - 1 && threadIdx.x == 0) *P.n_items = base.y + total.y;
+  if (tile == n_live - 1 && threadIdx.x == 0) *P.n_items = base.y + total.y;
   if (threadIdx.x == 0) {
     __threadfence();
-    s_last = atomicAdd(&P.scan_sync[1], 1) == P.n_tiles - 1;
+    s_last = atomicAdd(&P.scan_sync[1], 1) == n_live - 1;
   }
   __syncthreads();
   if (s_last) {  // every CTA is past its look-back: reset for the next scan
-    for (int t = threadIdx.x; t < P.n_tiles; t += blockDim.x) P.scan_state[t] = 0ull;
+    for (int t = threadIdx.x; t < n_live; t += blockDim.x) P.scan_state[t] = 0ull;
     if (threadIdx.x == 0) {
       P.scan_sync[0] = 0;
       P.scan_sync[1] = 0;

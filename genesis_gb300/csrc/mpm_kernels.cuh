@@ -150,7 +150,9 @@ struct KParams {
   int2* partials;              // scan tile partials
   unsigned long long* scan_state;  // one-pass scan: per tile, flag (2 bits) | count (31) | items (31)
   int32_t* scan_sync;          // one-pass scan: [0] tile ticket, [1] finished tiles
-  int32_t n_tiles;
+  int32_t n_tiles;             // one-pass scan CTAs launched (at least the live tiles)
+  const int2* scan_tiles;      // one-pass scan: bucket range [x, y) of each live tile, in bucket order
+  const int32_t* n_scan_tiles; // live tiles (device; the launch's extra CTAs return at once)
   int32_t scan_hold_tile0;     // failure-detection test only: tile 0 never publishes
   uint32_t scan_spin_limit;    // look-back wait limit (0: the default)
   uint32_t* pin;               // per-node bitmap of nodes touched by non-free particles (or null)

@@ -420,9 +420,8 @@ class MPMEntity:
         diff = self._solver._diff
         if diff is not None:  # autograd-connected slices of the differentiable state
             a, b = self._particle_start, self._particle_start + self._n_particles
-            x, v, C, F = diff.stacked()
-            st.pos, st.vel, st.C, st.F = x[:, a:b], v[:, a:b], C[:, a:b], F[:, a:b]
-            st.Jp = diff.Jp[a:b].expand(B, -1).clone()
+            x, v, C, F, Jp = diff.stacked()
+            st.pos, st.vel, st.C, st.F, st.Jp = x[:, a:b], v[:, a:b], C[:, a:b], F[:, a:b], Jp[:, a:b]
             st.active = torch.ones((B, self._n_particles), dtype=torch.int64, device="cuda")
             diff.queried.append((diff.substeps_taken, st, a))
             return st

@@ -16,9 +16,9 @@ hand-written adjoint substeps in reverse (mpm_diff_backward_seq_pp).  Entity inp
 steps enter the state through differentiable torch ops, so their gradients arrive where the
 reference's process_input_grad puts them.
 
-Materials: Elastic (corotated or neo-Hookean) and Liquid, any mix of entities; particle masses
-and Lame parameters per particle.  As in the reference, CPIC and emitters are rejected in this
-mode.
+Materials: Elastic (corotated or neo-Hookean), Liquid, Sand and Snow, any mix of entities;
+particle masses, Lame parameters and plasticity constants per particle, Jp part of the
+differentiated state.  As in the reference, CPIC and emitters are rejected in this mode.
 """
 
 from __future__ import annotations
@@ -31,42 +31,50 @@ import torch
 from . import _lib
 from .exceptions import GenesisException
 
-KIND_COROTATED, KIND_NEOHOOKEAN, KIND_LIQUID = 0, 1, 2
+KIND_COROTATED, KIND_NEOHOOKEAN, KIND_LIQUID, KIND_SAND, KIND_SNOW = 0, 1, 2, 3, 4
+FIELDS = ("pos", "vel", "C", "F", "Jp")
+_WIDTH = (3, 3, 9, 9, 1)       # floats per particle of each state field
+_OFFSET = (0, 3, 6, 15, 24)    # offsets (in units of n) in the packed gradient buffer of 25 n floats
 
 
-def material_kind(material) -> int:
-    from .materials import Elastic, Liquid
+def material_kind(material) -> tuple[int, float, float]:
+    """(kind, aux0, aux1) of a material in differentiable mode."""
+    from .materials import Elastic, Liquid, Sand, Snow
 
     if type(material) is Elastic:
-        return KIND_NEOHOOKEAN if material.model == "neohooken" else KIND_COROTATED
+        return (KIND_NEOHOOKEAN if material.model == "neohooken" else KIND_COROTATED), 0.0, 0.0
     if type(material) is Liquid:
-        return KIND_LIQUID
+        return KIND_LIQUID, 0.0, 0.0
+    if type(material) is Sand:
+        return KIND_SAND, float(material.alpha), 0.0
+    if type(material) is Snow:
+        return KIND_SNOW, 1.0 - float(material.yield_lower), 1.0 + float(material.yield_higher)
     raise GenesisException(
-        f"{type(material).__name__} is not differentiable here: requires_grad=True supports Elastic and Liquid "
-        "MPM materials."
+        f"{type(material).__name__} is not differentiable here: requires_grad=True supports Elastic, Liquid, Sand "
+        "and Snow MPM materials."
     )
 
 
 class _StepNode(torch.autograd.Function):
-    """One scene.step() of one env: (x, v, C, F) -> state after n_sub substeps."""
+    """One scene.step() of one env: (x, v, C, F, Jp) -> state after n_sub substeps."""
 
     @staticmethod
-    def forward(ctx, engine, n_sub, x, v, C, F):
-        st = tuple(t.detach().float().contiguous() for t in (x, v, C, F))
+    def forward(ctx, engine, n_sub, x, v, C, F, Jp):
+        st = tuple(t.detach().float().contiguous() for t in (x, v, C, F, Jp))
         out = engine.run_forward(st, n_sub)
         ctx.engine, ctx.n_sub = engine, n_sub
         ctx.save_for_backward(*st)  # the step's checkpoint
         return out
 
     @staticmethod
-    def backward(ctx, gx, gv, gC, gF):
-        grads = ctx.engine.run_backward(ctx.saved_tensors, ctx.n_sub, (gx, gv, gC, gF))
+    def backward(ctx, gx, gv, gC, gF, gJp):
+        grads = ctx.engine.run_backward(ctx.saved_tensors, ctx.n_sub, (gx, gv, gC, gF, gJp))
         return (None, None, *grads)
 
 
 class SceneDiffEngine:
-    """The differentiable MPM state of a built scene: per env (x [N,3], v [N,3], C [N,3,3], F [N,3,3])
-    torch tensors, Jp and active fixed (Elastic and Liquid do not update Jp)."""
+    """The differentiable MPM state of a built scene: per env (x [N,3], v [N,3], C [N,3,3], F [N,3,3],
+    Jp [N]) torch tensors; every particle active."""
 
     def __init__(self, solver, B: int):
         self.solver = solver
@@ -75,12 +83,13 @@ class SceneDiffEngine:
         ents = solver.entities
         n = solver.n_particles
         self.n = n
-        kinds, mass, mu, lam = [], [], [], []
+        kinds, mass, mu, lam, aux = [], [], [], [], []
         p_vol = solver.particle_volume
         for e in ents:
             m = e.material
-            k = material_kind(m)
+            k, a0, a1 = material_kind(m)
             kinds.append(np.full(e.n_particles, k, np.int32))
+            aux.append(np.tile(np.array([a0, a1], np.float32), (e.n_particles, 1)))
             mass.append(np.full(e.n_particles, p_vol * m.rho, np.float32))
             mu.append(np.full(e.n_particles, m.mu, np.float32))  # Liquid: 0 unless viscous (liquid.py:27-31)
             lam.append(np.full(e.n_particles, m.lam, np.float32))
@@ -89,6 +98,8 @@ class SceneDiffEngine:
         self.mass = cat(mass, np.float32).contiguous()
         self.mu = cat(mu, np.float32).contiguous()
         self.lam = cat(lam, np.float32).contiguous()
+        self.aux = torch.as_tensor(np.concatenate(aux) if aux else np.zeros((0, 2), np.float32),
+                                   device="cuda").contiguous()
         self.cfg = _lib.MpmSceneConfig()
         c = self.cfg
         c.substep_dt = solver.substep_dt
@@ -112,10 +123,10 @@ class SceneDiffEngine:
         x0 = torch.as_tensor(np.concatenate([e.init_particles for e in ents]) if ents else np.zeros((0, 3)),
                              dtype=torch.float32, device=dev)
         eye = torch.eye(3, device=dev)
-        self.states = [(x0.clone(), torch.zeros((n, 3), device=dev), torch.zeros((n, 3, 3), device=dev),
-                        eye.repeat(n, 1, 1)) for _ in range(B)]
-        self.Jp = torch.cat([torch.full((e.n_particles,), float(e.material._default_Jp), device=dev) for e in ents]) \
+        self.Jp0 = torch.cat([torch.full((e.n_particles,), float(e.material._default_Jp), device=dev) for e in ents]) \
             if ents else torch.zeros(0, device=dev)
+        self.states = [(x0.clone(), torch.zeros((n, 3), device=dev), torch.zeros((n, 3, 3), device=dev),
+                        eye.repeat(n, 1, 1), self.Jp0.clone()) for _ in range(B)]
         self.steps_taken = 0
         self.substeps_taken = 0
         self.step_inputs = []  # per step: (per-env state at the step start, substeps)
@@ -130,58 +141,66 @@ class SceneDiffEngine:
     def _s():
         return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
+    def _seq(self, ring, first=None):
+        n = self.n
+        seq = [torch.empty((ring, n, 3), device="cuda"), torch.empty((ring, n, 3), device="cuda"),
+               torch.empty((ring, n, 3, 3), device="cuda"), torch.empty((ring, n, 3, 3), device="cuda"),
+               torch.empty((ring, n), device="cuda")]
+        if first is not None:
+            for t, f in zip(seq, first):
+                t[0] = f.detach()
+        return seq
+
+    def _forward_seq(self, seq, n_sub, ring, gpm, gv, keep_grids):
+        r = self.lib.mpm_diff_forward_seq_pp(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(),
+                                             self.aux.data_ptr(), self.n, int(n_sub), *[t.data_ptr() for t in seq],
+                                             ring, self.mu.data_ptr(), self.lam.data_ptr(), gpm.data_ptr(),
+                                             gv.data_ptr(), int(keep_grids), self.status.data_ptr(), self._s())
+        _lib.check(r, None, "mpm_diff_forward_seq_pp")
+
+    def _backward_seq(self, seq, n_sub, gp, gpm, gv):
+        n = self.n
+        gmu = torch.zeros(n, device="cuda")
+        glam = torch.zeros(n, device="cuda")
+        r = self.lib.mpm_diff_backward_seq_pp(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(),
+                                              self.aux.data_ptr(), n, int(n_sub), *[t.data_ptr() for t in seq],
+                                              self.mu.data_ptr(), self.lam.data_ptr(), gp.data_ptr(), gmu.data_ptr(),
+                                              glam.data_ptr(), gpm.data_ptr(), gv.data_ptr(),
+                                              self.g_grid_v.data_ptr(), self.g_grid_pm.data_ptr(),
+                                              self.status.data_ptr(), self._s())
+        _lib.check(r, None, "mpm_diff_backward_seq_pp")
+
+    def _pack(self, grads):
+        n = self.n
+        gp = torch.zeros((2, 25 * n), device="cuda")
+        for k, g in enumerate(grads):
+            if g is not None:
+                gp[0, _OFFSET[k] * n: (_OFFSET[k] + _WIDTH[k]) * n] = g.reshape(-1).float()
+        return gp
+
+    def _unpack(self, gp):
+        n = self.n
+        shapes = ((n, 3), (n, 3), (n, 3, 3), (n, 3, 3), (n,))
+        return [gp[0, _OFFSET[k] * n: (_OFFSET[k] + _WIDTH[k]) * n].view(shapes[k]).clone() for k in range(5)]
+
     def run_forward(self, st, n_sub):
         """The state after n_sub substeps from st (new tensors)."""
-        x, v, C, F = st
-        n = self.n
-        xs = torch.empty((2, n, 3), device="cuda")
-        vs = torch.empty((2, n, 3), device="cuda")
-        Cs = torch.empty((2, n, 3, 3), device="cuda")
-        Fs = torch.empty((2, n, 3, 3), device="cuda")
-        xs[0], vs[0], Cs[0], Fs[0] = x, v, C, F
-        r = self.lib.mpm_diff_forward_seq_pp(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(), n,
-                                             int(n_sub), xs.data_ptr(), vs.data_ptr(), Cs.data_ptr(), Fs.data_ptr(),
-                                             2, self.mu.data_ptr(), self.lam.data_ptr(), self.scratch[0].data_ptr(),
-                                             self.scratch[1].data_ptr(), 0, self.status.data_ptr(), self._s())
-        _lib.check(r, None, "mpm_diff_forward_seq_pp")
+        seq = self._seq(2, st)
+        self._forward_seq(seq, n_sub, 2, self.scratch[0], self.scratch[1], False)
         k = n_sub % 2
-        return xs[k].clone(), vs[k].clone(), Cs[k].clone(), Fs[k].clone()
+        return tuple(t[k].clone() for t in seq)
 
     def run_backward(self, st, n_sub, grads):
         """dL/d(step input) from dL/d(step output): re-simulates the step keeping every substep's state
         and grid, then runs the adjoint substeps in reverse."""
-        n = self.n
-        dev = "cuda"
-        ring = n_sub + 1
-        xs = torch.empty((ring, n, 3), device=dev)
-        vs = torch.empty((ring, n, 3), device=dev)
-        Cs = torch.empty((ring, n, 3, 3), device=dev)
-        Fs = torch.empty((ring, n, 3, 3), device=dev)
-        xs[0], vs[0], Cs[0], Fs[0] = st
-        gpm = torch.empty((max(1, n_sub), self.nodes, 4), device=dev)
-        gv = torch.empty((max(1, n_sub), self.nodes, 4), device=dev)
-        r = self.lib.mpm_diff_forward_seq_pp(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(), n,
-                                             int(n_sub), xs.data_ptr(), vs.data_ptr(), Cs.data_ptr(), Fs.data_ptr(),
-                                             ring, self.mu.data_ptr(), self.lam.data_ptr(), gpm.data_ptr(),
-                                             gv.data_ptr(), 1, self.status.data_ptr(), self._s())
-        _lib.check(r, None, "mpm_diff_forward_seq_pp")
-        gp = torch.zeros((2, 24 * n), device=dev)
-        for k, (g, w) in enumerate(zip(grads, (3, 3, 9, 9))):
-            if g is not None:
-                off = (0, 3, 6, 15)[k] * n
-                gp[0, off: off + w * n] = g.reshape(-1).float()
-        gmu = torch.zeros(n, device=dev)
-        glam = torch.zeros(n, device=dev)
-        r = self.lib.mpm_diff_backward_seq_pp(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(), n,
-                                              int(n_sub), xs.data_ptr(), vs.data_ptr(), Cs.data_ptr(), Fs.data_ptr(),
-                                              self.mu.data_ptr(), self.lam.data_ptr(), gp.data_ptr(),
-                                              gmu.data_ptr(), glam.data_ptr(), gpm.data_ptr(), gv.data_ptr(),
-                                              self.g_grid_v.data_ptr(), self.g_grid_pm.data_ptr(),
-                                              self.status.data_ptr(), self._s())
-        _lib.check(r, None, "mpm_diff_backward_seq_pp")
+        seq = self._seq(n_sub + 1, st)
+        gpm = torch.empty((max(1, n_sub), self.nodes, 4), device="cuda")
+        gv = torch.empty((max(1, n_sub), self.nodes, 4), device="cuda")
+        self._forward_seq(seq, n_sub, n_sub + 1, gpm, gv, True)
+        gp = self._pack(grads)
+        self._backward_seq(seq, n_sub, gp, gpm, gv)
         self.check()
-        return (gp[0, : 3 * n].view(n, 3).clone(), gp[0, 3 * n: 6 * n].view(n, 3).clone(),
-                gp[0, 6 * n: 15 * n].view(n, 3, 3).clone(), gp[0, 15 * n:].view(n, 3, 3).clone())
+        return tuple(self._unpack(gp))
 
     def check(self):
         st = int(self.status.item())
@@ -209,19 +228,20 @@ class SceneDiffEngine:
         dev = "cuda"
         n = self.n
         self.adj = [[torch.zeros((n, 3), device=dev), torch.zeros((n, 3), device=dev),
-                     torch.zeros((n, 3, 3), device=dev), torch.zeros((n, 3, 3), device=dev)] for _ in range(self.B)]
+                     torch.zeros((n, 3, 3), device=dev), torch.zeros((n, 3, 3), device=dev),
+                     torch.zeros(n, device=dev)] for _ in range(self.B)]
         self.cursor = self.substeps_taken
         self._seg = None
         self.queried.clear()
 
     def add_grad(self, grads_by_field, envs=None) -> None:
-        """Add dL/d(pos, vel, C, F) ([B', N', ...] with N' = count particles from `start`) to the adjoint."""
+        """Add dL/d(pos, vel, C, F, Jp) ([B', N', ...] with N' = count particles from `start`) to the adjoint."""
         if self.adj is None:
             self.reset_grad()
         for field, (g, start) in grads_by_field.items():
             if g is None:
                 continue
-            k = {"pos": 0, "vel": 1, "C": 2, "F": 3}[field]
+            k = FIELDS.index(field)
             for i, b in enumerate(range(self.B) if envs is None else envs):
                 self.adj[b][k][start: start + g.shape[1]] += g[i].to(torch.float32)
 
@@ -247,36 +267,17 @@ class SceneDiffEngine:
             inputs, n_sub, _ = self.step_inputs[s_i]
             keep = []
             for b in range(self.B):
-                ring = n_sub + 1
-                seq = [torch.empty((ring, n, 3), device="cuda"), torch.empty((ring, n, 3), device="cuda"),
-                       torch.empty((ring, n, 3, 3), device="cuda"), torch.empty((ring, n, 3, 3), device="cuda")]
-                for j in range(4):
-                    seq[j][0] = inputs[b][j].detach()
+                seq = self._seq(n_sub + 1, inputs[b])
                 gpm = torch.empty((n_sub, self.nodes, 4), device="cuda")
                 gv = torch.empty((n_sub, self.nodes, 4), device="cuda")
-                r = self.lib.mpm_diff_forward_seq_pp(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(),
-                                                     n, n_sub, *[t.data_ptr() for t in seq], ring, self.mu.data_ptr(),
-                                                     self.lam.data_ptr(), gpm.data_ptr(), gv.data_ptr(), 1,
-                                                     self.status.data_ptr(), self._s())
-                _lib.check(r, None, "mpm_diff_forward_seq_pp")
+                self._forward_seq(seq, n_sub, n_sub + 1, gpm, gv, True)
                 keep.append((seq, gpm, gv))
             self._seg = (s_i, keep)
-        gmu = torch.zeros(n, device="cuda")
-        glam = torch.zeros(n, device="cuda")
         for b in range(self.B):
             seq, gpm, gv = self._seg[1][b]
-            gp = torch.zeros((2, 24 * n), device="cuda")
-            for j, off, w in ((0, 0, 3), (1, 3, 3), (2, 6, 9), (3, 15, 9)):
-                gp[0, off * n: (off + w) * n] = self.adj[b][j].reshape(-1)
-            one = [t[k: k + 1].contiguous() for t in seq]
-            r = self.lib.mpm_diff_backward_seq_pp(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(), n,
-                                                  1, *[t.data_ptr() for t in one], self.mu.data_ptr(),
-                                                  self.lam.data_ptr(), gp.data_ptr(), gmu.data_ptr(), glam.data_ptr(),
-                                                  gpm[k].data_ptr(), gv[k].data_ptr(), self.g_grid_v.data_ptr(),
-                                                  self.g_grid_pm.data_ptr(), self.status.data_ptr(), self._s())
-            _lib.check(r, None, "mpm_diff_backward_seq_pp")
-            self.adj[b] = [gp[0, : 3 * n].view(n, 3).clone(), gp[0, 3 * n: 6 * n].view(n, 3).clone(),
-                           gp[0, 6 * n: 15 * n].view(n, 3, 3).clone(), gp[0, 15 * n:].view(n, 3, 3).clone()]
+            gp = self._pack(self.adj[b])
+            self._backward_seq([t[k: k + 1].contiguous() for t in seq], 1, gp, gpm[k], gv[k])
+            self.adj[b] = self._unpack(gp)
         self.cursor -= 1
 
     def input_grad(self) -> None:
@@ -294,8 +295,8 @@ class SceneDiffEngine:
             if values.requires_grad:
                 vb = torch.broadcast_to(values.to(device="cuda", dtype=torch.float32), (len(envs), count, 3))
                 torch.autograd.backward([vb], [torch.stack([self.adj[b][j][rows] for b in envs])])
-            for b in envs:  # set_position also reset v, C, F of those rows
-                for jj in ((0, 1, 2, 3) if field == "pos" else (1,)):
+            for b in envs:  # set_position also reset v, C, F, Jp of those rows
+                for jj in ((0, 1, 2, 3, 4) if field == "pos" else (1,)):
                     self.adj[b][jj][rows] = 0.0
 
     def write(self, field: str, start: int, count: int, values: torch.Tensor, envs) -> None:
@@ -314,17 +315,13 @@ class SceneDiffEngine:
                 F0 = torch.eye(3, device="cuda").repeat(count, 1, 1)
                 st[2] = torch.cat([st[2][:start], C0, st[2][start + count:]], 0)
                 st[3] = torch.cat([st[3][:start], F0, st[3][start + count:]], 0)
+                st[4] = torch.cat([st[4][:start], self.Jp0[start: start + count], st[4][start + count:]], 0)
             self.states[b] = tuple(st)
 
     def stacked(self):
-        """[B, N, ...] views of the current state (autograd-connected)."""
-        x = torch.stack([s[0] for s in self.states])
-        v = torch.stack([s[1] for s in self.states])
-        C = torch.stack([s[2] for s in self.states])
-        F = torch.stack([s[3] for s in self.states])
-        return x, v, C, F
+        """[B, N, ...] tensors of the current state (pos, vel, C, F, Jp; autograd-connected)."""
+        return tuple(torch.stack([s[k] for s in self.states]) for k in range(5))
 
     def set_from_state(self, state, envs) -> None:
         for b in envs:
-            self.states[b] = tuple(getattr(state, k)[b].to(device="cuda", dtype=torch.float32)
-                                   for k in ("pos", "vel", "C", "F"))
+            self.states[b] = tuple(getattr(state, k)[b].to(device="cuda", dtype=torch.float32) for k in FIELDS)

@@ -254,8 +254,7 @@ class MPMSolver:
             return None
         s = MPMSolverState(self._B, self.n_particles, "cuda")
         if self._diff is not None:  # autograd-connected tensors (a loss on them back-propagates)
-            s.pos, s.vel, s.C, s.F = self._diff.stacked()
-            s.Jp = self._diff.Jp.expand(self._B, -1).clone()
+            s.pos, s.vel, s.C, s.F, s.Jp = self._diff.stacked()
             s.active = torch.ones((self._B, self.n_particles), dtype=torch.bool, device="cuda")
             self._diff.queried.append((self._diff.substeps_taken, s, 0))
             return s
@@ -480,14 +479,15 @@ class MPMSolver:
 
     def add_grad_from_state(self, state):
         """mpm_solver.py:614-670: add state.pos/vel/C/F .grad into the adjoint of the current substep."""
-        self._engine().add_grad({k: (getattr(getattr(state, k), "grad", None), 0) for k in ("pos", "vel", "C", "F")})
+        self._engine().add_grad({k: (getattr(getattr(state, k), "grad", None), 0) for k in ("pos", "vel", "C", "F", "Jp")})
 
     def collect_output_grads(self):
         """mpm_solver.py:607-612: the gradients of states queried (get_state) at the current substep."""
         eng = self._engine()
         for f_q, st, start in eng.queried:
             if f_q == eng.cursor:
-                eng.add_grad({k: (getattr(getattr(st, k), "grad", None), start) for k in ("pos", "vel", "C", "F")})
+                eng.add_grad({k: (getattr(getattr(st, k), "grad", None), start)
+                              for k in ("pos", "vel", "C", "F", "Jp")})
 
     def substep_post_coupling_grad(self, f=0):
         """g2p.grad (mpm_solver.py:548-554); the grid-op and P2G adjoints of the same substep run in the

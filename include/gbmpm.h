@@ -494,17 +494,20 @@ int mpm_diff_backward_seq(const mpm_scene_config* scene, double rho, int32_t neo
                           void* grid_v, void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream);
 
 /* mpm_diff_forward_seq / mpm_diff_backward_seq for scenes of several entities: per-particle
- * mass [n] and material kind [n] (0 corotated Elastic, 1 neo-Hookean Elastic, 2 Liquid) instead of
- * one rho and one material.  Replace the same reference autodiff kernels, whose material dispatch
- * and particle mass are per particle (mpm_solver.py:341-375, particles_info.mass). */
-int mpm_diff_forward_seq_pp(const mpm_scene_config* scene, const float* mass, const int32_t* kind, int64_t n,
-                            int32_t n_sub, float* x_seq, float* v_seq, float* C_seq, float* F_seq, int32_t ring,
-                            const float* mu, const float* lam, void* grid_pm, void* grid_v, int32_t grids_per_substep,
-                            uint32_t* status, void* stream);
-int mpm_diff_backward_seq_pp(const mpm_scene_config* scene, const float* mass, const int32_t* kind, int64_t n,
-                             int32_t n_sub, const float* x_seq, const float* v_seq, const float* C_seq,
-                             const float* F_seq, const float* mu, const float* lam, float* g_seq, float* gmu,
-                             float* glam, void* grid_pm, void* grid_v, void* g_grid_v, void* g_grid_pm,
+ * mass [n], material kind [n] (0 corotated Elastic, 1 neo-Hookean Elastic, 2 Liquid, 3 Sand,
+ * 4 Snow) and aux [n,2] (Sand: friction alpha; Snow: 1 - yield_lower, 1 + yield_higher) instead of
+ * one rho and one material; the state carries Jp (Jp_seq [ring,n]) and g_seq packs dL/dJp after
+ * (dx, dv, dC, dF): [2, 25n].  Replace the same reference autodiff kernels, whose material dispatch
+ * and particle mass are per particle (mpm_solver.py:341-375, particles_info.mass), and the SVD
+ * backward of the plastic laws (backward_svd, mpm_solver.py:1229-1252). */
+int mpm_diff_forward_seq_pp(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
+                            int64_t n, int32_t n_sub, float* x_seq, float* v_seq, float* C_seq, float* F_seq,
+                            float* Jp_seq, int32_t ring, const float* mu, const float* lam, void* grid_pm, void* grid_v,
+                            int32_t grids_per_substep, uint32_t* status, void* stream);
+int mpm_diff_backward_seq_pp(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
+                             int64_t n, int32_t n_sub, const float* x_seq, const float* v_seq, const float* C_seq,
+                             const float* F_seq, const float* Jp_seq, const float* mu, const float* lam, float* g_seq,
+                             float* gmu, float* glam, void* grid_pm, void* grid_v, void* g_grid_v, void* g_grid_pm,
                              uint32_t* status, void* stream);
 
 /* ABI version of this header (1). */

@@ -62,6 +62,9 @@ class QMat(np.ndarray):
     def dot(self, other):
         return float(np.dot(np.asarray(self), np.asarray(other)))
 
+    def cross(self, other):
+        return np.cross(np.asarray(self), np.asarray(other)).view(QMat)
+
     def fill(self, v):
         np.ndarray.fill(self, v)
 
@@ -324,7 +327,9 @@ def gen_materials(F, rng):
 
 
 # ----------------------------------------------------------------------------- one scene, full substeps
-def gen_substeps(F, rng):
+def gen_substeps(F, rng, ffs=(), n_steps=10):
+    """A 9-material scene on a 17^3 grid advanced by the reference's substep code; `ffs` are
+    reference force-field objects applied in its grid op (legacy_coupler.py:376-378)."""
     # domain [0, 0.25]^3 at density 64 -> 17^3 nodes, boundary [3/64, 0.25 - 3/64]
     density, dt = 64.0, 2e-4
     lower, upper = np.zeros(3), np.full(3, 0.25)
@@ -366,7 +371,7 @@ def gen_substeps(F, rng):
     solver._enable_CPIC = False
     solver.sim = types.SimpleNamespace(rigid_solver=types.SimpleNamespace(is_active=False))
     solver._gravity = QMat(np.array([[0.0, 0.0, -9.81]]))
-    solver._ffs = []
+    solver._ffs = list(ffs)
     bnd = types.SimpleNamespace(upper_qd=QMat(upper - 3 * dx), lower_qd=QMat(lower + 3 * dx), restitution=0.0)
     bind(bnd, F["boundary"])
     solver.boundary = bnd
@@ -396,7 +401,7 @@ def gen_substeps(F, rng):
 
     out = {"in/" + k: v for k, v in snapshot().items()}
     out.update({"in/mat": mat, "in/actu": actu, "in/mdir": mdir})
-    for step in range(10):
+    for step in range(n_steps):
         for k in G:
             G[k][...] = 0  # reset_grid_and_grad
         solver.compute_F_tmp(0)
@@ -410,11 +415,80 @@ def gen_substeps(F, rng):
             P[k][0] = P[k][1]
         if step == 0:
             out.update({"out1/" + k: v for k, v in snapshot().items()})
-    out.update({"out10/" + k: v for k, v in snapshot().items()})
+    out.update({f"out{n_steps}/" + k: v for k, v in snapshot().items()})
     out["scene"] = np.array([dt, density, p_size, *lower, *upper, EPS32])
     out["material_params"] = np.array([[p["type"], p["flags"], p["mu"], p["lam"], p.get("alpha", 0.0),
                                         p.get("yield_lower", 0.0), p.get("yield_higher", 0.0), p.get("vm_yield", 0.0),
                                         p.get("stiffness", 0.0), rho] for _, p in variants])
+    return out
+
+
+# ----------------------------------------------------------------------------- force fields
+class _FieldStandin:
+    """qd.field stand-in: scalar (shape ()) or 1-D integer field."""
+
+    def __init__(self, dtype, shape=()):
+        self.a = np.zeros(shape if shape != () else (1,), dtype=np.int64 if dtype in (np.int64, bool) else np.float64)
+
+    def __getitem__(self, i):
+        return self.a[0 if i is None else int(i)]
+
+    def __setitem__(self, i, v):
+        self.a[0 if i is None else int(i)] = v
+
+    def from_numpy(self, arr):
+        self.a[:] = arr
+
+
+def load_force_fields(ref):
+    """Execute genesis/engine/force_fields.py as written, against the stand-ins (the Quadrants
+    decorators are identities, fields are numpy arrays)."""
+    qd = make_qd()
+    qd.func = qd.kernel = qd.data_oriented = lambda f: f
+    qd.field = lambda dtype, shape=(): _FieldStandin(dtype, shape)
+    gs = make_gs()
+    gs.qd_bool = bool
+    repr_base = types.ModuleType("genesis.repr_base")
+    repr_base.RBC = object
+    saved = {k: sys.modules.get(k) for k in ("quadrants", "genesis", "genesis.repr_base")}
+    sys.modules.update({"quadrants": qd, "genesis": gs, "genesis.repr_base": repr_base})
+    try:
+        mod = types.ModuleType("reference_force_fields")
+        path = os.path.join(ref, "genesis/engine/force_fields.py")
+        exec(compile(open(path).read(), path, "exec"), mod.__dict__)
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                sys.modules.pop(k, None)
+            else:
+                sys.modules[k] = v
+    return mod
+
+
+# (class, keyword arguments) of the deterministic fields pinned here (Noise draws qd.random)
+FORCE_FIELDS = [
+    ("Constant", dict(direction=(1.0, 0.5, 0.0), strength=2.0)),
+    ("Wind", dict(direction=(0.0, 1.0, 0.2), strength=3.0, radius=0.05, center=(0.1, 0.12, 0.1))),
+    ("Point", dict(strength=-1.5, position=(0.125, 0.125, 0.2), falloff_pow=1.5, flow=0.3)),
+    ("Drag", dict(linear=0.8, quadratic=0.4)),
+    ("Vortex", dict(direction=(0.0, 0.0, 1.0), center=(0.12, 0.13, 0.0), strength_perpendicular=4.0,
+                    strength_radial=1.0, falloff_pow=2.0, falloff_min=0.02, falloff_max=0.2, damping=0.5)),
+    ("Turbulence", dict(strength=2.0, frequency=7, flow=0.2, seed=5)),
+]
+
+
+def gen_force_fields(F, ref, rng):
+    FF = load_force_fields(ref)
+    fields = []
+    for name, kw in FORCE_FIELDS:
+        f = getattr(FF, name)(**kw)
+        f.activate()
+        fields.append(f)
+    out = gen_substeps(F, rng, ffs=fields, n_steps=5)
+    out["fields"] = np.array([name for name, _ in FORCE_FIELDS])
+    for i, (name, kw) in enumerate(FORCE_FIELDS):
+        for k, v in kw.items():
+            out[f"field{i}/{k}"] = np.asarray(v, dtype=np.float64)
     return out
 
 
@@ -426,6 +500,8 @@ def main():
     rng = np.random.default_rng(20261204)
     np.savez_compressed(os.path.join(HERE, "materials.npz"), **gen_materials(F, rng))
     np.savez_compressed(os.path.join(HERE, "substep_small.npz"), **gen_substeps(F, rng))
+    np.savez_compressed(os.path.join(HERE, "force_fields.npz"),
+                        **gen_force_fields(F, ref, np.random.default_rng(20261205)))
     print("wrote", os.listdir(HERE))
 
 

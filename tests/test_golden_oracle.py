@@ -62,3 +62,40 @@ def test_ten_substeps_state(oracle, small):
     for k in ("pos", "vel", "C", "F", "Jp"):
         ref = small["out10/" + k]
         assert np.abs(out[k] - ref).max() <= 1e-8 * max(1.0, np.abs(ref).max()), k
+
+
+def _golden_fields(g):
+    """The facade's force fields built with the fixture's parameters (genesis_gb300.force_fields
+    mirrors the constructors of genesis/engine/force_fields.py)."""
+    import genesis_gb300.force_fields as ff
+
+    out = []
+    for i, name in enumerate(g["fields"]):
+        kw = {k.split("/")[1]: g[k] for k in g.files if k.startswith(f"field{i}/")}
+        kw = {k: (tuple(v.tolist()) if v.ndim else (int(v) if k == "seed" else float(v))) for k, v in kw.items()}
+        f = getattr(ff, str(name))(**kw)
+        f.activate()
+        out.append(f)
+    return out
+
+
+def test_force_fields_match_reference_code(oracle):
+    """The oracle's force fields (Constant, Wind, Point, Drag, Vortex, Turbulence, applied in order
+    after gravity in the grid op) against five substeps of the reference's own grid op and field
+    code (tests/golden/force_fields.npz)."""
+    g = np.load(os.path.join(GOLDEN, "force_fields.npz"))
+    sc, mats, st = _oracle_inputs(oracle, g)
+    oracle.set_force_fields([f.to_c() for f in _golden_fields(g)])
+    try:
+        out, grid, _ = oracle.run(sc, mats, st, 1, want_grid=True)
+        for k in ("pos", "vel", "C", "F", "Jp"):
+            ref = g["out1/" + k]
+            assert np.abs(out[k] - ref).max() <= 1e-9 * max(1.0, np.abs(ref).max()), k
+        out5, _, _ = oracle.run(sc, mats, st, 5)
+    finally:
+        oracle.set_force_fields([])
+    plain, _, _ = oracle.run(sc, mats, st, 5)
+    assert np.abs(plain["vel"] - g["out5/vel"]).max() > 1e-3  # the fields act on this scene
+    for k in ("pos", "vel", "C", "F", "Jp"):
+        ref = g["out5/" + k]
+        assert np.abs(out5[k] - ref).max() <= 1e-8 * max(1.0, np.abs(ref).max()), k

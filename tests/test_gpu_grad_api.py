@@ -2,8 +2,9 @@
 require grad, scene.step(), scene.get_state() / entity.get_state(), loss.backward().
 
 * The gradient of a loss on the final centre of mass w.r.t. the initial velocity set through
-  entity.set_velocity (a scene of an Elastic and a Liquid entity, 4 steps x 10 substeps) against
-  FP64 central differences of the CPU oracle (eps = 1e-4), tolerance 2e-2 relative.
+  entity.set_velocity (a scene of an Elastic and a Liquid entity, and one of a Sand and a Snow
+  entity, 4 steps x 10 substeps each, with floor contact) against FP64 central differences of the
+  CPU oracle (eps = 1e-4), tolerance 2e-2 relative.
 * The input pattern of the reference's tests/test_grad.py::test_differentiable_push (two envs, a
   position and a velocity set before the first step, a velocity input every step, a loss on the
   solver state at step 5 and one on the entity state at step 8): inputs that reach a loss get a
@@ -55,7 +56,8 @@ def _oracle_com_loss(O, scene, ents, v_box, target, n_sub):
     vel = np.zeros((n, 3))
     nb = ents[0].n_particles
     vel[:nb] = v_box
-    st = dict(pos=pos, vel=vel, C=np.zeros((n, 3, 3)), F=np.tile(np.eye(3), (n, 1, 1)), Jp=np.ones(n),
+    st = dict(pos=pos, vel=vel, C=np.zeros((n, 3, 3)), F=np.tile(np.eye(3), (n, 1, 1)),
+              Jp=np.concatenate([np.full(e.n_particles, float(e.material._default_Jp)) for e in ents]),
               mat=np.concatenate([np.full(e.n_particles, e.material.idx, np.int32) for e in ents]),
               active=np.ones(n, bool))
     sc = O.make_scene(solver.substep_dt, gravity=tuple(solver.gravity[0]), lower_bound=tuple(solver.lower_bound),
@@ -92,6 +94,63 @@ def test_grad_of_initial_velocity_matches_fp64_central_differences(gs, oracle):
         e[k] = eps
         fd[k] = (_oracle_com_loss(oracle, scene, [box, water], v0 + e, target, n_sub)
                  - _oracle_com_loss(oracle, scene, [box, water], v0 - e, target, n_sub)) / (2 * eps)
+    assert np.linalg.norm(g - fd) <= GRAD_RTOL * np.linalg.norm(fd), (g, fd)
+
+
+def test_plastic_materials_grad_matches_fp64_central_differences(gs, oracle):
+    """Sand (Drucker-Prager) and Snow (clamped, hardening) boxes thrown onto the floor boundary, 40
+    substeps: the impact deforms them past their yield limits (sand Jp leaves 0, snow Jp leaves 1), so
+    the gradient goes through the plastic return mappings and their Jp updates.  dL/dv0 of the sand box against FP64 central
+    differences of the oracle (2e-2)."""
+    scene = gs.Scene(
+        sim_options=gs.options.SimOptions(dt=2e-3, substeps=10, requires_grad=True),
+        mpm_options=gs.options.MPMOptions(lower_bound=(0, 0, 0), upper_bound=(1, 1, 1), grid_density=32,
+                                          particle_size=1.0 / 64),
+    )
+    sand = scene.add_entity(material=gs.materials.MPM.Sand(sampler="regular"),
+                            morph=gs.morphs.Box(pos=(0.4, 0.5, 0.16), size=(0.1, 0.1, 0.1)))
+    snow = scene.add_entity(material=gs.materials.MPM.Snow(sampler="regular"),
+                            morph=gs.morphs.Box(pos=(0.62, 0.5, 0.16), size=(0.1, 0.1, 0.1)))
+    scene.build()
+    v0 = np.array([0.3, 0.2, -2.0])
+    target = np.array([0.45, 0.5, 0.1])
+    v = torch.tensor(v0, dtype=torch.float32, device="cuda", requires_grad=True)
+    sand.set_velocity(v)
+    snow.set_velocity(torch.tensor([-0.2, 0.0, -2.5], device="cuda"))
+    steps = 4
+    for _ in range(steps):
+        scene.step()
+    st = sand.get_state()
+    assert (st.Jp[0].abs() > 1e-3).any(), "the sand never flowed plastically"  # Jp != 0: projected
+    assert (snow.get_state().Jp[0] != 1.0).any(), "the snow never reached a clamp bound"
+    loss = ((st.pos[0].mean(0) - torch.tensor(target, dtype=torch.float32, device="cuda")) ** 2).sum()
+    loss.backward()
+    g = v.grad.detach().cpu().numpy().astype(np.float64)
+    n_sub = steps * scene.substeps
+
+    def oracle_loss(vb):
+        solver = scene.sim.mpm_solver
+        ents = [sand, snow]
+        oms = [oracle.from_c_material(m.to_c(0)) for m in solver._unique_materials()]
+        pos = np.concatenate([e.init_particles.astype(np.float32).astype(np.float64) for e in ents])
+        n, ns = len(pos), sand.n_particles
+        vel = np.zeros((n, 3))
+        vel[:ns] = vb
+        vel[ns:] = np.array([-0.2, 0.0, -2.5], np.float32)
+        s0 = dict(pos=pos, vel=vel, C=np.zeros((n, 3, 3)), F=np.tile(np.eye(3), (n, 1, 1)),
+                  Jp=np.concatenate([np.zeros(ns), np.ones(n - ns)]),
+                  mat=np.concatenate([np.full(e.n_particles, e.material.idx, np.int32) for e in ents]),
+                  active=np.ones(n, bool))
+        sc = oracle.make_scene(solver.substep_dt, gravity=tuple(solver.gravity[0]),
+                               lower_bound=tuple(solver.lower_bound), upper_bound=tuple(solver.upper_bound),
+                               grid_density=solver.grid_density, particle_size=solver.particle_size)
+        out, _, _ = oracle.run(sc, oms, s0, n_sub)
+        return float(((out["pos"][:ns].mean(0) - target) ** 2).sum())
+
+    assert abs(loss.item() - oracle_loss(v0)) <= 1e-3 * loss.item() + 1e-8
+    eps = 1e-4
+    fd = np.array([(oracle_loss(v0 + eps * np.eye(3)[k]) - oracle_loss(v0 - eps * np.eye(3)[k])) / (2 * eps)
+                   for k in range(3)])
     assert np.linalg.norm(g - fd) <= GRAD_RTOL * np.linalg.norm(fd), (g, fd)
 
 
