@@ -65,6 +65,13 @@ class QMat(np.ndarray):
     def cross(self, other):
         return np.cross(np.asarray(self), np.asarray(other)).view(QMat)
 
+    def any(self, *a, **k):  # noqa: A003
+        return bool(np.asarray(self).any(*a, **k))
+
+    x = property(lambda self: float(self[0]))
+    y = property(lambda self: float(self[1]))
+    z = property(lambda self: float(self[2]))
+
     def fill(self, v):
         np.ndarray.fill(self, v)
 
@@ -118,7 +125,8 @@ def make_qd():
     qd.exp = lambda x: np.exp(x)
     qd.pow = lambda x, y: np.power(x, y)
     qd.sqrt = lambda x: np.sqrt(x)
-    qd.floor = lambda x: np.floor(x).view(QMat) if isinstance(x, np.ndarray) else math.floor(x)
+    qd.floor = lambda x, dt=None: (np.floor(x).astype(np.int64 if dt is not None else np.float64).view(QMat)
+                                   if isinstance(x, np.ndarray) else math.floor(x))
     qd.max = lambda a, b: np.maximum(a, b).view(QMat) if isinstance(a, np.ndarray) or isinstance(b, np.ndarray) else max(a, b)
     qd.min = lambda a, b: np.minimum(a, b).view(QMat) if isinstance(a, np.ndarray) or isinstance(b, np.ndarray) else min(a, b)
     qd.abs = abs
@@ -180,8 +188,75 @@ class _Record:
 
 
 # ----------------------------------------------------------------------------- source extraction
+def extract_functions(path, names, ns):
+    """Compile module-level functions `names` of `path` (decorators/annotations removed) into ns,
+    so that they call each other through ns."""
+    ns.setdefault("_qd_copy", _qd_copy)
+    tree = ast.parse(open(path).read())
+    found = set()
+    for node in tree.body:
+        if isinstance(node, ast.FunctionDef) and node.name in names:
+            node.decorator_list = []
+            node.returns = None
+            for a in node.args.args + node.args.kwonlyargs:
+                a.annotation = None
+            node = _ValueAssign().visit(node)
+            exec(compile(ast.fix_missing_locations(ast.Module(body=[node], type_ignores=[])), path, "exec"), ns)
+            found.add(node.name)
+    if set(names) - found:
+        raise RuntimeError(f"{path} lacks {set(names) - found}")
+    return {k: ns[k] for k in names}
+
+
+GEOM_TYPE = types.SimpleNamespace(PLANE=0, SPHERE=1, ELLIPSOID=2, CYLINDER=3, CAPSULE=4, BOX=5, MESH=6, TERRAIN=7)
+
+
+def rigid_namespace(ref, ns):
+    """Namespace for the coupler's rigid-collision methods: the reference's SDF functions
+    (genesis/utils/sdf.py), geometry helpers (genesis/utils/geom.py) and rigid-link velocity /
+    coupling-force functions (rigid/abd/forward_dynamics.py, rigid/abd/misc.py), all executed as written."""
+    gns = dict(ns)
+    gns["gs"] = types.SimpleNamespace(**vars(ns["gs"]))
+    gns["gs"].GEOM_TYPE = GEOM_TYPE
+    gns["gs"].qd_vec3 = lambda v: QMat(v)
+    gu = types.SimpleNamespace()
+    gns["gu"] = gu
+    extract_functions(os.path.join(ref, "genesis/utils/geom.py"),
+                      ["qd_normalize", "qd_transform_by_quat", "qd_inv_quat", "qd_inv_transform_by_quat",
+                       "qd_transform_by_T", "qd_inv_transform_by_trans_quat"], gns)
+    for k in ("qd_normalize", "qd_transform_by_quat", "qd_inv_quat", "qd_inv_transform_by_quat", "qd_transform_by_T",
+              "qd_inv_transform_by_trans_quat"):
+        setattr(gu, k, gns[k])
+    sdf_names = ["sdf_func_world", "sdf_func_world_local", "sdf_func_sdf", "sdf_func_is_outside_sdf_grid",
+                 "sdf_func_proxy_sdf", "sdf_func_true_sdf", "sdf_func_ravel_cell_idx", "sdf_func_grad",
+                 "sdf_func_proxy_grad", "sdf_func_true_grad", "sdf_func_normal_world", "sdf_func_normal_world_local",
+                 "sdf_func_grad_world_local"]
+    sdf = types.SimpleNamespace(**extract_functions(os.path.join(ref, "genesis/utils/sdf.py"), sdf_names, gns))
+    rig = extract_functions(os.path.join(ref, "genesis/engine/solvers/rigid/abd/forward_dynamics.py"),
+                            ["func_vel_at_point"], gns)
+    rig.update(extract_functions(os.path.join(ref, "genesis/engine/solvers/rigid/abd/misc.py"),
+                                 ["func_apply_coupling_force"], gns))
+    out = dict(gns)
+    out["sdf"] = sdf
+    out["rigid_funcs"] = rig
+    return out
+class _ValueAssign(ast.NodeTransformer):
+    """`a = b` between names copies b, as Quadrants assigns vectors and matrices by value (numpy
+    would alias them: `inc = pos; inc[i] += d` must leave pos unchanged)."""
+
+    def visit_Assign(self, node):
+        if len(node.targets) == 1 and isinstance(node.targets[0], ast.Name) and isinstance(node.value, ast.Name):
+            node.value = ast.Call(func=ast.Name(id="_qd_copy", ctx=ast.Load()), args=[node.value], keywords=[])
+        return node
+
+
+def _qd_copy(v):
+    return v.copy() if isinstance(v, np.ndarray) else v
+
+
 def extract(path, cls, names, ns):
     """Compile methods `names` of class `cls` in `path` (decorators/annotations removed) into ns."""
+    ns.setdefault("_qd_copy", _qd_copy)
     src = open(path).read()
     tree = ast.parse(src)
     out = {}
@@ -193,6 +268,7 @@ def extract(path, cls, names, ns):
                     fn.returns = None
                     for a in fn.args.args + fn.args.kwonlyargs:
                         a.annotation = None
+                    fn = _ValueAssign().visit(fn)
                     mod = ast.Module(body=[fn], type_ignores=[])
                     code = compile(ast.fix_missing_locations(mod), path, "exec")
                     loc = {}
@@ -239,6 +315,11 @@ def load_reference(ref):
                           ["stencil_range", "compute_F_tmp", "svd", "p2g", "g2p"], ns)
     F["coupler"] = extract(os.path.join(ref, "genesis/engine/couplers/legacy_coupler.py"), "LegacyCoupler",
                            ["mpm_grid_op"], ns)
+    rns = rigid_namespace(ref, ns)
+    F["coupler_rigid"] = extract(os.path.join(ref, "genesis/engine/couplers/legacy_coupler.py"), "LegacyCoupler",
+                                 ["_func_collide_with_rigid", "_func_collide_with_rigid_geom",
+                                  "_func_collide_in_rigid_geom"], rns)
+    F["rigid_funcs"] = rns["rigid_funcs"]
     F["boundary"] = extract(os.path.join(ref, "genesis/engine/boundaries/boundaries.py"), "CubeBoundary",
                             ["impose_pos_vel"], ns)
     return F
@@ -327,9 +408,10 @@ def gen_materials(F, rng):
 
 
 # ----------------------------------------------------------------------------- one scene, full substeps
-def gen_substeps(F, rng, ffs=(), n_steps=10):
+def gen_substeps(F, rng, ffs=(), n_steps=10, rigid=None):
     """A 9-material scene on a 17^3 grid advanced by the reference's substep code; `ffs` are
-    reference force-field objects applied in its grid op (legacy_coupler.py:376-378)."""
+    reference force-field objects applied in its grid op (legacy_coupler.py:376-378); `rigid`
+    (make_rigid_standins) couples the grid op with rigid geoms (legacy_coupler.py:389-403)."""
     # domain [0, 0.25]^3 at density 64 -> 17^3 nodes, boundary [3/64, 0.25 - 3/64]
     density, dt = 64.0, 2e-4
     lower, upper = np.zeros(3), np.full(3, 0.25)
@@ -389,6 +471,13 @@ def gen_substeps(F, rng, ffs=(), n_steps=10):
     coupler = types.SimpleNamespace(mpm_solver=solver, tool_solver=types.SimpleNamespace(is_active=False),
                                     _rigid_mpm=False, _mpm_sph=False, _mpm_pbd=False)
     bind(coupler, F["coupler"])
+    grid_op_args = (None, None, None, None, None, None)
+    if rigid is not None:
+        coupler._rigid_mpm = True
+        coupler.rigid_solver = rigid["rigid_solver"]
+        bind(coupler, F["coupler_rigid"])
+        grid_op_args = tuple(rigid[k] for k in ("geoms_state", "geoms_info", "links_state", "rigid_global_info",
+                                                "sdf_info", "collider_static_config"))
 
     P, I, G = solver.particles._d, solver.particles_info._d, solver.grid._d
     P["pos"][0, :, 0], P["vel"][0, :, 0], P["C"][0, :, 0], P["F"][0, :, 0] = pos, vel, C, Fm
@@ -409,7 +498,7 @@ def gen_substeps(F, rng, ffs=(), n_steps=10):
         solver.p2g(0, None, None, None, None, None, None)
         if step == 0:
             out["grid1"] = np.concatenate([G["vel_in"][0, ..., 0, :], G["mass"][0, ..., 0, None]], -1).copy()
-        coupler.mpm_grid_op(0, 0.0, None, None, None, None, None, None)
+        coupler.mpm_grid_op(0, 0.0, *grid_op_args)
         solver.g2p(0, None, None, None)
         for k in ("pos", "vel", "C", "F", "Jp"):  # copy_frame(1 -> 0)
             P[k][0] = P[k][1]
@@ -492,6 +581,109 @@ def gen_force_fields(F, ref, rng):
     return out
 
 
+# ----------------------------------------------------------------------------- rigid coupling
+def _quat_about(axis, deg):
+    a = np.asarray(axis, np.float64) / np.linalg.norm(axis)
+    h = math.radians(deg) / 2
+    return np.array([math.cos(h), *(math.sin(h) * a)])
+
+
+def box_sdf(p, half):
+    q = np.abs(p) - half
+    out = np.linalg.norm(np.maximum(q, 0), axis=-1)
+    return out + np.minimum(q.max(-1), 0)
+
+
+# geoms of the coupled scene: (type, pos, quat, data, link cd_vel, cd_ang, friction, softness, restitution)
+RIGID_GEOMS = [
+    ("sphere", (0.125, 0.125, 0.05), _quat_about((0, 0, 1), 0.0), (0.03,), (0.1, 0.0, 0.2), (0.0, 0.0, 1.0),
+     0.3, 0.002, 0.1),
+    ("plane", (0.125, 0.125, 0.07), _quat_about((1, 0, 0), 15.0), (0.0, 0.0, 1.0), (0.0, 0.0, 0.0), (0.0, 0.0, 0.0),
+     0.5, 0.004, 0.0),
+    ("box", (0.17, 0.1, 0.1), _quat_about((0, 0, 1), 20.0), (0.03, 0.02, 0.025), (0.0, -0.1, 0.0), (0.5, 0.0, 0.0),
+     0.2, 0.002, 0.2),
+]
+BOX_GRID = dict(res=24, lower=-0.05, upper=0.05)
+
+
+def box_grid(half):
+    """The box geom's SDF grid as the rigid solver stores it (values and mesh-frame gradients on a
+    res^3 lattice, T_mesh_to_sdf mapping mesh coordinates to voxel indices), in float32."""
+    res, lo, hi = BOX_GRID["res"], BOX_GRID["lower"], BOX_GRID["upper"]
+    h = (hi - lo) / (res - 1)
+    ax = lo + h * np.arange(res)
+    pts = np.stack(np.meshgrid(ax, ax, ax, indexing="ij"), -1).reshape(-1, 3)
+    val = box_sdf(pts, np.asarray(half))
+    eps = 1e-6
+    grad = np.stack([(box_sdf(pts + eps * e, half) - box_sdf(pts - eps * e, half)) / (2 * eps) for e in np.eye(3)], -1)
+    grad /= np.maximum(np.linalg.norm(grad, axis=-1, keepdims=True), 1e-12)
+    T = np.eye(4)
+    T[:3, :3] /= h
+    T[:3, 3] = -lo / h
+    return (val.astype(np.float32).reshape(res, res, res), grad.astype(np.float32).reshape(res, res, res, 3), T, h,
+            float(val.astype(np.float32).max()))
+
+
+def make_rigid_standins(F, dt):
+    """The rigid solver's data the coupler reads, for RIGID_GEOMS (one env, one link per geom)."""
+    G = len(RIGID_GEOMS)
+    types_ = {"sphere": GEOM_TYPE.SPHERE, "plane": GEOM_TYPE.PLANE, "box": GEOM_TYPE.BOX}
+    data = np.zeros((G, 7))
+    gpos = np.zeros((G, 1, 3)).view(QMat)
+    gquat = np.zeros((G, 1, 4)).view(QMat)
+    cd_vel = np.zeros((G, 1, 3)).view(QMat)
+    cd_ang = np.zeros((G, 1, 3)).view(QMat)
+    com = np.zeros((G, 1, 3)).view(QMat)
+    for i, (t, pos, quat, d, v, w, *_rest) in enumerate(RIGID_GEOMS):
+        data[i, : len(d)] = d
+        gpos[i, 0], gquat[i, 0], cd_vel[i, 0], cd_ang[i, 0], com[i, 0] = pos, quat, v, w, pos
+    geoms_info = types.SimpleNamespace(
+        needs_coup=[1] * G, type=[types_[g[0]] for g in RIGID_GEOMS], data=[QMat(r) for r in data],
+        coup_friction=[g[6] for g in RIGID_GEOMS], coup_softness=[g[7] for g in RIGID_GEOMS],
+        coup_restitution=[g[8] for g in RIGID_GEOMS], link_idx=list(range(G)))
+    geoms_state = types.SimpleNamespace(pos=gpos, quat=gquat)
+    links_state = types.SimpleNamespace(cd_vel=cd_vel, cd_ang=cd_ang, root_COM=com,
+                                        cfrc_coupling_vel=np.zeros((G, 1, 3)).view(QMat),
+                                        cfrc_coupling_ang=np.zeros((G, 1, 3)).view(QMat))
+    rgi = types.SimpleNamespace(substep_dt=_FieldStandin(np.float64), EPS=_FieldStandin(np.float64))
+    rgi.substep_dt[None] = dt
+    rgi.EPS[None] = EPS32
+    val, grad, T, h, smax = box_grid(RIGID_GEOMS[2][3])
+    res = QMat(np.array(val.shape), dtype=np.int64)
+    zero_T = np.eye(4)
+    sdf_geoms = types.SimpleNamespace(T_mesh_to_sdf=[QMat(zero_T), QMat(zero_T), QMat(T)], sdf_res=[res, res, res],
+                                      sdf_cell_size=[h, h, h], sdf_max=[smax] * 3, sdf_cell_start=[0, 0, 0])
+    sdf_info = types.SimpleNamespace(geoms_info=sdf_geoms, geoms_sdf_val=val.astype(np.float64).reshape(-1),
+                                     geoms_sdf_grad=grad.astype(np.float64).reshape(-1, 3).view(QMat))
+    fns = F["rigid_funcs"]
+    rigid_solver = types.SimpleNamespace(
+        n_geoms=G, is_active=True,
+        _func_vel_at_point=lambda pos_world, link_idx, i_b, links_state: fns["func_vel_at_point"](
+            pos_world, link_idx, i_b, links_state),
+        _func_apply_coupling_force=lambda pos, force, link_idx, env_idx, links_state: fns["func_apply_coupling_force"](
+            pos, force, link_idx, env_idx, links_state))
+    return dict(geoms_state=geoms_state, geoms_info=geoms_info, links_state=links_state, rigid_global_info=rgi,
+                sdf_info=sdf_info, collider_static_config=types.SimpleNamespace(has_terrain=False),
+                rigid_solver=rigid_solver)
+
+
+def gen_rigid(F, rng):
+    rigid = make_rigid_standins(F, 2e-4)
+    out = gen_substeps(F, rng, n_steps=3, rigid=rigid)
+    ls = rigid["links_state"]
+    out["link_force"] = np.asarray(ls.cfrc_coupling_vel)[:, 0].copy()
+    out["link_torque"] = np.asarray(ls.cfrc_coupling_ang)[:, 0].copy()
+    out["geom_types"] = np.array([g[0] for g in RIGID_GEOMS])
+    for i, g in enumerate(RIGID_GEOMS):
+        out[f"geom{i}/pos"], out[f"geom{i}/quat"], out[f"geom{i}/data"] = np.array(g[1]), np.array(g[2]), np.array(g[3])
+        out[f"geom{i}/lin_vel"], out[f"geom{i}/ang_vel"] = np.array(g[4]), np.array(g[5])
+        out[f"geom{i}/coup"] = np.array(g[6:9])
+    val, grad, T, h, smax = box_grid(RIGID_GEOMS[2][3])
+    out["box_sdf/values"], out["box_sdf/grads"], out["box_sdf/T"] = val, grad, T
+    out["box_sdf/cell_size"], out["box_sdf/sdf_max"] = np.array(h), np.array(smax)
+    return out
+
+
 def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GENESIS_REFERENCE")
     if not ref:
@@ -502,6 +694,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "substep_small.npz"), **gen_substeps(F, rng))
     np.savez_compressed(os.path.join(HERE, "force_fields.npz"),
                         **gen_force_fields(F, ref, np.random.default_rng(20261205)))
+    np.savez_compressed(os.path.join(HERE, "rigid_coupling.npz"), **gen_rigid(F, np.random.default_rng(20261206)))
     print("wrote", os.listdir(HERE))
 
 

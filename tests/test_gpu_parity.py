@@ -944,3 +944,43 @@ def test_mesh_morph_entity_steps(gs, tmp_path):
     p = ent.get_particles_pos()
     assert torch.isfinite(p).all() and (p[:, 2] < 0.4).any()
     assert ent.n_vverts == 8
+
+
+@pytest.mark.parametrize("substeps", [1, 10])
+def test_reference_scenario_rigid_mpm_legacy_coupling(gs, substeps):
+    """tests/test_hybrid.py::test_rigid_mpm_legacy_coupling through the collider API: a light rigid
+    box (rho = 1, 0.2 m, resting on the ground at y = -0.25) beside a 0.3 m liquid block; 100 substeps
+    of 4e-4 s as 100 steps of 1 substep or 10 steps of 10.  The box is the host's rigid body: after
+    every step its velocity takes the particles' reaction force (get_collider_forces, summed over the
+    step's substeps) with gravity balanced by the ground and Coulomb friction against it (mu = 1, the
+    rigid material default); the MPM side sees it as a moving box collider.  As in the reference, the
+    liquid pushes the box towards -y, with either step size."""
+    from genesis_gb300.coupling import Collider
+
+    dt = 4e-4
+    scene = gs.Scene(
+        sim_options=gs.options.SimOptions(dt=dt * substeps, substeps=substeps),
+        mpm_options=gs.options.MPMOptions(lower_bound=(-0.5, -1.0, 0.0), upper_bound=(0.5, 1.0, 1.0)),
+    )
+    scene.add_entity(material=gs.materials.MPM.Liquid(), morph=gs.morphs.Box(pos=(0.0, 0.0, 0.2), size=(0.3, 0.3, 0.3)))
+    scene.build()
+    solver = scene.sim.mpm_solver
+    mass, mu_ground, g = 1.0 * 0.2 ** 3, 1.0, 9.81
+    pos = np.array([0.0, -0.25, 0.1])
+    vel = np.zeros(3)
+    pushed = 0.0
+    for _ in range(100 // substeps):
+        solver.set_colliders([Collider("box", pos=tuple(pos), half_extents=(0.1, 0.1, 0.1), lin_vel=tuple(vel))])
+        scene.step()
+        f = solver.get_collider_forces()[0, :3] / substeps  # mean force over the step's substeps
+        pushed = min(pushed, f[1])
+        h = dt * substeps
+        fh = f[:2].copy()
+        vh = vel[:2] + h * fh / mass
+        speed = np.linalg.norm(vh)
+        dv_fric = h * mu_ground * g  # ground friction (normal force m g) brakes the sliding speed
+        vel[:2] = 0.0 if speed <= dv_fric else vh * (1.0 - dv_fric / speed)
+        pos[:2] += h * vel[:2]
+    solver.check_state()
+    assert pushed < 0.0  # the liquid pushed the box towards -y
+    assert pos[1] + 0.25 < 0.0, pos
