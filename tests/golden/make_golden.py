@@ -14,8 +14,24 @@ compared downstream.  gs.EPS is the float32 value (precision "32").
 
 Outputs (committed, small):
   materials.npz     per material variant: F_tmp, Jp, actu, mdir -> F_new, Jp_new, stress
-  substep_small.npz a 6-material scene on a 17^3 grid: input state, grid (momentum, mass)
+  substep_small.npz a 9-material scene on a 17^3 grid: input state, grid (momentum, mass)
                     after the first P2G, states after 1 and 10 substeps
+  force_fields.npz  the same scene with six force fields in the grid op (force_fields.py):
+                    states after 1 and 5 substeps
+  rigid_coupling.npz the same scene coupled with a sphere, a tilted plane and a voxel-SDF box
+                    (legacy_coupler.py rigid collision, utils/sdf.py, utils/geom.py): state after
+                    3 substeps, the reaction accumulated on each link
+  cpic_coupling.npz rigid_coupling's scene with MPMOptions.enable_CPIC (mpm_solver.py p2g/g2p,
+                    legacy_coupler.py mpm_surface_to_particle)
+  particle_coupling.npz the same scene coupled with an SPH and a PBD particle set through their
+                    spatial hash (legacy_coupler.py, utils/geom.py SpatialHasher): state and
+                    the sets' velocities after 4 substeps
+  particle_constraints.npz the same scene with particles attached to two moving kinematic links
+                    and to their start positions, some released midway (mpm_solver.py
+                    particle constraints): state after 5 substeps
+  tool_coupling.npz the same scene with a moving, spinning box tool (tool_entity/mesh.py,
+                    tool_entity.py, boundaries.py FloorBoundary): state and tool pose after 4
+                    substeps
 
 Run from the repository root with the reference checked out:
     python tests/golden/make_golden.py /path/to/genesis-reference
@@ -52,6 +68,15 @@ class QMat(np.ndarray):
 
     def norm(self, eps=0.0):
         return float(math.sqrt(float(np.sum(np.asarray(self, dtype=np.float64) ** 2)) + eps))
+
+    def norm_sqr(self):
+        return float(np.sum(np.asarray(self, dtype=np.float64) ** 2))
+
+    def normalized(self):
+        return (np.asarray(self) / self.norm()).view(QMat)
+
+    def inverse(self):
+        return np.linalg.inv(np.asarray(self, dtype=np.float64)).view(QMat)
 
     def outer_product(self, other):
         return np.outer(np.asarray(self), np.asarray(other)).view(QMat)
@@ -125,6 +150,9 @@ def make_qd():
     qd.exp = lambda x: np.exp(x)
     qd.pow = lambda x, y: np.power(x, y)
     qd.sqrt = lambda x: np.sqrt(x)
+    qd.cos = lambda x: math.cos(x)
+    qd.sin = lambda x: math.sin(x)
+    qd.cast = lambda x, dt: dt(x)
     qd.floor = lambda x, dt=None: (np.floor(x).astype(np.int64 if dt is not None else np.float64).view(QMat)
                                    if isinstance(x, np.ndarray) else math.floor(x))
     qd.max = lambda a, b: np.maximum(a, b).view(QMat) if isinstance(a, np.ndarray) or isinstance(b, np.ndarray) else max(a, b)
@@ -132,7 +160,7 @@ def make_qd():
     qd.abs = abs
     qd.select = lambda c, a, b: a if c else b
     qd.svd = _svd
-    qd.math = types.SimpleNamespace(isnan=lambda x: bool(np.isnan(x)))
+    qd.math = types.SimpleNamespace(isnan=lambda x: bool(np.isnan(x)), sqrt=lambda x: math.sqrt(x))
     qd.i32, qd.f32 = np.int64, np.float64
     return qd
 
@@ -240,6 +268,42 @@ def rigid_namespace(ref, ns):
     out["sdf"] = sdf
     out["rigid_funcs"] = rig
     return out
+TOOL_GEOM_FUNCS = ["qd_normalize", "qd_transform_by_quat", "qd_inv_quat", "qd_inv_transform_by_quat", "qd_transform_by_T",
+                   "qd_inv_transform_by_trans_quat", "qd_transform_by_trans_quat", "qd_rotvec_to_quat", "qd_quat_mul",
+                   "qd_transform_quat_by_quat"]
+
+
+def tool_namespace(ref, ns):
+    """Namespace for the tool entity's methods (tool_entity/mesh.py, tool_entity.py): the
+    reference's geometry helpers (genesis/utils/geom.py) as `gu` and by name, executed as written."""
+    tns = dict(ns)
+    extract_functions(os.path.join(ref, "genesis/utils/geom.py"), TOOL_GEOM_FUNCS, tns)
+    tns["gu"] = types.SimpleNamespace(**{k: tns[k] for k in TOOL_GEOM_FUNCS})
+    return tns
+
+
+class _AtomicAdd(ast.NodeTransformer):
+    """`qd.atomic_add(a[i], v)` adds v to the field element a[i] and returns its old value; as a
+    Python call it would receive a copy of a[i], so it becomes `_qd_atomic_add(a, i, v)`."""
+
+    def visit_Call(self, node):
+        self.generic_visit(node)
+        f = node.func
+        if (isinstance(f, ast.Attribute) and f.attr == "atomic_add" and isinstance(f.value, ast.Name)
+                and f.value.id == "qd" and node.args and isinstance(node.args[0], ast.Subscript)):
+            tgt = node.args[0]
+            node.func = ast.Name(id="_qd_atomic_add", ctx=ast.Load())
+            node.args = [tgt.value, tgt.slice] + node.args[1:]
+            tgt.value.ctx = ast.Load()
+        return node
+
+
+def _qd_atomic_add(a, idx, v):
+    old = a[idx]
+    a[idx] = old + v
+    return old
+
+
 class _ValueAssign(ast.NodeTransformer):
     """`a = b` between names copies b, as Quadrants assigns vectors and matrices by value (numpy
     would alias them: `inc = pos; inc[i] += d` must leave pos unchanged)."""
@@ -257,6 +321,7 @@ def _qd_copy(v):
 def extract(path, cls, names, ns):
     """Compile methods `names` of class `cls` in `path` (decorators/annotations removed) into ns."""
     ns.setdefault("_qd_copy", _qd_copy)
+    ns.setdefault("_qd_atomic_add", _qd_atomic_add)
     src = open(path).read()
     tree = ast.parse(src)
     out = {}
@@ -268,7 +333,7 @@ def extract(path, cls, names, ns):
                     fn.returns = None
                     for a in fn.args.args + fn.args.kwonlyargs:
                         a.annotation = None
-                    fn = _ValueAssign().visit(fn)
+                    fn = _AtomicAdd().visit(_ValueAssign().visit(fn))
                     mod = ast.Module(body=[fn], type_ignores=[])
                     code = compile(ast.fix_missing_locations(mod), path, "exec")
                     loc = {}
@@ -320,8 +385,27 @@ def load_reference(ref):
                                  ["_func_collide_with_rigid", "_func_collide_with_rigid_geom",
                                   "_func_collide_in_rigid_geom"], rns)
     F["rigid_funcs"] = rns["rigid_funcs"]
+    F["solver_cpic"] = extract(os.path.join(ref, "genesis/engine/solvers/mpm_solver.py"), "MPMSolver", ["p2g", "g2p"],
+                               rns)
+    F["coupler_cpic"] = extract(os.path.join(ref, "genesis/engine/couplers/legacy_coupler.py"), "LegacyCoupler",
+                                ["mpm_surface_to_particle"], rns)
     F["boundary"] = extract(os.path.join(ref, "genesis/engine/boundaries/boundaries.py"), "CubeBoundary",
                             ["impose_pos_vel"], ns)
+    tns = tool_namespace(ref, ns)
+    tdir = os.path.join(ref, "genesis/engine/entities/tool_entity")
+    F["tool_mesh"] = extract(os.path.join(tdir, "mesh.py"), "Mesh",
+                             ["sdf", "sdf_", "normal", "normal_", "vel_collider", "collide"], tns)
+    F["tool_entity"] = extract(os.path.join(tdir, "tool_entity.py"), "ToolEntity", ["collide", "advect", "copy_frame"],
+                               tns)
+    F["floor"] = extract(os.path.join(ref, "genesis/engine/boundaries/boundaries.py"), "FloorBoundary", ["impose_pos"],
+                         ns)
+    F["hasher"] = extract(os.path.join(ref, "genesis/utils/geom.py"), "SpatialHasher",
+                          ["compute_reordered_idx", "pos_to_grid", "grid_to_slot", "pos_to_slot"], ns)
+    F["constraints"] = extract(os.path.join(ref, "genesis/engine/solvers/mpm_solver.py"), "MPMSolver",
+                               ["_kernel_set_particle_constraints", "_kernel_remove_particle_constraints",
+                                "apply_particle_constraints"], tns)
+    F["coupler_tool"] = extract(os.path.join(ref, "genesis/engine/couplers/legacy_coupler.py"), "LegacyCoupler",
+                                ["_func_mpm_tool"], ns)
     return F
 
 
@@ -408,10 +492,20 @@ def gen_materials(F, rng):
 
 
 # ----------------------------------------------------------------------------- one scene, full substeps
-def gen_substeps(F, rng, ffs=(), n_steps=10, rigid=None):
+def gen_substeps(F, rng, ffs=(), n_steps=10, rigid=None, tool=None, cpic=False, coupled=None, constraints=None):
     """A 9-material scene on a 17^3 grid advanced by the reference's substep code; `ffs` are
     reference force-field objects applied in its grid op (legacy_coupler.py:376-378); `rigid`
-    (make_rigid_standins) couples the grid op with rigid geoms (legacy_coupler.py:389-403)."""
+    (make_rigid_standins) couples the grid op with rigid geoms (legacy_coupler.py:389-403); `tool`
+    (make_tool_standin) with a tool entity (legacy_coupler.py:385-387), which advects before the
+    grid op (ToolSolver.substep_pre_coupling) and copies its frame f+1 to f after the substep;
+    `cpic` (with `rigid`) turns on MPMOptions.enable_CPIC: the coupler's preprocess
+    (mpm_surface_to_particle) before P2G and the separated-cell branches of p2g and g2p;
+    `coupled` (make_coupled_standin, keys "sph" / "pbd") couples the grid op with another solver's
+    particles through its spatial hash (legacy_coupler.py:404-498); `constraints`
+    (CONSTRAINT_SETS) attaches particles to kinematic links before the first substep
+    (_kernel_set_particle_constraints), moves the links before every substep, removes some
+    constraints before one of them (_kernel_remove_particle_constraints) and applies the springs
+    after every G2P (apply_particle_constraints, mpm_solver.py:538-540)."""
     # domain [0, 0.25]^3 at density 64 -> 17^3 nodes, boundary [3/64, 0.25 - 3/64]
     density, dt = 64.0, 2e-4
     lower, upper = np.zeros(3), np.full(3, 0.25)
@@ -478,6 +572,31 @@ def gen_substeps(F, rng, ffs=(), n_steps=10, rigid=None):
         bind(coupler, F["coupler_rigid"])
         grid_op_args = tuple(rigid[k] for k in ("geoms_state", "geoms_info", "links_state", "rigid_global_info",
                                                 "sdf_info", "collider_static_config"))
+    for kind, other in (coupled or {}).items():  # stencil sizes as LegacyCoupler.build computes them
+        setattr(coupler, f"_mpm_{kind}", True)
+        setattr(coupler, f"{kind}_solver", other)
+        setattr(coupler, f"mpm_{kind}_stencil_size", int(np.floor(dx / other.sh.cell_size) + 2))
+    if constraints is not None:
+        solver.particle_constraints = StructField((n, 1), dict(is_constrained=(), target_pos=(3,), stiffness=(),
+                                                                link_idx=(), link_local_pos=(3,)))
+        solver.particle_constraints._d["is_constrained"] = np.zeros((n, 1), np.int64)
+        solver.particle_constraints._d["link_idx"] = np.full((n, 1), -1, np.int64)
+        bind(solver, F["constraints"])
+        links = types.SimpleNamespace(pos=constraints["link_pos"][0].copy().view(QMat),
+                                      quat=constraints["link_quat"][0].copy().view(QMat))
+    if cpic:
+        G = rigid["rigid_solver"].n_geoms
+        solver._enable_CPIC = True
+        solver.n_particles = n
+        solver.sim = types.SimpleNamespace(rigid_solver=rigid["rigid_solver"], coupler=coupler)
+        solver._coupler = coupler
+        bind(solver, F["solver_cpic"])
+        coupler.cpic_flag = np.zeros((n, 3, 3, 3, 1), np.int64)
+        coupler.mpm_rigid_normal = np.zeros((n, G, 1, 3)).view(QMat)
+        bind(coupler, F["coupler_cpic"])
+    if tool is not None:
+        coupler.tool_solver = tool["tool_solver"]
+        bind(coupler, F["coupler_tool"])
 
     P, I, G = solver.particles._d, solver.particles_info._d, solver.grid._d
     P["pos"][0, :, 0], P["vel"][0, :, 0], P["C"][0, :, 0], P["F"][0, :, 0] = pos, vel, C, Fm
@@ -488,20 +607,46 @@ def gen_substeps(F, rng, ffs=(), n_steps=10, rigid=None):
     def snapshot():
         return {k: P[k][0, :, 0].copy() for k in ("pos", "vel", "C", "F", "Jp")}
 
+    if constraints is not None:  # attached to the initial state
+        for start, mask, stiffness, link in constraints["sets"]:
+            lk = max(link, 0)
+            solver._kernel_set_particle_constraints(0, mask, start, stiffness, link, links.pos[lk], links.quat[lk])
+
     out = {"in/" + k: v for k, v in snapshot().items()}
     out.update({"in/mat": mat, "in/actu": actu, "in/mdir": mdir})
     for step in range(n_steps):
         for k in G:
             G[k][...] = 0  # reset_grid_and_grad
+        if constraints is not None:
+            links.pos[...], links.quat[...] = constraints["link_pos"][step + 1], constraints["link_quat"][step + 1]
+            if step == constraints["remove_before"]:
+                start, mask = constraints["remove"]
+                solver._kernel_remove_particle_constraints(mask, start)
+        if cpic:  # LegacyCoupler.preprocess
+            coupler.mpm_surface_to_particle(0, rigid["geoms_state"], rigid["geoms_info"], rigid["sdf_info"],
+                                            rigid["rigid_global_info"], rigid["collider_static_config"])
         solver.compute_F_tmp(0)
         solver.svd(0)
-        solver.p2g(0, None, None, None, None, None, None)
+        if cpic:
+            solver.p2g(0, rigid["geoms_state"], rigid["geoms_info"], rigid["links_state"], rigid["rigid_global_info"],
+                       rigid["sdf_info"], rigid["collider_static_config"])
+        else:
+            solver.p2g(0, None, None, None, None, None, None)
+        if tool is not None:
+            tool["entity"].advect(0)
         if step == 0:
             out["grid1"] = np.concatenate([G["vel_in"][0, ..., 0, :], G["mass"][0, ..., 0, None]], -1).copy()
         coupler.mpm_grid_op(0, 0.0, *grid_op_args)
-        solver.g2p(0, None, None, None)
+        if cpic:
+            solver.g2p(0, rigid["geoms_info"], rigid["links_state"], rigid["rigid_global_info"])
+        else:
+            solver.g2p(0, None, None, None)
+        if constraints is not None:
+            solver.apply_particle_constraints(0, links)
         for k in ("pos", "vel", "C", "F", "Jp"):  # copy_frame(1 -> 0)
             P[k][0] = P[k][1]
+        if tool is not None:
+            tool["entity"].copy_frame(1, 0)
         if step == 0:
             out.update({"out1/" + k: v for k, v in snapshot().items()})
     out.update({f"out{n_steps}/" + k: v for k, v in snapshot().items()})
@@ -603,19 +748,32 @@ RIGID_GEOMS = [
     ("box", (0.17, 0.1, 0.1), _quat_about((0, 0, 1), 20.0), (0.03, 0.02, 0.025), (0.0, -0.1, 0.0), (0.5, 0.0, 0.0),
      0.2, 0.002, 0.2),
 ]
+# the CPIC scene swaps the box for a thin tilted plate (an ellipsoid SDF, smooth gradients): the
+# box's face normals are exactly perpendicular across its edges, so CPIC's side test
+# (normal . normal < 0) would compare rounding noise against zero there
+CPIC_GEOMS = RIGID_GEOMS[:2] + [
+    ("plate", (0.125, 0.125, 0.12), _quat_about((0, 1, 0), 10.0), (0.035, 0.035, 0.005), (0.0, 0.05, -0.1),
+     (0.0, 0.0, 0.3), 0.2, 0.002, 0.1),
+]
 BOX_GRID = dict(res=24, lower=-0.05, upper=0.05)
 
 
-def box_grid(half):
-    """The box geom's SDF grid as the rigid solver stores it (values and mesh-frame gradients on a
+def plate_sdf(p, half):
+    """Scaled ellipsoid distance (|p / half| - 1) * min(half): zero on the ellipsoid, smooth."""
+    half = np.asarray(half)
+    return (np.linalg.norm(p / half, axis=-1) - 1.0) * half.min()
+
+
+def box_grid(half, fn=box_sdf):
+    """The SDF geom's grid as the rigid solver stores it (values and mesh-frame gradients on a
     res^3 lattice, T_mesh_to_sdf mapping mesh coordinates to voxel indices), in float32."""
     res, lo, hi = BOX_GRID["res"], BOX_GRID["lower"], BOX_GRID["upper"]
     h = (hi - lo) / (res - 1)
     ax = lo + h * np.arange(res)
     pts = np.stack(np.meshgrid(ax, ax, ax, indexing="ij"), -1).reshape(-1, 3)
-    val = box_sdf(pts, np.asarray(half))
+    val = fn(pts, np.asarray(half))
     eps = 1e-6
-    grad = np.stack([(box_sdf(pts + eps * e, half) - box_sdf(pts - eps * e, half)) / (2 * eps) for e in np.eye(3)], -1)
+    grad = np.stack([(fn(pts + eps * e, half) - fn(pts - eps * e, half)) / (2 * eps) for e in np.eye(3)], -1)
     grad /= np.maximum(np.linalg.norm(grad, axis=-1, keepdims=True), 1e-12)
     T = np.eye(4)
     T[:3, :3] /= h
@@ -624,23 +782,29 @@ def box_grid(half):
             float(val.astype(np.float32).max()))
 
 
-def make_rigid_standins(F, dt):
-    """The rigid solver's data the coupler reads, for RIGID_GEOMS (one env, one link per geom)."""
-    G = len(RIGID_GEOMS)
-    types_ = {"sphere": GEOM_TYPE.SPHERE, "plane": GEOM_TYPE.PLANE, "box": GEOM_TYPE.BOX}
+def geom_grid(geom):
+    """The grid of the SDF geom (a "box" or a "plate") of a geom list."""
+    return box_grid(geom[3], box_sdf if geom[0] == "box" else plate_sdf)
+
+
+def make_rigid_standins(F, dt, geoms=RIGID_GEOMS):
+    """The rigid solver's data the coupler reads, for `geoms` (one env, one link per geom; the
+    last geom is the one given by an SDF grid)."""
+    G = len(geoms)
+    types_ = {"sphere": GEOM_TYPE.SPHERE, "plane": GEOM_TYPE.PLANE, "box": GEOM_TYPE.BOX, "plate": GEOM_TYPE.MESH}
     data = np.zeros((G, 7))
     gpos = np.zeros((G, 1, 3)).view(QMat)
     gquat = np.zeros((G, 1, 4)).view(QMat)
     cd_vel = np.zeros((G, 1, 3)).view(QMat)
     cd_ang = np.zeros((G, 1, 3)).view(QMat)
     com = np.zeros((G, 1, 3)).view(QMat)
-    for i, (t, pos, quat, d, v, w, *_rest) in enumerate(RIGID_GEOMS):
+    for i, (t, pos, quat, d, v, w, *_rest) in enumerate(geoms):
         data[i, : len(d)] = d
         gpos[i, 0], gquat[i, 0], cd_vel[i, 0], cd_ang[i, 0], com[i, 0] = pos, quat, v, w, pos
     geoms_info = types.SimpleNamespace(
-        needs_coup=[1] * G, type=[types_[g[0]] for g in RIGID_GEOMS], data=[QMat(r) for r in data],
-        coup_friction=[g[6] for g in RIGID_GEOMS], coup_softness=[g[7] for g in RIGID_GEOMS],
-        coup_restitution=[g[8] for g in RIGID_GEOMS], link_idx=list(range(G)))
+        needs_coup=[1] * G, type=[types_[g[0]] for g in geoms], data=[QMat(r) for r in data],
+        coup_friction=[g[6] for g in geoms], coup_softness=[g[7] for g in geoms],
+        coup_restitution=[g[8] for g in geoms], link_idx=list(range(G)))
     geoms_state = types.SimpleNamespace(pos=gpos, quat=gquat)
     links_state = types.SimpleNamespace(cd_vel=cd_vel, cd_ang=cd_ang, root_COM=com,
                                         cfrc_coupling_vel=np.zeros((G, 1, 3)).view(QMat),
@@ -648,7 +812,7 @@ def make_rigid_standins(F, dt):
     rgi = types.SimpleNamespace(substep_dt=_FieldStandin(np.float64), EPS=_FieldStandin(np.float64))
     rgi.substep_dt[None] = dt
     rgi.EPS[None] = EPS32
-    val, grad, T, h, smax = box_grid(RIGID_GEOMS[2][3])
+    val, grad, T, h, smax = geom_grid(geoms[2])
     res = QMat(np.array(val.shape), dtype=np.int64)
     zero_T = np.eye(4)
     sdf_geoms = types.SimpleNamespace(T_mesh_to_sdf=[QMat(zero_T), QMat(zero_T), QMat(T)], sdf_res=[res, res, res],
@@ -667,20 +831,173 @@ def make_rigid_standins(F, dt):
                 rigid_solver=rigid_solver)
 
 
-def gen_rigid(F, rng):
-    rigid = make_rigid_standins(F, 2e-4)
-    out = gen_substeps(F, rng, n_steps=3, rigid=rigid)
+def gen_rigid(F, rng, cpic=False):
+    geoms = CPIC_GEOMS if cpic else RIGID_GEOMS
+    rigid = make_rigid_standins(F, 2e-4, geoms)
+    out = gen_substeps(F, rng, n_steps=3, rigid=rigid, cpic=cpic)
     ls = rigid["links_state"]
     out["link_force"] = np.asarray(ls.cfrc_coupling_vel)[:, 0].copy()
     out["link_torque"] = np.asarray(ls.cfrc_coupling_ang)[:, 0].copy()
-    out["geom_types"] = np.array([g[0] for g in RIGID_GEOMS])
-    for i, g in enumerate(RIGID_GEOMS):
+    out["geom_types"] = np.array([g[0] for g in geoms])
+    for i, g in enumerate(geoms):
         out[f"geom{i}/pos"], out[f"geom{i}/quat"], out[f"geom{i}/data"] = np.array(g[1]), np.array(g[2]), np.array(g[3])
         out[f"geom{i}/lin_vel"], out[f"geom{i}/ang_vel"] = np.array(g[4]), np.array(g[5])
         out[f"geom{i}/coup"] = np.array(g[6:9])
-    val, grad, T, h, smax = box_grid(RIGID_GEOMS[2][3])
-    out["box_sdf/values"], out["box_sdf/grads"], out["box_sdf/T"] = val, grad, T
-    out["box_sdf/cell_size"], out["box_sdf/sdf_max"] = np.array(h), np.array(smax)
+    val, grad, T, h, smax = geom_grid(geoms[2])
+    out["sdf_grid/values"], out["sdf_grid/grads"], out["sdf_grid/T"] = val, grad, T
+    out["sdf_grid/cell_size"], out["sdf_grid/sdf_max"] = np.array(h), np.array(smax)
+    return out
+
+
+# ----------------------------------------------------------------------------- tool coupling
+# a rotated box tool (values-only SDF grid) translating down onto its floor height and spinning
+TOOL = dict(pos=(0.11, 0.12, 0.1203), quat=_quat_about((1, 1, 0), 25.0), vel=(0.2, -0.1, -0.5), ang=(0.0, 1.0, 2.0),
+            half=(0.03, 0.02, 0.025), friction=0.3, coup_softness=0.002, floor_height=0.12015)
+
+
+class _VoxelField:
+    """qd.field stand-in indexed by an integer vector (Mesh.sdf_voxels[voxel_pos])."""
+
+    def __init__(self, a):
+        self.a = a
+
+    def __getitem__(self, idx):
+        return float(self.a[_flat_index(idx)])
+
+
+class _ScalarMatrixField:
+    """0-d qd.Matrix.field stand-in (Mesh.T_mesh_to_sdf[None])."""
+
+    def __init__(self, m):
+        self.m = QMat(m)
+
+    def __getitem__(self, idx):
+        return self.m.copy().view(QMat)
+
+
+def make_tool_standin(F, dt):
+    """One tool entity (ToolEntity with its Mesh, one env, frames 0 and 1) on the tool solver's
+    FloorBoundary, for TOOL."""
+    val = box_grid(TOOL["half"])[0]
+    T = box_grid(TOOL["half"])[2]
+    ent = types.SimpleNamespace()
+    for k, v in (("pos", TOOL["pos"]), ("quat", TOOL["quat"]), ("vel", TOOL["vel"]), ("ang", TOOL["ang"])):
+        a = np.zeros((2, 1, len(v))).view(QMat)
+        a[0, 0] = v
+        setattr(ent, k, a)
+    floor = types.SimpleNamespace(height=TOOL["floor_height"])
+    bind(floor, F["floor"])
+    ent._sim = types.SimpleNamespace(_B=1)
+    ent._solver = ent.solver = types.SimpleNamespace(boundary=floor, substep_dt=dt)
+    ent.material = types.SimpleNamespace(collision=True, coup_softness=TOOL["coup_softness"])
+    mesh = types.SimpleNamespace(entity=ent, material=ent.material, collision=True, friction=TOOL["friction"],
+                                 sdf_res=val.shape[0], sdf_voxels=_VoxelField(val.astype(np.float64)),
+                                 T_mesh_to_sdf=_ScalarMatrixField(T))
+    bind(mesh, F["tool_mesh"])
+    ent.mesh = mesh
+    bind(ent, F["tool_entity"])
+    return dict(entity=ent, tool_solver=types.SimpleNamespace(is_active=True, entities=[ent]))
+
+
+def gen_tool(F, rng, n_steps=4):
+    tool = make_tool_standin(F, 2e-4)
+    out = gen_substeps(F, rng, n_steps=n_steps, tool=tool)
+    ent = tool["entity"]
+    out["n_steps"] = np.array(n_steps)
+    out["tool/pos_out"], out["tool/quat_out"] = np.asarray(ent.pos[0, 0]).copy(), np.asarray(ent.quat[0, 0]).copy()
+    for k in ("pos", "quat", "vel", "ang"):
+        out[f"tool/{k}"] = np.asarray(TOOL[k], np.float64)
+    for k in ("friction", "coup_softness", "floor_height"):
+        out[f"tool/{k}"] = np.array(TOOL[k])
+    val, _, T, h, smax = box_grid(TOOL["half"])
+    out["tool_sdf/values"], out["tool_sdf/T"] = val, T
+    out["tool_sdf/cell_size"], out["tool_sdf/sdf_max"] = np.array(h), np.array(smax)
+    return out
+
+
+# ----------------------------------------------------------------------------- SPH / PBD coupling
+class _SoAField(StructField):
+    """A struct field read both ways the coupler reads the other solvers' particles:
+    `f.pos[i, b]` (member array) and `f[i, b].vel = ...` (write-through record)."""
+
+    def __getattr__(self, k):
+        return self._d[k].view(QMat)
+
+
+# (kind, block centre the set is spread around, hash cell size, hash grid resolution, mass)
+COUPLED_SETS = [("sph", (0.08, 0.125, 0.17), 0.01, (26, 26, 26), 4e-3),
+                ("pbd", (0.17, 0.125, 0.17), 0.02, (13, 13, 13), 6e-3)]
+
+
+def make_coupled_standin(F, rng, centre, cell_size, grid_res, mass, n=60):
+    """Another solver's particles as the coupler sees them: reordered by the reference's own
+    SpatialHasher (genesis/utils/geom.py) into its slots, with the slot tables it builds."""
+    pos = np.asarray(centre) + rng.uniform(-0.012, 0.012, size=(n, 3))
+    vel = rng.normal(scale=0.1, size=(n, 3))
+    m = np.full(n, mass) * rng.uniform(0.8, 1.2, size=n)
+    free = (rng.uniform(size=n) < 0.8).astype(np.int64)
+    sh = types.SimpleNamespace(cell_size=cell_size, grid_res=grid_res, n_slots=int(np.prod(grid_res)), _B=1)
+    sh.slot_size = np.zeros((sh.n_slots, 1), np.int64)
+    sh.slot_start = np.zeros((sh.n_slots, 1), np.int64)
+    sh.cur_cnt = np.zeros(1, np.int64)
+    bind(sh, F["hasher"])
+    order = np.zeros((n, 1), np.int64)
+    # its arguments are fields (passed by reference), so the method is called unwrapped
+    types.MethodType(F["hasher"]["compute_reordered_idx"], sh)(n, pos[:, None].view(QMat), np.ones((n, 1), np.int64),
+                                                              order)
+    order = order[:, 0]
+    P = _SoAField((n, 1), dict(pos=(3,), vel=(3,), free=()))
+    I = _SoAField((n, 1), dict(mass=()))
+    P._d["pos"][order, 0], P._d["vel"][order, 0], P._d["free"][order, 0], I._d["mass"][order, 0] = pos, vel, free, m
+    other = types.SimpleNamespace(sh=sh, particles_reordered=P, particles_info_reordered=I)
+    return other, dict(pos=pos, vel=vel, mass=m, free=free, order=order)
+
+
+def gen_coupled(F, rng, n_steps=4):
+    coupled, sets = {}, {}
+    for kind, centre, cell, res, mass in COUPLED_SETS:
+        coupled[kind], sets[kind] = make_coupled_standin(F, rng, centre, cell, res, mass)
+    out = gen_substeps(F, rng, n_steps=n_steps, coupled=coupled)
+    out["n_steps"] = np.array(n_steps)
+    for kind, st in sets.items():
+        for k in ("pos", "vel", "mass", "free"):
+            out[f"{kind}/{k}"] = st[k]
+        out[f"{kind}/vel_out"] = coupled[kind].particles_reordered._d["vel"][st["order"], 0].copy()
+    return out
+
+
+# ----------------------------------------------------------------------------- particle constraints
+# (first particle, particle count) of the two constrained blocks; (stiffness, link) of each set
+CONSTRAINT_SETS = [((192, 64), 300.0, 0), ((384, 64), 600.0, 1), ((448, 64), 150.0, -1)]
+
+
+def gen_constraints(F, rng, n_steps=5):
+    """Particles of three blocks attached to two moving links and (link -1) to their own start
+    positions, every other particle of each block; half of the first set released before the
+    fourth substep."""
+    L = 2
+    link_pos = np.zeros((n_steps + 1, L, 1, 3))
+    link_quat = np.zeros((n_steps + 1, L, 1, 4))
+    for k in range(n_steps + 1):
+        link_pos[k, 0, 0] = (0.125 + 0.001 * k, 0.1, 0.1 - 0.0005 * k)
+        link_pos[k, 1, 0] = (0.1, 0.15, 0.15 + 0.0008 * k)
+        link_quat[k, 0, 0] = _quat_about((0, 0, 1), 5.0 + 2.0 * k)
+        link_quat[k, 1, 0] = _quat_about((1, 0.5, 0), -3.0 * k)
+    sets = []
+    for (start, count), stiffness, link in CONSTRAINT_SETS:
+        mask = np.zeros((1, count), np.int64)
+        mask[0, ::2] = 1
+        sets.append((start, mask, stiffness, link))
+    rm = np.zeros((1, 64), np.int64)
+    rm[0, :32] = 1
+    cons = dict(link_pos=link_pos, link_quat=link_quat, sets=sets, remove_before=3, remove=(192, rm))
+    out = gen_substeps(F, rng, n_steps=n_steps, constraints=cons)
+    out["n_steps"] = np.array(n_steps)
+    out["link_pos"], out["link_quat"] = link_pos[:, :, 0], link_quat[:, :, 0]
+    for i, (start, mask, stiffness, link) in enumerate(sets):
+        out[f"set{i}/start"], out[f"set{i}/mask"] = np.array(start), mask[0]
+        out[f"set{i}/stiffness"], out[f"set{i}/link"] = np.array(stiffness), np.array(link)
+    out["remove/start"], out["remove/mask"], out["remove/before"] = np.array(192), rm[0], np.array(3)
     return out
 
 
@@ -695,6 +1012,13 @@ def main():
     np.savez_compressed(os.path.join(HERE, "force_fields.npz"),
                         **gen_force_fields(F, ref, np.random.default_rng(20261205)))
     np.savez_compressed(os.path.join(HERE, "rigid_coupling.npz"), **gen_rigid(F, np.random.default_rng(20261206)))
+    np.savez_compressed(os.path.join(HERE, "tool_coupling.npz"), **gen_tool(F, np.random.default_rng(20261207)))
+    np.savez_compressed(os.path.join(HERE, "cpic_coupling.npz"),
+                        **gen_rigid(F, np.random.default_rng(20261208), cpic=True))
+    np.savez_compressed(os.path.join(HERE, "particle_coupling.npz"),
+                        **gen_coupled(F, np.random.default_rng(20261209)))
+    np.savez_compressed(os.path.join(HERE, "particle_constraints.npz"),
+                        **gen_constraints(F, np.random.default_rng(20261210)))
     print("wrote", os.listdir(HERE))
 
 

@@ -119,8 +119,8 @@ def _golden_colliders(O, g):
         elif t == "plane":
             c = Collider("plane", normal=tuple(data), **kw)
         else:
-            grid = SDFGrid(values=g["box_sdf/values"], T_mesh_to_sdf=g["box_sdf/T"], grads=g["box_sdf/grads"],
-                           cell_size=float(g["box_sdf/cell_size"]), sdf_max=float(g["box_sdf/sdf_max"]))
+            grid = SDFGrid(values=g["sdf_grid/values"], T_mesh_to_sdf=g["sdf_grid/T"], grads=g["sdf_grid/grads"],
+                           cell_size=float(g["sdf_grid/cell_size"]), sdf_max=float(g["sdf_grid/sdf_max"]))
             c = Collider("sdf", sdf=grid, **kw)
             sid = O.add_sdf_grid(grid.values, grid.grads, grid.T_mesh_to_sdf, grid.cell_size, grid.sdf_max)
         out.append((c, sid))
@@ -154,3 +154,148 @@ def test_rigid_coupling_matches_reference_code(oracle):
     assert np.all(np.abs(g["link_force"]).max(1) > 0)
     assert np.abs(forces[:, :3] + g["link_force"]).max() <= 1e-6 * np.abs(g["link_force"]).max()
     assert np.abs(forces[:, 3:] + g["link_torque"]).max() <= 1e-6 * np.abs(g["link_torque"]).max()
+
+
+def _golden_tool(O, g):
+    """The facade's tool collider for tests/golden/tool_coupling.npz (a rotated box given by a
+    values-only SDF grid), the grid registered with the oracle."""
+    from genesis_gb300.coupling import SDFGrid, tool
+
+    grid = SDFGrid(values=g["tool_sdf/values"], T_mesh_to_sdf=g["tool_sdf/T"], cell_size=float(g["tool_sdf/cell_size"]),
+                   sdf_max=float(g["tool_sdf/sdf_max"]))
+    c = tool(grid, pos=tuple(g["tool/pos"]), quat=tuple(g["tool/quat"]), vel=tuple(g["tool/vel"]),
+             ang=tuple(g["tool/ang"]), friction=float(g["tool/friction"]), coup_softness=float(g["tool/coup_softness"]),
+             floor_height=float(g["tool/floor_height"]))
+    return c, O.add_sdf_grid(grid.values, None, grid.T_mesh_to_sdf, grid.cell_size, grid.sdf_max)
+
+
+def test_tool_coupling_matches_reference_code(oracle):
+    """The oracle's tool coupling (voxel-SDF trilinear value, finite-difference normal, collider
+    velocity from the next pose, friction and influence) and tool motion (advect with the floor
+    boundary) against substeps of the reference's own Mesh, ToolEntity and geometry code
+    (tests/golden/tool_coupling.npz): particle state and the tool's final pose."""
+    g = np.load(os.path.join(GOLDEN, "tool_coupling.npz"))
+    n_steps = int(g["n_steps"])
+    sc, mats, st = _oracle_inputs(oracle, g)
+    oracle.clear_sdf_grids()
+    c, sid = _golden_tool(oracle, g)
+    oracle.set_colliders([c.to_c(sid)])
+    try:
+        out, _, _ = oracle.run(sc, mats, st, n_steps)
+        pose = oracle.collider_poses(1)[0]
+    finally:
+        oracle.set_colliders([])
+        oracle.clear_sdf_grids()
+    plain, _, _ = oracle.run(sc, mats, st, n_steps)
+    assert np.abs(plain["vel"] - g[f"out{n_steps}/vel"]).max() > 1e-3  # the tool acts on this scene
+    assert g["tool/pos_out"][2] == g["tool/floor_height"]  # the floor stopped the tool
+    assert np.abs(pose[:3] - g["tool/pos_out"]).max() <= 1e-12
+    assert np.abs(pose[3:] - g["tool/quat_out"]).max() <= 1e-12
+    for k in ("pos", "vel", "C", "F", "Jp"):
+        ref = g[f"out{n_steps}/" + k]
+        assert np.abs(out[k] - ref).max() <= 1e-11 * max(1.0, np.abs(ref).max()), (k, np.abs(out[k] - ref).max())
+
+
+def test_cpic_matches_reference_code(oracle):
+    """The oracle's CPIC (particle-side normals updated before P2G, cells across a geom skipped in
+    P2G, their velocity replaced by the particle's own rigid collision in G2P, with its reaction on
+    the link) against three substeps of the reference's own p2g/g2p with enable_CPIC and the
+    coupler's mpm_surface_to_particle (tests/golden/cpic_coupling.npz, the rigid-coupling geoms)."""
+    g = np.load(os.path.join(GOLDEN, "cpic_coupling.npz"))
+    sc, mats, st = _oracle_inputs(oracle, g)
+    oracle.clear_sdf_grids()
+    cols = _golden_colliders(oracle, g)
+    oracle.set_colliders([c.to_c(sid) for c, sid in cols])
+    try:
+        plain, _, _ = oracle.run(sc, mats, st, 3)
+        oracle.set_colliders([c.to_c(sid) for c, sid in cols])
+        oracle.set_cpic(True)
+        out, _, _ = oracle.run(sc, mats, st, 3)
+        forces = oracle.collider_forces(len(cols))
+    finally:
+        oracle.set_cpic(False)
+        oracle.set_colliders([])
+        oracle.clear_sdf_grids()
+    assert np.abs(plain["vel"] - g["out3/vel"]).max() > 1e-3  # CPIC acts on this scene
+    for k in ("pos", "vel", "C", "F", "Jp"):
+        ref = g["out3/" + k]
+        assert np.abs(out[k] - ref).max() <= 1e-7 * max(1.0, np.abs(ref).max()), (k, np.abs(out[k] - ref).max())
+    assert np.abs(forces[:, :3] + g["link_force"]).max() <= 1e-6 * np.abs(g["link_force"]).max()
+    assert np.abs(forces[:, 3:] + g["link_torque"]).max() <= 1e-6 * np.abs(g["link_torque"]).max()
+
+
+def test_particle_coupling_matches_reference_code(oracle):
+    """The oracle's SPH and PBD grid coupling (a node takes the mean velocity of the other solver's
+    particles within dx/2 and gives the momentum change back to them; PBD: free particles only)
+    against substeps of the reference's own grid op, with the particle sets ordered and looked up
+    through the reference's SpatialHasher (tests/golden/particle_coupling.npz)."""
+    g = np.load(os.path.join(GOLDEN, "particle_coupling.npz"))
+    n_steps = int(g["n_steps"])
+    sc, mats, st = _oracle_inputs(oracle, g)
+    try:
+        oracle.set_coupled(0, g["sph/pos"], g["sph/vel"], g["sph/mass"])
+        oracle.set_coupled(1, g["pbd/pos"], g["pbd/vel"], g["pbd/mass"], free=g["pbd/free"])
+        out, _, _ = oracle.run(sc, mats, st, n_steps)
+        v_sph, v_pbd = oracle.coupled_velocities(0), oracle.coupled_velocities(1)
+    finally:
+        oracle.set_coupled(0)
+        oracle.set_coupled(1)
+    plain, _, _ = oracle.run(sc, mats, st, n_steps)
+    assert np.abs(plain["vel"] - g[f"out{n_steps}/vel"]).max() > 1e-3  # the sets act on this scene
+    assert np.abs(g["sph/vel_out"] - g["sph/vel"]).max() > 1e-2 and np.abs(g["pbd/vel_out"] - g["pbd/vel"]).max() > 1e-2
+    for k in ("pos", "vel", "C", "F", "Jp"):
+        ref = g[f"out{n_steps}/" + k]
+        assert np.abs(out[k] - ref).max() <= 1e-11 * max(1.0, np.abs(ref).max()), (k, np.abs(out[k] - ref).max())
+    assert np.abs(v_sph - g["sph/vel_out"]).max() <= 1e-12
+    assert np.abs(v_pbd - g["pbd/vel_out"]).max() <= 1e-12
+
+
+def _quat_rot(q, v):
+    w, x, y, z = q
+    R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                  [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                  [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+    return v @ R.T
+
+
+def test_particle_constraints_restatement_matches_reference_code(oracle):
+    """The spring update the GPU parity tests check against (attachment offset kept in the link
+    frame, target following the link, dv = dt (-k (x - target) - 2 sqrt(k m) v) / m after G2P,
+    link -1: the start position, released particles untouched), applied between single oracle
+    substeps, against the reference's own constraint kernels (tests/golden/particle_constraints.npz)."""
+    g = np.load(os.path.join(GOLDEN, "particle_constraints.npz"))
+    n_steps = int(g["n_steps"])
+    sc, mats, st = _oracle_inputs(oracle, g)
+    dt, p_size = g["scene"][0], g["scene"][2]
+    m = p_size ** 3 * g["material_params"][:, 9][g["in/mat"]]
+    n = len(st["pos"])
+    k = np.zeros(n)
+    link = np.full(n, -2)
+    local = np.zeros((n, 3))
+    target = np.zeros((n, 3))
+    for i in range(3):
+        start, mask = int(g[f"set{i}/start"]), g[f"set{i}/mask"].astype(bool)
+        idx = start + np.nonzero(mask)[0]
+        li = int(g[f"set{i}/link"])
+        k[idx], link[idx], target[idx] = g[f"set{i}/stiffness"], li, st["pos"][idx]
+        lp, lq = g["link_pos"][0, max(li, 0)], g["link_quat"][0, max(li, 0)]
+        local[idx] = _quat_rot(lq * np.array([1, -1, -1, -1]), st["pos"][idx] - lp)
+    st = dict(st)
+    for step in range(n_steps):
+        if step == int(g["remove/before"]):
+            idx = int(g["remove/start"]) + np.nonzero(g["remove/mask"])[0]
+            link[idx] = -2
+        out, _, _ = oracle.run(sc, mats, st, 1)
+        for li in (0, 1):
+            sel = link == li
+            target[sel] = _quat_rot(g["link_quat"][step + 1, li], local[sel]) + g["link_pos"][step + 1, li]
+        sel = link >= -1
+        v = out["vel"]
+        v[sel] += dt * (-k[sel, None] * (out["pos"][sel] - target[sel]) - 2 * np.sqrt(k[sel] * m[sel])[:, None]
+                        * v[sel]) / m[sel, None]
+        st.update({key: out[key] for key in ("pos", "vel", "C", "F", "Jp")})
+    plain, _, _ = oracle.run(sc, mats, _oracle_inputs(oracle, g)[2], n_steps)
+    assert np.abs(plain["vel"] - g[f"out{n_steps}/vel"]).max() > 1e-2  # the springs act on this scene
+    for key in ("pos", "vel", "C", "F", "Jp"):
+        ref = g[f"out{n_steps}/" + key]
+        assert np.abs(st[key] - ref).max() <= 1e-10 * max(1.0, np.abs(ref).max()), (key, np.abs(st[key] - ref).max())

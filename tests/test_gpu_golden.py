@@ -2,7 +2,8 @@
 
 Float32 kernels vs float64 reference execution, same inputs: grid mass/momentum after the
 first P2G within 1e-5 relative (L2); particle state after 1 and 10 substeps, after 5 substeps
-with force fields and after 3 with rigid coupling within the float32 tolerances stated below."""
+with force fields, after 3 with rigid coupling (with and without CPIC) and after 4 with a tool
+within the float32 tolerances stated below."""
 
 import os
 
@@ -113,13 +114,25 @@ def test_rigid_coupling_matches_reference(ctx, oracle):
     of the reference's own rigid-collision, SDF and geometry code (tests/golden/rigid_coupling.npz):
     particle state, and the reaction on each geom (the reference accumulates it into the link's
     cfrc_coupling with the opposite sign)."""
+    _check_rigid_golden(ctx, oracle, "rigid_coupling.npz", cpic=False)
+
+
+def test_cpic_matches_reference(ctx, oracle):
+    """CPIC in the CUDA P2G and G2P (particle-side normals, cells across a geom skipped, their
+    velocity replaced by the particle's own rigid collision) against three substeps of the
+    reference's own p2g/g2p with enable_CPIC (tests/golden/cpic_coupling.npz: a sphere, a tilted
+    plane and a thin tilted plate through one of the blocks)."""
+    _check_rigid_golden(ctx, oracle, "cpic_coupling.npz", cpic=True)
+
+
+def _check_rigid_golden(ctx, oracle, fixture, cpic):
     import ctypes
 
     from genesis_gb300 import _lib
     from test_golden_oracle import _golden_colliders
 
     c, _, n = ctx
-    gr = np.load(os.path.join(GOLDEN, "rigid_coupling.npz"))
+    gr = np.load(os.path.join(GOLDEN, fixture))
     oracle.clear_sdf_grids()
     cols = _golden_colliders(oracle, gr)
     oracle.clear_sdf_grids()
@@ -136,6 +149,8 @@ def test_rigid_coupling_matches_reference(ctx, oracle):
                    float(g.cell_size), float(g.sdf_max), ctypes.byref(out))
             sid = out.value
         recs.append(col.to_c(sid))
+    if cpic:
+        c.call("mpm_enable_cpic", len(recs), c.stream)
     arr = (_lib.MpmCollider * len(recs))(*recs)
     c.call("mpm_set_colliders", len(recs), arr)
     try:
@@ -151,9 +166,140 @@ def test_rigid_coupling_matches_reference(ctx, oracle):
             assert errs[k] <= tol, (k, errs[k])
         ferr = np.abs(forces[:, :3] + gr["link_force"]).max() / np.abs(gr["link_force"]).max()
         terr = np.abs(forces[:, 3:] + gr["link_torque"]).max() / np.abs(gr["link_torque"]).max()
-        print("rigid-coupling golden errors:", {k: f"{v:.2e}" for k, v in errs.items()}, f"force {ferr:.2e}",
+        print(fixture, "golden errors:", {k: f"{v:.2e}" for k, v in errs.items()}, f"force {ferr:.2e}",
               f"torque {terr:.2e}")
         assert ferr <= 1e-5 and terr <= 5e-5, (ferr, terr)
         assert c.status()[0] == 0
     finally:
         c.call("mpm_set_colliders", 0, None)
+        if cpic:
+            c.call("mpm_enable_cpic", 0, c.stream)
+
+
+def test_tool_coupling_matches_reference(ctx, oracle):
+    """The CUDA grid op's tool coupling and the library's tool motion (advect onto the floor
+    height) against substeps of the reference's own Mesh, ToolEntity and geometry code
+    (tests/golden/tool_coupling.npz): particle state and the tool's final pose."""
+    import ctypes
+
+    from genesis_gb300 import _lib
+    from test_golden_oracle import _golden_tool
+
+    c, _, n = ctx
+    gt = np.load(os.path.join(GOLDEN, "tool_coupling.npz"))
+    n_steps = int(gt["n_steps"])
+    oracle.clear_sdf_grids()
+    col, _ = _golden_tool(oracle, gt)
+    oracle.clear_sdf_grids()
+    g = col.sdf
+    vals = np.ascontiguousarray(g.values, np.float32)
+    res = np.asarray(vals.shape, np.int32)
+    T = np.ascontiguousarray(g.T_mesh_to_sdf, np.float64)
+    out = ctypes.c_int32()
+    c.call("mpm_add_sdf_grid", res.ctypes.data, vals.ctypes.data, None, T.ctypes.data, float(g.cell_size),
+           float(g.sdf_max), ctypes.byref(out))
+    arr = (_lib.MpmCollider * 1)(col.to_c(out.value))
+    c.call("mpm_set_colliders", 1, arr)
+    try:
+        _load(c, gt, n)
+        c.substeps(n_steps)
+        s = c.get_state(0, 1, n)
+        pose = np.zeros((1, 7))
+        c.call("mpm_get_collider_poses", pose.ctypes.data, c.stream)
+        errs = {}
+        for k, tol in GOLDEN_STATE_TOL:
+            ref = gt[f"out{n_steps}/" + k]
+            errs[k] = np.abs(s[k] - ref).max() / max(1.0, np.abs(ref).max())
+            assert errs[k] <= tol, (k, errs[k])
+        perr = np.abs(pose[0] - np.r_[gt["tool/pos_out"], gt["tool/quat_out"]]).max()
+        print("tool-coupling golden errors:", {k: f"{v:.2e}" for k, v in errs.items()}, f"pose {perr:.2e}")
+        assert perr <= 1e-6, perr
+        assert c.status()[0] == 0
+    finally:
+        c.call("mpm_set_colliders", 0, None)
+
+
+def test_particle_coupling_matches_reference(ctx):
+    """The CUDA grid op's SPH and PBD coupling (mean velocity of the other solver's particles in a
+    node's cell, momentum change given back, PBD free particles only) against substeps of the
+    reference's own grid op and SpatialHasher (tests/golden/particle_coupling.npz): particle state
+    and both sets' velocities."""
+    c, _, n = ctx
+    gp = np.load(os.path.join(GOLDEN, "particle_coupling.npz"))
+    n_steps = int(gp["n_steps"])
+    dev = lambda a, dt=torch.float32: torch.tensor(np.asarray(a), dtype=dt, device="cuda").contiguous()  # noqa: E731
+    sets = {}
+    for kind, name in ((0, "sph"), (1, "pbd")):
+        sets[name] = (dev(gp[f"{name}/pos"]), dev(gp[f"{name}/vel"]), dev(gp[f"{name}/mass"]),
+                      dev(gp[f"{name}/free"], torch.uint8) if name == "pbd" else None)
+    torch.cuda.synchronize()
+    try:
+        for kind, name in ((0, "sph"), (1, "pbd")):
+            p, v, m, f = sets[name]
+            c.call("mpm_set_coupled_particles", kind, len(p), p.data_ptr(), v.data_ptr(), m.data_ptr(),
+                   None if f is None else f.data_ptr(), c.stream)
+        _load(c, gp, n)
+        c.substeps(n_steps)
+        s = c.get_state(0, 1, n)
+        torch.cuda.synchronize()
+        errs = {}
+        for k, tol in GOLDEN_STATE_TOL:
+            ref = gp[f"out{n_steps}/" + k]
+            errs[k] = np.abs(s[k] - ref).max() / max(1.0, np.abs(ref).max())
+            assert errs[k] <= tol, (k, errs[k])
+        verr = {name: np.abs(sets[name][1].double().cpu().numpy() - gp[f"{name}/vel_out"]).max() for name in sets}
+        print("particle-coupling golden errors:", {k: f"{v:.2e}" for k, v in errs.items()},
+              {k: f"{v:.2e}" for k, v in verr.items()})
+        assert max(verr.values()) <= 2e-5, verr
+        assert c.status()[0] == 0
+    finally:
+        c.call("mpm_set_coupled_particles", 0, 0, None, None, None, None, c.stream)
+        c.call("mpm_set_coupled_particles", 1, 0, None, None, None, None, c.stream)
+
+
+def test_particle_constraints_match_reference(ctx):
+    """The CUDA spring update after G2P (particles attached to two moving links and to their start
+    positions, some released midway) against substeps of the reference's own constraint kernels
+    (tests/golden/particle_constraints.npz)."""
+    c, _, n = ctx
+    gc = np.load(os.path.join(GOLDEN, "particle_constraints.npz"))
+    n_steps = int(gc["n_steps"])
+    dev = lambda a, dt=torch.float32: torch.tensor(np.asarray(a), dtype=dt, device="cuda").contiguous()  # noqa: E731
+
+    def poses(k):
+        return np.ascontiguousarray(np.concatenate([gc["link_pos"][k], gc["link_quat"][k]], -1)[None], np.float32)
+
+    _load(c, gc, n)
+    p0 = poses(0)
+    c.call("mpm_set_link_poses", p0.shape[1], p0.ctypes.data)
+    keep = []
+    for i in range(3):
+        start, mask = int(gc[f"set{i}/start"]), dev(gc[f"set{i}/mask"], torch.uint8)
+        li = int(gc[f"set{i}/link"])
+        lp, lq = dev(gc["link_pos"][0, max(li, 0)][None]), dev(gc["link_quat"][0, max(li, 0)][None])
+        keep += [mask, lp, lq]
+        torch.cuda.synchronize()
+        c.call("mpm_set_particle_constraints", 0, 1, start, mask.numel(), mask.data_ptr(),
+               float(gc[f"set{i}/stiffness"]), li, lp.data_ptr(), lq.data_ptr(), c.stream)
+    rm = dev(gc["remove/mask"], torch.uint8)
+    torch.cuda.synchronize()
+    try:
+        for step in range(n_steps):
+            pk = poses(step + 1)
+            c.call("mpm_set_link_poses", pk.shape[1], pk.ctypes.data)
+            if step == int(gc["remove/before"]):
+                c.call("mpm_remove_particle_constraints", 0, 1, int(gc["remove/start"]), rm.numel(), rm.data_ptr(),
+                       c.stream)
+            c.substeps(1)
+        s = c.get_state(0, 1, n)
+        errs = {}
+        for k, tol in GOLDEN_STATE_TOL:
+            ref = gc[f"out{n_steps}/" + k]
+            errs[k] = np.abs(s[k] - ref).max() / max(1.0, np.abs(ref).max())
+            assert errs[k] <= tol, (k, errs[k])
+        print("particle-constraint golden errors:", {k: f"{v:.2e}" for k, v in errs.items()})
+        assert c.status()[0] == 0
+    finally:
+        ones = dev(np.ones(n), torch.uint8)
+        torch.cuda.synchronize()
+        c.call("mpm_remove_particle_constraints", 0, 1, 0, n, ones.data_ptr(), c.stream)
