@@ -714,15 +714,12 @@ def run_served_only(n_requests=48):
             "chunks": sat["chunks"], "status": sat["status"]}
 
 
-def run_diff(steps=64, substeps_per_step=10, ckpt_steps=16, seed=99):
-    """Differentiation config: ~216k-particle elastic cube (per-particle E ~ LogNormal(ln 3e5, 0.2)) on
-    a 97^3 grid, 64 steps x 10 substeps, checkpoint every 16 steps; loss = ||COM - target||^2;
-    gradients w.r.t. the initial velocity and every particle's E.  Reports forward+backward
-    particle-substeps/s (forward substeps counted once)."""
-    import torch
-
+def diff_config(seed=99):
+    """The differentiation workload: a ~216k-particle elastic cube (60^3 lattice at 1/240 m, jittered)
+    2 cm above the floor boundary of a 97^3 grid (density 96, dt 1e-4, gravity on), per-particle
+    E ~ LogNormal(ln 3e5, 0.2), nu 0.2, rho 1000, v0 = (0.1, 0, -1), a random COM target.
+    Returns (scene config, x0 [n, 3], E [n], v0 [3], target [3]) as numpy arrays."""
     from genesis_gb300 import _lib
-    from genesis_gb300.diff import DifferentiableMPM
 
     rng = np.random.default_rng(seed)
     cfg = _lib.MpmSceneConfig()
@@ -738,10 +735,25 @@ def run_diff(steps=64, substeps_per_step=10, ckpt_steps=16, seed=99):
     x0 = np.stack(np.meshgrid(ax, ax, ax, indexing="ij"), -1).reshape(-1, 3)
     x0[:, 2] += 0.18 - 0.5  # 2 cm above the floor boundary: the fall ends in contact, so E shapes the COM
     x0 = x0 + rng.uniform(-0.25 / 240, 0.25 / 240, size=x0.shape)
+    E = 3e5 * np.exp(0.2 * rng.normal(size=len(x0)))
+    v0 = np.array([0.1, 0.0, -1.0])
+    target = rng.uniform(0.3, 0.7, size=3)
+    return cfg, x0, E, v0, target
+
+
+def run_diff(steps=64, substeps_per_step=10, ckpt_steps=16, seed=99):
+    """Differentiation config (diff_config): 64 steps x 10 substeps, checkpoint every 16 steps;
+    loss = ||COM - target||^2; gradients w.r.t. the initial velocity and every particle's E.
+    Reports forward+backward particle-substeps/s (forward substeps counted once)."""
+    import torch
+
+    from genesis_gb300.diff import DifferentiableMPM
+
+    cfg, x0, E_np, v0_np, target_np = diff_config(seed)
     n = len(x0)
-    E = torch.tensor(3e5 * np.exp(0.2 * rng.normal(size=n)), dtype=torch.float32, device="cuda", requires_grad=True)
-    v0 = torch.tensor([0.1, 0.0, -1.0], device="cuda", requires_grad=True)
-    target = torch.tensor(rng.uniform(0.3, 0.7, size=3), dtype=torch.float32, device="cuda")
+    E = torch.tensor(E_np, dtype=torch.float32, device="cuda", requires_grad=True)
+    v0 = torch.tensor(v0_np, dtype=torch.float32, device="cuda", requires_grad=True)
+    target = torch.tensor(target_np, dtype=torch.float32, device="cuda")
     sim = DifferentiableMPM(cfg, nu=0.2, rho=1000.0, ckpt_every=ckpt_steps * substeps_per_step)
     x = torch.tensor(x0, dtype=torch.float32, device="cuda")
     n_sub = steps * substeps_per_step

@@ -1341,33 +1341,56 @@ __device__ __forceinline__ void p2g_body(const KParams& P) {
 #pragma unroll
         for (int oz = 0; oz < 3; ++oz) acc[oy][oz] = make_float4(0.f, 0.f, 0.f, 0.f);
       const float fo = (float)ox;
+      // the quadratic B-spline weights (mpm_solver.py:381) as polynomials in Horner form,
+      // w_o(f) = (p2_o f + p1_o) f + p0_o; this lane's x weight needs only its own o = ox
+      const float px2 = ox == 1 ? -1.f : 0.5f, px1 = ox == 0 ? -1.5f : (ox == 1 ? 2.f : -0.5f),
+                  px0 = ox == 0 ? 1.125f : (ox == 1 ? -0.25f : 0.125f);
       for (int j = 0; j < nmax; ++j) {
         if (j < len) {
           const float4* rec = s_rec + P2G_REC * (beg + j);
           const float4 r0 = rec[0], r1 = rec[1], r2 = rec[2], r3 = rec[3];
           uint32_t m9 = 0u;  // CPIC: the record's separated nodes of this ox
           if constexpr (CPIC) m9 = __float_as_uint(rec[4].x) >> (9 * ox);
-          float wxv[3], wy[3], wz[3];
-          bspline_w(r0.x, wxv);
-          bspline_w(r0.y, wy);
-          bspline_w(r0.z, wz);
-          const float wx = ox == 0 ? wxv[0] : (ox == 1 ? wxv[1] : wxv[2]);
-          // a (k-major, a[k*3 + r]) = r1.w, r2.x, r2.y | r2.z, r2.w, r3.x | r3.y, r3.z, r3.w
-          const float t0x = r1.x + fo * r1.w, t0y = r1.y + fo * r2.x, t0z = r1.z + fo * r2.y;
+          const float wx = fmaf(fmaf(px2, r0.x, px1), r0.x, px0);
+          const float wy[3] = {fmaf(fmaf(0.5f, r0.y, -1.5f), r0.y, 1.125f), fmaf(fmaf(-1.f, r0.y, 2.f), r0.y, -0.25f),
+                               fmaf(fmaf(0.5f, r0.y, -0.5f), r0.y, 0.125f)};
+          const float wz[3] = {fmaf(fmaf(0.5f, r0.z, -1.5f), r0.z, 1.125f), fmaf(fmaf(-1.f, r0.z, 2.f), r0.z, -0.25f),
+                               fmaf(fmaf(0.5f, r0.z, -0.5f), r0.z, 0.125f)};
+          // node value q + a_x ox + a_y oy + a_z oz with a (k-major, a[k*3 + r]) = r1.w, r2.x, r2.y |
+          // r2.z, r2.w, r3.x | r3.y, r3.z, r3.w; the offsets 0, 1, 2 are spelled out (without fast
+          // math a product by 0 or 1 is not folded away)
+          float ty[3][3];
+          ty[0][0] = fmaf(fo, r1.w, r1.x);
+          ty[0][1] = fmaf(fo, r2.x, r1.y);
+          ty[0][2] = fmaf(fo, r2.y, r1.z);
+          ty[1][0] = ty[0][0] + r2.z;
+          ty[1][1] = ty[0][1] + r2.w;
+          ty[1][2] = ty[0][2] + r3.x;
+          ty[2][0] = fmaf(2.f, r2.z, ty[0][0]);
+          ty[2][1] = fmaf(2.f, r2.w, ty[0][1]);
+          ty[2][2] = fmaf(2.f, r3.x, ty[0][2]);
 #pragma unroll
           for (int oy = 0; oy < 3; ++oy) {
-            const float t1x = t0x + (float)oy * r2.z, t1y = t0y + (float)oy * r2.w, t1z = t0z + (float)oy * r3.x;
             const float w01 = wx * wy[oy];
+            float tz[3][3];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) tz[0][r] = ty[oy][r];
+            tz[1][0] = ty[oy][0] + r3.y;
+            tz[1][1] = ty[oy][1] + r3.z;
+            tz[1][2] = ty[oy][2] + r3.w;
+            tz[2][0] = fmaf(2.f, r3.y, ty[oy][0]);
+            tz[2][1] = fmaf(2.f, r3.z, ty[oy][1]);
+            tz[2][2] = fmaf(2.f, r3.w, ty[oy][2]);
 #pragma unroll
             for (int oz = 0; oz < 3; ++oz) {
               float wt = w01 * wz[oz];
               if constexpr (CPIC) {
                 if ((m9 >> (oy * 3 + oz)) & 1u) wt = 0.f;
               }
-              acc[oy][oz].x += wt * (t1x + (float)oz * r3.y);
-              acc[oy][oz].y += wt * (t1y + (float)oz * r3.z);
-              acc[oy][oz].z += wt * (t1z + (float)oz * r3.w);
-              acc[oy][oz].w += wt * r0.w;
+              acc[oy][oz].x = fmaf(wt, tz[oz][0], acc[oy][oz].x);
+              acc[oy][oz].y = fmaf(wt, tz[oz][1], acc[oy][oz].y);
+              acc[oy][oz].z = fmaf(wt, tz[oz][2], acc[oy][oz].z);
+              acc[oy][oz].w = fmaf(wt, r0.w, acc[oy][oz].w);
             }
           }
         }
@@ -1579,12 +1602,12 @@ __device__ __forceinline__ void g2p_body(const KParams& P) {
               }
               const float wxy = w[0][ox] * w[1][oy];
 #pragma unroll
-              for (int r = 0; r < 3; ++r) {
+              for (int r = 0; r < 3; ++r) {  // offsets 0 spelled out: a product by 0 is not folded away
                 const float t = wxy * a[r];
                 v[r] += t;
-                M[r * 3 + 0] += (float)ox * t;
-                M[r * 3 + 1] += (float)oy * t;
-                M[r * 3 + 2] += wxy * bz[r];
+                if (ox > 0) M[r * 3 + 0] = fmaf((float)ox, t, M[r * 3 + 0]);
+                if (oy > 0) M[r * 3 + 1] = fmaf((float)oy, t, M[r * 3 + 1]);
+                M[r * 3 + 2] = fmaf(wxy, bz[r], M[r * 3 + 2]);
               }
             }
           float Cn[9];

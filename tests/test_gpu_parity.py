@@ -900,8 +900,8 @@ def test_entity_queries_frame_and_checkpoints(gs):
 def test_scene_checkpoint_roundtrip_and_lookup(gs, tmp_path):
     """Scene.save_checkpoint / load_checkpoint (scene.py:1402-1446) through the numpy dump of the
     solver (base_solver.py:63-126): a run continued from a loaded checkpoint follows the run that
-    wrote it; entity lookup by name; the gradient members of the Solver protocol point to the
-    differentiable form."""
+    wrote it; entity lookup by name; the gradient members of the Solver protocol need a scene
+    built with requires_grad."""
     scene, cube, _ = c1_scene(gs, n_envs=2, size=0.1)
     for _ in range(5):
         scene.step()
@@ -920,7 +920,7 @@ def test_scene_checkpoint_roundtrip_and_lookup(gs, tmp_path):
     assert (cube.get_particles_pos() - after).abs().max().item() < 1e-5
     assert scene.get_entity(cube.name) is cube and cube.name in scene.entity_names
     assert np.allclose(scene.gravity[0], (0.0, 0.0, -9.81))
-    with pytest.raises(gs.GenesisException, match="DifferentiableMPM"):
+    with pytest.raises(gs.GenesisException, match="requires_grad"):
         scene.sim.mpm_solver.reset_grad()
 
 
