@@ -272,3 +272,63 @@ def test_state_io_row_order_paths():
     assert a.status()[0] == 0 and b.status()[0] == 0
     a.close()
     b.close()
+
+
+def _ill_conditioned_F(n, seed=5):
+    """n deformation gradients (det > 0) whose FP32 SVD fails its own residual check by a wide
+    margin (residual > 5e-5 relative on the host build of the same code; the device switches to
+    FP64 above 1e-5): singular values (1, ~1e-4, ~1e-6), strongly compressed in two directions."""
+    import ctypes
+    import os
+    import subprocess
+    import tempfile
+
+    here = os.path.dirname(os.path.abspath(__file__))
+    so = os.path.join(tempfile.mkdtemp(), "libshim.so")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", os.path.join(here, "host_math_shim.cpp"), "-o", so],
+                   check=True)
+    lib = ctypes.CDLL(so)
+    lib.shim_svd3_f32.restype = ctypes.c_float
+    rng = np.random.default_rng(seed)
+    out = []
+    while len(out) < n:
+        q1, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        q2, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        q1, q2 = q1 * np.sign(np.linalg.det(q1)), q2 * np.sign(np.linalg.det(q2))
+        s = np.array([1.0, 10 ** rng.uniform(-4, -3), 10 ** rng.uniform(-6.5, -5)])
+        A = (q1 @ np.diag(s) @ q2.T).astype(np.float32)
+        buf = [np.zeros(9, np.float32), np.zeros(3, np.float32), np.zeros(9, np.float32)]
+        r = lib.shim_svd3_f32(np.ascontiguousarray(A).ctypes.data, *[b.ctypes.data for b in buf])
+        if r > 5e-5:
+            out.append(A.astype(np.float64))
+    return np.stack(out)
+
+
+def test_fp64_svd_fallback_matches_oracle(oracle):
+    """Particles whose FP32 SVD fails its residual check take the FP64 factorisation: the device
+    counts them, and the P2G grid (here momentum from the corotated stress alone: v = 0, C = 0)
+    matches the FP64 oracle within 1e-5 relative."""
+    n = 16
+    mu, lam = 1e5, 2e5
+    c = _ctx(n, mu=mu, lam=lam)
+    x = np.stack(np.meshgrid(*[np.array([0.3, 0.45, 0.6, 0.75])] * 2, indexing="ij"), -1).reshape(-1, 2)
+    x = np.concatenate([x, np.full((n, 1), 0.5)], 1) + np.random.default_rng(2).uniform(-0.01, 0.01, (n, 3))
+    c.add(0, 1, 0, x, 0)
+    F = _ill_conditioned_F(n)
+    c.set_state(0, 1, pos=x, vel=np.zeros((n, 3)), C=np.zeros((n, 3, 3)), F=F, Jp=np.ones(n),
+                active=np.ones(n, bool))
+    _, f64_before = c.status()
+    c.call("mpm_substep_pre", c.stream)
+    g1 = c.grid(0)
+    st, f64_after = c.status()
+    assert st == 0 and f64_after - f64_before >= n // 2, (f64_before, f64_after)
+    sc = oracle.make_scene(DT, gravity=(0.0, 0.0, 0.0), grid_density=DENSITY, particle_size=0.01 * 64.0 / DENSITY)
+    ref_st = dict(pos=x, vel=np.zeros((n, 3)), C=np.zeros((n, 3, 3)), F=F, Jp=np.ones(n), mat=np.zeros(n, np.int32),
+                  active=np.ones(n, bool))
+    _, grid, _ = oracle.run(sc, [oracle.make_material(0, mu, lam, 1000.0)], ref_st, 1, want_grid=True)
+    assert np.linalg.norm(g1[..., 3] - grid[..., 3]) <= 1e-6 * np.linalg.norm(grid[..., 3])
+    err = np.linalg.norm(g1[..., :3] - grid[..., :3]) / np.linalg.norm(grid[..., :3])
+    assert np.linalg.norm(grid[..., :3]) > 0 and err <= 1e-5, err
+    c.call("mpm_substep_grid_op", c.stream)
+    c.call("mpm_substep_post", c.stream)
+    c.close()
