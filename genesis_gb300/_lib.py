@@ -156,6 +156,9 @@ _SIGNATURES = {
     "mpm_substeps": (c_int32, [_P, c_int32, _P]),
     "mpm_substep_pre": (c_int32, [_P, _P]),
     "mpm_substep_grid_op": (c_int32, [_P, _P]),
+    "mpm_substep_grid_stage": (c_int32, [_P, c_int32, c_int32, c_int32, _P]),
+    "mpm_grid_nodes": (c_int32, [_P, ctypes.POINTER(_P), ctypes.POINTER(c_int64)]),
+    "mpm_grid_node_positions": (c_int32, [_P, _P, _P, _P]),
     "mpm_substep_post": (c_int32, [_P, _P]),
     "mpm_get_grid": (c_int32, [_P, c_int64, _P, _P]),
     "mpm_count_touched_nodes": (c_int32, [_P, ctypes.POINTER(c_int64), _P]),

@@ -113,7 +113,7 @@ struct mpm_ctx {
   // state machine
   int cur = 0;          // particle buffer holding the current state; grid parity of the next P2G
   bool sorted = false;  // perm/items valid for pbuf[cur]
-  int phase = 0;        // 0 ready, 1 after P2G, 2 after grid op
+  int phase = 0;        // 0 ready, 1 after P2G, 2 after grid op, 3 inside a staged grid op
 
   // tuning / launch
   // defaults: the fastest shape on the ~1M-particle plain scene and on the served pool (measured)
@@ -214,6 +214,9 @@ KParams make_params(mpm_ctx* ctx, int src, int dst, int g) {
   P.scan_state = ctx->d_scan_state;
   P.ffs = ctx->d_ffs;
   P.n_ffs = ctx->n_ffs;
+  P.grid_stage = 0;
+  P.ff_begin = 0;
+  P.ff_end = ctx->n_ffs;
   P.colliders = ctx->d_colliders;
   P.n_colliders = ctx->n_colliders;
   P.collider_acc = ctx->d_collider_acc;
@@ -308,17 +311,23 @@ int launch_pre(mpm_ctx* ctx, int c, cudaStream_t s) {
   return MPM_OK;
 }
 
-int launch_grid(mpm_ctx* ctx, int c, cudaStream_t s) {
+// The grid op, whole (stage 0) or one of its stages (see KParams::grid_stage); the coupled
+// particle sets are binned around the stages that apply them (0 and 3).
+int launch_grid(mpm_ctx* ctx, int c, cudaStream_t s, int stage = 0, int ff_begin = 0, int ff_end = -1) {
   KParams P = make_params(ctx, c, 1 - c, c);
+  P.grid_stage = stage;
+  P.ff_begin = ff_begin;
+  P.ff_end = ff_end < 0 ? ctx->n_ffs : ff_end;
   ctx->grid_momentum[c] = false;
+  const bool ext = stage == 0 || stage == 3;
   for (int k = 0; k < 2; ++k)
-    if (ctx->ext[k].n > 0) k_ext_bin<<<ctx->io_blocks, 256, 0, s>>>(P, k, 0);
+    if (ext && ctx->ext[k].n > 0) k_ext_bin<<<ctx->io_blocks, 256, 0, s>>>(P, k, 0);
   {
     Timer t(ctx, s, KT_GRID);
     k_grid_op<<<ctx->grid_blocks, 256, 0, s>>>(P);
   }
   for (int k = 0; k < 2; ++k)
-    if (ctx->ext[k].n > 0) k_ext_bin<<<ctx->io_blocks, 256, 0, s>>>(P, k, 1);
+    if (ext && ctx->ext[k].n > 0) k_ext_bin<<<ctx->io_blocks, 256, 0, s>>>(P, k, 1);
   CKL();
   return MPM_OK;
 }
@@ -963,6 +972,41 @@ int mpm_substep_grid_op(mpm_ctx* ctx, void* stream) {
   if (r) return r;
   if ((r = launch_grid(ctx, ctx->cur, ctx->cs))) return r;
   ctx->phase = 2;
+  return leave(ctx, stream);
+}
+
+int mpm_substep_grid_stage(mpm_ctx* ctx, int32_t stage, int32_t ff_begin, int32_t ff_end, void* stream) {
+  NvtxRange nvtx_range("mpm_substep_grid_stage");
+  if (!ctx) return MPM_ERR_BAD_ARG;
+  if (stage < 1 || stage > 3) return fail(ctx, MPM_ERR_BAD_ARG, "grid stage must be 1, 2 or 3");
+  if (ff_begin < 0 || ff_begin > ff_end || ff_end > ctx->n_ffs)
+    return fail(ctx, MPM_ERR_BAD_ARG, "force-field range outside the fields set");
+  if (stage == 1 ? ctx->phase != 1 : ctx->phase != 3)
+    return fail(ctx, MPM_ERR_STATE, stage == 1 ? "grid stage 1 must follow substep_pre"
+                                               : "grid stages 2 and 3 must follow stage 1");
+  int r = enter(ctx, stream);
+  if (r) return r;
+  if ((r = launch_grid(ctx, ctx->cur, ctx->cs, stage, ff_begin, ff_end))) return r;
+  ctx->phase = stage == 3 ? 2 : 3;
+  return leave(ctx, stream);
+}
+
+int mpm_grid_nodes(mpm_ctx* ctx, float** nodes, int64_t* n_nodes) {
+  if (!ctx || !nodes || !n_nodes) return MPM_ERR_BAD_ARG;
+  if (ctx->phase == 0) return fail(ctx, MPM_ERR_STATE, "the grid exists between substep_pre and substep_post");
+  *nodes = reinterpret_cast<float*>(ctx->d_grid[ctx->cur]);
+  *n_nodes = ctx->K * BLK_NODES;
+  return MPM_OK;
+}
+
+int mpm_grid_node_positions(mpm_ctx* ctx, float* pos, int32_t* scene, void* stream) {
+  NvtxRange nvtx_range("mpm_grid_node_positions");
+  if (!ctx || !pos) return MPM_ERR_BAD_ARG;
+  int r = enter(ctx, stream);
+  if (r) return r;
+  KParams P = make_params(ctx, ctx->cur, ctx->cur, ctx->cur);
+  k_node_positions<<<ctx->n_sm * 8, 256, 0, ctx->cs>>>(P, pos, scene);
+  CKL();
   return leave(ctx, stream);
 }
 

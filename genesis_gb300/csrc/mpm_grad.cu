@@ -115,7 +115,7 @@ __device__ __forceinline__ void f_tmp(const float* C, const float* F, float dt, 
 
 __device__ __forceinline__ void svd_f32(const float* Ft, float* U, float* sig, float* V) {
   const float res = svd3<float, SVD_SWEEPS>(Ft, U, sig, V);
-  if (!(res <= SVD_FP64_TOL)) {
+  if (!svd_accurate(res, sig, SVD_FP64_TOL)) {
     double Ad[9], Ud[9], sd[3], Vd[9];
     for (int k = 0; k < 9; ++k) Ad[k] = Ft[k];
     svd3<double, 8>(Ad, Ud, sd, Vd);

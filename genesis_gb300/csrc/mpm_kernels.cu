@@ -1270,7 +1270,7 @@ __device__ __forceinline__ void p2g_body(const KParams& P) {
         } else {
           float U[9], sig[3], V[9];
           const float res = svd3<float, SVD_SWEEPS>(Ft, U, sig, V);
-          if (!(res <= SVD_FP64_TOL)) {
+          if (!svd_accurate(res, sig, SVD_FP64_TOL)) {
             svd3_fp64(Ft, U, sig, V);
             atomicAdd(P.fp64_count, 1ull);
           }
@@ -1661,14 +1661,21 @@ __global__ void __launch_bounds__(256) k_g2p_cpic(KParams P) { g2p_body<true>(P)
 // legacy_coupler.py:356-501 without coupling partners: for nodes with mass > eps,
 // v = (1/m) p + dt g, then CubeBoundary.impose_pos_vel at the node position; 0 otherwise.
 // Also clears the other grid buffer's blocks touched in the previous substep.
+// Staged (KParams::grid_stage > 0) for callers that act on the node velocities between the
+// built-in force fields and the rest of the grid op (Custom force fields): stage 1 turns momentum
+// into velocity and applies fields [ff_begin, ff_end), stage 2 applies more fields to the
+// velocities, stage 3 applies colliders, coupled particle sets and the boundary.
 __global__ void __launch_bounds__(256) k_grid_op(KParams P) {
   const int sub = threadIdx.x >> 6, ln = threadIdx.x & 63;
   const int per_iter = (int)gridDim.x * (blockDim.x >> 6);
-  const int n_other = *P.nlist_other;
-  for (int i = blockIdx.x * (blockDim.x >> 6) + sub; i < n_other; i += per_iter) {
-    const int32_t blk = P.list_other[i];
-    P.grid_other[(int64_t)blk * BLK_NODES + ln] = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (ln == 0) P.flags_other[blk] = 0;
+  const int stage = P.grid_stage;
+  if (stage <= 1) {
+    const int n_other = *P.nlist_other;
+    for (int i = blockIdx.x * (blockDim.x >> 6) + sub; i < n_other; i += per_iter) {
+      const int32_t blk = P.list_other[i];
+      P.grid_other[(int64_t)blk * BLK_NODES + ln] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (ln == 0) P.flags_other[blk] = 0;
+    }
   }
   const int n_cur = *P.nlist;
   const unsigned long long step = P.ff_step ? *P.ff_step : 0ull;
@@ -1681,7 +1688,7 @@ __global__ void __launch_bounds__(256) k_grid_op(KParams P) {
     const int g[3] = {bx * BLK + (ln >> 4), by * BLK + ((ln >> 2) & 3), bz * BLK + (ln & 3)};
     float4* node = &P.grid[(int64_t)blk * BLK_NODES + ln];
     float4 q = *node;
-    if (P.pin) {  // nodes touched by a non-free particle keep no momentum (mpm_solver.py:420-421)
+    if (stage <= 1 && P.pin) {  // nodes touched by a non-free particle keep no momentum (mpm_solver.py:420-421)
       const int64_t a = (int64_t)blk * BLK_NODES + ln;
       const uint32_t bit = 1u << (a & 31);
       if (P.pin[a >> 5] & bit) {
@@ -1689,26 +1696,57 @@ __global__ void __launch_bounds__(256) k_grid_op(KParams P) {
         atomicAnd(&P.pin[a >> 5], ~bit);
       }
     }
-    if (P.n_colliders == 0 && P.n_ffs == 0 && P.ext[0].n == 0 && P.ext[1].n == 0) {
+    if (stage == 0 && P.n_colliders == 0 && P.n_ffs == 0 && P.ext[0].n == 0 && P.ext[1].n == 0) {
       *node = grid_velocity(S, q, g[0], g[1], g[2]);
     } else {  // gravity, force fields (:381-383), colliders (:389-403), SPH / PBD (:404-498), boundary
-      float v[3];
-      if (grid_free_velocity(S, q, v)) {
+      float v[3] = {0.f, 0.f, 0.f};
+      bool has;
+      if (stage <= 1) {
+        has = grid_free_velocity(S, q, v);
+      } else {  // the node already holds its velocity
+        has = q.w > S.eps;
+        if (has) v[0] = q.x, v[1] = q.y, v[2] = q.z;
+      }
+      if (has) {
         const float x[3] = {(float)(g[0] + S.offset[0]) * S.dx, (float)(g[1] + S.offset[1]) * S.dx,
                             (float)(g[2] + S.offset[2]) * S.dx};
-        for (int fi = 0; fi < P.n_ffs; ++fi) {
-          if (!P.ffs[fi].active) continue;
-          float a[3];
-          const int gw[3] = {g[0] + S.offset[0], g[1] + S.offset[1], g[2] + S.offset[2]};
-          ff_acc(P.ffs[fi], x, v, S.eps, a, P.block_scene[blk], gw, step);
-          for (int k = 0; k < 3; ++k) v[k] += a[k] * S.dt;
+        if (stage != 3) {
+          for (int fi = P.ff_begin; fi < P.ff_end; ++fi) {
+            if (!P.ffs[fi].active) continue;
+            float a[3];
+            const int gw[3] = {g[0] + S.offset[0], g[1] + S.offset[1], g[2] + S.offset[2]};
+            ff_acc(P.ffs[fi], x, v, S.eps, a, P.block_scene[blk], gw, step);
+            for (int k = 0; k < 3; ++k) v[k] += a[k] * S.dt;
+          }
         }
-        collide_node(P, S, P.block_scene[blk], x, v, q.w / 1e3f);
-        couple_ext(P, (int64_t)blk * BLK_NODES + ln, v, q.w / 1e3f);
-        grid_boundary(S, v, g[0], g[1], g[2]);
+        if (stage == 0 || stage == 3) {
+          collide_node(P, S, P.block_scene[blk], x, v, q.w / 1e3f);
+          couple_ext(P, (int64_t)blk * BLK_NODES + ln, v, q.w / 1e3f);
+          grid_boundary(S, v, g[0], g[1], g[2]);
+        }
       }
       *node = make_float4(v[0], v[1], v[2], q.w);
     }
+  }
+}
+
+// World position of every node of the grid buffer ([K * 64][3], block-major like the grid) and
+// its scene (-1 for the padding of a block past the scene's grid).
+__global__ void k_node_positions(KParams P, float* pos, int32_t* scene) {
+  const int64_t total = P.K * BLK_NODES;
+  for (int64_t i = grid_stride_begin(); i < total; i += grid_stride_step()) {
+    const int64_t blk = i / BLK_NODES;
+    const int ln = (int)(i % BLK_NODES);
+    const int32_t sid = P.block_scene[blk];
+    const SceneDev& S = P.scenes[sid];
+    const int64_t lb = blk - S.block_base;
+    const int bz = (int)(lb % S.bres[2]), by = (int)((lb / S.bres[2]) % S.bres[1]),
+              bx = (int)(lb / ((int64_t)S.bres[2] * S.bres[1]));
+    const int g[3] = {bx * BLK + (ln >> 4), by * BLK + ((ln >> 2) & 3), bz * BLK + (ln & 3)};
+    const bool in = g[0] < S.res[0] && g[1] < S.res[1] && g[2] < S.res[2];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) pos[i * 3 + d] = (float)(g[d] + S.offset[d]) * S.dx;
+    if (scene) scene[i] = in ? sid : -1;
   }
 }
 

@@ -48,7 +48,7 @@ constexpr int P2G_REC = 5;
 __host__ __device__ __forceinline__ size_t p2g_dyn_smem(int threads, int chunk) {
   return (size_t)(threads / 32) * TILE_NODES * 16 + (size_t)chunk * P2G_REC * 16 + (size_t)chunk * 8;
 }
-constexpr float SVD_FP64_TOL = 1e-5f;        // residual above which the SVD is redone in FP64
+constexpr float SVD_FP64_TOL = 1e-5f;        // accuracy bound of an FP32 SVD (svd_accurate); else FP64
 
 enum : int {
   PF_POS = 0,
@@ -167,6 +167,9 @@ struct KParams {
   int32_t n_colliders;
   double* collider_acc;        // [n_colliders][6] reaction force and torque
   int32_t fuse_grid;           // G2P applies the grid op while staging its tile and clears the other buffer
+  int32_t grid_stage;          // k_grid_op: 0 whole grid op; 1 momentum -> velocity + fields [ff_begin, ff_end);
+                               // 2 fields [ff_begin, ff_end) on velocities; 3 colliders, coupling, boundary
+  int32_t ff_begin, ff_end;    // the force fields k_grid_op applies (stage 0: all)
   int32_t* nlist_reset;        // active-list length that k_perm resets at the end of a fused substep
   int32_t cpic_slots;          // CPIC collider slots (normal planes PF_CPIC + 3 * slot); 0: CPIC off
   uint32_t* cpic_mask;         // CPIC: per slot, the particle's nodes behind a collider (bit ox*9+oy*3+oz)
@@ -258,6 +261,7 @@ __global__ void k_grid_op(KParams P);
 __global__ void k_fill_plane(float* p, int64_t n, float v);
 __global__ void k_ext_bin(KParams P, int k, int unbin);
 __global__ void k_get_grid(KParams P, int64_t scene, float* out);
+__global__ void k_node_positions(KParams P, float* pos, int32_t* scene);
 // Soft particle-to-link constraint of one reference particle row (mpm_solver.py:1052-1128).
 struct ConstraintDev {
   float local[3];   // offset in the link frame at attachment

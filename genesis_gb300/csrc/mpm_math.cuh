@@ -198,6 +198,16 @@ GB_HD T svd3(const T* A, T* U, T* sig, T* V) {
   return scale > T(0) ? off / scale : off;
 }
 
+// Whether a factorisation from svd3 is accurate enough to use: its residual (relative to |sig0|)
+// is below tol, and so is the rotation error it implies for the polar factor U V^T, which is
+// about the off-diagonal residual over the smallest pair sum |sig1| + |sig2| (a deformation
+// compressed to nearly nothing in two directions has an ill-determined FP32 rotation even when
+// the residual is small).  NaN fails.
+template <typename T>
+GB_HD bool svd_accurate(T res, const T* sig, T tol) {
+  return res <= tol && res * gabs(sig[0]) <= tol * (gabs(sig[1]) + gabs(sig[2]));
+}
+
 // ------------------------------------------------------------------------------------
 // Small matrix helpers (row-major 3x3)
 // ------------------------------------------------------------------------------------

@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(256) k_na_p2g(NoallocParams Q) {
     mat_mul(A, F, Ft);
     float U[9], sig[3], V[9];
     const float res = svd3<float, SVD_SWEEPS>(Ft, U, sig, V);
-    if (!(res <= SVD_FP64_TOL)) {
+    if (!svd_accurate(res, sig, SVD_FP64_TOL)) {
       double Ad[9], Ud[9], sd[3], Vd[9];
       for (int k = 0; k < 9; ++k) Ad[k] = Ft[k];
       svd3<double, 8>(Ad, Ud, sd, Vd);

@@ -3,7 +3,8 @@
 `scene.add_force_field(ff)` registers a field; it acts on grid velocities as
 v += acc(x, v) * dt after gravity (legacy_coupler.py:381-383), on the device.  Fields start
 inactive, as in the reference; `activate()` / `deactivate()` take effect at the next substep.
-Custom (a user Quadrants function) is not provided: it needs a device-code compiler at run time.
+`Custom(func)` takes a batched torch function in place of the reference's Quadrants function; it
+runs between stages of the grid op (mpm_substep_grid_stage), at its place in the field order.
 """
 
 from __future__ import annotations
@@ -245,3 +246,27 @@ class Turbulence(ForceField):
     @property
     def frequency(self):
         return self._frequency
+
+
+class Custom(ForceField):
+    """force_fields.py:424-437: a user-defined acceleration acc = func(pos, vel, t, i).
+
+    The reference compiles `func` (a Quadrants function of one node's position and velocity) into
+    its grid op, where i = -1 and t is the simulation time of the substep.  Here `func` is a batched
+    torch function: pos and vel are float32 CUDA tensors [M, 3] of the M grid nodes that hold mass
+    (velocity after gravity and the fields listed before this one), t a float, i = -1; it returns
+    the accelerations [M, 3].  As in the reference, `get_acc` is replaced by `func`, so the field
+    acts whether or not it was activated.  A scene with a Custom field runs its substeps through the
+    staged grid op (one library call per stage and a torch call per Custom field per substep)
+    instead of the captured graph."""
+
+    _type = -2
+
+    def __init__(self, func):
+        super().__init__()
+        if not callable(func):
+            raise TypeError("Custom force field needs a callable func(pos, vel, t, i) -> acc.")
+        self.get_acc = func
+
+    def to_c(self):
+        raise TypeError("a Custom force field has no device record")

@@ -43,6 +43,14 @@ def _stream_handle():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
+class _DeviceArray:
+    """A device buffer of the library seen by torch without a copy (CUDA array interface)."""
+
+    def __init__(self, ptr: int, shape, typestr: str = "<f4"):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(ptr), False),
+                                         "version": 2}
+
+
 class MPMSolver:
     def __init__(self, scene, sim, options):
         import genesis_gb300 as gs
@@ -211,6 +219,13 @@ class MPMSolver:
             return
         if self._ctx is None:
             return
+        if getattr(self, "_ff_plan", None):  # Custom force fields: the grid op in stages, per substep
+            t0 = self._sim.cur_t
+            for k in range(int(n)):
+                self.substep_pre_coupling()
+                self._staged_grid_op(t0 + k * self._substep_dt)
+                self.substep_post_coupling()
+            return
         _lib.check(self._lib.mpm_substeps(self._ctx, int(n), _stream_handle()), self._ctx, "mpm_substeps")
 
     def substep_pre_coupling(self, f=0):
@@ -218,7 +233,50 @@ class MPMSolver:
 
     def couple(self, f=0):
         """LegacyCoupler.mpm_grid_op for MPM alone (legacy_coupler.py:356-501)."""
+        if getattr(self, "_ff_plan", None):
+            self._staged_grid_op(self._sim.cur_t)
+            return
         _lib.check(self._lib.mpm_substep_grid_op(self._ctx, _stream_handle()), self._ctx, "mpm_substep_grid_op")
+
+    def _staged_grid_op(self, t: float) -> None:
+        """The grid op with Custom force fields (legacy_coupler.py:372-378 with the fields in list
+        order): stage 1 applies gravity and the built-in fields before the first Custom one, each
+        Custom field then acts on the node velocities in torch, stage 2 applies the built-in fields
+        up to the next Custom one, stage 3 the colliders, coupling and boundary."""
+        h = _stream_handle()
+        first = True
+        for step in self._ff_plan:
+            if step[0] == "custom":
+                self._apply_custom_field(step[1], t)
+            elif first or step[2] > step[1]:
+                _lib.check(self._lib.mpm_substep_grid_stage(self._ctx, 1 if first else 2, step[1], step[2], h),
+                           self._ctx, "mpm_substep_grid_stage")
+                first = False
+        _lib.check(self._lib.mpm_substep_grid_stage(self._ctx, 3, 0, 0, h), self._ctx, "mpm_substep_grid_stage")
+
+    def _grid_view(self):
+        """(nodes [n, 4] float32 view of the current grid buffer, node positions [n, 3], node scene [n])."""
+        ptr, count = ctypes.c_void_p(), ctypes.c_int64()
+        _lib.check(self._lib.mpm_grid_nodes(self._ctx, ctypes.byref(ptr), ctypes.byref(count)), self._ctx,
+                   "mpm_grid_nodes")
+        n = int(count.value)
+        if getattr(self, "_node_pos", None) is None or self._node_pos.shape[0] != n:
+            self._node_pos = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+            self._node_scene = torch.empty((n,), dtype=torch.int32, device="cuda")
+            _lib.check(self._lib.mpm_grid_node_positions(self._ctx, _lib.ptr(self._node_pos), _lib.ptr(self._node_scene),
+                                                         _stream_handle()), self._ctx, "mpm_grid_node_positions")
+        nodes = torch.as_tensor(_DeviceArray(ptr.value, (n, 4)), device="cuda")
+        return nodes, self._node_pos, self._node_scene
+
+    def _apply_custom_field(self, ff, t: float) -> None:
+        nodes, pos, scene = self._grid_view()
+        sel = torch.nonzero((scene >= 0) & (nodes[:, 3] > self._eps)).squeeze(1)
+        if sel.numel() == 0:
+            return
+        v = nodes.index_select(0, sel)[:, :3]
+        acc = ff.get_acc(pos.index_select(0, sel), v.clone(), float(t), -1)
+        acc = torch.as_tensor(acc, dtype=torch.float32, device=nodes.device).reshape(-1, 3)
+        nodes[sel, :3] = v + acc * self._substep_dt
 
     def substep_post_coupling(self, f=0):
         _lib.check(self._lib.mpm_substep_post(self._ctx, _stream_handle()), self._ctx, "mpm_substep_post")
@@ -374,10 +432,22 @@ class MPMSolver:
             self._upload_force_fields()
 
     def _upload_force_fields(self) -> None:
+        """Built-in fields go to the device in list order; Custom ones split that list into the
+        stages of the grid op (the plan _staged_grid_op follows)."""
+        from .force_fields import Custom
+
         ffs = getattr(self, "_ffs", [])
         if self._ctx is None:
             return
-        recs = [f.to_c() for f in ffs]
+        recs, plan, begin = [], [], 0
+        for f in ffs:
+            if isinstance(f, Custom):
+                plan += [("fields", begin, len(recs)), ("custom", f)]
+                begin = len(recs)
+            else:
+                recs.append(f.to_c())
+        plan.append(("fields", begin, len(recs)))
+        self._ff_plan = plan if len(plan) > 1 else None
         arr = (_lib.MpmForceField * max(1, len(recs)))(*recs)
         _lib.check(self._lib.mpm_set_force_fields(self._ctx, len(recs), arr), self._ctx, "mpm_set_force_fields")
 

@@ -178,6 +178,25 @@ int mpm_substep_pre(mpm_ctx* ctx, void* stream);
 int mpm_substep_grid_op(mpm_ctx* ctx, void* stream);
 int mpm_substep_post(mpm_ctx* ctx, void* stream);
 
+/* The grid op in stages, in place of mpm_substep_grid_op, for a caller that applies its own
+ * acceleration fields to the node velocities at their place in the field order (the reference's
+ * force_fields.Custom, a user function called in legacy_coupler.py:376-378 like the built-in
+ * fields).  stage 1 (after mpm_substep_pre): momentum -> velocity + gravity, then the force fields
+ * [ff_begin, ff_end) of the mpm_set_force_fields list; stage 2 (repeatable): fields
+ * [ff_begin, ff_end) on the velocities; stage 3: colliders, tools, SPH / PBD coupling and the
+ * boundary, after which mpm_substep_post follows.  Between stages the caller may change the
+ * velocities of nodes with mass > mass_eps in the buffer mpm_grid_nodes returns. */
+int mpm_substep_grid_stage(mpm_ctx* ctx, int32_t stage, int32_t ff_begin, int32_t ff_end, void* stream);
+
+/* The grid buffer of the current substep (valid from mpm_substep_pre to mpm_substep_post): *nodes
+ * = device float4 per node (momentum or velocity xyz, mass), block-major, *n_nodes of them (every
+ * scene's 4x4x4-node blocks, padding included).  Replaces reading MPMSolver.grid in place. */
+int mpm_grid_nodes(mpm_ctx* ctx, float** nodes, int64_t* n_nodes);
+
+/* World position pos [n_nodes][3] of every node of that buffer and its scene scene [n_nodes]
+ * (-1 for block padding past the scene's grid; scene may be NULL); device arrays. */
+int mpm_grid_node_positions(mpm_ctx* ctx, float* pos, int32_t* scene, void* stream);
+
 /* Copy the dense grid of one scene into out [gx, gy, gz, 4] (x-major, float32):
  * after mpm_substep_pre it holds (momentum xyz, mass); after mpm_substep_grid_op it
  * holds (vel_out xyz, mass).  Replaces reading MPMSolver.grid (mpm_solver.py:137-148). */

@@ -29,6 +29,8 @@ Outputs (committed, small):
   particle_constraints.npz the same scene with particles attached to two moving kinematic links
                     and to their start positions, some released midway (mpm_solver.py
                     particle constraints): state after 5 substeps
+  custom_field.npz  the same scene with a Custom force field (a user function) between Drag and
+                    Constant: state after 5 substeps
   tool_coupling.npz the same scene with a moving, spinning box tool (tool_entity/mesh.py,
                     tool_entity.py, boundaries.py FloorBoundary): state and tool pose after 4
                     substeps
@@ -636,7 +638,7 @@ def gen_substeps(F, rng, ffs=(), n_steps=10, rigid=None, tool=None, cpic=False, 
             tool["entity"].advect(0)
         if step == 0:
             out["grid1"] = np.concatenate([G["vel_in"][0, ..., 0, :], G["mass"][0, ..., 0, None]], -1).copy()
-        coupler.mpm_grid_op(0, 0.0, *grid_op_args)
+        coupler.mpm_grid_op(0, step * dt, *grid_op_args)  # t = Simulator.cur_t of the substep
         if cpic:
             solver.g2p(0, rigid["geoms_info"], rigid["links_state"], rigid["rigid_global_info"])
         else:
@@ -1001,6 +1003,29 @@ def gen_constraints(F, rng, n_steps=5):
     return out
 
 
+# ----------------------------------------------------------------------------- Custom force field
+def custom_acc(pos, vel, t, i):
+    """The user function of the Custom-field fixture (one node, as the reference calls it): a swirl
+    about the vertical axis through (0.125, 0.125), drag on the horizontal velocity, a time ramp and
+    a height-dependent lift.  tests/test_gpu_golden.py evaluates the same formula batched in torch."""
+    return QMat([-3.0 * (pos[1] - 0.125) - 0.5 * vel[0] + 2.0 * t,
+                 3.0 * (pos[0] - 0.125) - 0.5 * vel[1],
+                 -1.0 + 0.3 * pos[2] * (1.0 + t)])
+
+
+def gen_custom_field(F, ref, rng, n_steps=5):
+    """A Custom field (force_fields.py:424) between two built-in ones, Drag before it (it sees the
+    velocity Drag left) and Constant after it."""
+    FF = load_force_fields(ref)
+    fields = [FF.Drag(linear=0.8, quadratic=0.4), FF.Custom(custom_acc), FF.Constant(direction=(0.0, 1.0, 0.5),
+                                                                                  strength=1.5)]
+    for f in (fields[0], fields[2]):
+        f.activate()
+    out = gen_substeps(F, rng, ffs=fields, n_steps=n_steps)
+    out["n_steps"] = np.array(n_steps)
+    return out
+
+
 def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GENESIS_REFERENCE")
     if not ref:
@@ -1019,6 +1044,8 @@ def main():
                         **gen_coupled(F, np.random.default_rng(20261209)))
     np.savez_compressed(os.path.join(HERE, "particle_constraints.npz"),
                         **gen_constraints(F, np.random.default_rng(20261210)))
+    np.savez_compressed(os.path.join(HERE, "custom_field.npz"),
+                        **gen_custom_field(F, ref, np.random.default_rng(20261211)))
     print("wrote", os.listdir(HERE))
 
 

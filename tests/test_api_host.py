@@ -266,3 +266,37 @@ def test_sdf_grid_from_mesh_matches_the_analytic_box():
     pn = np.array([0.3, -0.15, 0.6])
     vox = g.T_mesh_to_sdf @ np.append(pn * 2.0, 1.0)
     assert np.allclose(vox[:3], (pn + 0.6) / 1.2 * (res - 1))
+
+
+def test_custom_force_field_splits_the_field_list_into_grid_op_stages():
+    """force_fields.Custom (force_fields.py:424-437): a callable replaces get_acc; it has no device
+    record, and the solver's plan runs the built-in fields before it in grid-op stage 1, the Custom
+    field, then the built-in fields after it in stage 2."""
+    from genesis_gb300.solver import MPMSolver
+
+    ff = gs.force_fields
+    with pytest.raises(TypeError):
+        ff.Custom(3.0)
+    c = ff.Custom(lambda pos, vel, t, i: vel)
+    assert c.get_acc is not None and not c.active
+    with pytest.raises(TypeError):
+        c.to_c()
+
+    class _Lib:
+        calls = []
+
+        def mpm_set_force_fields(self, ctx, n, arr):
+            self.calls.append(n)
+            return 0
+
+    s = MPMSolver.__new__(MPMSolver)
+    s._ctx, s._lib = object(), _Lib()
+    s._ffs = [ff.Drag(), c, ff.Constant(), ff.Wind(), ff.Custom(lambda p, v, t, i: p)]
+    s._upload_force_fields()
+    kinds = [p[0] for p in s._ff_plan]
+    assert kinds == ["fields", "custom", "fields", "custom", "fields"]
+    assert s._ff_plan[0][1:] == (0, 1) and s._ff_plan[2][1:] == (1, 3) and s._ff_plan[4][1:] == (3, 3)
+    assert _Lib.calls == [3]
+    s._ffs = [ff.Drag()]
+    s._upload_force_fields()
+    assert s._ff_plan is None

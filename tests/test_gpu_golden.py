@@ -303,3 +303,64 @@ def test_particle_constraints_match_reference(ctx):
         ones = dev(np.ones(n), torch.uint8)
         torch.cuda.synchronize()
         c.call("mpm_remove_particle_constraints", 0, 1, 0, n, ones.data_ptr(), c.stream)
+
+
+def _custom_acc_batched(pos, vel, t, i):
+    """tests/golden/make_golden.py custom_acc, batched over nodes (torch [M, 3])."""
+    return torch.stack([-3.0 * (pos[:, 1] - 0.125) - 0.5 * vel[:, 0] + 2.0 * t,
+                        3.0 * (pos[:, 0] - 0.125) - 0.5 * vel[:, 1],
+                        -1.0 + 0.3 * pos[:, 2] * (1.0 + t)], 1)
+
+
+def test_custom_force_field_matches_reference(ctx):
+    """A Custom force field between Drag and Constant, applied through the staged grid op
+    (mpm_substep_grid_stage: stage 1 gravity + Drag, the user function on the node velocities of
+    the buffer mpm_grid_nodes exposes, stage 2 Constant, stage 3 boundary) against five substeps of
+    the reference's grid op calling the same function (tests/golden/custom_field.npz)."""
+    import ctypes
+
+    from genesis_gb300 import _lib
+    from genesis_gb300 import force_fields as ff
+    from genesis_gb300.solver import _DeviceArray
+
+    c, _, n = ctx
+    gc = np.load(os.path.join(GOLDEN, "custom_field.npz"))
+    n_steps = int(gc["n_steps"])
+    fields = [ff.Drag(linear=0.8, quadratic=0.4), ff.Constant(direction=(0.0, 1.0, 0.5), strength=1.5)]
+    for f in fields:
+        f.activate()
+    recs = (_lib.MpmForceField * 2)(*[f.to_c() for f in fields])
+    c.call("mpm_set_force_fields", 2, recs)
+    dt = float(gc["scene"][0])
+    eps = float(np.finfo(np.float32).eps)
+    try:
+        _load(c, gc, n)
+        ptr, count = ctypes.c_void_p(), ctypes.c_int64()
+        for step in range(n_steps):
+            c.call("mpm_substep_pre", c.stream)
+            c.call("mpm_substep_grid_stage", 1, 0, 1, c.stream)
+            c.call("mpm_grid_nodes", ctypes.byref(ptr), ctypes.byref(count))
+            nn = int(count.value)
+            if step == 0:
+                pos = torch.empty((nn, 3), dtype=torch.float32, device="cuda")
+                scene = torch.empty((nn,), dtype=torch.int32, device="cuda")
+                c.call("mpm_grid_node_positions", pos.data_ptr(), scene.data_ptr(), c.stream)
+            torch.cuda.synchronize()
+            nodes = torch.as_tensor(_DeviceArray(ptr.value, (nn, 4)), device="cuda")
+            sel = torch.nonzero((scene >= 0) & (nodes[:, 3] > eps)).squeeze(1)
+            v = nodes.index_select(0, sel)[:, :3]
+            nodes[sel, :3] = v + _custom_acc_batched(pos.index_select(0, sel), v, step * dt, -1) * dt
+            torch.cuda.synchronize()
+            c.call("mpm_substep_grid_stage", 2, 1, 2, c.stream)
+            c.call("mpm_substep_grid_stage", 3, 0, 0, c.stream)
+            c.call("mpm_substep_post", c.stream)
+        s = c.get_state(0, 1, n)
+        errs = {}
+        for k, tol in GOLDEN_STATE_TOL:
+            ref = gc[f"out{n_steps}/" + k]
+            errs[k] = np.abs(s[k] - ref).max() / max(1.0, np.abs(ref).max())
+            assert errs[k] <= tol, (k, errs[k])
+        print("custom-field golden errors:", {k: f"{v:.2e}" for k, v in errs.items()})
+        assert c.status()[0] == 0
+    finally:
+        c.call("mpm_set_force_fields", 0, None)

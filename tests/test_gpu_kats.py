@@ -305,9 +305,12 @@ def _ill_conditioned_F(n, seed=5):
 
 
 def test_fp64_svd_fallback_matches_oracle(oracle):
-    """Particles whose FP32 SVD fails its residual check take the FP64 factorisation: the device
-    counts them, and the P2G grid (here momentum from the corotated stress alone: v = 0, C = 0)
-    matches the FP64 oracle within 1e-5 relative."""
+    """Particles whose FP32 SVD is not accurate enough (svd_accurate) take the FP64 factorisation:
+    the device counts every one of these ill-conditioned particles, and the P2G grid (momentum from
+    the corotated stress alone: v = 0, C = 0) is within 1e-3 of the FP64 oracle.  The bound is the
+    float32 evaluation of the stress itself: 2 mu (F - R) F^T is ~1e-4 of 2 mu here while F and R
+    are ~1, so the subtraction loses about eps_f32 / 1e-4 ~ 1e-3 (measured 2.1e-4).  With the
+    residual test alone some of these particles kept their FP32 rotation and the error was 3.4e-3."""
     n = 16
     mu, lam = 1e5, 2e5
     c = _ctx(n, mu=mu, lam=lam)
@@ -321,14 +324,14 @@ def test_fp64_svd_fallback_matches_oracle(oracle):
     c.call("mpm_substep_pre", c.stream)
     g1 = c.grid(0)
     st, f64_after = c.status()
-    assert st == 0 and f64_after - f64_before >= n // 2, (f64_before, f64_after)
+    assert st == 0 and f64_after - f64_before >= n, (f64_before, f64_after)
     sc = oracle.make_scene(DT, gravity=(0.0, 0.0, 0.0), grid_density=DENSITY, particle_size=0.01 * 64.0 / DENSITY)
     ref_st = dict(pos=x, vel=np.zeros((n, 3)), C=np.zeros((n, 3, 3)), F=F, Jp=np.ones(n), mat=np.zeros(n, np.int32),
                   active=np.ones(n, bool))
     _, grid, _ = oracle.run(sc, [oracle.make_material(0, mu, lam, 1000.0)], ref_st, 1, want_grid=True)
     assert np.linalg.norm(g1[..., 3] - grid[..., 3]) <= 1e-6 * np.linalg.norm(grid[..., 3])
     err = np.linalg.norm(g1[..., :3] - grid[..., :3]) / np.linalg.norm(grid[..., :3])
-    assert np.linalg.norm(grid[..., :3]) > 0 and err <= 1e-5, err
+    assert np.linalg.norm(grid[..., :3]) > 0 and err <= 1e-3, err
     c.call("mpm_substep_grid_op", c.stream)
     c.call("mpm_substep_post", c.stream)
     c.close()

@@ -984,3 +984,46 @@ def test_reference_scenario_rigid_mpm_legacy_coupling(gs, substeps):
     solver.check_state()
     assert pushed < 0.0  # the liquid pushed the box towards -y
     assert pos[1] + 0.25 < 0.0, pos
+
+
+def test_custom_force_field_through_scene_api(gs):
+    """force_fields.Custom through scene.add_force_field: a Custom field returning the Constant
+    field's acceleration reproduces the run with that Constant field (same trajectory within float
+    rounding: the library adds acc dt with a fused multiply-add, torch in two steps), both between
+    the same Drag fields; the user function sees the simulation time of each substep; a scene with
+    a Custom field also steps through the split phases (scene.sim.substep)."""
+    ff = gs.force_fields
+    direction, strength = np.array([1.0, 0.5, 0.0]) / np.linalg.norm([1.0, 0.5, 0.0]), 3.0
+    seen_t = []
+
+    def as_constant(pos, vel, t, i):
+        seen_t.append(t)
+        assert i == -1 and pos.shape == vel.shape and pos.shape[1] == 3
+        return torch.tensor(direction * strength, dtype=torch.float32, device=pos.device).expand_as(pos)
+
+    def run(middle):
+        scene = gs.Scene(
+            sim_options=gs.options.SimOptions(dt=2e-3, substeps=10),
+            mpm_options=gs.options.MPMOptions(lower_bound=(0, 0, 0), upper_bound=(1, 1, 1), grid_density=64,
+                                              particle_size=1 / 128),
+        )
+        mat = gs.materials.MPM.Elastic(E=3e5, nu=0.2, rho=1000, sampler="regular")
+        cube = scene.add_entity(material=mat, morph=gs.morphs.Box(pos=(0.5, 0.5, 0.4), size=(0.12,) * 3))
+        fields = [ff.Drag(linear=0.8, quadratic=0.3), middle, ff.Drag(linear=0.2, quadratic=0.0)]
+        for f in fields:
+            scene.add_force_field(f)
+        scene.build()
+        for f in fields:
+            f.activate()
+        for _ in range(4):
+            scene.step()
+        return scene, cube.get_particles_pos().double().cpu().numpy()
+
+    _, ref = run(ff.Constant(direction=tuple(direction), strength=strength))
+    scene, got = run(ff.Custom(as_constant))
+    assert np.abs(got - ref).max() <= 1e-6, np.abs(got - ref).max()
+    assert len(seen_t) == 40 and np.allclose(seen_t, np.arange(40) * 2e-4)
+    z0 = got[:, 2].mean()
+    scene.sim.substep()  # split phases: pre, the staged grid op, post
+    assert len(seen_t) == 41 and abs(seen_t[-1] - 40 * 2e-4) < 1e-12
+    assert np.isfinite(z0)
