@@ -165,6 +165,24 @@ int fail(mpm_ctx* c, int code, const std::string& msg) {
     if (e_ != cudaSuccess) return fail(ctx, MPM_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e_)); \
   } while (0)
 
+// Launch with programmatic stream serialisation: the kernel may begin launching while the previous
+// kernel of the stream drains; every kernel launched this way calls pdl_wait() before it reads
+// what its predecessor wrote.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), int grid, int block, size_t smem, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 template <typename T>
 int dalloc(mpm_ctx* ctx, T** p, size_t count) {
   *p = nullptr;
@@ -271,15 +289,15 @@ int launch_sort(mpm_ctx* ctx, const KParams& P, cudaStream_t s) {
   {
     Timer t(ctx, s, KT_SCAN);
     if (ctx->K + 2 <= SCAN_SINGLE_MAX) {
-      k_scan_single<<<1, 1024, 0, s>>>(P);
+      CK(launch_pdl(k_scan_single, 1, 1024, 0, s, P));
     } else {
-      k_scan_onepass<<<ctx->n_tiles, SCAN_THREADS, 0, s>>>(P);
+      CK(launch_pdl(k_scan_onepass, ctx->n_tiles, SCAN_THREADS, 0, s, P));
     }
   }
   CKL();
   if (P.n > 0 || P.steps || P.nlist_reset || P.colliders_rw) {
     Timer t(ctx, s, KT_PERM);
-    k_perm<<<ctx->n_sm * 8, 256, 0, s>>>(P);  // one wave; four particles per thread and pass
+    CK(launch_pdl(k_perm, ctx->n_sm * 8, 256, 0, s, P));  // one wave; four particles per thread and pass
   }
   CKL();
   return MPM_OK;
@@ -304,9 +322,9 @@ int launch_pre(mpm_ctx* ctx, int c, cudaStream_t s) {
   P.steps = ctx->d_steps;
   Timer t(ctx, s, KT_P2G);
   if (ctx->cpic_slots > 0 && ctx->n_colliders > 0)
-    k_p2g_cpic<<<ctx->p2g_cpic_blocks, ctx->p2g_threads, p2g_dyn_smem(ctx->p2g_threads, P.chunk), s>>>(P);
+    CK(launch_pdl(k_p2g_cpic, ctx->p2g_cpic_blocks, ctx->p2g_threads, p2g_dyn_smem(ctx->p2g_threads, P.chunk), s, P));
   else
-    k_p2g<<<ctx->p2g_blocks, ctx->p2g_threads, p2g_dyn_smem(ctx->p2g_threads, P.chunk), s>>>(P);
+    CK(launch_pdl(k_p2g, ctx->p2g_blocks, ctx->p2g_threads, p2g_dyn_smem(ctx->p2g_threads, P.chunk), s, P));
   CKL();
   return MPM_OK;
 }
@@ -345,9 +363,9 @@ int launch_post(mpm_ctx* ctx, int c, cudaStream_t s, bool fuse_grid = false) {
   {
     Timer t(ctx, s, KT_G2P);
     if (ctx->cpic_slots > 0 && ctx->n_colliders > 0)
-      k_g2p_cpic<<<ctx->g2p_cpic_blocks, ctx->g2p_threads, 0, s>>>(P);
+      CK(launch_pdl(k_g2p_cpic, ctx->g2p_cpic_blocks, ctx->g2p_threads, 0, s, P));
     else
-      k_g2p<<<ctx->g2p_blocks, ctx->g2p_threads, 0, s>>>(P);
+      CK(launch_pdl(k_g2p, ctx->g2p_blocks, ctx->g2p_threads, 0, s, P));
   }
   CKL();
   if (ctx->d_cons) {  // after g2p, as substep_post_coupling does (mpm_solver.py:538-540)

@@ -398,6 +398,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_onepass(KParams P) {
   // Only the live tiles take part (a pool's empty slots and the unused blocks of small grids hold
   // no particle, so their buckets are skipped; the captured launch keeps its full CTA count and the
   // extra CTAs return here, before any ticket).
+  pdl_wait();
   const int n_live = *P.n_scan_tiles;
   if ((int)blockIdx.x >= n_live) return;
   if (threadIdx.x == 0) s_tile = atomicAdd(&P.scan_sync[0], 1);
@@ -487,6 +488,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_onepass(KParams P) {
       P.scan_sync[1] = 0;
     }
   }
+  pdl_trigger();
 }
 
 // The whole scan in one CTA (1024 threads) when the bucket count is small: counts -> offsets,
@@ -496,6 +498,7 @@ __global__ void __launch_bounds__(1024) k_scan_single(KParams P) {
   __shared__ int2 s_carry;
   const int64_t nb = P.K + 2;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  pdl_wait();
   if (threadIdx.x == 0) s_carry = make_int2(0, 0);
   __syncthreads();
   for (int64_t k0 = 0; k0 < nb; k0 += blockDim.x) {
@@ -541,6 +544,7 @@ __global__ void __launch_bounds__(1024) k_scan_single(KParams P) {
     __syncthreads();
   }
   if (threadIdx.x == 0) *P.n_items = s_carry.y;
+  pdl_trigger();
 }
 
 
@@ -987,6 +991,7 @@ __device__ __noinline__ float4 cpic_g2p_node(const KParams& P, const SceneDev& S
 
 // Bucket permutation of the sort; also the end-of-substep bookkeeping.
 __global__ void k_perm(KParams P) {
+  pdl_wait();
   const int64_t n = P.n_dev ? *P.n_dev : P.n;
   const int64_t stride = grid_stride_step();
   // four particles per thread and pass, their loads issued together
@@ -1027,6 +1032,7 @@ __global__ void k_perm(KParams P) {
   if (P.steps && blockIdx.x == 0)  // end of a substep: count down per-scene substep budgets
     for (int s = threadIdx.x; s < P.n_scenes; s += blockDim.x)
       if (P.steps[s] > 0) P.steps[s] -= 1;
+  pdl_trigger();
 }
 
 // ------------------------------------------------------------------ P2G
@@ -1146,6 +1152,7 @@ __device__ __forceinline__ void p2g_body(const KParams& P) {
   // the item's scene record, read from shared memory: a reference into the global table would be
   // re-read after every particle store (the compiler cannot rule out aliasing)
   __shared__ SceneDev s_scene;
+  pdl_wait();  // the sort's items and the particles' previous substep
   const int n_items = *P.n_items;
   const int T = blockDim.x, nw = T >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float4* s_tile = reinterpret_cast<float4*>(p2g_smem);
@@ -1450,6 +1457,7 @@ __device__ __forceinline__ void p2g_body(const KParams& P) {
       }
     }
   }
+  pdl_trigger();
 }
 
 // Capped at 96 registers: five 128-thread CTAs per SM instead of four at 128 registers, which
@@ -1481,6 +1489,7 @@ template <bool CPIC>
 __device__ __forceinline__ void g2p_body(const KParams& P) {
   __shared__ float4 s_v[TILE_NODES];
   __shared__ SceneDev s_scene;  // the item's scene record (see p2g_body)
+  pdl_wait();
   if (P.fuse_grid) {
     // the grid op's other duty: zero the blocks the previous substep left in the other buffer
     // (the next P2G adds into it); k_perm resets that list's length after this kernel
@@ -1652,6 +1661,7 @@ __device__ __forceinline__ void g2p_body(const KParams& P) {
     }
     __syncthreads();
   }
+  pdl_trigger();
 }
 
 __global__ void __launch_bounds__(256) k_g2p(KParams P) { g2p_body<false>(P); }

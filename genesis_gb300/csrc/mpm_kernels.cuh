@@ -179,6 +179,13 @@ struct KParams {
   ColliderDev* colliders_rw;   // k_perm advances the tools' poses at the end of a substep (else null)
 };
 
+// Programmatic dependent launch (the substep kernels are launched with programmatic stream
+// serialisation): a kernel may start while its predecessor drains; pdl_wait() returns once the
+// predecessor grid has completed and its writes are visible, and must come before any read of
+// them; pdl_trigger() lets the successor start launching once every CTA of this grid has passed it.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // Block key of a world position; returns false if the stencil would leave the grid.
 __device__ __forceinline__ bool stencil_origin(const SceneDev& S, const float* x, int* b) {
 #pragma unroll
