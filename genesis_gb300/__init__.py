@@ -44,6 +44,7 @@ class options(_types.SimpleNamespace):
     SimOptions = _options_mod.SimOptions
     MPMOptions = _options_mod.MPMOptions
     LegacyCouplerOptions = _options_mod.LegacyCouplerOptions
+    ToolOptions = _options_mod.ToolOptions
     ViewerOptions = _options_mod.ViewerOptions
     VisOptions = _options_mod.VisOptions
     ProfilingOptions = _options_mod.ProfilingOptions
@@ -52,6 +53,7 @@ class options(_types.SimpleNamespace):
 
 class materials(_types.SimpleNamespace):
     MPM = _materials_mod.MPM
+    Tool = _materials_mod.Tool
 
 
 class surfaces(_types.SimpleNamespace):

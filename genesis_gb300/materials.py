@@ -185,3 +185,32 @@ class MPM:
     Snow = Snow
     ElastoPlastic = ElastoPlastic
     Muscle = Muscle
+
+
+class Tool:
+    """genesis/engine/materials/tool.py:13-32: the material of a tool entity (a kinematic mesh
+    that pushes MPM particles through its SDF in the grid op)."""
+
+    _fields = ("friction", "coup_softness", "collision", "sdf_res")
+    friction = 0.0
+    coup_softness = 0.01
+    collision = True
+    sdf_res = 128
+
+    def __init__(self, **kw):
+        unknown = set(kw) - set(self._fields)
+        if unknown:
+            raise GenesisException(f"Unrecognized attribute(s) for Tool: {sorted(unknown)}")
+        for f in self._fields:
+            setattr(self, f, kw.get(f, getattr(type(self), f)))
+        if not (self.friction >= 0) or not (self.coup_softness >= 0):
+            raise GenesisException("Tool friction and coup_softness must be non-negative.")
+        if not isinstance(self.collision, bool):
+            raise GenesisException("Tool collision must be a bool.")
+        if int(self.sdf_res) != self.sdf_res or self.sdf_res < 2:
+            raise GenesisException("Tool sdf_res must be an integer >= 2.")
+        self.sdf_res = int(self.sdf_res)
+        self.idx = None
+
+    def __eq__(self, other) -> bool:
+        return type(self) is type(other) and all(getattr(self, f) == getattr(other, f) for f in self._fields)

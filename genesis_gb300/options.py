@@ -112,6 +112,15 @@ class MPMOptions(Options):
             raise GenesisException("Invalid pair of upper_bound and lower_bound.")
 
 
+class ToolOptions(Options):
+    """genesis/options/solvers.py:376-393: the tool solver's dt and floor height (None: inherited
+    from SimOptions); a tool's position never goes below the floor (FloorBoundary.impose_pos)."""
+
+    _fields = ("dt", "floor_height")
+    dt = None
+    floor_height = None
+
+
 class LegacyCouplerOptions(Options):
     """Accepted for API compatibility; no coupling partner exists in this path."""
 

@@ -14,7 +14,8 @@ import torch
 
 from . import morphs as _morphs
 from .exceptions import GenesisException
-from .options import LegacyCouplerOptions, MPMOptions, ProfilingOptions, SimOptions, ViewerOptions, VisOptions
+from .options import (LegacyCouplerOptions, MPMOptions, ProfilingOptions, SimOptions, ToolOptions, ViewerOptions,
+                      VisOptions)
 from .solver import MPMSolver
 from .states import SimState
 
@@ -127,6 +128,10 @@ class Scene:
         self.vis_options = vis_options or VisOptions()
         self.show_viewer = False
         self._sim = Simulator(self, self.sim_options, self.mpm_options)
+        # ToolOptions.floor_height inherits SimOptions.floor_height (options/solvers.py:376-393)
+        self.tool_options = other_solver_options.get("tool_options") or ToolOptions()
+        floor = self.tool_options.floor_height
+        self._sim.mpm_solver._tool_floor = float(self.sim_options.floor_height if floor is None else floor)
         self._entities = []
         self._emitters = []
         self._is_built = False
@@ -136,10 +141,14 @@ class Scene:
 
     # ------------------------------------------------------------------ construction
     def add_entity(self, morph, material=None, surface=None, visualize_contact=False, vis_mode=None, name=None):
-        from .materials import _MPMBase
+        from .materials import Tool, _MPMBase
 
         if self._is_built:
             raise GenesisException("Scene is already built.")
+        if isinstance(material, Tool):  # ToolSolver.add_entity: a kinematic mesh coupled to MPM
+            entity = self._sim.mpm_solver.add_tool(len(self._entities), material, morph, surface, name=name)
+            self._entities.append(entity)
+            return entity
         if material is None or not isinstance(material, _MPMBase):
             raise GenesisException("Only MPM materials (gs.materials.MPM.*) are supported by this MPM path.")
         if not isinstance(morph, _morphs.Morph):
@@ -202,6 +211,11 @@ class Scene:
             state = state.solvers_state[0]
         if state is not None:
             self._sim.mpm_solver.set_state(0, state, envs_idx)
+        solver = self._sim.mpm_solver
+        if solver._tools:
+            for t in solver._tools:
+                t.reset()
+            solver._upload_colliders()
         self._sim._cur_substep_global = 0
 
     def get_state(self) -> SimState:

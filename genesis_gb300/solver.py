@@ -62,6 +62,9 @@ class MPMSolver:
         self._substep_dt = options.dt / sim.substeps
         self._init_gravity = options.gravity
         self._entities = []
+        self._tools = []  # genesis_gb300.tool.ToolEntity (colliders of shape "tool", after the user's)
+        self._user_colliders = []
+        self._tool_floor = 0.0
         self._materials = []
         self._materials_idx = []
         self._ctx = None
@@ -128,6 +131,14 @@ class MPMSolver:
         self._entities.append(entity)
         return entity
 
+    def add_tool(self, idx, material, morph, surface=None, name=None):
+        """A tool entity (ToolSolver.add_entity) coupled to the MPM particles in the grid op."""
+        from .tool import ToolEntity
+
+        tool = ToolEntity(self._scene, idx, self, material, morph, surface, name=name)
+        self._tools.append(tool)
+        return tool
+
     def _unique_materials(self):
         seen = {}
         for m in self._materials:
@@ -180,11 +191,17 @@ class MPMSolver:
             entity._add_to_solver()
         if getattr(self, "_ffs", None):
             self._upload_force_fields()
+        for t in self._tools:
+            t._build(B, self._tool_floor)
+        if self._tools:
+            self._upload_colliders()
         if self._sim.requires_grad:  # the state lives in torch tensors advanced by the adjoint kernels
             from .grad import SceneDiffEngine
 
             if getattr(self, "_ffs", None):
                 raise GenesisException("Force fields are not supported in differentiable mode.")
+            if self._tools:
+                raise GenesisException("Tool entities are not supported in differentiable mode.")
             self._diff = SceneDiffEngine(self, B)
 
     def _add_particles(self, particle_start, n, material_idx, active, pos_np):
@@ -210,6 +227,11 @@ class MPMSolver:
     def process_input(self, in_backward=False):
         for e in self._entities:
             e.process_input(in_backward=in_backward)
+        if any(t._pending() for t in self._tools):
+            self._sync_tool_poses(user_too=True)
+            for t in self._tools:
+                t.process_input(in_backward=in_backward)
+            self._upload_colliders()
 
     def substeps(self, n: int) -> None:
         """Run n fused substeps (no host sync).  In differentiable mode the n substeps are one autograd
@@ -456,7 +478,33 @@ class MPMSolver:
         """Kinematic rigid colliders coupled in the grid op (genesis_gb300.coupling.Collider list;
         call again whenever they move).  Shapes "sdf" and "tool" carry an SDFGrid, uploaded to the
         device once per grid object; tools then move by themselves every substep (see
-        get_collider_poses)."""
+        get_collider_poses).  The scene's tool entities follow these colliders in the library's
+        list and keep their current poses."""
+        self._sync_tool_poses()
+        self._user_colliders = list(colliders)
+        self._upload_colliders()
+
+    def _sync_tool_poses(self, user_too: bool = False) -> None:
+        """Read back the poses the library advanced: every tool entity's, and with user_too the
+        user colliders of shape "tool" (before their list is uploaded again unchanged)."""
+        if self._ctx is None or not getattr(self, "_n_colliders", 0):
+            return
+        poses = self.get_collider_poses()
+        for t in self._tools:
+            t._sync_pose(poses)
+        if user_too:
+            from .tool import replace_pose
+
+            self._user_colliders = [replace_pose(c, poses[i]) if c.shape == "tool" else c
+                                    for i, c in enumerate(self._user_colliders)]
+
+    def _upload_colliders(self, sync: bool = False) -> None:
+        if sync:
+            self._sync_tool_poses(user_too=True)
+        colliders = list(self._user_colliders)
+        for t in self._tools:
+            t._col0 = len(colliders)
+            colliders += t._colliders()
         if not hasattr(self, "_sdf_ids"):
             self._sdf_ids = {}  # id(SDFGrid) -> (grid, library grid id)
         ids = []

@@ -35,6 +35,25 @@ class MPMEntityState(MPMSolverState):
         self.s_global = s_global
 
 
+class ToolEntityState:
+    """genesis/engine/states/entities.py (ToolEntityState): pos [B, 3], quat [B, 4] (w, x, y, z),
+    vel [B, 3], ang [B, 3] of one tool entity at the current frame."""
+
+    def __init__(self, entity, s_global: int, B: int, device):
+        kw = dict(dtype=torch.float32, device=device)
+        self.entity = entity
+        self.s_global = s_global
+        self.pos = torch.zeros((B, 3), **kw)
+        self.quat = torch.zeros((B, 4), **kw)
+        self.vel = torch.zeros((B, 3), **kw)
+        self.ang = torch.zeros((B, 3), **kw)
+
+    def serializable(self):
+        for k in ("pos", "quat", "vel", "ang"):
+            setattr(self, k, getattr(self, k).detach())
+        return self
+
+
 class SimState:
     """genesis/engine/states/solvers.py:5-43 (only the MPM solver state here)."""
 

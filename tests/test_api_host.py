@@ -300,3 +300,50 @@ def test_custom_force_field_splits_the_field_list_into_grid_op_stages():
     s._ffs = [ff.Drag()]
     s._upload_force_fields()
     assert s._ff_plan is None
+
+
+def test_tool_entity_colliders_inputs_and_sdf(tmp_path):
+    """Tool entity (tool_entity.py, mesh.py) without a GPU: its SDF is the normalised, scaled mesh's
+    (negative at the centre, zero on the faces), it makes one "tool" collider per environment with
+    the Tool material's friction and softness and the floor height, inputs set before a step are
+    applied by process_input (broadcast over environments), and reset returns it to the morph's
+    pose at rest."""
+    import numpy as np
+
+    from genesis_gb300.materials import Tool
+    from genesis_gb300.tool import ToolEntity, replace_pose
+
+    obj = tmp_path / "cube.obj"
+    _cube_obj(obj, half=1.0)
+    morph = morphs.Mesh(file=str(obj), scale=0.1, pos=(0.3, 0.1, 0.28), euler=(90.0, 0.0, 0.0))
+    mat = Tool(friction=8.0, sdf_res=24)
+    with pytest.raises(GenesisException):
+        Tool(friction=-1.0)
+    t = ToolEntity(scene=None, idx=2, solver=None, material=mat, morph=morph)
+    g = t.sdf
+    assert g.values.shape == (24, 24, 24) and g.grads is None
+    # the cube spans [-0.5, 0.5] after normalisation, scaled by 0.1: its centre maps to the grid centre
+    pv = g.T_mesh_to_sdf @ np.array([0.0, 0.0, 0.0, 1.0])
+    assert np.allclose(pv[:3], 11.5)
+    assert g.values.min() < -0.04 and abs(g.values.min() + 0.5) < 0.05  # distance in normalised units
+    t._build(2, floor_height=0.05)
+    cols = t._colliders()
+    assert [c.env for c in cols] == [0, 1] and all(c.shape == "tool" and c.sdf is g for c in cols)
+    assert cols[0].coup_friction == 8.0 and cols[0].coup_softness == 0.01 and cols[0].floor_height == 0.05
+    assert np.allclose(cols[1].pos, (0.3, 0.1, 0.28)) and np.allclose(cols[1].quat, morph.quat)
+    t.set_velocity(vel=(0.0, 1.0, 0.0))
+    t.set_position([[0.3, 0.1, 0.28], [0.3, 0.1, 0.5]])
+    assert t._pending()
+    t.process_input()
+    assert not t._pending()
+    assert np.allclose(t._vel, [[0, 1, 0], [0, 1, 0]]) and np.allclose(t._pos[1], (0.3, 0.1, 0.5))
+    with pytest.raises(GenesisException):
+        t.set_velocity(vel=np.zeros((3, 3)))
+        t.process_input()
+    t._col0 = 1
+    t._sync_pose(np.array([[9.0] * 7, [1, 2, 3, 1, 0, 0, 0], [4, 5, 6, 0, 1, 0, 0]], dtype=np.float64))
+    assert np.allclose(t._pos, [[1, 2, 3], [4, 5, 6]]) and np.allclose(t._quat[1], (0, 1, 0, 0))
+    t.reset()
+    assert np.allclose(t._pos, [(0.3, 0.1, 0.28)] * 2) and not t._vel.any()
+    c2 = replace_pose(cols[0], np.array([1.0, 2.0, 3.0, 0.0, 0.0, 0.0, 1.0]))
+    assert c2.pos == (1.0, 2.0, 3.0) and c2.quat == (0.0, 0.0, 0.0, 1.0) and c2.coup_friction == 8.0

@@ -1027,3 +1027,66 @@ def test_custom_force_field_through_scene_api(gs):
     scene.sim.substep()  # split phases: pre, the staged grid op, post
     assert len(seen_t) == 41 and abs(seen_t[-1] - 40 * 2e-4) < 1e-12
     assert np.isfinite(z0)
+
+
+def test_tool_entity_through_scene_api(gs, tmp_path):
+    """A tool entity through the reference's API (scene.add_entity(morph=gs.morphs.Mesh(...),
+    material=gs.materials.Tool(...)), set_velocity / set_position before a step, get_state) pushing
+    an elastic block: the same run as the tool given through the collider API with the entity's
+    SDF grid; the pose advances by vel * dt every substep and stops at ToolOptions.floor_height;
+    with two environments, tools moving apart leave the two blocks in different places."""
+    from test_api_host import _cube_obj
+
+    from genesis_gb300 import coupling
+
+    obj = tmp_path / "cube.obj"
+    _cube_obj(obj, half=1.0)
+    n_steps, dt, substeps = 6, 2e-3, 10
+
+    def make(n_envs=0, tool=True):
+        scene = gs.Scene(sim_options=gs.options.SimOptions(dt=dt, substeps=substeps),
+                         mpm_options=gs.options.MPMOptions(lower_bound=(0.0, -0.5, 0.0), upper_bound=(1.0, 1.0, 0.55)),
+                         tool_options=gs.options.ToolOptions(floor_height=0.02))
+        t = None
+        if tool:
+            t = scene.add_entity(morph=gs.morphs.Mesh(file=str(obj), scale=0.1, pos=(0.3, 0.16, 0.1)),
+                                 material=gs.materials.Tool(friction=2.0))
+        block = scene.add_entity(morph=gs.morphs.Box(lower=(0.2, 0.2, 0.05), upper=(0.4, 0.35, 0.15)),
+                                 material=gs.materials.MPM.Elastic(rho=500, sampler="regular"))
+        scene.build(n_envs=n_envs)
+        return scene, t, block
+
+    scene, tool, block = make()
+    tool.set_velocity(vel=(0.0, 1.0, -0.5))
+    for _ in range(n_steps):
+        scene.step()
+    got = block.get_particles_pos().double().cpu().numpy()
+    st = tool.get_state()
+    t_end = n_steps * dt
+    want = np.array([0.3, 0.16 + t_end, max(0.1 - 0.5 * t_end, 0.02)])
+    assert np.abs(st.pos[0].double().cpu().numpy() - want).max() < 1e-5, st.pos
+    assert np.allclose(st.vel[0].cpu().numpy(), (0.0, 1.0, -0.5))
+
+    ref_scene, _, ref_block = make(tool=False)
+    ref_scene.sim.mpm_solver.set_colliders([coupling.tool(tool.sdf, pos=(0.3, 0.16, 0.1), vel=(0.0, 1.0, -0.5),
+                                                         friction=2.0, coup_softness=0.01, floor_height=0.02)])
+    for _ in range(n_steps):
+        ref_scene.step()
+    ref = ref_block.get_particles_pos().double().cpu().numpy()
+    assert np.abs(got - ref).max() <= 1e-6, np.abs(got - ref).max()
+    moved = np.abs(got - block.init_particles).max()
+    assert moved > 1e-3  # the tool pushed the block
+
+    # the floor stops it: 0.1 - 50 * t > 0.02 fails after 1.6 ms
+    tool.set_velocity(vel=(0.0, 0.0, -50.0))
+    scene.step()
+    assert abs(tool.get_state().pos[0, 2].item() - 0.02) < 1e-6
+
+    scene2, tool2, block2 = make(n_envs=2)
+    tool2.set_velocity(vel=[[0.0, 1.0, 0.0], [0.0, -1.0, 0.0]])
+    for _ in range(n_steps):
+        scene2.step()
+    p = block2.get_particles_pos().double().cpu().numpy()
+    assert np.abs(p[0] - p[1]).max() > 1e-3
+    s2 = tool2.get_state().pos.double().cpu().numpy()
+    assert abs(s2[0, 1] - (0.16 + t_end)) < 1e-5 and abs(s2[1, 1] - (0.16 - t_end)) < 1e-5
