@@ -127,6 +127,23 @@ class MpmForceField(ctypes.Structure):
 FF_CONSTANT, FF_WIND, FF_POINT, FF_DRAG, FF_VORTEX, FF_NOISE, FF_TURBULENCE = 0, 1, 2, 3, 4, 5, 6
 
 
+class MpmDiffTool(ctypes.Structure):
+    """mpm_diff_tool (gbmpm.h): a tool of the differentiable form."""
+
+    _fields_ = [
+        ("sdf", c_void_p),
+        ("res", c_int32 * 3),
+        ("pad0", c_int32),
+        ("T_mesh_to_sdf", c_double * 16),
+        ("friction", c_double),
+        ("softness", c_double),
+        ("floor_height", c_double),
+    ]
+
+
+DIFF_MAX_TOOLS = 4
+
+
 class MpmSceneConfig(ctypes.Structure):
     _fields_ = [
         ("substep_dt", c_double),
@@ -182,6 +199,10 @@ _SIGNATURES = {
                                           _P, _P, c_int32, _P, _P]),
     "mpm_diff_backward_seq_pp": (c_int32, [_P, _P, _P, _P, c_int64, c_int32, _P, _P, _P, _P, _P, _P, _P, _P,
                                            _P, _P, _P, _P, _P, _P, _P, _P]),
+    "mpm_diff_forward_seq_tools": (c_int32, [_P, _P, _P, _P, c_int64, c_int32, _P, _P, _P, _P, _P, c_int32, _P, _P,
+                                             _P, c_int32, _P, _P, _P, c_int32, _P, _P]),
+    "mpm_diff_backward_seq_tools": (c_int32, [_P, _P, _P, _P, c_int64, c_int32, _P, _P, _P, _P, _P, _P, _P, _P,
+                                              c_int32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "mpm_set_force_fields": (c_int32, [_P, c_int32, _P]),
     "mpm_sample_regular": (c_int32, [c_int32, _P, _P, c_double, _P, c_int64, _P, _P]),
     "mpm_test_wait_timeout": (c_int32, [_P, _P]),

@@ -14,12 +14,14 @@
 // scatter uses global vector atomics (no sort): the differentiable path favours clarity.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstring>
 #include <string>
 
 #include "gbmpm.h"
 #include "mpm_adjoint.cuh"
 #include "mpm_kernels.cuh"
+#include "mpm_tool_adjoint.cuh"
 
 namespace gbmpm {
 int derive_scene(const mpm_scene_config& c, SceneDev& S, std::string& err);
@@ -48,6 +50,12 @@ struct DiffParams {
   float4* g_grid_v;   // adjoint of the node velocity (xyz)
   float4* g_grid_pm;  // adjoint of (momentum, mass)
   uint32_t* status;
+  // tool entities of the scene (Mesh.collide in the grid op, legacy_coupler.py:386-387)
+  int32_t n_tools;
+  DiffToolDev tools[MPM_DIFF_MAX_TOOLS];
+  const float* tool_f;  // tool states (pos 3, quat 4, vel 3, ang 3) at this substep [n_tools][13]
+  float* tool_f1;       // ... one substep later (written by k_dtool_advance)
+  float* g_tool;        // [n_tools][12]: dL/d(pos, vel) of the next state (in) / this one (out); accumulator
 };
 
 __device__ __forceinline__ int64_t didx(const SceneDev& S, int gx, int gy, int gz) {
@@ -193,6 +201,18 @@ __global__ void __launch_bounds__(256) k_dp2g(DiffParams Q) {
   }
 }
 
+// Tools advance one substep (ToolEntity.advect) before the grid op that needs both poses.
+__global__ void k_dtool_advance(DiffParams Q) {
+  const int t = threadIdx.x;
+  if (t < Q.n_tools)
+    tool_advance_state(Q.tool_f + t * 13, Q.S.dt, Q.S.eps, Q.tools[t].floor_h, Q.tool_f1 + t * 13);
+}
+
+__device__ __forceinline__ void node_world_pos(const SceneDev& S, const int* g, float* x) {
+#pragma unroll
+  for (int d = 0; d < 3; ++d) x[d] = (float)(g[d] + S.offset[d]) * S.dx;
+}
+
 __global__ void k_dgrid(DiffParams Q, int64_t nodes) {
   const SceneDev& S = Q.S;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nodes; i += (int64_t)gridDim.x * blockDim.x) {
@@ -204,6 +224,14 @@ __global__ void k_dgrid(DiffParams Q, int64_t nodes) {
       v[0] = inv * q.x + S.dt * S.grav[0];
       v[1] = inv * q.y + S.dt * S.grav[1];
       v[2] = inv * q.z + S.dt * S.grav[2];
+      if (Q.n_tools > 0) {
+        float x[3];
+        node_world_pos(S, g, x);
+        for (int t = 0; t < Q.n_tools; ++t) {
+          const float* st = Q.tool_f + t * 13;
+          tool_collide_t<float>(Q.tools[t], x, v, st, st + 3, st + 7, Q.tool_f1 + t * 13 + 3, S.dt, S.eps);
+        }
+      }
       for (int d = 0; d < 3; ++d) {
         const float p = (float)(g[d] + S.offset[d]) * S.dx;
         if ((p >= S.hi[d] && v[d] >= 0.f) || (p <= S.lo[d] && v[d] <= 0.f)) v[d] = 0.f;
@@ -314,26 +342,86 @@ __global__ void __launch_bounds__(256) k_dg2p_adj(DiffParams Q) {
 // grid-op adjoint: v = B(p/m + dt g) -> dL/dp, dL/dm
 __global__ void k_dgrid_adj(DiffParams Q, int64_t nodes) {
   const SceneDev& S = Q.S;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nodes; i += (int64_t)gridDim.x * blockDim.x) {
-    const float4 q = Q.pm[i];
+  const int lane = threadIdx.x & 31;
+  for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x; i0 < nodes; i0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = i0 + threadIdx.x;  // warp-uniform loop: the tool sums are reduced across the warp
+    const float4 q = i < nodes ? Q.pm[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (q.w > S.eps) {
+    float tacc[MPM_DIFF_MAX_TOOLS][6];
+    for (int t = 0; t < Q.n_tools; ++t)
+      for (int k = 0; k < 6; ++k) tacc[t][k] = 0.f;
+    if (i < nodes && q.w > S.eps) {
       const float4 gv = Q.g_grid_v[i];
       const int g[3] = {(int)(i / ((int64_t)S.res[1] * S.res[2])), (int)((i / S.res[2]) % S.res[1]), (int)(i % S.res[2])};
       const float inv = 1.f / q.w;
-      const float u[3] = {inv * q.x + S.dt * S.grav[0], inv * q.y + S.dt * S.grav[1], inv * q.z + S.dt * S.grav[2]};
+      float u[3] = {inv * q.x + S.dt * S.grav[0], inv * q.y + S.dt * S.grav[1], inv * q.z + S.dt * S.grav[2]};
       float gu[3] = {gv.x, gv.y, gv.z};
-      for (int d = 0; d < 3; ++d) {
+      float vin[MPM_DIFF_MAX_TOOLS][3];
+      float x[3];
+      node_world_pos(S, g, x);
+      for (int t = 0; t < Q.n_tools; ++t) {  // forward through the tools, keeping each one's input
+        for (int k = 0; k < 3; ++k) vin[t][k] = u[k];
+        const float* st = Q.tool_f + t * 13;
+        tool_collide_t<float>(Q.tools[t], x, u, st, st + 3, st + 7, Q.tool_f1 + t * 13 + 3, S.dt, S.eps);
+      }
+      for (int d = 0; d < 3; ++d) {  // the boundary acts on the velocity the tools left
         const float p = (float)(g[d] + S.offset[d]) * S.dx;
         if ((p >= S.hi[d] && u[d] >= 0.f) || (p <= S.lo[d] && u[d] <= 0.f)) gu[d] = 0.f;
+      }
+      for (int t = Q.n_tools - 1; t >= 0; --t) {  // back through the tools: Jacobians from dual numbers
+        const float* st = Q.tool_f + t * 13;
+        TD vt[3], pt[3], ut[3];
+        for (int k = 0; k < 3; ++k) {
+          vt[k] = td_var(vin[t][k], k);
+          pt[k] = td_var(st[k], 3 + k);
+          ut[k] = td_var(st[7 + k], 6 + k);
+        }
+        tool_collide_t<TD>(Q.tools[t], x, vt, pt, st + 3, ut, Q.tool_f1 + t * 13 + 3, S.dt, S.eps);
+        float gin[3];
+        for (int j = 0; j < 3; ++j) {
+          gin[j] = gu[0] * vt[0].d[j] + gu[1] * vt[1].d[j] + gu[2] * vt[2].d[j];
+          tacc[t][j] = gu[0] * vt[0].d[3 + j] + gu[1] * vt[1].d[3 + j] + gu[2] * vt[2].d[3 + j];
+          tacc[t][3 + j] = gu[0] * vt[0].d[6 + j] + gu[1] * vt[1].d[6 + j] + gu[2] * vt[2].d[6 + j];
+        }
+        for (int j = 0; j < 3; ++j) gu[j] = gin[j];
       }
       out.x = gu[0] * inv;
       out.y = gu[1] * inv;
       out.z = gu[2] * inv;
       out.w = -(gu[0] * q.x + gu[1] * q.y + gu[2] * q.z) * inv * inv;
     }
-    Q.g_grid_pm[i] = out;
+    if (i < nodes) Q.g_grid_pm[i] = out;
+    for (int t = 0; t < Q.n_tools; ++t)  // the tool's share of dL/d(pos, vel), one atomic per warp
+      for (int k = 0; k < 6; ++k) {
+        float a = tacc[t][k];
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+        if (lane == 0 && a != 0.f) atomicAdd(Q.g_tool + t * 12 + 6 + k, a);
+      }
   }
+}
+
+// The tool state chain backwards over one substep (ToolEntity.advect: pos' = max(pos + vel dt,
+// floor) in z, vel' = vel), plus this substep's collision terms; the accumulator is cleared.
+__global__ void k_dtool_adj(DiffParams Q) {
+  const int t = threadIdx.x;
+  if (t >= Q.n_tools) return;
+  float* g = Q.g_tool + t * 12;
+  const float* s = Q.tool_f + t * 13;
+  const bool clamped = s[2] + s[9] * Q.S.dt < Q.tools[t].floor_h;
+  float gp[3] = {g[0], g[1], clamped ? 0.f : g[2]};
+  for (int k = 0; k < 3; ++k) {
+    const float gpk = gp[k];
+    g[k] = gpk + g[6 + k];
+    g[3 + k] = g[3 + k] + Q.S.dt * gpk + g[9 + k];
+    g[6 + k] = 0.f;
+    g[9 + k] = 0.f;
+  }
+}
+
+__global__ void k_dtool_zero_acc(DiffParams Q) {
+  const int t = threadIdx.x;
+  if (t < Q.n_tools)
+    for (int k = 6; k < 12; ++k) Q.g_tool[t * 12 + k] = 0.f;
 }
 
 // Adjoint of the rotation of the polar decomposition: given Rbar = dL/dR, returns dL/dF
@@ -569,7 +657,8 @@ namespace {
 int diff_forward(const mpm_scene_config* scene, double rho, int32_t neohookean, const float* mass_pp,
                  const int32_t* kind_pp, const float* aux, int64_t n, const float* x, const float* v, const float* C,
                  const float* F, const float* Jp, const float* mu, const float* lam, float* x1, float* v1, float* C1,
-                 float* F1, float* Jp1, void* grid_pm, void* grid_v, uint32_t* status, void* stream) {
+                 float* F1, float* Jp1, void* grid_pm, void* grid_v, uint32_t* status, void* stream, int n_tools = 0,
+                 const DiffToolDev* tools = nullptr, const float* tool_f = nullptr, float* tool_f1 = nullptr) {
   if (!scene || n < 0 || !grid_pm || !grid_v || !status) return MPM_ERR_BAD_ARG;
   DiffParams Q;
   std::memset(&Q, 0, sizeof(Q));
@@ -588,12 +677,17 @@ int diff_forward(const mpm_scene_config* scene, double rho, int32_t neohookean, 
   Q.pm = (float4*)grid_pm;
   Q.gvel = (float4*)grid_v;
   Q.status = status;
+  Q.n_tools = n_tools;
+  for (int t = 0; t < n_tools; ++t) Q.tools[t] = tools[t];
+  Q.tool_f = tool_f;
+  Q.tool_f1 = tool_f1;
   const int64_t nodes = (int64_t)Q.S.res[0] * Q.S.res[1] * Q.S.res[2];
   cudaStream_t s = (cudaStream_t)stream;
   const int gb = (int)((nodes + 255) / 256 < 8192 ? (nodes + 255) / 256 : 8192);
   const int pb = (int)((n + 255) / 256 < 8192 ? (n + 255) / 256 : 8192);
   k_dclear<<<gb, 256, 0, s>>>(Q, nodes, Q.pm);
   if (n > 0) k_dp2g<<<pb, 256, 0, s>>>(Q);
+  if (n_tools > 0) k_dtool_advance<<<1, 32, 0, s>>>(Q);
   k_dgrid<<<gb, 256, 0, s>>>(Q, nodes);
   if (n > 0) k_dg2p<<<pb, 256, 0, s>>>(Q);
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_ERR_CUDA;
@@ -604,7 +698,9 @@ int diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean,
                   const float* F, const float* Jp, const float* mu, const float* lam, const float* gx1,
                   const float* gv1, const float* gC1, const float* gF1, const float* gJp1, float* gx, float* gv,
                   float* gC, float* gF, float* gJp, float* gmu, float* glam, void* grid_pm, void* grid_v,
-                  void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream) {
+                  void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream, int n_tools = 0,
+                  const DiffToolDev* tools = nullptr, const float* tool_f = nullptr, const float* tool_f1 = nullptr,
+                  float* g_tool = nullptr) {
   if (!scene || n < 0 || !grid_pm || !grid_v || !g_grid_v || !g_grid_pm) return MPM_ERR_BAD_ARG;
   DiffParams Q;
   std::memset(&Q, 0, sizeof(Q));
@@ -626,6 +722,11 @@ int diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean,
   Q.g_grid_v = (float4*)g_grid_v;
   Q.g_grid_pm = (float4*)g_grid_pm;
   Q.status = status;
+  Q.n_tools = n_tools;
+  for (int t = 0; t < n_tools; ++t) Q.tools[t] = tools[t];
+  Q.tool_f = tool_f;
+  Q.tool_f1 = const_cast<float*>(tool_f1);
+  Q.g_tool = g_tool;
   const int64_t nodes = (int64_t)Q.S.res[0] * Q.S.res[1] * Q.S.res[2];
   cudaStream_t s = (cudaStream_t)stream;
   const int gb = (int)((nodes + 255) / 256 < 8192 ? (nodes + 255) / 256 : 8192);
@@ -633,6 +734,7 @@ int diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean,
   k_dclear<<<gb, 256, 0, s>>>(Q, nodes, Q.g_grid_v);
   if (n > 0) k_dg2p_adj<<<pb, 256, 0, s>>>(Q);
   k_dgrid_adj<<<gb, 256, 0, s>>>(Q, nodes);
+  if (n_tools > 0) k_dtool_adj<<<1, 32, 0, s>>>(Q);
   if (n > 0) k_dp2g_adj<<<pb, 256, 0, s>>>(Q);
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_ERR_CUDA;
 }
@@ -640,7 +742,8 @@ int diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean,
 int diff_forward_seq(const mpm_scene_config* scene, double rho, int32_t neohookean, const float* mass_pp,
                      const int32_t* kind_pp, const float* aux, int64_t n, int32_t n_sub, float* x_seq, float* v_seq,
                      float* C_seq, float* F_seq, float* Jp_seq, int32_t ring, const float* mu, const float* lam,
-                     void* grid_pm, void* grid_v, int32_t grids_per_substep, uint32_t* status, void* stream) {
+                     void* grid_pm, void* grid_v, int32_t grids_per_substep, uint32_t* status, void* stream,
+                     int n_tools = 0, const DiffToolDev* tools = nullptr, float* tool_seq = nullptr) {
   if (!scene || n < 0 || n_sub < 0 || ring < 2 || !x_seq || !v_seq || !C_seq || !F_seq) return MPM_ERR_BAD_ARG;
   SceneDev S;
   std::string err;
@@ -653,7 +756,8 @@ int diff_forward_seq(const mpm_scene_config* scene, double rho, int32_t neohooke
                                v_seq + a * n * 3, C_seq + a * n * 9, F_seq + a * n * 9, Jp_seq ? Jp_seq + a * n : nullptr,
                                mu, lam, x_seq + b * n * 3, v_seq + b * n * 3, C_seq + b * n * 9, F_seq + b * n * 9,
                                Jp_seq ? Jp_seq + b * n : nullptr, (float4*)grid_pm + go, (float4*)grid_v + go, status,
-                               stream);
+                               stream, n_tools, tools, tool_seq ? tool_seq + (int64_t)k * n_tools * 13 : nullptr,
+                               tool_seq ? tool_seq + (int64_t)(k + 1) * n_tools * 13 : nullptr);
     if (r) return r;
   }
   return MPM_OK;
@@ -664,8 +768,16 @@ int diff_backward_seq(const mpm_scene_config* scene, double rho, int32_t neohook
                       const int32_t* kind_pp, const float* aux, int64_t n, int32_t n_sub, const float* x_seq,
                       const float* v_seq, const float* C_seq, const float* F_seq, const float* Jp_seq, const float* mu,
                       const float* lam, float* g_seq, float* gmu, float* glam, void* grid_pm, void* grid_v,
-                      void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream) {
+                      void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream, int n_tools = 0,
+                      const DiffToolDev* tools = nullptr, const float* tool_seq = nullptr, float* g_tool = nullptr) {
   if (!scene || n < 0 || n_sub < 0 || !g_seq) return MPM_ERR_BAD_ARG;
+  if (n_tools > 0) {
+    DiffParams Qz;
+    std::memset(&Qz, 0, sizeof(Qz));
+    Qz.n_tools = n_tools;
+    Qz.g_tool = g_tool;
+    k_dtool_zero_acc<<<1, 32, 0, (cudaStream_t)stream>>>(Qz);
+  }
   SceneDev S;
   std::string err;
   if (derive_scene(*scene, S, err)) return MPM_ERR_BAD_ARG;
@@ -680,13 +792,43 @@ int diff_backward_seq(const mpm_scene_config* scene, double rho, int32_t neohook
                                 Jp_seq ? Jp_seq + (int64_t)k * n : nullptr, mu, lam, gi, gi + 3 * n, gi + 6 * n,
                                 gi + 15 * n, Jp_seq ? gi + 24 * n : nullptr, go, go + 3 * n, go + 6 * n, go + 15 * n,
                                 Jp_seq ? go + 24 * n : nullptr, gmu, glam, (float4*)grid_pm + (int64_t)k * nodes,
-                                (float4*)grid_v + (int64_t)k * nodes, g_grid_v, g_grid_pm, status, stream);
+                                (float4*)grid_v + (int64_t)k * nodes, g_grid_v, g_grid_pm, status, stream, n_tools,
+                                tools, tool_seq ? tool_seq + (int64_t)k * n_tools * 13 : nullptr,
+                                tool_seq ? tool_seq + (int64_t)(k + 1) * n_tools * 13 : nullptr, g_tool);
     if (r) return r;
     cur = 1 - cur;
   }
   if (cur == 1 && cudaMemcpyAsync(g_seq, g_seq + gs, sizeof(float) * gs, cudaMemcpyDeviceToDevice,
                                   (cudaStream_t)stream) != cudaSuccess)
     return MPM_ERR_CUDA;
+  return MPM_OK;
+}
+
+// The caller's tool records as the kernels read them (T_mesh_to_sdf rows and the inverse of
+// its 3x3 block in float, computed in double).
+int diff_tools_dev(const mpm_diff_tool* tools, int32_t n_tools, const void* tool_seq, DiffToolDev* out) {
+  if (n_tools < 0 || n_tools > MPM_DIFF_MAX_TOOLS || (n_tools > 0 && (!tools || !tool_seq))) return MPM_ERR_BAD_ARG;
+  for (int t = 0; t < n_tools; ++t) {
+    const mpm_diff_tool& a = tools[t];
+    DiffToolDev& d = out[t];
+    if (!a.sdf || a.res[0] < 2 || a.res[1] < 2 || a.res[2] < 2) return MPM_ERR_BAD_ARG;
+    d.sdf = a.sdf;
+    for (int k = 0; k < 3; ++k) d.res[k] = a.res[k];
+    for (int k = 0; k < 12; ++k) d.T[k] = (float)a.T_mesh_to_sdf[k];
+    const double* T = a.T_mesh_to_sdf;
+    const double det = T[0] * (T[5] * T[10] - T[6] * T[9]) - T[1] * (T[4] * T[10] - T[6] * T[8]) +
+                       T[2] * (T[4] * T[9] - T[5] * T[8]);
+    if (!(std::fabs(det) > 0)) return MPM_ERR_BAD_ARG;
+    const double inv[9] = {(T[5] * T[10] - T[6] * T[9]) / det, (T[2] * T[9] - T[1] * T[10]) / det,
+                           (T[1] * T[6] - T[2] * T[5]) / det,  (T[6] * T[8] - T[4] * T[10]) / det,
+                           (T[0] * T[10] - T[2] * T[8]) / det, (T[2] * T[4] - T[0] * T[6]) / det,
+                           (T[4] * T[9] - T[5] * T[8]) / det,  (T[1] * T[8] - T[0] * T[9]) / det,
+                           (T[0] * T[5] - T[1] * T[4]) / det};
+    for (int k = 0; k < 9; ++k) d.Rinv[k] = (float)inv[k];
+    d.friction = (float)a.friction;
+    d.softness = (float)a.softness;
+    d.floor_h = (float)a.floor_height;
+  }
   return MPM_OK;
 }
 
@@ -767,6 +909,35 @@ int mpm_diff_backward_seq_pp(const mpm_scene_config* scene, const float* mass, c
   if (n > 0 && (!mass || !kind || !aux || !Jp_seq)) return MPM_ERR_BAD_ARG;
   return diff_backward_seq(scene, 0.0, 0, mass, kind, aux, n, n_sub, x_seq, v_seq, C_seq, F_seq, Jp_seq, mu, lam,
                            g_seq, gmu, glam, grid_pm, grid_v, g_grid_v, g_grid_pm, status, stream);
+}
+
+int mpm_diff_forward_seq_tools(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
+                               int64_t n, int32_t n_sub, float* x_seq, float* v_seq, float* C_seq, float* F_seq,
+                               float* Jp_seq, int32_t ring, const float* mu, const float* lam,
+                               const mpm_diff_tool* tools, int32_t n_tools, float* tool_seq, void* grid_pm,
+                               void* grid_v, int32_t grids_per_substep, uint32_t* status, void* stream) {
+  if (n > 0 && (!mass || !kind || !aux || !Jp_seq)) return MPM_ERR_BAD_ARG;
+  DiffToolDev td[MPM_DIFF_MAX_TOOLS];
+  const int r = diff_tools_dev(tools, n_tools, tool_seq, td);
+  if (r) return r;
+  return diff_forward_seq(scene, 0.0, 0, mass, kind, aux, n, n_sub, x_seq, v_seq, C_seq, F_seq, Jp_seq, ring, mu, lam,
+                          grid_pm, grid_v, grids_per_substep, status, stream, n_tools, td, tool_seq);
+}
+
+int mpm_diff_backward_seq_tools(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
+                                int64_t n, int32_t n_sub, const float* x_seq, const float* v_seq, const float* C_seq,
+                                const float* F_seq, const float* Jp_seq, const float* mu, const float* lam,
+                                const mpm_diff_tool* tools, int32_t n_tools, const float* tool_seq, float* g_tool,
+                                float* g_seq, float* gmu, float* glam, void* grid_pm, void* grid_v, void* g_grid_v,
+                                void* g_grid_pm, uint32_t* status, void* stream) {
+  if (n > 0 && (!mass || !kind || !aux || !Jp_seq)) return MPM_ERR_BAD_ARG;
+  DiffToolDev td[MPM_DIFF_MAX_TOOLS];
+  const int r = diff_tools_dev(tools, n_tools, tool_seq, td);
+  if (r) return r;
+  if (n_tools > 0 && !g_tool) return MPM_ERR_BAD_ARG;
+  return diff_backward_seq(scene, 0.0, 0, mass, kind, aux, n, n_sub, x_seq, v_seq, C_seq, F_seq, Jp_seq, mu, lam,
+                           g_seq, gmu, glam, grid_pm, grid_v, g_grid_v, g_grid_pm, status, stream, n_tools, td,
+                           tool_seq, g_tool);
 }
 
 }  // extern "C"

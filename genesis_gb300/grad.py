@@ -18,7 +18,11 @@ reference's process_input_grad puts them.
 
 Materials: Elastic (corotated or neo-Hookean), Liquid, Sand and Snow, any mix of entities;
 particle masses, Lame parameters and plasticity constants per particle, Jp part of the
-differentiated state.  As in the reference, CPIC and emitters are rejected in this mode.
+differentiated state.  Tool entities (tool_entity/) are part of the step: each env's state also
+holds every tool's position and velocity ([n_tools, 6], differentiated through Mesh.collide in the
+grid op and ToolEntity.advect, mpm_diff_forward_seq_tools / mpm_diff_backward_seq_tools) and, as
+plain tensors, its orientation and angular velocity.  As in the reference, CPIC and emitters are
+rejected in this mode.
 """
 
 from __future__ import annotations
@@ -56,20 +60,24 @@ def material_kind(material) -> tuple[int, float, float]:
 
 
 class _StepNode(torch.autograd.Function):
-    """One scene.step() of one env: (x, v, C, F, Jp) -> state after n_sub substeps."""
+    """One scene.step() of one env: (x, v, C, F, Jp, tool pos/vel) -> the state after n_sub substeps,
+    plus the tools' orientation and angular velocity (not differentiated)."""
 
     @staticmethod
-    def forward(ctx, engine, n_sub, x, v, C, F, Jp):
-        st = tuple(t.detach().float().contiguous() for t in (x, v, C, F, Jp))
-        out = engine.run_forward(st, n_sub)
+    def forward(ctx, engine, n_sub, qa, x, v, C, F, Jp, T):
+        st = tuple(t.detach().float().contiguous() for t in (x, v, C, F, Jp, T))
+        qa = qa.detach().float().contiguous()
+        out, qa_end = engine.run_forward(st, n_sub, qa)
         ctx.engine, ctx.n_sub = engine, n_sub
-        ctx.save_for_backward(*st)  # the step's checkpoint
-        return out
+        ctx.save_for_backward(*st, qa)  # the step's checkpoint
+        ctx.mark_non_differentiable(qa_end)
+        return (*out, qa_end)
 
     @staticmethod
-    def backward(ctx, gx, gv, gC, gF, gJp):
-        grads = ctx.engine.run_backward(ctx.saved_tensors, ctx.n_sub, (gx, gv, gC, gF, gJp))
-        return (None, None, *grads)
+    def backward(ctx, gx, gv, gC, gF, gJp, gT, _gqa):
+        saved = ctx.saved_tensors
+        grads = ctx.engine.run_backward(saved[:6], ctx.n_sub, (gx, gv, gC, gF, gJp, gT), saved[6])
+        return (None, None, None, *grads)
 
 
 class SceneDiffEngine:
@@ -125,8 +133,10 @@ class SceneDiffEngine:
         eye = torch.eye(3, device=dev)
         self.Jp0 = torch.cat([torch.full((e.n_particles,), float(e.material._default_Jp), device=dev) for e in ents]) \
             if ents else torch.zeros(0, device=dev)
+        self._init_tools(solver)
         self.states = [(x0.clone(), torch.zeros((n, 3), device=dev), torch.zeros((n, 3, 3), device=dev),
-                        eye.repeat(n, 1, 1), self.Jp0.clone()) for _ in range(B)]
+                        eye.repeat(n, 1, 1), self.Jp0.clone(), self.T0.clone()) for _ in range(B)]
+        self.tool_qa = [self.qa0.clone() for _ in range(B)]
         self.steps_taken = 0
         self.substeps_taken = 0
         self.step_inputs = []  # per step: (per-env state at the step start, substeps)
@@ -134,7 +144,43 @@ class SceneDiffEngine:
         self.cursor = 0
         self._seg = None
         self.queried = []      # (global substep, state, first row) returned by get_state, for collect_output_grads
+        self.queried_tools = []  # (global substep, tool state, tool index) returned by ToolEntity.get_state
         self.pending = []      # entity inputs written since the last step: (field, start, count, values, envs)
+
+    def _init_tools(self, solver) -> None:
+        """The tools of the scene as the library's differentiable form takes them."""
+        tools = list(getattr(solver, "_tools", []))
+        if len(tools) > _lib.DIFF_MAX_TOOLS:
+            raise GenesisException(f"At most {_lib.DIFF_MAX_TOOLS} tool entities in differentiable mode.")
+        if any(t.sdf is None for t in tools):
+            raise GenesisException("Tool entities without collision are not supported in differentiable mode.")
+        self.tools = tools
+        self.tool_sdf = [torch.as_tensor(t.sdf.values, dtype=torch.float32, device="cuda").contiguous() for t in tools]
+        self.tool_recs = (_lib.MpmDiffTool * max(1, len(tools)))()
+        for rec, t, sdf in zip(self.tool_recs, tools, self.tool_sdf):
+            rec.sdf = sdf.data_ptr()
+            rec.res[:] = tuple(int(r) for r in sdf.shape)
+            rec.T_mesh_to_sdf[:] = tuple(float(v) for v in np.asarray(t.sdf.T_mesh_to_sdf, np.float64).reshape(-1))
+            rec.friction = float(t.material.friction)
+            rec.softness = float(t.material.coup_softness)
+            rec.floor_height = float(solver._tool_floor)
+        nt = len(tools)
+        self.T0 = torch.zeros((nt, 6), device="cuda")
+        self.qa0 = torch.zeros((nt, 7), device="cuda")
+        for i, t in enumerate(tools):
+            self.T0[i, :3] = torch.as_tensor(t.init_pos, dtype=torch.float32)
+            self.qa0[i, :4] = torch.as_tensor(t.init_quat, dtype=torch.float32)
+
+    def _tool_seq(self, n_sub, T, qa):
+        """[(n_sub + 1), n_tools, 13] tool states, entry 0 from (pos, vel) T and (quat, ang) qa."""
+        nt = len(self.tools)
+        seq = torch.zeros((n_sub + 1, max(1, nt), 13), device="cuda")
+        if nt:
+            seq[0, :nt, 0:3] = T[:, 0:3].detach()
+            seq[0, :nt, 3:7] = qa[:, 0:4]
+            seq[0, :nt, 7:10] = T[:, 3:6].detach()
+            seq[0, :nt, 10:13] = qa[:, 4:7]
+        return seq
 
     # ---------------------------------------------------------------- kernels
     @staticmethod
@@ -151,24 +197,35 @@ class SceneDiffEngine:
                 t[0] = f.detach()
         return seq
 
-    def _forward_seq(self, seq, n_sub, ring, gpm, gv, keep_grids):
-        r = self.lib.mpm_diff_forward_seq_pp(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(),
-                                             self.aux.data_ptr(), self.n, int(n_sub), *[t.data_ptr() for t in seq],
-                                             ring, self.mu.data_ptr(), self.lam.data_ptr(), gpm.data_ptr(),
-                                             gv.data_ptr(), int(keep_grids), self.status.data_ptr(), self._s())
-        _lib.check(r, None, "mpm_diff_forward_seq_pp")
+    def _forward_seq(self, seq, n_sub, ring, gpm, gv, keep_grids, tool_seq):
+        nt = len(self.tools)
+        r = self.lib.mpm_diff_forward_seq_tools(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(),
+                                                self.aux.data_ptr(), self.n, int(n_sub), *[t.data_ptr() for t in seq],
+                                                ring, self.mu.data_ptr(), self.lam.data_ptr(), self.tool_recs, nt,
+                                                tool_seq.data_ptr() if nt else None, gpm.data_ptr(), gv.data_ptr(),
+                                                int(keep_grids), self.status.data_ptr(), self._s())
+        _lib.check(r, None, "mpm_diff_forward_seq_tools")
 
-    def _backward_seq(self, seq, n_sub, gp, gpm, gv):
+    def _backward_seq(self, seq, n_sub, gp, gpm, gv, tool_seq, g_tool):
         n = self.n
+        nt = len(self.tools)
         gmu = torch.zeros(n, device="cuda")
         glam = torch.zeros(n, device="cuda")
-        r = self.lib.mpm_diff_backward_seq_pp(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(),
-                                              self.aux.data_ptr(), n, int(n_sub), *[t.data_ptr() for t in seq],
-                                              self.mu.data_ptr(), self.lam.data_ptr(), gp.data_ptr(), gmu.data_ptr(),
-                                              glam.data_ptr(), gpm.data_ptr(), gv.data_ptr(),
-                                              self.g_grid_v.data_ptr(), self.g_grid_pm.data_ptr(),
-                                              self.status.data_ptr(), self._s())
-        _lib.check(r, None, "mpm_diff_backward_seq_pp")
+        r = self.lib.mpm_diff_backward_seq_tools(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(),
+                                                 self.aux.data_ptr(), n, int(n_sub), *[t.data_ptr() for t in seq],
+                                                 self.mu.data_ptr(), self.lam.data_ptr(), self.tool_recs, nt,
+                                                 tool_seq.data_ptr() if nt else None,
+                                                 g_tool.data_ptr() if nt else None, gp.data_ptr(), gmu.data_ptr(),
+                                                 glam.data_ptr(), gpm.data_ptr(), gv.data_ptr(),
+                                                 self.g_grid_v.data_ptr(), self.g_grid_pm.data_ptr(),
+                                                 self.status.data_ptr(), self._s())
+        _lib.check(r, None, "mpm_diff_backward_seq_tools")
+
+    def _g_tool(self, gT):
+        g = torch.zeros((max(1, len(self.tools)), 12), device="cuda")
+        if gT is not None and len(self.tools):
+            g[:len(self.tools), :6] = gT.float()
+        return g
 
     def _pack(self, grads):
         n = self.n
@@ -183,24 +240,31 @@ class SceneDiffEngine:
         shapes = ((n, 3), (n, 3), (n, 3, 3), (n, 3, 3), (n,))
         return [gp[0, _OFFSET[k] * n: (_OFFSET[k] + _WIDTH[k]) * n].view(shapes[k]).clone() for k in range(5)]
 
-    def run_forward(self, st, n_sub):
-        """The state after n_sub substeps from st (new tensors)."""
-        seq = self._seq(2, st)
-        self._forward_seq(seq, n_sub, 2, self.scratch[0], self.scratch[1], False)
+    def run_forward(self, st, n_sub, qa):
+        """The state after n_sub substeps from st (new tensors), and the tools' (quat, ang) then."""
+        seq = self._seq(2, st[:5])
+        tseq = self._tool_seq(n_sub, st[5], qa)
+        self._forward_seq(seq, n_sub, 2, self.scratch[0], self.scratch[1], False, tseq)
         k = n_sub % 2
-        return tuple(t[k].clone() for t in seq)
+        nt = len(self.tools)
+        end = tseq[n_sub, :nt]
+        T_end = torch.cat([end[:, 0:3], end[:, 7:10]], 1).clone()
+        qa_end = torch.cat([end[:, 3:7], end[:, 10:13]], 1).clone()
+        return (*(t[k].clone() for t in seq), T_end), qa_end
 
-    def run_backward(self, st, n_sub, grads):
+    def run_backward(self, st, n_sub, grads, qa):
         """dL/d(step input) from dL/d(step output): re-simulates the step keeping every substep's state
         and grid, then runs the adjoint substeps in reverse."""
-        seq = self._seq(n_sub + 1, st)
+        seq = self._seq(n_sub + 1, st[:5])
+        tseq = self._tool_seq(n_sub, st[5], qa)
         gpm = torch.empty((max(1, n_sub), self.nodes, 4), device="cuda")
         gv = torch.empty((max(1, n_sub), self.nodes, 4), device="cuda")
-        self._forward_seq(seq, n_sub, n_sub + 1, gpm, gv, True)
-        gp = self._pack(grads)
-        self._backward_seq(seq, n_sub, gp, gpm, gv)
+        self._forward_seq(seq, n_sub, n_sub + 1, gpm, gv, True, tseq)
+        gp = self._pack(grads[:5])
+        g_tool = self._g_tool(grads[5])
+        self._backward_seq(seq, n_sub, gp, gpm, gv, tseq, g_tool)
         self.check()
-        return tuple(self._unpack(gp))
+        return (*self._unpack(gp), g_tool[:len(self.tools), :6].clone())
 
     def check(self):
         st = int(self.status.item())
@@ -213,9 +277,11 @@ class SceneDiffEngine:
     # ---------------------------------------------------------------- scene-level operations
     def step(self, n_sub: int) -> None:
         # checkpoint of the step (after its inputs) and the inputs written before it
-        self.step_inputs.append((list(self.states), int(n_sub), self.pending))
+        self.step_inputs.append((list(self.states), int(n_sub), self.pending, list(self.tool_qa)))
         self.pending = []
-        self.states = [_StepNode.apply(self, int(n_sub), *st) for st in self.states]
+        for b, st in enumerate(self.states):
+            out = _StepNode.apply(self, int(n_sub), self.tool_qa[b], *st)
+            self.states[b], self.tool_qa[b] = tuple(out[:6]), out[6]
         self.steps_taken += 1
         self.substeps_taken += int(n_sub)
 
@@ -229,10 +295,12 @@ class SceneDiffEngine:
         n = self.n
         self.adj = [[torch.zeros((n, 3), device=dev), torch.zeros((n, 3), device=dev),
                      torch.zeros((n, 3, 3), device=dev), torch.zeros((n, 3, 3), device=dev),
-                     torch.zeros(n, device=dev)] for _ in range(self.B)]
+                     torch.zeros(n, device=dev), torch.zeros((len(self.tools), 6), device=dev)]
+                    for _ in range(self.B)]
         self.cursor = self.substeps_taken
         self._seg = None
         self.queried.clear()
+        self.queried_tools.clear()
 
     def add_grad(self, grads_by_field, envs=None) -> None:
         """Add dL/d(pos, vel, C, F, Jp) ([B', N', ...] with N' = count particles from `start`) to the adjoint."""
@@ -245,10 +313,20 @@ class SceneDiffEngine:
             for i, b in enumerate(range(self.B) if envs is None else envs):
                 self.adj[b][k][start: start + g.shape[1]] += g[i].to(torch.float32)
 
+    def add_tool_grad(self, tool: int, gpos, gvel, envs=None) -> None:
+        """Add dL/d(pos, vel) ([B', 3] each, or None) of a tool to the adjoint."""
+        if self.adj is None:
+            self.reset_grad()
+        for i, b in enumerate(range(self.B) if envs is None else envs):
+            if gpos is not None:
+                self.adj[b][5][tool, 0:3] += gpos[i].to(torch.float32)
+            if gvel is not None:
+                self.adj[b][5][tool, 3:6] += gvel[i].to(torch.float32)
+
     def _locate(self, f_global):
         """(step index, substep within the step) of the substep that ends at global substep f_global."""
         acc = 0
-        for s_i, (_, n_sub, _) in enumerate(self.step_inputs):
+        for s_i, (_, n_sub, _, _) in enumerate(self.step_inputs):
             if f_global <= acc + n_sub:
                 return s_i, f_global - acc - 1
             acc += n_sub
@@ -264,20 +342,23 @@ class SceneDiffEngine:
         s_i, k = self._locate(self.cursor)
         n = self.n
         if self._seg is None or self._seg[0] != s_i:  # re-simulate the step from its checkpoint (load_ckpt)
-            inputs, n_sub, _ = self.step_inputs[s_i]
+            inputs, n_sub, _, qas = self.step_inputs[s_i]
             keep = []
             for b in range(self.B):
-                seq = self._seq(n_sub + 1, inputs[b])
+                seq = self._seq(n_sub + 1, inputs[b][:5])
+                tseq = self._tool_seq(n_sub, inputs[b][5], qas[b])
                 gpm = torch.empty((n_sub, self.nodes, 4), device="cuda")
                 gv = torch.empty((n_sub, self.nodes, 4), device="cuda")
-                self._forward_seq(seq, n_sub, n_sub + 1, gpm, gv, True)
-                keep.append((seq, gpm, gv))
+                self._forward_seq(seq, n_sub, n_sub + 1, gpm, gv, True, tseq)
+                keep.append((seq, gpm, gv, tseq))
             self._seg = (s_i, keep)
         for b in range(self.B):
-            seq, gpm, gv = self._seg[1][b]
-            gp = self._pack(self.adj[b])
-            self._backward_seq([t[k: k + 1].contiguous() for t in seq], 1, gp, gpm[k], gv[k])
-            self.adj[b] = self._unpack(gp)
+            seq, gpm, gv, tseq = self._seg[1][b]
+            gp = self._pack(self.adj[b][:5])
+            g_tool = self._g_tool(self.adj[b][5])
+            self._backward_seq([t[k: k + 1].contiguous() for t in seq], 1, gp, gpm[k], gv[k],
+                               tseq[k: k + 2].contiguous(), g_tool)
+            self.adj[b] = [*self._unpack(gp), g_tool[:len(self.tools), :6].clone()]
         self.cursor -= 1
 
     def input_grad(self) -> None:
@@ -290,6 +371,14 @@ class SceneDiffEngine:
         if k != 0:
             raise GenesisException("process_input_grad must follow the first substep of a step.")
         for field, start, count, values, envs in reversed(self.step_inputs[s_i][2]):
+            if field.startswith("tool_"):  # a tool's position / velocity input (ToolEntity.process_input_grad)
+                cols = slice(0, 3) if field == "tool_pos" else slice(3, 6)
+                if values.requires_grad:
+                    vb = torch.broadcast_to(values.to(device="cuda", dtype=torch.float32), (len(envs), 3))
+                    torch.autograd.backward([vb], [torch.stack([self.adj[b][5][start, cols] for b in envs])])
+                for b in envs:
+                    self.adj[b][5][start, cols] = 0.0
+                continue
             rows = slice(start, start + count)
             j = 0 if field == "pos" else 1
             if values.requires_grad:
@@ -318,10 +407,42 @@ class SceneDiffEngine:
                 st[4] = torch.cat([st[4][:start], self.Jp0[start: start + count], st[4][start + count:]], 0)
             self.states[b] = tuple(st)
 
+    def write_tool(self, field: str, tool: int, values: torch.Tensor, envs) -> None:
+        """Set tool `tool`'s position ("tool_pos") or velocity ("tool_vel") in envs through
+        differentiable torch ops (values broadcast to [len(envs), 3])."""
+        self.pending.append((field, tool, 1, values, list(envs)))
+        vals = torch.broadcast_to(values.to(device="cuda", dtype=torch.float32), (len(envs), 3))
+        c0 = 0 if field == "tool_pos" else 3
+        for i, b in enumerate(envs):
+            st = list(self.states[b])
+            T = st[5]
+            row = torch.cat([T[tool, :c0], vals[i], T[tool, c0 + 3:]], 0)
+            st[5] = torch.cat([T[:tool], row[None], T[tool + 1:]], 0)
+            self.states[b] = tuple(st)
+
+    def set_tool_orientation(self, tool: int, quat=None, ang=None, envs=None) -> None:
+        """Set a tool's orientation or angular velocity (not differentiated)."""
+        for i, b in enumerate(range(self.B) if envs is None else envs):
+            qa = self.tool_qa[b].clone()
+            if quat is not None:
+                qa[tool, :4] = torch.broadcast_to(torch.as_tensor(quat, dtype=torch.float32, device="cuda"),
+                                                  (len(envs) if envs is not None else self.B, 4))[i]
+            if ang is not None:
+                qa[tool, 4:] = torch.broadcast_to(torch.as_tensor(ang, dtype=torch.float32, device="cuda"),
+                                                  (len(envs) if envs is not None else self.B, 3))[i]
+            self.tool_qa[b] = qa
+
+    def tool_state(self, tool: int):
+        """(pos [B, 3], quat [B, 4], vel [B, 3], ang [B, 3]) of a tool; pos and vel autograd-connected."""
+        T = torch.stack([s[5][tool] for s in self.states])
+        qa = torch.stack([q[tool] for q in self.tool_qa])
+        return T[:, :3], qa[:, :4], T[:, 3:], qa[:, 4:]
+
     def stacked(self):
         """[B, N, ...] tensors of the current state (pos, vel, C, F, Jp; autograd-connected)."""
         return tuple(torch.stack([s[k] for s in self.states]) for k in range(5))
 
     def set_from_state(self, state, envs) -> None:
         for b in envs:
-            self.states[b] = tuple(getattr(state, k)[b].to(device="cuda", dtype=torch.float32) for k in FIELDS)
+            self.states[b] = (*(getattr(state, k)[b].to(device="cuda", dtype=torch.float32) for k in FIELDS),
+                              self.states[b][5])

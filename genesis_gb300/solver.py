@@ -200,8 +200,6 @@ class MPMSolver:
 
             if getattr(self, "_ffs", None):
                 raise GenesisException("Force fields are not supported in differentiable mode.")
-            if self._tools:
-                raise GenesisException("Tool entities are not supported in differentiable mode.")
             self._diff = SceneDiffEngine(self, B)
 
     def _add_particles(self, particle_start, n, material_idx, active, pos_np):
@@ -228,6 +226,10 @@ class MPMSolver:
         for e in self._entities:
             e.process_input(in_backward=in_backward)
         if any(t._pending() for t in self._tools):
+            if self._diff is not None:  # the tools' state lives in the differentiable engine
+                for t in self._tools:
+                    t.process_input(in_backward=in_backward)
+                return
             self._sync_tool_poses(user_too=True)
             for t in self._tools:
                 t.process_input(in_backward=in_backward)
@@ -606,6 +608,9 @@ class MPMSolver:
             if f_q == eng.cursor:
                 eng.add_grad({k: (getattr(getattr(st, k), "grad", None), start)
                               for k in ("pos", "vel", "C", "F", "Jp")})
+        for f_q, st, t in eng.queried_tools:  # ToolEntity.collect_output_grads
+            if f_q == eng.cursor:
+                eng.add_tool_grad(t, getattr(st.pos, "grad", None), getattr(st.vel, "grad", None))
 
     def substep_post_coupling_grad(self, f=0):
         """g2p.grad (mpm_solver.py:548-554); the grid-op and P2G adjoints of the same substep run in the

@@ -105,10 +105,32 @@ class ToolEntity:
     def _pending(self) -> bool:
         return any(v is not None for v in self._tgt.values())
 
+    def _tool_index(self) -> int:
+        return self._solver._tools.index(self)
+
     def process_input(self, in_backward: bool = False) -> None:
         """Apply the inputs set since the last step to the host copy of the state (the solver then
-        uploads the colliders)."""
+        uploads the colliders); in differentiable mode position and velocity enter the scene's
+        differentiable state through torch ops (their gradients reach the tensors passed in, as
+        process_input_grad delivers them in the reference)."""
         B = self._B
+        diff = getattr(self._solver, "_diff", None)
+        if diff is not None:
+            t = self._tool_index()
+            envs = list(range(B))
+            for field, key in (("tool_pos", "pos"), ("tool_vel", "vel")):
+                v = self._tgt[key]
+                if v is not None:
+                    v = v if isinstance(v, torch.Tensor) else torch.as_tensor(np.asarray(v, np.float64))
+                    if tuple(v.shape) not in ((3,), (B, 3)):
+                        raise GenesisException(f"{key} must have shape (3,) or ({B}, 3).")
+                    diff.write_tool(field, t, v, envs)
+            if self._tgt["quat"] is not None or self._tgt["ang"] is not None:
+                q = None if self._tgt["quat"] is None else _rows(self._tgt["quat"], B, 4, "quat")
+                a = None if self._tgt["ang"] is None else _rows(self._tgt["ang"], B, 3, "ang")
+                diff.set_tool_orientation(t, quat=q, ang=a, envs=envs)
+            self._tgt = {"pos": None, "quat": None, "vel": None, "ang": None}
+            return
         if self._tgt["pos"] is not None:
             self._pos = _rows(self._tgt["pos"], B, 3, "pos")
         if self._tgt["quat"] is not None:
@@ -121,7 +143,14 @@ class ToolEntity:
 
     # ------------------------------------------------------------------ state
     def get_state(self) -> ToolEntityState:
-        """pos, quat, vel, ang at the current frame (ToolEntity.get_state)."""
+        """pos, quat, vel, ang at the current frame (ToolEntity.get_state); in differentiable mode
+        pos and vel are on the autograd graph of the steps."""
+        diff = self._solver._diff
+        if diff is not None:
+            st = ToolEntityState(self, self._scene.t if hasattr(self._scene, "t") else 0, self._B, "cuda")
+            st.pos, st.quat, st.vel, st.ang = diff.tool_state(self._tool_index())
+            diff.queried_tools.append((diff.substeps_taken, st, self._tool_index()))
+            return st
         self._solver._sync_tool_poses()
         st = ToolEntityState(self, self._scene.t if hasattr(self._scene, "t") else 0, self._B, "cuda")
         st.pos.copy_(torch.as_tensor(self._pos, dtype=torch.float32))

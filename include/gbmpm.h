@@ -529,6 +529,35 @@ int mpm_diff_backward_seq_pp(const mpm_scene_config* scene, const float* mass, c
                              float* gmu, float* glam, void* grid_pm, void* grid_v, void* g_grid_v, void* g_grid_pm,
                              uint32_t* status, void* stream);
 
+/* Tool entities in the differentiable form (tool_entity/mesh.py Mesh.collide in the grid op,
+ * ToolEntity.advect between substeps; the reference differentiates both through its autodiff).
+ * A tool: its SDF values (device, [res0][res1][res2], the layout of Mesh.sdf_voxels),
+ * T_mesh_to_sdf (row-major 4x4; rows 0-2 used), Tool friction and coup_softness, the tool solver's
+ * floor height.  tool_seq: device [(n_sub + 1)][n_tools][13] states (pos 3, quat wxyz 4, vel 3,
+ * ang 3); the caller fills entry 0, the forward writes entries 1..n_sub.  The backward takes g_tool
+ * [n_tools][12] with dL/d(pos, vel) of the last state in [0..5] and returns dL/d(pos, vel) of the
+ * first state there ([6..11] is scratch).  The orientation and the angular velocity are carried
+ * but not differentiated.  At most MPM_DIFF_MAX_TOOLS tools. */
+#define MPM_DIFF_MAX_TOOLS 4
+typedef struct mpm_diff_tool {
+  const float* sdf;
+  int32_t res[3];
+  int32_t pad0;
+  double T_mesh_to_sdf[16];
+  double friction, softness, floor_height;
+} mpm_diff_tool;
+int mpm_diff_forward_seq_tools(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
+                               int64_t n, int32_t n_sub, float* x_seq, float* v_seq, float* C_seq, float* F_seq,
+                               float* Jp_seq, int32_t ring, const float* mu, const float* lam,
+                               const mpm_diff_tool* tools, int32_t n_tools, float* tool_seq, void* grid_pm,
+                               void* grid_v, int32_t grids_per_substep, uint32_t* status, void* stream);
+int mpm_diff_backward_seq_tools(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
+                                int64_t n, int32_t n_sub, const float* x_seq, const float* v_seq, const float* C_seq,
+                                const float* F_seq, const float* Jp_seq, const float* mu, const float* lam,
+                                const mpm_diff_tool* tools, int32_t n_tools, const float* tool_seq, float* g_tool,
+                                float* g_seq, float* gmu, float* glam, void* grid_pm, void* grid_v, void* g_grid_v,
+                                void* g_grid_pm, uint32_t* status, void* stream);
+
 /* ABI version of this header (1). */
 int mpm_version(void);
 

@@ -8,9 +8,11 @@ require grad, scene.step(), scene.get_state() / entity.get_state(), loss.backwar
 * The input pattern of the reference's tests/test_grad.py::test_differentiable_push (two envs, a
   position and a velocity set before the first step, a velocity input every step, a loss on the
   solver state at step 5 and one on the entity state at step 8): inputs that reach a loss get a
-  non-zero gradient and the last step's input gets none.  The reference scene's tool entity (a
-  stirrer mesh, whose per-step velocity is the input there) is not part of this MPM path; the
-  per-step input here is the liquid entity's velocity.
+  non-zero gradient and the last step's input gets none, here with the liquid entity's velocity
+  as the per-step input, and (test_reference_scenario_differentiable_push_with_tool) with the
+  reference's own inputs: a tool entity's velocity every step.
+* Tool entities in differentiable mode: gradients w.r.t. a tool's start position and velocity
+  against FP64 central differences of the oracle.
 * The forward of differentiable mode equals the product path on the same scene (1e-4 m).
 """
 
@@ -233,3 +235,153 @@ def test_solver_protocol_gradient_walk_equals_autograd(gs):
     a = run(False)
     b = run(True)
     assert torch.allclose(a, b, rtol=1e-4, atol=1e-7), (a, b)
+
+
+def _rod_obj(path, hx=0.05, hy=0.05, hz=0.5):
+    """A closed box mesh (a rod along z, 0.1 x 0.1 x 1 before the tool's normalisation)."""
+    v = [(x, y, z) for x in (-hx, hx) for y in (-hy, hy) for z in (-hz, hz)]
+    quads = [(1, 2, 4, 3), (5, 7, 8, 6), (1, 5, 6, 2), (3, 4, 8, 7), (1, 3, 7, 5), (2, 6, 8, 4)]
+    with open(path, "w") as f:
+        for p in v:
+            f.write("v %f %f %f\n" % p)
+        for q in quads:
+            f.write("f " + " ".join(str(i) for i in q) + "\n")
+
+
+def _tool_scene(gs, obj, requires_grad=True, n_envs=0):
+    scene = gs.Scene(sim_options=gs.options.SimOptions(dt=2e-3, substeps=10, requires_grad=requires_grad),
+                     mpm_options=gs.options.MPMOptions(lower_bound=(0.0, 0.0, 0.0), upper_bound=(1.0, 1.0, 0.55)))
+    tool = scene.add_entity(morph=gs.morphs.Mesh(file=str(obj), scale=0.08, pos=(0.275, 0.16, 0.1)),
+                            material=gs.materials.Tool(friction=1.0, sdf_res=48))
+    block = scene.add_entity(morph=gs.morphs.Box(lower=(0.2, 0.2, 0.05), upper=(0.35, 0.35, 0.15)),
+                             material=gs.materials.MPM.Elastic(rho=500, sampler="regular"))
+    scene.build(n_envs=n_envs)
+    return scene, tool, block
+
+
+def test_tool_gradients_match_fp64_central_differences(gs, oracle, tmp_path):
+    """A tool entity (a cube mesh) pushed into an Elastic block through the scene API in
+    differentiable mode: d loss / d (tool velocity) along a random direction and d loss / d (tool
+    start position) along x and z, through Mesh.collide in the grid op and ToolEntity.advect (loss:
+    a fixed random projection of the block's final particle positions), against FP64 central
+    differences of the oracle running the same tool as a collider, tolerance 5e-2 relative; the
+    forward of differentiable mode follows the oracle (1e-4 m).  The start position is not checked
+    along y, the push direction: there a shift moves the tool's influence front across grid nodes,
+    whose velocity jumps where the influence passes 0.1 (mesh.py:156-157), and the central
+    differences follow those jumps (they change by 2x between eps = 1e-4 and 1e-5 m) while the
+    adjoint, like the reference's autodiff, differentiates the smooth part."""
+    from test_api_host import _cube_obj
+
+    from genesis_gb300.coupling import tool as tool_collider
+
+    obj = tmp_path / "cube.obj"
+    _cube_obj(obj, half=1.0)
+    scene, tool, block = _tool_scene(gs, obj)
+    n = block.n_particles
+    w = torch.tensor(np.random.default_rng(3).normal(size=(n, 3)), dtype=torch.float32, device="cuda")
+    p0 = np.array([0.275, 0.16, 0.1])  # the cube's face at the block's (y = 0.2)
+    u0 = np.array([0.0, 1.0, -0.2])
+    p = torch.tensor(p0, dtype=torch.float32, device="cuda", requires_grad=True)
+    u = torch.tensor(u0, dtype=torch.float32, device="cuda", requires_grad=True)
+    tool.set_position(p)
+    tool.set_velocity(vel=u)
+    steps = 8
+    for _ in range(steps):
+        scene.step()
+    x = block.get_state().pos[0]
+    loss = (x * w).sum() / n
+    loss.backward()
+    gp, gu = p.grad.double().cpu().numpy(), u.grad.double().cpu().numpy()
+    assert np.abs(gu).max() > 0 and np.abs(gp).max() > 0
+
+    solver = scene.sim.mpm_solver
+    sc = oracle.make_scene(solver.substep_dt, gravity=tuple(solver.gravity[0]), lower_bound=tuple(solver.lower_bound),
+                           upper_bound=tuple(solver.upper_bound), grid_density=solver.grid_density,
+                           particle_size=solver.particle_size)
+    om = [oracle.from_c_material(block.material.to_c(0))]
+    x0 = block.init_particles.astype(np.float32).astype(np.float64)
+    st = dict(pos=x0, vel=np.zeros((n, 3)), C=np.zeros((n, 3, 3)), F=np.tile(np.eye(3), (n, 1, 1)), Jp=np.ones(n),
+              mat=np.zeros(n, np.int32), active=np.ones(n, bool))
+    wn = w.double().cpu().numpy()
+    g = tool.sdf
+
+    def L(pos, vel):
+        oracle.clear_sdf_grids()
+        sid = oracle.add_sdf_grid(g.values, None, g.T_mesh_to_sdf, g.cell_size, g.sdf_max)
+        c = tool_collider(g, pos=tuple(pos), vel=tuple(vel), friction=1.0, coup_softness=0.01, floor_height=0.0)
+        oracle.set_colliders([c.to_c(sid)])
+        try:
+            out, _, _ = oracle.run(sc, om, st, steps * 10)
+        finally:
+            oracle.set_colliders([])
+            oracle.clear_sdf_grids()
+        return float((out["pos"] * wn).sum() / n), out["pos"]
+
+    base, xo = L(p0, u0)
+    assert np.abs(x.detach().double().cpu().numpy() - xo).max() < 1e-4
+    assert np.abs(xo - L(p0 + np.array([0.0, -0.2, 0.0]), u0)[1]).max() > 5e-3  # the tool acts on the block
+    rng = np.random.default_rng(11)
+    d = rng.normal(size=3)
+    d /= np.linalg.norm(d)
+    checks = [("vel", gu, d, 1e-4), ("pos x", gp, np.array([1.0, 0.0, 0.0]), 1e-5),
+              ("pos z", gp, np.array([0.0, 0.0, 1.0]), 1e-5)]
+    for which, grad, dirn, eps in checks:
+        if which == "vel":
+            fd = (L(p0, u0 + eps * dirn)[0] - L(p0, u0 - eps * dirn)[0]) / (2 * eps)
+        else:
+            fd = (L(p0 + eps * dirn, u0)[0] - L(p0 - eps * dirn, u0)[0]) / (2 * eps)
+        ad = float(grad @ dirn)
+        print(f"tool d loss / d {which}: adjoint {ad:.6e} fd {fd:.6e}")
+        assert abs(fd) > 1e-6, (which, fd)
+        assert abs(ad - fd) <= 5e-2 * abs(fd), (which, ad, fd)
+
+
+def test_reference_scenario_differentiable_push_with_tool(gs, tmp_path):
+    """tests/test_grad.py::test_differentiable_push with its tool entity: two envs, a rod-shaped tool
+    (set_position with a tensor that requires grad, then a velocity input every step), an Elastic
+    box (position and velocity inputs), losses on the solver state at step 5 and on the entity
+    state at step 8; after loss.backward() every velocity input but the last has a non-zero
+    gradient and the last one none, as the reference asserts; the tool's start positions get
+    gradients too.  The stirrer asset is replaced by a 0.6 m rod turned along y (euler (90, 0, 0)
+    as in the reference) that lies on the box in env 0 (z = 0.16) and clear of it in env 1; the
+    rod slides along its axis, dragging the box's top layer by friction."""
+    obj = tmp_path / "rod.obj"
+    _rod_obj(obj)
+    scene = gs.Scene(sim_options=gs.options.SimOptions(dt=2e-3, substeps=10, requires_grad=True),
+                     mpm_options=gs.options.MPMOptions(lower_bound=(0.0, -1.0, 0.0), upper_bound=(1.0, 1.0, 0.55)))
+    stick = scene.add_entity(morph=gs.morphs.Mesh(file=str(obj), scale=0.6, pos=(0.5, 0.5, 0.05),
+                                                  euler=(90.0, 0.0, 0.0)),
+                             material=gs.materials.Tool(friction=8.0, sdf_res=64))
+    obj_e = scene.add_entity(morph=gs.morphs.Box(lower=(0.2, 0.1, 0.05), upper=(0.4, 0.3, 0.15)),
+                             material=gs.materials.MPM.Elastic(rho=500))
+    scene.build(n_envs=2)
+    init_pos = torch.tensor([[0.3, 0.1, 0.16], [0.3, 0.1, 0.5]], device="cuda", requires_grad=True)
+    stick.set_position(init_pos)
+    pos_obj_init = torch.tensor([0.3, 0.3, 0.1], device="cuda", requires_grad=True)
+    obj_e.set_position(pos_obj_init)
+    v_obj_init = torch.tensor([0.0, -1.0, 0.0], device="cuda", requires_grad=True)
+    obj_e.set_velocity(v_obj_init)
+    goal = torch.tensor([0.5, 0.8, 0.05], device="cuda")
+    horizon = 10
+    loss = 0.0
+    v_list = []
+    for i in range(horizon):
+        v_i = torch.tensor([[0.0, 1.0, 0.0], [0.0, 1.0, 0.0]], device="cuda", requires_grad=True)
+        stick.set_velocity(vel=v_i)
+        v_list.append(v_i)
+        scene.step()
+        if i == horizon // 2:
+            mpm = scene.get_state().solvers_state[0]
+            loss = loss + torch.pow(mpm.pos[mpm.active == 1] - goal, 2).sum()
+        if i == horizon - 2:
+            state = obj_e.get_state()
+            loss = loss + torch.pow(state.pos - goal, 2).sum()
+    loss.backward()
+    eps = float(np.finfo(np.float32).eps)
+    for v_i in v_list[:-1]:
+        assert (v_i.grad.abs() > eps).any()
+    # the last input never reaches a loss: torch leaves its grad None where the reference's
+    # backward walk writes zeros
+    assert v_list[-1].grad is None or (v_list[-1].grad.abs() < eps).all()
+    assert init_pos.grad is not None and (init_pos.grad.abs() > eps).any()
+    assert (pos_obj_init.grad.abs() > eps).any() and (v_obj_init.grad.abs() > eps).any()
