@@ -142,6 +142,7 @@ class MpmDiffTool(ctypes.Structure):
 
 
 DIFF_MAX_TOOLS = 4
+DIFF_MAX_FORCE_FIELDS = 8
 
 
 class MpmSceneConfig(ctypes.Structure):
@@ -203,6 +204,12 @@ _SIGNATURES = {
                                              _P, c_int32, _P, _P, _P, c_int32, _P, _P]),
     "mpm_diff_backward_seq_tools": (c_int32, [_P, _P, _P, _P, c_int64, c_int32, _P, _P, _P, _P, _P, _P, _P, _P,
                                               c_int32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "mpm_diff_forward_seq_ff": (c_int32, [_P, _P, _P, _P, c_int64, c_int32, _P, _P, _P, _P, _P, c_int32, _P, _P,
+                                          _P, c_int32, _P, _P, c_int32, c_int32, ctypes.c_uint64, _P, _P, c_int32,
+                                          _P, _P]),
+    "mpm_diff_backward_seq_ff": (c_int32, [_P, _P, _P, _P, c_int64, c_int32, _P, _P, _P, _P, _P, _P, _P, _P,
+                                           c_int32, _P, _P, _P, c_int32, c_int32, ctypes.c_uint64, _P, _P, _P, _P,
+                                           _P, _P, _P, _P, _P]),
     "mpm_set_force_fields": (c_int32, [_P, c_int32, _P]),
     "mpm_sample_regular": (c_int32, [c_int32, _P, _P, c_double, _P, c_int64, _P, _P]),
     "mpm_test_wait_timeout": (c_int32, [_P, _P]),

@@ -558,6 +558,33 @@ MaterialDev derive_material(const mpm_material& m, const mpm_scene_config& c) {
   return M;
 }
 
+// A force field as the grid op reads it (float copies of the ABI record); false for an unknown type.
+bool force_field_dev(const mpm_force_field& f, ForceFieldDev& d) {
+  if (f.type < MPM_FF_CONSTANT || f.type > MPM_FF_TURBULENCE) return false;
+  std::memset(&d, 0, sizeof(d));
+  d.type = f.type;
+  d.active = f.active ? 1 : 0;
+  for (int k = 0; k < 3; ++k) {
+    d.dir[k] = (float)f.direction[k];
+    d.center[k] = (float)f.center[k];
+  }
+  d.strength = (float)f.strength;
+  d.radius = (float)f.radius;
+  d.falloff_pow = (float)f.falloff_pow;
+  d.flow = (float)f.flow;
+  d.linear = (float)f.linear;
+  d.quadratic = (float)f.quadratic;
+  d.s_perp = (float)f.strength_perpendicular;
+  d.s_radial = (float)f.strength_radial;
+  d.falloff_min = (float)f.falloff_min;
+  d.falloff_max = (float)f.falloff_max;  // +inf stays +inf
+  d.damping = (float)f.damping;
+  d.frequency = (float)f.frequency;
+  d.seed = (unsigned long long)f.seed;
+  std::memcpy(d.perm, f.perm, sizeof(d.perm));
+  return true;
+}
+
 }  // namespace gbmpm
 
 namespace {
@@ -1063,32 +1090,8 @@ int mpm_set_force_fields(mpm_ctx* ctx, int32_t n, const mpm_force_field* fields)
   if (n < 0 || n > MAX_FORCE_FIELDS || (n > 0 && !fields)) return fail(ctx, MPM_ERR_BAD_ARG, "bad force-field arguments");
   if (ctx->phase != 0) return fail(ctx, MPM_ERR_STATE, "force fields inside a substep");
   std::vector<ForceFieldDev> h((size_t)n);
-  for (int32_t i = 0; i < n; ++i) {
-    const mpm_force_field& f = fields[i];
-    if (f.type < MPM_FF_CONSTANT || f.type > MPM_FF_TURBULENCE) return fail(ctx, MPM_ERR_BAD_ARG, "unknown force field");
-    ForceFieldDev& d = h[(size_t)i];
-    std::memset(&d, 0, sizeof(d));
-    d.type = f.type;
-    d.active = f.active ? 1 : 0;
-    for (int k = 0; k < 3; ++k) {
-      d.dir[k] = (float)f.direction[k];
-      d.center[k] = (float)f.center[k];
-    }
-    d.strength = (float)f.strength;
-    d.radius = (float)f.radius;
-    d.falloff_pow = (float)f.falloff_pow;
-    d.flow = (float)f.flow;
-    d.linear = (float)f.linear;
-    d.quadratic = (float)f.quadratic;
-    d.s_perp = (float)f.strength_perpendicular;
-    d.s_radial = (float)f.strength_radial;
-    d.falloff_min = (float)f.falloff_min;
-    d.falloff_max = (float)f.falloff_max;  // +inf stays +inf
-    d.damping = (float)f.damping;
-    d.frequency = (float)f.frequency;
-    d.seed = (unsigned long long)f.seed;
-    std::memcpy(d.perm, f.perm, sizeof(d.perm));
-  }
+  for (int32_t i = 0; i < n; ++i)
+    if (!force_field_dev(fields[i], h[(size_t)i])) return fail(ctx, MPM_ERR_BAD_ARG, "unknown force field");
   CK(cudaSetDevice(ctx->device));
   if (!ctx->d_ffs && n > 0) {
     cudaError_t e = cudaMalloc((void**)&ctx->d_ffs, sizeof(ForceFieldDev) * MAX_FORCE_FIELDS);

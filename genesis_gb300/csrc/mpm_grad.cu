@@ -9,7 +9,8 @@
 // dF^T R) V)_ij / (s_i + s_j); it has no 1/(s_j^2 - s_i^2) factors, so it stays finite at
 // F = I where the generic SVD backward relies on cancelling 1e6-sized terms.
 //
-// Materials: Elastic (corotated and neo-Hookean) and Liquid.  Grid: dense [res^3] float4 buffers owned
+// Materials: Elastic (corotated and neo-Hookean), Liquid, Sand and Snow; the grid op also applies
+// the built-in force fields and tool entities.  Grid: dense [res^3] float4 buffers owned
 // by the caller (torch tensors); particles: caller arrays in the reference layout.  The
 // scatter uses global vector atomics (no sort): the differentiable path favours clarity.
 #include <cuda_runtime.h>
@@ -20,6 +21,7 @@
 
 #include "gbmpm.h"
 #include "mpm_adjoint.cuh"
+#include "mpm_force_fields.cuh"
 #include "mpm_kernels.cuh"
 #include "mpm_tool_adjoint.cuh"
 
@@ -56,6 +58,15 @@ struct DiffParams {
   const float* tool_f;  // tool states (pos 3, quat 4, vel 3, ang 3) at this substep [n_tools][13]
   float* tool_f1;       // ... one substep later (written by k_dtool_advance)
   float* g_tool;        // [n_tools][12]: dL/d(pos, vel) of the next state (in) / this one (out); accumulator
+};
+
+// Force fields of the differentiable grid op (legacy_coupler.py:381-383), passed by value to the
+// two grid kernels only: scene index and substep counter of the noise draws, then the fields in
+// the order they act.
+struct DiffFields {
+  int32_t n, scene;
+  unsigned long long step;
+  ForceFieldDev f[MPM_DIFF_MAX_FORCE_FIELDS];
 };
 
 __device__ __forceinline__ int64_t didx(const SceneDev& S, int gx, int gy, int gz) {
@@ -213,7 +224,16 @@ __device__ __forceinline__ void node_world_pos(const SceneDev& S, const int* g, 
   for (int d = 0; d < 3; ++d) x[d] = (float)(g[d] + S.offset[d]) * S.dx;
 }
 
-__global__ void k_dgrid(DiffParams Q, int64_t nodes) {
+// The velocity one force field leaves at node g (world position x), as the product grid op adds it.
+__device__ __forceinline__ void dfield_apply(const DiffFields& FF, int f, const SceneDev& S, const int* g,
+                                             const float* x, float* v) {
+  const int gw[3] = {g[0] + S.offset[0], g[1] + S.offset[1], g[2] + S.offset[2]};
+  float a[3];
+  ff_acc(FF.f[f], x, v, S.eps, a, FF.scene, gw, FF.step);
+  for (int k = 0; k < 3; ++k) v[k] += a[k] * S.dt;
+}
+
+__global__ void k_dgrid(DiffParams Q, int64_t nodes, const DiffFields FF) {
   const SceneDev& S = Q.S;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nodes; i += (int64_t)gridDim.x * blockDim.x) {
     const float4 q = Q.pm[i];
@@ -224,9 +244,11 @@ __global__ void k_dgrid(DiffParams Q, int64_t nodes) {
       v[0] = inv * q.x + S.dt * S.grav[0];
       v[1] = inv * q.y + S.dt * S.grav[1];
       v[2] = inv * q.z + S.dt * S.grav[2];
-      if (Q.n_tools > 0) {
+      if (Q.n_tools > 0 || FF.n > 0) {
         float x[3];
         node_world_pos(S, g, x);
+        for (int f = 0; f < FF.n; ++f)  // force fields after gravity, before the tools
+          if (FF.f[f].active) dfield_apply(FF, f, S, g, x, v);
         for (int t = 0; t < Q.n_tools; ++t) {
           const float* st = Q.tool_f + t * 13;
           tool_collide_t<float>(Q.tools[t], x, v, st, st + 3, st + 7, Q.tool_f1 + t * 13 + 3, S.dt, S.eps);
@@ -339,8 +361,8 @@ __global__ void __launch_bounds__(256) k_dg2p_adj(DiffParams Q) {
   }
 }
 
-// grid-op adjoint: v = B(p/m + dt g) -> dL/dp, dL/dm
-__global__ void k_dgrid_adj(DiffParams Q, int64_t nodes) {
+// grid-op adjoint: v = B(T(F(p/m + dt g))) (force fields F, tools T, boundary B) -> dL/dp, dL/dm
+__global__ void k_dgrid_adj(DiffParams Q, int64_t nodes, const DiffFields FF) {
   const SceneDev& S = Q.S;
   const int lane = threadIdx.x & 31;
   for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x; i0 < nodes; i0 += (int64_t)gridDim.x * blockDim.x) {
@@ -356,9 +378,13 @@ __global__ void k_dgrid_adj(DiffParams Q, int64_t nodes) {
       const float inv = 1.f / q.w;
       float u[3] = {inv * q.x + S.dt * S.grav[0], inv * q.y + S.dt * S.grav[1], inv * q.z + S.dt * S.grav[2]};
       float gu[3] = {gv.x, gv.y, gv.z};
-      float vin[MPM_DIFF_MAX_TOOLS][3];
+      float vin[MPM_DIFF_MAX_TOOLS][3], fin[MPM_DIFF_MAX_FORCE_FIELDS][3];
       float x[3];
       node_world_pos(S, g, x);
+      for (int f = 0; f < FF.n; ++f) {  // forward through the force fields, keeping each one's input
+        for (int k = 0; k < 3; ++k) fin[f][k] = u[k];
+        if (FF.f[f].active) dfield_apply(FF, f, S, g, x, u);
+      }
       for (int t = 0; t < Q.n_tools; ++t) {  // forward through the tools, keeping each one's input
         for (int k = 0; k < 3; ++k) vin[t][k] = u[k];
         const float* st = Q.tool_f + t * 13;
@@ -385,6 +411,8 @@ __global__ void k_dgrid_adj(DiffParams Q, int64_t nodes) {
         }
         for (int j = 0; j < 3; ++j) gu[j] = gin[j];
       }
+      for (int f = FF.n - 1; f >= 0; --f)  // back through the force fields: g += dt J^T g
+        if (FF.f[f].active) ff_acc_vjp(FF.f[f], x, fin[f], S.eps, S.dt, gu);
       out.x = gu[0] * inv;
       out.y = gu[1] * inv;
       out.z = gu[2] * inv;
@@ -653,12 +681,23 @@ using namespace gbmpm;
 
 namespace {
 
+const DiffFields kNoFields{};
+
+// The fields of substep k of a sequence that starts at the fields' substep counter ff->step.
+const DiffFields* fields_at(const DiffFields* ff, int32_t k, DiffFields& tmp) {
+  if (!ff || ff->n == 0) return nullptr;
+  tmp = *ff;
+  tmp.step = ff->step + (unsigned long long)k;
+  return &tmp;
+}
+
 // One forward substep; mass_pp / kind_pp (per particle) override rho / neohookean when given.
 int diff_forward(const mpm_scene_config* scene, double rho, int32_t neohookean, const float* mass_pp,
                  const int32_t* kind_pp, const float* aux, int64_t n, const float* x, const float* v, const float* C,
                  const float* F, const float* Jp, const float* mu, const float* lam, float* x1, float* v1, float* C1,
                  float* F1, float* Jp1, void* grid_pm, void* grid_v, uint32_t* status, void* stream, int n_tools = 0,
-                 const DiffToolDev* tools = nullptr, const float* tool_f = nullptr, float* tool_f1 = nullptr) {
+                 const DiffToolDev* tools = nullptr, const float* tool_f = nullptr, float* tool_f1 = nullptr,
+                 const DiffFields* ff = nullptr) {
   if (!scene || n < 0 || !grid_pm || !grid_v || !status) return MPM_ERR_BAD_ARG;
   DiffParams Q;
   std::memset(&Q, 0, sizeof(Q));
@@ -688,7 +727,7 @@ int diff_forward(const mpm_scene_config* scene, double rho, int32_t neohookean, 
   k_dclear<<<gb, 256, 0, s>>>(Q, nodes, Q.pm);
   if (n > 0) k_dp2g<<<pb, 256, 0, s>>>(Q);
   if (n_tools > 0) k_dtool_advance<<<1, 32, 0, s>>>(Q);
-  k_dgrid<<<gb, 256, 0, s>>>(Q, nodes);
+  k_dgrid<<<gb, 256, 0, s>>>(Q, nodes, ff ? *ff : kNoFields);
   if (n > 0) k_dg2p<<<pb, 256, 0, s>>>(Q);
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_ERR_CUDA;
 }
@@ -700,7 +739,7 @@ int diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean,
                   float* gC, float* gF, float* gJp, float* gmu, float* glam, void* grid_pm, void* grid_v,
                   void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream, int n_tools = 0,
                   const DiffToolDev* tools = nullptr, const float* tool_f = nullptr, const float* tool_f1 = nullptr,
-                  float* g_tool = nullptr) {
+                  float* g_tool = nullptr, const DiffFields* ff = nullptr) {
   if (!scene || n < 0 || !grid_pm || !grid_v || !g_grid_v || !g_grid_pm) return MPM_ERR_BAD_ARG;
   DiffParams Q;
   std::memset(&Q, 0, sizeof(Q));
@@ -733,7 +772,7 @@ int diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean,
   const int pb = (int)((n + 255) / 256 < 8192 ? (n + 255) / 256 : 8192);
   k_dclear<<<gb, 256, 0, s>>>(Q, nodes, Q.g_grid_v);
   if (n > 0) k_dg2p_adj<<<pb, 256, 0, s>>>(Q);
-  k_dgrid_adj<<<gb, 256, 0, s>>>(Q, nodes);
+  k_dgrid_adj<<<gb, 256, 0, s>>>(Q, nodes, ff ? *ff : kNoFields);
   if (n_tools > 0) k_dtool_adj<<<1, 32, 0, s>>>(Q);
   if (n > 0) k_dp2g_adj<<<pb, 256, 0, s>>>(Q);
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_ERR_CUDA;
@@ -743,8 +782,10 @@ int diff_forward_seq(const mpm_scene_config* scene, double rho, int32_t neohooke
                      const int32_t* kind_pp, const float* aux, int64_t n, int32_t n_sub, float* x_seq, float* v_seq,
                      float* C_seq, float* F_seq, float* Jp_seq, int32_t ring, const float* mu, const float* lam,
                      void* grid_pm, void* grid_v, int32_t grids_per_substep, uint32_t* status, void* stream,
-                     int n_tools = 0, const DiffToolDev* tools = nullptr, float* tool_seq = nullptr) {
+                     int n_tools = 0, const DiffToolDev* tools = nullptr, float* tool_seq = nullptr,
+                     const DiffFields* ff = nullptr) {
   if (!scene || n < 0 || n_sub < 0 || ring < 2 || !x_seq || !v_seq || !C_seq || !F_seq) return MPM_ERR_BAD_ARG;
+  DiffFields tmp;
   SceneDev S;
   std::string err;
   if (derive_scene(*scene, S, err)) return MPM_ERR_BAD_ARG;
@@ -757,7 +798,8 @@ int diff_forward_seq(const mpm_scene_config* scene, double rho, int32_t neohooke
                                mu, lam, x_seq + b * n * 3, v_seq + b * n * 3, C_seq + b * n * 9, F_seq + b * n * 9,
                                Jp_seq ? Jp_seq + b * n : nullptr, (float4*)grid_pm + go, (float4*)grid_v + go, status,
                                stream, n_tools, tools, tool_seq ? tool_seq + (int64_t)k * n_tools * 13 : nullptr,
-                               tool_seq ? tool_seq + (int64_t)(k + 1) * n_tools * 13 : nullptr);
+                               tool_seq ? tool_seq + (int64_t)(k + 1) * n_tools * 13 : nullptr,
+                               fields_at(ff, k, tmp));
     if (r) return r;
   }
   return MPM_OK;
@@ -769,8 +811,10 @@ int diff_backward_seq(const mpm_scene_config* scene, double rho, int32_t neohook
                       const float* v_seq, const float* C_seq, const float* F_seq, const float* Jp_seq, const float* mu,
                       const float* lam, float* g_seq, float* gmu, float* glam, void* grid_pm, void* grid_v,
                       void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream, int n_tools = 0,
-                      const DiffToolDev* tools = nullptr, const float* tool_seq = nullptr, float* g_tool = nullptr) {
+                      const DiffToolDev* tools = nullptr, const float* tool_seq = nullptr, float* g_tool = nullptr,
+                      const DiffFields* ff = nullptr) {
   if (!scene || n < 0 || n_sub < 0 || !g_seq) return MPM_ERR_BAD_ARG;
+  DiffFields tmp;
   if (n_tools > 0) {
     DiffParams Qz;
     std::memset(&Qz, 0, sizeof(Qz));
@@ -794,7 +838,8 @@ int diff_backward_seq(const mpm_scene_config* scene, double rho, int32_t neohook
                                 Jp_seq ? go + 24 * n : nullptr, gmu, glam, (float4*)grid_pm + (int64_t)k * nodes,
                                 (float4*)grid_v + (int64_t)k * nodes, g_grid_v, g_grid_pm, status, stream, n_tools,
                                 tools, tool_seq ? tool_seq + (int64_t)k * n_tools * 13 : nullptr,
-                                tool_seq ? tool_seq + (int64_t)(k + 1) * n_tools * 13 : nullptr, g_tool);
+                                tool_seq ? tool_seq + (int64_t)(k + 1) * n_tools * 13 : nullptr, g_tool,
+                                fields_at(ff, k, tmp));
     if (r) return r;
     cur = 1 - cur;
   }
@@ -829,6 +874,18 @@ int diff_tools_dev(const mpm_diff_tool* tools, int32_t n_tools, const void* tool
     d.softness = (float)a.softness;
     d.floor_h = (float)a.floor_height;
   }
+  return MPM_OK;
+}
+
+// The caller's force fields as the differentiable grid kernels take them.
+int diff_fields(const mpm_force_field* fields, int32_t n, int32_t scene_index, uint64_t step0, DiffFields& out) {
+  if (n < 0 || n > MPM_DIFF_MAX_FORCE_FIELDS || (n > 0 && !fields) || scene_index < 0) return MPM_ERR_BAD_ARG;
+  std::memset(&out, 0, sizeof(out));
+  out.n = n;
+  out.scene = scene_index;
+  out.step = (unsigned long long)step0;
+  for (int32_t i = 0; i < n; ++i)
+    if (!force_field_dev(fields[i], out.f[i])) return MPM_ERR_BAD_ARG;
   return MPM_OK;
 }
 
@@ -911,17 +968,49 @@ int mpm_diff_backward_seq_pp(const mpm_scene_config* scene, const float* mass, c
                            g_seq, gmu, glam, grid_pm, grid_v, g_grid_v, g_grid_pm, status, stream);
 }
 
+int mpm_diff_forward_seq_ff(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
+                            int64_t n, int32_t n_sub, float* x_seq, float* v_seq, float* C_seq, float* F_seq,
+                            float* Jp_seq, int32_t ring, const float* mu, const float* lam, const mpm_diff_tool* tools,
+                            int32_t n_tools, float* tool_seq, const mpm_force_field* force_fields,
+                            int32_t n_force_fields, int32_t scene_index, uint64_t ff_step, void* grid_pm, void* grid_v,
+                            int32_t grids_per_substep, uint32_t* status, void* stream) {
+  if (n > 0 && (!mass || !kind || !aux || !Jp_seq)) return MPM_ERR_BAD_ARG;
+  DiffToolDev td[MPM_DIFF_MAX_TOOLS];
+  int r = diff_tools_dev(tools, n_tools, tool_seq, td);
+  if (r) return r;
+  DiffFields ff;
+  if ((r = diff_fields(force_fields, n_force_fields, scene_index, ff_step, ff))) return r;
+  return diff_forward_seq(scene, 0.0, 0, mass, kind, aux, n, n_sub, x_seq, v_seq, C_seq, F_seq, Jp_seq, ring, mu, lam,
+                          grid_pm, grid_v, grids_per_substep, status, stream, n_tools, td, tool_seq, &ff);
+}
+
+int mpm_diff_backward_seq_ff(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
+                             int64_t n, int32_t n_sub, const float* x_seq, const float* v_seq, const float* C_seq,
+                             const float* F_seq, const float* Jp_seq, const float* mu, const float* lam,
+                             const mpm_diff_tool* tools, int32_t n_tools, const float* tool_seq, float* g_tool,
+                             const mpm_force_field* force_fields, int32_t n_force_fields, int32_t scene_index,
+                             uint64_t ff_step, float* g_seq, float* gmu, float* glam, void* grid_pm, void* grid_v,
+                             void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream) {
+  if (n > 0 && (!mass || !kind || !aux || !Jp_seq)) return MPM_ERR_BAD_ARG;
+  DiffToolDev td[MPM_DIFF_MAX_TOOLS];
+  int r = diff_tools_dev(tools, n_tools, tool_seq, td);
+  if (r) return r;
+  if (n_tools > 0 && !g_tool) return MPM_ERR_BAD_ARG;
+  DiffFields ff;
+  if ((r = diff_fields(force_fields, n_force_fields, scene_index, ff_step, ff))) return r;
+  return diff_backward_seq(scene, 0.0, 0, mass, kind, aux, n, n_sub, x_seq, v_seq, C_seq, F_seq, Jp_seq, mu, lam,
+                           g_seq, gmu, glam, grid_pm, grid_v, g_grid_v, g_grid_pm, status, stream, n_tools, td,
+                           tool_seq, g_tool, &ff);
+}
+
 int mpm_diff_forward_seq_tools(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
                                int64_t n, int32_t n_sub, float* x_seq, float* v_seq, float* C_seq, float* F_seq,
                                float* Jp_seq, int32_t ring, const float* mu, const float* lam,
                                const mpm_diff_tool* tools, int32_t n_tools, float* tool_seq, void* grid_pm,
                                void* grid_v, int32_t grids_per_substep, uint32_t* status, void* stream) {
-  if (n > 0 && (!mass || !kind || !aux || !Jp_seq)) return MPM_ERR_BAD_ARG;
-  DiffToolDev td[MPM_DIFF_MAX_TOOLS];
-  const int r = diff_tools_dev(tools, n_tools, tool_seq, td);
-  if (r) return r;
-  return diff_forward_seq(scene, 0.0, 0, mass, kind, aux, n, n_sub, x_seq, v_seq, C_seq, F_seq, Jp_seq, ring, mu, lam,
-                          grid_pm, grid_v, grids_per_substep, status, stream, n_tools, td, tool_seq);
+  return mpm_diff_forward_seq_ff(scene, mass, kind, aux, n, n_sub, x_seq, v_seq, C_seq, F_seq, Jp_seq, ring, mu, lam,
+                                 tools, n_tools, tool_seq, nullptr, 0, 0, 0, grid_pm, grid_v, grids_per_substep,
+                                 status, stream);
 }
 
 int mpm_diff_backward_seq_tools(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
@@ -930,14 +1019,9 @@ int mpm_diff_backward_seq_tools(const mpm_scene_config* scene, const float* mass
                                 const mpm_diff_tool* tools, int32_t n_tools, const float* tool_seq, float* g_tool,
                                 float* g_seq, float* gmu, float* glam, void* grid_pm, void* grid_v, void* g_grid_v,
                                 void* g_grid_pm, uint32_t* status, void* stream) {
-  if (n > 0 && (!mass || !kind || !aux || !Jp_seq)) return MPM_ERR_BAD_ARG;
-  DiffToolDev td[MPM_DIFF_MAX_TOOLS];
-  const int r = diff_tools_dev(tools, n_tools, tool_seq, td);
-  if (r) return r;
-  if (n_tools > 0 && !g_tool) return MPM_ERR_BAD_ARG;
-  return diff_backward_seq(scene, 0.0, 0, mass, kind, aux, n, n_sub, x_seq, v_seq, C_seq, F_seq, Jp_seq, mu, lam,
-                           g_seq, gmu, glam, grid_pm, grid_v, g_grid_v, g_grid_pm, status, stream, n_tools, td,
-                           tool_seq, g_tool);
+  return mpm_diff_backward_seq_ff(scene, mass, kind, aux, n, n_sub, x_seq, v_seq, C_seq, F_seq, Jp_seq, mu, lam, tools,
+                                  n_tools, tool_seq, g_tool, nullptr, 0, 0, 0, g_seq, gmu, glam, grid_pm, grid_v,
+                                  g_grid_v, g_grid_pm, status, stream);
 }
 
 }  // extern "C"

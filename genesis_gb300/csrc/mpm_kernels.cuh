@@ -105,6 +105,8 @@ struct ForceFieldDev {
   unsigned long long seed;  // NOISE
   uint8_t perm[3][256];     // TURBULENCE
 };
+// The device record of an ABI force field (float copies); false for an unknown type.
+bool force_field_dev(const mpm_force_field& f, ForceFieldDev& d);
 
 // Another solver's particles coupled through the grid op (SPH or PBD), caller-owned device arrays.
 struct ExtSetDev {

@@ -21,8 +21,10 @@ particle masses, Lame parameters and plasticity constants per particle, Jp part 
 differentiated state.  Tool entities (tool_entity/) are part of the step: each env's state also
 holds every tool's position and velocity ([n_tools, 6], differentiated through Mesh.collide in the
 grid op and ToolEntity.advect, mpm_diff_forward_seq_tools / mpm_diff_backward_seq_tools) and, as
-plain tensors, its orientation and angular velocity.  As in the reference, CPIC and emitters are
-rejected in this mode.
+plain tensors, its orientation and angular velocity.  Built-in force fields act in the
+differentiable grid op (mpm_diff_forward_seq_ff / mpm_diff_backward_seq_ff), each step with the
+fields as they were when it ran.  As in the reference, CPIC and emitters are rejected in this mode;
+Custom force fields (a torch function here) are too.
 """
 
 from __future__ import annotations
@@ -64,11 +66,11 @@ class _StepNode(torch.autograd.Function):
     plus the tools' orientation and angular velocity (not differentiated)."""
 
     @staticmethod
-    def forward(ctx, engine, n_sub, qa, x, v, C, F, Jp, T):
+    def forward(ctx, engine, n_sub, fields, qa, x, v, C, F, Jp, T):
         st = tuple(t.detach().float().contiguous() for t in (x, v, C, F, Jp, T))
         qa = qa.detach().float().contiguous()
-        out, qa_end = engine.run_forward(st, n_sub, qa)
-        ctx.engine, ctx.n_sub = engine, n_sub
+        out, qa_end = engine.run_forward(st, n_sub, qa, fields)
+        ctx.engine, ctx.n_sub, ctx.fields = engine, n_sub, fields
         ctx.save_for_backward(*st, qa)  # the step's checkpoint
         ctx.mark_non_differentiable(qa_end)
         return (*out, qa_end)
@@ -76,8 +78,8 @@ class _StepNode(torch.autograd.Function):
     @staticmethod
     def backward(ctx, gx, gv, gC, gF, gJp, gT, _gqa):
         saved = ctx.saved_tensors
-        grads = ctx.engine.run_backward(saved[:6], ctx.n_sub, (gx, gv, gC, gF, gJp, gT), saved[6])
-        return (None, None, None, *grads)
+        grads = ctx.engine.run_backward(saved[:6], ctx.n_sub, (gx, gv, gC, gF, gJp, gT), saved[6], ctx.fields)
+        return (None, None, None, None, *grads)
 
 
 class SceneDiffEngine:
@@ -134,6 +136,7 @@ class SceneDiffEngine:
         self.Jp0 = torch.cat([torch.full((e.n_particles,), float(e.material._default_Jp), device=dev) for e in ents]) \
             if ents else torch.zeros(0, device=dev)
         self._init_tools(solver)
+        self.set_force_fields(getattr(solver, "_ffs", []))
         self.states = [(x0.clone(), torch.zeros((n, 3), device=dev), torch.zeros((n, 3, 3), device=dev),
                         eye.repeat(n, 1, 1), self.Jp0.clone(), self.T0.clone()) for _ in range(B)]
         self.tool_qa = [self.qa0.clone() for _ in range(B)]
@@ -171,6 +174,23 @@ class SceneDiffEngine:
             self.T0[i, :3] = torch.as_tensor(t.init_pos, dtype=torch.float32)
             self.qa0[i, :4] = torch.as_tensor(t.init_quat, dtype=torch.float32)
 
+    def set_force_fields(self, ffs) -> None:
+        """The scene's force fields for the following steps (their substep counter restarts, as the
+        library's does when mpm_set_force_fields replaces them)."""
+        from .force_fields import Custom
+
+        if any(isinstance(f, Custom) for f in ffs):
+            raise GenesisException("Custom force fields are not supported in differentiable mode.")
+        if len(ffs) > _lib.DIFF_MAX_FORCE_FIELDS:
+            raise GenesisException(f"At most {_lib.DIFF_MAX_FORCE_FIELDS} force fields in differentiable mode.")
+        self.ff_recs = (_lib.MpmForceField * max(1, len(ffs)))(*[f.to_c() for f in ffs])
+        self.n_ffs = len(ffs)
+        self.ff_base = getattr(self, "substeps_taken", 0)
+
+    def _fields(self, b: int):
+        """(records, count, env, substep counter) of the force fields for a step of env b starting now."""
+        return (self.ff_recs, self.n_ffs, b, self.substeps_taken - self.ff_base)
+
     def _tool_seq(self, n_sub, T, qa):
         """[(n_sub + 1), n_tools, 13] tool states, entry 0 from (pos, vel) T and (quat, ang) qa."""
         nt = len(self.tools)
@@ -197,29 +217,32 @@ class SceneDiffEngine:
                 t[0] = f.detach()
         return seq
 
-    def _forward_seq(self, seq, n_sub, ring, gpm, gv, keep_grids, tool_seq):
+    def _forward_seq(self, seq, n_sub, ring, gpm, gv, keep_grids, tool_seq, fields):
         nt = len(self.tools)
-        r = self.lib.mpm_diff_forward_seq_tools(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(),
-                                                self.aux.data_ptr(), self.n, int(n_sub), *[t.data_ptr() for t in seq],
-                                                ring, self.mu.data_ptr(), self.lam.data_ptr(), self.tool_recs, nt,
-                                                tool_seq.data_ptr() if nt else None, gpm.data_ptr(), gv.data_ptr(),
-                                                int(keep_grids), self.status.data_ptr(), self._s())
-        _lib.check(r, None, "mpm_diff_forward_seq_tools")
+        recs, nf, env, ff_step = fields
+        r = self.lib.mpm_diff_forward_seq_ff(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(),
+                                             self.aux.data_ptr(), self.n, int(n_sub), *[t.data_ptr() for t in seq],
+                                             ring, self.mu.data_ptr(), self.lam.data_ptr(), self.tool_recs, nt,
+                                             tool_seq.data_ptr() if nt else None, recs, nf, env, ff_step,
+                                             gpm.data_ptr(), gv.data_ptr(), int(keep_grids), self.status.data_ptr(),
+                                             self._s())
+        _lib.check(r, None, "mpm_diff_forward_seq_ff")
 
-    def _backward_seq(self, seq, n_sub, gp, gpm, gv, tool_seq, g_tool):
+    def _backward_seq(self, seq, n_sub, gp, gpm, gv, tool_seq, g_tool, fields):
         n = self.n
         nt = len(self.tools)
+        recs, nf, env, ff_step = fields
         gmu = torch.zeros(n, device="cuda")
         glam = torch.zeros(n, device="cuda")
-        r = self.lib.mpm_diff_backward_seq_tools(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(),
-                                                 self.aux.data_ptr(), n, int(n_sub), *[t.data_ptr() for t in seq],
-                                                 self.mu.data_ptr(), self.lam.data_ptr(), self.tool_recs, nt,
-                                                 tool_seq.data_ptr() if nt else None,
-                                                 g_tool.data_ptr() if nt else None, gp.data_ptr(), gmu.data_ptr(),
-                                                 glam.data_ptr(), gpm.data_ptr(), gv.data_ptr(),
-                                                 self.g_grid_v.data_ptr(), self.g_grid_pm.data_ptr(),
-                                                 self.status.data_ptr(), self._s())
-        _lib.check(r, None, "mpm_diff_backward_seq_tools")
+        r = self.lib.mpm_diff_backward_seq_ff(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(),
+                                              self.aux.data_ptr(), n, int(n_sub), *[t.data_ptr() for t in seq],
+                                              self.mu.data_ptr(), self.lam.data_ptr(), self.tool_recs, nt,
+                                              tool_seq.data_ptr() if nt else None,
+                                              g_tool.data_ptr() if nt else None, recs, nf, env, ff_step,
+                                              gp.data_ptr(), gmu.data_ptr(), glam.data_ptr(), gpm.data_ptr(),
+                                              gv.data_ptr(), self.g_grid_v.data_ptr(), self.g_grid_pm.data_ptr(),
+                                              self.status.data_ptr(), self._s())
+        _lib.check(r, None, "mpm_diff_backward_seq_ff")
 
     def _g_tool(self, gT):
         g = torch.zeros((max(1, len(self.tools)), 12), device="cuda")
@@ -240,11 +263,11 @@ class SceneDiffEngine:
         shapes = ((n, 3), (n, 3), (n, 3, 3), (n, 3, 3), (n,))
         return [gp[0, _OFFSET[k] * n: (_OFFSET[k] + _WIDTH[k]) * n].view(shapes[k]).clone() for k in range(5)]
 
-    def run_forward(self, st, n_sub, qa):
+    def run_forward(self, st, n_sub, qa, fields):
         """The state after n_sub substeps from st (new tensors), and the tools' (quat, ang) then."""
         seq = self._seq(2, st[:5])
         tseq = self._tool_seq(n_sub, st[5], qa)
-        self._forward_seq(seq, n_sub, 2, self.scratch[0], self.scratch[1], False, tseq)
+        self._forward_seq(seq, n_sub, 2, self.scratch[0], self.scratch[1], False, tseq, fields)
         k = n_sub % 2
         nt = len(self.tools)
         end = tseq[n_sub, :nt]
@@ -252,17 +275,17 @@ class SceneDiffEngine:
         qa_end = torch.cat([end[:, 3:7], end[:, 10:13]], 1).clone()
         return (*(t[k].clone() for t in seq), T_end), qa_end
 
-    def run_backward(self, st, n_sub, grads, qa):
+    def run_backward(self, st, n_sub, grads, qa, fields):
         """dL/d(step input) from dL/d(step output): re-simulates the step keeping every substep's state
         and grid, then runs the adjoint substeps in reverse."""
         seq = self._seq(n_sub + 1, st[:5])
         tseq = self._tool_seq(n_sub, st[5], qa)
         gpm = torch.empty((max(1, n_sub), self.nodes, 4), device="cuda")
         gv = torch.empty((max(1, n_sub), self.nodes, 4), device="cuda")
-        self._forward_seq(seq, n_sub, n_sub + 1, gpm, gv, True, tseq)
+        self._forward_seq(seq, n_sub, n_sub + 1, gpm, gv, True, tseq, fields)
         gp = self._pack(grads[:5])
         g_tool = self._g_tool(grads[5])
-        self._backward_seq(seq, n_sub, gp, gpm, gv, tseq, g_tool)
+        self._backward_seq(seq, n_sub, gp, gpm, gv, tseq, g_tool, fields)
         self.check()
         return (*self._unpack(gp), g_tool[:len(self.tools), :6].clone())
 
@@ -277,10 +300,11 @@ class SceneDiffEngine:
     # ---------------------------------------------------------------- scene-level operations
     def step(self, n_sub: int) -> None:
         # checkpoint of the step (after its inputs) and the inputs written before it
-        self.step_inputs.append((list(self.states), int(n_sub), self.pending, list(self.tool_qa)))
+        fields = [self._fields(b) for b in range(self.B)]
+        self.step_inputs.append((list(self.states), int(n_sub), self.pending, list(self.tool_qa), fields))
         self.pending = []
         for b, st in enumerate(self.states):
-            out = _StepNode.apply(self, int(n_sub), self.tool_qa[b], *st)
+            out = _StepNode.apply(self, int(n_sub), fields[b], self.tool_qa[b], *st)
             self.states[b], self.tool_qa[b] = tuple(out[:6]), out[6]
         self.steps_taken += 1
         self.substeps_taken += int(n_sub)
@@ -326,7 +350,7 @@ class SceneDiffEngine:
     def _locate(self, f_global):
         """(step index, substep within the step) of the substep that ends at global substep f_global."""
         acc = 0
-        for s_i, (_, n_sub, _, _) in enumerate(self.step_inputs):
+        for s_i, (_, n_sub, _, _, _) in enumerate(self.step_inputs):
             if f_global <= acc + n_sub:
                 return s_i, f_global - acc - 1
             acc += n_sub
@@ -342,22 +366,22 @@ class SceneDiffEngine:
         s_i, k = self._locate(self.cursor)
         n = self.n
         if self._seg is None or self._seg[0] != s_i:  # re-simulate the step from its checkpoint (load_ckpt)
-            inputs, n_sub, _, qas = self.step_inputs[s_i]
+            inputs, n_sub, _, qas, fields = self.step_inputs[s_i]
             keep = []
             for b in range(self.B):
                 seq = self._seq(n_sub + 1, inputs[b][:5])
                 tseq = self._tool_seq(n_sub, inputs[b][5], qas[b])
                 gpm = torch.empty((n_sub, self.nodes, 4), device="cuda")
                 gv = torch.empty((n_sub, self.nodes, 4), device="cuda")
-                self._forward_seq(seq, n_sub, n_sub + 1, gpm, gv, True, tseq)
-                keep.append((seq, gpm, gv, tseq))
+                self._forward_seq(seq, n_sub, n_sub + 1, gpm, gv, True, tseq, fields[b])
+                keep.append((seq, gpm, gv, tseq, fields[b]))
             self._seg = (s_i, keep)
         for b in range(self.B):
-            seq, gpm, gv, tseq = self._seg[1][b]
+            seq, gpm, gv, tseq, (recs, nf, env, ff_step) = self._seg[1][b]
             gp = self._pack(self.adj[b][:5])
             g_tool = self._g_tool(self.adj[b][5])
             self._backward_seq([t[k: k + 1].contiguous() for t in seq], 1, gp, gpm[k], gv[k],
-                               tseq[k: k + 2].contiguous(), g_tool)
+                               tseq[k: k + 2].contiguous(), g_tool, (recs, nf, env, ff_step + k))
             self.adj[b] = [*self._unpack(gp), g_tool[:len(self.tools), :6].clone()]
         self.cursor -= 1
 

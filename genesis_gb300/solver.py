@@ -198,8 +198,6 @@ class MPMSolver:
         if self._sim.requires_grad:  # the state lives in torch tensors advanced by the adjoint kernels
             from .grad import SceneDiffEngine
 
-            if getattr(self, "_ffs", None):
-                raise GenesisException("Force fields are not supported in differentiable mode.")
             self._diff = SceneDiffEngine(self, B)
 
     def _add_particles(self, particle_start, n, material_idx, active, pos_np):
@@ -472,6 +470,8 @@ class MPMSolver:
                 recs.append(f.to_c())
         plan.append(("fields", begin, len(recs)))
         self._ff_plan = plan if len(plan) > 1 else None
+        if getattr(self, "_diff", None) is not None:  # the differentiable steps take the fields from here on
+            self._diff.set_force_fields(ffs)
         arr = (_lib.MpmForceField * max(1, len(recs)))(*recs)
         _lib.check(self._lib.mpm_set_force_fields(self._ctx, len(recs), arr), self._ctx, "mpm_set_force_fields")
 

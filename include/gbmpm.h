@@ -558,6 +558,30 @@ int mpm_diff_backward_seq_tools(const mpm_scene_config* scene, const float* mass
                                 float* g_seq, float* gmu, float* glam, void* grid_pm, void* grid_v, void* g_grid_v,
                                 void* g_grid_pm, uint32_t* status, void* stream);
 
+/* mpm_diff_forward_seq_tools / mpm_diff_backward_seq_tools with the scene's force fields in the
+ * differentiable grid op (legacy_coupler.py:381-383: v += acc(x, v) dt after gravity, before the
+ * tools; the reference differentiates them through its autodiff).  force_fields: host array of
+ * n_force_fields records (at most MPM_DIFF_MAX_FORCE_FIELDS, inactive ones skipped), copied in
+ * the call; scene_index and ff_step (the substep counter of the first substep since the fields
+ * were set) seed the noise draws as mpm_set_force_fields' fields draw them in env scene_index.
+ * The backward needs the same fields, scene_index and ff_step as the forward it reverses; it
+ * carries dL/dv through each field's Jacobian in the node velocity (the noise draws and the
+ * node positions are constants). */
+#define MPM_DIFF_MAX_FORCE_FIELDS 8
+int mpm_diff_forward_seq_ff(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
+                            int64_t n, int32_t n_sub, float* x_seq, float* v_seq, float* C_seq, float* F_seq,
+                            float* Jp_seq, int32_t ring, const float* mu, const float* lam, const mpm_diff_tool* tools,
+                            int32_t n_tools, float* tool_seq, const mpm_force_field* force_fields,
+                            int32_t n_force_fields, int32_t scene_index, uint64_t ff_step, void* grid_pm, void* grid_v,
+                            int32_t grids_per_substep, uint32_t* status, void* stream);
+int mpm_diff_backward_seq_ff(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
+                             int64_t n, int32_t n_sub, const float* x_seq, const float* v_seq, const float* C_seq,
+                             const float* F_seq, const float* Jp_seq, const float* mu, const float* lam,
+                             const mpm_diff_tool* tools, int32_t n_tools, const float* tool_seq, float* g_tool,
+                             const mpm_force_field* force_fields, int32_t n_force_fields, int32_t scene_index,
+                             uint64_t ff_step, float* g_seq, float* gmu, float* glam, void* grid_pm, void* grid_v,
+                             void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream);
+
 /* ABI version of this header (1). */
 int mpm_version(void);
 

@@ -13,6 +13,10 @@ require grad, scene.step(), scene.get_state() / entity.get_state(), loss.backwar
   reference's own inputs: a tool entity's velocity every step.
 * Tool entities in differentiable mode: gradients w.r.t. a tool's start position and velocity
   against FP64 central differences of the oracle.
+* Force fields in differentiable mode: dL/dv0 through seven active built-in fields (Drag, Point,
+  Vortex, Turbulence, Noise, Wind, Constant) against FP64 central differences of the oracle running
+  the same fields; the forward with fields (two envs, a field switched off mid-run) equals the
+  product path; the solver-protocol walk equals autograd with fields.
 * The forward of differentiable mode equals the product path on the same scene (1e-4 m).
 """
 
@@ -35,7 +39,7 @@ def gs():
     return gs
 
 
-def _scene(gs, requires_grad=True, n_envs=0, box_z=0.35):
+def _scene(gs, requires_grad=True, n_envs=0, box_z=0.35, fields=()):
     scene = gs.Scene(
         sim_options=gs.options.SimOptions(dt=2e-3, substeps=10, requires_grad=requires_grad),
         mpm_options=gs.options.MPMOptions(lower_bound=(0, 0, 0), upper_bound=(1, 1, 1), grid_density=32,
@@ -45,11 +49,33 @@ def _scene(gs, requires_grad=True, n_envs=0, box_z=0.35):
                            morph=gs.morphs.Box(pos=(0.45, 0.5, box_z), size=(0.12, 0.12, 0.12)))
     water = scene.add_entity(material=gs.materials.MPM.Liquid(E=1e5, nu=0.3, sampler="regular"),
                              morph=gs.morphs.Box(pos=(0.6, 0.5, 0.22), size=(0.1, 0.1, 0.1)))
+    for f in fields:
+        scene.add_force_field(f)
     scene.build(n_envs=n_envs)
     return scene, box, water
 
 
-def _oracle_com_loss(O, scene, ents, v_box, target, n_sub):
+def _field_set(gs):
+    """Every built-in field type, all but the last active; the velocity-dependent ones (Drag, Point
+    with flow, Vortex damping, Turbulence with flow) strong enough to change dL/dv0 by tens of %."""
+    ff = gs.force_fields
+    fields = [
+        ff.Drag(linear=10.0, quadratic=10.0),
+        ff.Point(strength=-3.0, position=(0.5, 0.5, 0.25), falloff_pow=1.0, flow=2.0),
+        ff.Vortex(center=(0.5, 0.5, 0.0), strength_perpendicular=4.0, strength_radial=1.0, falloff_min=0.02,
+                  falloff_max=0.5, damping=3.0),
+        ff.Turbulence(strength=3.0, frequency=4, flow=1.5, seed=5),
+        ff.Noise(strength=2.0, seed=3),
+        ff.Wind(direction=(0.0, 1.0, 0.0), strength=2.0, radius=0.1, center=(0.5, 0.5, 0.2)),
+        ff.Constant(direction=(1.0, 0.0, 0.0), strength=1.0),
+        ff.Constant(direction=(0.0, 0.0, 1.0), strength=40.0),  # stays inactive
+    ]
+    for f in fields[:-1]:
+        f.activate()
+    return fields
+
+
+def _oracle_com_loss(O, scene, ents, v_box, target, n_sub, fields=()):
     solver = scene.sim.mpm_solver
     mats = solver._unique_materials()
     oms = [O.from_c_material(m.to_c(0)) for m in mats]
@@ -65,7 +91,11 @@ def _oracle_com_loss(O, scene, ents, v_box, target, n_sub):
     sc = O.make_scene(solver.substep_dt, gravity=tuple(solver.gravity[0]), lower_bound=tuple(solver.lower_bound),
                       upper_bound=tuple(solver.upper_bound), grid_density=solver.grid_density,
                       particle_size=solver.particle_size)
-    out, _, _ = O.run(sc, oms, st, n_sub)
+    O.set_force_fields([f.to_c() for f in fields])  # also restarts the noise draws' substep counter
+    try:
+        out, _, _ = O.run(sc, oms, st, n_sub)
+    finally:
+        O.set_force_fields([])
     com = out["pos"][:nb].mean(0)
     return float(((com - target) ** 2).sum())
 
@@ -97,6 +127,63 @@ def test_grad_of_initial_velocity_matches_fp64_central_differences(gs, oracle):
         fd[k] = (_oracle_com_loss(oracle, scene, [box, water], v0 + e, target, n_sub)
                  - _oracle_com_loss(oracle, scene, [box, water], v0 - e, target, n_sub)) / (2 * eps)
     assert np.linalg.norm(g - fd) <= GRAD_RTOL * np.linalg.norm(fd), (g, fd)
+
+
+def test_force_field_gradients_match_fp64_central_differences(gs, oracle):
+    """dL/dv0 of the box thrown onto the floor through seven active force fields (and one inactive)
+    against FP64 central differences of the oracle with the same fields; without the fields the
+    differences move by more than 10%, so the fields' Jacobians are what the check resolves."""
+    fields = _field_set(gs)
+    scene, box, water = _scene(gs, box_z=0.165, fields=fields)
+    v0 = np.array([0.4, -0.3, -1.5])
+    target = np.array([0.52, 0.47, 0.3])
+    v = torch.tensor(v0, dtype=torch.float32, device="cuda", requires_grad=True)
+    box.set_velocity(v)
+    steps = 4
+    for _ in range(steps):
+        scene.step()
+    loss = ((box.get_state().pos[0].mean(0) - torch.tensor(target, dtype=torch.float32, device="cuda")) ** 2).sum()
+    loss.backward()
+    g = v.grad.detach().cpu().numpy().astype(np.float64)
+    n_sub = steps * scene.substeps
+    ents = [box, water]
+    ref_loss = _oracle_com_loss(oracle, scene, ents, v0, target, n_sub, fields)
+    assert abs(loss.item() - ref_loss) <= 1e-4 * max(ref_loss, 1e-6) + 1e-8, (loss.item(), ref_loss)
+
+    def fd(fs):
+        eps = 1e-4
+        return np.array([(_oracle_com_loss(oracle, scene, ents, v0 + eps * np.eye(3)[k], target, n_sub, fs)
+                          - _oracle_com_loss(oracle, scene, ents, v0 - eps * np.eye(3)[k], target, n_sub, fs))
+                         / (2 * eps) for k in range(3)])
+
+    fd_ff, fd_plain = fd(fields), fd(())
+    assert np.linalg.norm(fd_ff - fd_plain) > 0.1 * np.linalg.norm(fd_ff), (fd_ff, fd_plain)
+    assert np.linalg.norm(g - fd_ff) <= GRAD_RTOL * np.linalg.norm(fd_ff), (g, fd_ff)
+
+
+def test_differentiable_forward_with_force_fields_equals_product_path(gs):
+    """Two envs (the noise draws differ per env), every field type, Drag switched off after two
+    steps (the fields' substep counter restarts in both forms): the differentiable forward equals
+    the product path (1e-4 m), and the backward through it gives a finite gradient."""
+    fg, fp = _field_set(gs), _field_set(gs)
+    sg, box_g, _ = _scene(gs, requires_grad=True, n_envs=2, fields=fg)
+    sp, box_p, _ = _scene(gs, requires_grad=False, n_envs=2, fields=fp)
+    v0 = torch.tensor([0.3, 0.1, -0.4], device="cuda", requires_grad=True)
+    box_g.set_velocity(v0)
+    box_p.set_velocity(v0.detach())
+    for k in range(5):
+        if k == 2:
+            fg[0].deactivate()
+            fp[0].deactivate()
+        sg.step()
+        sp.step()
+    a = sg.get_state().solvers_state[0].pos
+    b = sp.get_state().solvers_state[0].pos
+    assert (a.detach() - b).abs().max().item() <= 1e-4
+    assert (a.detach()[0] - a.detach()[1]).abs().max().item() > 1e-6  # the envs' noise differs
+    a.mean().backward()
+    assert torch.isfinite(v0.grad).all() and v0.grad.abs().max().item() > 0
+    sp.sim.mpm_solver.destroy()
 
 
 def test_plastic_materials_grad_matches_fp64_central_differences(gs, oracle):
@@ -201,7 +288,8 @@ def test_differentiable_forward_equals_product_path(gs):
     sp.sim.mpm_solver.destroy()
 
 
-def test_solver_protocol_gradient_walk_equals_autograd(gs):
+@pytest.mark.parametrize("with_fields", [False, True])
+def test_solver_protocol_gradient_walk_equals_autograd(gs, with_fields):
     """The reference's imperative walk (Scene._backward: add_grad_from_state, then per step in reverse
     substep_post_coupling_grad / substep_pre_coupling_grad per substep and process_input_grad) through
     the solver's protocol members gives the same input gradient as loss.backward()."""
@@ -209,7 +297,7 @@ def test_solver_protocol_gradient_walk_equals_autograd(gs):
     steps = 3
 
     def run(imperative):
-        scene, box, water = _scene(gs, box_z=0.165)
+        scene, box, water = _scene(gs, box_z=0.165, fields=_field_set(gs) if with_fields else ())
         v = torch.tensor([0.2, 0.1, -1.0], device="cuda", requires_grad=True)
         box.set_velocity(v)
         for _ in range(steps):
