@@ -30,7 +30,7 @@ __device__ __forceinline__ float perlin_grad(int h, float x, float y, float z) {
   if (h >= 4) v = (h == 12 || h == 14) ? x : z;
   return ((h & 1) == 0 ? u : -u) + ((h & 2) == 0 ? v : -v);
 }
-__device__ __noinline__ float perlin(const uint8_t* p, float f, float x, float y, float z) {
+__device__ float perlin(const uint8_t* p, float f, float x, float y, float z) {
   x *= f;
   y *= f;
   z *= f;

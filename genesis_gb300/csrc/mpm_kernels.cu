@@ -1208,11 +1208,11 @@ __device__ __forceinline__ void p2g_body(const KParams& P) {
           float qv[3];
 #pragma unroll
           for (int r = 0; r < 3; ++r) qv[r] = mass * pt.v[r] - (a[r] * fx[0] + a[3 + r] * fx[1] + a[6 + r] * fx[2]);
-          float4* rec = s_rec + P2G_REC * p;
-          rec[0] = make_float4(fx[0], fx[1], fx[2], mass);
-          rec[1] = make_float4(qv[0], qv[1], qv[2], a[0]);
-          rec[2] = make_float4(a[1], a[2], a[3], a[4]);
-          rec[3] = make_float4(a[5], a[6], a[7], a[8]);
+          float4* rec = s_rec + P2G_REC * p;  // layout: P2G_REC
+          rec[0] = make_float4(qv[0], qv[1], qv[2], mass);
+          rec[1] = make_float4(a[0], a[1], a[3], a[4]);
+          rec[2] = make_float4(a[6], a[7], a[2], a[5]);
+          rec[3] = make_float4(a[8], fx[0], fx[1], fx[2]);
           if constexpr (CPIC) rec[4] = make_float4(__uint_as_float(cmask), 0.f, 0.f, 0.f);
           scattered = true;
           if (!(pt.info & INFO_FREE) && P.pin) {  // its 27 nodes lose all momentum (mpm_solver.py:420-421)
@@ -1227,8 +1227,8 @@ __device__ __forceinline__ void p2g_body(const KParams& P) {
       }
       if (!scattered && cell < BLK_NODES) {  // holds a place in its cell's run: contributes nothing
         float4* rec = s_rec + P2G_REC * p;
-        rec[0] = make_float4(0.5f, 0.5f, 0.5f, 0.f);
-        rec[1] = rec[2] = rec[3] = make_float4(0.f, 0.f, 0.f, 0.f);
+        rec[0] = rec[1] = rec[2] = make_float4(0.f, 0.f, 0.f, 0.f);
+        rec[3] = make_float4(0.f, 0.5f, 0.5f, 0.5f);
         if constexpr (CPIC) rec[4] = make_float4(0.f, 0.f, 0.f, 0.f);
       }
       store_particle(P, Dx, slot, pt);
@@ -1251,62 +1251,64 @@ __device__ __forceinline__ void p2g_body(const KParams& P) {
       const int len = has ? end - beg : 0;
       const int nmax = __reduce_max_sync(0xffffffffu, len);
       if (nmax == 0) continue;  // warp-uniform
-      float4 acc[3][3];
+      // node sums in channel pairs (momentum x, y) and (momentum z, mass), accumulated with the
+      // paired FP32 operations (__ffma2_rn etc.: each half rounds as fmaf does, so the sums are
+      // those of the scalar form, at half the instructions)
+      float2 acc01[3][3], acc2m[3][3];
 #pragma unroll
       for (int oy = 0; oy < 3; ++oy)
 #pragma unroll
-        for (int oz = 0; oz < 3; ++oz) acc[oy][oz] = make_float4(0.f, 0.f, 0.f, 0.f);
-      const float fo = (float)ox;
+        for (int oz = 0; oz < 3; ++oz) acc01[oy][oz] = acc2m[oy][oz] = make_float2(0.f, 0.f);
+      const float2 fod = make_float2((float)ox, (float)ox), two = make_float2(2.f, 2.f);
       // the quadratic B-spline weights (mpm_solver.py:381) as polynomials in Horner form,
-      // w_o(f) = (p2_o f + p1_o) f + p0_o; this lane's x weight needs only its own o = ox
+      // w_o(f) = (p2_o f + p1_o) f + p0_o, each held twice (a pair) for the paired products;
+      // this lane's x weight needs only its own o = ox
       const float px2 = ox == 1 ? -1.f : 0.5f, px1 = ox == 0 ? -1.5f : (ox == 1 ? 2.f : -0.5f),
                   px0 = ox == 0 ? 1.125f : (ox == 1 ? -0.25f : 0.125f);
+      const float2 px2d = make_float2(px2, px2), px1d = make_float2(px1, px1), px0d = make_float2(px0, px0);
       for (int j = 0; j < nmax; ++j) {
         if (j < len) {
           const float4* rec = s_rec + P2G_REC * (beg + j);
           const float4 r0 = rec[0], r1 = rec[1], r2 = rec[2], r3 = rec[3];
           uint32_t m9 = 0u;  // CPIC: the record's separated nodes of this ox
           if constexpr (CPIC) m9 = __float_as_uint(rec[4].x) >> (9 * ox);
-          const float wx = fmaf(fmaf(px2, r0.x, px1), r0.x, px0);
-          const float wy[3] = {fmaf(fmaf(0.5f, r0.y, -1.5f), r0.y, 1.125f), fmaf(fmaf(-1.f, r0.y, 2.f), r0.y, -0.25f),
-                               fmaf(fmaf(0.5f, r0.y, -0.5f), r0.y, 0.125f)};
-          const float wz[3] = {fmaf(fmaf(0.5f, r0.z, -1.5f), r0.z, 1.125f), fmaf(fmaf(-1.f, r0.z, 2.f), r0.z, -0.25f),
-                               fmaf(fmaf(0.5f, r0.z, -0.5f), r0.z, 0.125f)};
-          // node value q + a_x ox + a_y oy + a_z oz with a (k-major, a[k*3 + r]) = r1.w, r2.x, r2.y |
-          // r2.z, r2.w, r3.x | r3.y, r3.z, r3.w; the offsets 0, 1, 2 are spelled out (without fast
-          // math a product by 0 or 1 is not folded away)
-          float ty[3][3];
-          ty[0][0] = fmaf(fo, r1.w, r1.x);
-          ty[0][1] = fmaf(fo, r2.x, r1.y);
-          ty[0][2] = fmaf(fo, r2.y, r1.z);
-          ty[1][0] = ty[0][0] + r2.z;
-          ty[1][1] = ty[0][1] + r2.w;
-          ty[1][2] = ty[0][2] + r3.x;
-          ty[2][0] = fmaf(2.f, r2.z, ty[0][0]);
-          ty[2][1] = fmaf(2.f, r2.w, ty[0][1]);
-          ty[2][2] = fmaf(2.f, r3.x, ty[0][2]);
+          const float2 fxd = make_float2(r3.y, r3.y), fyd = make_float2(r3.z, r3.z), fzd = make_float2(r3.w, r3.w);
+          const float2 wxd = __ffma2_rn(__ffma2_rn(px2d, fxd, px1d), fxd, px0d);
+          const float2 wyd[3] = {
+              __ffma2_rn(__ffma2_rn(make_float2(0.5f, 0.5f), fyd, make_float2(-1.5f, -1.5f)), fyd,
+                         make_float2(1.125f, 1.125f)),
+              __ffma2_rn(__ffma2_rn(make_float2(-1.f, -1.f), fyd, make_float2(2.f, 2.f)), fyd,
+                         make_float2(-0.25f, -0.25f)),
+              __ffma2_rn(__ffma2_rn(make_float2(0.5f, 0.5f), fyd, make_float2(-0.5f, -0.5f)), fyd,
+                         make_float2(0.125f, 0.125f))};
+          const float2 wzd[3] = {
+              __ffma2_rn(__ffma2_rn(make_float2(0.5f, 0.5f), fzd, make_float2(-1.5f, -1.5f)), fzd,
+                         make_float2(1.125f, 1.125f)),
+              __ffma2_rn(__ffma2_rn(make_float2(-1.f, -1.f), fzd, make_float2(2.f, 2.f)), fzd,
+                         make_float2(-0.25f, -0.25f)),
+              __ffma2_rn(__ffma2_rn(make_float2(0.5f, 0.5f), fzd, make_float2(-0.5f, -0.5f)), fzd,
+                         make_float2(0.125f, 0.125f))};
+          // node value (q + ox a_x + oy a_y + oz a_z, m): the offsets 0, 1, 2 spelled out (without
+          // fast math a product by 0 or 1 is not folded away); the mass half takes a zero step
+          const float2 ax01 = make_float2(r1.x, r1.y), ay01 = make_float2(r1.z, r1.w), az01 = make_float2(r2.x, r2.y);
+          const float2 ax2z = make_float2(r2.z, 0.f), ay2z = make_float2(r2.w, 0.f), az2z = make_float2(r3.x, 0.f);
+          const float2 s01 = __ffma2_rn(fod, ax01, make_float2(r0.x, r0.y));
+          const float2 s2m = __ffma2_rn(fod, ax2z, make_float2(r0.z, r0.w));
 #pragma unroll
           for (int oy = 0; oy < 3; ++oy) {
-            const float w01 = wx * wy[oy];
-            float tz[3][3];
-#pragma unroll
-            for (int r = 0; r < 3; ++r) tz[0][r] = ty[oy][r];
-            tz[1][0] = ty[oy][0] + r3.y;
-            tz[1][1] = ty[oy][1] + r3.z;
-            tz[1][2] = ty[oy][2] + r3.w;
-            tz[2][0] = fmaf(2.f, r3.y, ty[oy][0]);
-            tz[2][1] = fmaf(2.f, r3.z, ty[oy][1]);
-            tz[2][2] = fmaf(2.f, r3.w, ty[oy][2]);
+            const float2 u01 = oy == 0 ? s01 : (oy == 1 ? __fadd2_rn(s01, ay01) : __ffma2_rn(two, ay01, s01));
+            const float2 u2m = oy == 0 ? s2m : (oy == 1 ? __fadd2_rn(s2m, ay2z) : __ffma2_rn(two, ay2z, s2m));
+            const float2 w01 = __fmul2_rn(wxd, wyd[oy]);
 #pragma unroll
             for (int oz = 0; oz < 3; ++oz) {
-              float wt = w01 * wz[oz];
+              const float2 v01 = oz == 0 ? u01 : (oz == 1 ? __fadd2_rn(u01, az01) : __ffma2_rn(two, az01, u01));
+              const float2 v2m = oz == 0 ? u2m : (oz == 1 ? __fadd2_rn(u2m, az2z) : __ffma2_rn(two, az2z, u2m));
+              float2 wt = __fmul2_rn(w01, wzd[oz]);
               if constexpr (CPIC) {
-                if ((m9 >> (oy * 3 + oz)) & 1u) wt = 0.f;
+                if ((m9 >> (oy * 3 + oz)) & 1u) wt = make_float2(0.f, 0.f);
               }
-              acc[oy][oz].x = fmaf(wt, tz[oz][0], acc[oy][oz].x);
-              acc[oy][oz].y = fmaf(wt, tz[oz][1], acc[oy][oz].y);
-              acc[oy][oz].z = fmaf(wt, tz[oz][2], acc[oy][oz].z);
-              acc[oy][oz].w = fmaf(wt, r0.w, acc[oy][oz].w);
+              acc01[oy][oz] = __ffma2_rn(wt, v01, acc01[oy][oz]);
+              acc2m[oy][oz] = __ffma2_rn(wt, v2m, acc2m[oy][oz]);
             }
           }
         }
@@ -1321,10 +1323,10 @@ __device__ __forceinline__ void p2g_body(const KParams& P) {
           if (len > 0) {
             float4* g = my_tile + ((tb0 + ox) * TILE + (tb1 + oy)) * TILE + (tb2 + oz);
             float4 h = *g;
-            h.x += acc[oy][oz].x;
-            h.y += acc[oy][oz].y;
-            h.z += acc[oy][oz].z;
-            h.w += acc[oy][oz].w;
+            h.x += acc01[oy][oz].x;
+            h.y += acc01[oy][oz].y;
+            h.z += acc2m[oy][oz].x;
+            h.w += acc2m[oy][oz].y;
             *g = h;
           }
           __syncwarp();

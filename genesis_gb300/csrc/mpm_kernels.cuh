@@ -40,10 +40,12 @@ constexpr int P2G_MAX_WARPS = P2G_MAX_THREADS / 32;
 constexpr int P2G_MAX_CHUNK = 1024;          // particles per P2G work item
 
 // Shared-memory layout of k_p2g (dynamic part): warp tiles, then one scatter record per particle
-// at its cell-sorted position (P2G_REC float4 each: fx | mass, q | a0, a1..a4, a5..a8, then the
-// CPIC node mask in .x of the fifth, unused without CPIC; the odd stride of 5 float4 puts
-// consecutive records in different bank groups), then the item's (cell, rank) words and the old
-// slots of its particles.
+// at its cell-sorted position, then the item's (cell, rank) words and the old slots of its
+// particles.  A record is P2G_REC float4: (q0, q1, q2, mass), (ax0, ax1, ay0, ay1),
+// (az0, az1, ax2, ay2), (az2, fx, fy, fz), then the CPIC node mask in .x of the fifth (unused
+// without CPIC; the odd stride of 5 float4 puts consecutive records in different bank groups),
+// with a_k = dx * affine[:, k]: the pairs (q0, q1), (q2, mass), (ak0, ak1) sit in aligned register
+// pairs for the scatter's paired FP32 operations.
 constexpr int P2G_REC = 5;
 __host__ __device__ __forceinline__ size_t p2g_dyn_smem(int threads, int chunk) {
   return (size_t)(threads / 32) * TILE_NODES * 16 + (size_t)chunk * P2G_REC * 16 + (size_t)chunk * 8;
