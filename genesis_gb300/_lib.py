@@ -141,6 +141,25 @@ class MpmDiffTool(ctypes.Structure):
     ]
 
 
+class MpmDiffExtras(ctypes.Structure):
+    """mpm_diff_extras (gbmpm.h): tools, force fields and Muscle inputs of a differentiable sequence."""
+
+    _fields_ = [
+        ("tools", c_void_p),
+        ("n_tools", c_int32),
+        ("n_force_fields", c_int32),
+        ("tool_seq", c_void_p),
+        ("g_tool", c_void_p),
+        ("force_fields", c_void_p),
+        ("scene_index", c_int32),
+        ("pad0", c_int32),
+        ("ff_step", ctypes.c_uint64),
+        ("actu", c_void_p),
+        ("muscle_dir", c_void_p),
+        ("g_actu", c_void_p),
+    ]
+
+
 DIFF_MAX_TOOLS = 4
 DIFF_MAX_FORCE_FIELDS = 8
 
@@ -204,12 +223,10 @@ _SIGNATURES = {
                                              _P, c_int32, _P, _P, _P, c_int32, _P, _P]),
     "mpm_diff_backward_seq_tools": (c_int32, [_P, _P, _P, _P, c_int64, c_int32, _P, _P, _P, _P, _P, _P, _P, _P,
                                               c_int32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
-    "mpm_diff_forward_seq_ff": (c_int32, [_P, _P, _P, _P, c_int64, c_int32, _P, _P, _P, _P, _P, c_int32, _P, _P,
-                                          _P, c_int32, _P, _P, c_int32, c_int32, ctypes.c_uint64, _P, _P, c_int32,
-                                          _P, _P]),
-    "mpm_diff_backward_seq_ff": (c_int32, [_P, _P, _P, _P, c_int64, c_int32, _P, _P, _P, _P, _P, _P, _P, _P,
-                                           c_int32, _P, _P, _P, c_int32, c_int32, ctypes.c_uint64, _P, _P, _P, _P,
-                                           _P, _P, _P, _P, _P]),
+    "mpm_diff_forward_seq_ex": (c_int32, [_P, _P, _P, _P, c_int64, c_int32, _P, _P, _P, _P, _P, c_int32, _P, _P,
+                                          _P, _P, _P, c_int32, _P, _P]),
+    "mpm_diff_backward_seq_ex": (c_int32, [_P, _P, _P, _P, c_int64, c_int32, _P, _P, _P, _P, _P, _P, _P, _P,
+                                           _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "mpm_set_force_fields": (c_int32, [_P, c_int32, _P]),
     "mpm_sample_regular": (c_int32, [c_int32, _P, _P, c_double, _P, c_int64, _P, _P]),
     "mpm_test_wait_timeout": (c_int32, [_P, _P]),

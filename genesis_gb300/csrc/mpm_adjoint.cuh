@@ -12,6 +12,10 @@
 //   Snow (snow.py:56-74):  sn = clamp(s, 1 - yl, 1 + yh), Jp_new = Jp prod s/sn, J = prod s,
 //     h = exp(10 (1 - Jp)), tau_i = 2 mu h (sn_i - 1) sn_i + lam h J (J - 1)
 //     (the corotated stress 2 mu h (F_new - U V^T) F_new^T + lam h J (J-1) I).
+//   ElastoPlastic (elasto_plastic.py:44-71), Jp unchanged, tau_i = 2 mu (sn_i - 1) sn_i + lam J (J - 1):
+//     clamped (MT_ELASTOPLASTIC): sn = clamp(s, 1 - yl, 1 + yh);
+//     von Mises (EP_VON_MISES): e = log max(s, 0.05), e^ = e - mean(e), |e^| = sqrt(|e^|^2 + eps),
+//     dg = |e^| - yield_stress / (2 mu); dg > 0: sn = exp(e - dg/|e^| e^), else sn = s.
 // The per-axis functions and their Jacobians w.r.t. (s0, s1, s2, Jp, mu, lam) come from forward-
 // mode dual numbers.  The off-diagonal part of the adjoint uses the divided differences
 // (f_i - f_j)/(s_i - s_j), taken from the Jacobian (J_ii - J_ij) when s_i and s_j nearly coincide
@@ -108,8 +112,9 @@ template <typename T> GB_HD Dual<T> dsqrt(const Dual<T>& a) {
 }
 
 // ---------------------------------------------------------------- principal-axis material laws
-// type: MT_SAND or MT_SNOW; p0, p1: sand alpha and (3 lam + 2 mu)/(2 mu) is derived here;
-// snow clamp_lo, clamp_hi.
+// type: MT_SAND, MT_SNOW, MT_ELASTOPLASTIC or EP_VON_MISES; p0, p1: sand alpha ((3 lam + 2 mu)/(2 mu)
+// is derived here); snow and clamped ElastoPlastic clamp_lo, clamp_hi; von Mises yield_stress/(2 mu).
+constexpr int EP_VON_MISES = 64 + MT_ELASTOPLASTIC;
 template <typename T>
 GB_HD void plastic_principal(int type, const Dual<T>* s, const Dual<T>& Jp, const Dual<T>& mu, const Dual<T>& lam,
                              T p0, T p1, T eps, Dual<T>* sn, Dual<T>* tau, Dual<T>& Jpn) {
@@ -153,6 +158,37 @@ GB_HD void plastic_principal(int type, const Dual<T>* s, const Dual<T>& Jp, cons
     const Dual<T> L = l[0] + l[1] + l[2];
 #pragma unroll
     for (int i = 0; i < 3; ++i) tau[i] = two * mu * l[i] + lam * L;
+  } else if (type == MT_ELASTOPLASTIC || type == EP_VON_MISES) {
+    Jpn = Jp;
+    if (type == MT_ELASTOPLASTIC) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        if (s[i].v < p0) sn[i] = dconst(p0);
+        else if (s[i].v > p1) sn[i] = dconst(p1);
+        else sn[i] = s[i];
+      }
+    } else {
+      Dual<T> e[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) e[i] = s[i].v > T(0.05) ? dlog(s[i]) : dconst(glog(T(0.05)));
+      const Dual<T> m3 = (e[0] + e[1] + e[2]) / dconst(T(3));
+      Dual<T> eh[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) eh[i] = e[i] - m3;
+      const Dual<T> ehn = dsqrt(eh[0] * eh[0] + eh[1] * eh[1] + eh[2] * eh[2] + dconst(eps));
+      const Dual<T> dg = ehn - dconst(p0);
+      if (dg.v > T(0)) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) sn[i] = dexp(e[i] - (dg / ehn) * eh[i]);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) sn[i] = s[i];
+      }
+    }
+    const Dual<T> J = s[0] * s[1] * s[2];
+    const Dual<T> lj = lam * J * (J - dconst(T(1)));
+#pragma unroll
+    for (int i = 0; i < 3; ++i) tau[i] = two * mu * (sn[i] - dconst(T(1))) * sn[i] + lj;
   } else {  // MT_SNOW
     Jpn = Jp;
 #pragma unroll
@@ -243,8 +279,13 @@ GB_HD void plastic_adjoint(int type, const T* U, const T* s, const T* V, T Jp, T
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = i + 1; j < 3; ++j) {
-      // Snow clamps each axis on its own: a bound may lie between s_i and s_j
-      const bool same = type != MT_SNOW || ((s[i] < p0) == (s[j] < p0) && (s[i] > p1) == (s[j] > p1));
+      // Snow and the clamped ElastoPlastic clamp each axis on its own: a bound may lie between s_i
+      // and s_j; von Mises floors each log strain at 0.05
+      bool same = true;
+      if (type == MT_SNOW || type == MT_ELASTOPLASTIC)
+        same = (s[i] < p0) == (s[j] < p0) && (s[i] > p1) == (s[j] > p1);
+      else if (type == EP_VON_MISES)
+        same = (s[i] > T(0.05)) == (s[j] > T(0.05));
       const T a = divided_difference(s, f, sn[i].d[i], sn[i].d[j], sn[j].d[j], sn[j].d[i], i, j, same);
       const T b = (f[i] + f[j]) / signmax(s[i] + s[j], T(1e-6));
       A[i * 3 + j] += T(0.5) * (a + b) * G[i * 3 + j] + T(0.5) * (a - b) * G[j * 3 + i];

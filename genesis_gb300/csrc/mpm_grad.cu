@@ -58,6 +58,11 @@ struct DiffParams {
   const float* tool_f;  // tool states (pos 3, quat 4, vel 3, ang 3) at this substep [n_tools][13]
   float* tool_f1;       // ... one substep later (written by k_dtool_advance)
   float* g_tool;        // [n_tools][12]: dL/d(pos, vel) of the next state (in) / this one (out); accumulator
+  // Muscle particles (kinds DIFF_MUSCLE_*): actuation [n] (constant over the substeps of a call),
+  // fibre direction [n][3], dL/dactuation [n] (added)
+  const float* actu;
+  const float* mdir;
+  float* g_actu;
 };
 
 // Force fields of the differentiable grid op (legacy_coupler.py:381-383), passed by value to the
@@ -93,21 +98,46 @@ __device__ __forceinline__ bool make_stencil(const SceneDev& S, const float* x, 
   return true;
 }
 
-// Material of the differentiable form (the `neohookean` argument of the entry points).
-constexpr int DIFF_COROTATED = 0, DIFF_NEOHOOKEAN = 1, DIFF_LIQUID = 2, DIFF_SAND = 3, DIFF_SNOW = 4;
+// Material of the differentiable form (the `neohookean` argument of the entry points, or the
+// per-particle kind): aux holds Sand alpha | Snow and clamped ElastoPlastic clamp bounds | von Mises
+// yield_stress / (2 mu) | Muscle stiffness.
+constexpr int DIFF_COROTATED = 0, DIFF_NEOHOOKEAN = 1, DIFF_LIQUID = 2, DIFF_SAND = 3, DIFF_SNOW = 4,
+              DIFF_MUSCLE_COROTATED = 5, DIFF_MUSCLE_NEOHOOKEAN = 6, DIFF_EP_CLAMP = 7, DIFF_EP_VON_MISES = 8;
 
-// Sand / Snow of one particle as the product path's material table holds them (mpm_math.cuh)
+__device__ __forceinline__ bool diff_plastic(int kind) {
+  return kind == DIFF_SAND || kind == DIFF_SNOW || kind == DIFF_EP_CLAMP || kind == DIFF_EP_VON_MISES;
+}
+__device__ __forceinline__ bool diff_muscle(int kind) {
+  return kind == DIFF_MUSCLE_COROTATED || kind == DIFF_MUSCLE_NEOHOOKEAN;
+}
+// the law of plastic_adjoint (mpm_adjoint.cuh) for a plastic kind
+__device__ __forceinline__ int diff_plastic_law(int kind) {
+  return kind == DIFF_SAND ? MT_SAND : (kind == DIFF_SNOW ? MT_SNOW : (kind == DIFF_EP_CLAMP ? MT_ELASTOPLASTIC : EP_VON_MISES));
+}
+
+// A plastic particle's material as the product path's material table holds it (mpm_math.cuh)
 __device__ __forceinline__ MaterialDev plastic_material(int kind, float mu, float lam, const float* aux) {
   MaterialDev M;
-  M.type = kind == DIFF_SAND ? MT_SAND : MT_SNOW;
-  M.flags = 0;
+  M.type = kind == DIFF_SAND ? MT_SAND : (kind == DIFF_SNOW ? MT_SNOW : MT_ELASTOPLASTIC);
+  M.flags = kind == DIFF_EP_VON_MISES ? MF_VON_MISES : 0;
   M.mu = mu;
   M.lam = lam;
   M.alpha = kind == DIFF_SAND ? aux[0] : 0.f;
   M.sand_coef = (3.f * lam + 2.f * mu) / (2.f * mu);
   M.clamp_lo = aux[0];
   M.clamp_hi = aux[1];
+  M.vm_ratio = aux[0];
   return M;
+}
+
+// Muscle actuation stress (muscle.py:46-53): stiffness * actu * (F m)(F m)^T, added as the product
+// path's material_update adds it
+__device__ __forceinline__ void muscle_stress(const float* Ft, const float* m, float stiffness, float actu, float* P) {
+  float fm[3];
+  for (int r = 0; r < 3; ++r) fm[r] = Ft[r * 3 + 0] * m[0] + Ft[r * 3 + 1] * m[1] + Ft[r * 3 + 2] * m[2];
+  const float k = stiffness * actu;
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) P[r * 3 + c] += k * fm[r] * fm[c];
 }
 
 __device__ __forceinline__ float p_mass(const DiffParams& Q, int64_t i) { return Q.pmass ? Q.pmass[i] : Q.mass; }
@@ -174,7 +204,8 @@ __global__ void __launch_bounds__(256) k_dp2g(DiffParams Q) {
     float Ft[9], U[9], sig[3], V[9], P[9];
     f_tmp(C, F, S.dt, Ft);
     svd_f32(Ft, U, sig, V);
-    if (kind == DIFF_SAND || kind == DIFF_SNOW) {  // sand.py:47-84, snow.py:56-74 (the product path's code)
+    const bool plastic = diff_plastic(kind);
+    if (plastic) {  // sand.py:47-84, snow.py:56-74, elasto_plastic.py:44-71 (the product path's code)
       const MaterialDev M = plastic_material(kind, Q.mu[i], Q.lam[i], Q.aux + i * 2);
       const float mdir[3] = {0.f, 0.f, 1.f};
       float Fn[9], Jpn;
@@ -183,10 +214,11 @@ __global__ void __launch_bounds__(256) k_dp2g(DiffParams Q) {
         for (int k = 0; k < 9; ++k) Q.F1[i * 9 + k] = Fn[k];
       if (Q.Jp1) Q.Jp1[i] = Jpn;
     } else {
-      elastic_stress(Ft, Q.mu[i], Q.lam[i], kind == DIFF_NEOHOOKEAN, U, sig, V, P);
+      elastic_stress(Ft, Q.mu[i], Q.lam[i], kind == DIFF_NEOHOOKEAN || kind == DIFF_MUSCLE_NEOHOOKEAN, U, sig, V, P);
+      if (diff_muscle(kind) && Q.actu) muscle_stress(Ft, Q.mdir + i * 3, Q.aux[i * 2], Q.actu[i], P);
       if (Q.Jp1) Q.Jp1[i] = Q.Jp[i];
     }
-    if (Q.F1 && kind != DIFF_SAND && kind != DIFF_SNOW) {
+    if (Q.F1 && !plastic) {
       if (kind == DIFF_LIQUID) {  // liquid.py:36-40: F_new = J^(1/3) I
         const float j3 = powf(sig[0] * sig[1] * sig[2], 1.f / 3.f);
         for (int k = 0; k < 9; ++k) Q.F1[i * 9 + k] = (k % 4 == 0) ? j3 : 0.f;
@@ -511,7 +543,7 @@ __global__ void __launch_bounds__(256) k_dp2g_adj(DiffParams Q) {
     const float mu = Q.mu[i], lam = Q.lam[i];
     const float mass = p_mass(Q, i);
     const int kind = p_kind(Q, i);
-    const bool plastic = kind == DIFF_SAND || kind == DIFF_SNOW;
+    const bool plastic = diff_plastic(kind), neo = kind == DIFF_NEOHOOKEAN || kind == DIFF_MUSCLE_NEOHOOKEAN;
     float Ft[9], U[9], sig[3], V[9], P[9];
     f_tmp(C, F, S.dt, Ft);
     svd_f32(Ft, U, sig, V);
@@ -521,7 +553,8 @@ __global__ void __launch_bounds__(256) k_dp2g_adj(DiffParams Q) {
       float Fn[9], Jpn;
       material_update<float>(M, Ft, U, sig, V, Q.Jp[i], 0.f, mdir, S.eps, Fn, Jpn, P);
     } else {
-      elastic_stress(Ft, mu, lam, kind == DIFF_NEOHOOKEAN, U, sig, V, P);
+      elastic_stress(Ft, mu, lam, neo, U, sig, V, P);
+      if (diff_muscle(kind) && Q.actu) muscle_stress(Ft, Q.mdir + i * 3, Q.aux[i * 2], Q.actu[i], P);
     }
     float A[9];
     for (int k = 0; k < 9; ++k) A[k] = S.stress_scale * P[k] + mass * C[k];
@@ -578,11 +611,11 @@ __global__ void __launch_bounds__(256) k_dp2g_adj(DiffParams Q) {
       float gFn[9];
       for (int k = 0; k < 9; ++k) gFn[k] = Q.gF1 ? Q.gF1[i * 9 + k] : 0.f;
       float gJ = 0.f;
-      plastic_adjoint<float>(kind == DIFF_SAND ? MT_SAND : MT_SNOW, U, sig, V, Q.Jp[i], mu, lam, aux[0],
-                             kind == DIFF_SAND ? 0.f : aux[1], S.eps, gFn, gP, Q.gJp1 ? Q.gJp1[i] : 0.f, gFt, gJ, gmu,
-                             glam);
+      plastic_adjoint<float>(diff_plastic_law(kind), U, sig, V, Q.Jp[i], mu, lam, aux[0],
+                             (kind == DIFF_SAND || kind == DIFF_EP_VON_MISES) ? 0.f : aux[1], S.eps, gFn, gP,
+                             Q.gJp1 ? Q.gJp1[i] : 0.f, gFt, gJ, gmu, glam);
       if (Q.gJp) Q.gJp[i] = gJ;
-    } else if (kind == DIFF_NEOHOOKEAN) {
+    } else if (neo) {
       // P = mu F F^T + (lam log J - mu) I
       float FFt[9];
       mat_mul_bt(Ft, Ft, FFt);
@@ -650,6 +683,24 @@ __global__ void __launch_bounds__(256) k_dp2g_adj(DiffParams Q) {
       cof[8] = Ft[0] * Ft[4] - Ft[1] * Ft[3];
       for (int k = 0; k < 9; ++k) gFt[k] += lam * (2.f * J - 1.f) * trP * cof[k];
     }
+    if (diff_muscle(kind) && Q.actu) {
+      // P += k a w w^T, w = F_tmp m: dL/dF_tmp += k a (gP + gP^T) w m^T, dL/da += k w^T gP w
+      const float* m = Q.mdir + i * 3;
+      const float k = Q.aux[i * 2], a = Q.actu[i];
+      float w[3], y[3];
+      for (int r = 0; r < 3; ++r) w[r] = Ft[r * 3 + 0] * m[0] + Ft[r * 3 + 1] * m[1] + Ft[r * 3 + 2] * m[2];
+      float ga = 0.f;
+      for (int r = 0; r < 3; ++r) {
+        y[r] = 0.f;
+        for (int c = 0; c < 3; ++c) {
+          y[r] += (gP[r * 3 + c] + gP[c * 3 + r]) * w[c];
+          ga += w[r] * gP[r * 3 + c] * w[c];
+        }
+      }
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) gFt[r * 3 + c] += k * a * y[r] * m[c];
+      if (Q.g_actu) Q.g_actu[i] += k * ga;
+    }
     if (!plastic && Q.gJp) Q.gJp[i] = Q.gJp1 ? Q.gJp1[i] : 0.f;  // Jp passes through unchanged
     // F_tmp = (I + dt C) F
     float Am[9];
@@ -683,6 +734,13 @@ namespace {
 
 const DiffFields kNoFields{};
 
+// Muscle inputs of a call (null members: no actuation stress)
+struct DiffMuscle {
+  const float* actu;
+  const float* mdir;
+  float* g_actu;
+};
+
 // The fields of substep k of a sequence that starts at the fields' substep counter ff->step.
 const DiffFields* fields_at(const DiffFields* ff, int32_t k, DiffFields& tmp) {
   if (!ff || ff->n == 0) return nullptr;
@@ -697,7 +755,7 @@ int diff_forward(const mpm_scene_config* scene, double rho, int32_t neohookean, 
                  const float* F, const float* Jp, const float* mu, const float* lam, float* x1, float* v1, float* C1,
                  float* F1, float* Jp1, void* grid_pm, void* grid_v, uint32_t* status, void* stream, int n_tools = 0,
                  const DiffToolDev* tools = nullptr, const float* tool_f = nullptr, float* tool_f1 = nullptr,
-                 const DiffFields* ff = nullptr) {
+                 const DiffFields* ff = nullptr, const DiffMuscle* mus = nullptr) {
   if (!scene || n < 0 || !grid_pm || !grid_v || !status) return MPM_ERR_BAD_ARG;
   DiffParams Q;
   std::memset(&Q, 0, sizeof(Q));
@@ -720,6 +778,7 @@ int diff_forward(const mpm_scene_config* scene, double rho, int32_t neohookean, 
   for (int t = 0; t < n_tools; ++t) Q.tools[t] = tools[t];
   Q.tool_f = tool_f;
   Q.tool_f1 = tool_f1;
+  if (mus && mus->actu && mus->mdir) Q.actu = mus->actu, Q.mdir = mus->mdir;
   const int64_t nodes = (int64_t)Q.S.res[0] * Q.S.res[1] * Q.S.res[2];
   cudaStream_t s = (cudaStream_t)stream;
   const int gb = (int)((nodes + 255) / 256 < 8192 ? (nodes + 255) / 256 : 8192);
@@ -739,7 +798,7 @@ int diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean,
                   float* gC, float* gF, float* gJp, float* gmu, float* glam, void* grid_pm, void* grid_v,
                   void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream, int n_tools = 0,
                   const DiffToolDev* tools = nullptr, const float* tool_f = nullptr, const float* tool_f1 = nullptr,
-                  float* g_tool = nullptr, const DiffFields* ff = nullptr) {
+                  float* g_tool = nullptr, const DiffFields* ff = nullptr, const DiffMuscle* mus = nullptr) {
   if (!scene || n < 0 || !grid_pm || !grid_v || !g_grid_v || !g_grid_pm) return MPM_ERR_BAD_ARG;
   DiffParams Q;
   std::memset(&Q, 0, sizeof(Q));
@@ -766,6 +825,7 @@ int diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean,
   Q.tool_f = tool_f;
   Q.tool_f1 = const_cast<float*>(tool_f1);
   Q.g_tool = g_tool;
+  if (mus && mus->actu && mus->mdir) Q.actu = mus->actu, Q.mdir = mus->mdir, Q.g_actu = mus->g_actu;
   const int64_t nodes = (int64_t)Q.S.res[0] * Q.S.res[1] * Q.S.res[2];
   cudaStream_t s = (cudaStream_t)stream;
   const int gb = (int)((nodes + 255) / 256 < 8192 ? (nodes + 255) / 256 : 8192);
@@ -783,7 +843,7 @@ int diff_forward_seq(const mpm_scene_config* scene, double rho, int32_t neohooke
                      float* C_seq, float* F_seq, float* Jp_seq, int32_t ring, const float* mu, const float* lam,
                      void* grid_pm, void* grid_v, int32_t grids_per_substep, uint32_t* status, void* stream,
                      int n_tools = 0, const DiffToolDev* tools = nullptr, float* tool_seq = nullptr,
-                     const DiffFields* ff = nullptr) {
+                     const DiffFields* ff = nullptr, const DiffMuscle* mus = nullptr) {
   if (!scene || n < 0 || n_sub < 0 || ring < 2 || !x_seq || !v_seq || !C_seq || !F_seq) return MPM_ERR_BAD_ARG;
   DiffFields tmp;
   SceneDev S;
@@ -799,7 +859,7 @@ int diff_forward_seq(const mpm_scene_config* scene, double rho, int32_t neohooke
                                Jp_seq ? Jp_seq + b * n : nullptr, (float4*)grid_pm + go, (float4*)grid_v + go, status,
                                stream, n_tools, tools, tool_seq ? tool_seq + (int64_t)k * n_tools * 13 : nullptr,
                                tool_seq ? tool_seq + (int64_t)(k + 1) * n_tools * 13 : nullptr,
-                               fields_at(ff, k, tmp));
+                               fields_at(ff, k, tmp), mus);
     if (r) return r;
   }
   return MPM_OK;
@@ -812,7 +872,7 @@ int diff_backward_seq(const mpm_scene_config* scene, double rho, int32_t neohook
                       const float* lam, float* g_seq, float* gmu, float* glam, void* grid_pm, void* grid_v,
                       void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream, int n_tools = 0,
                       const DiffToolDev* tools = nullptr, const float* tool_seq = nullptr, float* g_tool = nullptr,
-                      const DiffFields* ff = nullptr) {
+                      const DiffFields* ff = nullptr, const DiffMuscle* mus = nullptr) {
   if (!scene || n < 0 || n_sub < 0 || !g_seq) return MPM_ERR_BAD_ARG;
   DiffFields tmp;
   if (n_tools > 0) {
@@ -839,7 +899,7 @@ int diff_backward_seq(const mpm_scene_config* scene, double rho, int32_t neohook
                                 (float4*)grid_v + (int64_t)k * nodes, g_grid_v, g_grid_pm, status, stream, n_tools,
                                 tools, tool_seq ? tool_seq + (int64_t)k * n_tools * 13 : nullptr,
                                 tool_seq ? tool_seq + (int64_t)(k + 1) * n_tools * 13 : nullptr, g_tool,
-                                fields_at(ff, k, tmp));
+                                fields_at(ff, k, tmp), mus);
     if (r) return r;
     cur = 1 - cur;
   }
@@ -886,6 +946,20 @@ int diff_fields(const mpm_force_field* fields, int32_t n, int32_t scene_index, u
   out.step = (unsigned long long)step0;
   for (int32_t i = 0; i < n; ++i)
     if (!force_field_dev(fields[i], out.f[i])) return MPM_ERR_BAD_ARG;
+  return MPM_OK;
+}
+
+// The extras of a sequence (tools, force fields, Muscle inputs) as the internal calls take them.
+int diff_extras(const mpm_diff_extras* ex, DiffToolDev* td, DiffFields& ff, DiffMuscle& mus) {
+  std::memset(&mus, 0, sizeof(mus));
+  if (!ex) return diff_fields(nullptr, 0, 0, 0, ff);
+  int r = diff_tools_dev(ex->tools, ex->n_tools, ex->tool_seq, td);
+  if (r) return r;
+  if ((r = diff_fields(ex->force_fields, ex->n_force_fields, ex->scene_index, ex->ff_step, ff))) return r;
+  if ((ex->actu == nullptr) != (ex->muscle_dir == nullptr)) return MPM_ERR_BAD_ARG;
+  mus.actu = ex->actu;
+  mus.mdir = ex->muscle_dir;
+  mus.g_actu = ex->g_actu;
   return MPM_OK;
 }
 
@@ -968,39 +1042,38 @@ int mpm_diff_backward_seq_pp(const mpm_scene_config* scene, const float* mass, c
                            g_seq, gmu, glam, grid_pm, grid_v, g_grid_v, g_grid_pm, status, stream);
 }
 
-int mpm_diff_forward_seq_ff(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
+int mpm_diff_forward_seq_ex(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
                             int64_t n, int32_t n_sub, float* x_seq, float* v_seq, float* C_seq, float* F_seq,
-                            float* Jp_seq, int32_t ring, const float* mu, const float* lam, const mpm_diff_tool* tools,
-                            int32_t n_tools, float* tool_seq, const mpm_force_field* force_fields,
-                            int32_t n_force_fields, int32_t scene_index, uint64_t ff_step, void* grid_pm, void* grid_v,
-                            int32_t grids_per_substep, uint32_t* status, void* stream) {
+                            float* Jp_seq, int32_t ring, const float* mu, const float* lam, const mpm_diff_extras* ex,
+                            void* grid_pm, void* grid_v, int32_t grids_per_substep, uint32_t* status, void* stream) {
   if (n > 0 && (!mass || !kind || !aux || !Jp_seq)) return MPM_ERR_BAD_ARG;
   DiffToolDev td[MPM_DIFF_MAX_TOOLS];
-  int r = diff_tools_dev(tools, n_tools, tool_seq, td);
-  if (r) return r;
   DiffFields ff;
-  if ((r = diff_fields(force_fields, n_force_fields, scene_index, ff_step, ff))) return r;
+  DiffMuscle mus;
+  const int r = diff_extras(ex, td, ff, mus);
+  if (r) return r;
+  const int nt = ex ? ex->n_tools : 0;
   return diff_forward_seq(scene, 0.0, 0, mass, kind, aux, n, n_sub, x_seq, v_seq, C_seq, F_seq, Jp_seq, ring, mu, lam,
-                          grid_pm, grid_v, grids_per_substep, status, stream, n_tools, td, tool_seq, &ff);
+                          grid_pm, grid_v, grids_per_substep, status, stream, nt, td, ex ? ex->tool_seq : nullptr, &ff,
+                          &mus);
 }
 
-int mpm_diff_backward_seq_ff(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
+int mpm_diff_backward_seq_ex(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
                              int64_t n, int32_t n_sub, const float* x_seq, const float* v_seq, const float* C_seq,
                              const float* F_seq, const float* Jp_seq, const float* mu, const float* lam,
-                             const mpm_diff_tool* tools, int32_t n_tools, const float* tool_seq, float* g_tool,
-                             const mpm_force_field* force_fields, int32_t n_force_fields, int32_t scene_index,
-                             uint64_t ff_step, float* g_seq, float* gmu, float* glam, void* grid_pm, void* grid_v,
-                             void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream) {
+                             const mpm_diff_extras* ex, float* g_seq, float* gmu, float* glam, void* grid_pm,
+                             void* grid_v, void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream) {
   if (n > 0 && (!mass || !kind || !aux || !Jp_seq)) return MPM_ERR_BAD_ARG;
   DiffToolDev td[MPM_DIFF_MAX_TOOLS];
-  int r = diff_tools_dev(tools, n_tools, tool_seq, td);
-  if (r) return r;
-  if (n_tools > 0 && !g_tool) return MPM_ERR_BAD_ARG;
   DiffFields ff;
-  if ((r = diff_fields(force_fields, n_force_fields, scene_index, ff_step, ff))) return r;
+  DiffMuscle mus;
+  const int r = diff_extras(ex, td, ff, mus);
+  if (r) return r;
+  const int nt = ex ? ex->n_tools : 0;
+  if (nt > 0 && !ex->g_tool) return MPM_ERR_BAD_ARG;
   return diff_backward_seq(scene, 0.0, 0, mass, kind, aux, n, n_sub, x_seq, v_seq, C_seq, F_seq, Jp_seq, mu, lam,
-                           g_seq, gmu, glam, grid_pm, grid_v, g_grid_v, g_grid_pm, status, stream, n_tools, td,
-                           tool_seq, g_tool, &ff);
+                           g_seq, gmu, glam, grid_pm, grid_v, g_grid_v, g_grid_pm, status, stream, nt, td,
+                           ex ? ex->tool_seq : nullptr, ex ? ex->g_tool : nullptr, &ff, &mus);
 }
 
 int mpm_diff_forward_seq_tools(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
@@ -1008,9 +1081,13 @@ int mpm_diff_forward_seq_tools(const mpm_scene_config* scene, const float* mass,
                                float* Jp_seq, int32_t ring, const float* mu, const float* lam,
                                const mpm_diff_tool* tools, int32_t n_tools, float* tool_seq, void* grid_pm,
                                void* grid_v, int32_t grids_per_substep, uint32_t* status, void* stream) {
-  return mpm_diff_forward_seq_ff(scene, mass, kind, aux, n, n_sub, x_seq, v_seq, C_seq, F_seq, Jp_seq, ring, mu, lam,
-                                 tools, n_tools, tool_seq, nullptr, 0, 0, 0, grid_pm, grid_v, grids_per_substep,
-                                 status, stream);
+  mpm_diff_extras ex;
+  std::memset(&ex, 0, sizeof(ex));
+  ex.tools = tools;
+  ex.n_tools = n_tools;
+  ex.tool_seq = tool_seq;
+  return mpm_diff_forward_seq_ex(scene, mass, kind, aux, n, n_sub, x_seq, v_seq, C_seq, F_seq, Jp_seq, ring, mu, lam,
+                                 &ex, grid_pm, grid_v, grids_per_substep, status, stream);
 }
 
 int mpm_diff_backward_seq_tools(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
@@ -1019,9 +1096,14 @@ int mpm_diff_backward_seq_tools(const mpm_scene_config* scene, const float* mass
                                 const mpm_diff_tool* tools, int32_t n_tools, const float* tool_seq, float* g_tool,
                                 float* g_seq, float* gmu, float* glam, void* grid_pm, void* grid_v, void* g_grid_v,
                                 void* g_grid_pm, uint32_t* status, void* stream) {
-  return mpm_diff_backward_seq_ff(scene, mass, kind, aux, n, n_sub, x_seq, v_seq, C_seq, F_seq, Jp_seq, mu, lam, tools,
-                                  n_tools, tool_seq, g_tool, nullptr, 0, 0, 0, g_seq, gmu, glam, grid_pm, grid_v,
-                                  g_grid_v, g_grid_pm, status, stream);
+  mpm_diff_extras ex;
+  std::memset(&ex, 0, sizeof(ex));
+  ex.tools = tools;
+  ex.n_tools = n_tools;
+  ex.tool_seq = const_cast<float*>(tool_seq);
+  ex.g_tool = g_tool;
+  return mpm_diff_backward_seq_ex(scene, mass, kind, aux, n, n_sub, x_seq, v_seq, C_seq, F_seq, Jp_seq, mu, lam, &ex,
+                                  g_seq, gmu, glam, grid_pm, grid_v, g_grid_v, g_grid_pm, status, stream);
 }
 
 }  // extern "C"

@@ -291,8 +291,8 @@ class MPMEntity:
         if diff is not None:  # differentiable mode: the targets enter the torch state (their grads flow back)
             if self._tgt["act"] is not None:
                 raise GenesisException("Activation changes are not supported in differentiable mode.")
-            for key in ("pos", "vel"):  # positions first: setting positions resets velocities
-                if self._tgt[key] is not None:
+            for key in ("pos", "vel", "actu"):  # positions first: setting positions resets velocities
+                if self._tgt.get(key) is not None:
                     val, envs_idx = self._tgt[key]
                     diff.write(key, self._particle_start, self._n_particles, val, self._envs(envs_idx))
             self._tgt = {"pos": None, "vel": None, "act": None}
@@ -340,6 +340,11 @@ class MPMEntity:
             if particles_idx_local is not None:
                 grp = grp[torch.as_tensor(particles_idx_local, device="cuda", dtype=torch.long).reshape(-1)]
             a = torch.gather(a, 2, grp.reshape(1, -1, 1).expand(a.shape[0], -1, 1))[..., 0]
+        if self._solver._diff is not None:  # differentiable mode: an input of the next step (process_input)
+            if particles_idx_local is not None:
+                raise GenesisException("In differentiable mode the actuation is set for all of an entity's particles.")
+            self._tgt["actu"] = (a, envs_idx)
+            return
         self._set_field(_lib.FIELD_ACTU, 1, a[..., None], envs_idx, particles_idx_local)
 
     def set_actuation(self, actus, envs_idx=None):
@@ -359,6 +364,9 @@ class MPMEntity:
         a = torch.broadcast_to(a, (B, self._n_particles, n_groups))
         grp = self._muscle_groups()
         per = torch.gather(a, 2, grp.reshape(1, -1, 1).expand(B, -1, 1))
+        if self._solver._diff is not None:  # differentiable mode: an input of the next step, on the graph of actus
+            self._tgt["actu"] = (per[..., 0], envs_idx)
+            return
         self._set_field(_lib.FIELD_ACTU, 1, per, envs_idx)
 
     def set_muscle_group(self, muscle_group):
@@ -383,6 +391,8 @@ class MPMEntity:
         d = torch.as_tensor(muscle_direction, dtype=torch.float32, device="cuda").reshape(-1, 3)
         d = d.expand(self._n_particles, 3) if d.shape[0] == 1 else d
         self._set_field(_lib.FIELD_MUSCLE_DIR, 3, d, None)
+        if self._solver._diff is not None:
+            self._solver._diff.set_muscle_direction(self._particle_start, self._n_particles, d)
 
     def set_free(self, free):
         f = torch.as_tensor(free, device="cuda").to(torch.float32).reshape(-1)

@@ -16,13 +16,16 @@ hand-written adjoint substeps in reverse (mpm_diff_backward_seq_pp).  Entity inp
 steps enter the state through differentiable torch ops, so their gradients arrive where the
 reference's process_input_grad puts them.
 
-Materials: Elastic (corotated or neo-Hookean), Liquid, Sand and Snow, any mix of entities;
-particle masses, Lame parameters and plasticity constants per particle, Jp part of the
-differentiated state.  Tool entities (tool_entity/) are part of the step: each env's state also
+Materials: Elastic (corotated or neo-Hookean), Liquid, Sand, Snow, ElastoPlastic (clamped or von
+Mises) and Muscle, any mix of entities; particle masses, Lame parameters and plasticity constants
+per particle, Jp part of the differentiated state.  Muscle actuation (entity.set_actuation /
+set_particles_actu) is part of each env's state too: constant over a step, it enters the stress of
+every substep, and its gradient reaches the tensors passed in (the reference's
+_set_particles_actu_grad).  Tool entities (tool_entity/) are part of the step: each env's state also
 holds every tool's position and velocity ([n_tools, 6], differentiated through Mesh.collide in the
-grid op and ToolEntity.advect, mpm_diff_forward_seq_tools / mpm_diff_backward_seq_tools) and, as
+grid op and ToolEntity.advect) and, as
 plain tensors, its orientation and angular velocity.  Built-in force fields act in the
-differentiable grid op (mpm_diff_forward_seq_ff / mpm_diff_backward_seq_ff), each step with the
+differentiable grid op (mpm_diff_forward_seq_ex / mpm_diff_backward_seq_ex), each step with the
 fields as they were when it ran.  As in the reference, CPIC and emitters are rejected in this mode;
 Custom force fields (a torch function here) are too.
 """
@@ -38,6 +41,7 @@ from . import _lib
 from .exceptions import GenesisException
 
 KIND_COROTATED, KIND_NEOHOOKEAN, KIND_LIQUID, KIND_SAND, KIND_SNOW = 0, 1, 2, 3, 4
+KIND_MUSCLE_COROTATED, KIND_MUSCLE_NEOHOOKEAN, KIND_EP_CLAMP, KIND_EP_VON_MISES = 5, 6, 7, 8
 FIELDS = ("pos", "vel", "C", "F", "Jp")
 _WIDTH = (3, 3, 9, 9, 1)       # floats per particle of each state field
 _OFFSET = (0, 3, 6, 15, 24)    # offsets (in units of n) in the packed gradient buffer of 25 n floats
@@ -45,10 +49,17 @@ _OFFSET = (0, 3, 6, 15, 24)    # offsets (in units of n) in the packed gradient 
 
 def material_kind(material) -> tuple[int, float, float]:
     """(kind, aux0, aux1) of a material in differentiable mode."""
-    from .materials import Elastic, Liquid, Sand, Snow
+    from .materials import Elastic, ElastoPlastic, Liquid, Muscle, Sand, Snow
 
     if type(material) is Elastic:
         return (KIND_NEOHOOKEAN if material.model == "neohooken" else KIND_COROTATED), 0.0, 0.0
+    if type(material) is Muscle:  # aux: the actuation stiffness (muscle.py: stiffness = E)
+        kind = KIND_MUSCLE_NEOHOOKEAN if material.model == "neohooken" else KIND_MUSCLE_COROTATED
+        return kind, float(material.stiffness), 0.0
+    if type(material) is ElastoPlastic:  # the product path's material record (clamp bounds | yield ratio)
+        if material.use_von_mises:
+            return KIND_EP_VON_MISES, float(material.von_mises_yield_stress) / (2.0 * float(material.mu)), 0.0
+        return KIND_EP_CLAMP, 1.0 - float(material.yield_lower), 1.0 + float(material.yield_higher)
     if type(material) is Liquid:
         return KIND_LIQUID, 0.0, 0.0
     if type(material) is Sand:
@@ -56,18 +67,18 @@ def material_kind(material) -> tuple[int, float, float]:
     if type(material) is Snow:
         return KIND_SNOW, 1.0 - float(material.yield_lower), 1.0 + float(material.yield_higher)
     raise GenesisException(
-        f"{type(material).__name__} is not differentiable here: requires_grad=True supports Elastic, Liquid, Sand "
-        "and Snow MPM materials."
+        f"{type(material).__name__} is not differentiable here: requires_grad=True supports the MPM materials "
+        "Elastic, Liquid, Sand, Snow, ElastoPlastic and Muscle."
     )
 
 
 class _StepNode(torch.autograd.Function):
-    """One scene.step() of one env: (x, v, C, F, Jp, tool pos/vel) -> the state after n_sub substeps,
-    plus the tools' orientation and angular velocity (not differentiated)."""
+    """One scene.step() of one env: (x, v, C, F, Jp, tool pos/vel, actuation) -> the state after n_sub
+    substeps, plus the tools' orientation and angular velocity (not differentiated)."""
 
     @staticmethod
-    def forward(ctx, engine, n_sub, fields, qa, x, v, C, F, Jp, T):
-        st = tuple(t.detach().float().contiguous() for t in (x, v, C, F, Jp, T))
+    def forward(ctx, engine, n_sub, fields, qa, x, v, C, F, Jp, T, A):
+        st = tuple(t.detach().float().contiguous() for t in (x, v, C, F, Jp, T, A))
         qa = qa.detach().float().contiguous()
         out, qa_end = engine.run_forward(st, n_sub, qa, fields)
         ctx.engine, ctx.n_sub, ctx.fields = engine, n_sub, fields
@@ -76,9 +87,9 @@ class _StepNode(torch.autograd.Function):
         return (*out, qa_end)
 
     @staticmethod
-    def backward(ctx, gx, gv, gC, gF, gJp, gT, _gqa):
+    def backward(ctx, gx, gv, gC, gF, gJp, gT, gA, _gqa):
         saved = ctx.saved_tensors
-        grads = ctx.engine.run_backward(saved[:6], ctx.n_sub, (gx, gv, gC, gF, gJp, gT), saved[6], ctx.fields)
+        grads = ctx.engine.run_backward(saved[:7], ctx.n_sub, (gx, gv, gC, gF, gJp, gT, gA), saved[7], ctx.fields)
         return (None, None, None, None, *grads)
 
 
@@ -110,6 +121,9 @@ class SceneDiffEngine:
         self.lam = cat(lam, np.float32).contiguous()
         self.aux = torch.as_tensor(np.concatenate(aux) if aux else np.zeros((0, 2), np.float32),
                                    device="cuda").contiguous()
+        # Muscle particles: fibre direction (set_muscle; default +z as mpm_solver.py:825) and actuation
+        self.has_muscle = bool(((self.kind == KIND_MUSCLE_COROTATED) | (self.kind == KIND_MUSCLE_NEOHOOKEAN)).any())
+        self.mdir = torch.tensor([0.0, 0.0, 1.0], device="cuda").repeat(n, 1).contiguous()
         self.cfg = _lib.MpmSceneConfig()
         c = self.cfg
         c.substep_dt = solver.substep_dt
@@ -138,7 +152,8 @@ class SceneDiffEngine:
         self._init_tools(solver)
         self.set_force_fields(getattr(solver, "_ffs", []))
         self.states = [(x0.clone(), torch.zeros((n, 3), device=dev), torch.zeros((n, 3, 3), device=dev),
-                        eye.repeat(n, 1, 1), self.Jp0.clone(), self.T0.clone()) for _ in range(B)]
+                        eye.repeat(n, 1, 1), self.Jp0.clone(), self.T0.clone(), torch.zeros(n, device=dev))
+                       for _ in range(B)]
         self.tool_qa = [self.qa0.clone() for _ in range(B)]
         self.steps_taken = 0
         self.substeps_taken = 0
@@ -217,32 +232,46 @@ class SceneDiffEngine:
                 t[0] = f.detach()
         return seq
 
-    def _forward_seq(self, seq, n_sub, ring, gpm, gv, keep_grids, tool_seq, fields):
+    def _extras(self, tool_seq, fields, actu, g_tool=None, g_actu=None):
+        """The mpm_diff_extras record of one call (the arrays stay referenced by the caller)."""
         nt = len(self.tools)
         recs, nf, env, ff_step = fields
-        r = self.lib.mpm_diff_forward_seq_ff(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(),
+        ex = _lib.MpmDiffExtras()
+        ex.tools = ctypes.addressof(self.tool_recs)
+        ex.n_tools = nt
+        ex.tool_seq = tool_seq.data_ptr() if nt else None
+        ex.g_tool = g_tool.data_ptr() if (nt and g_tool is not None) else None
+        ex.force_fields = ctypes.addressof(recs)
+        ex.n_force_fields = nf
+        ex.scene_index = env
+        ex.ff_step = ff_step
+        if self.has_muscle:
+            ex.actu = actu.data_ptr()
+            ex.muscle_dir = self.mdir.data_ptr()
+            ex.g_actu = g_actu.data_ptr() if g_actu is not None else None
+        return ex
+
+    def _forward_seq(self, seq, n_sub, ring, gpm, gv, keep_grids, tool_seq, fields, actu):
+        ex = self._extras(tool_seq, fields, actu)
+        r = self.lib.mpm_diff_forward_seq_ex(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(),
                                              self.aux.data_ptr(), self.n, int(n_sub), *[t.data_ptr() for t in seq],
-                                             ring, self.mu.data_ptr(), self.lam.data_ptr(), self.tool_recs, nt,
-                                             tool_seq.data_ptr() if nt else None, recs, nf, env, ff_step,
+                                             ring, self.mu.data_ptr(), self.lam.data_ptr(), ctypes.byref(ex),
                                              gpm.data_ptr(), gv.data_ptr(), int(keep_grids), self.status.data_ptr(),
                                              self._s())
-        _lib.check(r, None, "mpm_diff_forward_seq_ff")
+        _lib.check(r, None, "mpm_diff_forward_seq_ex")
 
-    def _backward_seq(self, seq, n_sub, gp, gpm, gv, tool_seq, g_tool, fields):
+    def _backward_seq(self, seq, n_sub, gp, gpm, gv, tool_seq, g_tool, fields, actu, g_actu):
         n = self.n
-        nt = len(self.tools)
-        recs, nf, env, ff_step = fields
         gmu = torch.zeros(n, device="cuda")
         glam = torch.zeros(n, device="cuda")
-        r = self.lib.mpm_diff_backward_seq_ff(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(),
+        ex = self._extras(tool_seq, fields, actu, g_tool, g_actu)
+        r = self.lib.mpm_diff_backward_seq_ex(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(),
                                               self.aux.data_ptr(), n, int(n_sub), *[t.data_ptr() for t in seq],
-                                              self.mu.data_ptr(), self.lam.data_ptr(), self.tool_recs, nt,
-                                              tool_seq.data_ptr() if nt else None,
-                                              g_tool.data_ptr() if nt else None, recs, nf, env, ff_step,
+                                              self.mu.data_ptr(), self.lam.data_ptr(), ctypes.byref(ex),
                                               gp.data_ptr(), gmu.data_ptr(), glam.data_ptr(), gpm.data_ptr(),
                                               gv.data_ptr(), self.g_grid_v.data_ptr(), self.g_grid_pm.data_ptr(),
                                               self.status.data_ptr(), self._s())
-        _lib.check(r, None, "mpm_diff_backward_seq_ff")
+        _lib.check(r, None, "mpm_diff_backward_seq_ex")
 
     def _g_tool(self, gT):
         g = torch.zeros((max(1, len(self.tools)), 12), device="cuda")
@@ -267,13 +296,13 @@ class SceneDiffEngine:
         """The state after n_sub substeps from st (new tensors), and the tools' (quat, ang) then."""
         seq = self._seq(2, st[:5])
         tseq = self._tool_seq(n_sub, st[5], qa)
-        self._forward_seq(seq, n_sub, 2, self.scratch[0], self.scratch[1], False, tseq, fields)
+        self._forward_seq(seq, n_sub, 2, self.scratch[0], self.scratch[1], False, tseq, fields, st[6])
         k = n_sub % 2
         nt = len(self.tools)
         end = tseq[n_sub, :nt]
         T_end = torch.cat([end[:, 0:3], end[:, 7:10]], 1).clone()
         qa_end = torch.cat([end[:, 3:7], end[:, 10:13]], 1).clone()
-        return (*(t[k].clone() for t in seq), T_end), qa_end
+        return (*(t[k].clone() for t in seq), T_end, st[6].clone()), qa_end
 
     def run_backward(self, st, n_sub, grads, qa, fields):
         """dL/d(step input) from dL/d(step output): re-simulates the step keeping every substep's state
@@ -282,12 +311,13 @@ class SceneDiffEngine:
         tseq = self._tool_seq(n_sub, st[5], qa)
         gpm = torch.empty((max(1, n_sub), self.nodes, 4), device="cuda")
         gv = torch.empty((max(1, n_sub), self.nodes, 4), device="cuda")
-        self._forward_seq(seq, n_sub, n_sub + 1, gpm, gv, True, tseq, fields)
+        self._forward_seq(seq, n_sub, n_sub + 1, gpm, gv, True, tseq, fields, st[6])
         gp = self._pack(grads[:5])
         g_tool = self._g_tool(grads[5])
-        self._backward_seq(seq, n_sub, gp, gpm, gv, tseq, g_tool, fields)
+        g_actu = grads[6].float().clone() if grads[6] is not None else torch.zeros(self.n, device="cuda")
+        self._backward_seq(seq, n_sub, gp, gpm, gv, tseq, g_tool, fields, st[6], g_actu)
         self.check()
-        return (*self._unpack(gp), g_tool[:len(self.tools), :6].clone())
+        return (*self._unpack(gp), g_tool[:len(self.tools), :6].clone(), g_actu)
 
     def check(self):
         st = int(self.status.item())
@@ -305,7 +335,7 @@ class SceneDiffEngine:
         self.pending = []
         for b, st in enumerate(self.states):
             out = _StepNode.apply(self, int(n_sub), fields[b], self.tool_qa[b], *st)
-            self.states[b], self.tool_qa[b] = tuple(out[:6]), out[6]
+            self.states[b], self.tool_qa[b] = tuple(out[:7]), out[7]
         self.steps_taken += 1
         self.substeps_taken += int(n_sub)
 
@@ -319,7 +349,8 @@ class SceneDiffEngine:
         n = self.n
         self.adj = [[torch.zeros((n, 3), device=dev), torch.zeros((n, 3), device=dev),
                      torch.zeros((n, 3, 3), device=dev), torch.zeros((n, 3, 3), device=dev),
-                     torch.zeros(n, device=dev), torch.zeros((len(self.tools), 6), device=dev)]
+                     torch.zeros(n, device=dev), torch.zeros((len(self.tools), 6), device=dev),
+                     torch.zeros(n, device=dev)]
                     for _ in range(self.B)]
         self.cursor = self.substeps_taken
         self._seg = None
@@ -373,16 +404,17 @@ class SceneDiffEngine:
                 tseq = self._tool_seq(n_sub, inputs[b][5], qas[b])
                 gpm = torch.empty((n_sub, self.nodes, 4), device="cuda")
                 gv = torch.empty((n_sub, self.nodes, 4), device="cuda")
-                self._forward_seq(seq, n_sub, n_sub + 1, gpm, gv, True, tseq, fields[b])
-                keep.append((seq, gpm, gv, tseq, fields[b]))
+                self._forward_seq(seq, n_sub, n_sub + 1, gpm, gv, True, tseq, fields[b], inputs[b][6])
+                keep.append((seq, gpm, gv, tseq, fields[b], inputs[b][6]))
             self._seg = (s_i, keep)
         for b in range(self.B):
-            seq, gpm, gv, tseq, (recs, nf, env, ff_step) = self._seg[1][b]
+            seq, gpm, gv, tseq, (recs, nf, env, ff_step), actu = self._seg[1][b]
             gp = self._pack(self.adj[b][:5])
             g_tool = self._g_tool(self.adj[b][5])
+            g_actu = self.adj[b][6]  # the step's actuation adjoint gathers every substep's share
             self._backward_seq([t[k: k + 1].contiguous() for t in seq], 1, gp, gpm[k], gv[k],
-                               tseq[k: k + 2].contiguous(), g_tool, (recs, nf, env, ff_step + k))
-            self.adj[b] = [*self._unpack(gp), g_tool[:len(self.tools), :6].clone()]
+                               tseq[k: k + 2].contiguous(), g_tool, (recs, nf, env, ff_step + k), actu, g_actu)
+            self.adj[b] = [*self._unpack(gp), g_tool[:len(self.tools), :6].clone(), g_actu]
         self.cursor -= 1
 
     def input_grad(self) -> None:
@@ -404,6 +436,13 @@ class SceneDiffEngine:
                     self.adj[b][5][start, cols] = 0.0
                 continue
             rows = slice(start, start + count)
+            if field == "actu":  # a Muscle entity's actuation (MPMEntity.process_input_grad)
+                if values.requires_grad:
+                    vb = torch.broadcast_to(values.to(device="cuda", dtype=torch.float32), (len(envs), count))
+                    torch.autograd.backward([vb], [torch.stack([self.adj[b][6][rows] for b in envs])])
+                for b in envs:
+                    self.adj[b][6][rows] = 0.0
+                continue
             j = 0 if field == "pos" else 1
             if values.requires_grad:
                 vb = torch.broadcast_to(values.to(device="cuda", dtype=torch.float32), (len(envs), count, 3))
@@ -413,8 +452,16 @@ class SceneDiffEngine:
                     self.adj[b][jj][rows] = 0.0
 
     def write(self, field: str, start: int, count: int, values: torch.Tensor, envs) -> None:
-        """Set one entity's particles [start, start+count) of `field` (pos / vel) in envs, through
-        differentiable torch ops (values broadcast to [len(envs), count, 3])."""
+        """Set one entity's particles [start, start+count) of `field` (pos / vel: values broadcast to
+        [len(envs), count, 3]; actu: to [len(envs), count]) in envs, through differentiable torch ops."""
+        if field == "actu":
+            self.pending.append((field, start, count, values, list(envs)))
+            vals = torch.broadcast_to(values.to(device="cuda", dtype=torch.float32), (len(envs), count))
+            for i, b in enumerate(envs):
+                st = list(self.states[b])
+                st[6] = torch.cat([st[6][:start], vals[i], st[6][start + count:]], 0)
+                self.states[b] = tuple(st)
+            return
         k = {"pos": 0, "vel": 1}[field]
         self.pending.append((field, start, count, values, list(envs)))
         vals = torch.broadcast_to(values.to(device="cuda", dtype=torch.float32), (len(envs), count, 3))
@@ -469,4 +516,8 @@ class SceneDiffEngine:
     def set_from_state(self, state, envs) -> None:
         for b in envs:
             self.states[b] = (*(getattr(state, k)[b].to(device="cuda", dtype=torch.float32) for k in FIELDS),
-                              self.states[b][5])
+                              self.states[b][5], self.states[b][6])
+
+    def set_muscle_direction(self, start: int, count: int, dirs: torch.Tensor) -> None:
+        """Fibre directions [count, 3] of particles [start, start+count) (constants of the steps to come)."""
+        self.mdir[start: start + count] = dirs.to(device="cuda", dtype=torch.float32)

@@ -558,29 +558,48 @@ int mpm_diff_backward_seq_tools(const mpm_scene_config* scene, const float* mass
                                 float* g_seq, float* gmu, float* glam, void* grid_pm, void* grid_v, void* g_grid_v,
                                 void* g_grid_pm, uint32_t* status, void* stream);
 
-/* mpm_diff_forward_seq_tools / mpm_diff_backward_seq_tools with the scene's force fields in the
- * differentiable grid op (legacy_coupler.py:381-383: v += acc(x, v) dt after gravity, before the
- * tools; the reference differentiates them through its autodiff).  force_fields: host array of
- * n_force_fields records (at most MPM_DIFF_MAX_FORCE_FIELDS, inactive ones skipped), copied in
- * the call; scene_index and ff_step (the substep counter of the first substep since the fields
- * were set) seed the noise draws as mpm_set_force_fields' fields draw them in env scene_index.
- * The backward needs the same fields, scene_index and ff_step as the forward it reverses; it
- * carries dL/dv through each field's Jacobian in the node velocity (the noise draws and the
- * node positions are constants). */
+/* The general differentiable sequence: mpm_diff_forward_seq_pp / mpm_diff_backward_seq_pp plus
+ * the optional parts of a scene in one record (zero-initialise it and fill what the scene has):
+ * - tool entities: tools, n_tools, tool_seq and (backward) g_tool, as mpm_diff_forward_seq_tools
+ *   takes them;
+ * - force fields (legacy_coupler.py:381-383: v += acc(x, v) dt after gravity, before the tools;
+ *   the reference differentiates them through its autodiff): host array of n_force_fields
+ *   mpm_force_field records (at most MPM_DIFF_MAX_FORCE_FIELDS, inactive ones skipped, copied in
+ *   the call); scene_index and ff_step (the fields' substep counter at the first substep) seed the
+ *   noise draws as mpm_set_force_fields' fields draw them in env scene_index.  The backward
+ *   carries dL/dv through each field's Jacobian in the node velocity (noise draws and node
+ *   positions are constants);
+ * - Muscle particles (kind 5: corotated, 6: neo-Hookean elastic plus the actuation stress
+ *   stiffness * actu * (F m)(F m)^T of muscle.py:46-53, aux[0] = stiffness): actu [n] and
+ *   muscle_dir [n][3] device arrays (both or neither; actu constant over the call), and for the
+ *   backward g_actu [n], into which dL/dactu is added (mpm_entity.py _set_particles_actu_grad).
+ * Kinds 7 and 8 are ElastoPlastic (elasto_plastic.py:44-71) with clamped principal stretches
+ * (aux = 1 - yield_lower, 1 + yield_higher) and with von Mises yield (aux[0] = yield stress / (2 mu)).
+ * The backward needs the same record contents as the forward it reverses. */
 #define MPM_DIFF_MAX_FORCE_FIELDS 8
-int mpm_diff_forward_seq_ff(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
+typedef struct mpm_diff_extras {
+  const mpm_diff_tool* tools;
+  int32_t n_tools;
+  int32_t n_force_fields;
+  float* tool_seq;
+  float* g_tool;
+  const mpm_force_field* force_fields;
+  int32_t scene_index;
+  int32_t pad0;
+  uint64_t ff_step;
+  const float* actu;
+  const float* muscle_dir;
+  float* g_actu;
+} mpm_diff_extras;
+int mpm_diff_forward_seq_ex(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
                             int64_t n, int32_t n_sub, float* x_seq, float* v_seq, float* C_seq, float* F_seq,
-                            float* Jp_seq, int32_t ring, const float* mu, const float* lam, const mpm_diff_tool* tools,
-                            int32_t n_tools, float* tool_seq, const mpm_force_field* force_fields,
-                            int32_t n_force_fields, int32_t scene_index, uint64_t ff_step, void* grid_pm, void* grid_v,
-                            int32_t grids_per_substep, uint32_t* status, void* stream);
-int mpm_diff_backward_seq_ff(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
+                            float* Jp_seq, int32_t ring, const float* mu, const float* lam, const mpm_diff_extras* ex,
+                            void* grid_pm, void* grid_v, int32_t grids_per_substep, uint32_t* status, void* stream);
+int mpm_diff_backward_seq_ex(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
                              int64_t n, int32_t n_sub, const float* x_seq, const float* v_seq, const float* C_seq,
                              const float* F_seq, const float* Jp_seq, const float* mu, const float* lam,
-                             const mpm_diff_tool* tools, int32_t n_tools, const float* tool_seq, float* g_tool,
-                             const mpm_force_field* force_fields, int32_t n_force_fields, int32_t scene_index,
-                             uint64_t ff_step, float* g_seq, float* gmu, float* glam, void* grid_pm, void* grid_v,
-                             void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream);
+                             const mpm_diff_extras* ex, float* g_seq, float* gmu, float* glam, void* grid_pm,
+                             void* grid_v, void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream);
 
 /* ABI version of this header (1). */
 int mpm_version(void);

@@ -44,16 +44,20 @@ void shim_material_f32(int type, int flags, double mu, double lam, double alpha,
 
 void shim_bspline_w(float fx, float* w) { bspline_w<float>(fx, w); }
 
-// Sand (type 2: p0 = alpha) / Snow (type 3: p0, p1 = clamp bounds) update in double, and its adjoint
-// (T = double or float) for the same F_tmp, Jp.
+// Sand (type 2: p0 = alpha) / Snow (type 3: p0, p1 = clamp bounds) / clamped ElastoPlastic (type 4:
+// p0, p1 = clamp bounds) / von Mises ElastoPlastic (EP_VON_MISES: p0 = yield stress / (2 mu)) update in
+// double, and its adjoint (T = double or float) for the same F_tmp, Jp.
 static MaterialDev plastic_material(int type, double mu, double lam, double p0, double p1) {
   MaterialDev M{};
-  M.type = type;
+  M.type = type == EP_VON_MISES ? MT_ELASTOPLASTIC : type;
+  M.flags = type == EP_VON_MISES ? MF_VON_MISES : 0;
   M.mu = (float)mu;
   M.lam = (float)lam;
   if (type == MT_SAND) {
     M.alpha = (float)p0;
     M.sand_coef = (float)((3.0 * lam + 2.0 * mu) / (2.0 * mu));
+  } else if (type == EP_VON_MISES) {
+    M.vm_ratio = (float)p0;
   } else {
     M.clamp_lo = (float)p0;
     M.clamp_hi = (float)p1;

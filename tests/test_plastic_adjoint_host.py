@@ -1,10 +1,11 @@
-"""The Sand and Snow adjoints of the differentiable substep (genesis_gb300/csrc/mpm_adjoint.cuh),
-compiled for the host, against FP64 central differences of the same material update
-(material_update, the code the kernels run): dL/dF_tmp and dL/dJp for
-L = <gFn, F_new> + <gP, P> + gJpn Jp_new with random weights, in every regime of the two laws
-(Sand: expanding tr >= 0, compressed and elastic (dg <= 0), compressed and yielding; Snow: inside
-the clamp, stretched past the upper bound, compressed past the lower bound), including F_tmp = I
-and nearly coinciding singular values."""
+"""The Sand, Snow and ElastoPlastic adjoints of the differentiable substep
+(genesis_gb300/csrc/mpm_adjoint.cuh), compiled for the host, against FP64 central differences of the
+same material update (material_update, the code the kernels run): dL/dF_tmp and dL/dJp for
+L = <gFn, F_new> + <gP, P> + gJpn Jp_new with random weights, in every regime of the laws
+(Sand: expanding tr >= 0, compressed and elastic (dg <= 0), compressed and yielding; Snow and the
+clamped ElastoPlastic: inside the clamp, stretched past the upper bound, compressed past the lower
+bound; von Mises ElastoPlastic: below and past the yield surface), including F_tmp = I and nearly
+coinciding singular values."""
 
 import ctypes
 import math
@@ -17,7 +18,9 @@ import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 EPS32 = float(np.finfo(np.float32).eps)
-MT_SAND, MT_SNOW = 2, 3
+MT_SAND, MT_SNOW, MT_ELASTOPLASTIC = 2, 3, 4
+EP_VON_MISES = 64 + MT_ELASTOPLASTIC  # the von Mises law's id in mpm_adjoint.cuh
+KINDS = [MT_SAND, MT_SNOW, MT_ELASTOPLASTIC, EP_VON_MISES]
 
 
 @pytest.fixture(scope="module")
@@ -35,11 +38,13 @@ def shim():
 
 
 def _params(kind):
-    E, nu = (1e6, 0.2) if kind == MT_SAND else (1.4e5, 0.2)
+    E, nu = {MT_SAND: (1e6, 0.2), MT_SNOW: (1.4e5, 0.2)}.get(kind, (3e5, 0.2))
     mu, lam = E / (2 * (1 + nu)), E * nu / ((1 + nu) * (1 - 2 * nu))
     if kind == MT_SAND:
         s = math.sin(math.radians(45.0))
         return mu, lam, math.sqrt(2 / 3) * 2 * s / (3 - s), 0.0
+    if kind == EP_VON_MISES:
+        return mu, lam, 1e4 / (2 * mu), 0.0  # von_mises_yield_stress 1e4
     return mu, lam, 1 - 2.5e-2, 1 + 4.5e-3
 
 
@@ -54,8 +59,12 @@ def _forward(lib, kind, Ft, Jp):
 
 def _regime(kind, Ft, Jp):
     s = np.linalg.svd(Ft.reshape(3, 3), compute_uv=False)
-    if kind == MT_SNOW:
+    if kind in (MT_SNOW, MT_ELASTOPLASTIC):
         return tuple(int(v < 1 - 2.5e-2) - int(v > 1 + 4.5e-3) for v in s)
+    if kind == EP_VON_MISES:
+        e = np.log(np.maximum(s, 0.05))
+        eh = e - e.mean()
+        return (int(math.sqrt((eh ** 2).sum() + EPS32) - _params(kind)[2] > 0),)
     e = np.log(np.maximum(np.abs(s), 1e-4))
     tr = e.sum() + Jp
     if tr >= 0:
@@ -78,13 +87,15 @@ def _cases(kind, rng):
                 Ft = -Ft
         if kind == MT_SAND:
             Jp = rng.choice([0.0, rng.uniform(-0.05, 0.05)])
-        else:
+        elif kind == MT_SNOW:
             Jp = rng.uniform(0.9, 1.1)
+        else:
+            Jp = 1.0
         out.append((Ft, Jp))
     return out
 
 
-@pytest.mark.parametrize("kind", [MT_SAND, MT_SNOW])
+@pytest.mark.parametrize("kind", KINDS)
 def test_plastic_adjoint_matches_fp64_central_differences(shim, kind):
     rng = np.random.default_rng(7 + kind)
     seen = set()
@@ -120,13 +131,13 @@ def test_plastic_adjoint_matches_fp64_central_differences(shim, kind):
         if _regime(kind, Fr, Jp + h) == reg and _regime(kind, Fr, Jp - h) == reg:
             fj = (L(Fr, Jp + h) - L(Fr, Jp - h)) / (2 * h)
             assert abs(gJp.value - fj) <= 2e-5 * max(abs(fj), scale) + 1e-9, (reg, gJp.value, fj)
-    want = {(0,), (1, 0), (1, 1)} if kind == MT_SAND else {(0, 0, 0)}
+    want = {MT_SAND: {(0,), (1, 0), (1, 1)}, EP_VON_MISES: {(0,), (1,)}}.get(kind, {(0, 0, 0)})
     assert want <= seen, seen
-    if kind == MT_SNOW:
+    if kind in (MT_SNOW, MT_ELASTOPLASTIC):
         assert any(r != (0, 0, 0) for r in seen), seen
 
 
-@pytest.mark.parametrize("kind", [MT_SAND, MT_SNOW])
+@pytest.mark.parametrize("kind", KINDS)
 def test_plastic_adjoint_float_close_to_double(shim, kind):
     """The float build the kernel runs stays within float rounding of the double one, F = I included."""
     rng = np.random.default_rng(3)
