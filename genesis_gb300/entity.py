@@ -82,6 +82,8 @@ class MPMEntity:
         pose from MPMSolver.set_link_poses) with a critically damped spring of `stiffness`."""
         if not isinstance(link_idx, int):
             raise GenesisException("link_idx must be an integer.")
+        if self._solver._diff is not None:
+            raise GenesisException("Particle constraints are not supported in differentiable mode.")
         lp, lq = self._solver.get_link_pose(link_idx)
         m = self._mask(particles_mask)
         pos = torch.as_tensor(np.array(lp, dtype=np.float32), device="cuda")

@@ -482,6 +482,8 @@ class MPMSolver:
         device once per grid object; tools then move by themselves every substep (see
         get_collider_poses).  The scene's tool entities follow these colliders in the library's
         list and keep their current poses."""
+        if self._diff is not None and list(colliders):
+            raise GenesisException("Rigid colliders are not supported in differentiable mode (tool entities are).")
         self._sync_tool_poses()
         self._user_colliders = list(colliders)
         self._upload_colliders()
@@ -683,6 +685,8 @@ class MPMSolver:
         k = {"sph": 0, "pbd": 1}.get(kind)
         if k is None:
             gs_exc(f"Unsupported coupled particle kind: {kind!r} (expected 'sph' or 'pbd').")
+        if self._diff is not None and pos is not None:
+            gs_exc("MPM <-> SPH / PBD coupling is not supported in differentiable mode.")
         if not hasattr(self, "_coupled"):
             self._coupled = [None, None]
         if pos is None:

@@ -473,3 +473,22 @@ def test_reference_scenario_differentiable_push_with_tool(gs, tmp_path):
     assert v_list[-1].grad is None or (v_list[-1].grad.abs() < eps).all()
     assert init_pos.grad is not None and (init_pos.grad.abs() > eps).any()
     assert (pos_obj_init.grad.abs() > eps).any() and (v_obj_init.grad.abs() > eps).any()
+
+
+def test_couplings_outside_the_differentiable_form_raise(gs):
+    """Rigid colliders, SPH / PBD coupling and particle constraints have no differentiable form here:
+    differentiable mode refuses them instead of stepping without them."""
+    from genesis_gb300.coupling import Collider
+    from genesis_gb300.exceptions import GenesisException
+
+    scene, box, _ = _scene(gs)
+    solver = scene.sim.mpm_solver
+    with pytest.raises(GenesisException, match="differentiable mode"):
+        solver.set_colliders([Collider("sphere", pos=(0.5, 0.5, 0.1), radius=0.05)])
+    p = torch.zeros((4, 3), device="cuda")
+    with pytest.raises(GenesisException, match="differentiable mode"):
+        solver.set_coupled_particles("sph", pos=p, vel=p.clone(), mass=torch.ones(4, device="cuda"))
+    with pytest.raises(GenesisException, match="differentiable mode"):
+        box.set_particle_constraints(np.ones(box.n_particles, bool), 0, 1e3)
+    solver.set_colliders([])  # an empty list stays allowed
+
