@@ -157,11 +157,16 @@ class MpmDiffExtras(ctypes.Structure):
         ("actu", c_void_p),
         ("muscle_dir", c_void_p),
         ("g_actu", c_void_p),
+        ("colliders", c_void_p),
+        ("sdf_ctx", c_void_p),
+        ("n_colliders", c_int32),
+        ("pad1", c_int32),
     ]
 
 
 DIFF_MAX_TOOLS = 4
 DIFF_MAX_FORCE_FIELDS = 8
+DIFF_MAX_COLLIDERS = 8
 
 
 class MpmSceneConfig(ctypes.Structure):

@@ -585,6 +585,52 @@ bool force_field_dev(const mpm_force_field& f, ForceFieldDev& d) {
   return true;
 }
 
+// A collider as the grid op reads it (float copies; SDF grids from ctx's table); null on success,
+// else what is wrong with the record.
+const char* collider_dev(const mpm_ctx* ctx, const mpm_collider& c, ColliderDev& d) {
+  if (c.type < MPM_COLLIDER_SPHERE || c.type > MPM_COLLIDER_TOOL) return "unknown collider type";
+  const bool gridded = c.type == MPM_COLLIDER_SDF || c.type == MPM_COLLIDER_TOOL;
+  if (gridded && (!ctx || c.sdf_grid < 0 || c.sdf_grid >= (int32_t)ctx->sdf_grids.size()))
+    return "collider SDF grid id out of range (mpm_add_sdf_grid)";
+  if (c.type == MPM_COLLIDER_SDF && !ctx->sdf_grids[(size_t)c.sdf_grid].grad)
+    return "an SDF collider needs a grid with gradients";
+  std::memset(&d, 0, sizeof(d));
+  d.type = c.type;
+  d.scene = c.scene;
+  for (int k = 0; k < 3; ++k) {
+    d.pos[k] = (float)c.pos[k];
+    d.size[k] = (float)c.size[k];
+    d.com[k] = (float)c.com[k];
+    d.lin[k] = (float)c.lin_vel[k];
+    d.ang[k] = (float)c.ang_vel[k];
+  }
+  for (int k = 0; k < 4; ++k) d.quat[k] = (float)c.quat[k];
+  d.friction = (float)c.friction;
+  d.softness = (float)c.softness;
+  d.restitution = (float)c.restitution;
+  if (gridded) {
+    const mpm_ctx::SdfGrid& g = ctx->sdf_grids[(size_t)c.sdf_grid];
+    d.pad0 = c.sdf_grid;
+    d.val = g.val;
+    d.grad = g.grad;
+    for (int k = 0; k < 3; ++k) d.res[k] = g.res[k];
+    for (int k = 0; k < 12; ++k) d.T[k] = (float)g.T[k];
+    // inverse of the 3x3 block (tool normals: voxel frame -> mesh frame), by cofactors in double
+    const double* T = g.T;
+    const double a = T[0], b = T[1], cc = T[2], e = T[4], f = T[5], gg = T[6], h = T[8], i2 = T[9], j = T[10];
+    const double det = a * (f * j - gg * i2) - b * (e * j - gg * h) + cc * (e * i2 - f * h);
+    if (!(std::fabs(det) > 0)) return "T_mesh_to_sdf is singular";
+    const double inv[9] = {(f * j - gg * i2) / det, (cc * i2 - b * j) / det, (b * gg - cc * f) / det,
+                           (gg * h - e * j) / det,  (a * j - cc * h) / det,  (cc * e - a * gg) / det,
+                           (e * i2 - f * h) / det,  (b * h - a * i2) / det,  (a * f - b * e) / det};
+    for (int k = 0; k < 9; ++k) d.Rinv[k] = (float)inv[k];
+    d.cell_size = (float)g.cell_size;
+    d.sdf_max = (float)g.sdf_max;
+    d.floor_h = (float)c.floor_height;
+  }
+  return nullptr;
+}
+
 }  // namespace gbmpm
 
 namespace {
@@ -1120,51 +1166,10 @@ int mpm_set_colliders(mpm_ctx* ctx, int32_t n, const mpm_collider* colliders) {
   std::vector<ColliderDev> h((size_t)n);
   for (int32_t i = 0; i < n; ++i) {
     const mpm_collider& c = colliders[i];
-    if (c.type < MPM_COLLIDER_SPHERE || c.type > MPM_COLLIDER_TOOL)
-      return fail(ctx, MPM_ERR_BAD_ARG, "unknown collider type");
-    const bool gridded = c.type == MPM_COLLIDER_SDF || c.type == MPM_COLLIDER_TOOL;
-    if (gridded && (c.sdf_grid < 0 || c.sdf_grid >= (int32_t)ctx->sdf_grids.size()))
-      return fail(ctx, MPM_ERR_BAD_ARG, "collider SDF grid id out of range (mpm_add_sdf_grid)");
-    if (c.type == MPM_COLLIDER_SDF && !ctx->sdf_grids[(size_t)c.sdf_grid].grad)
-      return fail(ctx, MPM_ERR_BAD_ARG, "an SDF collider needs a grid with gradients");
     if (c.scene < -1 || c.scene >= ctx->n_scenes) return fail(ctx, MPM_ERR_BAD_ARG, "collider scene out of range");
     if (ctx->cpic_slots > 0 && i >= ctx->cpic_slots)
       return fail(ctx, MPM_ERR_BAD_ARG, "more colliders than CPIC slots (mpm_enable_cpic)");
-    ColliderDev& d = h[(size_t)i];
-    std::memset(&d, 0, sizeof(d));
-    d.type = c.type;
-    d.scene = c.scene;
-    for (int k = 0; k < 3; ++k) {
-      d.pos[k] = (float)c.pos[k];
-      d.size[k] = (float)c.size[k];
-      d.com[k] = (float)c.com[k];
-      d.lin[k] = (float)c.lin_vel[k];
-      d.ang[k] = (float)c.ang_vel[k];
-    }
-    for (int k = 0; k < 4; ++k) d.quat[k] = (float)c.quat[k];
-    d.friction = (float)c.friction;
-    d.softness = (float)c.softness;
-    d.restitution = (float)c.restitution;
-    if (gridded) {
-      const mpm_ctx::SdfGrid& g = ctx->sdf_grids[(size_t)c.sdf_grid];
-      d.pad0 = c.sdf_grid;
-      d.val = g.val;
-      d.grad = g.grad;
-      for (int k = 0; k < 3; ++k) d.res[k] = g.res[k];
-      for (int k = 0; k < 12; ++k) d.T[k] = (float)g.T[k];
-      // inverse of the 3x3 block (tool normals: voxel frame -> mesh frame), by cofactors in double
-      const double* T = g.T;
-      const double a = T[0], b = T[1], cc = T[2], e = T[4], f = T[5], gg = T[6], h = T[8], i2 = T[9], j = T[10];
-      const double det = a * (f * j - gg * i2) - b * (e * j - gg * h) + cc * (e * i2 - f * h);
-      if (!(std::fabs(det) > 0)) return fail(ctx, MPM_ERR_BAD_ARG, "T_mesh_to_sdf is singular");
-      const double inv[9] = {(f * j - gg * i2) / det, (cc * i2 - b * j) / det, (b * gg - cc * f) / det,
-                             (gg * h - e * j) / det,  (a * j - cc * h) / det,  (cc * e - a * gg) / det,
-                             (e * i2 - f * h) / det,  (b * h - a * i2) / det,  (a * f - b * e) / det};
-      for (int k = 0; k < 9; ++k) d.Rinv[k] = (float)inv[k];
-      d.cell_size = (float)g.cell_size;
-      d.sdf_max = (float)g.sdf_max;
-      d.floor_h = (float)c.floor_height;
-    }
+    if (const char* e = collider_dev(ctx, c, h[(size_t)i])) return fail(ctx, MPM_ERR_BAD_ARG, e);
   }
   int32_t n_tools = 0;
   for (int32_t i = 0; i < n; ++i) n_tools += colliders[i].type == MPM_COLLIDER_TOOL ? 1 : 0;

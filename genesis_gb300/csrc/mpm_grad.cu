@@ -21,6 +21,7 @@
 
 #include "gbmpm.h"
 #include "mpm_adjoint.cuh"
+#include "mpm_colliders.cuh"
 #include "mpm_force_fields.cuh"
 #include "mpm_kernels.cuh"
 #include "mpm_tool_adjoint.cuh"
@@ -73,6 +74,21 @@ struct DiffFields {
   unsigned long long step;
   ForceFieldDev f[MPM_DIFF_MAX_FORCE_FIELDS];
 };
+
+// Kinematic rigid colliders of the differentiable grid op (legacy_coupler.py:389-403), by value like
+// the fields: poses fixed over the call, applied after the tools; scene -1 or the env index.
+struct DiffColliders {
+  int32_t n, pad0;
+  ColliderDev c[MPM_DIFF_MAX_COLLIDERS];
+};
+
+// The influence of collider c at x (normal in n), or 0 when the node is outside its reach
+// (_func_collide_with_rigid: exp(-sd / softness) capped at 1, acting above 0.1).
+__device__ __forceinline__ float dcollider_influence(const ColliderDev& c, const float* x, float eps, float* n) {
+  const float sd = collider_sdf(c, x, eps, n);
+  const float influence = fminf(expf(-sd / fmaxf(1e-10f, c.softness)), 1.f);
+  return influence > 0.1f ? influence : 0.f;
+}
 
 __device__ __forceinline__ int64_t didx(const SceneDev& S, int gx, int gy, int gz) {
   return ((int64_t)gx * S.res[1] + gy) * S.res[2] + gz;
@@ -265,7 +281,7 @@ __device__ __forceinline__ void dfield_apply(const DiffFields& FF, int f, const 
   for (int k = 0; k < 3; ++k) v[k] += a[k] * S.dt;
 }
 
-__global__ void k_dgrid(DiffParams Q, int64_t nodes, const DiffFields FF) {
+__global__ void k_dgrid(DiffParams Q, int64_t nodes, const DiffFields FF, const DiffColliders CC) {
   const SceneDev& S = Q.S;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nodes; i += (int64_t)gridDim.x * blockDim.x) {
     const float4 q = Q.pm[i];
@@ -276,7 +292,7 @@ __global__ void k_dgrid(DiffParams Q, int64_t nodes, const DiffFields FF) {
       v[0] = inv * q.x + S.dt * S.grav[0];
       v[1] = inv * q.y + S.dt * S.grav[1];
       v[2] = inv * q.z + S.dt * S.grav[2];
-      if (Q.n_tools > 0 || FF.n > 0) {
+      if (Q.n_tools > 0 || FF.n > 0 || CC.n > 0) {
         float x[3];
         node_world_pos(S, g, x);
         for (int f = 0; f < FF.n; ++f)  // force fields after gravity, before the tools
@@ -284,6 +300,13 @@ __global__ void k_dgrid(DiffParams Q, int64_t nodes, const DiffFields FF) {
         for (int t = 0; t < Q.n_tools; ++t) {
           const float* st = Q.tool_f + t * 13;
           tool_collide_t<float>(Q.tools[t], x, v, st, st + 3, st + 7, Q.tool_f1 + t * 13 + 3, S.dt, S.eps);
+        }
+        for (int ci = 0; ci < CC.n; ++ci) {  // rigid colliders after the tools (legacy_coupler.py:386-403)
+          const ColliderDev& c = CC.c[ci];
+          if (c.scene >= 0 && c.scene != FF.scene) continue;
+          float n[3];
+          const float infl = dcollider_influence(c, x, S.eps, n);
+          if (infl > 0.f) collide_in_velocity(c, S.eps, x, v, n, infl);
         }
       }
       for (int d = 0; d < 3; ++d) {
@@ -394,7 +417,7 @@ __global__ void __launch_bounds__(256) k_dg2p_adj(DiffParams Q) {
 }
 
 // grid-op adjoint: v = B(T(F(p/m + dt g))) (force fields F, tools T, boundary B) -> dL/dp, dL/dm
-__global__ void k_dgrid_adj(DiffParams Q, int64_t nodes, const DiffFields FF) {
+__global__ void k_dgrid_adj(DiffParams Q, int64_t nodes, const DiffFields FF, const DiffColliders CC) {
   const SceneDev& S = Q.S;
   const int lane = threadIdx.x & 31;
   for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x; i0 < nodes; i0 += (int64_t)gridDim.x * blockDim.x) {
@@ -410,7 +433,7 @@ __global__ void k_dgrid_adj(DiffParams Q, int64_t nodes, const DiffFields FF) {
       const float inv = 1.f / q.w;
       float u[3] = {inv * q.x + S.dt * S.grav[0], inv * q.y + S.dt * S.grav[1], inv * q.z + S.dt * S.grav[2]};
       float gu[3] = {gv.x, gv.y, gv.z};
-      float vin[MPM_DIFF_MAX_TOOLS][3], fin[MPM_DIFF_MAX_FORCE_FIELDS][3];
+      float vin[MPM_DIFF_MAX_TOOLS][3], fin[MPM_DIFF_MAX_FORCE_FIELDS][3], cin[MPM_DIFF_MAX_COLLIDERS][3];
       float x[3];
       node_world_pos(S, g, x);
       for (int f = 0; f < FF.n; ++f) {  // forward through the force fields, keeping each one's input
@@ -422,9 +445,24 @@ __global__ void k_dgrid_adj(DiffParams Q, int64_t nodes, const DiffFields FF) {
         const float* st = Q.tool_f + t * 13;
         tool_collide_t<float>(Q.tools[t], x, u, st, st + 3, st + 7, Q.tool_f1 + t * 13 + 3, S.dt, S.eps);
       }
-      for (int d = 0; d < 3; ++d) {  // the boundary acts on the velocity the tools left
+      for (int ci = 0; ci < CC.n; ++ci) {  // forward through the rigid colliders, keeping each one's input
+        for (int k = 0; k < 3; ++k) cin[ci][k] = u[k];
+        const ColliderDev& c = CC.c[ci];
+        if (c.scene >= 0 && c.scene != FF.scene) continue;
+        float n[3];
+        const float infl = dcollider_influence(c, x, S.eps, n);
+        if (infl > 0.f) collide_in_velocity(c, S.eps, x, u, n, infl);
+      }
+      for (int d = 0; d < 3; ++d) {  // the boundary acts on the velocity the tools and colliders left
         const float p = (float)(g[d] + S.offset[d]) * S.dx;
         if ((p >= S.hi[d] && u[d] >= 0.f) || (p <= S.lo[d] && u[d] <= 0.f)) gu[d] = 0.f;
+      }
+      for (int ci = CC.n - 1; ci >= 0; --ci) {  // back through the rigid colliders
+        const ColliderDev& c = CC.c[ci];
+        if (c.scene >= 0 && c.scene != FF.scene) continue;
+        float n[3];
+        const float infl = dcollider_influence(c, x, S.eps, n);
+        if (infl > 0.f) collide_in_vjp(c, S.eps, x, cin[ci], n, infl, gu);
       }
       for (int t = Q.n_tools - 1; t >= 0; --t) {  // back through the tools: Jacobians from dual numbers
         const float* st = Q.tool_f + t * 13;
@@ -733,6 +771,7 @@ using namespace gbmpm;
 namespace {
 
 const DiffFields kNoFields{};
+const DiffColliders kNoColliders{};
 
 // Muscle inputs of a call (null members: no actuation stress)
 struct DiffMuscle {
@@ -743,7 +782,7 @@ struct DiffMuscle {
 
 // The fields of substep k of a sequence that starts at the fields' substep counter ff->step.
 const DiffFields* fields_at(const DiffFields* ff, int32_t k, DiffFields& tmp) {
-  if (!ff || ff->n == 0) return nullptr;
+  if (!ff) return nullptr;
   tmp = *ff;
   tmp.step = ff->step + (unsigned long long)k;
   return &tmp;
@@ -755,7 +794,8 @@ int diff_forward(const mpm_scene_config* scene, double rho, int32_t neohookean, 
                  const float* F, const float* Jp, const float* mu, const float* lam, float* x1, float* v1, float* C1,
                  float* F1, float* Jp1, void* grid_pm, void* grid_v, uint32_t* status, void* stream, int n_tools = 0,
                  const DiffToolDev* tools = nullptr, const float* tool_f = nullptr, float* tool_f1 = nullptr,
-                 const DiffFields* ff = nullptr, const DiffMuscle* mus = nullptr) {
+                 const DiffFields* ff = nullptr, const DiffMuscle* mus = nullptr,
+                 const DiffColliders* cc = nullptr) {
   if (!scene || n < 0 || !grid_pm || !grid_v || !status) return MPM_ERR_BAD_ARG;
   DiffParams Q;
   std::memset(&Q, 0, sizeof(Q));
@@ -786,7 +826,7 @@ int diff_forward(const mpm_scene_config* scene, double rho, int32_t neohookean, 
   k_dclear<<<gb, 256, 0, s>>>(Q, nodes, Q.pm);
   if (n > 0) k_dp2g<<<pb, 256, 0, s>>>(Q);
   if (n_tools > 0) k_dtool_advance<<<1, 32, 0, s>>>(Q);
-  k_dgrid<<<gb, 256, 0, s>>>(Q, nodes, ff ? *ff : kNoFields);
+  k_dgrid<<<gb, 256, 0, s>>>(Q, nodes, ff ? *ff : kNoFields, cc ? *cc : kNoColliders);
   if (n > 0) k_dg2p<<<pb, 256, 0, s>>>(Q);
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_ERR_CUDA;
 }
@@ -798,7 +838,8 @@ int diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean,
                   float* gC, float* gF, float* gJp, float* gmu, float* glam, void* grid_pm, void* grid_v,
                   void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream, int n_tools = 0,
                   const DiffToolDev* tools = nullptr, const float* tool_f = nullptr, const float* tool_f1 = nullptr,
-                  float* g_tool = nullptr, const DiffFields* ff = nullptr, const DiffMuscle* mus = nullptr) {
+                  float* g_tool = nullptr, const DiffFields* ff = nullptr, const DiffMuscle* mus = nullptr,
+                  const DiffColliders* cc = nullptr) {
   if (!scene || n < 0 || !grid_pm || !grid_v || !g_grid_v || !g_grid_pm) return MPM_ERR_BAD_ARG;
   DiffParams Q;
   std::memset(&Q, 0, sizeof(Q));
@@ -832,7 +873,7 @@ int diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean,
   const int pb = (int)((n + 255) / 256 < 8192 ? (n + 255) / 256 : 8192);
   k_dclear<<<gb, 256, 0, s>>>(Q, nodes, Q.g_grid_v);
   if (n > 0) k_dg2p_adj<<<pb, 256, 0, s>>>(Q);
-  k_dgrid_adj<<<gb, 256, 0, s>>>(Q, nodes, ff ? *ff : kNoFields);
+  k_dgrid_adj<<<gb, 256, 0, s>>>(Q, nodes, ff ? *ff : kNoFields, cc ? *cc : kNoColliders);
   if (n_tools > 0) k_dtool_adj<<<1, 32, 0, s>>>(Q);
   if (n > 0) k_dp2g_adj<<<pb, 256, 0, s>>>(Q);
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_ERR_CUDA;
@@ -843,7 +884,8 @@ int diff_forward_seq(const mpm_scene_config* scene, double rho, int32_t neohooke
                      float* C_seq, float* F_seq, float* Jp_seq, int32_t ring, const float* mu, const float* lam,
                      void* grid_pm, void* grid_v, int32_t grids_per_substep, uint32_t* status, void* stream,
                      int n_tools = 0, const DiffToolDev* tools = nullptr, float* tool_seq = nullptr,
-                     const DiffFields* ff = nullptr, const DiffMuscle* mus = nullptr) {
+                     const DiffFields* ff = nullptr, const DiffMuscle* mus = nullptr,
+                     const DiffColliders* cc = nullptr) {
   if (!scene || n < 0 || n_sub < 0 || ring < 2 || !x_seq || !v_seq || !C_seq || !F_seq) return MPM_ERR_BAD_ARG;
   DiffFields tmp;
   SceneDev S;
@@ -859,7 +901,7 @@ int diff_forward_seq(const mpm_scene_config* scene, double rho, int32_t neohooke
                                Jp_seq ? Jp_seq + b * n : nullptr, (float4*)grid_pm + go, (float4*)grid_v + go, status,
                                stream, n_tools, tools, tool_seq ? tool_seq + (int64_t)k * n_tools * 13 : nullptr,
                                tool_seq ? tool_seq + (int64_t)(k + 1) * n_tools * 13 : nullptr,
-                               fields_at(ff, k, tmp), mus);
+                               fields_at(ff, k, tmp), mus, cc);
     if (r) return r;
   }
   return MPM_OK;
@@ -872,7 +914,8 @@ int diff_backward_seq(const mpm_scene_config* scene, double rho, int32_t neohook
                       const float* lam, float* g_seq, float* gmu, float* glam, void* grid_pm, void* grid_v,
                       void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream, int n_tools = 0,
                       const DiffToolDev* tools = nullptr, const float* tool_seq = nullptr, float* g_tool = nullptr,
-                      const DiffFields* ff = nullptr, const DiffMuscle* mus = nullptr) {
+                      const DiffFields* ff = nullptr, const DiffMuscle* mus = nullptr,
+                      const DiffColliders* cc = nullptr) {
   if (!scene || n < 0 || n_sub < 0 || !g_seq) return MPM_ERR_BAD_ARG;
   DiffFields tmp;
   if (n_tools > 0) {
@@ -899,7 +942,7 @@ int diff_backward_seq(const mpm_scene_config* scene, double rho, int32_t neohook
                                 (float4*)grid_v + (int64_t)k * nodes, g_grid_v, g_grid_pm, status, stream, n_tools,
                                 tools, tool_seq ? tool_seq + (int64_t)k * n_tools * 13 : nullptr,
                                 tool_seq ? tool_seq + (int64_t)(k + 1) * n_tools * 13 : nullptr, g_tool,
-                                fields_at(ff, k, tmp), mus);
+                                fields_at(ff, k, tmp), mus, cc);
     if (r) return r;
     cur = 1 - cur;
   }
@@ -950,8 +993,9 @@ int diff_fields(const mpm_force_field* fields, int32_t n, int32_t scene_index, u
 }
 
 // The extras of a sequence (tools, force fields, Muscle inputs) as the internal calls take them.
-int diff_extras(const mpm_diff_extras* ex, DiffToolDev* td, DiffFields& ff, DiffMuscle& mus) {
+int diff_extras(const mpm_diff_extras* ex, DiffToolDev* td, DiffFields& ff, DiffMuscle& mus, DiffColliders& cc) {
   std::memset(&mus, 0, sizeof(mus));
+  std::memset(&cc, 0, sizeof(cc));
   if (!ex) return diff_fields(nullptr, 0, 0, 0, ff);
   int r = diff_tools_dev(ex->tools, ex->n_tools, ex->tool_seq, td);
   if (r) return r;
@@ -960,6 +1004,14 @@ int diff_extras(const mpm_diff_extras* ex, DiffToolDev* td, DiffFields& ff, Diff
   mus.actu = ex->actu;
   mus.mdir = ex->muscle_dir;
   mus.g_actu = ex->g_actu;
+  if (ex->n_colliders < 0 || ex->n_colliders > MPM_DIFF_MAX_COLLIDERS || (ex->n_colliders > 0 && !ex->colliders))
+    return MPM_ERR_BAD_ARG;
+  cc.n = ex->n_colliders;
+  for (int32_t i = 0; i < cc.n; ++i) {
+    const mpm_collider& c = ex->colliders[i];
+    if (c.type == MPM_COLLIDER_TOOL || c.scene < -1) return MPM_ERR_BAD_ARG;  // tools: the tool records
+    if (collider_dev(ex->sdf_ctx, c, cc.c[i])) return MPM_ERR_BAD_ARG;
+  }
   return MPM_OK;
 }
 
@@ -1050,12 +1102,13 @@ int mpm_diff_forward_seq_ex(const mpm_scene_config* scene, const float* mass, co
   DiffToolDev td[MPM_DIFF_MAX_TOOLS];
   DiffFields ff;
   DiffMuscle mus;
-  const int r = diff_extras(ex, td, ff, mus);
+  DiffColliders cc;
+  const int r = diff_extras(ex, td, ff, mus, cc);
   if (r) return r;
   const int nt = ex ? ex->n_tools : 0;
   return diff_forward_seq(scene, 0.0, 0, mass, kind, aux, n, n_sub, x_seq, v_seq, C_seq, F_seq, Jp_seq, ring, mu, lam,
                           grid_pm, grid_v, grids_per_substep, status, stream, nt, td, ex ? ex->tool_seq : nullptr, &ff,
-                          &mus);
+                          &mus, &cc);
 }
 
 int mpm_diff_backward_seq_ex(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
@@ -1067,13 +1120,14 @@ int mpm_diff_backward_seq_ex(const mpm_scene_config* scene, const float* mass, c
   DiffToolDev td[MPM_DIFF_MAX_TOOLS];
   DiffFields ff;
   DiffMuscle mus;
-  const int r = diff_extras(ex, td, ff, mus);
+  DiffColliders cc;
+  const int r = diff_extras(ex, td, ff, mus, cc);
   if (r) return r;
   const int nt = ex ? ex->n_tools : 0;
   if (nt > 0 && !ex->g_tool) return MPM_ERR_BAD_ARG;
   return diff_backward_seq(scene, 0.0, 0, mass, kind, aux, n, n_sub, x_seq, v_seq, C_seq, F_seq, Jp_seq, mu, lam,
                            g_seq, gmu, glam, grid_pm, grid_v, g_grid_v, g_grid_pm, status, stream, nt, td,
-                           ex ? ex->tool_seq : nullptr, ex ? ex->g_tool : nullptr, &ff, &mus);
+                           ex ? ex->tool_seq : nullptr, ex ? ex->g_tool : nullptr, &ff, &mus, &cc);
 }
 
 int mpm_diff_forward_seq_tools(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,

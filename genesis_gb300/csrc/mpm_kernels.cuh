@@ -109,6 +109,8 @@ struct ForceFieldDev {
 };
 // The device record of an ABI force field (float copies); false for an unknown type.
 bool force_field_dev(const mpm_force_field& f, ForceFieldDev& d);
+// The device record of an ABI collider (float copies, SDF grids from ctx); null, or the problem.
+const char* collider_dev(const mpm_ctx* ctx, const mpm_collider& c, ColliderDev& d);
 
 // Another solver's particles coupled through the grid op (SPH or PBD), caller-owned device arrays.
 struct ExtSetDev {

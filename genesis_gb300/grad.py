@@ -26,7 +26,8 @@ holds every tool's position and velocity ([n_tools, 6], differentiated through M
 grid op and ToolEntity.advect) and, as
 plain tensors, its orientation and angular velocity.  Built-in force fields act in the
 differentiable grid op (mpm_diff_forward_seq_ex / mpm_diff_backward_seq_ex), each step with the
-fields as they were when it ran.  As in the reference, CPIC and emitters are rejected in this mode;
+fields as they were when it ran, and so do kinematic rigid colliders (solver.set_colliders: the
+shapes of the product grid op, poses fixed within a step, no reaction forces in this mode).  As in the reference, CPIC and emitters are rejected in this mode;
 Custom force fields (a torch function here) are too.
 """
 
@@ -151,6 +152,7 @@ class SceneDiffEngine:
             if ents else torch.zeros(0, device=dev)
         self._init_tools(solver)
         self.set_force_fields(getattr(solver, "_ffs", []))
+        self.set_colliders([])
         self.states = [(x0.clone(), torch.zeros((n, 3), device=dev), torch.zeros((n, 3, 3), device=dev),
                         eye.repeat(n, 1, 1), self.Jp0.clone(), self.T0.clone(), torch.zeros(n, device=dev))
                        for _ in range(B)]
@@ -202,9 +204,17 @@ class SceneDiffEngine:
         self.n_ffs = len(ffs)
         self.ff_base = getattr(self, "substeps_taken", 0)
 
+    def set_colliders(self, recs) -> None:
+        """The user colliders (MpmCollider records) for the following steps."""
+        if len(recs) > _lib.DIFF_MAX_COLLIDERS:
+            raise GenesisException(f"At most {_lib.DIFF_MAX_COLLIDERS} rigid colliders in differentiable mode.")
+        self.col_recs = (_lib.MpmCollider * max(1, len(recs)))(*recs)
+        self.n_col = len(recs)
+
     def _fields(self, b: int):
-        """(records, count, env, substep counter) of the force fields for a step of env b starting now."""
-        return (self.ff_recs, self.n_ffs, b, self.substeps_taken - self.ff_base)
+        """The grid op's inputs for a step of env b starting now: force-field records and count, env,
+        the fields' substep counter, collider records and count."""
+        return (self.ff_recs, self.n_ffs, b, self.substeps_taken - self.ff_base, self.col_recs, self.n_col)
 
     def _tool_seq(self, n_sub, T, qa):
         """[(n_sub + 1), n_tools, 13] tool states, entry 0 from (pos, vel) T and (quat, ang) qa."""
@@ -235,7 +245,7 @@ class SceneDiffEngine:
     def _extras(self, tool_seq, fields, actu, g_tool=None, g_actu=None):
         """The mpm_diff_extras record of one call (the arrays stay referenced by the caller)."""
         nt = len(self.tools)
-        recs, nf, env, ff_step = fields
+        recs, nf, env, ff_step, col_recs, n_col = fields
         ex = _lib.MpmDiffExtras()
         ex.tools = ctypes.addressof(self.tool_recs)
         ex.n_tools = nt
@@ -245,6 +255,9 @@ class SceneDiffEngine:
         ex.n_force_fields = nf
         ex.scene_index = env
         ex.ff_step = ff_step
+        ex.colliders = ctypes.addressof(col_recs)
+        ex.n_colliders = n_col
+        ex.sdf_ctx = self.solver._ctx
         if self.has_muscle:
             ex.actu = actu.data_ptr()
             ex.muscle_dir = self.mdir.data_ptr()
@@ -408,12 +421,13 @@ class SceneDiffEngine:
                 keep.append((seq, gpm, gv, tseq, fields[b], inputs[b][6]))
             self._seg = (s_i, keep)
         for b in range(self.B):
-            seq, gpm, gv, tseq, (recs, nf, env, ff_step), actu = self._seg[1][b]
+            seq, gpm, gv, tseq, (recs, nf, env, ff_step, col_recs, n_col), actu = self._seg[1][b]
             gp = self._pack(self.adj[b][:5])
             g_tool = self._g_tool(self.adj[b][5])
             g_actu = self.adj[b][6]  # the step's actuation adjoint gathers every substep's share
             self._backward_seq([t[k: k + 1].contiguous() for t in seq], 1, gp, gpm[k], gv[k],
-                               tseq[k: k + 2].contiguous(), g_tool, (recs, nf, env, ff_step + k), actu, g_actu)
+                               tseq[k: k + 2].contiguous(), g_tool, (recs, nf, env, ff_step + k, col_recs, n_col),
+                               actu, g_actu)
             self.adj[b] = [*self._unpack(gp), g_tool[:len(self.tools), :6].clone(), g_actu]
         self.cursor -= 1
 

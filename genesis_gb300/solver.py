@@ -482,8 +482,8 @@ class MPMSolver:
         device once per grid object; tools then move by themselves every substep (see
         get_collider_poses).  The scene's tool entities follow these colliders in the library's
         list and keep their current poses."""
-        if self._diff is not None and list(colliders):
-            raise GenesisException("Rigid colliders are not supported in differentiable mode (tool entities are).")
+        if self._diff is not None and any(c.shape == "tool" for c in colliders):
+            raise GenesisException("Collider shape 'tool' is not supported in differentiable mode; add a tool entity.")
         self._sync_tool_poses()
         self._user_colliders = list(colliders)
         self._upload_colliders()
@@ -541,6 +541,8 @@ class MPMSolver:
             self._cpic_slots = len(recs)
         _lib.check(self._lib.mpm_set_colliders(self._ctx, len(recs), arr), self._ctx, "mpm_set_colliders")
         self._n_colliders = len(recs)
+        if getattr(self, "_diff", None) is not None:  # the differentiable steps take the user colliders
+            self._diff.set_colliders(recs[:len(self._user_colliders)])
 
     # ------------------------------------------------------------------ numpy checkpoints (base_solver.py:63-126)
     def dump_ckpt_to_numpy(self) -> dict:
@@ -666,6 +668,8 @@ class MPMSolver:
     def get_collider_forces(self, reset: bool = True) -> np.ndarray:
         """[n_colliders, 6]: force (xyz) and torque about each collider's com exerted by the
         particles, summed over the substeps since the last reset."""
+        if self._diff is not None:
+            raise GenesisException("Collider reaction forces are not accumulated in differentiable mode.")
         n = getattr(self, "_n_colliders", 0)
         out = np.zeros((max(1, n), 6), dtype=np.float64)
         _lib.check(self._lib.mpm_get_collider_forces(self._ctx, out.ctypes.data, int(reset), _stream_handle()),

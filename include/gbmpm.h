@@ -573,10 +573,17 @@ int mpm_diff_backward_seq_tools(const mpm_scene_config* scene, const float* mass
  *   stiffness * actu * (F m)(F m)^T of muscle.py:46-53, aux[0] = stiffness): actu [n] and
  *   muscle_dir [n][3] device arrays (both or neither; actu constant over the call), and for the
  *   backward g_actu [n], into which dL/dactu is added (mpm_entity.py _set_particles_actu_grad).
+ * - kinematic rigid colliders (legacy_coupler.py:134-218, 284-347, called at :389-403 after the
+ *   tools): host array of n_colliders mpm_collider records (at most MPM_DIFF_MAX_COLLIDERS; no
+ *   MPM_COLLIDER_TOOL: tools go in the tool records), poses fixed over the call; SDF colliders
+ *   name a grid registered with mpm_add_sdf_grid on sdf_ctx (NULL when none is of that type).
+ *   The backward carries dL/dv through each collider's velocity update; poses are constants and no
+ *   reaction force is accumulated.
  * Kinds 7 and 8 are ElastoPlastic (elasto_plastic.py:44-71) with clamped principal stretches
  * (aux = 1 - yield_lower, 1 + yield_higher) and with von Mises yield (aux[0] = yield stress / (2 mu)).
  * The backward needs the same record contents as the forward it reverses. */
 #define MPM_DIFF_MAX_FORCE_FIELDS 8
+#define MPM_DIFF_MAX_COLLIDERS 8
 typedef struct mpm_diff_extras {
   const mpm_diff_tool* tools;
   int32_t n_tools;
@@ -590,6 +597,10 @@ typedef struct mpm_diff_extras {
   const float* actu;
   const float* muscle_dir;
   float* g_actu;
+  const mpm_collider* colliders;
+  const mpm_ctx* sdf_ctx;
+  int32_t n_colliders;
+  int32_t pad1;
 } mpm_diff_extras;
 int mpm_diff_forward_seq_ex(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
                             int64_t n, int32_t n_sub, float* x_seq, float* v_seq, float* C_seq, float* F_seq,

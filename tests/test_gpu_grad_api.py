@@ -12,7 +12,8 @@ require grad, scene.step(), scene.get_state() / entity.get_state(), loss.backwar
   as the per-step input, and (test_reference_scenario_differentiable_push_with_tool) with the
   reference's own inputs: a tool entity's velocity every step.
 * Tool entities in differentiable mode: gradients w.r.t. a tool's start position and velocity
-  against FP64 central differences of the oracle.
+  against FP64 central differences of the oracle; likewise dL/dv0 of a box falling onto kinematic
+  rigid colliders (sphere, tilted moving box, SDF grid).
 * Force fields in differentiable mode: dL/dv0 through seven active built-in fields (Drag, Point,
   Vortex, Turbulence, Noise, Wind, Constant) against FP64 central differences of the oracle running
   the same fields; the forward with fields (two envs, a field switched off mid-run) equals the
@@ -476,15 +477,21 @@ def test_reference_scenario_differentiable_push_with_tool(gs, tmp_path):
 
 
 def test_couplings_outside_the_differentiable_form_raise(gs):
-    """Rigid colliders, SPH / PBD coupling and particle constraints have no differentiable form here:
-    differentiable mode refuses them instead of stepping without them."""
-    from genesis_gb300.coupling import Collider
+    """Tool-shaped colliders (tool entities are the differentiable form), reaction forces, SPH / PBD
+    coupling and particle constraints have no differentiable form here: differentiable mode refuses
+    them instead of stepping without them."""
+    from genesis_gb300.coupling import Collider, SDFGrid
     from genesis_gb300.exceptions import GenesisException
 
     scene, box, _ = _scene(gs)
     solver = scene.sim.mpm_solver
+    knob = SDFGrid.from_function(lambda p: np.linalg.norm(p, axis=-1) - 0.03, (-0.06,) * 3, (0.06,) * 3, 17,
+                                 grads=False)
     with pytest.raises(GenesisException, match="differentiable mode"):
-        solver.set_colliders([Collider("sphere", pos=(0.5, 0.5, 0.1), radius=0.05)])
+        solver.set_colliders([Collider("tool", pos=(0.5, 0.5, 0.1), sdf=knob)])
+    solver.set_colliders([Collider("sphere", pos=(0.5, 0.5, 0.1), radius=0.05)])
+    with pytest.raises(GenesisException, match="differentiable mode"):
+        solver.get_collider_forces()
     p = torch.zeros((4, 3), device="cuda")
     with pytest.raises(GenesisException, match="differentiable mode"):
         solver.set_coupled_particles("sph", pos=p, vel=p.clone(), mass=torch.ones(4, device="cuda"))
@@ -492,3 +499,68 @@ def test_couplings_outside_the_differentiable_form_raise(gs):
         box.set_particle_constraints(np.ones(box.n_particles, bool), 0, 1e3)
     solver.set_colliders([])  # an empty list stays allowed
 
+
+
+def _collider_set():
+    from genesis_gb300.coupling import Collider, SDFGrid
+
+    knob = SDFGrid.from_function(lambda p: np.linalg.norm(p, axis=-1) - 0.03, (-0.06,) * 3, (0.06,) * 3, 25)
+    cols = [
+        Collider("sphere", pos=(0.42, 0.5, 0.10), radius=0.06, coup_friction=0.4, coup_softness=0.002),
+        Collider("box", pos=(0.49, 0.47, 0.13), quat=(np.cos(0.2), np.sin(0.2), 0.0, 0.0),
+                 half_extents=(0.03, 0.05, 0.02), lin_vel=(0.3, 0.0, 0.1), ang_vel=(0.0, 0.0, 2.0),
+                 coup_friction=0.2, coup_restitution=0.2, coup_softness=0.004),
+        Collider("sdf", sdf=knob, pos=(0.40, 0.56, 0.12), coup_friction=0.3, coup_softness=0.003),
+    ]
+    return cols, knob
+
+
+def test_rigid_collider_gradients_match_fp64_central_differences(gs, oracle):
+    """The box falls onto a sphere, a tilted moving box and an SDF-grid geom (legacy_coupler.py:134-218,
+    284-347 in the differentiable grid op): dL/dv0 against FP64 central differences of the oracle
+    with the same colliders (2%); the colliders move the differences by more than 10%, and the
+    forward equals the product path (1e-4 m)."""
+    cols, knob = _collider_set()
+    scene, box, water = _scene(gs, box_z=0.215)
+    scene.sim.mpm_solver.set_colliders(cols)
+    v0 = np.array([0.1, 0.05, -2.0])
+    target = np.array([0.5, 0.5, 0.2])
+    v = torch.tensor(v0, dtype=torch.float32, device="cuda", requires_grad=True)
+    box.set_velocity(v)
+    steps = 4
+    for _ in range(steps):
+        scene.step()
+    pos = box.get_state().pos
+    loss = ((pos[0].mean(0) - torch.tensor(target, dtype=torch.float32, device="cuda")) ** 2).sum()
+    loss.backward()
+    g = v.grad.detach().cpu().numpy().astype(np.float64)
+    sp, bp, _ = _scene(gs, requires_grad=False, box_z=0.215)
+    sp.sim.mpm_solver.set_colliders(cols)
+    bp.set_velocity(torch.tensor(v0, dtype=torch.float32, device="cuda"))
+    for _ in range(steps):
+        sp.step()
+    assert (bp.get_state().pos[0] - pos[0].detach()).abs().max().item() <= 1e-4
+    sp.sim.mpm_solver.destroy()
+    n_sub = steps * scene.substeps
+    ents = [box, water]
+
+    def L(vb, with_colliders=True):
+        oracle.clear_sdf_grids()
+        ids = [oracle.add_sdf_grid(knob.values, knob.grads, knob.T_mesh_to_sdf, knob.cell_size, knob.sdf_max)]
+        oracle.set_colliders([c.to_c(ids[0] if c.sdf is not None else -1) for c in cols] if with_colliders else [])
+        try:
+            return _oracle_com_loss(oracle, scene, ents, vb, target, n_sub)
+        finally:
+            oracle.set_colliders([])
+            oracle.clear_sdf_grids()
+
+    assert abs(loss.item() - L(v0.astype(np.float32).astype(np.float64))) <= 1e-4 * loss.item() + 1e-8
+    eps = 1e-4
+
+    def fd(wc):
+        return np.array([(L(v0 + eps * np.eye(3)[k], wc) - L(v0 - eps * np.eye(3)[k], wc)) / (2 * eps)
+                         for k in range(3)])
+
+    fd_c, fd_free = fd(True), fd(False)
+    assert np.linalg.norm(fd_c - fd_free) > 0.1 * np.linalg.norm(fd_c), (fd_c, fd_free)
+    assert np.linalg.norm(g - fd_c) <= GRAD_RTOL * np.linalg.norm(fd_c), (g, fd_c)

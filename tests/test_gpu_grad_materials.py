@@ -159,3 +159,40 @@ def test_muscle_and_elastoplastic_forward_equals_product_path(gs):
     b = ep.get_state().solvers_state[0].pos
     assert (a - b).abs().max().item() <= 1e-4
     ep.sim.mpm_solver.destroy()
+
+
+def test_solver_protocol_walk_delivers_actuation_gradients(gs):
+    """The reference's imperative walk (reset_grad, add_grad_from_state, substep_post_coupling_grad /
+    substep_pre_coupling_grad per substep, process_input_grad per step) gives the actuation tensor
+    the same gradient as loss.backward()."""
+    steps = 3
+
+    def run(imperative):
+        scene, worm, _, _ = _muscle_scene(gs, True)
+        a = torch.tensor([0.25, -0.15], device="cuda", requires_grad=True)
+        for _ in range(steps):
+            worm.set_actuation(a)
+            scene.step()
+        solver = scene.sim.mpm_solver
+        st = solver.get_state()
+        W = torch.linspace(-1.0, 1.0, st.pos[0].numel(), device="cuda").reshape(st.pos[0].shape)
+        if not imperative:
+            (st.pos[0] * W).sum().backward()
+            return a.grad.clone()
+        leaf = type(st)(1, solver.n_particles, "cuda")
+        for k in ("pos", "vel", "C", "F"):
+            setattr(leaf, k, getattr(st, k).detach().clone().requires_grad_(True))
+        (leaf.pos[0] * W).sum().backward()
+        solver.reset_grad()
+        solver.add_grad_from_state(leaf)
+        for _ in range(steps):
+            for f in range(scene.substeps - 1, -1, -1):
+                solver.substep_post_coupling_grad(f)
+                solver.substep_pre_coupling_grad(f)
+            solver.process_input_grad()
+        return a.grad.clone()
+
+    g_auto = run(False)
+    g_walk = run(True)
+    assert g_auto.abs().min().item() > 0
+    assert torch.allclose(g_auto, g_walk, rtol=1e-4, atol=1e-7), (g_auto, g_walk)
