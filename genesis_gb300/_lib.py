@@ -161,6 +161,8 @@ class MpmDiffExtras(ctypes.Structure):
         ("sdf_ctx", c_void_p),
         ("n_colliders", c_int32),
         ("pad1", c_int32),
+        ("constraint_stiffness", c_void_p),
+        ("constraint_target", c_void_p),
     ]
 
 

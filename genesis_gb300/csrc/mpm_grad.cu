@@ -64,7 +64,22 @@ struct DiffParams {
   const float* actu;
   const float* mdir;
   float* g_actu;
+  // particle constraints (apply_particle_constraints, mpm_solver.py:1099-1128, after G2P):
+  // stiffness [n] (0: none) and target [n][3], fixed over the substeps of a call; null: none
+  const float* con_k;
+  const float* con_t;
 };
+
+// The critically damped spring of a constrained particle of real mass m: v' = a v + b x + c with
+// a = 1 - dt 2 sqrt(k m) / m, b = -dt k / m (the reference's dv = dt (-k (x - t) - 2 sqrt(k m) v) / m).
+__device__ __forceinline__ void constraint_apply(float k, float m, float dt, const float* t, const float* x,
+                                                 float* v) {
+  const float damp = 2.f * sqrtf(k * m);
+  for (int d = 0; d < 3; ++d) {
+    const float f = -k * (x[d] - t[d]) - damp * v[d];
+    v[d] = v[d] + dt * f / m;
+  }
+}
 
 // Force fields of the differentiable grid op (legacy_coupler.py:381-383), passed by value to the
 // two grid kernels only: scene index and substep counter of the noise draws, then the fields in
@@ -338,13 +353,19 @@ __global__ void __launch_bounds__(256) k_dg2p(DiffParams Q) {
             for (int c = 0; c < 3; ++c) Cn[r * 3 + c] += 4.f * S.inv_dx * wt * gv[r] * dp[c];
           }
         }
+    float x1[3], v1[3];
     for (int d = 0; d < 3; ++d) {
       const float xn = x[d] + S.dt * v[d];
       float vd = v[d];
       if ((xn >= S.hi[d] && vd >= 0.f) || (xn <= S.lo[d] && vd <= 0.f)) vd = 0.f;
-      Q.x1[i * 3 + d] = fmaxf(fminf(xn, S.hi[d]), S.lo[d]);
-      Q.v1[i * 3 + d] = vd;
+      x1[d] = fmaxf(fminf(xn, S.hi[d]), S.lo[d]);
+      v1[d] = vd;
       if (!isfinite(xn)) atomicOr(Q.status, 1u);
+    }
+    if (Q.con_k && Q.con_k[i] > 0.f) constraint_apply(Q.con_k[i], p_mass(Q, i) / 1e3f, S.dt, Q.con_t + i * 3, x1, v1);
+    for (int d = 0; d < 3; ++d) {
+      Q.x1[i * 3 + d] = x1[d];
+      Q.v1[i * 3 + d] = v1[d];
     }
     for (int k = 0; k < 9; ++k) Q.C1[i * 9 + k] = Cn[k];
   }
@@ -374,13 +395,26 @@ __global__ void __launch_bounds__(256) k_dg2p_adj(DiffParams Q) {
           v[1] += wt * g.y;
           v[2] += wt * g.z;
         }
+    float gx1[3], gv1[3];
+    for (int d = 0; d < 3; ++d) {
+      gx1[d] = Q.gx1[i * 3 + d];
+      gv1[d] = Q.gv1[i * 3 + d];
+    }
+    if (Q.con_k && Q.con_k[i] > 0.f) {  // back through the constraint spring: v' = a v + b x + c
+      const float k = Q.con_k[i], m = p_mass(Q, i) / 1e3f;
+      const float a = 1.f - S.dt * 2.f * sqrtf(k * m) / m, b = -S.dt * k / m;
+      for (int d = 0; d < 3; ++d) {
+        gx1[d] += b * gv1[d];
+        gv1[d] *= a;
+      }
+    }
     float gxn[3], gvv[3], gx[3];
     for (int d = 0; d < 3; ++d) {
       const float xn = x[d] + S.dt * v[d];
       const bool zero_v = (xn >= S.hi[d] && v[d] >= 0.f) || (xn <= S.lo[d] && v[d] <= 0.f);
       const bool inside = xn > S.lo[d] && xn < S.hi[d];
-      gxn[d] = inside ? Q.gx1[i * 3 + d] : 0.f;
-      gvv[d] = (zero_v ? 0.f : Q.gv1[i * 3 + d]) + S.dt * gxn[d];
+      gxn[d] = inside ? gx1[d] : 0.f;
+      gvv[d] = (zero_v ? 0.f : gv1[d]) + S.dt * gxn[d];
       gx[d] = gxn[d];
     }
     float gC[9];
@@ -773,11 +807,14 @@ namespace {
 const DiffFields kNoFields{};
 const DiffColliders kNoColliders{};
 
-// Muscle inputs of a call (null members: no actuation stress)
+// Per-particle inputs of a call: Muscle actuation (null: no actuation stress) and particle
+// constraints (null: none)
 struct DiffMuscle {
   const float* actu;
   const float* mdir;
   float* g_actu;
+  const float* con_k;
+  const float* con_t;
 };
 
 // The fields of substep k of a sequence that starts at the fields' substep counter ff->step.
@@ -819,6 +856,7 @@ int diff_forward(const mpm_scene_config* scene, double rho, int32_t neohookean, 
   Q.tool_f = tool_f;
   Q.tool_f1 = tool_f1;
   if (mus && mus->actu && mus->mdir) Q.actu = mus->actu, Q.mdir = mus->mdir;
+  if (mus && mus->con_k && mus->con_t) Q.con_k = mus->con_k, Q.con_t = mus->con_t;
   const int64_t nodes = (int64_t)Q.S.res[0] * Q.S.res[1] * Q.S.res[2];
   cudaStream_t s = (cudaStream_t)stream;
   const int gb = (int)((nodes + 255) / 256 < 8192 ? (nodes + 255) / 256 : 8192);
@@ -867,6 +905,7 @@ int diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean,
   Q.tool_f1 = const_cast<float*>(tool_f1);
   Q.g_tool = g_tool;
   if (mus && mus->actu && mus->mdir) Q.actu = mus->actu, Q.mdir = mus->mdir, Q.g_actu = mus->g_actu;
+  if (mus && mus->con_k && mus->con_t) Q.con_k = mus->con_k, Q.con_t = mus->con_t;
   const int64_t nodes = (int64_t)Q.S.res[0] * Q.S.res[1] * Q.S.res[2];
   cudaStream_t s = (cudaStream_t)stream;
   const int gb = (int)((nodes + 255) / 256 < 8192 ? (nodes + 255) / 256 : 8192);
@@ -1004,6 +1043,9 @@ int diff_extras(const mpm_diff_extras* ex, DiffToolDev* td, DiffFields& ff, Diff
   mus.actu = ex->actu;
   mus.mdir = ex->muscle_dir;
   mus.g_actu = ex->g_actu;
+  if ((ex->constraint_stiffness == nullptr) != (ex->constraint_target == nullptr)) return MPM_ERR_BAD_ARG;
+  mus.con_k = ex->constraint_stiffness;
+  mus.con_t = ex->constraint_target;
   if (ex->n_colliders < 0 || ex->n_colliders > MPM_DIFF_MAX_COLLIDERS || (ex->n_colliders > 0 && !ex->colliders))
     return MPM_ERR_BAD_ARG;
   cc.n = ex->n_colliders;

@@ -82,10 +82,10 @@ class MPMEntity:
         pose from MPMSolver.set_link_poses) with a critically damped spring of `stiffness`."""
         if not isinstance(link_idx, int):
             raise GenesisException("link_idx must be an integer.")
-        if self._solver._diff is not None:
-            raise GenesisException("Particle constraints are not supported in differentiable mode.")
         lp, lq = self._solver.get_link_pose(link_idx)
         m = self._mask(particles_mask)
+        if self._solver._diff is not None:  # differentiable mode: the springs act in the torch state
+            self._solver._diff.set_constraints(self._particle_start, m, link_idx, float(stiffness))
         pos = torch.as_tensor(np.array(lp, dtype=np.float32), device="cuda")
         quat = torch.as_tensor(np.array(lq, dtype=np.float32), device="cuda")
         lib = self._solver._lib
@@ -98,6 +98,8 @@ class MPMEntity:
     def remove_particle_constraints(self, particles_mask=None):
         """mpm_entity.py:674-690: remove the constraints of the masked particles (all if None)."""
         m = self._mask(particles_mask)
+        if self._solver._diff is not None:
+            self._solver._diff.remove_constraints(self._particle_start, m)
         lib = self._solver._lib
         _lib.check(lib.mpm_remove_particle_constraints(self._solver._ctx, 0, self._solver._B, self._particle_start,
                                                        self._n_particles, m.data_ptr(), _stream_ptr()),

@@ -27,7 +27,9 @@ grid op and ToolEntity.advect) and, as
 plain tensors, its orientation and angular velocity.  Built-in force fields act in the
 differentiable grid op (mpm_diff_forward_seq_ex / mpm_diff_backward_seq_ex), each step with the
 fields as they were when it ran, and so do kinematic rigid colliders (solver.set_colliders: the
-shapes of the product grid op, poses fixed within a step, no reaction forces in this mode).  As in the reference, CPIC and emitters are rejected in this mode;
+shapes of the product grid op, poses fixed within a step, no reaction forces in this mode) and
+particle constraints (entity.set_particle_constraints: springs towards targets that follow the
+links' poses of solver.set_link_poses, differentiated in the particle state).  As in the reference, CPIC and emitters are rejected in this mode;
 Custom force fields (a torch function here) are too.
 """
 
@@ -153,6 +155,10 @@ class SceneDiffEngine:
         self._init_tools(solver)
         self.set_force_fields(getattr(solver, "_ffs", []))
         self.set_colliders([])
+        self.con_k = [torch.zeros(n, device="cuda") for _ in range(B)]   # constraint stiffness (0: none)
+        self.con_link = [torch.full((n,), -1, dtype=torch.long, device="cuda") for _ in range(B)]
+        self.con_local = [torch.zeros((n, 3), device="cuda") for _ in range(B)]
+        self.has_con = False
         self.states = [(x0.clone(), torch.zeros((n, 3), device=dev), torch.zeros((n, 3, 3), device=dev),
                         eye.repeat(n, 1, 1), self.Jp0.clone(), self.T0.clone(), torch.zeros(n, device=dev))
                        for _ in range(B)]
@@ -211,10 +217,57 @@ class SceneDiffEngine:
         self.col_recs = (_lib.MpmCollider * max(1, len(recs)))(*recs)
         self.n_col = len(recs)
 
+    # ---------------------------------------------------------------- particle constraints
+    @staticmethod
+    def _rotate(q, v):
+        """Rotate v [n, 3] by unit quaternions q [n, 4] (w, x, y, z)."""
+        w, u = q[:, :1], q[:, 1:]
+        t = 2.0 * torch.cross(u, v, dim=1)
+        return v + w * t + torch.cross(u, t, dim=1)
+
+    def set_constraints(self, start: int, mask, link: int, stiffness: float) -> None:
+        """Attach the masked particles ([B, count] over rows [start, start+count)) to link `link` at
+        their current positions (_kernel_set_particle_constraints: the link-frame offset from the
+        link's pose now)."""
+        lp, lq = self.solver.get_link_pose(link)
+        for b in range(self.B):
+            rows = torch.nonzero(mask[b].to(torch.bool)).reshape(-1) + start
+            if rows.numel() == 0:
+                continue
+            x = self.states[b][0].detach()[rows]
+            p = torch.as_tensor(np.asarray(lp[b], np.float32), device="cuda")
+            q = torch.as_tensor(np.asarray(lq[b], np.float32), device="cuda")
+            qi = torch.cat([q[:1], -q[1:]]).expand(len(rows), 4)
+            self.con_local[b][rows] = self._rotate(qi, x - p)
+            self.con_link[b][rows] = link
+            self.con_k[b][rows] = float(stiffness)
+        self.has_con = any(bool((k > 0).any()) for k in self.con_k)
+
+    def remove_constraints(self, start: int, mask) -> None:
+        for b in range(self.B):
+            rows = torch.nonzero(mask[b].to(torch.bool)).reshape(-1) + start
+            self.con_k[b][rows] = 0.0
+            self.con_link[b][rows] = -1
+        self.has_con = any(bool((k > 0).any()) for k in self.con_k)
+
+    def _constraint_targets(self, b: int):
+        """(stiffness, targets) of env b for a step starting now (the links' current poses), or None."""
+        if not self.has_con:
+            return None
+        link = self.con_link[b]
+        t = torch.zeros((self.n, 3), device="cuda")
+        on = link >= 0
+        if bool(on.any()):
+            lp = torch.as_tensor(np.asarray(self.solver._link_pos[b], np.float32), device="cuda")
+            lq = torch.as_tensor(np.asarray(self.solver._link_quat[b], np.float32), device="cuda")
+            li = link[on]
+            t[on] = self._rotate(lq[li], self.con_local[b][on]) + lp[li]
+        return self.con_k[b].clone(), t.contiguous()
+
     def _fields(self, b: int):
-        """The grid op's inputs for a step of env b starting now: force-field records and count, env,
-        the fields' substep counter, collider records and count."""
-        return (self.ff_recs, self.n_ffs, b, self.substeps_taken - self.ff_base, self.col_recs, self.n_col)
+        """The grid op's and the particles' inputs for a step of env b starting now."""
+        return {"ff": self.ff_recs, "n_ff": self.n_ffs, "env": b, "ff_step": self.substeps_taken - self.ff_base,
+                "col": self.col_recs, "n_col": self.n_col, "con": self._constraint_targets(b)}
 
     def _tool_seq(self, n_sub, T, qa):
         """[(n_sub + 1), n_tools, 13] tool states, entry 0 from (pos, vel) T and (quat, ang) qa."""
@@ -245,19 +298,21 @@ class SceneDiffEngine:
     def _extras(self, tool_seq, fields, actu, g_tool=None, g_actu=None):
         """The mpm_diff_extras record of one call (the arrays stay referenced by the caller)."""
         nt = len(self.tools)
-        recs, nf, env, ff_step, col_recs, n_col = fields
         ex = _lib.MpmDiffExtras()
         ex.tools = ctypes.addressof(self.tool_recs)
         ex.n_tools = nt
         ex.tool_seq = tool_seq.data_ptr() if nt else None
         ex.g_tool = g_tool.data_ptr() if (nt and g_tool is not None) else None
-        ex.force_fields = ctypes.addressof(recs)
-        ex.n_force_fields = nf
-        ex.scene_index = env
-        ex.ff_step = ff_step
-        ex.colliders = ctypes.addressof(col_recs)
-        ex.n_colliders = n_col
+        ex.force_fields = ctypes.addressof(fields["ff"])
+        ex.n_force_fields = fields["n_ff"]
+        ex.scene_index = fields["env"]
+        ex.ff_step = fields["ff_step"]
+        ex.colliders = ctypes.addressof(fields["col"])
+        ex.n_colliders = fields["n_col"]
         ex.sdf_ctx = self.solver._ctx
+        if fields["con"] is not None:
+            ex.constraint_stiffness = fields["con"][0].data_ptr()
+            ex.constraint_target = fields["con"][1].data_ptr()
         if self.has_muscle:
             ex.actu = actu.data_ptr()
             ex.muscle_dir = self.mdir.data_ptr()
@@ -421,12 +476,12 @@ class SceneDiffEngine:
                 keep.append((seq, gpm, gv, tseq, fields[b], inputs[b][6]))
             self._seg = (s_i, keep)
         for b in range(self.B):
-            seq, gpm, gv, tseq, (recs, nf, env, ff_step, col_recs, n_col), actu = self._seg[1][b]
+            seq, gpm, gv, tseq, fields, actu = self._seg[1][b]
             gp = self._pack(self.adj[b][:5])
             g_tool = self._g_tool(self.adj[b][5])
             g_actu = self.adj[b][6]  # the step's actuation adjoint gathers every substep's share
             self._backward_seq([t[k: k + 1].contiguous() for t in seq], 1, gp, gpm[k], gv[k],
-                               tseq[k: k + 2].contiguous(), g_tool, (recs, nf, env, ff_step + k, col_recs, n_col),
+                               tseq[k: k + 2].contiguous(), g_tool, dict(fields, ff_step=fields["ff_step"] + k),
                                actu, g_actu)
             self.adj[b] = [*self._unpack(gp), g_tool[:len(self.tools), :6].clone(), g_actu]
         self.cursor -= 1

@@ -579,6 +579,10 @@ int mpm_diff_backward_seq_tools(const mpm_scene_config* scene, const float* mass
  *   name a grid registered with mpm_add_sdf_grid on sdf_ctx (NULL when none is of that type).
  *   The backward carries dL/dv through each collider's velocity update; poses are constants and no
  *   reaction force is accumulated.
+ * - particle constraints (apply_particle_constraints, mpm_solver.py:1099-1128, after G2P):
+ *   constraint_stiffness [n] (0: unconstrained) and constraint_target [n][3] device arrays, both or
+ *   neither, fixed over the call (the targets the links' poses give); the backward carries dL/d(x, v)
+ *   through the spring's velocity update.
  * Kinds 7 and 8 are ElastoPlastic (elasto_plastic.py:44-71) with clamped principal stretches
  * (aux = 1 - yield_lower, 1 + yield_higher) and with von Mises yield (aux[0] = yield stress / (2 mu)).
  * The backward needs the same record contents as the forward it reverses. */
@@ -601,6 +605,8 @@ typedef struct mpm_diff_extras {
   const mpm_ctx* sdf_ctx;
   int32_t n_colliders;
   int32_t pad1;
+  const float* constraint_stiffness;
+  const float* constraint_target;
 } mpm_diff_extras;
 int mpm_diff_forward_seq_ex(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
                             int64_t n, int32_t n_sub, float* x_seq, float* v_seq, float* C_seq, float* F_seq,

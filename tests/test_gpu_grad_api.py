@@ -13,7 +13,8 @@ require grad, scene.step(), scene.get_state() / entity.get_state(), loss.backwar
   reference's own inputs: a tool entity's velocity every step.
 * Tool entities in differentiable mode: gradients w.r.t. a tool's start position and velocity
   against FP64 central differences of the oracle; likewise dL/dv0 of a box falling onto kinematic
-  rigid colliders (sphere, tilted moving box, SDF grid).
+  rigid colliders (sphere, tilted moving box, SDF grid), and of a box hung on a moving link by
+  particle constraints.
 * Force fields in differentiable mode: dL/dv0 through seven active built-in fields (Drag, Point,
   Vortex, Turbulence, Noise, Wind, Constant) against FP64 central differences of the oracle running
   the same fields; the forward with fields (two envs, a field switched off mid-run) equals the
@@ -477,9 +478,9 @@ def test_reference_scenario_differentiable_push_with_tool(gs, tmp_path):
 
 
 def test_couplings_outside_the_differentiable_form_raise(gs):
-    """Tool-shaped colliders (tool entities are the differentiable form), reaction forces, SPH / PBD
-    coupling and particle constraints have no differentiable form here: differentiable mode refuses
-    them instead of stepping without them."""
+    """Tool-shaped colliders (tool entities are the differentiable form), reaction forces and SPH /
+    PBD coupling have no differentiable form here: differentiable mode refuses them instead of
+    stepping without them."""
     from genesis_gb300.coupling import Collider, SDFGrid
     from genesis_gb300.exceptions import GenesisException
 
@@ -495,8 +496,6 @@ def test_couplings_outside_the_differentiable_form_raise(gs):
     p = torch.zeros((4, 3), device="cuda")
     with pytest.raises(GenesisException, match="differentiable mode"):
         solver.set_coupled_particles("sph", pos=p, vel=p.clone(), mass=torch.ones(4, device="cuda"))
-    with pytest.raises(GenesisException, match="differentiable mode"):
-        box.set_particle_constraints(np.ones(box.n_particles, bool), 0, 1e3)
     solver.set_colliders([])  # an empty list stays allowed
 
 
@@ -564,3 +563,86 @@ def test_rigid_collider_gradients_match_fp64_central_differences(gs, oracle):
     fd_c, fd_free = fd(True), fd(False)
     assert np.linalg.norm(fd_c - fd_free) > 0.1 * np.linalg.norm(fd_c), (fd_c, fd_free)
     assert np.linalg.norm(g - fd_c) <= GRAD_RTOL * np.linalg.norm(fd_c), (g, fd_c)
+
+
+def _qrot(q, v):
+    w, u = q[0], np.asarray(q[1:])
+    t = 2.0 * np.cross(u, v)
+    return v + w * t + np.cross(u, t)
+
+
+def test_particle_constraint_gradients_match_fp64_central_differences(gs, oracle):
+    """A quarter of the box's particles hang on a link that moves and turns between steps
+    (apply_particle_constraints after G2P, mpm_solver.py:1099-1128): dL/dv0 against FP64 central
+    differences of the oracle's substeps with the same spring applied after each (2%); the springs
+    move the differences by more than 10%, and the forward equals the product path (1e-4 m)."""
+    steps, k = 4, 300.0
+    p0, q0 = np.array([0.45, 0.5, 0.35]), np.array([1.0, 0.0, 0.0, 0.0])
+    poses = [(p0 + np.array([0.01, 0.0, 0.005]) * (s + 1),
+              np.array([np.cos(0.05 * (s + 1)), 0.0, 0.0, np.sin(0.05 * (s + 1))])) for s in range(steps)]
+    v0 = np.array([0.3, -0.2, 0.5])
+    target = np.array([0.47, 0.5, 0.37])
+
+    def run(requires_grad, vel):
+        scene, box, water = _scene(gs, requires_grad=requires_grad)
+        solver = scene.sim.mpm_solver
+        solver.set_link_poses(p0[None], q0[None])
+        mask = np.zeros(box.n_particles, bool)
+        mask[::4] = True
+        box.set_particle_constraints(mask, 0, k)
+        box.set_velocity(vel)
+        for p, q in poses:
+            solver.set_link_poses(p[None], q[None])
+            scene.step()
+        return scene, box, water, mask
+
+    v = torch.tensor(v0, dtype=torch.float32, device="cuda", requires_grad=True)
+    scene, box, water, mask = run(True, v)
+    pos = box.get_state().pos[0]
+    loss = ((pos.mean(0) - torch.tensor(target, dtype=torch.float32, device="cuda")) ** 2).sum()
+    loss.backward()
+    g = v.grad.detach().cpu().numpy().astype(np.float64)
+    sp, bp, _, _ = run(False, torch.tensor(v0, dtype=torch.float32, device="cuda"))
+    assert (bp.get_state().pos[0] - pos.detach()).abs().max().item() <= 1e-4
+    sp.sim.mpm_solver.destroy()
+
+    solver = scene.sim.mpm_solver
+    ents = [box, water]
+    oms = [oracle.from_c_material(m.to_c(0)) for m in solver._unique_materials()]
+    x0 = np.concatenate([e.init_particles.astype(np.float32).astype(np.float64) for e in ents])
+    n, nb = len(x0), box.n_particles
+    sel = np.zeros(n, bool)
+    sel[:nb] = mask
+    local = np.array([_qrot(q0 * np.array([1, -1, -1, -1]), x - p0) for x in x0[sel]])
+    m_real = float(np.float32(np.float32(solver.particle_volume) * np.float32(box.material.rho))) / 1e3
+    sc = oracle.make_scene(solver.substep_dt, gravity=tuple(solver.gravity[0]), lower_bound=tuple(solver.lower_bound),
+                           upper_bound=tuple(solver.upper_bound), grid_density=solver.grid_density,
+                           particle_size=solver.particle_size)
+
+    def L(vb, springs=True):
+        vel = np.zeros((n, 3))
+        vel[:nb] = vb
+        st = dict(pos=x0, vel=vel, C=np.zeros((n, 3, 3)), F=np.tile(np.eye(3), (n, 1, 1)),
+                  Jp=np.concatenate([np.full(e.n_particles, float(e.material._default_Jp)) for e in ents]),
+                  mat=np.concatenate([np.full(e.n_particles, e.material.idx, np.int32) for e in ents]),
+                  active=np.ones(n, bool))
+        for p, q in poses:
+            tgt = np.array([_qrot(q, l) for l in local]) + p
+            for _ in range(scene.substeps):
+                st, _, _ = oracle.run(sc, oms, st, 1)
+                if springs:
+                    vv = st["vel"][sel]
+                    st["vel"][sel] = vv + solver.substep_dt * (-k * (st["pos"][sel] - tgt)
+                                                                - 2.0 * np.sqrt(k * m_real) * vv) / m_real
+        return float(((st["pos"][:nb].mean(0) - target) ** 2).sum())
+
+    assert abs(loss.item() - L(v0.astype(np.float32).astype(np.float64))) <= 1e-4 * loss.item() + 1e-8
+    eps = 1e-4
+
+    def fd(springs):
+        return np.array([(L(v0 + eps * np.eye(3)[j], springs) - L(v0 - eps * np.eye(3)[j], springs)) / (2 * eps)
+                         for j in range(3)])
+
+    fd_s, fd_free = fd(True), fd(False)
+    assert np.linalg.norm(fd_s - fd_free) > 0.1 * np.linalg.norm(fd_s), (fd_s, fd_free)
+    assert np.linalg.norm(g - fd_s) <= GRAD_RTOL * np.linalg.norm(fd_s), (g, fd_s)
