@@ -587,6 +587,26 @@ class SceneDiffEngine:
             self.states[b] = (*(getattr(state, k)[b].to(device="cuda", dtype=torch.float32) for k in FIELDS),
                               self.states[b][5], self.states[b][6])
 
+    def reset(self, envs) -> None:
+        """Scene.reset (simulator.py:223-232): the tools of envs back to their initial pose, at rest;
+        with every env reset the substep count restarts and the recorded steps are dropped (the
+        adjoint walk cannot pass a reset), as the reference's reset zeroes _cur_substep_global."""
+        for b in envs:
+            st = list(self.states[b])
+            st[5] = self.T0.clone()
+            st[6] = st[6].detach().clone()  # the actuation stays set, off the graph of the steps before
+            self.states[b] = tuple(st)
+            self.tool_qa[b] = self.qa0.clone()
+        if len(list(envs)) == self.B:
+            self.step_inputs = []
+            self.pending = []
+            self.steps_taken = self.substeps_taken = 0
+            self.ff_base = 0
+            self.queried.clear()
+            self.queried_tools.clear()
+            self.adj = None
+            self._seg = None
+
     def set_muscle_direction(self, start: int, count: int, dirs: torch.Tensor) -> None:
         """Fibre directions [count, 3] of particles [start, start+count) (constants of the steps to come)."""
         self.mdir[start: start + count] = dirs.to(device="cuda", dtype=torch.float32)

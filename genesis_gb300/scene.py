@@ -216,6 +216,8 @@ class Scene:
             for t in solver._tools:
                 t.reset()
             solver._upload_colliders()
+        if solver._diff is not None:
+            solver._diff.reset(list(range(solver._B)) if envs_idx is None else [int(e) for e in np.atleast_1d(envs_idx)])
         self._sim._cur_substep_global = 0
 
     def get_state(self) -> SimState:

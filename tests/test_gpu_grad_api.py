@@ -646,3 +646,34 @@ def test_particle_constraint_gradients_match_fp64_central_differences(gs, oracle
     fd_s, fd_free = fd(True), fd(False)
     assert np.linalg.norm(fd_s - fd_free) > 0.1 * np.linalg.norm(fd_s), (fd_s, fd_free)
     assert np.linalg.norm(g - fd_s) <= GRAD_RTOL * np.linalg.norm(fd_s), (g, fd_s)
+
+
+def test_reset_in_differentiable_mode_restores_tools_and_restarts(gs, tmp_path):
+    """scene.reset() in differentiable mode puts the particles and the tool back at their initial
+    state and restarts the step count (simulator.py:223-232): the same inputs then give the same
+    trajectory and the same gradient as the first run."""
+    from test_api_host import _cube_obj
+
+    obj = tmp_path / "cube.obj"
+    _cube_obj(obj, half=1.0)
+    scene, tool, block = _tool_scene(gs, obj)
+    w = torch.tensor(np.random.default_rng(4).normal(size=(block.n_particles, 3)), dtype=torch.float32,
+                     device="cuda")
+
+    def run():
+        u = torch.tensor([0.0, 1.0, -0.2], device="cuda", requires_grad=True)
+        tool.set_velocity(vel=u)
+        for _ in range(6):
+            scene.step()
+        x = block.get_state().pos[0]
+        (x * w).sum().backward()
+        return x.detach().clone(), tool.get_state().pos.detach().clone(), u.grad.clone()
+
+    x1, t1, g1 = run()
+    assert g1.abs().max().item() > 0
+    scene.reset()
+    assert scene.sim.mpm_solver._diff.substeps_taken == 0
+    x2, t2, g2 = run()
+    assert (x1 - x2).abs().max().item() < 1e-6
+    assert (t1 - t2).abs().max().item() < 1e-6
+    assert torch.allclose(g1, g2, rtol=1e-4, atol=1e-7), (g1, g2)

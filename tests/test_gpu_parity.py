@@ -205,6 +205,25 @@ def test_nan_position_raises(gs):
         scene.step()
 
 
+def test_particle_outside_the_grid_raises_and_the_context_recovers(gs):
+    """A particle put outside the grid (its stencil would leave it) is never scattered or gathered:
+    the keying's bounds check flags it, scene.step() raises, and once it is back inside the scene
+    steps on and matches a scene that never left (the status word is read and cleared)."""
+    scene, cube, _ = c1_scene(gs, size=0.1)
+    ref, ref_cube, _ = c1_scene(gs, size=0.1)
+    pos0 = cube.get_particles_pos().clone()
+    bad = pos0.clone()
+    bad[3] = torch.tensor([1.5, 0.5, 0.5], device="cuda")
+    cube.set_particles_pos(bad)
+    with pytest.raises(gs.GenesisException, match="left the simulation grid"):
+        scene.step()
+    cube.set_particles_pos(pos0)
+    for _ in range(5):
+        scene.step()
+        ref.step()
+    assert (cube.get_particles_pos() - ref_cube.get_particles_pos()).abs().max().item() < 1e-6
+
+
 def test_graph_and_split_paths_agree(gs):
     sa, ca, _ = c1_scene(gs, size=0.1)
     sb, cb, _ = c1_scene(gs, size=0.1)
