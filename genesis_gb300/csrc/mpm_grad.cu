@@ -590,7 +590,7 @@ __device__ __forceinline__ void polar_rotation_adj(const float* U, const float* 
 
 // P2G adjoint + stress adjoint + F_tmp adjoint: from dL/d(node momentum, mass) and dL/dF1 to
 // dL/d(x, v, C, F, mu, lam); adds the P2G part of dL/dx to the G2P part already in gx.
-__global__ void __launch_bounds__(256) k_dp2g_adj(DiffParams Q) {
+__global__ void __launch_bounds__(128) k_dp2g_adj(DiffParams Q) {
   const SceneDev& S = Q.S;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < Q.n; i += (int64_t)gridDim.x * blockDim.x) {
     float x[3], v[3], C[9], F[9];
@@ -914,7 +914,9 @@ int diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean,
   if (n > 0) k_dg2p_adj<<<pb, 256, 0, s>>>(Q);
   k_dgrid_adj<<<gb, 256, 0, s>>>(Q, nodes, ff ? *ff : kNoFields, cc ? *cc : kNoColliders);
   if (n_tools > 0) k_dtool_adj<<<1, 32, 0, s>>>(Q);
-  if (n > 0) k_dp2g_adj<<<pb, 256, 0, s>>>(Q);
+  // 128-thread CTAs: at its ~160 registers three of them fit an SM (12 warps) where one of 256 threads
+  // does (8 warps)
+  if (n > 0) k_dp2g_adj<<<(int)((n + 127) / 128 < 16384 ? (n + 127) / 128 : 16384), 128, 0, s>>>(Q);
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_ERR_CUDA;
 }
 
