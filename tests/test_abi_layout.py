@@ -17,6 +17,8 @@ STRUCTS = {
     "mpm_pool_config": "MpmPoolConfig",
     "mpm_collider": "MpmCollider",
     "mpm_force_field": "MpmForceField",
+    "mpm_diff_tool": "MpmDiffTool",
+    "mpm_diff_extras": "MpmDiffExtras",
 }
 
 
