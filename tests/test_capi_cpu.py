@@ -107,3 +107,53 @@ def test_product_fails_loudly_without_library(tmp_path):
 
     with pytest.raises(GenesisException):
         _lib.load(str(tmp_path / "missing.so"))
+
+
+def test_differentiable_extras_are_validated_on_the_host(lib):
+    """mpm_diff_forward_seq_ex / mpm_diff_backward_seq_ex reject malformed extras records before any
+    CUDA call: too many force fields or tools, an unknown field type, a tool-shaped or SDF collider
+    without its context, and half-given Muscle or constraint inputs."""
+    from genesis_gb300 import _lib
+
+    cfg = _cfg(n=0)
+    buf = (ctypes.c_float * 64)()  # stands in for the device arrays; never touched on rejection
+    p = ctypes.cast(buf, ctypes.c_void_p)
+
+    def fwd(ex):
+        return lib.mpm_diff_forward_seq_ex(ctypes.byref(cfg), p, p, p, 0, 1, p, p, p, p, p, 2, p, p,
+                                           ctypes.byref(ex), p, p, 0, p, None)
+
+    def bwd(ex):
+        return lib.mpm_diff_backward_seq_ex(ctypes.byref(cfg), p, p, p, 0, 1, p, p, p, p, p, p, p,
+                                            ctypes.byref(ex), p, p, p, p, p, p, p, p, None)
+
+    ff = (_lib.MpmForceField * 9)()
+    col = (_lib.MpmCollider * 1)()
+    cases = []
+    ex = _lib.MpmDiffExtras()
+    ex.force_fields, ex.n_force_fields = ctypes.addressof(ff), 9
+    cases.append(ex)
+    ex = _lib.MpmDiffExtras()
+    ff[0].type = 99
+    ex.force_fields, ex.n_force_fields = ctypes.addressof(ff), 1
+    cases.append(ex)
+    ex = _lib.MpmDiffExtras()
+    ex.n_tools = _lib.DIFF_MAX_TOOLS + 1
+    cases.append(ex)
+    for ctype in (4, 3):  # MPM_COLLIDER_TOOL; MPM_COLLIDER_SDF with no context to hold its grid
+        col[0].type = ctype
+        ex = _lib.MpmDiffExtras()
+        ex.colliders, ex.n_colliders = ctypes.addressof(col), 1
+        cases.append(ex)
+    ex = _lib.MpmDiffExtras()
+    ex.colliders, ex.n_colliders = ctypes.addressof(col), _lib.DIFF_MAX_COLLIDERS + 1
+    cases.append(ex)
+    ex = _lib.MpmDiffExtras()
+    ex.actu = p.value
+    cases.append(ex)
+    ex = _lib.MpmDiffExtras()
+    ex.constraint_stiffness = p.value
+    cases.append(ex)
+    for i, ex in enumerate(cases):
+        assert fwd(ex) == 1, i
+        assert bwd(ex) == 1, i
