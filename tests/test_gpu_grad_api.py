@@ -677,3 +677,29 @@ def test_reset_in_differentiable_mode_restores_tools_and_restarts(gs, tmp_path):
     assert (x1 - x2).abs().max().item() < 1e-6
     assert (t1 - t2).abs().max().item() < 1e-6
     assert torch.allclose(g1, g2, rtol=1e-4, atol=1e-7), (g1, g2)
+
+
+def test_env_specific_collider_in_differentiable_mode(gs):
+    """A collider given to one env only (Collider.env) acts in that env's differentiable grid op and
+    not in the other's, as in the product path (two envs, 1e-4 m), and the gradient reaches both
+    envs' inputs."""
+    from genesis_gb300.coupling import Collider
+
+    col = [Collider("sphere", pos=(0.45, 0.5, 0.22), radius=0.06, coup_friction=0.3, env=1)]
+    sg, bg, _ = _scene(gs, requires_grad=True, n_envs=2, box_z=0.33)
+    sp, bp, _ = _scene(gs, requires_grad=False, n_envs=2, box_z=0.33)
+    sg.sim.mpm_solver.set_colliders(col)
+    sp.sim.mpm_solver.set_colliders(col)
+    v = torch.tensor([0.0, 0.0, -2.0], device="cuda", requires_grad=True)
+    bg.set_velocity(v)
+    bp.set_velocity(v.detach())
+    for _ in range(4):
+        sg.step()
+        sp.step()
+    a = bg.get_state().pos
+    b = bp.get_state().pos
+    assert (a.detach() - b).abs().max().item() <= 1e-4
+    assert (a.detach()[0] - a.detach()[1]).abs().max().item() > 1e-3  # the sphere met env 1's box only
+    a[1].mean(0)[2].backward()
+    assert torch.isfinite(v.grad).all() and v.grad.abs().max().item() > 0
+    sp.sim.mpm_solver.destroy()
