@@ -234,6 +234,11 @@ _SIGNATURES = {
                                           _P, _P, _P, c_int32, _P, _P]),
     "mpm_diff_backward_seq_ex": (c_int32, [_P, _P, _P, _P, c_int64, c_int32, _P, _P, _P, _P, _P, _P, _P, _P,
                                            _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "mpm_diff_substep_stage": (c_int32, [_P, _P, _P, _P, c_int64, _P, _P, _P, _P, _P, _P, _P, _P, c_int32, c_int32,
+                                         c_int32, c_int32, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "mpm_diff_substep_stage_adj": (c_int32, [_P, _P, _P, _P, c_int64, _P, _P, _P, _P, _P, _P, _P, _P, c_int32,
+                                             c_int32, c_int32, c_int32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
+                                             _P, _P, _P, _P, _P, _P, _P, _P]),
     "mpm_set_force_fields": (c_int32, [_P, c_int32, _P]),
     "mpm_sample_regular": (c_int32, [c_int32, _P, _P, c_double, _P, c_int64, _P, _P]),
     "mpm_test_wait_timeout": (c_int32, [_P, _P]),

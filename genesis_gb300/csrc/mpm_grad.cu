@@ -296,38 +296,52 @@ __device__ __forceinline__ void dfield_apply(const DiffFields& FF, int f, const 
   for (int k = 0; k < 3; ++k) v[k] += a[k] * S.dt;
 }
 
-__global__ void k_dgrid(DiffParams Q, int64_t nodes, const DiffFields FF, const DiffColliders CC) {
+// The grid op, whole (stage 0) or in the stages a Custom force field splits it into (the product
+// path's mpm_substep_grid_stage): stage 1 gravity and the fields given, from the P2G grid into the
+// velocity buffer; stage 2 more fields on the velocity buffer; stage 3 the tools, colliders and
+// boundary on it.  Nodes without mass hold zero velocity.
+__global__ void k_dgrid(DiffParams Q, int64_t nodes, const DiffFields FF, const DiffColliders CC, int stage) {
   const SceneDev& S = Q.S;
+  const bool fields = stage <= 2, tail = stage == 0 || stage == 3;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nodes; i += (int64_t)gridDim.x * blockDim.x) {
     const float4 q = Q.pm[i];
     float v[3] = {0.f, 0.f, 0.f};
     if (q.w > S.eps) {
       const int g[3] = {(int)(i / ((int64_t)S.res[1] * S.res[2])), (int)((i / S.res[2]) % S.res[1]), (int)(i % S.res[2])};
-      const float inv = 1.f / q.w;
-      v[0] = inv * q.x + S.dt * S.grav[0];
-      v[1] = inv * q.y + S.dt * S.grav[1];
-      v[2] = inv * q.z + S.dt * S.grav[2];
-      if (Q.n_tools > 0 || FF.n > 0 || CC.n > 0) {
+      if (stage <= 1) {
+        const float inv = 1.f / q.w;
+        v[0] = inv * q.x + S.dt * S.grav[0];
+        v[1] = inv * q.y + S.dt * S.grav[1];
+        v[2] = inv * q.z + S.dt * S.grav[2];
+      } else {  // the velocity the earlier stages (and the Custom fields between them) left
+        const float4 u = Q.gvel[i];
+        v[0] = u.x, v[1] = u.y, v[2] = u.z;
+      }
+      if ((fields && FF.n > 0) || (tail && (Q.n_tools > 0 || CC.n > 0))) {
         float x[3];
         node_world_pos(S, g, x);
-        for (int f = 0; f < FF.n; ++f)  // force fields after gravity, before the tools
-          if (FF.f[f].active) dfield_apply(FF, f, S, g, x, v);
-        for (int t = 0; t < Q.n_tools; ++t) {
-          const float* st = Q.tool_f + t * 13;
-          tool_collide_t<float>(Q.tools[t], x, v, st, st + 3, st + 7, Q.tool_f1 + t * 13 + 3, S.dt, S.eps);
-        }
-        for (int ci = 0; ci < CC.n; ++ci) {  // rigid colliders after the tools (legacy_coupler.py:386-403)
-          const ColliderDev& c = CC.c[ci];
-          if (c.scene >= 0 && c.scene != FF.scene) continue;
-          float n[3];
-          const float infl = dcollider_influence(c, x, S.eps, n);
-          if (infl > 0.f) collide_in_velocity(c, S.eps, x, v, n, infl);
+        if (fields)
+          for (int f = 0; f < FF.n; ++f)  // force fields after gravity, before the tools
+            if (FF.f[f].active) dfield_apply(FF, f, S, g, x, v);
+        if (tail) {
+          for (int t = 0; t < Q.n_tools; ++t) {
+            const float* st = Q.tool_f + t * 13;
+            tool_collide_t<float>(Q.tools[t], x, v, st, st + 3, st + 7, Q.tool_f1 + t * 13 + 3, S.dt, S.eps);
+          }
+          for (int ci = 0; ci < CC.n; ++ci) {  // rigid colliders after the tools (legacy_coupler.py:386-403)
+            const ColliderDev& c = CC.c[ci];
+            if (c.scene >= 0 && c.scene != FF.scene) continue;
+            float n[3];
+            const float infl = dcollider_influence(c, x, S.eps, n);
+            if (infl > 0.f) collide_in_velocity(c, S.eps, x, v, n, infl);
+          }
         }
       }
-      for (int d = 0; d < 3; ++d) {
-        const float p = (float)(g[d] + S.offset[d]) * S.dx;
-        if ((p >= S.hi[d] && v[d] >= 0.f) || (p <= S.lo[d] && v[d] <= 0.f)) v[d] = 0.f;
-      }
+      if (tail)
+        for (int d = 0; d < 3; ++d) {
+          const float p = (float)(g[d] + S.offset[d]) * S.dx;
+          if ((p >= S.hi[d] && v[d] >= 0.f) || (p <= S.lo[d] && v[d] <= 0.f)) v[d] = 0.f;
+        }
     }
     Q.gvel[i] = make_float4(v[0], v[1], v[2], q.w);
   }
@@ -451,7 +465,12 @@ __global__ void __launch_bounds__(256) k_dg2p_adj(DiffParams Q) {
 }
 
 // grid-op adjoint: v = B(T(F(p/m + dt g))) (force fields F, tools T, boundary B) -> dL/dp, dL/dm
-__global__ void k_dgrid_adj(DiffParams Q, int64_t nodes, const DiffFields FF, const DiffColliders CC) {
+// Adjoint of one stage of k_dgrid (0: whole).  Stages 2 and 3 take the velocity that stage began
+// from in vin and turn dL/d(its output) in g_grid_v into dL/d(its input) in place; stages 0 and 1
+// end at the P2G grid, dL/d(momentum, mass) into g_grid_pm.
+__global__ void k_dgrid_adj(DiffParams Q, int64_t nodes, const DiffFields FF, const DiffColliders CC, int stage,
+                            const float4* vstage) {
+  const bool fields = stage <= 2, tail = stage == 0 || stage == 3, from_pm = stage <= 1;
   const SceneDev& S = Q.S;
   const int lane = threadIdx.x & 31;
   for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x; i0 < nodes; i0 += (int64_t)gridDim.x * blockDim.x) {
@@ -466,20 +485,25 @@ __global__ void k_dgrid_adj(DiffParams Q, int64_t nodes, const DiffFields FF, co
       const int g[3] = {(int)(i / ((int64_t)S.res[1] * S.res[2])), (int)((i / S.res[2]) % S.res[1]), (int)(i % S.res[2])};
       const float inv = 1.f / q.w;
       float u[3] = {inv * q.x + S.dt * S.grav[0], inv * q.y + S.dt * S.grav[1], inv * q.z + S.dt * S.grav[2]};
+      if (!from_pm) {
+        const float4 w = vstage[i];
+        u[0] = w.x, u[1] = w.y, u[2] = w.z;
+      }
       float gu[3] = {gv.x, gv.y, gv.z};
       float vin[MPM_DIFF_MAX_TOOLS][3], fin[MPM_DIFF_MAX_FORCE_FIELDS][3], cin[MPM_DIFF_MAX_COLLIDERS][3];
       float x[3];
       node_world_pos(S, g, x);
-      for (int f = 0; f < FF.n; ++f) {  // forward through the force fields, keeping each one's input
+      const int n_ff = fields ? FF.n : 0, n_tools = tail ? Q.n_tools : 0, n_col = tail ? CC.n : 0;
+      for (int f = 0; f < n_ff; ++f) {  // forward through the force fields, keeping each one's input
         for (int k = 0; k < 3; ++k) fin[f][k] = u[k];
         if (FF.f[f].active) dfield_apply(FF, f, S, g, x, u);
       }
-      for (int t = 0; t < Q.n_tools; ++t) {  // forward through the tools, keeping each one's input
+      for (int t = 0; t < n_tools; ++t) {  // forward through the tools, keeping each one's input
         for (int k = 0; k < 3; ++k) vin[t][k] = u[k];
         const float* st = Q.tool_f + t * 13;
         tool_collide_t<float>(Q.tools[t], x, u, st, st + 3, st + 7, Q.tool_f1 + t * 13 + 3, S.dt, S.eps);
       }
-      for (int ci = 0; ci < CC.n; ++ci) {  // forward through the rigid colliders, keeping each one's input
+      for (int ci = 0; ci < n_col; ++ci) {  // forward through the rigid colliders, keeping each one's input
         for (int k = 0; k < 3; ++k) cin[ci][k] = u[k];
         const ColliderDev& c = CC.c[ci];
         if (c.scene >= 0 && c.scene != FF.scene) continue;
@@ -487,18 +511,19 @@ __global__ void k_dgrid_adj(DiffParams Q, int64_t nodes, const DiffFields FF, co
         const float infl = dcollider_influence(c, x, S.eps, n);
         if (infl > 0.f) collide_in_velocity(c, S.eps, x, u, n, infl);
       }
-      for (int d = 0; d < 3; ++d) {  // the boundary acts on the velocity the tools and colliders left
-        const float p = (float)(g[d] + S.offset[d]) * S.dx;
-        if ((p >= S.hi[d] && u[d] >= 0.f) || (p <= S.lo[d] && u[d] <= 0.f)) gu[d] = 0.f;
-      }
-      for (int ci = CC.n - 1; ci >= 0; --ci) {  // back through the rigid colliders
+      if (tail)
+        for (int d = 0; d < 3; ++d) {  // the boundary acts on the velocity the tools and colliders left
+          const float p = (float)(g[d] + S.offset[d]) * S.dx;
+          if ((p >= S.hi[d] && u[d] >= 0.f) || (p <= S.lo[d] && u[d] <= 0.f)) gu[d] = 0.f;
+        }
+      for (int ci = n_col - 1; ci >= 0; --ci) {  // back through the rigid colliders
         const ColliderDev& c = CC.c[ci];
         if (c.scene >= 0 && c.scene != FF.scene) continue;
         float n[3];
         const float infl = dcollider_influence(c, x, S.eps, n);
         if (infl > 0.f) collide_in_vjp(c, S.eps, x, cin[ci], n, infl, gu);
       }
-      for (int t = Q.n_tools - 1; t >= 0; --t) {  // back through the tools: Jacobians from dual numbers
+      for (int t = n_tools - 1; t >= 0; --t) {  // back through the tools: Jacobians from dual numbers
         const float* st = Q.tool_f + t * 13;
         TD vt[3], pt[3], ut[3];
         for (int k = 0; k < 3; ++k) {
@@ -515,14 +540,21 @@ __global__ void k_dgrid_adj(DiffParams Q, int64_t nodes, const DiffFields FF, co
         }
         for (int j = 0; j < 3; ++j) gu[j] = gin[j];
       }
-      for (int f = FF.n - 1; f >= 0; --f)  // back through the force fields: g += dt J^T g
+      for (int f = n_ff - 1; f >= 0; --f)  // back through the force fields: g += dt J^T g
         if (FF.f[f].active) ff_acc_vjp(FF.f[f], x, fin[f], S.eps, S.dt, gu);
-      out.x = gu[0] * inv;
-      out.y = gu[1] * inv;
-      out.z = gu[2] * inv;
-      out.w = -(gu[0] * q.x + gu[1] * q.y + gu[2] * q.z) * inv * inv;
+      if (from_pm) {
+        out.x = gu[0] * inv;
+        out.y = gu[1] * inv;
+        out.z = gu[2] * inv;
+        out.w = -(gu[0] * q.x + gu[1] * q.y + gu[2] * q.z) * inv * inv;
+      } else {  // dL/d(the stage's input velocity)
+        out = make_float4(gu[0], gu[1], gu[2], 0.f);
+      }
     }
-    if (i < nodes) Q.g_grid_pm[i] = out;
+    if (i < nodes) {
+      if (from_pm) Q.g_grid_pm[i] = out;
+      else Q.g_grid_v[i] = out;
+    }
     for (int t = 0; t < Q.n_tools; ++t)  // the tool's share of dL/d(pos, vel), one atomic per warp
       for (int k = 0; k < 6; ++k) {
         float a = tacc[t][k];
@@ -832,7 +864,7 @@ int diff_forward(const mpm_scene_config* scene, double rho, int32_t neohookean, 
                  float* F1, float* Jp1, void* grid_pm, void* grid_v, uint32_t* status, void* stream, int n_tools = 0,
                  const DiffToolDev* tools = nullptr, const float* tool_f = nullptr, float* tool_f1 = nullptr,
                  const DiffFields* ff = nullptr, const DiffMuscle* mus = nullptr,
-                 const DiffColliders* cc = nullptr) {
+                 const DiffColliders* cc = nullptr, int phase = -1, int stage = 0) {
   if (!scene || n < 0 || !grid_pm || !grid_v || !status) return MPM_ERR_BAD_ARG;
   DiffParams Q;
   std::memset(&Q, 0, sizeof(Q));
@@ -861,11 +893,15 @@ int diff_forward(const mpm_scene_config* scene, double rho, int32_t neohookean, 
   cudaStream_t s = (cudaStream_t)stream;
   const int gb = (int)((nodes + 255) / 256 < 8192 ? (nodes + 255) / 256 : 8192);
   const int pb = (int)((n + 255) / 256 < 8192 ? (n + 255) / 256 : 8192);
-  k_dclear<<<gb, 256, 0, s>>>(Q, nodes, Q.pm);
-  if (n > 0) k_dp2g<<<pb, 256, 0, s>>>(Q);
-  if (n_tools > 0) k_dtool_advance<<<1, 32, 0, s>>>(Q);
-  k_dgrid<<<gb, 256, 0, s>>>(Q, nodes, ff ? *ff : kNoFields, cc ? *cc : kNoColliders);
-  if (n > 0) k_dg2p<<<pb, 256, 0, s>>>(Q);
+  // phase -1: the whole substep; else one part of a staged one (0: P2G, 1: grid stage, 2: G2P)
+  if (phase < 0 || phase == 0) {
+    k_dclear<<<gb, 256, 0, s>>>(Q, nodes, Q.pm);
+    if (n > 0) k_dp2g<<<pb, 256, 0, s>>>(Q);
+    if (n_tools > 0) k_dtool_advance<<<1, 32, 0, s>>>(Q);
+  }
+  if (phase < 0 || phase == 1)
+    k_dgrid<<<gb, 256, 0, s>>>(Q, nodes, ff ? *ff : kNoFields, cc ? *cc : kNoColliders, phase < 0 ? 0 : stage);
+  if ((phase < 0 || phase == 2) && n > 0) k_dg2p<<<pb, 256, 0, s>>>(Q);
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_ERR_CUDA;
 }
 
@@ -877,7 +913,7 @@ int diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean,
                   void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream, int n_tools = 0,
                   const DiffToolDev* tools = nullptr, const float* tool_f = nullptr, const float* tool_f1 = nullptr,
                   float* g_tool = nullptr, const DiffFields* ff = nullptr, const DiffMuscle* mus = nullptr,
-                  const DiffColliders* cc = nullptr) {
+                  const DiffColliders* cc = nullptr, int phase = -1, int stage = 0, const void* vstage = nullptr) {
   if (!scene || n < 0 || !grid_pm || !grid_v || !g_grid_v || !g_grid_pm) return MPM_ERR_BAD_ARG;
   DiffParams Q;
   std::memset(&Q, 0, sizeof(Q));
@@ -910,13 +946,21 @@ int diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean,
   cudaStream_t s = (cudaStream_t)stream;
   const int gb = (int)((nodes + 255) / 256 < 8192 ? (nodes + 255) / 256 : 8192);
   const int pb = (int)((n + 255) / 256 < 8192 ? (n + 255) / 256 : 8192);
-  k_dclear<<<gb, 256, 0, s>>>(Q, nodes, Q.g_grid_v);
-  if (n > 0) k_dg2p_adj<<<pb, 256, 0, s>>>(Q);
-  k_dgrid_adj<<<gb, 256, 0, s>>>(Q, nodes, ff ? *ff : kNoFields, cc ? *cc : kNoColliders);
-  if (n_tools > 0) k_dtool_adj<<<1, 32, 0, s>>>(Q);
-  // 128-thread CTAs: at its ~160 registers three of them fit an SM (12 warps) where one of 256 threads
-  // does (8 warps)
-  if (n > 0) k_dp2g_adj<<<(int)((n + 127) / 128 < 16384 ? (n + 127) / 128 : 16384), 128, 0, s>>>(Q);
+  // phase -1: the whole adjoint substep; else one part of a staged one, in reverse order (2: G2P
+  // adjoint, 1: a grid stage's adjoint, 0: the tools' chain and the P2G adjoint)
+  if (phase < 0 || phase == 2) {
+    k_dclear<<<gb, 256, 0, s>>>(Q, nodes, Q.g_grid_v);
+    if (n > 0) k_dg2p_adj<<<pb, 256, 0, s>>>(Q);
+  }
+  if (phase < 0 || phase == 1)
+    k_dgrid_adj<<<gb, 256, 0, s>>>(Q, nodes, ff ? *ff : kNoFields, cc ? *cc : kNoColliders, phase < 0 ? 0 : stage,
+                                   (const float4*)vstage);
+  if (phase < 0 || phase == 0) {
+    if (n_tools > 0) k_dtool_adj<<<1, 32, 0, s>>>(Q);
+    // 128-thread CTAs: at its ~160 registers three of them fit an SM (12 warps) where one of 256
+    // threads does (8 warps)
+    if (n > 0) k_dp2g_adj<<<(int)((n + 127) / 128 < 16384 ? (n + 127) / 128 : 16384), 128, 0, s>>>(Q);
+  }
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_ERR_CUDA;
 }
 
@@ -1172,6 +1216,64 @@ int mpm_diff_backward_seq_ex(const mpm_scene_config* scene, const float* mass, c
   return diff_backward_seq(scene, 0.0, 0, mass, kind, aux, n, n_sub, x_seq, v_seq, C_seq, F_seq, Jp_seq, mu, lam,
                            g_seq, gmu, glam, grid_pm, grid_v, g_grid_v, g_grid_pm, status, stream, nt, td,
                            ex ? ex->tool_seq : nullptr, ex ? ex->g_tool : nullptr, &ff, &mus, &cc);
+}
+
+// One part of a differentiable substep in stages (a Custom force field acts in the caller between
+// grid stages); see gbmpm.h.
+int mpm_diff_substep_stage(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
+                           int64_t n, const float* x, const float* v, const float* C, const float* F, const float* Jp,
+                           const float* mu, const float* lam, const mpm_diff_extras* ex, int32_t phase, int32_t stage,
+                           int32_t ff_begin, int32_t ff_end, float* x1, float* v1, float* C1, float* F1, float* Jp1,
+                           void* grid_pm, void* grid_v, uint32_t* status, void* stream) {
+  if (n > 0 && (!mass || !kind || !aux || !Jp)) return MPM_ERR_BAD_ARG;
+  if (phase < 0 || phase > 2 || (phase == 1 && (stage < 1 || stage > 3))) return MPM_ERR_BAD_ARG;
+  if (phase == 1 && stage <= 2 && (!ex || ff_begin < 0 || ff_end < ff_begin || ff_end > ex->n_force_fields))
+    return MPM_ERR_BAD_ARG;
+  DiffToolDev td[MPM_DIFF_MAX_TOOLS];
+  DiffFields ff;
+  DiffMuscle mus;
+  DiffColliders cc;
+  int r = diff_extras(ex, td, ff, mus, cc);
+  if (r) return r;
+  if (phase == 1 && stage <= 2 &&
+      (r = diff_fields(ex->force_fields + ff_begin, ff_end - ff_begin, ex->scene_index, ex->ff_step, ff)))
+    return r;
+  const int nt = ex ? ex->n_tools : 0;
+  float* ts = ex ? ex->tool_seq : nullptr;
+  return diff_forward(scene, 0.0, 0, mass, kind, aux, n, x, v, C, F, Jp, mu, lam, x1, v1, C1, F1, Jp1, grid_pm,
+                      grid_v, status, stream, nt, td, ts, ts ? ts + (int64_t)nt * 13 : nullptr, &ff, &mus, &cc, phase,
+                      stage);
+}
+
+int mpm_diff_substep_stage_adj(const mpm_scene_config* scene, const float* mass, const int32_t* kind,
+                               const float* aux, int64_t n, const float* x, const float* v, const float* C,
+                               const float* F, const float* Jp, const float* mu, const float* lam,
+                               const mpm_diff_extras* ex, int32_t phase, int32_t stage, int32_t ff_begin,
+                               int32_t ff_end, const void* vstage, const float* gx1, const float* gv1,
+                               const float* gC1, const float* gF1, const float* gJp1, float* gx, float* gv, float* gC,
+                               float* gF, float* gJp, float* gmu, float* glam, void* grid_pm, void* grid_v,
+                               void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream) {
+  if (n > 0 && (!mass || !kind || !aux || !Jp)) return MPM_ERR_BAD_ARG;
+  if (phase < 0 || phase > 2 || (phase == 1 && (stage < 1 || stage > 3)) || (phase == 1 && stage >= 2 && !vstage))
+    return MPM_ERR_BAD_ARG;
+  if (phase == 1 && stage <= 2 && (!ex || ff_begin < 0 || ff_end < ff_begin || ff_end > ex->n_force_fields))
+    return MPM_ERR_BAD_ARG;
+  DiffToolDev td[MPM_DIFF_MAX_TOOLS];
+  DiffFields ff;
+  DiffMuscle mus;
+  DiffColliders cc;
+  int r = diff_extras(ex, td, ff, mus, cc);
+  if (r) return r;
+  if (phase == 1 && stage <= 2 &&
+      (r = diff_fields(ex->force_fields + ff_begin, ff_end - ff_begin, ex->scene_index, ex->ff_step, ff)))
+    return r;
+  const int nt = ex ? ex->n_tools : 0;
+  if (nt > 0 && !ex->g_tool) return MPM_ERR_BAD_ARG;
+  const float* ts = ex ? ex->tool_seq : nullptr;
+  return diff_backward(scene, 0.0, 0, mass, kind, aux, n, x, v, C, F, Jp, mu, lam, gx1, gv1, gC1, gF1, gJp1, gx, gv,
+                       gC, gF, gJp, gmu, glam, grid_pm, grid_v, g_grid_v, g_grid_pm, status, stream, nt, td, ts,
+                       ts ? ts + (int64_t)nt * 13 : nullptr, ex ? ex->g_tool : nullptr, &ff, &mus, &cc, phase, stage,
+                       vstage);
 }
 
 int mpm_diff_forward_seq_tools(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,

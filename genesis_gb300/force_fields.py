@@ -258,7 +258,8 @@ class Custom(ForceField):
     the accelerations [M, 3].  As in the reference, `get_acc` is replaced by `func`, so the field
     acts whether or not it was activated.  A scene with a Custom field runs its substeps through the
     staged grid op (one library call per stage and a torch call per Custom field per substep)
-    instead of the captured graph."""
+    instead of the captured graph.  In differentiable mode `func` is differentiated by torch
+    autograd (its parameters that require grad receive gradients too)."""
 
     _type = -2
 

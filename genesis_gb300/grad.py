@@ -29,8 +29,9 @@ differentiable grid op (mpm_diff_forward_seq_ex / mpm_diff_backward_seq_ex), eac
 fields as they were when it ran, and so do kinematic rigid colliders (solver.set_colliders: the
 shapes of the product grid op, poses fixed within a step, no reaction forces in this mode) and
 particle constraints (entity.set_particle_constraints: springs towards targets that follow the
-links' poses of solver.set_link_poses, differentiated in the particle state).  As in the reference, CPIC and emitters are rejected in this mode;
-Custom force fields (a torch function here) are too.
+links' poses of solver.set_link_poses, differentiated in the particle state).  Custom force fields (a torch function here) run between grid stages
+of the substep (mpm_diff_substep_stage), their Jacobian taken by torch autograd in the adjoint.  As
+in the reference, CPIC and emitters are rejected in this mode.
 """
 
 from __future__ import annotations
@@ -202,12 +203,19 @@ class SceneDiffEngine:
         library's does when mpm_set_force_fields replaces them)."""
         from .force_fields import Custom
 
-        if any(isinstance(f, Custom) for f in ffs):
-            raise GenesisException("Custom force fields are not supported in differentiable mode.")
-        if len(ffs) > _lib.DIFF_MAX_FORCE_FIELDS:
+        recs, plan, begin = [], [], 0
+        for f in ffs:  # Custom fields split the built-in ones into grid stages, as in the product path
+            if isinstance(f, Custom):
+                plan += [("fields", begin, len(recs)), ("custom", f)]
+                begin = len(recs)
+            else:
+                recs.append(f.to_c())
+        plan.append(("fields", begin, len(recs)))
+        if len(recs) > _lib.DIFF_MAX_FORCE_FIELDS:
             raise GenesisException(f"At most {_lib.DIFF_MAX_FORCE_FIELDS} force fields in differentiable mode.")
-        self.ff_recs = (_lib.MpmForceField * max(1, len(ffs)))(*[f.to_c() for f in ffs])
-        self.n_ffs = len(ffs)
+        self.ff_recs = (_lib.MpmForceField * max(1, len(recs)))(*recs)
+        self.n_ffs = len(recs)
+        self.ff_plan = plan if len(plan) > 1 else None
         self.ff_base = getattr(self, "substeps_taken", 0)
 
     def set_colliders(self, recs) -> None:
@@ -267,7 +275,8 @@ class SceneDiffEngine:
     def _fields(self, b: int):
         """The grid op's and the particles' inputs for a step of env b starting now."""
         return {"ff": self.ff_recs, "n_ff": self.n_ffs, "env": b, "ff_step": self.substeps_taken - self.ff_base,
-                "col": self.col_recs, "n_col": self.n_col, "con": self._constraint_targets(b)}
+                "col": self.col_recs, "n_col": self.n_col, "con": self._constraint_targets(b), "plan": self.ff_plan,
+                "t0": self.substeps_taken * self.solver.substep_dt}
 
     def _tool_seq(self, n_sub, T, qa):
         """[(n_sub + 1), n_tools, 13] tool states, entry 0 from (pos, vel) T and (quat, ang) qa."""
@@ -320,6 +329,10 @@ class SceneDiffEngine:
         return ex
 
     def _forward_seq(self, seq, n_sub, ring, gpm, gv, keep_grids, tool_seq, fields, actu):
+        """The step's substeps; with Custom force fields, staged (returns each substep's stage inputs
+        when keep_grids, for the backward)."""
+        if fields["plan"] is not None:
+            return self._staged_forward(seq, n_sub, ring, gpm, gv, keep_grids, tool_seq, fields, actu)
         ex = self._extras(tool_seq, fields, actu)
         r = self.lib.mpm_diff_forward_seq_ex(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(),
                                              self.aux.data_ptr(), self.n, int(n_sub), *[t.data_ptr() for t in seq],
@@ -328,7 +341,10 @@ class SceneDiffEngine:
                                              self._s())
         _lib.check(r, None, "mpm_diff_forward_seq_ex")
 
-    def _backward_seq(self, seq, n_sub, gp, gpm, gv, tool_seq, g_tool, fields, actu, g_actu):
+    def _backward_seq(self, seq, n_sub, gp, gpm, gv, tool_seq, g_tool, fields, actu, g_actu, stage_inputs=None):
+        if fields["plan"] is not None:
+            return self._staged_backward(seq, n_sub, gp, gpm, gv, tool_seq, g_tool, fields, actu, g_actu,
+                                         stage_inputs)
         n = self.n
         gmu = torch.zeros(n, device="cuda")
         glam = torch.zeros(n, device="cuda")
@@ -340,6 +356,124 @@ class SceneDiffEngine:
                                               gv.data_ptr(), self.g_grid_v.data_ptr(), self.g_grid_pm.data_ptr(),
                                               self.status.data_ptr(), self._s())
         _lib.check(r, None, "mpm_diff_backward_seq_ex")
+
+    # ---------------------------------------------------------------- Custom force fields (staged)
+    # A Custom field is a torch function of the node velocities: the substep runs in parts
+    # (mpm_diff_substep_stage: P2G, grid stages, G2P) with the function applied between grid stages,
+    # and its transposed Jacobian applied in the adjoint by torch autograd between the stages'
+    # adjoints (mpm_diff_substep_stage_adj).  The velocity each stage and each Custom field began
+    # from is kept for the backward.
+    def _node_pos(self):
+        """[nodes, 3] positions of the dense differentiable grid's nodes ((g + offset) dx in float)."""
+        if getattr(self, "_npos", None) is None:
+            res = [int(r) for r in self.solver.grid_res]
+            g = torch.stack(torch.meshgrid(*[torch.arange(r, device="cuda") for r in res], indexing="ij"), -1)
+            off = torch.as_tensor(np.asarray(self.solver.grid_offset), device="cuda")
+            dx = torch.tensor(self.solver.dx, dtype=torch.float32, device="cuda")
+            self._npos = ((g.reshape(-1, 3) + off).to(torch.float32) * dx).contiguous()
+        return self._npos
+
+    def _custom_apply(self, f, grid_v, t):
+        sel = torch.nonzero(grid_v[:, 3] > self.solver._eps).squeeze(1)
+        if sel.numel() == 0:
+            return
+        v = grid_v.index_select(0, sel)[:, :3]
+        with torch.no_grad():
+            acc = f.get_acc(self._node_pos().index_select(0, sel), v.clone(), float(t), -1)
+        acc = torch.as_tensor(acc, dtype=torch.float32, device="cuda").reshape(-1, 3)
+        grid_v[sel, :3] = v + acc * self.solver.substep_dt
+
+    def _custom_vjp(self, f, v_in, g, t):
+        """g (dL/d(node velocity after the field), [nodes, 4]) <- dL/d(before): g + dt J^T g on the
+        nodes with mass; the function's own parameters collect their gradients on the way."""
+        sel = torch.nonzero(v_in[:, 3] > self.solver._eps).squeeze(1)
+        if sel.numel() == 0:
+            return
+        with torch.enable_grad():
+            vin = v_in.index_select(0, sel)[:, :3].clone().requires_grad_(True)
+            acc = f.get_acc(self._node_pos().index_select(0, sel), vin, float(t), -1)
+            acc = torch.as_tensor(acc, dtype=torch.float32, device="cuda").reshape(-1, 3)
+            if acc.requires_grad:
+                torch.autograd.backward([acc], [g.index_select(0, sel)[:, :3] * self.solver.substep_dt])
+        if vin.grad is not None:
+            g[sel, :3] += vin.grad
+
+    def _stage_call(self, adj, ex, k_state, args):
+        """One mpm_diff_substep_stage(_adj) call on state k_state (x, v, C, F, Jp tensors)."""
+        x, v, C, F, Jp = k_state
+        fn = self.lib.mpm_diff_substep_stage_adj if adj else self.lib.mpm_diff_substep_stage
+        r = fn(ctypes.byref(self.cfg), self.mass.data_ptr(), self.kind.data_ptr(), self.aux.data_ptr(), self.n,
+               x.data_ptr(), v.data_ptr(), C.data_ptr(), F.data_ptr(), Jp.data_ptr(), self.mu.data_ptr(),
+               self.lam.data_ptr(), ctypes.byref(ex), *args, self.status.data_ptr(), self._s())
+        _lib.check(r, None, "mpm_diff_substep_stage_adj" if adj else "mpm_diff_substep_stage")
+
+    def _tool_ptr(self, tool_seq, k):
+        nt = len(self.tools)
+        return tool_seq[k].data_ptr() if nt else None
+
+    def _staged_forward(self, seq, n_sub, ring, gpm, gv, keep, tool_seq, fields, actu):
+        plan = fields["plan"]
+        dt = self.solver.substep_dt
+        kept = []
+        for k in range(n_sub):
+            a, b = k % ring, (k + 1) % ring
+            cur = [t[a] for t in seq]
+            nxt = [t[b] for t in seq]
+            pm, vel = (gpm[k], gv[k]) if keep else (gpm, gv)
+            ex = self._extras(tool_seq, dict(fields, ff_step=fields["ff_step"] + k), actu)
+            ex.tool_seq = self._tool_ptr(tool_seq, k)
+            t_k = fields["t0"] + k * dt
+            grids = (pm.data_ptr(), vel.data_ptr())
+            self._stage_call(False, ex, cur, (0, 0, 0, 0, *[u.data_ptr() for u in nxt], *grids))
+            inputs = [None]
+            for idx, item in enumerate(plan):
+                if idx > 0:
+                    inputs.append(vel.clone() if keep else None)
+                if item[0] == "fields":
+                    self._stage_call(False, ex, cur, (1, 1 if idx == 0 else 2, item[1], item[2],
+                                                      *[u.data_ptr() for u in nxt], *grids))
+                else:
+                    self._custom_apply(item[1], vel, t_k)
+            inputs.append(vel.clone() if keep else None)  # the tail's input
+            self._stage_call(False, ex, cur, (1, 3, 0, 0, *[u.data_ptr() for u in nxt], *grids))
+            self._stage_call(False, ex, cur, (2, 0, 0, 0, *[u.data_ptr() for u in nxt], *grids))
+            kept.append(inputs)
+        return kept if keep else None
+
+    def _staged_backward(self, seq, n_sub, gp, gpm, gv, tool_seq, g_tool, fields, actu, g_actu, stage_inputs):
+        plan = fields["plan"]
+        dt = self.solver.substep_dt
+        n = self.n
+        gmu = torch.zeros(n, device="cuda")
+        glam = torch.zeros(n, device="cuda")
+        gpm = gpm.reshape(-1, self.nodes, 4)
+        gv = gv.reshape(-1, self.nodes, 4)
+        cur = 0
+        for k in range(n_sub - 1, -1, -1):
+            g_in, g_out = gp[cur], gp[1 - cur]
+            gi = [g_in[o * n: (o + w) * n] for o, w in zip(_OFFSET, _WIDTH)]
+            go = [g_out[o * n: (o + w) * n] for o, w in zip(_OFFSET, _WIDTH)]
+            state = [t[k] for t in seq]
+            ex = self._extras(tool_seq, dict(fields, ff_step=fields["ff_step"] + k), actu, g_tool, g_actu)
+            ex.tool_seq = self._tool_ptr(tool_seq, k)
+            t_k = fields["t0"] + k * dt
+            inputs = stage_inputs[k]
+            ptrs = (*[u.data_ptr() for u in gi], *[u.data_ptr() for u in go], gmu.data_ptr(), glam.data_ptr(),
+                    gpm[k].data_ptr(), gv[k].data_ptr(), self.g_grid_v.data_ptr(), self.g_grid_pm.data_ptr())
+            self._stage_call(True, ex, state, (2, 0, 0, 0, None, *ptrs))
+            self._stage_call(True, ex, state, (1, 3, 0, 0, inputs[len(plan)].data_ptr(), *ptrs))
+            for idx in range(len(plan) - 1, -1, -1):
+                item = plan[idx]
+                if item[0] == "custom":
+                    self._custom_vjp(item[1], inputs[idx], self.g_grid_v, t_k)
+                elif idx == 0:
+                    self._stage_call(True, ex, state, (1, 1, item[1], item[2], None, *ptrs))
+                else:
+                    self._stage_call(True, ex, state, (1, 2, item[1], item[2], inputs[idx].data_ptr(), *ptrs))
+            self._stage_call(True, ex, state, (0, 0, 0, 0, None, *ptrs))
+            cur = 1 - cur
+        if cur == 1:
+            gp[0].copy_(gp[1])
 
     def _g_tool(self, gT):
         g = torch.zeros((max(1, len(self.tools)), 12), device="cuda")
@@ -379,11 +513,11 @@ class SceneDiffEngine:
         tseq = self._tool_seq(n_sub, st[5], qa)
         gpm = torch.empty((max(1, n_sub), self.nodes, 4), device="cuda")
         gv = torch.empty((max(1, n_sub), self.nodes, 4), device="cuda")
-        self._forward_seq(seq, n_sub, n_sub + 1, gpm, gv, True, tseq, fields, st[6])
+        kept = self._forward_seq(seq, n_sub, n_sub + 1, gpm, gv, True, tseq, fields, st[6])
         gp = self._pack(grads[:5])
         g_tool = self._g_tool(grads[5])
         g_actu = grads[6].float().clone() if grads[6] is not None else torch.zeros(self.n, device="cuda")
-        self._backward_seq(seq, n_sub, gp, gpm, gv, tseq, g_tool, fields, st[6], g_actu)
+        self._backward_seq(seq, n_sub, gp, gpm, gv, tseq, g_tool, fields, st[6], g_actu, kept)
         self.check()
         return (*self._unpack(gp), g_tool[:len(self.tools), :6].clone(), g_actu)
 
@@ -472,17 +606,18 @@ class SceneDiffEngine:
                 tseq = self._tool_seq(n_sub, inputs[b][5], qas[b])
                 gpm = torch.empty((n_sub, self.nodes, 4), device="cuda")
                 gv = torch.empty((n_sub, self.nodes, 4), device="cuda")
-                self._forward_seq(seq, n_sub, n_sub + 1, gpm, gv, True, tseq, fields[b], inputs[b][6])
-                keep.append((seq, gpm, gv, tseq, fields[b], inputs[b][6]))
+                kept = self._forward_seq(seq, n_sub, n_sub + 1, gpm, gv, True, tseq, fields[b], inputs[b][6])
+                keep.append((seq, gpm, gv, tseq, fields[b], inputs[b][6], kept))
             self._seg = (s_i, keep)
         for b in range(self.B):
-            seq, gpm, gv, tseq, fields, actu = self._seg[1][b]
+            seq, gpm, gv, tseq, fields, actu, kept = self._seg[1][b]
             gp = self._pack(self.adj[b][:5])
             g_tool = self._g_tool(self.adj[b][5])
             g_actu = self.adj[b][6]  # the step's actuation adjoint gathers every substep's share
             self._backward_seq([t[k: k + 1].contiguous() for t in seq], 1, gp, gpm[k], gv[k],
-                               tseq[k: k + 2].contiguous(), g_tool, dict(fields, ff_step=fields["ff_step"] + k),
-                               actu, g_actu)
+                               tseq[k: k + 2].contiguous(), g_tool,
+                               dict(fields, ff_step=fields["ff_step"] + k, t0=fields["t0"] + k * self.solver.substep_dt),
+                               actu, g_actu, None if kept is None else kept[k: k + 1])
             self.adj[b] = [*self._unpack(gp), g_tool[:len(self.tools), :6].clone(), g_actu]
         self.cursor -= 1
 

@@ -618,6 +618,32 @@ int mpm_diff_backward_seq_ex(const mpm_scene_config* scene, const float* mass, c
                              const mpm_diff_extras* ex, float* g_seq, float* gmu, float* glam, void* grid_pm,
                              void* grid_v, void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream);
 
+/* A differentiable substep in parts, for scenes with Custom force fields (a user function that acts
+ * on the node velocities between grid stages, as mpm_substep_grid_stage splits the product grid op):
+ * phase 0 clears grid_pm and runs P2G (writing F1, Jp1) and advances the tools (ex->tool_seq holds
+ * this substep's [2][n_tools][13] states, entry 1 written); phase 1 runs grid stage `stage`:
+ * 1 = velocity from grid_pm plus gravity and the fields [ff_begin, ff_end) of ex into grid_v,
+ * 2 = the fields [ff_begin, ff_end) on grid_v, 3 = the tools, colliders and boundary on grid_v;
+ * phase 2 runs G2P from grid_v (writing x1, v1, C1).  ex->ff_step is this substep's counter.
+ * The adjoint runs the parts in reverse: phase 2 clears g_grid_v and writes the G2P adjoint (dL/dx
+ * in gx, dL/d(node velocity) in g_grid_v); phase 1, stage 3 or 2, takes the velocity that stage began
+ * from in vstage and turns g_grid_v into dL/d(that velocity) in place, stage 1 ends in g_grid_pm;
+ * phase 0 runs the tools' chain and the P2G adjoint (adding to gx).  The caller applies each
+ * Custom field's transposed Jacobian to g_grid_v between stages. */
+int mpm_diff_substep_stage(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
+                           int64_t n, const float* x, const float* v, const float* C, const float* F, const float* Jp,
+                           const float* mu, const float* lam, const mpm_diff_extras* ex, int32_t phase, int32_t stage,
+                           int32_t ff_begin, int32_t ff_end, float* x1, float* v1, float* C1, float* F1, float* Jp1,
+                           void* grid_pm, void* grid_v, uint32_t* status, void* stream);
+int mpm_diff_substep_stage_adj(const mpm_scene_config* scene, const float* mass, const int32_t* kind,
+                               const float* aux, int64_t n, const float* x, const float* v, const float* C,
+                               const float* F, const float* Jp, const float* mu, const float* lam,
+                               const mpm_diff_extras* ex, int32_t phase, int32_t stage, int32_t ff_begin,
+                               int32_t ff_end, const void* vstage, const float* gx1, const float* gv1,
+                               const float* gC1, const float* gF1, const float* gJp1, float* gx, float* gv, float* gC,
+                               float* gF, float* gJp, float* gmu, float* glam, void* grid_pm, void* grid_v,
+                               void* g_grid_v, void* g_grid_pm, uint32_t* status, void* stream);
+
 /* ABI version of this header (1). */
 int mpm_version(void);
 

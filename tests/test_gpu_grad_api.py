@@ -290,7 +290,7 @@ def test_differentiable_forward_equals_product_path(gs):
     sp.sim.mpm_solver.destroy()
 
 
-@pytest.mark.parametrize("with_fields", [False, True])
+@pytest.mark.parametrize("with_fields", [False, True, "custom"])
 def test_solver_protocol_gradient_walk_equals_autograd(gs, with_fields):
     """The reference's imperative walk (Scene._backward: add_grad_from_state, then per step in reverse
     substep_post_coupling_grad / substep_pre_coupling_grad per substep and process_input_grad) through
@@ -299,7 +299,11 @@ def test_solver_protocol_gradient_walk_equals_autograd(gs, with_fields):
     steps = 3
 
     def run(imperative):
-        scene, box, water = _scene(gs, box_z=0.165, fields=_field_set(gs) if with_fields else ())
+        if with_fields == "custom":  # a Custom field between two built-in ones: the staged substeps
+            fs = _field_set(gs)[:2] + [gs.force_fields.Custom(lambda p, u, t, i: -2.0 * u + 0.5 * p)]
+        else:
+            fs = _field_set(gs) if with_fields else ()
+        scene, box, water = _scene(gs, box_z=0.165, fields=fs)
         v = torch.tensor([0.2, 0.1, -1.0], device="cuda", requires_grad=True)
         box.set_velocity(v)
         for _ in range(steps):
@@ -703,3 +707,63 @@ def test_env_specific_collider_in_differentiable_mode(gs):
     a[1].mean(0)[2].backward()
     assert torch.isfinite(v.grad).all() and v.grad.abs().max().item() > 0
     sp.sim.mpm_solver.destroy()
+
+
+def test_custom_force_field_gradients_match_fp64_central_differences(gs, oracle):
+    """A Custom force field (a torch function of the node velocities, between a built-in field before
+    it and one after it) in differentiable mode: the substeps run in stages with the function applied
+    between them and its Jacobian taken by torch autograd in the adjoint.  The function is a drag with a
+    learnable coefficient k, so the oracle can run the same field as a built-in Drag: dL/dv0 and dL/dk
+    against FP64 central differences of the oracle (2%), and the forward equals the product path."""
+    ff = gs.force_fields
+    k0 = 3.0
+    k = torch.tensor(k0, device="cuda", requires_grad=True)
+
+    def drag(pos, vel, t, i):
+        return -k * vel - 1.5 * vel.norm(dim=1, keepdim=True) * vel
+
+    def fields(custom_k):
+        fs = [ff.Constant(direction=(1.0, 0.0, 0.0), strength=2.0), ff.Custom(custom_k),
+              ff.Point(strength=-3.0, position=(0.5, 0.5, 0.25), falloff_pow=1.0, flow=2.0)]
+        for f in (fs[0], fs[2]):
+            f.activate()
+        return fs
+
+    scene, box, water = _scene(gs, box_z=0.165, fields=fields(drag))
+    v0 = np.array([0.4, -0.3, -1.5])
+    target = np.array([0.52, 0.47, 0.3])
+    v = torch.tensor(v0, dtype=torch.float32, device="cuda", requires_grad=True)
+    box.set_velocity(v)
+    steps = 3
+    for _ in range(steps):
+        scene.step()
+    pos = box.get_state().pos
+    loss = ((pos[0].mean(0) - torch.tensor(target, dtype=torch.float32, device="cuda")) ** 2).sum()
+    loss.backward()
+    g_v = v.grad.detach().cpu().numpy().astype(np.float64)
+    g_k = float(k.grad)
+
+    sp, bp, _ = _scene(gs, requires_grad=False, box_z=0.165,
+                       fields=fields(lambda p, u, t, i: -k0 * u - 1.5 * u.norm(dim=1, keepdim=True) * u))
+    bp.set_velocity(torch.tensor(v0, dtype=torch.float32, device="cuda"))
+    for _ in range(steps):
+        sp.step()
+    assert (bp.get_state().pos[0] - pos[0].detach()).abs().max().item() <= 1e-4
+    sp.sim.mpm_solver.destroy()
+
+    n_sub = steps * scene.substeps
+    ents = [box, water]
+
+    def L(vb, kv):
+        fs = [ff.Constant(direction=(1.0, 0.0, 0.0), strength=2.0), ff.Drag(linear=kv, quadratic=1.5),
+              ff.Point(strength=-3.0, position=(0.5, 0.5, 0.25), falloff_pow=1.0, flow=2.0)]
+        for f in fs:
+            f.activate()
+        return _oracle_com_loss(oracle, scene, ents, vb, target, n_sub, fs)
+
+    assert abs(loss.item() - L(v0.astype(np.float32).astype(np.float64), k0)) <= 1e-4 * loss.item() + 1e-8
+    eps = 1e-4
+    fd_v = np.array([(L(v0 + eps * np.eye(3)[j], k0) - L(v0 - eps * np.eye(3)[j], k0)) / (2 * eps) for j in range(3)])
+    fd_k = (L(v0, k0 + 1e-3) - L(v0, k0 - 1e-3)) / 2e-3
+    assert np.linalg.norm(g_v - fd_v) <= GRAD_RTOL * np.linalg.norm(fd_v), (g_v, fd_v)
+    assert abs(fd_k) > 1e-6 and abs(g_k - fd_k) <= GRAD_RTOL * abs(fd_k), (g_k, fd_k)
