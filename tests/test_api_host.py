@@ -347,3 +347,20 @@ def test_tool_entity_colliders_inputs_and_sdf(tmp_path):
     assert np.allclose(t._pos, [(0.3, 0.1, 0.28)] * 2) and not t._vel.any()
     c2 = replace_pose(cols[0], np.array([1.0, 2.0, 3.0, 0.0, 0.0, 0.0, 1.0]))
     assert c2.pos == (1.0, 2.0, 3.0) and c2.quat == (0.0, 0.0, 0.0, 1.0) and c2.coup_friction == 8.0
+
+
+def test_add_entity_checks_particles_like_the_reference(monkeypatch):
+    """particle_entity.py:278-302 (and the Nowhere morph's own validation): an entity without
+    particles, or with particles outside the solver boundary (the domain less its safety padding),
+    is refused when it is added."""
+    monkeypatch.setattr(gs, "_initialized", True)
+    monkeypatch.setattr(gs, "EPS", float(np.finfo(np.float32).eps))
+    scene = gs.Scene(sim_options=gs.options.SimOptions(dt=2e-4),
+                     mpm_options=gs.options.MPMOptions(lower_bound=(0, 0, 0), upper_bound=(1, 1, 1)))
+    mat = gs.materials.MPM.Elastic(sampler="regular")
+    with pytest.raises(GenesisException, match="must be positive"):
+        scene.add_entity(material=mat, morph=gs.morphs.Nowhere(n_particles=0))
+    with pytest.raises(GenesisException, match="outside solver boundary"):
+        scene.add_entity(material=mat, morph=gs.morphs.Box(pos=(0.98, 0.5, 0.5), size=(0.1, 0.1, 0.1)))
+    e = scene.add_entity(material=mat, morph=gs.morphs.Box(pos=(0.5, 0.5, 0.5), size=(0.1, 0.1, 0.1)))
+    assert e.n_particles == 1000  # 10 per axis at the default particle size 0.01
