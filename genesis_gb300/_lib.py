@@ -163,6 +163,7 @@ class MpmDiffExtras(ctypes.Structure):
         ("pad1", c_int32),
         ("constraint_stiffness", c_void_p),
         ("constraint_target", c_void_p),
+        ("active", c_void_p),
     ]
 
 

@@ -68,7 +68,12 @@ struct DiffParams {
   // stiffness [n] (0: none) and target [n][3], fixed over the substeps of a call; null: none
   const float* con_k;
   const float* con_t;
+  // particle activity (particles_ng.active; null: all active): an inactive particle takes no part in
+  // P2G and G2P and keeps its state, as mpm_solver.py's p2g / g2p skip it and copy it to f + 1
+  const uint8_t* active;
 };
+
+__device__ __forceinline__ bool d_active(const DiffParams& Q, int64_t i) { return !Q.active || Q.active[i]; }
 
 // The critically damped spring of a constrained particle of real mass m: v' = a v + b x + c with
 // a = 1 - dt 2 sqrt(k m) / m, b = -dt k / m (the reference's dv = dt (-k (x - t) - 2 sqrt(k m) v) / m).
@@ -225,6 +230,12 @@ __global__ void __launch_bounds__(256) k_dp2g(DiffParams Q) {
       C[k] = Q.C[i * 9 + k];
       F[k] = Q.F[i * 9 + k];
     }
+    if (!d_active(Q, i)) {  // carried unchanged (g2p's else branch copies F and Jp)
+      if (Q.F1)
+        for (int k = 0; k < 9; ++k) Q.F1[i * 9 + k] = F[k];
+      if (Q.Jp1) Q.Jp1[i] = Q.Jp[i];
+      continue;
+    }
     Stencil st;
     if (!make_stencil(S, x, st)) {
       atomicOr(Q.status, 2u);
@@ -352,6 +363,14 @@ __global__ void __launch_bounds__(256) k_dg2p(DiffParams Q) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < Q.n; i += (int64_t)gridDim.x * blockDim.x) {
     float x[3];
     for (int d = 0; d < 3; ++d) x[d] = Q.x[i * 3 + d];
+    if (!d_active(Q, i)) {
+      for (int d = 0; d < 3; ++d) {
+        Q.x1[i * 3 + d] = x[d];
+        Q.v1[i * 3 + d] = Q.v[i * 3 + d];
+      }
+      for (int k = 0; k < 9; ++k) Q.C1[i * 9 + k] = Q.C[i * 9 + k];
+      continue;
+    }
     Stencil st;
     if (!make_stencil(S, x, st)) continue;
     float v[3] = {0.f, 0.f, 0.f}, Cn[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -393,6 +412,10 @@ __global__ void __launch_bounds__(256) k_dg2p_adj(DiffParams Q) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < Q.n; i += (int64_t)gridDim.x * blockDim.x) {
     float x[3];
     for (int d = 0; d < 3; ++d) x[d] = Q.x[i * 3 + d];
+    if (!d_active(Q, i)) {  // x1 = x
+      for (int d = 0; d < 3; ++d) Q.gx[i * 3 + d] = Q.gx1[i * 3 + d];
+      continue;
+    }
     Stencil st;
     if (!make_stencil(S, x, st)) {
       for (int d = 0; d < 3; ++d) Q.gx[i * 3 + d] = 0.f;
@@ -634,6 +657,15 @@ __global__ void __launch_bounds__(128) k_dp2g_adj(DiffParams Q) {
       C[k] = Q.C[i * 9 + k];
       F[k] = Q.F[i * 9 + k];
     }
+    if (!d_active(Q, i)) {  // (v1, C1, F1, Jp1) = (v, C, F, Jp); dL/dx already holds dL/dx1
+      for (int d = 0; d < 3; ++d) Q.gv[i * 3 + d] = Q.gv1[i * 3 + d];
+      for (int k = 0; k < 9; ++k) {
+        Q.gC[i * 9 + k] = Q.gC1[i * 9 + k];
+        Q.gF[i * 9 + k] = Q.gF1 ? Q.gF1[i * 9 + k] : 0.f;
+      }
+      if (Q.gJp) Q.gJp[i] = Q.gJp1 ? Q.gJp1[i] : 0.f;
+      continue;
+    }
     Stencil st;
     if (!make_stencil(S, x, st)) {
       for (int d = 0; d < 3; ++d) Q.gv[i * 3 + d] = 0.f;
@@ -847,6 +879,7 @@ struct DiffMuscle {
   float* g_actu;
   const float* con_k;
   const float* con_t;
+  const uint8_t* active;
 };
 
 // The fields of substep k of a sequence that starts at the fields' substep counter ff->step.
@@ -889,6 +922,7 @@ int diff_forward(const mpm_scene_config* scene, double rho, int32_t neohookean, 
   Q.tool_f1 = tool_f1;
   if (mus && mus->actu && mus->mdir) Q.actu = mus->actu, Q.mdir = mus->mdir;
   if (mus && mus->con_k && mus->con_t) Q.con_k = mus->con_k, Q.con_t = mus->con_t;
+  if (mus) Q.active = mus->active;
   const int64_t nodes = (int64_t)Q.S.res[0] * Q.S.res[1] * Q.S.res[2];
   cudaStream_t s = (cudaStream_t)stream;
   const int gb = (int)((nodes + 255) / 256 < 8192 ? (nodes + 255) / 256 : 8192);
@@ -942,6 +976,7 @@ int diff_backward(const mpm_scene_config* scene, double rho, int32_t neohookean,
   Q.g_tool = g_tool;
   if (mus && mus->actu && mus->mdir) Q.actu = mus->actu, Q.mdir = mus->mdir, Q.g_actu = mus->g_actu;
   if (mus && mus->con_k && mus->con_t) Q.con_k = mus->con_k, Q.con_t = mus->con_t;
+  if (mus) Q.active = mus->active;
   const int64_t nodes = (int64_t)Q.S.res[0] * Q.S.res[1] * Q.S.res[2];
   cudaStream_t s = (cudaStream_t)stream;
   const int gb = (int)((nodes + 255) / 256 < 8192 ? (nodes + 255) / 256 : 8192);
@@ -1092,6 +1127,7 @@ int diff_extras(const mpm_diff_extras* ex, DiffToolDev* td, DiffFields& ff, Diff
   if ((ex->constraint_stiffness == nullptr) != (ex->constraint_target == nullptr)) return MPM_ERR_BAD_ARG;
   mus.con_k = ex->constraint_stiffness;
   mus.con_t = ex->constraint_target;
+  mus.active = ex->active;
   if (ex->n_colliders < 0 || ex->n_colliders > MPM_DIFF_MAX_COLLIDERS || (ex->n_colliders > 0 && !ex->colliders))
     return MPM_ERR_BAD_ARG;
   cc.n = ex->n_colliders;

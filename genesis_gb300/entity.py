@@ -293,8 +293,12 @@ class MPMEntity:
     def process_input(self, in_backward=False):
         diff = self._solver._diff
         if diff is not None:  # differentiable mode: the targets enter the torch state (their grads flow back)
-            if self._tgt["act"] is not None:
-                raise GenesisException("Activation changes are not supported in differentiable mode.")
+            if self._tgt["act"] is not None:  # activity: a constant of the steps to come
+                a, envs_idx = self._tgt["act"]
+                a = torch.as_tensor(a, device="cuda")
+                if a.ndim == 0:
+                    a = a.reshape(1).expand(self._n_particles)
+                diff.set_active(self._particle_start, self._n_particles, a == ACTIVE, self._envs(envs_idx))
             for key in ("pos", "vel", "actu"):  # positions first: setting positions resets velocities
                 if self._tgt.get(key) is not None:
                     val, envs_idx = self._tgt[key]

@@ -160,6 +160,9 @@ class SceneDiffEngine:
         self.con_link = [torch.full((n,), -1, dtype=torch.long, device="cuda") for _ in range(B)]
         self.con_local = [torch.zeros((n, 3), device="cuda") for _ in range(B)]
         self.has_con = False
+        # particle activity (entity.set_active): a constant of each step, not differentiated
+        self.active = [torch.ones(n, dtype=torch.uint8, device="cuda") for _ in range(B)]
+        self.has_inactive = False
         self.states = [(x0.clone(), torch.zeros((n, 3), device=dev), torch.zeros((n, 3, 3), device=dev),
                         eye.repeat(n, 1, 1), self.Jp0.clone(), self.T0.clone(), torch.zeros(n, device=dev))
                        for _ in range(B)]
@@ -276,6 +279,7 @@ class SceneDiffEngine:
         """The grid op's and the particles' inputs for a step of env b starting now."""
         return {"ff": self.ff_recs, "n_ff": self.n_ffs, "env": b, "ff_step": self.substeps_taken - self.ff_base,
                 "col": self.col_recs, "n_col": self.n_col, "con": self._constraint_targets(b), "plan": self.ff_plan,
+                "active": self.active[b].clone() if self.has_inactive else None,
                 "t0": self.substeps_taken * self.solver.substep_dt}
 
     def _tool_seq(self, n_sub, T, qa):
@@ -322,6 +326,8 @@ class SceneDiffEngine:
         if fields["con"] is not None:
             ex.constraint_stiffness = fields["con"][0].data_ptr()
             ex.constraint_target = fields["con"][1].data_ptr()
+        if fields.get("active") is not None:
+            ex.active = fields["active"].data_ptr()
         if self.has_muscle:
             ex.actu = actu.data_ptr()
             ex.muscle_dir = self.mdir.data_ptr()
@@ -741,6 +747,14 @@ class SceneDiffEngine:
             self.queried_tools.clear()
             self.adj = None
             self._seg = None
+
+    def set_active(self, start: int, count: int, values, envs) -> None:
+        """Activity of particles [start, start+count) in envs (values broadcast to [len(envs), count]);
+        from the next step on, inactive particles keep their state."""
+        vals = torch.broadcast_to(torch.as_tensor(values, device="cuda").to(torch.uint8), (len(envs), count))
+        for i, b in enumerate(envs):
+            self.active[b][start: start + count] = vals[i]
+        self.has_inactive = any(bool((a == 0).any()) for a in self.active)
 
     def set_muscle_direction(self, start: int, count: int, dirs: torch.Tensor) -> None:
         """Fibre directions [count, 3] of particles [start, start+count) (constants of the steps to come)."""

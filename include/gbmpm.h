@@ -583,6 +583,8 @@ int mpm_diff_backward_seq_tools(const mpm_scene_config* scene, const float* mass
  *   constraint_stiffness [n] (0: unconstrained) and constraint_target [n][3] device arrays, both or
  *   neither, fixed over the call (the targets the links' poses give); the backward carries dL/d(x, v)
  *   through the spring's velocity update.
+ * - particle activity: active [n] device uint8 (NULL: all active); an inactive particle takes no
+ *   part in P2G and G2P and keeps its state (mpm_solver.py p2g / g2p), its adjoint passes through.
  * Kinds 7 and 8 are ElastoPlastic (elasto_plastic.py:44-71) with clamped principal stretches
  * (aux = 1 - yield_lower, 1 + yield_higher) and with von Mises yield (aux[0] = yield stress / (2 mu)).
  * The backward needs the same record contents as the forward it reverses. */
@@ -607,6 +609,7 @@ typedef struct mpm_diff_extras {
   int32_t pad1;
   const float* constraint_stiffness;
   const float* constraint_target;
+  const uint8_t* active;
 } mpm_diff_extras;
 int mpm_diff_forward_seq_ex(const mpm_scene_config* scene, const float* mass, const int32_t* kind, const float* aux,
                             int64_t n, int32_t n_sub, float* x_seq, float* v_seq, float* C_seq, float* F_seq,

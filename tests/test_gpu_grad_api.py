@@ -767,3 +767,62 @@ def test_custom_force_field_gradients_match_fp64_central_differences(gs, oracle)
     fd_k = (L(v0, k0 + 1e-3) - L(v0, k0 - 1e-3)) / 2e-3
     assert np.linalg.norm(g_v - fd_v) <= GRAD_RTOL * np.linalg.norm(fd_v), (g_v, fd_v)
     assert abs(fd_k) > 1e-6 and abs(g_k - fd_k) <= GRAD_RTOL * abs(fd_k), (g_k, fd_k)
+
+
+def test_activity_changes_in_differentiable_mode(gs, oracle):
+    """entity.deactivate() between steps in differentiable mode: the Liquid block stops taking part
+    (mpm_solver.py p2g / g2p skip an inactive particle and keep its state), the forward equals the
+    product path with the same activity (1e-4 m), and dL/dv0 of the box matches FP64 central
+    differences of the oracle with the same activity per substep (2%)."""
+    v0 = np.array([0.4, -0.3, -1.5])
+    target = np.array([0.52, 0.47, 0.3])
+    steps = 4
+
+    def run(requires_grad, vel):
+        scene, box, water = _scene(gs, requires_grad=requires_grad, box_z=0.165)
+        box.set_velocity(vel)
+        water.set_velocity(torch.tensor([-2.0, 0.0, 0.0], device="cuda"))
+        for s_i in range(steps):
+            if s_i == 1:
+                water.deactivate()
+            scene.step()
+        return scene, box, water
+
+    v = torch.tensor(v0, dtype=torch.float32, device="cuda", requires_grad=True)
+    scene, box, water = run(True, v)
+    pos = box.get_state().pos
+    wpos = water.get_state().pos
+    loss = ((pos[0].mean(0) - torch.tensor(target, dtype=torch.float32, device="cuda")) ** 2).sum()
+    loss.backward()
+    g = v.grad.detach().cpu().numpy().astype(np.float64)
+    sp, bp, wp = run(False, torch.tensor(v0, dtype=torch.float32, device="cuda"))
+    assert (bp.get_state().pos[0] - pos[0].detach()).abs().max().item() <= 1e-4
+    assert (wp.get_state().pos[0] - wpos[0].detach()).abs().max().item() <= 1e-4
+    sp.sim.mpm_solver.destroy()
+
+    solver = scene.sim.mpm_solver
+    ents = [box, water]
+    oms = [oracle.from_c_material(m.to_c(0)) for m in solver._unique_materials()]
+    x0 = np.concatenate([e.init_particles.astype(np.float32).astype(np.float64) for e in ents])
+    n, nb = len(x0), box.n_particles
+    sc = oracle.make_scene(solver.substep_dt, gravity=tuple(solver.gravity[0]), lower_bound=tuple(solver.lower_bound),
+                           upper_bound=tuple(solver.upper_bound), grid_density=solver.grid_density,
+                           particle_size=solver.particle_size)
+
+    def L(vb):
+        vel = np.zeros((n, 3))
+        vel[:nb] = vb
+        vel[nb:] = (-2.0, 0.0, 0.0)
+        st = dict(pos=x0, vel=vel, C=np.zeros((n, 3, 3)), F=np.tile(np.eye(3), (n, 1, 1)),
+                  Jp=np.concatenate([np.full(e.n_particles, float(e.material._default_Jp)) for e in ents]),
+                  mat=np.concatenate([np.full(e.n_particles, e.material.idx, np.int32) for e in ents]),
+                  active=np.ones(n, bool))
+        st, _, _ = oracle.run(sc, oms, st, scene.substeps)
+        st["active"] = np.concatenate([np.ones(nb, bool), np.zeros(n - nb, bool)])
+        st, _, _ = oracle.run(sc, oms, st, (steps - 1) * scene.substeps)
+        return float(((st["pos"][:nb].mean(0) - target) ** 2).sum())
+
+    assert abs(loss.item() - L(v0.astype(np.float32).astype(np.float64))) <= 1e-4 * loss.item() + 1e-8
+    eps = 1e-4
+    fd = np.array([(L(v0 + eps * np.eye(3)[j]) - L(v0 - eps * np.eye(3)[j])) / (2 * eps) for j in range(3)])
+    assert np.linalg.norm(g - fd) <= GRAD_RTOL * np.linalg.norm(fd), (g, fd)
