@@ -6,32 +6,28 @@ steps in reverse (Simulator._step_grad: load_ckpt, re-simulate the step, then
 substep_post_coupling_grad / couple_grad / substep_pre_coupling_grad per substep,
 process_input_grad), scene.py:1365-1379, simulator.py:298-404, mpm_solver.py:517-670.
 
-Here the same user-facing flow (entity.set_position / set_velocity with tensors that require
-grad, scene.step(), scene.get_state() / entity.get_state(), loss.backward()) runs on torch
-autograd: the MPM state of every env is a set of torch tensors, and every scene.step() is one
-autograd node per env whose forward runs the step's substeps with the libgbmpm differentiable
-kernels (mpm_diff_forward_seq_pp) and whose backward re-simulates the step from its input state
-(the checkpoint, as the reference's save_ckpt / load_ckpt keep one per step) and runs the
-hand-written adjoint substeps in reverse (mpm_diff_backward_seq_pp).  Entity inputs set between
-steps enter the state through differentiable torch ops, so their gradients arrive where the
-reference's process_input_grad puts them.
+Here the same user-facing flow (entity.set_position / set_velocity / set_actuation and
+tool.set_position / set_velocity with tensors that require grad, scene.step(), get_state(),
+loss.backward()) runs on torch autograd.  The state of every env is a set of torch tensors:
+particles (x, v, C, F, Jp), the tools' position and velocity ([n_tools, 6]) and the Muscle
+actuation ([N], constant over a step).  Every scene.step() is one autograd node per env whose
+forward runs the step's substeps with the libgbmpm differentiable kernels
+(mpm_diff_forward_seq_ex) and whose backward re-simulates the step from its input state (the
+checkpoint, as the reference's save_ckpt / load_ckpt keep one per step) and runs the hand-written
+adjoint substeps in reverse (mpm_diff_backward_seq_ex).  Entity inputs set between steps enter the
+state through differentiable torch ops, so their gradients arrive where the reference's
+process_input_grad puts them; the Solver protocol's *_grad members walk the same adjoint
+imperatively.
 
-Materials: Elastic (corotated or neo-Hookean), Liquid, Sand, Snow, ElastoPlastic (clamped or von
-Mises) and Muscle, any mix of entities; particle masses, Lame parameters and plasticity constants
-per particle, Jp part of the differentiated state.  Muscle actuation (entity.set_actuation /
-set_particles_actu) is part of each env's state too: constant over a step, it enters the stress of
-every substep, and its gradient reaches the tensors passed in (the reference's
-_set_particles_actu_grad).  Tool entities (tool_entity/) are part of the step: each env's state also
-holds every tool's position and velocity ([n_tools, 6], differentiated through Mesh.collide in the
-grid op and ToolEntity.advect) and, as
-plain tensors, its orientation and angular velocity.  Built-in force fields act in the
-differentiable grid op (mpm_diff_forward_seq_ex / mpm_diff_backward_seq_ex), each step with the
-fields as they were when it ran, and so do kinematic rigid colliders (solver.set_colliders: the
-shapes of the product grid op, poses fixed within a step, no reaction forces in this mode) and
-particle constraints (entity.set_particle_constraints: springs towards targets that follow the
-links' poses of solver.set_link_poses, differentiated in the particle state).  Custom force fields (a torch function here) run between grid stages
-of the substep (mpm_diff_substep_stage), their Jacobian taken by torch autograd in the adjoint.  As
-in the reference, CPIC and emitters are rejected in this mode.
+What a step differentiates: every MPM material (Elastic corotated or neo-Hookean, Liquid, Sand,
+Snow, ElastoPlastic clamped or von Mises, Muscle; any mix, per-particle constants); tool entities
+(Mesh.collide in the grid op and ToolEntity.advect; orientation and angular velocity are carried
+as plain tensors); built-in force fields; kinematic rigid colliders (solver.set_colliders, poses
+fixed within a step, no reaction forces in this mode); particle constraints (springs towards the
+links' poses of solver.set_link_poses); and Custom force fields (a torch function, run between
+grid stages of the substep with mpm_diff_substep_stage, its Jacobian taken by torch autograd in
+the adjoint).  Each step keeps the fields, colliders, constraint targets and particle activity it
+ran with.  As in the reference, CPIC and emitters are rejected in this mode.
 """
 
 from __future__ import annotations
