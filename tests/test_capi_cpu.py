@@ -157,3 +157,29 @@ def test_differentiable_extras_are_validated_on_the_host(lib):
     for i, ex in enumerate(cases):
         assert fwd(ex) == 1, i
         assert bwd(ex) == 1, i
+
+
+def test_staged_differentiable_substep_arguments_are_validated_on_the_host(lib):
+    """mpm_diff_substep_stage / _adj reject a phase or stage out of range, a field range outside the
+    record and a stage adjoint without the velocity it began from, before any CUDA call."""
+    from genesis_gb300 import _lib
+
+    cfg = _cfg(n=0)
+    buf = (ctypes.c_float * 64)()
+    p = ctypes.cast(buf, ctypes.c_void_p)
+    ex = _lib.MpmDiffExtras()
+
+    def fwd(phase, stage, b=0, e=0):
+        return lib.mpm_diff_substep_stage(ctypes.byref(cfg), p, p, p, 0, p, p, p, p, p, p, p, ctypes.byref(ex),
+                                          phase, stage, b, e, p, p, p, p, p, p, p, p, None)
+
+    def adj(phase, stage, vstage, b=0, e=0):
+        return lib.mpm_diff_substep_stage_adj(ctypes.byref(cfg), p, p, p, 0, p, p, p, p, p, p, p, ctypes.byref(ex),
+                                              phase, stage, b, e, vstage, p, p, p, p, p, p, p, p, p, p, p, p,
+                                              p, p, p, p, p, None)
+
+    assert fwd(3, 0) == 1 and fwd(-1, 0) == 1
+    assert fwd(1, 0) == 1 and fwd(1, 4) == 1
+    assert fwd(1, 1, 0, 1) == 1  # the record holds no field
+    assert adj(1, 2, None) == 1 and adj(1, 3, None) == 1
+    assert adj(1, 2, p, 2, 1) == 1
