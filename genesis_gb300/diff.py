@@ -6,7 +6,8 @@ the final particle positions; its backward runs the adjoint substeps of libgbmpm
 (mpm_diff_backward) in reverse.  Memory follows checkpoint-and-recompute like Genesis's
 differentiable mode (simulator.py:372-404): the forward keeps the particle state only every
 `ckpt_every` substeps; the backward re-simulates each segment from its checkpoint, keeping
-that segment's states, and then walks it backwards.
+that segment's states, and then walks it backwards.  The last segment's states and grids are kept
+by the forward itself when they fit the same memory budget, so its re-simulation is skipped.
 """
 
 from __future__ import annotations
@@ -180,14 +181,19 @@ class _Advance(torch.autograd.Function):
         mu_d, lam_d = mu.detach().float().contiguous(), lam.detach().float().contiguous()
         st = (x, v, C, F)
         ckpts = {}
+        kept = None  # the last segment's states and grids, kept from this forward when they fit
         s = 0
         while s < n_substeps:
             seg = min(sim.ckpt_every, n_substeps - s)
             ckpts[s] = tuple(t.clone() for t in st)
-            st = sim.forward_segment(st, mu_d, lam_d, seg)
+            if s + seg == n_substeps and sim.segment_bytes(x.shape[0], seg) <= sim.grid_budget_bytes():
+                kept = sim.forward_segment(st, mu_d, lam_d, seg, keep=True)
+                st = tuple(t[seg].clone() for t in kept[0])
+            else:
+                st = sim.forward_segment(st, mu_d, lam_d, seg)
             s += seg
         sim.check()
-        ctx.sim, ctx.n_substeps, ctx.ckpts = sim, n_substeps, ckpts
+        ctx.sim, ctx.n_substeps, ctx.ckpts, ctx.kept = sim, n_substeps, ckpts, kept
         ctx.save_for_backward(mu_d, lam_d)
         if n_substeps == 0:
             st = tuple(t.clone() for t in st)
@@ -218,7 +224,11 @@ class _Advance(torch.autograd.Function):
             for seg_i in range(len(starts) - 1, -1, -1):
                 s0 = starts[seg_i]
                 s1 = starts[seg_i + 1] if seg_i + 1 < len(starts) else n_sub
-                states, grids = sim.forward_segment(ctx.ckpts[s0], mu, lam, s1 - s0, keep=True)
+                if s1 == n_sub and ctx.kept is not None:  # the forward kept the last segment
+                    states, grids = ctx.kept
+                    ctx.kept = None
+                else:
+                    states, grids = sim.forward_segment(ctx.ckpts[s0], mu, lam, s1 - s0, keep=True)
                 sim.backward_segment(states, grids, mu, lam, gp, gmu, glam, s1 - s0)
                 del states, grids
             sim.check()
