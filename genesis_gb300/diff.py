@@ -33,10 +33,12 @@ MATERIALS = {"elastic": 0, "neohookean": 1, "liquid": 2}
 class DifferentiableMPM:
     def __init__(self, scene_cfg: "_lib.MpmSceneConfig", nu: float = 0.2, rho: float = 1000.0,
                  neohookean: bool = False, ckpt_every: int = 160, material: str | None = None,
-                 viscous: bool = False):
+                 viscous: bool = False, keep_segments: bool = False):
         """material: "elastic" (corotated; "neohookean" or neohookean=True for the neo-Hookean
         model) or "liquid" (liquid.py: mu = 0 unless viscous, F reset to J^(1/3) I every substep).
-        Young's modulus E is per particle; nu and rho are shared."""
+        Young's modulus E is per particle; nu and rho are shared.  keep_segments: the forward keeps
+        every segment's states and grids while they fit a quarter of the free device memory (the
+        backward then re-simulates none of them; memory for time), instead of the last one only."""
         self.lib = _lib.load()
         self.cfg = scene_cfg
         self.nu = float(nu)
@@ -48,6 +50,7 @@ class DifferentiableMPM:
         self.viscous = bool(viscous)
         self.neo = MATERIALS[name]
         self.ckpt_every = int(ckpt_every)
+        self.keep_segments = bool(keep_segments)
         d = scene_cfg.grid_density
         res = [int(round(d * scene_cfg.upper_bound[k]) - round(d * scene_cfg.lower_bound[k]) + 1) for k in range(3)]
         self.nodes = res[0] * res[1] * res[2]
@@ -181,14 +184,15 @@ class _Advance(torch.autograd.Function):
         mu_d, lam_d = mu.detach().float().contiguous(), lam.detach().float().contiguous()
         st = (x, v, C, F)
         ckpts = {}
-        kept = None  # the last segment's states and grids, kept from this forward when they fit
-        s = 0
+        kept = {}  # segments whose states and grids this forward keeps (the last one, or all with
+        s = 0      # keep_segments), each while it fits the memory budget
         while s < n_substeps:
             seg = min(sim.ckpt_every, n_substeps - s)
             ckpts[s] = tuple(t.clone() for t in st)
-            if s + seg == n_substeps and sim.segment_bytes(x.shape[0], seg) <= sim.grid_budget_bytes():
-                kept = sim.forward_segment(st, mu_d, lam_d, seg, keep=True)
-                st = tuple(t[seg].clone() for t in kept[0])
+            if ((sim.keep_segments or s + seg == n_substeps)
+                    and sim.segment_bytes(x.shape[0], seg) <= sim.grid_budget_bytes()):
+                kept[s] = sim.forward_segment(st, mu_d, lam_d, seg, keep=True)
+                st = tuple(t[seg].clone() for t in kept[s][0])
             else:
                 st = sim.forward_segment(st, mu_d, lam_d, seg)
             s += seg
@@ -224,9 +228,8 @@ class _Advance(torch.autograd.Function):
             for seg_i in range(len(starts) - 1, -1, -1):
                 s0 = starts[seg_i]
                 s1 = starts[seg_i + 1] if seg_i + 1 < len(starts) else n_sub
-                if s1 == n_sub and ctx.kept is not None:  # the forward kept the last segment
-                    states, grids = ctx.kept
-                    ctx.kept = None
+                if s0 in ctx.kept:  # kept by the forward
+                    states, grids = ctx.kept.pop(s0)
                 else:
                     states, grids = sim.forward_segment(ctx.ckpts[s0], mu, lam, s1 - s0, keep=True)
                 sim.backward_segment(states, grids, mu, lam, gp, gmu, glam, s1 - s0)

@@ -142,6 +142,11 @@ def test_checkpointing_does_not_change_gradients(oracle):
     _, _, gvb, gEb = _gpu_loss_and_grads(b, x0, v0, E, target, 32, vfield=vf, proj=pj)
     assert np.allclose(gva, gvb, rtol=1e-3, atol=1e-9 + 1e-4 * np.abs(gvb).max())
     assert np.linalg.norm(gEa - gEb) <= 1e-2 * np.linalg.norm(gEb)
+    # keeping every segment from the forward (no re-simulation in the backward) changes nothing
+    c = DifferentiableMPM(_scene(), ckpt_every=8, keep_segments=True)
+    _, _, gvc, gEc = _gpu_loss_and_grads(c, x0, v0, E, target, 32, vfield=vf, proj=pj)
+    assert np.allclose(gvc, gva, rtol=1e-3, atol=1e-9 + 1e-4 * np.abs(gva).max())
+    assert np.linalg.norm(gEc - gEa) <= 1e-2 * np.linalg.norm(gEa)
 
 
 def _oracle_two_loss(O, x0, v0, E, target, n1, n2, nu=0.2, dt=2e-4, vfield=None, proj=None):
