@@ -771,12 +771,24 @@ def run_diff(steps=64, substeps_per_step=10, ckpt_steps=16, seed=99):
     v0.grad = None
     E.grad = None
     t = _timed(fwd_bwd)
+    g_v0, g_E = v0.grad.tolist(), float(E.grad.norm())
+    # the same rollout keeping every segment's states and grids (the backward re-simulates none)
+    sim.keep_segments = True
+    fwd_bwd()
+    v0.grad = None
+    E.grad = None
+    t_keep = _timed(fwd_bwd)
+    keep_mode = getattr(sim, "last_backward", None)
+    kept, total = getattr(sim, "last_segments", (None, None))
     return {
         "workload": f"elastic cube {n} particles, 97^3 grid, {steps} steps x {substeps_per_step} substeps, "
                     f"checkpoint every {ckpt_steps} steps, grads w.r.t. v0 and per-particle E",
         "n_particles": n, "seconds_fwd_bwd": t, "value": n * n_sub / t, "unit": "particle-substeps/s (fwd+bwd)",
-        "grad_v0": v0.grad.tolist(), "grad_E_norm": float(E.grad.norm()),
-        "backward_mode": getattr(sim, "last_backward", None), "free_device_gb": free_gb,
+        "grad_v0": g_v0, "grad_E_norm": g_E, "backward_mode": getattr(sim, "last_backward", None),
+        "free_device_gb": free_gb,
+        "keep_segments": {"seconds_fwd_bwd": t_keep, "value": n * n_sub / t_keep, "backward_mode": keep_mode,
+                          "segments_kept": kept, "segments": total,
+                          "grad_v0": v0.grad.tolist(), "grad_E_norm": float(E.grad.norm())},
     }
 
 

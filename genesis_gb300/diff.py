@@ -197,6 +197,7 @@ class _Advance(torch.autograd.Function):
                 st = sim.forward_segment(st, mu_d, lam_d, seg)
             s += seg
         sim.check()
+        sim.last_segments = (len(kept), len(ckpts))  # (kept by the forward, all)
         ctx.sim, ctx.n_substeps, ctx.ckpts, ctx.kept = sim, n_substeps, ckpts, kept
         ctx.save_for_backward(mu_d, lam_d)
         if n_substeps == 0:
