@@ -839,11 +839,16 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-forms", action="store_true", help="skip the batched/served form measurements")
     ap.add_argument("--tuning", default="", help="fixed P2G threads,particles per thread,G2P threads (no autotune)")
-    ap.add_argument("--form", default="", choices=["", "served"],
-                    help="diagnostic: run only the saturated served workload (for profiling captures)")
+    ap.add_argument("--form", default="", choices=["", "served", "differentiation"],
+                    help="diagnostic: run only the saturated served workload or the differentiation rollout "
+                         "(for profiling captures)")
+    ap.add_argument("--diff-steps", type=int, default=64, help="steps of the differentiation rollout (--form)")
     args = ap.parse_args()
     if args.form == "served":
         print(json.dumps(run_served_only()))
+        return
+    if args.form == "differentiation":
+        print(json.dumps(run_diff(steps=args.diff_steps)))
         return
     if args.warmup < 3:
         args.warmup = 3
