@@ -149,6 +149,52 @@ def test_checkpointing_does_not_change_gradients(oracle):
     assert np.linalg.norm(gEc - gEa) <= 1e-2 * np.linalg.norm(gEa)
 
 
+def test_memory_budget_fallbacks_do_not_change_gradients(oracle):
+    """The backward's memory-bound modes give the default mode's gradients: a forward that keeps only
+    some segments, a substep-by-substep backward that keeps each re-simulated substep's grid, and one
+    that keeps none (every adjoint substep re-runs its forward).  The memory budget is overridden on
+    the instance to reach each mode at this size."""
+    import __graft_entry__ as g
+
+    g.build()
+    from genesis_gb300.diff import DifferentiableMPM
+
+    x0, v0, E, target = _setup(seed=6)
+    n = len(x0)
+    vf, pj = _shear(x0), _proj(n)
+    ref = DifferentiableMPM(_scene(), ckpt_every=8)
+    _, _, gv_ref, gE_ref = _gpu_loss_and_grads(ref, x0, v0, E, target, 32, vfield=vf, proj=pj)
+    assert ref.last_backward == "segments" and ref.last_segments == (1, 4)
+
+    def check(sim, mode):
+        _, _, gv, gE = _gpu_loss_and_grads(sim, x0, v0, E, target, 32, vfield=vf, proj=pj)
+        assert sim.last_backward == mode
+        assert np.allclose(gv, gv_ref, rtol=1e-3, atol=1e-9 + 1e-4 * np.abs(gv_ref).max())
+        assert np.linalg.norm(gE - gE_ref) <= 1e-2 * np.linalg.norm(gE_ref)
+
+    # the forward asks once per segment (four), the backward once: segments 3 and 4 do not fit
+    part = DifferentiableMPM(_scene(), ckpt_every=8, keep_segments=True)
+    calls = []
+
+    def budget():
+        calls.append(1)
+        return 0 if len(calls) in (3, 4) else 1 << 50
+
+    part.grid_budget_bytes = budget
+    check(part, "segments")
+    assert part.last_segments == (2, 4)
+    # a segment does not fit, its grids do
+    sub = DifferentiableMPM(_scene(), ckpt_every=8)
+    sub.grid_budget_bytes = lambda: sub.segment_bytes(n, 8) - 1
+    assert sub.nodes * 32 * 8 <= sub.segment_bytes(n, 8) - 1
+    check(sub, "substeps")
+    assert sub.last_segments == (0, 4)
+    # nothing fits
+    bare = DifferentiableMPM(_scene(), ckpt_every=8)
+    bare.grid_budget_bytes = lambda: 0
+    check(bare, "substeps")
+
+
 def _oracle_two_loss(O, x0, v0, E, target, n1, n2, nu=0.2, dt=2e-4, vfield=None, proj=None):
     """Loss on the state after n1 substeps plus the loss on the state after n1 + n2 (the oracle
     continues from its own intermediate state)."""
