@@ -218,70 +218,123 @@ __global__ void k_dclear(DiffParams Q, int64_t nodes, float4* buf) {
     buf[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
+// One particle's part of P2G: the material update (F1, Jp1 written), its stencil, A = s P + m C and
+// m v.  False when it scatters nothing (inactive: carried unchanged; outside the grid: flagged).
+__device__ __forceinline__ bool dp2g_particle(const DiffParams& Q, int64_t i, Stencil& st, float* A, float* mv,
+                                              float& mass) {
+  const SceneDev& S = Q.S;
+  float x[3], v[3], C[9], F[9];
+  for (int d = 0; d < 3; ++d) {
+    x[d] = Q.x[i * 3 + d];
+    v[d] = Q.v[i * 3 + d];
+  }
+  for (int k = 0; k < 9; ++k) {
+    C[k] = Q.C[i * 9 + k];
+    F[k] = Q.F[i * 9 + k];
+  }
+  if (!d_active(Q, i)) {  // carried unchanged (g2p's else branch copies F and Jp)
+    if (Q.F1)
+      for (int k = 0; k < 9; ++k) Q.F1[i * 9 + k] = F[k];
+    if (Q.Jp1) Q.Jp1[i] = Q.Jp[i];
+    return false;
+  }
+  if (!make_stencil(S, x, st)) {
+    atomicOr(Q.status, 2u);
+    return false;
+  }
+  mass = p_mass(Q, i);
+  const int kind = p_kind(Q, i);
+  float Ft[9], U[9], sig[3], V[9], P[9];
+  f_tmp(C, F, S.dt, Ft);
+  svd_f32(Ft, U, sig, V);
+  const bool plastic = diff_plastic(kind);
+  if (plastic) {  // sand.py:47-84, snow.py:56-74, elasto_plastic.py:44-71 (the product path's code)
+    const MaterialDev M = plastic_material(kind, Q.mu[i], Q.lam[i], Q.aux + i * 2);
+    const float mdir[3] = {0.f, 0.f, 1.f};
+    float Fn[9], Jpn;
+    material_update<float>(M, Ft, U, sig, V, Q.Jp[i], 0.f, mdir, S.eps, Fn, Jpn, P);
+    if (Q.F1)
+      for (int k = 0; k < 9; ++k) Q.F1[i * 9 + k] = Fn[k];
+    if (Q.Jp1) Q.Jp1[i] = Jpn;
+  } else {
+    elastic_stress(Ft, Q.mu[i], Q.lam[i], kind == DIFF_NEOHOOKEAN || kind == DIFF_MUSCLE_NEOHOOKEAN, U, sig, V, P);
+    if (diff_muscle(kind) && Q.actu) muscle_stress(Ft, Q.mdir + i * 3, Q.aux[i * 2], Q.actu[i], P);
+    if (Q.Jp1) Q.Jp1[i] = Q.Jp[i];
+  }
+  if (Q.F1 && !plastic) {
+    if (kind == DIFF_LIQUID) {  // liquid.py:36-40: F_new = J^(1/3) I
+      const float j3 = powf(sig[0] * sig[1] * sig[2], 1.f / 3.f);
+      for (int k = 0; k < 9; ++k) Q.F1[i * 9 + k] = (k % 4 == 0) ? j3 : 0.f;
+    } else {
+      for (int k = 0; k < 9; ++k) Q.F1[i * 9 + k] = Ft[k];
+    }
+  }
+  for (int k = 0; k < 9; ++k) A[k] = S.stress_scale * P[k] + mass * C[k];
+  for (int d = 0; d < 3; ++d) mv[d] = mass * v[d];
+  return true;
+}
+
+// P2G with the float4 global atomics of each node summed first over the lanes of a warp whose
+// particles share a stencil origin (neighbours in memory often share a cell): the group's lowest
+// lane adds the sum.  The sum is a tree over the group's ranks: in round r every lane adds the value
+// of its next remaining peer above (nxt[r] = that lane + 1, 0 for none), then the lanes whose rank
+// has bit r set drop out; five rounds cover a group of 32.
 __global__ void __launch_bounds__(256) k_dp2g(DiffParams Q) {
   const SceneDev& S = Q.S;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < Q.n; i += (int64_t)gridDim.x * blockDim.x) {
-    float x[3], v[3], C[9], F[9];
-    for (int d = 0; d < 3; ++d) {
-      x[d] = Q.x[i * 3 + d];
-      v[d] = Q.v[i * 3 + d];
-    }
-    for (int k = 0; k < 9; ++k) {
-      C[k] = Q.C[i * 9 + k];
-      F[k] = Q.F[i * 9 + k];
-    }
-    if (!d_active(Q, i)) {  // carried unchanged (g2p's else branch copies F and Jp)
-      if (Q.F1)
-        for (int k = 0; k < 9; ++k) Q.F1[i * 9 + k] = F[k];
-      if (Q.Jp1) Q.Jp1[i] = Q.Jp[i];
-      continue;
-    }
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  // the trip count is the same for the whole warp (blockDim and the stride are multiples of 32),
+  // so every lane reaches the warp-wide operations below
+  for (int64_t w0 = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); w0 < Q.n;
+       w0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = w0 + lane;
     Stencil st;
-    if (!make_stencil(S, x, st)) {
-      atomicOr(Q.status, 2u);
-      continue;
-    }
-    const float mass = p_mass(Q, i);
-    const int kind = p_kind(Q, i);
-    float Ft[9], U[9], sig[3], V[9], P[9];
-    f_tmp(C, F, S.dt, Ft);
-    svd_f32(Ft, U, sig, V);
-    const bool plastic = diff_plastic(kind);
-    if (plastic) {  // sand.py:47-84, snow.py:56-74, elasto_plastic.py:44-71 (the product path's code)
-      const MaterialDev M = plastic_material(kind, Q.mu[i], Q.lam[i], Q.aux + i * 2);
-      const float mdir[3] = {0.f, 0.f, 1.f};
-      float Fn[9], Jpn;
-      material_update<float>(M, Ft, U, sig, V, Q.Jp[i], 0.f, mdir, S.eps, Fn, Jpn, P);
-      if (Q.F1)
-        for (int k = 0; k < 9; ++k) Q.F1[i * 9 + k] = Fn[k];
-      if (Q.Jp1) Q.Jp1[i] = Jpn;
-    } else {
-      elastic_stress(Ft, Q.mu[i], Q.lam[i], kind == DIFF_NEOHOOKEAN || kind == DIFF_MUSCLE_NEOHOOKEAN, U, sig, V, P);
-      if (diff_muscle(kind) && Q.actu) muscle_stress(Ft, Q.mdir + i * 3, Q.aux[i * 2], Q.actu[i], P);
-      if (Q.Jp1) Q.Jp1[i] = Q.Jp[i];
-    }
-    if (Q.F1 && !plastic) {
-      if (kind == DIFF_LIQUID) {  // liquid.py:36-40: F_new = J^(1/3) I
-        const float j3 = powf(sig[0] * sig[1] * sig[2], 1.f / 3.f);
-        for (int k = 0; k < 9; ++k) Q.F1[i * 9 + k] = (k % 4 == 0) ? j3 : 0.f;
-      } else {
-        for (int k = 0; k < 9; ++k) Q.F1[i * 9 + k] = Ft[k];
+    float A[9], mv[3], mass = 0.f;
+    const bool has = i < Q.n && dp2g_particle(Q, i, st, A, mv, mass);
+    const unsigned long long key =
+        has ? (unsigned long long)didx(S, st.b[0], st.b[1], st.b[2]) : ~0ull - (unsigned long long)lane;
+    const unsigned peers = __match_any_sync(full, key);
+    const bool lead = (peers & ((1u << lane) - 1u)) == 0u;
+    unsigned above = peers & (0xfffffffeu << lane);
+    unsigned rank = __popc(peers & ((1u << lane) - 1u));
+    int nxt[5];
+    int rounds = 0;
+#pragma unroll
+    for (int r = 0; r < 5; ++r) {
+      nxt[r] = 0;
+      if (__any_sync(full, above != 0u)) {
+        nxt[r] = __ffs(above);
+        above &= ~__ballot_sync(full, (rank & 1u) != 0u);
+        rank >>= 1;
+        rounds = r + 1;
       }
     }
-    float A[9];
-    for (int k = 0; k < 9; ++k) A[k] = S.stress_scale * P[k] + mass * C[k];
+#pragma unroll
     for (int ox = 0; ox < 3; ++ox)
+#pragma unroll
       for (int oy = 0; oy < 3; ++oy)
+#pragma unroll
         for (int oz = 0; oz < 3; ++oz) {
-          const float wt = st.w[0][ox] * st.w[1][oy] * st.w[2][oz];
-          const float dp[3] = {((float)ox - st.fx[0]) * S.dx, ((float)oy - st.fx[1]) * S.dx,
-                               ((float)oz - st.fx[2]) * S.dx};
-          float4 g;
-          g.x = wt * (mass * v[0] + A[0] * dp[0] + A[1] * dp[1] + A[2] * dp[2]);
-          g.y = wt * (mass * v[1] + A[3] * dp[0] + A[4] * dp[1] + A[5] * dp[2]);
-          g.z = wt * (mass * v[2] + A[6] * dp[0] + A[7] * dp[1] + A[8] * dp[2]);
-          g.w = wt * mass;
-          atomicAdd(&Q.pm[didx(S, st.b[0] + ox, st.b[1] + oy, st.b[2] + oz)], g);
+          float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (has) {
+            const float wt = st.w[0][ox] * st.w[1][oy] * st.w[2][oz];
+            const float dp[3] = {((float)ox - st.fx[0]) * S.dx, ((float)oy - st.fx[1]) * S.dx,
+                                 ((float)oz - st.fx[2]) * S.dx};
+            g.x = wt * (mv[0] + A[0] * dp[0] + A[1] * dp[1] + A[2] * dp[2]);
+            g.y = wt * (mv[1] + A[3] * dp[0] + A[4] * dp[1] + A[5] * dp[2]);
+            g.z = wt * (mv[2] + A[6] * dp[0] + A[7] * dp[1] + A[8] * dp[2]);
+            g.w = wt * mass;
+          }
+#pragma unroll
+          for (int r = 0; r < 5; ++r) {
+            if (r < rounds) {  // the same for the whole warp
+              const int src = nxt[r] ? nxt[r] - 1 : lane;
+              const float tx = __shfl_sync(full, g.x, src), ty = __shfl_sync(full, g.y, src);
+              const float tz = __shfl_sync(full, g.z, src), tw = __shfl_sync(full, g.w, src);
+              if (nxt[r]) g.x += tx, g.y += ty, g.z += tz, g.w += tw;
+            }
+          }
+          if (has && lead) atomicAdd(&Q.pm[didx(S, st.b[0] + ox, st.b[1] + oy, st.b[2] + oz)], g);
         }
   }
 }
