@@ -274,41 +274,70 @@ __device__ __forceinline__ bool dp2g_particle(const DiffParams& Q, int64_t i, St
   return true;
 }
 
-// P2G with the float4 global atomics of each node summed first over the lanes of a warp whose
-// particles share a stencil origin (neighbours in memory often share a cell): the group's lowest
-// lane adds the sum.  The sum is a tree over the group's ranks: in round r every lane adds the value
-// of its next remaining peer above (nxt[r] = that lane + 1, 0 for none), then the lanes whose rank
-// has bit r set drop out; five rounds cover a group of 32.
-__global__ void __launch_bounds__(256) k_dp2g(DiffParams Q) {
-  const SceneDev& S = Q.S;
+// Groups of the lanes of a warp with equal keys (particles with the same stencil origin scatter to
+// the same 27 nodes; neighbours in memory often share a cell).  peer_sum adds a value over the group
+// into its lowest lane (`lead`), which alone then issues the float4 global atomic.  The sum is a tree
+// over the group's ranks: in round r every lane adds the value of its next remaining peer above
+// (nxt[r] = that lane + 1, 0 for none), then the lanes whose rank has bit r set drop out; five rounds
+// cover a group of 32.  Every lane of the warp must call both (full-warp shuffles).
+struct PeerTree {
+  int nxt[5];
+  int rounds;  // the same for the whole warp
+  bool lead;
+};
+
+__device__ __forceinline__ PeerTree peer_tree(unsigned long long key) {
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
+  const unsigned peers = __match_any_sync(full, key);
+  PeerTree t;
+  t.lead = (peers & ((1u << lane) - 1u)) == 0u;
+  unsigned above = peers & (0xfffffffeu << lane);
+  unsigned rank = __popc(peers & ((1u << lane) - 1u));
+  t.rounds = 0;
+#pragma unroll
+  for (int r = 0; r < 5; ++r) {
+    t.nxt[r] = 0;
+    if (__any_sync(full, above != 0u)) {
+      t.nxt[r] = __ffs(above);
+      above &= ~__ballot_sync(full, (rank & 1u) != 0u);
+      rank >>= 1;
+      t.rounds = r + 1;
+    }
+  }
+  return t;
+}
+
+__device__ __forceinline__ float4 peer_sum(const PeerTree& t, float4 g) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int r = 0; r < 5; ++r) {
+    if (r < t.rounds) {
+      const int src = t.nxt[r] ? t.nxt[r] - 1 : lane;
+      const float tx = __shfl_sync(full, g.x, src), ty = __shfl_sync(full, g.y, src);
+      const float tz = __shfl_sync(full, g.z, src), tw = __shfl_sync(full, g.w, src);
+      if (t.nxt[r]) g.x += tx, g.y += ty, g.z += tz, g.w += tw;
+    }
+  }
+  return g;
+}
+
+// A key no stencil origin has, distinct per lane (a lane without a particle to scatter).
+__device__ __forceinline__ unsigned long long no_peer_key() { return ~0ull - (unsigned long long)(threadIdx.x & 31); }
+
+// P2G, its float4 global atomics summed over peer groups first.
+__global__ void __launch_bounds__(256) k_dp2g(DiffParams Q) {
+  const SceneDev& S = Q.S;
   // the trip count is the same for the whole warp (blockDim and the stride are multiples of 32),
   // so every lane reaches the warp-wide operations below
   for (int64_t w0 = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); w0 < Q.n;
        w0 += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = w0 + lane;
+    const int64_t i = w0 + (threadIdx.x & 31);
     Stencil st;
     float A[9], mv[3], mass = 0.f;
     const bool has = i < Q.n && dp2g_particle(Q, i, st, A, mv, mass);
-    const unsigned long long key =
-        has ? (unsigned long long)didx(S, st.b[0], st.b[1], st.b[2]) : ~0ull - (unsigned long long)lane;
-    const unsigned peers = __match_any_sync(full, key);
-    const bool lead = (peers & ((1u << lane) - 1u)) == 0u;
-    unsigned above = peers & (0xfffffffeu << lane);
-    unsigned rank = __popc(peers & ((1u << lane) - 1u));
-    int nxt[5];
-    int rounds = 0;
-#pragma unroll
-    for (int r = 0; r < 5; ++r) {
-      nxt[r] = 0;
-      if (__any_sync(full, above != 0u)) {
-        nxt[r] = __ffs(above);
-        above &= ~__ballot_sync(full, (rank & 1u) != 0u);
-        rank >>= 1;
-        rounds = r + 1;
-      }
-    }
+    const PeerTree pt = peer_tree(has ? (unsigned long long)didx(S, st.b[0], st.b[1], st.b[2]) : no_peer_key());
 #pragma unroll
     for (int ox = 0; ox < 3; ++ox)
 #pragma unroll
@@ -325,16 +354,8 @@ __global__ void __launch_bounds__(256) k_dp2g(DiffParams Q) {
             g.z = wt * (mv[2] + A[6] * dp[0] + A[7] * dp[1] + A[8] * dp[2]);
             g.w = wt * mass;
           }
-#pragma unroll
-          for (int r = 0; r < 5; ++r) {
-            if (r < rounds) {  // the same for the whole warp
-              const int src = nxt[r] ? nxt[r] - 1 : lane;
-              const float tx = __shfl_sync(full, g.x, src), ty = __shfl_sync(full, g.y, src);
-              const float tz = __shfl_sync(full, g.z, src), tw = __shfl_sync(full, g.w, src);
-              if (nxt[r]) g.x += tx, g.y += ty, g.z += tz, g.w += tw;
-            }
-          }
-          if (has && lead) atomicAdd(&Q.pm[didx(S, st.b[0] + ox, st.b[1] + oy, st.b[2] + oz)], g);
+          g = peer_sum(pt, g);
+          if (has && pt.lead) atomicAdd(&Q.pm[didx(S, st.b[0] + ox, st.b[1] + oy, st.b[2] + oz)], g);
         }
   }
 }
