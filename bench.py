@@ -520,6 +520,7 @@ def run_ours(args, rank, world):
     if rank == 0 and not args.skip_forms:
         result["forms"] = run_forms()
         result["forms"]["differentiation"] = run_diff()
+        result["forms"]["differentiation"]["scene_api"] = run_diff_scene()
     if rank == 0 and not args.skip_cpu:
         result["cpu_baseline"] = cpu_baseline()
     return result
@@ -792,6 +793,49 @@ def run_diff(steps=64, substeps_per_step=10, ckpt_steps=16, seed=99):
     }
 
 
+def run_diff_scene(steps=64, substeps_per_step=10, seed=99):
+    """The differentiation rollout through the reference's own API: SimOptions(requires_grad=True),
+    the cube as one Elastic entity (E = 3e5, nu 0.2, rho 1000: one material per entity, as that API
+    gives it; a 0.25 m box at particle size 1/240 on the same 97^3 grid, dt 1e-4), a v0 tensor
+    through entity.set_velocity, `steps` scene.step() calls, the COM loss on get_state().pos and
+    loss.backward().  Each step is a checkpoint, re-simulated in the backward.  Timed: scene.reset()
+    through the backward, host loop included."""
+    import torch
+
+    import genesis_gb300 as gs
+
+    if not gs._initialized:
+        gs.init(backend=gs.gpu, seed=SEED)
+    _, _, _, v0_np, target_np = diff_config(seed)
+    scene = gs.Scene(sim_options=gs.options.SimOptions(dt=substeps_per_step * 1e-4, substeps=substeps_per_step,
+                                                       requires_grad=True),
+                     mpm_options=gs.options.MPMOptions(lower_bound=(0, 0, 0), upper_bound=(1, 1, 1), grid_density=96,
+                                                       particle_size=1.0 / 240))
+    cube = scene.add_entity(material=gs.materials.MPM.Elastic(E=3e5, nu=0.2, rho=1000.0, sampler="regular"),
+                            morph=gs.morphs.Box(pos=(0.5, 0.5, 0.18), size=(0.25, 0.25, 0.25)))
+    scene.build()
+    target = torch.tensor(target_np, dtype=torch.float32, device="cuda")
+    out = {}
+
+    def fwd_bwd():
+        scene.reset()
+        v0 = torch.tensor(v0_np, dtype=torch.float32, device="cuda", requires_grad=True)
+        cube.set_velocity(v0)
+        for _ in range(steps):
+            scene.step()
+        loss = ((cube.get_state().pos[0].mean(0) - target) ** 2).sum()
+        loss.backward()
+        out["v0"] = v0
+
+    fwd_bwd()
+    t = _timed(fwd_bwd)
+    n = cube.n_particles
+    res = {"n_particles": n, "seconds_fwd_bwd": t, "value": n * steps * substeps_per_step / t,
+           "grad_v0": out["v0"].grad.tolist()}
+    scene.sim.mpm_solver.destroy()
+    return res
+
+
 def run_reference(args):
     """The CPU implementation of the path (oracle restatement), all host cores, same metric."""
     O, sc, oms, st = oracle_c2_state()
@@ -848,7 +892,9 @@ def main():
         print(json.dumps(run_served_only()))
         return
     if args.form == "differentiation":
-        print(json.dumps(run_diff(steps=args.diff_steps)))
+        d = run_diff(steps=args.diff_steps)
+        d["scene_api"] = run_diff_scene(steps=args.diff_steps)
+        print(json.dumps(d))
         return
     if args.warmup < 3:
         args.warmup = 3
